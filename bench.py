@@ -1,0 +1,334 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 SU(2) pf-FRG flow core: cutoff steps per second of one flow.
+
+Workload (default): SU(2) J1-J2 Heisenberg model on the simple cubic lattice, J1 = 1,
+J2 = 0.25, lattice range 6 (23 symmetry-reduced site pairs, 4095 RPA pairs), 64 positive
+Matsubara frequencies exponentially spaced in [0.005, 100], cutoff 100 -> 0.05 x 0.98.
+A step is one cutoff step as SpinParser's loop runs it: flow right-hand side (self-energy
+flow + vertex flow), correlation measurement, explicit Euler update.  Synthetic in the sense
+that the state is the model's initial condition advanced by the flow itself (no dataset).
+
+Lines printed (rank 0, one JSON line):
+  value     steps/s with the state resident in HBM, device time from CUDA events on the
+            flow's stream; L2 is flushed (256 MB write) before every timed step
+  e2e       steps/s through the C ABI with host buffers: every step uploads the state from
+            pinned host memory, runs the step and reads the state and the correlations back
+  roofline  the vertex-flow kernel: nominal algorithmic FP32 work per launch
+            F_RHS = F_N (2N+8) (3*100*Nl + 4*sum O) over its CUDA-event launch time, against
+            the FP32 FMA throughput measured in-run on the same GPU
+  cpu_baseline  the CPU oracle (restatement of the reference's SU(2) core) on this host's
+            cores, on a bounded random sample of vertex triples, extrapolated to one step
+
+--impl reference times the CPU oracle alone (the reference's C++ code needs Boost and HDF5,
+which this environment does not provide, so its own build cannot run here).
+--gpus N > 1: replicas only (independent flows, one per GPU, no collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "cubic-j1j2-r6-n64": dict(lattice="cubic", range=6, model="cubic-j1j2heisenberg", params={"j1": "1.0", "j2": "0.25"},
+                              n_freq=64, fmin=0.005, fmax=100.0, cmax=100.0, cmin=0.05, cstep=0.98),
+    "square-r3-n32": dict(lattice="square", range=3, model="square-heisenberg", params={"j": "1.0"},
+                          n_freq=32, fmin=0.005, fmax=50.0, cmax=50.0, cmin=0.05, cstep=0.98),
+    "pyrochlore-r5-n64": dict(lattice="pyrochlore", range=5, model="pyrochlore-heisenberg", params={"j": "1.0"},
+                              n_freq=64, fmin=0.002, fmax=100.0, cmax=100.0, cmin=0.01, cstep=0.99),
+}
+DEFAULT_WORKLOAD = "cubic-j1j2-r6-n64"
+METRIC = "cutoff steps/s per flow"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU work budget of the baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def setup(wl):
+    import spinparser_gb300 as spn
+
+    lat = spn.Lattice(wl["lattice"], wl["range"], wl["model"], wl["params"])
+    tab = lat.tables()
+    freq = spn.frequency_exponential(wl["fmin"], wl["fmax"], wl["n_freq"])
+    cut = spn.cutoff_exponential(wl["cmax"], wl["cmin"], wl["cstep"])
+    return tab, freq, cut
+
+
+def flops_per_rhs(tab, n):
+    fn = n * n * (n + 1) // 2
+    return float(fn) * (2 * n + 8) * (3 * 100 * tab.n_sites + 4 * tab.n_overlap)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) >= 9:
+                    rows.append(p)
+        os.unlink(self.file.name)
+        if not rows:
+            return None
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return float("nan")
+
+        sm = [num(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.nanmedian(sm)), "sm_max_mhz": float(np.nanmax([num(r[2]) for r in rows])),
+                "reasons": reasons, "samples": len(rows), "power_w_max": float(np.nanmax([num(r[3]) for r in rows]))}
+
+
+def cpu_baseline(tab, freq, state_cutoff, state, budget_s):
+    """Times the oracle on a bounded random sample of vertex triples on all host cores and
+    extrapolates to one full step (vertex flow of all triples + self-energy flow)."""
+    from oracle import Oracle
+
+    threads = os.cpu_count() or 1
+    orc = Oracle(tab, freq)
+    v2, ss, dd = state
+    t0 = time.perf_counter()
+    dv2 = orc.self_energy(state_cutoff, v2, ss, dd)
+    t_se = time.perf_counter() - t0
+    fn = orc.fn
+    rng = np.random.default_rng(20261203)
+    probe = rng.choice(fn, size=min(fn, 4 * threads), replace=False)
+    t0 = time.perf_counter()
+    orc.vertex_sample(state_cutoff, v2, dv2, ss, dd, probe, threads)
+    t_probe = time.perf_counter() - t0
+    per_triple = t_probe / len(probe)
+    n = int(min(fn, max(len(probe), budget_s / max(per_triple, 1e-9))))
+    sample = rng.choice(fn, size=n, replace=False)
+    t0 = time.perf_counter()
+    orc.vertex_sample(state_cutoff, v2, dv2, ss, dd, sample, threads)
+    t_s = time.perf_counter() - t0
+    t_step = t_s * fn / n + t_se
+    return {"value": 1.0 / t_step, "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": f"{n} of {fn} vertex triples (uniform random, seed 20261203) + full self-energy flow, "
+                      f"{t_s:.1f} s on {threads} threads; one step extrapolated to {t_step:.1f} s"}
+
+
+def run_reference(args, wl):
+    """--impl reference: the CPU oracle only (rank 0)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    tab, freq, cut = setup(wl)
+    state = tab.initial_state(len(freq))
+    per_step = max(2.0, min(10.0, 150.0 / max(1, args.steps + args.warmup)))
+    for _ in range(args.warmup):
+        cpu_baseline(tab, freq, float(cut[0]), state, 0.2)
+    vals = []
+    t0 = time.perf_counter()
+    last = None
+    for _ in range(args.steps):
+        last = cpu_baseline(tab, freq, float(cut[0]), state, per_step)
+        vals.append(last["value"])
+    wall = time.perf_counter() - t0
+    value = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (model initial condition)",
+            "config": {"workload": args.workload, **{k: v for k, v in wl.items() if k != "params"},
+                       "params": wl["params"], "l2": "n/a (CPU)"},
+            "cpu_baseline": {**last, "value": value},
+            "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": wall}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, wl)
+        return
+    if args.warmup < 3:
+        raise SystemExit("--warmup must be >= 3")
+
+    import torch
+
+    import spinparser_gb300 as spn
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    tab, freq, cut = setup(wl)
+    n = len(freq)
+    total_steps = args.warmup + args.steps
+    if total_steps + 1 > len(cut):
+        raise SystemExit("more steps than cutoff values")
+    flow = spn.Su2Flow(tab, freq, device=local)
+    stream = torch.cuda.Stream(device=local)
+    flow.set_stream(stream.cuda_stream)
+    state0 = tab.initial_state(n)
+    flow.set_state(float(cut[0]), *state0)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
+
+    def step(k):
+        flow.compute_step()
+        flow.launch_correlation()
+        flow.finalize_step(float(cut[k + 1]))
+
+    for k in range(args.warmup):
+        step(k)
+    torch.cuda.synchronize()
+    if flow.is_diverged():
+        raise SystemExit("flow diverged during warm-up")
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sampler = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    flow.set_profiling(True)
+    sampler.start()
+    wall0 = time.perf_counter()
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(i))
+        starts[i].record(stream)
+        step(args.warmup + i)
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    clocks = sampler.stop()
+    if dist:
+        dist.barrier()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = float(np.sum(step_ms))
+    prof = flow.profile()
+    diverged = flow.is_diverged()
+
+    if dist:
+        t = torch.tensor([total_ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+
+    # end to end through the C ABI with pinned host buffers
+    e2e_steps = args.e2e_steps or max(3, min(args.steps, 10))
+    fn_nl = flow.fn * flow.nl
+    pin = lambda m: torch.empty(m, dtype=torch.float32, pin_memory=True).numpy()  # noqa: E731
+    h_v2, h_ss, h_dd = pin(n), pin(fn_nl), pin(fn_nl)
+    h_zz, h_dc = pin(flow.n_corr), pin(flow.n_corr)
+    c0, a, b, c = flow.get_state()
+    h_v2[:], h_ss[:], h_dd[:] = a, b, c
+    torch.cuda.synchronize()
+    e0 = time.perf_counter()
+    kc = args.warmup + args.steps
+    for i in range(e2e_steps):
+        k = min(kc + i, len(cut) - 2)
+        flow.set_state(float(cut[k]), h_v2, h_ss, h_dd)
+        flow.compute_step()
+        flow.launch_correlation()
+        flow.get_correlation(h_zz, h_dc)
+        flow.finalize_step(float(cut[k + 1]))
+        flow.get_state(h_v2, h_ss, h_dd)
+    e2e_s = time.perf_counter() - e0
+    state_bytes = 4 * (n + 2 * fn_nl)
+
+    fp32_peak, clk = spn.measure_fp32_peak(local)
+    flops = flops_per_rhs(tab, n)
+    avg_vertex_ms = prof["vertex_ms"] / max(1, prof["vertex_launches"])
+    achieved = flops / (avg_vertex_ms * 1e-3) / 1e12
+    traffic = None
+    prof_file = os.path.join(ROOT, "profiles", f"vertex_flow_{args.workload}.json")
+    if os.path.exists(prof_file):
+        traffic = json.load(open(prof_file)).get("dram_bytes_per_launch")
+
+    if rank != 0:
+        return
+    value = world * args.steps / (total_ms * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (model initial condition, advanced by the flow)",
+        "config": {"workload": args.workload, "lattice": wl["lattice"], "range": wl["range"], "model": wl["model"],
+                   "params": wl["params"], "n_freq": n, "freq_range": [wl["fmin"], wl["fmax"]],
+                   "cutoff": [wl["cmax"], wl["cmin"], wl["cstep"]], "n_sites": tab.n_sites,
+                   "n_overlap": tab.n_overlap, "n_triples": flow.fn, "parallelism": f"replicas x{world}",
+                   "l2": "flushed (256 MB write) before every timed step"},
+        "e2e": {"value": e2e_steps / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": state_bytes,
+                "d2h_bytes_per_step": state_bytes + 8 * flow.n_corr},
+        "roofline": {"bound": "fp32", "kernel": "su2_vertex_flow_kernel", "achieved": achieved, "peak": fp32_peak,
+                     "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": traffic,
+                     "algorithmic_flops_per_launch": flops, "avg_launch_ms": avg_vertex_ms,
+                     "peak_source": "measured in-run: pure-FFMA kernel on this GPU (MEASURED_PEAKS.json has no "
+                                    "FP32 CUDA-core figure)", "fp32_clock_ghz_implied": clk},
+        "gpu_launches": 8 * args.steps,
+        "clocks": clocks,
+        "diverged": diverged,
+        "wall_s": wall,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        c, v2, ss, dd = flow.get_state()
+        line["cpu_baseline"] = cpu_baseline(tab, freq, c, (v2, ss, dd), args.cpu_seconds)
+    print(json.dumps(line))
+    flow.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,201 @@
+/*
+ * spn_su2.h — C ABI of the GB300 SU(2) pf-FRG flow core (libspn_su2.so).
+ *
+ * The library replaces, for one SpinParser flow, the work that the reference runs inside
+ * SU2FrgCore (src/SU2/SU2FrgCore.cpp) through its LoadManager, and the correlation
+ * measurement of SU2MeasurementCorrelation (src/SU2/SU2MeasurementCorrelation.cpp).
+ * Host code above this ABI (the C++ FrgCore mirror in the package, or any FFI caller)
+ * owns the cutoff loop, checkpoints and output files, as SpinParser::runCore does.
+ *
+ * Conventions
+ *   - Every function returns 0 on success or a negative status (SPN_E_*); the message of
+ *     the last failure on the calling thread is available through spn_last_error().
+ *   - No C++ exception crosses this boundary.
+ *   - Pointers named host_* / plain arrays are host memory; the library copies them.
+ *   - Vertex arrays use the reference layout: index ((s*(s+1)/2 + u) * N + t) * Nl + rid,
+ *     s >= u, i.e. SU2VertexTwoParticle::_dataSS/_dataDD (src/SU2/SU2VertexTwoParticle.hpp:603).
+ */
+#ifndef SPN_SU2_H
+#define SPN_SU2_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define SPN_OK 0
+#define SPN_E_ARGUMENT (-2)
+#define SPN_E_INIT (-3)
+#define SPN_E_IO (-4)
+#define SPN_E_CUDA (-5)
+#define SPN_E_DEVICE (-6)
+#define SPN_E_INTERNAL (-7)
+#define SPN_E_UNSUPPORTED (-8)
+
+/* Copies the message of the last failed call on this thread into buf (NUL-terminated,
+ * truncated to len).  Returns the full message length. */
+int spn_last_error(char *buf, size_t len);
+
+/* Library / device information: number of CUDA devices visible (0 without a GPU). */
+int spn_device_count(int *count);
+
+/* Measured FP32 FMA throughput of a device (TFLOP/s, best of several runs of a pure-FFMA
+ * kernel) and the SM clock it implies.  The vertex-flow kernel runs on the FP32 CUDA cores;
+ * this is its roofline denominator.  No reference counterpart (benchmark support). */
+int spn_measure_fp32_peak(int device, double *tflops, double *sm_clock_ghz_est);
+
+/* ------------------------------------------------------------------------------------
+ * Host side: lattice / spin model (LatticeModelFactory::newLatticeModel,
+ * src/LatticeModelFactory.cpp:733-1047) and discretisations (src/TaskFileParser.cpp:107-198).
+ * These run on the CPU only and need no GPU.
+ * ------------------------------------------------------------------------------------ */
+typedef struct spn_lattice spn_lattice;
+
+typedef struct {
+    int n_sites;         /* Nl: number of representative site pairs (Lattice::size) */
+    int n_sites_total;   /* all sites the lattice stores (Lattice::_dataSize) */
+    int n_basis;         /* basis sites per unit cell */
+    int n_range;         /* sites within range of basis site 0 (getRange(0)) */
+    int n_overlap;       /* total RPA pairs, sum over rid of getOverlap(rid).size */
+    int n_interactions;  /* couplings of the origin to representatives (SpinModel::interactions) */
+} spn_lattice_info;
+
+/* Builds the lattice named `lattice_name` from the unit cells in `resource_dir`, with
+ * the spin model `model_name` whose coupling parameters are given as name/value strings
+ * (values use the reference's number syntax, e.g. "1/sqrt(2)").
+ * Replaces: LatticeUnitCell ctor (src/LatticeModelFactory.cpp:102), SpinModelUnitCell ctor
+ * (:239) and newLatticeModel (:733). */
+int spn_lattice_create(const char *resource_dir, const char *lattice_name, int range, const char *model_name,
+                       int n_params, const char *const *param_names, const char *const *param_values,
+                       spn_lattice **out);
+int spn_lattice_destroy(spn_lattice *lat);
+int spn_lattice_get_info(const spn_lattice *lat, spn_lattice_info *info);
+
+/* Gather tables (any pointer may be NULL to skip that table):
+ *   sites_rid[Nl]        Lattice::getSites()[j].rid            (src/Lattice.hpp:492)
+ *   inv_sites_rid[Nl]    Lattice::getInvertedSites()[j].rid    (src/Lattice.hpp:481)
+ *   overlap_ptr[Nl+1], overlap_rid1[n_overlap], overlap_rid2[n_overlap]
+ *                        Lattice::getOverlap(rid).rid1/rid2    (src/Lattice.hpp:472)
+ *   range_rid[n_range]   symmetryTransform(origin, j), j in getRange(0)
+ *   range_inv_rid[n_range] symmetryTransform(j, origin)
+ *   corr_rid[n_basis*n_range] symmetryTransform(basis b, j), j in getRange(b)
+ *                        (the scatter of SU2MeasurementCorrelation.cpp:161-176)
+ *   site_pos[3*n_basis*n_range] positions of getRange(b) sites (obs "meta/sites")
+ *   basis_pos[3*n_basis], lattice_vectors[9]                   (obs "meta") */
+int spn_lattice_get_tables(const spn_lattice *lat, int *sites_rid, int *inv_sites_rid, int *overlap_ptr,
+                           int *overlap_rid1, int *overlap_rid2, int *range_rid, int *range_inv_rid, int *corr_rid,
+                           double *site_pos, double *basis_pos, double *lattice_vectors);
+
+/* All stored sites (Lattice::getSiteParameters, src/Lattice.hpp:397): site_params[4*i..] =
+ * (a0, a1, a2, basis) of site id i, i < n_sites_total; and, if pair_rid is not NULL, the
+ * full symmetry table pair_rid[i1*n_sites_total + i2] = symmetryTransform(i1, i2)
+ * (-1 where the pair is out of range).  Diagnostics for the lattice KATs. */
+int spn_lattice_get_sites(const spn_lattice *lat, int *site_params, int *pair_rid);
+
+/* Interactions of the origin with representative rid: rid[n] and the 3x3 coupling matrix
+ * (row-major, 9 floats each).  SpinModel::interactions (src/SpinModel.hpp). */
+int spn_lattice_get_interactions(const spn_lattice *lat, int *rid, float *coupling);
+
+/* Writes the lattice debug file (.ldf) as `--debugLattice`-free SpinParser always does. */
+int spn_lattice_write_ldf(const spn_lattice *lat, const char *path);
+
+/* Exponential frequency mesh: min * powf(powf(max/min, 1/(count-1)), i), i < count
+ * (src/TaskFileParser.cpp:121-123).  out has room for `count` floats. */
+int spn_frequency_exponential(float min, float max, int count, float *out);
+
+/* Exponential cutoff list: repeated float multiplication max, max*step, ... while > min
+ * (src/TaskFileParser.cpp:171-176).  Writes at most `cap` values, *n receives the count
+ * (which may exceed cap; call again with a larger buffer). */
+int spn_cutoff_exponential(float max, float min, float step, float *out, int cap, int *n);
+
+/* Initial condition of SU2EffectiveAction (src/SU2/SU2EffectiveAction.hpp:38-60): zeros,
+ * then v4ss[it*Nl + rid] += J_xx(rid) / normalization for every frequency triple it. */
+int spn_su2_initial_state(const spn_lattice *lat, int n_freq, float normalization, float *v2, float *v4ss,
+                          float *v4dd);
+
+/* ------------------------------------------------------------------------------------
+ * Device side: one SU(2) flow resident in GPU memory.
+ * ------------------------------------------------------------------------------------ */
+typedef struct spn_su2 spn_su2;
+
+/* Description of one flow; the library copies every table at create time. */
+typedef struct {
+    int n_freq;                 /* N positive Matsubara frequencies */
+    const float *freq;          /* [N] ascending, positive (FrequencyDiscretization values) */
+    int n_sites;                /* Nl */
+    const int *sites_rid;       /* [Nl] */
+    const int *inv_sites_rid;   /* [Nl] */
+    const int *overlap_ptr;     /* [Nl+1] */
+    const int *overlap_rid1;    /* [overlap_ptr[Nl]] */
+    const int *overlap_rid2;    /* [overlap_ptr[Nl]] */
+    int n_range;                /* sites in range of the origin */
+    const int *range_rid;       /* [n_range] */
+    const int *range_inv_rid;   /* [n_range] */
+    int n_corr;                 /* n_basis * n_range entries of the correlation output */
+    const int *corr_rid;        /* [n_corr] rid each correlation entry reads */
+    float spin_length;          /* S (SU2FrgCore option "spin", default 0.5) */
+    int device;                 /* CUDA device ordinal */
+    int flags;                  /* SPN_SU2_* flags below */
+} spn_su2_desc;
+
+/* Self-energy and its flow are kept in FP64 on the device (plain mode keeps FP32, the
+ * reference's type). */
+#define SPN_SU2_FP64_SELF_ENERGY 0x1
+
+/* Creates a flow (allocates its device memory).  State starts at zero, cutoff 0.
+ * Replaces SU2FrgCore's constructor (src/SU2/SU2FrgCore.cpp:17-81). */
+int spn_su2_create(const spn_su2_desc *desc, spn_su2 **out);
+int spn_su2_destroy(spn_su2 *h);
+
+/* Work is queued on this stream (a cudaStream_t; NULL selects the library's own). */
+int spn_su2_set_stream(spn_su2 *h, void *stream);
+
+/* Sizes: N, Nl and F_N = N*N*(N+1)/2 (so each vertex array holds F_N*Nl floats). */
+int spn_su2_get_sizes(const spn_su2 *h, int *n_freq, int *n_sites, long long *n_triples);
+
+/* Copy the flowing state (EffectiveAction) in / out: cutoff, v2[N], v4ss/v4dd[F_N*Nl].
+ * Replaces readCheckpoint / writeCheckpoint data movement (src/SU2/SU2EffectiveAction.hpp:79-205). */
+int spn_su2_set_state(spn_su2 *h, float cutoff, const float *v2, const float *v4ss, const float *v4dd);
+int spn_su2_get_state(spn_su2 *h, float *cutoff, float *v2, float *v4ss, float *v4dd);
+
+/* FrgCore::computeStep (src/SU2/SU2FrgCore.cpp:89-109): self-energy flow, then the
+ * two-particle vertex flow, into the device-resident flow buffers.  Asynchronous. */
+int spn_su2_compute_step(spn_su2 *h);
+
+/* Copies the flow computed by the last compute_step: dv2[N], dv4ss/dv4dd[F_N*Nl]. */
+int spn_su2_get_flow(spn_su2 *h, float *dv2, float *dv4ss, float *dv4dd);
+
+/* FrgCore::finalizeStep (src/SU2/SU2FrgCore.cpp:111-137): explicit Euler step of the
+ * state by (new_cutoff - cutoff) * flow, then cutoff = new_cutoff.  Asynchronous. */
+int spn_su2_finalize_step(spn_su2 *h, float new_cutoff);
+
+/* SU2MeasurementCorrelation::_calculateCorrelation at the current cutoff (nu = 0):
+ * zz[n_corr] and dd[n_corr] in the reference's (basis, site-in-range) order.  Either
+ * pointer may be NULL.  chi_zz/chi_dd (may be NULL) receive the per-rid susceptibility. */
+int spn_su2_measure_correlation(spn_su2 *h, float *zz, float *dd, float *chi_zz, float *chi_dd);
+
+/* The same measurement split in two: launch (asynchronous, result stays on the device) and
+ * copy-out of the last launched measurement (synchronises). */
+int spn_su2_launch_correlation(spn_su2 *h);
+int spn_su2_get_correlation(spn_su2 *h, float *zz, float *dd, float *chi_zz, float *chi_dd);
+
+/* EffectiveAction::isDiverged on the last computed flow (any NaN).  Synchronises. */
+int spn_su2_is_diverged(spn_su2 *h, int *diverged);
+
+/* Waits for all queued work of this flow. */
+int spn_su2_synchronize(spn_su2 *h);
+
+/* Kernel timing with CUDA events recorded on the flow's stream around each compute_step
+ * kernel.  enable != 0 starts recording (and clears the totals). */
+int spn_su2_set_profiling(spn_su2 *h, int enable);
+/* Totals since profiling was enabled: milliseconds and launches of the vertex-flow kernel
+ * and of the whole compute_step (self-energy + tables + vertex). */
+int spn_su2_get_profile(spn_su2 *h, double *vertex_ms, int *vertex_launches, double *step_ms, int *steps);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPN_SU2_H */

@@ -1,0 +1,151 @@
+"""ORACLE — test infrastructure only (the CPU checker of the GB300 SU(2) flow core).
+
+Python binding of oracle/su2_oracle.cpp, a plain C++ restatement of SpinParser's SU(2) flow
+right-hand side, Euler update and correlation measurement.  Imported only by the tests,
+``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg; the product never calls it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import platform
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+class OracleDesc(C.Structure):
+    _fields_ = [
+        ("n_freq", C.c_int), ("freq", C.POINTER(C.c_float)), ("n_sites", C.c_int),
+        ("sites_rid", C.POINTER(C.c_int)), ("inv_sites_rid", C.POINTER(C.c_int)),
+        ("overlap_ptr", C.POINTER(C.c_int)), ("overlap_rid1", C.POINTER(C.c_int)),
+        ("overlap_rid2", C.POINTER(C.c_int)), ("n_range", C.c_int), ("range_rid", C.POINTER(C.c_int)),
+        ("range_inv_rid", C.POINTER(C.c_int)), ("spin_length", C.c_float),
+    ]
+
+
+def library_path() -> str:
+    return os.path.join(_HERE, "_build", platform.machine(), "liboracle_su2.so")
+
+
+_LIB = None
+
+
+def _lib():
+    global _LIB
+    if _LIB is None:
+        path = library_path()
+        if not os.path.exists(path):
+            raise RuntimeError(f"oracle library not built ({path}); run __graft_entry__.build()")
+        lib = C.CDLL(path)
+        f, d, i, fp, dp = C.c_float, C.c_double, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_double)
+        dsc = C.POINTER(OracleDesc)
+        lib.oracle_su2_rhs_f32.argtypes = [dsc, f, fp, fp, fp, fp, fp, fp, i]
+        lib.oracle_su2_rhs_f64.argtypes = [dsc, d, dp, dp, dp, dp, dp, dp, i]
+        lib.oracle_su2_self_energy_f32.argtypes = [dsc, f, fp, fp, fp, fp]
+        lib.oracle_su2_vertex_range_f32.argtypes = [dsc, f, fp, fp, fp, fp, i, i, fp, fp]
+        lib.oracle_su2_vertex_range_f64.argtypes = [dsc, d, dp, dp, dp, dp, i, i, dp, dp]
+        lib.oracle_su2_vertex_sample_f32.argtypes = [dsc, f, fp, fp, fp, fp, C.POINTER(C.c_int), i, fp, fp, i]
+        lib.oracle_su2_correlation_f32.argtypes = [dsc, f, fp, fp, fp, fp, fp]
+        lib.oracle_su2_correlation_f64.argtypes = [dsc, d, dp, dp, dp, dp, dp]
+        lib.oracle_su2_euler_f32.argtypes = [f, f, C.c_longlong, fp, fp]
+        lib.oracle_su2_euler_f32.restype = None
+        lib.oracle_su2_flow_f32.argtypes = [dsc, fp, i, fp, fp, fp, fp, fp, i]
+        _LIB = lib
+    return _LIB
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class Oracle:
+    """CPU restatement of the reference SU(2) core for one lattice + frequency mesh."""
+
+    def __init__(self, tables, freq, spin_length: float = 0.5):
+        self.lib = _lib()
+        self.freq = np.ascontiguousarray(freq, np.float32)
+        self.n = len(self.freq)
+        self.nl = int(tables.n_sites)
+        self.fn = self.n * self.n * (self.n + 1) // 2
+        self._keep = [np.ascontiguousarray(x, np.int32) for x in
+                      (tables.sites_rid, tables.inv_sites_rid, tables.overlap_ptr, tables.overlap_rid1,
+                       tables.overlap_rid2, tables.range_rid, tables.range_inv_rid)]
+        k = self._keep
+        d = OracleDesc()
+        d.n_freq, d.freq, d.n_sites = self.n, _p(self.freq, C.c_float), self.nl
+        d.sites_rid, d.inv_sites_rid = _p(k[0], C.c_int), _p(k[1], C.c_int)
+        d.overlap_ptr, d.overlap_rid1, d.overlap_rid2 = _p(k[2], C.c_int), _p(k[3], C.c_int), _p(k[4], C.c_int)
+        d.n_range, d.range_rid, d.range_inv_rid = len(k[5]), _p(k[5], C.c_int), _p(k[6], C.c_int)
+        d.spin_length = spin_length
+        self.desc = d
+
+    def rhs(self, cutoff, v2, ss, dd, fp64: bool = False, threads: int = 0):
+        """Self-energy flow [N] and vertex flow [F_N*Nl] x2."""
+        t = np.float64 if fp64 else np.float32
+        ct = C.c_double if fp64 else C.c_float
+        v2, ss, dd = (np.ascontiguousarray(x, t).reshape(-1) for x in (v2, ss, dd))
+        dv2 = np.empty(self.n, t)
+        dss = np.empty(self.fn * self.nl, t)
+        ddd = np.empty(self.fn * self.nl, t)
+        fn = self.lib.oracle_su2_rhs_f64 if fp64 else self.lib.oracle_su2_rhs_f32
+        rc = fn(C.byref(self.desc), cutoff, _p(v2, ct), _p(ss, ct), _p(dd, ct), _p(dv2, ct), _p(dss, ct), _p(ddd, ct),
+                threads)
+        assert rc == 0
+        return dv2, dss, ddd
+
+    def self_energy(self, cutoff, v2, ss, dd):
+        v2, ss, dd = (np.ascontiguousarray(x, np.float32).reshape(-1) for x in (v2, ss, dd))
+        dv2 = np.empty(self.n, np.float32)
+        f = C.c_float
+        assert self.lib.oracle_su2_self_energy_f32(C.byref(self.desc), cutoff, _p(v2, f), _p(ss, f), _p(dd, f),
+                                                   _p(dv2, f)) == 0
+        return dv2
+
+    def vertex_range(self, cutoff, v2, dv2, ss, dd, it0: int, it1: int, fp64: bool = False):
+        """Vertex flow of triples [it0, it1) given the self-energy flow dv2."""
+        t = np.float64 if fp64 else np.float32
+        ct = C.c_double if fp64 else C.c_float
+        v2, dv2, ss, dd = (np.ascontiguousarray(x, t).reshape(-1) for x in (v2, dv2, ss, dd))
+        dss = np.empty((it1 - it0) * self.nl, t)
+        ddd = np.empty((it1 - it0) * self.nl, t)
+        fn = self.lib.oracle_su2_vertex_range_f64 if fp64 else self.lib.oracle_su2_vertex_range_f32
+        assert fn(C.byref(self.desc), cutoff, _p(v2, ct), _p(dv2, ct), _p(ss, ct), _p(dd, ct), it0, it1, _p(dss, ct),
+                  _p(ddd, ct)) == 0
+        return dss, ddd
+
+    def vertex_sample(self, cutoff, v2, dv2, ss, dd, triples, threads: int = 0):
+        """Vertex flow of the listed triples, computed in parallel on `threads` host threads."""
+        its = np.ascontiguousarray(triples, np.int32)
+        v2, dv2, ss, dd = (np.ascontiguousarray(x, np.float32).reshape(-1) for x in (v2, dv2, ss, dd))
+        dss = np.empty(len(its) * self.nl, np.float32)
+        ddd = np.empty(len(its) * self.nl, np.float32)
+        f = C.c_float
+        assert self.lib.oracle_su2_vertex_sample_f32(C.byref(self.desc), cutoff, _p(v2, f), _p(dv2, f), _p(ss, f),
+                                                     _p(dd, f), _p(its, C.c_int), len(its), _p(dss, f), _p(ddd, f),
+                                                     threads) == 0
+        return dss, ddd
+
+    def correlation(self, cutoff, v2, ss, dd, fp64: bool = False):
+        """Per-rid static susceptibility (spin, density)."""
+        t = np.float64 if fp64 else np.float32
+        ct = C.c_double if fp64 else C.c_float
+        v2, ss, dd = (np.ascontiguousarray(x, t).reshape(-1) for x in (v2, ss, dd))
+        cs = np.empty(self.nl, t)
+        cd = np.empty(self.nl, t)
+        fn = self.lib.oracle_su2_correlation_f64 if fp64 else self.lib.oracle_su2_correlation_f32
+        assert fn(C.byref(self.desc), cutoff, _p(v2, ct), _p(ss, ct), _p(dd, ct), _p(cs, ct), _p(cd, ct)) == 0
+        return cs, cd
+
+    def flow(self, cutoffs, v2, ss, dd, threads: int = 0):
+        """Whole flow; returns (n_measured, chi_s[n_cut, Nl], chi_d[n_cut, Nl], final state)."""
+        cut = np.ascontiguousarray(cutoffs, np.float32)
+        v2, ss, dd = (np.array(x, np.float32).reshape(-1) for x in (v2, ss, dd))
+        cs = np.zeros((len(cut), self.nl), np.float32)
+        cd = np.zeros((len(cut), self.nl), np.float32)
+        f = C.c_float
+        n = self.lib.oracle_su2_flow_f32(C.byref(self.desc), _p(cut, f), len(cut), _p(v2, f), _p(ss, f), _p(dd, f),
+                                         _p(cs, f), _p(cd, f), threads)
+        assert n > 0
+        return n, cs, cd, (v2, ss, dd)

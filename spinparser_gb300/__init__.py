@@ -1,0 +1,14 @@
+"""GB300-native SU(2) pf-FRG flow core (SpinParser's SU2 hot path) behind a C ABI.
+
+Compute runs in libspn_su2.so (hand-written CUDA for sm_103a); this package is the Python
+host layer over that ABI.  Build with ``__graft_entry__.build()`` (or ``python -m
+spinparser_gb300._build``).
+"""
+from ._capi import SpnError, load_library
+from .core import (FP64_SELF_ENERGY, RES_DIR, Lattice, LatticeTables, Su2Flow, cutoff_exponential, device_count,
+                   frequency_exponential)
+
+__all__ = [
+    "SpnError", "load_library", "Lattice", "LatticeTables", "Su2Flow", "frequency_exponential", "cutoff_exponential",
+    "device_count", "RES_DIR", "FP64_SELF_ENERGY",
+]

@@ -1,0 +1,121 @@
+"""ctypes binding of include/spn_su2.h (libspn_su2.so).
+
+This is the same binding a Python host of the reference-facing C ABI would write; the
+package's Python classes and the tests call the library only through it.  Loading fails
+loudly when the library has not been built: there is no fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import _build
+
+c_int_p = C.POINTER(C.c_int)
+c_float_p = C.POINTER(C.c_float)
+c_double_p = C.POINTER(C.c_double)
+c_ll_p = C.POINTER(C.c_longlong)
+
+
+class LatticeInfo(C.Structure):
+    _fields_ = [
+        ("n_sites", C.c_int),
+        ("n_sites_total", C.c_int),
+        ("n_basis", C.c_int),
+        ("n_range", C.c_int),
+        ("n_overlap", C.c_int),
+        ("n_interactions", C.c_int),
+    ]
+
+
+class Su2Desc(C.Structure):
+    _fields_ = [
+        ("n_freq", C.c_int),
+        ("freq", c_float_p),
+        ("n_sites", C.c_int),
+        ("sites_rid", c_int_p),
+        ("inv_sites_rid", c_int_p),
+        ("overlap_ptr", c_int_p),
+        ("overlap_rid1", c_int_p),
+        ("overlap_rid2", c_int_p),
+        ("n_range", C.c_int),
+        ("range_rid", c_int_p),
+        ("range_inv_rid", c_int_p),
+        ("n_corr", C.c_int),
+        ("corr_rid", c_int_p),
+        ("spin_length", C.c_float),
+        ("device", C.c_int),
+        ("flags", C.c_int),
+    ]
+
+
+# name -> (restype, argtypes); every function declared in include/spn_su2.h
+SIGNATURES = {
+    "spn_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
+    "spn_device_count": (C.c_int, [c_int_p]),
+    "spn_measure_fp32_peak": (C.c_int, [C.c_int, c_double_p, c_double_p]),
+    "spn_lattice_create": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_char_p, C.c_int,
+                                     C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.POINTER(C.c_void_p)]),
+    "spn_lattice_destroy": (C.c_int, [C.c_void_p]),
+    "spn_lattice_get_info": (C.c_int, [C.c_void_p, C.POINTER(LatticeInfo)]),
+    "spn_lattice_get_tables": (C.c_int, [C.c_void_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p,
+                                         c_int_p, c_double_p, c_double_p, c_double_p]),
+    "spn_lattice_get_sites": (C.c_int, [C.c_void_p, c_int_p, c_int_p]),
+    "spn_lattice_get_interactions": (C.c_int, [C.c_void_p, c_int_p, c_float_p]),
+    "spn_lattice_write_ldf": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "spn_frequency_exponential": (C.c_int, [C.c_float, C.c_float, C.c_int, c_float_p]),
+    "spn_cutoff_exponential": (C.c_int, [C.c_float, C.c_float, C.c_float, c_float_p, C.c_int, c_int_p]),
+    "spn_su2_initial_state": (C.c_int, [C.c_void_p, C.c_int, C.c_float, c_float_p, c_float_p, c_float_p]),
+    "spn_su2_create": (C.c_int, [C.POINTER(Su2Desc), C.POINTER(C.c_void_p)]),
+    "spn_su2_destroy": (C.c_int, [C.c_void_p]),
+    "spn_su2_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "spn_su2_get_sizes": (C.c_int, [C.c_void_p, c_int_p, c_int_p, c_ll_p]),
+    "spn_su2_set_state": (C.c_int, [C.c_void_p, C.c_float, c_float_p, c_float_p, c_float_p]),
+    "spn_su2_get_state": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p, c_float_p]),
+    "spn_su2_compute_step": (C.c_int, [C.c_void_p]),
+    "spn_su2_get_flow": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p]),
+    "spn_su2_finalize_step": (C.c_int, [C.c_void_p, C.c_float]),
+    "spn_su2_measure_correlation": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p, c_float_p]),
+    "spn_su2_launch_correlation": (C.c_int, [C.c_void_p]),
+    "spn_su2_get_correlation": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p, c_float_p]),
+    "spn_su2_is_diverged": (C.c_int, [C.c_void_p, c_int_p]),
+    "spn_su2_synchronize": (C.c_int, [C.c_void_p]),
+    "spn_su2_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "spn_su2_get_profile": (C.c_int, [C.c_void_p, c_double_p, c_int_p, c_double_p, c_int_p]),
+}
+
+
+class SpnError(RuntimeError):
+    """A negative status returned by libspn_su2, with the library's message."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+_LIB = None
+
+
+def load_library() -> C.CDLL:
+    """Loads the in-tree libspn_su2.so; raises if it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.library_path()
+    if not os.path.exists(path):
+        raise RuntimeError(f"libspn_su2.so is not built ({path}); run __graft_entry__.build() first")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def check(status: int) -> None:
+    if status != 0:
+        lib = load_library()
+        buf = C.create_string_buffer(4096)
+        lib.spn_last_error(buf, len(buf))
+        raise SpnError(status, buf.value.decode(errors="replace"))

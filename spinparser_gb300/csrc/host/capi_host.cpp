@@ -1,0 +1,207 @@
+// Host half of the C ABI (include/spn_su2.h): error reporting, lattice construction,
+// discretisations and the initial state.  None of these touch the GPU.
+#include "capi_common.hpp"
+#include "lattice.hpp"
+#include "../../../include/spn_su2.h"
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+
+namespace spn {
+namespace {
+thread_local std::string g_last_error;
+}
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+}  // namespace spn
+
+struct spn_lattice {
+    spn::LatticeUnitCell uc;
+    spn::SpinModelUnitCell model;
+    spn::Lattice lat;
+};
+
+extern "C" int spn_last_error(char *buf, size_t len) {
+    const std::string &m = spn::g_last_error;
+    if (buf && len > 0) {
+        size_t n = m.size() < len - 1 ? m.size() : len - 1;
+        std::memcpy(buf, m.data(), n);
+        buf[n] = '\0';
+    }
+    return int(m.size());
+}
+
+extern "C" int spn_lattice_create(const char *resource_dir, const char *lattice_name, int range, const char *model_name,
+                                  int n_params, const char *const *param_names, const char *const *param_values,
+                                  spn_lattice **out) {
+    return spn::guarded([&] {
+        if (!resource_dir || !lattice_name || !model_name || !out || n_params < 0 || (n_params > 0 && (!param_names || !param_values)))
+            throw spn::Error(spn::ErrorType::Argument, "spn_lattice_create: null argument");
+        std::map<std::string, std::string> params;
+        for (int i = 0; i < n_params; ++i) {
+            if (!param_names[i] || !param_values[i]) throw spn::Error(spn::ErrorType::Argument, "spn_lattice_create: null parameter");
+            if (!params.emplace(param_names[i], param_values[i]).second)
+                throw spn::Error(spn::ErrorType::Initialization, std::string("Multiple definitions of parameter '") + param_names[i] + "'");
+        }
+        auto *h = new spn_lattice;
+        try {
+            h->uc = spn::read_unit_cell(resource_dir, lattice_name);
+            h->model = spn::read_spin_model(resource_dir, model_name, params);
+            h->lat = spn::build_lattice(h->uc, h->model, range);
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+    });
+}
+
+extern "C" int spn_lattice_destroy(spn_lattice *lat) {
+    delete lat;
+    return SPN_OK;
+}
+
+extern "C" int spn_lattice_get_info(const spn_lattice *lat, spn_lattice_info *info) {
+    return spn::guarded([&] {
+        if (!lat || !info) throw spn::Error(spn::ErrorType::Argument, "spn_lattice_get_info: null argument");
+        const spn::Lattice &L = lat->lat;
+        info->n_sites = L.size;
+        info->n_sites_total = L.n_sites();
+        info->n_basis = int(L.basis.size());
+        info->n_range = int(L.range_ids[0].size());
+        info->n_overlap = int(L.overlap_rid1.size());
+        info->n_interactions = int(L.interactions.size());
+    });
+}
+
+extern "C" int spn_lattice_get_tables(const spn_lattice *lat, int *sites_rid, int *inv_sites_rid, int *overlap_ptr,
+                                      int *overlap_rid1, int *overlap_rid2, int *range_rid, int *range_inv_rid,
+                                      int *corr_rid, double *site_pos, double *basis_pos, double *lattice_vectors) {
+    return spn::guarded([&] {
+        if (!lat) throw spn::Error(spn::ErrorType::Argument, "spn_lattice_get_tables: null lattice");
+        const spn::Lattice &L = lat->lat;
+        const int nb = int(L.basis.size());
+        const int nr = int(L.range_ids[0].size());
+        for (int b = 0; b < nb; ++b)
+            if (int(L.range_ids[b].size()) != nr)
+                throw spn::Error(spn::ErrorType::Unsupported, "basis sites with different range sizes are not supported");
+        if (sites_rid) {
+            auto v = L.sites_rid();
+            std::memcpy(sites_rid, v.data(), v.size() * sizeof(int));
+        }
+        if (inv_sites_rid) {
+            auto v = L.inverted_sites_rid();
+            std::memcpy(inv_sites_rid, v.data(), v.size() * sizeof(int));
+        }
+        if (overlap_ptr) std::memcpy(overlap_ptr, L.overlap_ptr.data(), L.overlap_ptr.size() * sizeof(int));
+        if (overlap_rid1) std::memcpy(overlap_rid1, L.overlap_rid1.data(), L.overlap_rid1.size() * sizeof(int));
+        if (overlap_rid2) std::memcpy(overlap_rid2, L.overlap_rid2.data(), L.overlap_rid2.size() * sizeof(int));
+        for (int n = 0; n < nr; ++n) {
+            int j = L.range_ids[0][n];
+            if (range_rid) range_rid[n] = L.transform(0, j);
+            if (range_inv_rid) range_inv_rid[n] = L.transform(j, 0);
+        }
+        for (int b = 0; b < nb; ++b)
+            for (int n = 0; n < nr; ++n) {
+                int j = L.range_ids[b][n];
+                if (corr_rid) corr_rid[b * nr + n] = L.transform(L.basis_ids[b], j);
+                if (site_pos) {
+                    spn::Vec3 p = L.position(j);
+                    double *o = site_pos + 3 * (size_t(b) * nr + n);
+                    o[0] = p.x; o[1] = p.y; o[2] = p.z;
+                }
+            }
+        if (basis_pos)
+            for (int b = 0; b < nb; ++b) {
+                spn::Vec3 p = L.position(L.basis_ids[b]);
+                basis_pos[3 * b] = p.x; basis_pos[3 * b + 1] = p.y; basis_pos[3 * b + 2] = p.z;
+            }
+        if (lattice_vectors)
+            for (int i = 0; i < 3; ++i) {
+                lattice_vectors[3 * i] = L.primitives[i].x;
+                lattice_vectors[3 * i + 1] = L.primitives[i].y;
+                lattice_vectors[3 * i + 2] = L.primitives[i].z;
+            }
+    });
+}
+
+extern "C" int spn_lattice_get_sites(const spn_lattice *lat, int *site_params, int *pair_rid) {
+    return spn::guarded([&] {
+        if (!lat) throw spn::Error(spn::ErrorType::Argument, "spn_lattice_get_sites: null lattice");
+        const spn::Lattice &L = lat->lat;
+        if (site_params)
+            for (int i = 0; i < L.n_sites(); ++i) {
+                site_params[4 * i] = L.sites[i].a0;
+                site_params[4 * i + 1] = L.sites[i].a1;
+                site_params[4 * i + 2] = L.sites[i].a2;
+                site_params[4 * i + 3] = L.sites[i].b;
+            }
+        if (pair_rid) std::memcpy(pair_rid, L.sym_rid.data(), L.sym_rid.size() * sizeof(int));
+    });
+}
+
+extern "C" int spn_lattice_get_interactions(const spn_lattice *lat, int *rid, float *coupling) {
+    return spn::guarded([&] {
+        if (!lat) throw spn::Error(spn::ErrorType::Argument, "spn_lattice_get_interactions: null lattice");
+        const auto &I = lat->lat.interactions;
+        for (size_t n = 0; n < I.size(); ++n) {
+            if (rid) rid[n] = I[n].rid;
+            if (coupling)
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 3; ++b) coupling[9 * n + 3 * a + b] = I[n].J[a][b];
+        }
+    });
+}
+
+extern "C" int spn_lattice_write_ldf(const spn_lattice *lat, const char *path) {
+    return spn::guarded([&] {
+        if (!lat || !path) throw spn::Error(spn::ErrorType::Argument, "spn_lattice_write_ldf: null argument");
+        spn::write_ldf(lat->lat, lat->uc, lat->model, path);
+    });
+}
+
+extern "C" int spn_frequency_exponential(float min, float max, int count, float *out) {
+    return spn::guarded([&] {
+        if (!out) throw spn::Error(spn::ErrorType::Argument, "spn_frequency_exponential: null output");
+        if (!(min > 0)) throw spn::Error(spn::ErrorType::Initialization, "frequency min must be positive");
+        if (!(max > min)) throw spn::Error(spn::ErrorType::Initialization, "frequency max must be greater than min");
+        if (count <= 1) throw spn::Error(spn::ErrorType::Initialization, "frequency count must be greater than 1");
+        float fc = float(count);
+        float step = powf(max / min, 1.0f / (fc - 1));
+        for (int i = 0; i < count; ++i) out[i] = min * powf(step, float(i));
+    });
+}
+
+extern "C" int spn_cutoff_exponential(float max, float min, float step, float *out, int cap, int *n) {
+    return spn::guarded([&] {
+        if (!n || (cap > 0 && !out)) throw spn::Error(spn::ErrorType::Argument, "spn_cutoff_exponential: null output");
+        if (!(min > 0)) throw spn::Error(spn::ErrorType::Initialization, "cutoff min must be positive");
+        if (!(max > min)) throw spn::Error(spn::ErrorType::Initialization, "cutoff max must be greater than min");
+        if (!(step > 0 && step < 1)) throw spn::Error(spn::ErrorType::Initialization, "cutoff step must be in (0,1)");
+        int k = 0;
+        float v = max;
+        while (v > min) {
+            if (k < cap) out[k] = v;
+            ++k;
+            v *= step;
+        }
+        *n = k;
+    });
+}
+
+extern "C" int spn_su2_initial_state(const spn_lattice *lat, int n_freq, float normalization, float *v2, float *v4ss,
+                                     float *v4dd) {
+    return spn::guarded([&] {
+        if (!lat || n_freq < 2) throw spn::Error(spn::ErrorType::Argument, "spn_su2_initial_state: bad argument");
+        const spn::Lattice &L = lat->lat;
+        const long long nl = L.size;
+        const long long fn = (long long)n_freq * n_freq * (n_freq + 1) / 2;
+        if (v2) std::memset(v2, 0, sizeof(float) * n_freq);
+        if (v4dd) std::memset(v4dd, 0, sizeof(float) * size_t(fn * nl));
+        if (v4ss) {
+            std::memset(v4ss, 0, sizeof(float) * size_t(fn * nl));
+            for (long long it = 0; it < fn; ++it)
+                for (const auto &ia : L.interactions) v4ss[it * nl + ia.rid] += ia.J[0][0] / normalization;
+        }
+    });
+}

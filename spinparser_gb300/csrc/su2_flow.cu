@@ -1,0 +1,1125 @@
+// GB300 (sm_103a) kernels of the SU(2) pf-FRG flow right-hand side and the device half of
+// the C ABI in include/spn_su2.h.
+//
+// One flow's state lives in HBM in the reference layout (vertex index
+// ((s(s+1)/2+u)*N + t)*Nl + rid, src/SU2/SU2VertexTwoParticle.hpp:603).  A compute step is
+//   1. su2_self_energy_kernel   Sigma-dot(w_i), one CTA per frequency   (SU2FrgCore.cpp:139-169)
+//   2. su2_node_table_kernel    per transfer frequency x: the loop-frequency nodes wp of the
+//                               conventional (wp = +-Lambda) and Katanin (trapezoid) terms with
+//                               their propagator x quadrature coefficients, in FP64
+//                               (SU2FrgCore.cpp:336-424, Integrator.hpp:137-287)
+//   3. su2_vertex_flow_kernel   Gamma-dot for every (s,t,u) triple (SU2FrgCore.cpp:171-431)
+// and finalize_step is su2_euler_kernel (SU2FrgCore.cpp:111-137).
+//
+// Vertex-flow work distribution: a persistent grid whose warps pull triples from a device
+// atomic counter (this replaces the reference's MPI/OpenMP LoadManager).  Inside a warp the
+// lanes are split into G groups of W lanes: lane = (loop-frequency node group, lattice site),
+// so each group evaluates one loop-frequency node for all Nl sites at once, the slab reads of
+// a support are one coalesced segment, and the group results are combined with warp shuffles.
+// The T-channel RPA lattice sum exchanges the per-site bubble values through shared memory.
+// Accumulation over loop frequencies is Kahan-compensated FP32.
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "su2_device.cuh"
+#include "host/capi_common.hpp"
+#include "../../include/spn_su2.h"
+
+using namespace spn;
+using namespace spn::dev;
+
+namespace {
+
+constexpr int kVertexThreads = 128;
+constexpr int kVertexWarps = kVertexThreads / 32;
+constexpr unsigned kStatusNaN = 1u;
+constexpr unsigned kStatusNodeOverflow = 2u;
+constexpr double kPiD = 3.14159265358979323846;
+
+struct FlowArgs {
+    int n, nl, fn, wsite, max_nodes, n_range;
+    float cutoff, spin;
+    const float *freq;
+    const float *ss, *dd;  // state
+    float *dss, *ddd;      // flow
+    const float *v2;       // self-energy state
+    float *dv2;            // self-energy flow
+    const int *sites, *inv_sites, *ov_ptr, *ov_r1, *ov_r2, *range_rid, *range_inv;
+    float *node_wp, *node_c;
+    int *node_cnt;
+    int *work_counter;
+    unsigned *status;
+};
+
+// ------------------------------------------------------------------------------------
+// 1. self-energy flow
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) su2_self_energy_kernel(FlowArgs a) {
+    __shared__ float pos[kMaxFreq];
+    __shared__ double red[4];
+    for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
+    __syncthreads();
+    const int i = blockIdx.x;
+    const float w = pos[i], L = a.cutoff;
+    const float wpl = w + L, wml = w - L;
+    double part = 0.0;
+    for (int j = threadIdx.x; j < a.n_range; j += blockDim.x) {
+        const int r12 = a.range_rid[j], r21 = a.range_inv[j];
+        float x1 = value_none(pos, a.n, a.nl, a.dd, true, r12, r21, wpl, 0.0f, wml);
+        float x2 = value_none(pos, a.n, a.nl, a.dd, true, r12, r21, wml, 0.0f, wpl);
+        part += double(x1) - double(x2);
+    }
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sum = 0.0;
+        for (int k = 0; k < int(blockDim.x >> 5); ++k) sum += red[k];
+        double val = -4.0 * double(a.spin) * sum;
+        val += 0.75 * (double(value_none(pos, a.n, a.nl, a.ss, false, 0, 0, wpl, wml, 0.0f)) -
+                       double(value_none(pos, a.n, a.nl, a.ss, false, 0, 0, wml, wpl, 0.0f)));
+        val += (double(value_none(pos, a.n, a.nl, a.dd, true, 0, 0, wpl, wml, 0.0f)) -
+                double(value_none(pos, a.n, a.nl, a.dd, true, 0, 0, wml, wpl, 0.0f)));
+        val /= (2.0 * kPiD * (double(L) + odd_interp(pos, a.n, a.v2, L)));
+        float out = float(val);
+        a.dv2[i] = out;
+        if (isnan(out)) atomicOr(a.status, kStatusNaN);
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// 2. loop-frequency node tables
+// ------------------------------------------------------------------------------------
+__global__ void su2_node_table_kernel(FlowArgs a) {
+    __shared__ float pos[kMaxFreq];
+    for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
+    __syncthreads();
+    const int xi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (xi >= a.n) return;
+    const int n = a.n;
+    const float x = pos[xi], L = a.cutoff;
+    float *wp_out = a.node_wp + size_t(xi) * a.max_nodes;
+    float *c_out = a.node_c + size_t(xi) * a.max_nodes;
+    int cnt = 0;
+    bool overflow = false;
+    auto put = [&](float wp, double c) {
+        if (cnt < a.max_nodes) {
+            wp_out[cnt] = wp;
+            c_out[cnt] = float(c);
+            ++cnt;
+        } else {
+            overflow = true;
+        }
+    };
+    auto sig = [&](float w) { return odd_interp(pos, n, a.v2, w); };
+    auto p = [&](float w1, float w2) { return 1.0 / ((double(w1) + sig(w1)) * (double(w2) + sig(w2))); };
+    auto pk = [&](float w1, float w2) {
+        double d1 = double(w1) + sig(w1);
+        return odd_interp(pos, n, a.dv2, w1) / (d1 * d1 * (double(w2) + sig(w2)));
+    };
+    // conventional contribution (SU2FrgCore.cpp:351-371)
+    put(L, p(L, L + x));
+    if (x > 2.0f * L) put(-L, p(L, L - x));
+    // Katanin contribution (SU2FrgCore.cpp:374-424)
+    auto kat = [&](float wp, double weight) { put(wp, weight * pk(wp, x + wp)); };
+    if (-(x + L) > -pos[n - 1]) nodes_right(pos, n, -(x + L), kat);
+    if (x - L > L) nodes_both(pos, n, L - x, -L, kat);
+    if (L < pos[n - 1]) nodes_left(pos, n, L, kat);
+    a.node_cnt[xi] = cnt;
+    if (overflow) atomicOr(a.status, kStatusNodeOverflow);
+}
+
+// ------------------------------------------------------------------------------------
+// 3. two-particle vertex flow
+// ------------------------------------------------------------------------------------
+template <int SPT>
+struct Lane {
+    int site[SPT], isite[SPT], j[SPT];
+    bool valid[SPT];
+};
+
+template <int SPT>
+__device__ __forceinline__ void gather(const FlowArgs &a, const AB4 &ab, const Lane<SPT> &ln, float *vs, float *vd) {
+#pragma unroll
+    for (int k = 0; k < SPT; ++k) {
+        const int st = ab.exch ? ln.isite[k] : ln.site[k];
+        float gs = 0.0f, gd = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            gs += ab.w[q] * __ldg(a.ss + ab.off[q] + st);
+            gd += ab.sw[q] * __ldg(a.dd + ab.off[q] + st);
+        }
+        vs[k] = gs;
+        vd[k] = gd;
+    }
+}
+
+__device__ __forceinline__ void local_values(const FlowArgs &a, const AB4 &ab, float &vs, float &vd) {
+    float gs = 0.0f, gd = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        gs += ab.w[q] * __ldg(a.ss + ab.off[q]);
+        gd += ab.sw[q] * __ldg(a.dd + ab.off[q]);
+    }
+    vs = gs;
+    vd = gd;
+}
+
+struct Transfer {
+    float s, t, u, w1p, w1, w2p, w2;
+};
+
+// integralKernelS (SU2FrgCore.cpp:199-227)
+template <int SPT>
+__device__ __forceinline__ void kernel_s(const FlowArgs &a, const float *pos, const Transfer &f, float wp, const Lane<SPT> &ln,
+                                         float *rs, float *rd) {
+    AB4 ab;
+    float S0[SPT], S1[SPT], S2[SPT], S3[SPT], D0[SPT], D1[SPT], D2[SPT], D3[SPT];
+    access4<kS>(pos, a.n, a.nl, f.s, -f.w1 - wp, -f.w2 - wp, ab);
+    gather(a, ab, ln, S0, D0);
+    access4<kS>(pos, a.n, a.nl, f.s, f.w1p + wp, -f.w2p - wp, ab);
+    gather(a, ab, ln, S1, D1);
+    access4<kS>(pos, a.n, a.nl, f.s, f.w2 + wp, f.w1 + wp, ab);
+    gather(a, ab, ln, S2, D2);
+    access4<kS>(pos, a.n, a.nl, f.s, -f.w2p - wp, f.w1p + wp, ab);
+    gather(a, ab, ln, S3, D3);
+#pragma unroll
+    for (int k = 0; k < SPT; ++k) {
+        float x = 0.0f;
+        x -= 0.5f * S0[k] * S1[k];
+        x -= 0.5f * S2[k] * S3[k];
+        x += D0[k] * S1[k];
+        x += D2[k] * S3[k];
+        x += S0[k] * D1[k];
+        x += S2[k] * D3[k];
+        float y = 0.0f;
+        y += (3.0f / 16.0f) * S0[k] * S1[k];
+        y += (3.0f / 16.0f) * S2[k] * S3[k];
+        y += D0[k] * D1[k];
+        y += D2[k] * D3[k];
+        rs[k] = x;
+        rd[k] = y;
+    }
+}
+
+// integralKernelU (SU2FrgCore.cpp:305-334)
+template <int SPT>
+__device__ __forceinline__ void kernel_u(const FlowArgs &a, const float *pos, const Transfer &f, float wp, const Lane<SPT> &ln,
+                                         float *rs, float *rd) {
+    AB4 ab;
+    float S0[SPT], S1[SPT], S2[SPT], S3[SPT], D0[SPT], D1[SPT], D2[SPT], D3[SPT];
+    access4<kU>(pos, a.n, a.nl, f.w1 + wp, wp - f.w2p, f.u, ab);
+    gather(a, ab, ln, S0, D0);
+    access4<kU>(pos, a.n, a.nl, f.w1p + wp, f.w2 - wp, f.u, ab);
+    gather(a, ab, ln, S1, D1);
+    access4<kU>(pos, a.n, a.nl, f.w2p - wp, -f.w1 - wp, f.u, ab);
+    gather(a, ab, ln, S2, D2);
+    access4<kU>(pos, a.n, a.nl, f.w2 - wp, f.w1p + wp, f.u, ab);
+    gather(a, ab, ln, S3, D3);
+#pragma unroll
+    for (int k = 0; k < SPT; ++k) {
+        float x = 0.0f;
+        x += 0.5f * S0[k] * S1[k];
+        x += 0.5f * S2[k] * S3[k];
+        x += S0[k] * D1[k];
+        x += S2[k] * D3[k];
+        x += D0[k] * S1[k];
+        x += D2[k] * S3[k];
+        float y = 0.0f;
+        y += (3.0f / 16.0f) * S0[k] * S1[k];
+        y += (3.0f / 16.0f) * S2[k] * S3[k];
+        y += D0[k] * D1[k];
+        y += D2[k] * D3[k];
+        rs[k] = x;
+        rd[k] = y;
+    }
+}
+
+// integralKernelT (SU2FrgCore.cpp:229-303).  `xb` is this group's shared-memory exchange
+// area: four arrays of `stride` floats (spin A, spin B, density A, density B by site).
+template <int SPT>
+__device__ __forceinline__ void kernel_t(const FlowArgs &a, const float *pos, const Transfer &f, float wp, const Lane<SPT> &ln,
+                                         float *xb, int stride, float *rs, float *rd) {
+    AB4 ab;
+    float S0[SPT], S1[SPT], S2[SPT], S3[SPT], D0[SPT], D1[SPT], D2[SPT], D3[SPT];
+    access4<kT>(pos, a.n, a.nl, f.w1 - wp, f.t, f.w1p + wp, ab);
+    gather(a, ab, ln, S0, D0);
+    access4<kT>(pos, a.n, a.nl, f.w2p - wp, f.t, -f.w2 - wp, ab);
+    gather(a, ab, ln, S1, D1);
+    access4<kT>(pos, a.n, a.nl, f.w1p + wp, f.t, f.w1 - wp, ab);
+    gather(a, ab, ln, S2, D2);
+    access4<kT>(pos, a.n, a.nl, f.w2 + wp, f.t, wp - f.w2p, ab);
+    gather(a, ab, ln, S3, D3);
+#pragma unroll
+    for (int k = 0; k < SPT; ++k)
+        if (ln.valid[k]) {
+            const int j = ln.j[k];
+            xb[j] = S2[k];
+            xb[stride + j] = S3[k];
+            xb[2 * stride + j] = D2[k];
+            xb[3 * stride + j] = D3[k];
+        }
+    __syncwarp();
+    float cbs, cbd, icas, icad, cbs2, cbd2, icas2, icad2;
+    access4<kU>(pos, a.n, a.nl, f.w2p - wp, -f.w2 - wp, f.t, ab);
+    local_values(a, ab, cbs, cbd);
+    access4<kU>(pos, a.n, a.nl, f.w1 - wp, -f.w1p - wp, -f.t, ab);
+    local_values(a, ab, icas, icad);
+    access4<kU>(pos, a.n, a.nl, f.w2 + wp, wp - f.w2p, f.t, ab);
+    local_values(a, ab, cbs2, cbd2);
+    access4<kU>(pos, a.n, a.nl, f.w1p + wp, wp - f.w1, -f.t, ab);
+    local_values(a, ab, icas2, icad2);
+    const float s2 = 2.0f * a.spin, s8 = 8.0f * a.spin;
+#pragma unroll
+    for (int k = 0; k < SPT; ++k) {
+        float rpa_s = 0.0f, rpa_d = 0.0f;
+        if (ln.valid[k]) {
+            const int rid = ln.j[k];
+            const int i0 = __ldg(a.ov_ptr + rid), i1 = __ldg(a.ov_ptr + rid + 1);
+            for (int i = i0; i < i1; ++i) {
+                const int r1 = __ldg(a.ov_r1 + i), r2 = __ldg(a.ov_r2 + i);
+                rpa_s += xb[r1] * xb[stride + r2];
+                rpa_d += xb[2 * stride + r1] * xb[3 * stride + r2];
+            }
+        }
+        float x = 0.0f + s2 * rpa_s;
+        x -= cbd * S0[k];
+        x += (0.25f * cbs) * S0[k];
+        x -= icad * S1[k];
+        x += (0.25f * icas) * S1[k];
+        x -= cbd2 * S2[k];
+        x += (0.25f * cbs2) * S2[k];
+        x -= icad2 * S3[k];
+        x += (0.25f * icas2) * S3[k];
+        float y = 0.0f + s8 * rpa_d;
+        y -= cbd * D0[k];
+        y -= (0.75f * cbs) * D0[k];
+        y -= icad * D1[k];
+        y -= (0.75f * icas) * D1[k];
+        y -= cbd2 * D2[k];
+        y -= (0.75f * cbs2) * D2[k];
+        y -= icad2 * D3[k];
+        y -= (0.75f * icas2) * D3[k];
+        rs[k] = x;
+        rd[k] = y;
+    }
+    __syncwarp();
+}
+
+__device__ __forceinline__ void kahan_add(float &sum, float &comp, float v) {
+    const float y = v - comp;
+    const float t = sum + y;
+    comp = (t - sum) - y;
+    sum = t;
+}
+
+template <int CH, int SPT>
+__device__ __forceinline__ void channel_sum(const FlowArgs &a, const float *pos, const Transfer &f, int xi, int g, int G,
+                                            const Lane<SPT> &ln, float *xb, int stride, float *acc_s, float *cmp_s,
+                                            float *acc_d, float *cmp_d) {
+    const int cnt = __ldg(a.node_cnt + xi);
+    const float *nwp = a.node_wp + size_t(xi) * a.max_nodes;
+    const float *nc = a.node_c + size_t(xi) * a.max_nodes;
+    const int trips = (cnt + G - 1) / G;
+    for (int r = 0; r < trips; ++r) {
+        const int k = r * G + g;
+        const bool active = k < cnt;
+        const float wp = active ? __ldg(nwp + k) : 0.0f;
+        float c = active ? __ldg(nc + k) : 0.0f;
+        if (CH == kU) c = -c;
+        float rs[SPT], rd[SPT];
+        if (CH == kS) kernel_s<SPT>(a, pos, f, wp, ln, rs, rd);
+        else if (CH == kT) kernel_t<SPT>(a, pos, f, wp, ln, xb, stride, rs, rd);
+        else kernel_u<SPT>(a, pos, f, wp, ln, rs, rd);
+        if (active) {
+#pragma unroll
+            for (int q = 0; q < SPT; ++q) {
+                kahan_add(acc_s[q], cmp_s[q], c * rs[q]);
+                kahan_add(acc_d[q], cmp_d[q], c * rd[q]);
+            }
+        }
+    }
+}
+
+template <int SPT>
+__global__ void __launch_bounds__(kVertexThreads) su2_vertex_flow_kernel(FlowArgs a) {
+    extern __shared__ float smem[];
+    float *pos = smem;
+    for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int W = (SPT == 1) ? a.wsite : 32;
+    const int G = 32 / W;
+    const int g = lane / W, jl = lane - g * W;
+    const int stride = 32 * SPT;
+    float *xb = smem + kMaxFreq + warp * 4 * stride + (SPT == 1 ? g * W : 0);
+
+    Lane<SPT> ln;
+#pragma unroll
+    for (int k = 0; k < SPT; ++k) {
+        const int j = jl + k * W;
+        ln.j[k] = j;
+        ln.valid[k] = j < a.nl;
+        ln.site[k] = ln.valid[k] ? a.sites[j] : 0;
+        ln.isite[k] = ln.valid[k] ? a.inv_sites[j] : 0;
+    }
+    const float two_pi = 2.0f * float(kPiD);
+
+    for (;;) {
+        int it = 0;
+        if (lane == 0) it = atomicAdd(a.work_counter, 1);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= a.fn) break;
+        const int su = it / a.n, ti = it - su * a.n;
+        int si = int((sqrtf(8.0f * float(su) + 1.0f) - 1.0f) * 0.5f);
+        while (si * (si + 1) / 2 > su) --si;
+        while ((si + 1) * (si + 2) / 2 <= su) ++si;
+        const int ui = su - si * (si + 1) / 2;
+
+        Transfer f;
+        f.s = pos[si];
+        f.t = pos[ti];
+        f.u = pos[ui];
+        f.w1p = 0.5f * (f.s + f.t + f.u);
+        f.w1 = 0.5f * (f.s - f.t + f.u);
+        f.w2p = 0.5f * (f.s - f.t - f.u);
+        f.w2 = 0.5f * (f.s + f.t - f.u);
+
+        float acc_s[SPT], cmp_s[SPT], acc_d[SPT], cmp_d[SPT];
+#pragma unroll
+        for (int k = 0; k < SPT; ++k) acc_s[k] = cmp_s[k] = acc_d[k] = cmp_d[k] = 0.0f;
+        channel_sum<kS, SPT>(a, pos, f, si, g, G, ln, xb, stride, acc_s, cmp_s, acc_d, cmp_d);
+        channel_sum<kT, SPT>(a, pos, f, ti, g, G, ln, xb, stride, acc_s, cmp_s, acc_d, cmp_d);
+        channel_sum<kU, SPT>(a, pos, f, ui, g, G, ln, xb, stride, acc_s, cmp_s, acc_d, cmp_d);
+
+#pragma unroll
+        for (int k = 0; k < SPT; ++k) {
+            float vs = acc_s[k] - cmp_s[k], vd = acc_d[k] - cmp_d[k];
+            for (int o = W; o < 32; o <<= 1) {
+                vs += __shfl_xor_sync(0xffffffffu, vs, o);
+                vd += __shfl_xor_sync(0xffffffffu, vd, o);
+            }
+            if (g == 0 && ln.valid[k]) {
+                const float os = vs / two_pi, od = vd / two_pi;
+                const size_t idx = size_t(it) * a.nl + ln.j[k];
+                a.dss[idx] = os;
+                a.ddd[idx] = od;
+                if (isnan(os) || isnan(od)) atomicOr(a.status, kStatusNaN);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// Euler step  x += step * dx  (rounded like the reference: product, then sum)
+// ------------------------------------------------------------------------------------
+__global__ void su2_euler_kernel(float *__restrict__ x, const float *__restrict__ dx, long long n, float step) {
+    const long long n4 = n / 4;
+    float4 *x4 = reinterpret_cast<float4 *>(x);
+    const float4 *d4 = reinterpret_cast<const float4 *>(dx);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += (long long)gridDim.x * blockDim.x) {
+        float4 v = x4[i], d = __ldg(d4 + i);
+        v.x = __fadd_rn(v.x, __fmul_rn(step, d.x));
+        v.y = __fadd_rn(v.y, __fmul_rn(step, d.y));
+        v.z = __fadd_rn(v.z, __fmul_rn(step, d.z));
+        v.w = __fadd_rn(v.w, __fmul_rn(step, d.w));
+        x4[i] = v;
+    }
+    for (long long i = 4 * n4 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        x[i] = __fadd_rn(x[i], __fmul_rn(step, dx[i]));
+}
+
+// ------------------------------------------------------------------------------------
+// correlation measurement (nu = 0), SU2MeasurementCorrelation.cpp:77-177
+// ------------------------------------------------------------------------------------
+struct CorrArgs {
+    int n, nl, n_corr;
+    float cutoff, spin;
+    const float *freq, *ss, *dd, *v2;
+    const int *sites, *inv_sites, *corr_rid;
+    double *partial;  // [max_nodes][2][nl]
+    float *out;       // zz[n_corr], dd[n_corr], chi_s[nl], chi_d[nl]
+    int wsite;
+};
+
+// Loop-frequency nodes of the measurement's trapezoid rules at nu = 0 (outer and inner
+// integrals use the same ranges): (-inf, -cutoff] and [cutoff, inf).
+__device__ int corr_nodes(const float *pos, int n, float cut, float *wp, double *w) {
+    int cnt = 0;
+    auto put = [&](float x, double c) {
+        wp[cnt] = x;
+        w[cnt] = c;
+        ++cnt;
+    };
+    if (-(0.0f + cut) > -pos[n - 1]) nodes_right(pos, n, -cut - 0.0f, put);
+    if (cut < pos[n - 1]) nodes_left(pos, n, cut, put);
+    return cnt;
+}
+
+constexpr int kMaxCorrNodes = 2 * kMaxFreq + 8;
+
+template <int SPT>
+__global__ void __launch_bounds__(128) su2_corr_inner_kernel(CorrArgs a) {
+    __shared__ float pos[kMaxFreq];
+    __shared__ float nwp[kMaxCorrNodes];
+    __shared__ double nw[kMaxCorrNodes];
+    __shared__ int ncnt;
+    __shared__ double red[4][2][32 * SPT];
+    for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
+    __syncthreads();
+    if (threadIdx.x == 0) ncnt = corr_nodes(pos, a.n, a.cutoff, nwp, nw);
+    __syncthreads();
+    const int ia = blockIdx.x;
+    if (ia >= ncnt) return;
+    const float w = nwp[ia];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int W = (SPT == 1) ? a.wsite : 32;
+    const int G = 32 / W;
+    const int g = lane / W, jl = lane - g * W;
+    const int nl = a.nl;
+    int site[SPT], isite[SPT];
+    bool valid[SPT];
+    for (int k = 0; k < SPT; ++k) {
+        const int j = jl + k * W;
+        valid[k] = j < nl;
+        site[k] = valid[k] ? a.sites[j] : 0;
+        isite[k] = valid[k] ? a.inv_sites[j] : 0;
+    }
+    const double S = a.spin;
+    auto sig = [&](float x) { return odd_interp(pos, a.n, a.v2, x); };
+    const double dw = double(w) + sig(w);
+    double acc_s[SPT], acc_d[SPT];
+    for (int k = 0; k < SPT; ++k) acc_s[k] = acc_d[k] = 0.0;
+    const int groups = kVertexWarps * G;
+    const int gid = warp * G + g;
+    for (int b = gid; b < ncnt; b += groups) {
+        const float wp = nwp[b];
+        AB8 ab;
+        access8(pos, a.n, nl, w + wp + 0.0f, 0.0f, w - wp, ab);
+        const float vs = value_none(pos, a.n, nl, a.ss, false, 0, 0, w + wp + 0.0f, w - wp, 0.0f);
+        const float vd = value_none(pos, a.n, nl, a.dd, true, 0, 0, w + wp + 0.0f, w - wp, 0.0f);
+        const double dwp = double(wp) + sig(wp);
+        const double norm = 1.0 / (dw * dw * dwp * dwp * (4.0 * kPiD * kPiD));
+        const double cw = nw[b] * norm;
+        for (int k = 0; k < SPT; ++k) {
+            const int st = ab.exch ? isite[k] : site[k];
+            float gs = 0.0f, gd = 0.0f;
+            for (int q = 0; q < 8; ++q) {
+                gs += ab.w[q] * __ldg(a.ss + ab.off[q] + st);
+                gd += ab.sw[q] * __ldg(a.dd + ab.off[q] + st);
+            }
+            double rs = -S * S * double(gs);
+            double rd = -16.0 * S * S * double(gd);
+            if (jl + k * W == 0) {
+                rs += S * (-double(vs) / 4.0 + double(vd));
+                rd += S * (3.0 * double(vs) + 4.0 * double(vd));
+            }
+            if (valid[k]) {
+                acc_s[k] += cw * rs;
+                acc_d[k] += cw * rd;
+            }
+        }
+    }
+    for (int k = 0; k < SPT; ++k) {
+        for (int o = W; o < 32; o <<= 1) {
+            acc_s[k] += __shfl_xor_sync(0xffffffffu, acc_s[k], o);
+            acc_d[k] += __shfl_xor_sync(0xffffffffu, acc_d[k], o);
+        }
+        if (g == 0) {
+            red[warp][0][jl + k * W] = acc_s[k];
+            red[warp][1][jl + k * W] = acc_d[k];
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < nl; j += blockDim.x) {
+        double s = 0.0, d = 0.0;
+        for (int q = 0; q < kVertexWarps; ++q) {
+            s += red[q][0][j];
+            d += red[q][1][j];
+        }
+        a.partial[(size_t(ia) * 2 + 0) * nl + j] = s;
+        a.partial[(size_t(ia) * 2 + 1) * nl + j] = d;
+    }
+}
+
+__global__ void su2_corr_final_kernel(CorrArgs a) {
+    __shared__ float pos[kMaxFreq];
+    __shared__ float nwp[kMaxCorrNodes];
+    __shared__ double nw[kMaxCorrNodes];
+    __shared__ int ncnt;
+    extern __shared__ double chi[];  // [2][nl]
+    for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
+    __syncthreads();
+    if (threadIdx.x == 0) ncnt = corr_nodes(pos, a.n, a.cutoff, nwp, nw);
+    __syncthreads();
+    const double S = a.spin;
+    for (int j = threadIdx.x; j < a.nl; j += blockDim.x) {
+        double cs = 0.0, cd = 0.0;
+        for (int ia = 0; ia < ncnt; ++ia) {
+            double ls = a.partial[(size_t(ia) * 2 + 0) * a.nl + j];
+            double ld = a.partial[(size_t(ia) * 2 + 1) * a.nl + j];
+            if (j == 0) {
+                const float w = nwp[ia];
+                const double dw = double(w) + odd_interp(pos, a.n, a.v2, w);
+                const double t1 = 1.0 / (dw * dw);
+                ls += S * t1 / (2.0 * kPiD);
+                ld += 2.0 * S * t1 / kPiD;
+            }
+            cs += nw[ia] * ls;
+            cd += nw[ia] * ld;
+        }
+        chi[j] = cs;
+        chi[a.nl + j] = cd;
+        a.out[2 * a.n_corr + j] = float(cs);
+        a.out[2 * a.n_corr + a.nl + j] = float(cd);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < a.n_corr; q += blockDim.x) {
+        const int r = a.corr_rid[q];
+        a.out[q] = float(chi[r]);
+        a.out[a.n_corr + q] = float(chi[a.nl + r]);
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// FP32 FMA throughput probe: independent FMA chains, no memory traffic (the roofline
+// denominator for the vertex-flow kernel, which runs on the FP32 CUDA cores).
+// ------------------------------------------------------------------------------------
+constexpr int kPeakChains = 8;
+constexpr int kPeakIters = 4096;
+
+__global__ void __launch_bounds__(256) fp32_peak_kernel(float *out, float seed) {
+    float a[kPeakChains];
+#pragma unroll
+    for (int k = 0; k < kPeakChains; ++k) a[k] = seed + float(threadIdx.x + k);
+    const float m = 0.999999f, c = 1e-7f;
+    for (int i = 0; i < kPeakIters; ++i) {
+#pragma unroll
+        for (int k = 0; k < kPeakChains; ++k) a[k] = fmaf(a[k], m, c);
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kPeakChains; ++k) s += a[k];
+    if (s == 12345.678f) out[0] = s;  // keeps the chains live
+}
+
+// ------------------------------------------------------------------------------------
+// host helpers
+// ------------------------------------------------------------------------------------
+void cuda_check(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) throw Error(ErrorType::Cuda, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int wsite_for(int nl) {
+    if (nl > 32) return 32;
+    int w = 1;
+    while (w < nl) w <<= 1;
+    return w;
+}
+
+int spt_for(int nl) { return nl <= 32 ? 1 : (nl <= 64 ? 2 : 4); }
+
+constexpr int kMaxSites = 128;
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------
+// the flow handle
+// ------------------------------------------------------------------------------------
+struct spn_su2 {
+    int device = 0;
+    int n = 0, nl = 0, n_range = 0, n_corr = 0, max_nodes = 0, flags = 0, n_overlap = 0;
+    long long fn = 0;
+    float spin = 0.5f, cutoff = 0.0f;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int vertex_grid = 0;
+    float *freq = nullptr, *ss = nullptr, *dd = nullptr, *dss = nullptr, *ddd = nullptr, *v2 = nullptr, *dv2 = nullptr;
+    float *node_wp = nullptr, *node_c = nullptr, *corr_out = nullptr;
+    int *node_cnt = nullptr, *work_counter = nullptr;
+    unsigned *status = nullptr;
+    int *sites = nullptr, *inv_sites = nullptr, *ov_ptr = nullptr, *ov_r1 = nullptr, *ov_r2 = nullptr;
+    int *range_rid = nullptr, *range_inv = nullptr, *corr_rid = nullptr;
+    double *corr_partial = nullptr;
+    bool profiling = false;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<int, int>> ev_vertex, ev_step;  // indices into ev_pool
+
+    FlowArgs args() const {
+        FlowArgs a;
+        a.n = n;
+        a.nl = nl;
+        a.fn = int(fn);
+        a.wsite = wsite_for(nl);
+        a.max_nodes = max_nodes;
+        a.n_range = n_range;
+        a.cutoff = cutoff;
+        a.spin = spin;
+        a.freq = freq;
+        a.ss = ss;
+        a.dd = dd;
+        a.dss = dss;
+        a.ddd = ddd;
+        a.v2 = v2;
+        a.dv2 = dv2;
+        a.sites = sites;
+        a.inv_sites = inv_sites;
+        a.ov_ptr = ov_ptr;
+        a.ov_r1 = ov_r1;
+        a.ov_r2 = ov_r2;
+        a.range_rid = range_rid;
+        a.range_inv = range_inv;
+        a.node_wp = node_wp;
+        a.node_c = node_c;
+        a.node_cnt = node_cnt;
+        a.work_counter = work_counter;
+        a.status = status;
+        return a;
+    }
+
+    int event() {
+        cudaEvent_t e;
+        cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+        ev_pool.push_back(e);
+        return int(ev_pool.size()) - 1;
+    }
+
+    void release() {
+        cudaSetDevice(device);
+        for (auto e : ev_pool) cudaEventDestroy(e);
+        ev_pool.clear();
+        void *ptrs[] = {freq, ss, dd, dss, ddd, v2, dv2, node_wp, node_c, corr_out, node_cnt, work_counter, status,
+                        sites, inv_sites, ov_ptr, ov_r1, ov_r2, range_rid, range_inv, corr_rid, corr_partial};
+        for (void *p : ptrs)
+            if (p) cudaFree(p);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+template <class T>
+T *dev_alloc(size_t count, const char *what) {
+    void *p = nullptr;
+    cuda_check(cudaMalloc(&p, count * sizeof(T) + 16), what);
+    return static_cast<T *>(p);
+}
+
+template <class T>
+void upload(T *dst, const T *src, size_t count, cudaStream_t s) {
+    if (count) cuda_check(cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync H2D");
+}
+
+size_t vertex_smem_bytes(int spt) { return sizeof(float) * (kMaxFreq + kVertexWarps * 4 * 32 * spt); }
+
+void launch_vertex(spn_su2 *h) {
+    FlowArgs a = h->args();
+    const int spt = spt_for(h->nl);
+    const size_t smem = vertex_smem_bytes(spt);
+    if (spt == 1) su2_vertex_flow_kernel<1><<<h->vertex_grid, kVertexThreads, smem, h->stream>>>(a);
+    else if (spt == 2) su2_vertex_flow_kernel<2><<<h->vertex_grid, kVertexThreads, smem, h->stream>>>(a);
+    else su2_vertex_flow_kernel<4><<<h->vertex_grid, kVertexThreads, smem, h->stream>>>(a);
+    cuda_check(cudaGetLastError(), "vertex flow launch");
+}
+
+void validate_desc(const spn_su2_desc *d) {
+    if (!d) throw Error(ErrorType::Argument, "null descriptor");
+    if (d->n_freq < 2 || d->n_freq > kMaxFreq)
+        throw Error(ErrorType::Unsupported, "n_freq must be in [2, " + std::to_string(kMaxFreq) + "]");
+    if (d->n_sites < 1 || d->n_sites > kMaxSites)
+        throw Error(ErrorType::Unsupported, "n_sites must be in [1, " + std::to_string(kMaxSites) + "]");
+    if (!d->freq || !d->sites_rid || !d->inv_sites_rid || !d->overlap_ptr || (d->n_range > 0 && (!d->range_rid || !d->range_inv_rid)) ||
+        (d->n_corr > 0 && !d->corr_rid))
+        throw Error(ErrorType::Argument, "descriptor table pointer is NULL");
+    for (int i = 0; i < d->n_freq; ++i) {
+        if (!(d->freq[i] > 0.0f)) throw Error(ErrorType::Argument, "frequencies must be positive");
+        if (i > 0 && !(d->freq[i] > d->freq[i - 1])) throw Error(ErrorType::Argument, "frequencies must be strictly ascending");
+    }
+    const long long fn = (long long)d->n_freq * d->n_freq * (d->n_freq + 1) / 2;
+    if (fn * d->n_sites >= (1ll << 31)) throw Error(ErrorType::Unsupported, "vertex larger than 2^31 elements");
+    auto in_range = [&](const int *v, int cnt, int hi, const char *what) {
+        for (int i = 0; i < cnt; ++i)
+            if (v[i] < 0 || v[i] >= hi) throw Error(ErrorType::Argument, std::string(what) + " entry out of range");
+    };
+    in_range(d->sites_rid, d->n_sites, d->n_sites, "sites_rid");
+    in_range(d->inv_sites_rid, d->n_sites, d->n_sites, "inv_sites_rid");
+    if (d->overlap_ptr[0] != 0) throw Error(ErrorType::Argument, "overlap_ptr[0] must be 0");
+    for (int r = 0; r < d->n_sites; ++r)
+        if (d->overlap_ptr[r + 1] < d->overlap_ptr[r]) throw Error(ErrorType::Argument, "overlap_ptr must be non-decreasing");
+    const int nov = d->overlap_ptr[d->n_sites];
+    if (nov > 0 && (!d->overlap_rid1 || !d->overlap_rid2)) throw Error(ErrorType::Argument, "overlap pair table is NULL");
+    in_range(d->overlap_rid1, nov, d->n_sites, "overlap_rid1");
+    in_range(d->overlap_rid2, nov, d->n_sites, "overlap_rid2");
+    in_range(d->range_rid, d->n_range, d->n_sites, "range_rid");
+    in_range(d->range_inv_rid, d->n_range, d->n_sites, "range_inv_rid");
+    in_range(d->corr_rid, d->n_corr, d->n_sites, "corr_rid");
+}
+
+}  // namespace
+
+extern "C" int spn_device_count(int *count) {
+    return guarded([&] {
+        if (!count) throw Error(ErrorType::Argument, "null count");
+        int c = 0;
+        if (cudaGetDeviceCount(&c) != cudaSuccess) c = 0;
+        cudaGetLastError();
+        *count = c;
+    });
+}
+
+extern "C" int spn_measure_fp32_peak(int device, double *tflops, double *sm_clock_ghz_est) {
+    return guarded([&] {
+        if (!tflops) throw Error(ErrorType::Argument, "null output");
+        cuda_check(cudaSetDevice(device), "cudaSetDevice");
+        int sms = 0;
+        cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "device attribute");
+        float *out = nullptr;
+        cuda_check(cudaMalloc(&out, sizeof(float)), "alloc");
+        cudaEvent_t e0, e1;
+        cuda_check(cudaEventCreate(&e0), "event");
+        cuda_check(cudaEventCreate(&e1), "event");
+        const int blocks = sms * 8, threads = 256;
+        double best = 0.0;
+        for (int rep = 0; rep < 6; ++rep) {
+            cuda_check(cudaEventRecord(e0), "record");
+            fp32_peak_kernel<<<blocks, threads>>>(out, 1.0f + rep);
+            cuda_check(cudaEventRecord(e1), "record");
+            cuda_check(cudaEventSynchronize(e1), "sync");
+            float ms = 0.0f;
+            cuda_check(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+            const double flops = 2.0 * double(blocks) * threads * kPeakChains * kPeakIters;
+            if (rep > 0) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFree(out);
+        *tflops = best;
+        // 128 FP32 lanes x 2 flops per SM per clock
+        if (sm_clock_ghz_est) *sm_clock_ghz_est = best * 1e12 / (double(sms) * 256.0) / 1e9;
+    });
+}
+
+extern "C" int spn_su2_create(const spn_su2_desc *d, spn_su2 **out) {
+    return guarded([&] {
+        if (!out) throw Error(ErrorType::Argument, "null output handle");
+        validate_desc(d);
+        auto *h = new spn_su2;
+        try {
+            h->device = d->device;
+            cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+            h->n = d->n_freq;
+            h->nl = d->n_sites;
+            h->fn = (long long)h->n * h->n * (h->n + 1) / 2;
+            h->n_range = d->n_range;
+            h->n_corr = d->n_corr;
+            h->n_overlap = d->overlap_ptr[d->n_sites];
+            h->flags = d->flags;
+            h->spin = d->spin_length;
+            h->max_nodes = 2 * h->n + 8;
+            cuda_check(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+            h->own_stream = true;
+            const size_t vsz = size_t(h->fn) * h->nl;
+            h->freq = dev_alloc<float>(h->n, "alloc freq");
+            h->ss = dev_alloc<float>(vsz, "alloc v4ss");
+            h->dd = dev_alloc<float>(vsz, "alloc v4dd");
+            h->dss = dev_alloc<float>(vsz, "alloc dv4ss");
+            h->ddd = dev_alloc<float>(vsz, "alloc dv4dd");
+            h->v2 = dev_alloc<float>(h->n, "alloc v2");
+            h->dv2 = dev_alloc<float>(h->n, "alloc dv2");
+            h->node_wp = dev_alloc<float>(size_t(h->n) * h->max_nodes, "alloc node table");
+            h->node_c = dev_alloc<float>(size_t(h->n) * h->max_nodes, "alloc node table");
+            h->node_cnt = dev_alloc<int>(h->n, "alloc node counts");
+            h->work_counter = dev_alloc<int>(1, "alloc work counter");
+            h->status = dev_alloc<unsigned>(1, "alloc status");
+            h->sites = dev_alloc<int>(h->nl, "alloc sites");
+            h->inv_sites = dev_alloc<int>(h->nl, "alloc inv sites");
+            h->ov_ptr = dev_alloc<int>(h->nl + 1, "alloc overlap ptr");
+            h->ov_r1 = dev_alloc<int>(h->n_overlap + 1, "alloc overlap");
+            h->ov_r2 = dev_alloc<int>(h->n_overlap + 1, "alloc overlap");
+            h->range_rid = dev_alloc<int>(h->n_range + 1, "alloc range");
+            h->range_inv = dev_alloc<int>(h->n_range + 1, "alloc range");
+            h->corr_rid = dev_alloc<int>(h->n_corr + 1, "alloc corr map");
+            h->corr_partial = dev_alloc<double>(size_t(kMaxCorrNodes) * 2 * h->nl, "alloc corr scratch");
+            h->corr_out = dev_alloc<float>(2 * size_t(h->n_corr) + 2 * h->nl, "alloc corr out");
+            upload(h->freq, d->freq, h->n, h->stream);
+            upload(h->sites, d->sites_rid, h->nl, h->stream);
+            upload(h->inv_sites, d->inv_sites_rid, h->nl, h->stream);
+            upload(h->ov_ptr, d->overlap_ptr, h->nl + 1, h->stream);
+            upload(h->ov_r1, d->overlap_rid1, h->n_overlap, h->stream);
+            upload(h->ov_r2, d->overlap_rid2, h->n_overlap, h->stream);
+            upload(h->range_rid, d->range_rid, h->n_range, h->stream);
+            upload(h->range_inv, d->range_inv_rid, h->n_range, h->stream);
+            upload(h->corr_rid, d->corr_rid, h->n_corr, h->stream);
+            cuda_check(cudaMemsetAsync(h->ss, 0, vsz * sizeof(float), h->stream), "memset");
+            cuda_check(cudaMemsetAsync(h->dd, 0, vsz * sizeof(float), h->stream), "memset");
+            cuda_check(cudaMemsetAsync(h->dss, 0, vsz * sizeof(float), h->stream), "memset");
+            cuda_check(cudaMemsetAsync(h->ddd, 0, vsz * sizeof(float), h->stream), "memset");
+            cuda_check(cudaMemsetAsync(h->v2, 0, h->n * sizeof(float), h->stream), "memset");
+            cuda_check(cudaMemsetAsync(h->dv2, 0, h->n * sizeof(float), h->stream), "memset");
+            cuda_check(cudaMemsetAsync(h->status, 0, sizeof(unsigned), h->stream), "memset");
+            // persistent vertex grid: every SM filled to its occupancy limit
+            int sms = 0, per_sm = 0;
+            cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device), "device attribute");
+            const int spt = spt_for(h->nl);
+            const size_t smem = vertex_smem_bytes(spt);
+            if (spt == 1)
+                cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, su2_vertex_flow_kernel<1>, kVertexThreads, smem), "occupancy");
+            else if (spt == 2)
+                cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, su2_vertex_flow_kernel<2>, kVertexThreads, smem), "occupancy");
+            else
+                cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, su2_vertex_flow_kernel<4>, kVertexThreads, smem), "occupancy");
+            h->vertex_grid = sms * (per_sm > 0 ? per_sm : 1);
+            cuda_check(cudaStreamSynchronize(h->stream), "create sync");
+        } catch (...) {
+            h->release();
+            delete h;
+            throw;
+        }
+        *out = h;
+    });
+}
+
+extern "C" int spn_su2_destroy(spn_su2 *h) {
+    if (!h) return SPN_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    h->release();
+    delete h;
+    return SPN_OK;
+}
+
+extern "C" int spn_su2_set_stream(spn_su2 *h, void *stream) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        cuda_check(cudaStreamSynchronize(h->stream), "stream sync");
+        if (stream) {
+            if (h->own_stream) cudaStreamDestroy(h->stream);
+            h->stream = static_cast<cudaStream_t>(stream);
+            h->own_stream = false;
+        } else if (!h->own_stream) {
+            cuda_check(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+            h->own_stream = true;
+        }
+    });
+}
+
+extern "C" int spn_su2_get_sizes(const spn_su2 *h, int *n_freq, int *n_sites, long long *n_triples) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        if (n_freq) *n_freq = h->n;
+        if (n_sites) *n_sites = h->nl;
+        if (n_triples) *n_triples = h->fn;
+    });
+}
+
+extern "C" int spn_su2_set_state(spn_su2 *h, float cutoff, const float *v2, const float *v4ss, const float *v4dd) {
+    return guarded([&] {
+        if (!h || !v2 || !v4ss || !v4dd) throw Error(ErrorType::Argument, "null argument");
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        const size_t vsz = size_t(h->fn) * h->nl;
+        upload(h->v2, v2, h->n, h->stream);
+        upload(h->ss, v4ss, vsz, h->stream);
+        upload(h->dd, v4dd, vsz, h->stream);
+        h->cutoff = cutoff;
+        cuda_check(cudaStreamSynchronize(h->stream), "set_state sync");
+    });
+}
+
+extern "C" int spn_su2_get_state(spn_su2 *h, float *cutoff, float *v2, float *v4ss, float *v4dd) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        const size_t vsz = size_t(h->fn) * h->nl;
+        if (cutoff) *cutoff = h->cutoff;
+        if (v2) cuda_check(cudaMemcpyAsync(v2, h->v2, h->n * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        if (v4ss) cuda_check(cudaMemcpyAsync(v4ss, h->ss, vsz * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        if (v4dd) cuda_check(cudaMemcpyAsync(v4dd, h->dd, vsz * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        cuda_check(cudaStreamSynchronize(h->stream), "get_state sync");
+    });
+}
+
+extern "C" int spn_su2_compute_step(spn_su2 *h) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        int e0 = -1, e1 = -1, e2 = -1;
+        if (h->profiling) {
+            e0 = h->event();
+            cuda_check(cudaEventRecord(h->ev_pool[e0], h->stream), "event record");
+        }
+        cuda_check(cudaMemsetAsync(h->status, 0, sizeof(unsigned), h->stream), "memset status");
+        cuda_check(cudaMemsetAsync(h->work_counter, 0, sizeof(int), h->stream), "memset counter");
+        FlowArgs a = h->args();
+        su2_self_energy_kernel<<<h->n, 128, 0, h->stream>>>(a);
+        cuda_check(cudaGetLastError(), "self-energy launch");
+        su2_node_table_kernel<<<(h->n + 63) / 64, 64, 0, h->stream>>>(a);
+        cuda_check(cudaGetLastError(), "node table launch");
+        if (h->profiling) {
+            e1 = h->event();
+            cuda_check(cudaEventRecord(h->ev_pool[e1], h->stream), "event record");
+        }
+        launch_vertex(h);
+        if (h->profiling) {
+            e2 = h->event();
+            cuda_check(cudaEventRecord(h->ev_pool[e2], h->stream), "event record");
+            h->ev_vertex.emplace_back(e1, e2);
+            h->ev_step.emplace_back(e0, e2);
+        }
+    });
+}
+
+extern "C" int spn_su2_get_flow(spn_su2 *h, float *dv2, float *dv4ss, float *dv4dd) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        const size_t vsz = size_t(h->fn) * h->nl;
+        if (dv2) cuda_check(cudaMemcpyAsync(dv2, h->dv2, h->n * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        if (dv4ss) cuda_check(cudaMemcpyAsync(dv4ss, h->dss, vsz * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        if (dv4dd) cuda_check(cudaMemcpyAsync(dv4dd, h->ddd, vsz * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        cuda_check(cudaStreamSynchronize(h->stream), "get_flow sync");
+    });
+}
+
+extern "C" int spn_su2_finalize_step(spn_su2 *h, float new_cutoff) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        const float step = new_cutoff - h->cutoff;
+        const long long vsz = h->fn * h->nl;
+        su2_euler_kernel<<<1, 64, 0, h->stream>>>(h->v2, h->dv2, h->n, step);
+        const int grid = int(std::min<long long>((vsz / 4 + 255) / 256 + 1, 4096));
+        su2_euler_kernel<<<grid, 256, 0, h->stream>>>(h->dd, h->ddd, vsz, step);
+        su2_euler_kernel<<<grid, 256, 0, h->stream>>>(h->ss, h->dss, vsz, step);
+        cuda_check(cudaGetLastError(), "euler launch");
+        h->cutoff = new_cutoff;
+    });
+}
+
+namespace {
+
+void launch_correlation(spn_su2 *h) {
+        CorrArgs a;
+        a.n = h->n;
+        a.nl = h->nl;
+        a.n_corr = h->n_corr;
+        a.cutoff = h->cutoff;
+        a.spin = h->spin;
+        a.freq = h->freq;
+        a.ss = h->ss;
+        a.dd = h->dd;
+        a.v2 = h->v2;
+        a.sites = h->sites;
+        a.inv_sites = h->inv_sites;
+        a.corr_rid = h->corr_rid;
+        a.partial = h->corr_partial;
+        a.out = h->corr_out;
+        a.wsite = wsite_for(h->nl);
+        const int spt = spt_for(h->nl);
+        const int blocks = 2 * h->n + 4;
+        if (spt == 1) su2_corr_inner_kernel<1><<<blocks, 128, 0, h->stream>>>(a);
+        else if (spt == 2) su2_corr_inner_kernel<2><<<blocks, 128, 0, h->stream>>>(a);
+        else su2_corr_inner_kernel<4><<<blocks, 128, 0, h->stream>>>(a);
+        cuda_check(cudaGetLastError(), "correlation launch");
+        su2_corr_final_kernel<<<1, 128, 2 * h->nl * sizeof(double), h->stream>>>(a);
+        cuda_check(cudaGetLastError(), "correlation final launch");
+}
+
+void copy_correlation(spn_su2 *h, float *zz, float *dd, float *chi_zz, float *chi_dd) {
+        if (zz) cuda_check(cudaMemcpyAsync(zz, h->corr_out, h->n_corr * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        if (dd)
+            cuda_check(cudaMemcpyAsync(dd, h->corr_out + h->n_corr, h->n_corr * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        if (chi_zz)
+            cuda_check(cudaMemcpyAsync(chi_zz, h->corr_out + 2 * h->n_corr, h->nl * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        if (chi_dd)
+            cuda_check(cudaMemcpyAsync(chi_dd, h->corr_out + 2 * h->n_corr + h->nl, h->nl * sizeof(float), cudaMemcpyDeviceToHost, h->stream),
+                       "D2H");
+        cuda_check(cudaStreamSynchronize(h->stream), "correlation sync");
+}
+
+}  // namespace
+
+extern "C" int spn_su2_measure_correlation(spn_su2 *h, float *zz, float *dd, float *chi_zz, float *chi_dd) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        launch_correlation(h);
+        copy_correlation(h, zz, dd, chi_zz, chi_dd);
+    });
+}
+
+extern "C" int spn_su2_launch_correlation(spn_su2 *h) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        launch_correlation(h);
+    });
+}
+
+extern "C" int spn_su2_get_correlation(spn_su2 *h, float *zz, float *dd, float *chi_zz, float *chi_dd) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        copy_correlation(h, zz, dd, chi_zz, chi_dd);
+    });
+}
+
+extern "C" int spn_su2_is_diverged(spn_su2 *h, int *diverged) {
+    return guarded([&] {
+        if (!h || !diverged) throw Error(ErrorType::Argument, "null argument");
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        unsigned st = 0;
+        cuda_check(cudaMemcpyAsync(&st, h->status, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        cuda_check(cudaStreamSynchronize(h->stream), "status sync");
+        if (st & kStatusNodeOverflow) throw Error(ErrorType::Device, "loop-frequency node table overflow");
+        *diverged = (st & kStatusNaN) ? 1 : 0;
+    });
+}
+
+extern "C" int spn_su2_synchronize(spn_su2 *h) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        cuda_check(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize");
+    });
+}
+
+extern "C" int spn_su2_set_profiling(spn_su2 *h, int enable) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        cuda_check(cudaStreamSynchronize(h->stream), "stream sync");
+        for (auto e : h->ev_pool) cudaEventDestroy(e);
+        h->ev_pool.clear();
+        h->ev_vertex.clear();
+        h->ev_step.clear();
+        h->profiling = enable != 0;
+    });
+}
+
+extern "C" int spn_su2_get_profile(spn_su2 *h, double *vertex_ms, int *vertex_launches, double *step_ms, int *steps) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        cuda_check(cudaStreamSynchronize(h->stream), "stream sync");
+        double vm = 0.0, sm = 0.0;
+        for (auto &p : h->ev_vertex) {
+            float ms = 0.0f;
+            cuda_check(cudaEventElapsedTime(&ms, h->ev_pool[p.first], h->ev_pool[p.second]), "elapsed");
+            vm += ms;
+        }
+        for (auto &p : h->ev_step) {
+            float ms = 0.0f;
+            cuda_check(cudaEventElapsedTime(&ms, h->ev_pool[p.first], h->ev_pool[p.second]), "elapsed");
+            sm += ms;
+        }
+        if (vertex_ms) *vertex_ms = vm;
+        if (vertex_launches) *vertex_launches = int(h->ev_vertex.size());
+        if (step_ms) *step_ms = sm;
+        if (steps) *steps = int(h->ev_step.size());
+    });
+}

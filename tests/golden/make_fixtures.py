@@ -1,0 +1,115 @@
+"""Regenerates the golden fixtures under tests/golden/ from the SpinParser reference tree.
+
+Run in a checkout where the reference sources are available:
+    python tests/golden/make_fixtures.py /path/to/SpinParser
+
+Outputs (committed, so the tests need no reference tree at run time):
+  reference1_su2.npz      golden SU(2) correlations of test/scripted/test_reference1.sh
+                          (hyperkagome r=3, 14 manual frequencies, cutoff 10 -> 0.3 x0.9),
+                          read from test/scripted/assets/test_reference1.ref, plus the task's
+                          frequency list and cutoff specification parsed from the script
+  hyperkagome_r3_tables.npz  lattice tables of that task, built by this package's lattice
+                          factory from the reference's res/ unit cell and model
+  python_obs_honeycomb.json  the numeric expectations of test/scripted/assets/test_python_obs.py
+                          (honeycomb r=3 SU(2) run of test_pythonObs.sh) and the task parameters
+"""
+from __future__ import annotations
+
+import json
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+import h5lite  # noqa: E402
+
+
+def task_parameters(script: str) -> dict:
+    freq = [float(x) for x in re.findall(r"<value>([0-9.]+)</value>", script)]
+    cmax = float(re.search(r"<max>([0-9.]+)</max>", script).group(1))
+    cmin = float(re.search(r"<min>([0-9.]+)</min>", script).group(1))
+    step = float(re.search(r"<step>([0-9.]+)</step>", script).group(1))
+    lat = re.search(r'<lattice name="([^"]+)" range="(\d+)"', script)
+    model = re.search(r'<model name="([^"]+)"', script)
+    j = float(re.search(r"<j>([-0-9.]+)</j>", script).group(1))
+    return {"frequencies": sorted(freq), "cutoff_max": cmax, "cutoff_min": cmin, "cutoff_step": step,
+            "lattice": lat.group(1), "range": int(lat.group(2)), "model": model.group(1), "j": j}
+
+
+def lattice_kats(src: str) -> dict:
+    """Site lists and counts of test/test_Lattice.cpp, per test case."""
+    out = {}
+    cases = re.split(r"BOOST_FIXTURE_TEST_CASE\(", src)[1:]
+    for case in cases:
+        name = case.split(",")[0].strip()
+        lists = {}
+        for lname, body in re.findall(r"std::vector<SiteParameters> (\w+) = \{(.*?)\};", case, re.S):
+            lists[lname] = [[int(x) for x in t.split(",")] for t in re.findall(r"SiteParameters\(([-0-9, ]+)\)", body)]
+        entry = {"lists": lists}
+        m = re.search(r"getOverlap\(l->symmetryTransform\(l->zero\(\), fromParameters\(SiteParameters\(([-0-9, ]+)\)\)\)\)", case)
+        if m:
+            entry["overlap_site"] = [int(x) for x in m.group(1).split(",")]
+            entry["overlap_size"] = int(re.search(r"BOOST_CHECK_EQUAL\(o\.size, (\d+)\)", case).group(1))
+        m = re.search(r"BOOST_CHECK_EQUAL\(n, (\d+)\);\s*BOOST_CHECK_EQUAL\(l->size, (\d+)\)", case)
+        if m:
+            entry["n_in_range"], entry["size"] = int(m.group(1)), int(m.group(2))
+        out[name] = entry
+    return out
+
+
+def main(ref_root: str) -> None:
+    import spinparser_gb300 as spn
+
+    # --- test_Lattice.cpp: lattice known-answer tests ---
+    kats = lattice_kats(open(os.path.join(ref_root, "test", "test_Lattice.cpp")).read())
+    with open(os.path.join(HERE, "lattice_kats.json"), "w") as f:
+        json.dump(kats, f)
+
+    scripted = os.path.join(ref_root, "test", "scripted")
+    # --- test_reference1: hyperkagome golden ---
+    p1 = task_parameters(open(os.path.join(scripted, "test_reference1.sh")).read())
+    ref = os.path.join(scripted, "assets", "test_reference1.ref")
+    cut, zz = h5lite.read_correlations(ref, "SU2CorZZ")
+    cut_dd, dd = h5lite.read_correlations(ref, "SU2CorDD")
+    assert np.array_equal(cut, cut_dd)
+    meta = h5lite.open_file(ref)["SU2CorZZ/meta"]
+    np.savez_compressed(os.path.join(HERE, "reference1_su2.npz"), cutoffs=cut, zz=zz, dd=dd,
+                        frequencies=np.array(p1["frequencies"], np.float32),
+                        cutoff_spec=np.array([p1["cutoff_max"], p1["cutoff_min"], p1["cutoff_step"]], np.float32),
+                        j=np.float32(p1["j"]), sites=meta["sites"].read(), basis=meta["basis"].read(),
+                        lattice_vectors=meta["latticeVectors"].read())
+    lat = spn.Lattice(p1["lattice"], p1["range"], p1["model"], {"j": str(p1["j"])},
+                      resource_dir=os.path.join(ref_root, "res"))
+    lat.tables().to_npz(os.path.join(HERE, "hyperkagome_r3_tables.npz"))
+
+    # --- test_pythonObs: honeycomb expectations ---
+    p2 = task_parameters(open(os.path.join(scripted, "test_pythonObs.sh")).read())
+    src = open(os.path.join(scripted, "assets", "test_python_obs.py")).read()
+    refs = [json.loads(m) for m in re.findall(r"reference = (\[.*\])", src)]
+    queries = [
+        {"what": "basis", "expect": refs[0]},
+        {"what": "primitives", "expect": refs[1]},
+        {"what": "sites", "reference": [0.0, 0.0, 0.0], "expect": refs[2]},
+        {"what": "sites", "reference": [1.0, 0.0, 0.0], "expect": refs[3]},
+        {"what": "correlation", "cutoff": "all", "site": [1.0, 0.0, 0.0], "reference": [0.0, 0.0, 0.0],
+         "component": "all", "expect": refs[4]},
+        {"what": "correlation", "cutoff": "all", "site": [1.0, 0.0, 0.0], "reference": [0.0, 0.0, 0.0],
+         "component": "XX", "expect": refs[5]},
+        {"what": "correlation", "cutoff": [0.309031], "site": "all", "reference": [0.0, 0.0, 0.0],
+         "component": "ZZ", "expect": refs[6]},
+        {"what": "correlation", "cutoff": [0.381520, 2.058910], "site": [[0.0, 0.0, 0.0], [2.5, 0.866025, 0.0]],
+         "reference": [1.0, 0.0, 0.0], "component": "ZZ", "expect": refs[7]},
+        {"what": "structure_factor", "momentum": [[0.0, 0.0, 0.0], [4.188790, 0.0, 0.0]], "cutoff": [0.381520],
+         "expect": refs[8]},
+    ]
+    with open(os.path.join(HERE, "python_obs_honeycomb.json"), "w") as f:
+        json.dump({"task": p2, "queries": queries}, f, indent=1)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
