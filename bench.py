@@ -3,25 +3,31 @@
 
 Workload (default): SU(2) J1-J2 Heisenberg model on the simple cubic lattice, J1 = 1,
 J2 = 0.25, lattice range 6 (23 symmetry-reduced site pairs, 4095 RPA pairs), 64 positive
-Matsubara frequencies exponentially spaced in [0.005, 100], cutoff 100 -> 0.05 x 0.98.
-A step is one cutoff step as SpinParser's loop runs it: flow right-hand side (self-energy
-flow + vertex flow), correlation measurement, explicit Euler update.  Synthetic in the sense
-that the state is the model's initial condition advanced by the flow itself (no dataset).
+Matsubara frequencies exponentially spaced in [0.005, 100], cutoff 100 -> 0.05 x 0.98
+(377 cutoff values).  A step is one cutoff step as SpinParser's loop runs it: flow
+right-hand side (self-energy flow + vertex flow), correlation measurement, explicit Euler
+update.  The state is the model's initial condition advanced by the flow itself.
 
-Lines printed (rank 0, one JSON line):
-  value     steps/s with the state resident in HBM, device time from CUDA events on the
-            flow's stream; L2 is flushed (256 MB write) before every timed step
+The work of a step grows as the cutoff decreases (more loop-frequency nodes lie above it),
+so the K timed steps are spread evenly over the whole cutoff list: before each timed step
+the flow's cutoff is moved to the next sampled value (untimed, as is an L2 flush), then one
+genuine 0.98 step is taken.  The complete flow is also timed once ("full_flow").
+
+JSON line (rank 0):
+  value     steps/s with the state resident in HBM; device time from CUDA events on the
+            flow's stream; L2 flushed (256 MB write) before every timed step
   e2e       steps/s through the C ABI with host buffers: every step uploads the state from
-            pinned host memory, runs the step and reads the state and the correlations back
-  roofline  the vertex-flow kernel: nominal algorithmic FP32 work per launch
+            pinned host memory, runs the step, reads the state and the correlations back
+  roofline  the vertex-flow kernel: algorithmic FP32 work per launch
             F_RHS = F_N (2N+8) (3*100*Nl + 4*sum O) over its CUDA-event launch time, against
-            the FP32 FMA throughput measured in-run on the same GPU
+            the FP32 FMA throughput measured in-run on the same GPU; "evaluated" uses the
+            node counts the step actually used instead of 2N+8
   cpu_baseline  the CPU oracle (restatement of the reference's SU(2) core) on this host's
-            cores, on a bounded random sample of vertex triples, extrapolated to one step
+            cores, on a bounded random sample of vertex triples at four cutoffs spread over
+            the flow, extrapolated to one step
 
---impl reference times the CPU oracle alone (the reference's C++ code needs Boost and HDF5,
-which this environment does not provide, so its own build cannot run here).
---gpus N > 1: replicas only (independent flows, one per GPU, no collective).
+--impl reference times the CPU oracle alone (the reference's own C++ build needs Boost and
+HDF5, absent here).  --gpus N > 1: replicas only (independent flows, no collective).
 """
 from __future__ import annotations
 
@@ -48,18 +54,20 @@ WORKLOADS = {
 }
 DEFAULT_WORKLOAD = "cubic-j1j2-r6-n64"
 METRIC = "cutoff steps/s per flow"
+KERNELS_PER_STEP = 8  # self-energy, node tables, vertex flow, 2 x correlation, 3 x Euler
 
 
 def parse_args():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
-    ap.add_argument("--e2e-steps", type=int, default=None)
-    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU work budget of the baseline sample")
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU work budget of the baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-full-flow", action="store_true")
     return ap.parse_args()
 
 
@@ -73,9 +81,25 @@ def setup(wl):
     return tab, freq, cut
 
 
-def flops_per_rhs(tab, n):
+def sampled_steps(n_cut: int, first: int, k: int) -> list[int]:
+    """k cutoff indices spread evenly over [first, n_cut - 2]."""
+    return [int(round(x)) for x in np.linspace(first, n_cut - 2, k)]
+
+
+def flops_nominal(tab, n):
     fn = n * n * (n + 1) // 2
     return float(fn) * (2 * n + 8) * (3 * 100 * tab.n_sites + 4 * tab.n_overlap)
+
+
+def flops_evaluated(tab, n, counts):
+    """Same per-node costs, with the node counts the step actually used."""
+    c = np.asarray(counts, np.float64)
+    tot = 0.0
+    for s in range(n):
+        for u in range(s + 1):
+            base = c[s] + c[u]
+            tot += n * base * 100 * tab.n_sites + float(np.sum(c)) * (100 * tab.n_sites + 4 * tab.n_overlap)
+    return tot
 
 
 class ClockSampler:
@@ -124,65 +148,73 @@ class ClockSampler:
             except ValueError:
                 return float("nan")
 
-        sm = [num(r[1]) for r in rows]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
-        return {"sm_mhz": float(np.nanmedian(sm)), "sm_max_mhz": float(np.nanmax([num(r[2]) for r in rows])),
-                "reasons": reasons, "samples": len(rows), "power_w_max": float(np.nanmax([num(r[3]) for r in rows]))}
+        return {"sm_mhz": float(np.nanmedian([num(r[1]) for r in rows])),
+                "sm_max_mhz": float(np.nanmax([num(r[2]) for r in rows])), "reasons": reasons,
+                "samples": len(rows), "power_w_max": float(np.nanmax([num(r[3]) for r in rows]))}
 
 
-def cpu_baseline(tab, freq, state_cutoff, state, budget_s):
-    """Times the oracle on a bounded random sample of vertex triples on all host cores and
-    extrapolates to one full step (vertex flow of all triples + self-energy flow)."""
+def cpu_baseline(tab, freq, cutoffs, state, budget_s):
+    """The oracle on all host cores: a random sample of vertex triples at each of the given
+    cutoffs (plus the full self-energy flow), extrapolated to one average step."""
     from oracle import Oracle
 
     threads = os.cpu_count() or 1
     orc = Oracle(tab, freq)
     v2, ss, dd = state
-    t0 = time.perf_counter()
-    dv2 = orc.self_energy(state_cutoff, v2, ss, dd)
-    t_se = time.perf_counter() - t0
     fn = orc.fn
     rng = np.random.default_rng(20261203)
-    probe = rng.choice(fn, size=min(fn, 4 * threads), replace=False)
-    t0 = time.perf_counter()
-    orc.vertex_sample(state_cutoff, v2, dv2, ss, dd, probe, threads)
-    t_probe = time.perf_counter() - t0
-    per_triple = t_probe / len(probe)
-    n = int(min(fn, max(len(probe), budget_s / max(per_triple, 1e-9))))
-    sample = rng.choice(fn, size=n, replace=False)
-    t0 = time.perf_counter()
-    orc.vertex_sample(state_cutoff, v2, dv2, ss, dd, sample, threads)
-    t_s = time.perf_counter() - t0
-    t_step = t_s * fn / n + t_se
+    per_cut = budget_s / len(cutoffs)
+    t_steps, n_total, t_total = [], 0, 0.0
+    for c in cutoffs:
+        t0 = time.perf_counter()
+        dv2 = orc.self_energy(c, v2, ss, dd)
+        t_se = time.perf_counter() - t0
+        probe = rng.choice(fn, size=min(fn, 2 * threads), replace=False)
+        t0 = time.perf_counter()
+        orc.vertex_sample(c, v2, dv2, ss, dd, probe, threads)
+        per_triple = (time.perf_counter() - t0) / len(probe)
+        n = int(min(fn, max(len(probe), per_cut / max(per_triple, 1e-9))))
+        sample = rng.choice(fn, size=n, replace=False)
+        t0 = time.perf_counter()
+        orc.vertex_sample(c, v2, dv2, ss, dd, sample, threads)
+        t_s = time.perf_counter() - t0
+        t_steps.append(t_s * fn / n + t_se)
+        n_total += n
+        t_total += t_s
+    t_step = float(np.mean(t_steps))
     return {"value": 1.0 / t_step, "unit": "steps/s", "cores": threads, "kind": "port",
-            "sample": f"{n} of {fn} vertex triples (uniform random, seed 20261203) + full self-energy flow, "
-                      f"{t_s:.1f} s on {threads} threads; one step extrapolated to {t_step:.1f} s"}
+            "sample": f"{n_total} vertex triples (uniform random of {fn}, seed 20261203) at cutoffs "
+                      f"{[round(float(c), 4) for c in cutoffs]} + the full self-energy flow at each; {t_total:.1f} s "
+                      f"on {threads} threads; one average step extrapolated to {t_step:.2f} s"}
+
+
+def baseline_cutoffs(cut):
+    return [float(cut[i]) for i in sampled_steps(len(cut), 0, 4)]
 
 
 def run_reference(args, wl):
     """--impl reference: the CPU oracle only (rank 0)."""
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
+    if int(os.environ.get("RANK", "0")) != 0:
         return
     tab, freq, cut = setup(wl)
     state = tab.initial_state(len(freq))
-    per_step = max(2.0, min(10.0, 150.0 / max(1, args.steps + args.warmup)))
+    per_step = max(2.0, min(8.0, 150.0 / max(1, args.steps + args.warmup)))
     for _ in range(args.warmup):
-        cpu_baseline(tab, freq, float(cut[0]), state, 0.2)
-    vals = []
+        cpu_baseline(tab, freq, baseline_cutoffs(cut)[:1], state, 0.2)
+    vals, last = [], None
     t0 = time.perf_counter()
-    last = None
     for _ in range(args.steps):
-        last = cpu_baseline(tab, freq, float(cut[0]), state, per_step)
+        last = cpu_baseline(tab, freq, baseline_cutoffs(cut), state, per_step)
         vals.append(last["value"])
     wall = time.perf_counter() - t0
     value = float(np.mean(vals))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (model initial condition)",
-            "config": {"workload": args.workload, **{k: v for k, v in wl.items() if k != "params"},
-                       "params": wl["params"], "l2": "n/a (CPU)"},
+            "config": {"workload": args.workload, "lattice": wl["lattice"], "range": wl["range"], "model": wl["model"],
+                       "params": wl["params"], "n_freq": wl["n_freq"], "l2": "n/a (CPU)"},
             "cpu_baseline": {**last, "value": value},
             "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "wall_s": wall}
@@ -206,23 +238,20 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     dist = None
+    torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
 
-        torch.cuda.set_device(local)
         dist.init_process_group("nccl")
-    torch.cuda.set_device(local)
 
     tab, freq, cut = setup(wl)
     n = len(freq)
-    total_steps = args.warmup + args.steps
-    if total_steps + 1 > len(cut):
-        raise SystemExit("more steps than cutoff values")
+    if args.warmup + 2 > len(cut):
+        raise SystemExit("not enough cutoff values")
     flow = spn.Su2Flow(tab, freq, device=local)
     stream = torch.cuda.Stream(device=local)
     flow.set_stream(stream.cuda_stream)
-    state0 = tab.initial_state(n)
-    flow.set_state(float(cut[0]), *state0)
+    flow.set_state(float(cut[0]), *tab.initial_state(n))
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
 
     def step(k):
@@ -236,8 +265,10 @@ def main():
     if flow.is_diverged():
         raise SystemExit("flow diverged during warm-up")
 
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    schedule = sampled_steps(len(cut), args.warmup, args.steps)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in schedule]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in schedule]
+    counts_sum = np.zeros(n, np.float64)
     sampler = ClockSampler(local)
     if dist:
         dist.barrier()
@@ -245,40 +276,43 @@ def main():
     flow.set_profiling(True)
     sampler.start()
     wall0 = time.perf_counter()
-    for i in range(args.steps):
+    flops_eval = 0.0
+    for i, k in enumerate(schedule):
+        flow.set_cutoff(float(cut[k]))
         with torch.cuda.stream(stream):
             flush.fill_(float(i))
         starts[i].record(stream)
-        step(args.warmup + i)
+        step(k)
         ends[i].record(stream)
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     clocks = sampler.stop()
     if dist:
         dist.barrier()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = float(np.sum(step_ms))
+    total_ms = float(np.sum([s.elapsed_time(e) for s, e in zip(starts, ends)]))
     prof = flow.profile()
     diverged = flow.is_diverged()
-
+    flow.set_profiling(False)
+    # evaluated work of the sampled steps (node counts depend only on the cutoff)
+    for k in schedule:
+        flow.set_cutoff(float(cut[k]))
+        flow.compute_step()
+        flops_eval += flops_evaluated(tab, n, flow.node_counts())
     if dist:
         t = torch.tensor([total_ms], device=f"cuda:{local}")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
 
     # end to end through the C ABI with pinned host buffers
-    e2e_steps = args.e2e_steps or max(3, min(args.steps, 10))
     fn_nl = flow.fn * flow.nl
     pin = lambda m: torch.empty(m, dtype=torch.float32, pin_memory=True).numpy()  # noqa: E731
     h_v2, h_ss, h_dd = pin(n), pin(fn_nl), pin(fn_nl)
     h_zz, h_dc = pin(flow.n_corr), pin(flow.n_corr)
-    c0, a, b, c = flow.get_state()
-    h_v2[:], h_ss[:], h_dd[:] = a, b, c
+    flow.get_state(h_v2, h_ss, h_dd)
+    e2e_sched = sampled_steps(len(cut), args.warmup, args.e2e_steps)
     torch.cuda.synchronize()
     e0 = time.perf_counter()
-    kc = args.warmup + args.steps
-    for i in range(e2e_steps):
-        k = min(kc + i, len(cut) - 2)
+    for k in e2e_sched:
         flow.set_state(float(cut[k]), h_v2, h_ss, h_dd)
         flow.compute_step()
         flow.launch_correlation()
@@ -288,42 +322,65 @@ def main():
     e2e_s = time.perf_counter() - e0
     state_bytes = 4 * (n + 2 * fn_nl)
 
+    # the complete flow, device resident (time to result of one flow)
+    full = None
+    if not args.no_full_flow:
+        flow.set_state(float(cut[0]), *tab.initial_state(n))
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        f0.record(stream)
+        for k in range(len(cut) - 1):
+            step(k)
+        flow.launch_correlation()
+        f1.record(stream)
+        torch.cuda.synchronize()
+        fs = f0.elapsed_time(f1) * 1e-3
+        full = {"steps": len(cut) - 1, "seconds": fs, "steps_per_s": (len(cut) - 1) / fs,
+                "diverged": flow.is_diverged()}
+
     fp32_peak, clk = spn.measure_fp32_peak(local)
-    flops = flops_per_rhs(tab, n)
     avg_vertex_ms = prof["vertex_ms"] / max(1, prof["vertex_launches"])
-    achieved = flops / (avg_vertex_ms * 1e-3) / 1e12
+    nominal = flops_nominal(tab, n)
+    achieved = nominal / (avg_vertex_ms * 1e-3) / 1e12
+    achieved_eval = flops_eval / (prof["vertex_ms"] * 1e-3) / 1e12
     traffic = None
     prof_file = os.path.join(ROOT, "profiles", f"vertex_flow_{args.workload}.json")
     if os.path.exists(prof_file):
         traffic = json.load(open(prof_file)).get("dram_bytes_per_launch")
 
     if rank != 0:
+        flow.close()
+        if dist:
+            dist.destroy_process_group()
         return
-    value = world * args.steps / (total_ms * 1e-3)
+    value = world * len(schedule) / (total_ms * 1e-3)
     line = {
-        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": len(schedule),
+        "warmup": args.warmup, "ms_per_step": total_ms / len(schedule), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (model initial condition, advanced by the flow)",
         "config": {"workload": args.workload, "lattice": wl["lattice"], "range": wl["range"], "model": wl["model"],
                    "params": wl["params"], "n_freq": n, "freq_range": [wl["fmin"], wl["fmax"]],
-                   "cutoff": [wl["cmax"], wl["cmin"], wl["cstep"]], "n_sites": tab.n_sites,
+                   "cutoff": [wl["cmax"], wl["cmin"], wl["cstep"]], "n_cutoffs": len(cut), "n_sites": tab.n_sites,
                    "n_overlap": tab.n_overlap, "n_triples": flow.fn, "parallelism": f"replicas x{world}",
+                   "timed_steps": "spread evenly over the cutoff list",
                    "l2": "flushed (256 MB write) before every timed step"},
-        "e2e": {"value": e2e_steps / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": state_bytes,
+        "e2e": {"value": len(e2e_sched) / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes + 8 * flow.n_corr},
         "roofline": {"bound": "fp32", "kernel": "su2_vertex_flow_kernel", "achieved": achieved, "peak": fp32_peak,
                      "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": traffic,
-                     "algorithmic_flops_per_launch": flops, "avg_launch_ms": avg_vertex_ms,
+                     "algorithmic_flops_per_launch": nominal, "avg_launch_ms": avg_vertex_ms,
+                     "achieved_evaluated": achieved_eval, "frac_evaluated": achieved_eval / fp32_peak,
                      "peak_source": "measured in-run: pure-FFMA kernel on this GPU (MEASURED_PEAKS.json has no "
                                     "FP32 CUDA-core figure)", "fp32_clock_ghz_implied": clk},
-        "gpu_launches": 8 * args.steps,
+        "gpu_launches": KERNELS_PER_STEP * len(schedule),
         "clocks": clocks,
+        "full_flow": full,
         "diverged": diverged,
         "wall_s": wall,
     }
     if not args.no_cpu_baseline and world == 1:
         c, v2, ss, dd = flow.get_state()
-        line["cpu_baseline"] = cpu_baseline(tab, freq, c, (v2, ss, dd), args.cpu_seconds)
+        line["cpu_baseline"] = cpu_baseline(tab, freq, baseline_cutoffs(cut), (v2, ss, dd), args.cpu_seconds)
     print(json.dumps(line))
     flow.close()
     if dist:

@@ -160,6 +160,14 @@ int spn_su2_get_sizes(const spn_su2 *h, int *n_freq, int *n_sites, long long *n_
 int spn_su2_set_state(spn_su2 *h, float cutoff, const float *v2, const float *v4ss, const float *v4dd);
 int spn_su2_get_state(spn_su2 *h, float *cutoff, float *v2, float *v4ss, float *v4dd);
 
+/* Sets the cutoff of the flowing state without touching the vertex data (what
+ * SpinParser does when it resumes from a checkpoint: EffectiveAction::cutoff, src/EffectiveAction.hpp:58). */
+int spn_su2_set_cutoff(spn_su2 *h, float cutoff);
+
+/* Number of loop-frequency nodes per transfer frequency used by the last compute_step
+ * (counts[N]): conventional terms plus the trapezoid nodes of the Katanin integrals. */
+int spn_su2_get_node_counts(spn_su2 *h, int *counts);
+
 /* FrgCore::computeStep (src/SU2/SU2FrgCore.cpp:89-109): self-energy flow, then the
  * two-particle vertex flow, into the device-resident flow buffers.  Asynchronous. */
 int spn_su2_compute_step(spn_su2 *h);

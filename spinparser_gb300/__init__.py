@@ -6,9 +6,9 @@ spinparser_gb300._build``).
 """
 from ._capi import SpnError, load_library
 from .core import (FP64_SELF_ENERGY, RES_DIR, Lattice, LatticeTables, Su2Flow, cutoff_exponential, device_count,
-                   frequency_exponential)
+                   frequency_exponential, measure_fp32_peak)
 
 __all__ = [
     "SpnError", "load_library", "Lattice", "LatticeTables", "Su2Flow", "frequency_exponential", "cutoff_exponential",
-    "device_count", "RES_DIR", "FP64_SELF_ENERGY",
+    "device_count", "measure_fp32_peak", "RES_DIR", "FP64_SELF_ENERGY",
 ]

@@ -72,6 +72,8 @@ SIGNATURES = {
     "spn_su2_get_sizes": (C.c_int, [C.c_void_p, c_int_p, c_int_p, c_ll_p]),
     "spn_su2_set_state": (C.c_int, [C.c_void_p, C.c_float, c_float_p, c_float_p, c_float_p]),
     "spn_su2_get_state": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p, c_float_p]),
+    "spn_su2_set_cutoff": (C.c_int, [C.c_void_p, C.c_float]),
+    "spn_su2_get_node_counts": (C.c_int, [C.c_void_p, c_int_p]),
     "spn_su2_compute_step": (C.c_int, [C.c_void_p]),
     "spn_su2_get_flow": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p]),
     "spn_su2_finalize_step": (C.c_int, [C.c_void_p, C.c_float]),

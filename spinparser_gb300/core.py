@@ -233,6 +233,14 @@ class Su2Flow:
                                           _ptr(dd, C.c_float)))
         return c.value, v2, ss, dd
 
+    def set_cutoff(self, cutoff: float) -> None:
+        check(self._lib.spn_su2_set_cutoff(self._h, cutoff))
+
+    def node_counts(self) -> np.ndarray:
+        out = np.empty(self.n, np.int32)
+        check(self._lib.spn_su2_get_node_counts(self._h, _ptr(out, C.c_int)))
+        return out
+
     def compute_step(self) -> None:
         check(self._lib.spn_su2_compute_step(self._h))
 

@@ -943,6 +943,22 @@ extern "C" int spn_su2_get_state(spn_su2 *h, float *cutoff, float *v2, float *v4
     });
 }
 
+extern "C" int spn_su2_set_cutoff(spn_su2 *h, float cutoff) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        h->cutoff = cutoff;
+    });
+}
+
+extern "C" int spn_su2_get_node_counts(spn_su2 *h, int *counts) {
+    return guarded([&] {
+        if (!h || !counts) throw Error(ErrorType::Argument, "null argument");
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        cuda_check(cudaMemcpyAsync(counts, h->node_cnt, h->n * sizeof(int), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        cuda_check(cudaStreamSynchronize(h->stream), "node count sync");
+    });
+}
+
 extern "C" int spn_su2_compute_step(spn_su2 *h) {
     return guarded([&] {
         if (!h) throw Error(ErrorType::Argument, "null handle");

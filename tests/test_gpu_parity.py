@@ -192,7 +192,12 @@ def test_honeycomb_flow_matches_python_obs_expectations():
 
     for q in spec["queries"]:
         got = evaluate_query(q, measured, zz, tab)
-        assert np.isclose(got, np.array(q["expect"]), rtol=1e-5, atol=1e-16).all(), q["what"]
+        atol = 1e-16
+        if q["what"] == "structure_factor":
+            # a sum over sites with strong cancellation at k = 0: the error budget of a sum is
+            # rtol times the sum of the magnitudes of its terms, not times its (small) result
+            atol = 1e-5 * float(np.max(evaluate_query(q, measured, np.abs(zz), tab)))
+        assert np.isclose(got, np.array(q["expect"]), rtol=1e-5, atol=atol).all(), q["what"]
 
 
 def test_repeated_step_is_bit_identical(square_r3):
@@ -210,12 +215,13 @@ def test_repeated_step_is_bit_identical(square_r3):
 
 
 def test_nan_state_reports_divergence(square_r3):
-    """isDiverged: a NaN injected on the host into the state propagates into the flow."""
+    """isDiverged: a NaN injected on the host into the state propagates into the flow.
+    (The local site column is read by every channel; a single entry may never be read.)"""
     tab = square_r3
     freq = spn.frequency_exponential(0.05, 50.0, 8)
     v2, ss, dd = tab.initial_state(8)
     ss = ss.copy()
-    ss[5] = np.nan
+    ss[::tab.n_sites] = np.nan
     flow = spn.Su2Flow(tab, freq)
     flow.set_state(2.0, v2, ss, dd)
     flow.compute_step()
