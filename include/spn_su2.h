@@ -189,6 +189,25 @@ int spn_su2_measure_correlation(spn_su2 *h, float *zz, float *dd, float *chi_zz,
 int spn_su2_launch_correlation(spn_su2 *h);
 int spn_su2_get_correlation(spn_su2 *h, float *zz, float *dd, float *chi_zz, float *chi_dd);
 
+/* Correlation measurement that allocates no device memory.  No counterpart in the reference:
+ * it exists for callers that cannot allocate device memory when they measure, such as a host
+ * framework that reserves the GPU's memory up front in its own pool (a cudaMalloc here would
+ * fail or bypass its accounting) or a time-critical loop that must not enter the CUDA allocator.
+ * Every pointer is DEVICE memory owned by the caller: freq[n_freq], sites_rid and
+ * inv_sites_rid[n_sites], corr_rid[n_corr], the state v2[n_freq], v4ss and v4dd[F_N*n_sites],
+ * and out[2*n_corr + 2*n_sites] which receives zz, dd, chi_zz and chi_dd as in
+ * spn_su2_measure_correlation.  The kernels' scratch is a fixed array inside the library
+ * (1 064 960 bytes per GPU, held until the process exits), which limits n_freq <= 256 and
+ * n_sites <= 128; larger sizes are rejected with SPN_E_UNSUPPORTED.  The first call on a device
+ * looks up that array's device address (with the device current) and should come before any
+ * stream capture.  Work is queued on `stream` (a cudaStream_t, NULL = default stream) and
+ * the call returns without waiting.  All calls on one device share the array: calls whose
+ * work overlaps on the GPU race and must be ordered by the caller. */
+int spn_su2_correlation_noalloc(int n_freq, const float *freq, int n_sites, const int *sites_rid,
+                                const int *inv_sites_rid, int n_corr, const int *corr_rid, float spin_length,
+                                float cutoff, const float *v2, const float *v4ss, const float *v4dd, float *out,
+                                void *stream);
+
 /* EffectiveAction::isDiverged on the last computed flow (any NaN).  Synchronises. */
 int spn_su2_is_diverged(spn_su2 *h, int *diverged);
 

@@ -80,6 +80,9 @@ SIGNATURES = {
     "spn_su2_measure_correlation": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p, c_float_p]),
     "spn_su2_launch_correlation": (C.c_int, [C.c_void_p]),
     "spn_su2_get_correlation": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p, c_float_p]),
+    "spn_su2_correlation_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                              C.c_void_p, C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p,
+                                              C.c_void_p, C.c_void_p]),
     "spn_su2_is_diverged": (C.c_int, [C.c_void_p, c_int_p]),
     "spn_su2_synchronize": (C.c_int, [C.c_void_p]),
     "spn_su2_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),

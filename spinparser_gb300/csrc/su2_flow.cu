@@ -1139,3 +1139,88 @@ extern "C" int spn_su2_get_profile(spn_su2 *h, double *vertex_ms, int *vertex_la
         if (steps) *steps = int(h->ev_step.size());
     });
 }
+
+// ------------------------------------------------------------------------------------
+// Allocation-free correlation measurement
+//
+// Some callers cannot allocate device memory when they want a measurement: a host framework
+// that reserves the GPU's memory up front in its own pool (a cudaMalloc from this library
+// would fail or bypass the pool's accounting), or a time-critical loop that must not enter the
+// CUDA allocator (cudaMalloc/cudaFree can synchronise the device and take driver locks).  For
+// them spn_su2_correlation_noalloc runs the same two measurement kernels as
+// spn_su2_measure_correlation, with the per-node partial sums in the fixed array below instead
+// of memory owned by a flow handle.  The caller passes every input and the output in device
+// memory it already owns; this entry point allocates nothing.
+//
+// The array holds (2 * kMaxFreq + 8) x 2 x kMaxSites doubles (1 064 960 bytes) and is
+// resident on every GPU that loads the library until the process exits.  It is shared by all
+// calls on a device and keeps the contents of the last call; no entry needs clearing, because
+// the first kernel writes every partial sum the second kernel reads.  Two calls whose work
+// overlaps on the GPU (different streams, no ordering between them) race on it.
+// ------------------------------------------------------------------------------------
+namespace {
+
+constexpr int kNoAllocMaxDevices = 64;
+static __device__ __align__(256) double g_corr_scratch[size_t(kMaxCorrNodes) * 2 * kMaxSites];
+
+// Device address of g_corr_scratch per device.  In host code the array's name is only a
+// host-side stand-in, so the address is looked up once per device with that device current.
+double *g_corr_scratch_addr[kNoAllocMaxDevices] = {};
+
+double *corr_scratch_for_current_device() {
+    int dev = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= kNoAllocMaxDevices) throw Error(ErrorType::Unsupported, "device ordinal beyond 63");
+    double *p = __atomic_load_n(&g_corr_scratch_addr[dev], __ATOMIC_ACQUIRE);
+    if (!p) {
+        void *addr = nullptr;
+        cuda_check(cudaGetSymbolAddress(&addr, g_corr_scratch), "cudaGetSymbolAddress(g_corr_scratch)");
+        p = static_cast<double *>(addr);
+        __atomic_store_n(&g_corr_scratch_addr[dev], p, __ATOMIC_RELEASE);
+    }
+    return p;
+}
+
+}  // namespace
+
+extern "C" int spn_su2_correlation_noalloc(int n_freq, const float *freq, int n_sites, const int *sites_rid,
+                                           const int *inv_sites_rid, int n_corr, const int *corr_rid, float spin_length,
+                                           float cutoff, const float *v2, const float *v4ss, const float *v4dd, float *out,
+                                           void *stream) {
+    return guarded([&] {
+        if (n_freq < 2 || n_freq > kMaxFreq)
+            throw Error(ErrorType::Unsupported, "spn_su2_correlation_noalloc: n_freq must be in [2, " +
+                                                    std::to_string(kMaxFreq) + "] (fixed scratch size)");
+        if (n_sites < 1 || n_sites > kMaxSites)
+            throw Error(ErrorType::Unsupported, "spn_su2_correlation_noalloc: n_sites must be in [1, " +
+                                                    std::to_string(kMaxSites) + "] (fixed scratch size)");
+        if (n_corr < 0) throw Error(ErrorType::Argument, "spn_su2_correlation_noalloc: n_corr must be >= 0");
+        if (!freq || !sites_rid || !inv_sites_rid || (n_corr > 0 && !corr_rid) || !v2 || !v4ss || !v4dd || !out)
+            throw Error(ErrorType::Argument, "spn_su2_correlation_noalloc: null device pointer");
+        CorrArgs a;
+        a.n = n_freq;
+        a.nl = n_sites;
+        a.n_corr = n_corr;
+        a.cutoff = cutoff;
+        a.spin = spin_length;
+        a.freq = freq;
+        a.ss = v4ss;
+        a.dd = v4dd;
+        a.v2 = v2;
+        a.sites = sites_rid;
+        a.inv_sites = inv_sites_rid;
+        a.corr_rid = corr_rid;
+        a.partial = corr_scratch_for_current_device();
+        a.out = out;
+        a.wsite = wsite_for(n_sites);
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        const int spt = spt_for(n_sites);
+        const int blocks = 2 * n_freq + 4;
+        if (spt == 1) su2_corr_inner_kernel<1><<<blocks, 128, 0, s>>>(a);
+        else if (spt == 2) su2_corr_inner_kernel<2><<<blocks, 128, 0, s>>>(a);
+        else su2_corr_inner_kernel<4><<<blocks, 128, 0, s>>>(a);
+        cuda_check(cudaGetLastError(), "correlation launch");
+        su2_corr_final_kernel<<<1, 128, 2 * n_sites * sizeof(double), s>>>(a);
+        cuda_check(cudaGetLastError(), "correlation final launch");
+    });
+}
