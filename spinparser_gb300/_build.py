@@ -19,7 +19,7 @@ CSRC = os.path.join(PKG, "csrc")
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 
 HOST_SOURCES = ["host/xml.cpp", "host/lattice.cpp", "host/capi_host.cpp"]
-CUDA_SOURCES = ["su2_flow.cu"]
+CUDA_SOURCES = ["su2_flow.cu", "su2_vertex.cu"]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

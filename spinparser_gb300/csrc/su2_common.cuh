@@ -1,0 +1,48 @@
+// Types shared by the SU(2) flow translation units: the per-flow kernel argument block and
+// the launch interface of the vertex-flow kernel.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace spn {
+
+constexpr unsigned kStatusNaN = 1u;           // a NaN was written into the flow
+constexpr unsigned kStatusNodeOverflow = 2u;  // a loop-frequency node table overflowed
+
+// Lane-balanced RPA schedule: the RPA pair lists of all rids, merged into distinct
+// (rid1, rid2) pairs with their multiplicity, sorted by output rid, and cut into `lanes`
+// contiguous chunks.  Entry i of lane l is sched[i * lanes + l]:
+//   bits 0-6 rid1, bits 7-13 rid2, bits 14-21 multiplicity, bit 22 "last pair of a segment".
+// A segment is a run of pairs of one output rid inside one chunk; its partial sum goes to the
+// next slot of the lane (slot_base[l], slot_base[l]+1, ...), and rid r sums the slots
+// seg_ptr[r] .. seg_ptr[r+1]-1 in order.
+struct RpaSchedule {
+    const int *sched;
+    const int *count;      // [lanes] entries of each lane
+    const int *slot_base;  // [lanes]
+    const int *seg_ptr;    // [Nl + 1]
+    int lanes, n_seg;
+};
+
+struct FlowArgs {
+    int n, nl, fn, wsite, max_nodes, n_range;
+    float cutoff, spin;
+    const float *freq;
+    const float *ss, *dd;  // state
+    float *dss, *ddd;      // flow
+    const float *v2;       // self-energy state
+    float *dv2;            // self-energy flow
+    const int *sites, *inv_sites, *ov_ptr, *ov_r1, *ov_r2, *range_rid, *range_inv;
+    float *node_wp, *node_c;
+    int *node_cnt;
+    int *work_counter;
+    unsigned *status;
+    RpaSchedule rpa;
+};
+
+// Vertex-flow kernel (su2_vertex.cu): dynamic shared memory per block, the number of blocks
+// per SM it achieves, and the launch.
+size_t vertex_flow_smem_bytes(int nl, int n_seg);
+int vertex_flow_blocks_per_sm(int nl, int n_seg);
+void launch_vertex_flow(const FlowArgs &a, int grid, cudaStream_t stream);
+
+}  // namespace spn

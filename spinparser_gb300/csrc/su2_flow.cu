@@ -24,6 +24,7 @@
 #include <cstring>
 #include <string>
 #include <vector>
+#include "su2_common.cuh"
 #include "su2_device.cuh"
 #include "host/capi_common.hpp"
 #include "../../include/spn_su2.h"
@@ -33,26 +34,8 @@ using namespace spn::dev;
 
 namespace {
 
-constexpr int kVertexThreads = 128;
-constexpr int kVertexWarps = kVertexThreads / 32;
-constexpr unsigned kStatusNaN = 1u;
-constexpr unsigned kStatusNodeOverflow = 2u;
 constexpr double kPiD = 3.14159265358979323846;
-
-struct FlowArgs {
-    int n, nl, fn, wsite, max_nodes, n_range;
-    float cutoff, spin;
-    const float *freq;
-    const float *ss, *dd;  // state
-    float *dss, *ddd;      // flow
-    const float *v2;       // self-energy state
-    float *dv2;            // self-energy flow
-    const int *sites, *inv_sites, *ov_ptr, *ov_r1, *ov_r2, *range_rid, *range_inv;
-    float *node_wp, *node_c;
-    int *node_cnt;
-    int *work_counter;
-    unsigned *status;
-};
+constexpr int kCorrWarps = 4;  // the correlation kernels run 128-thread blocks
 
 // ------------------------------------------------------------------------------------
 // 1. self-energy flow
@@ -130,288 +113,6 @@ __global__ void su2_node_table_kernel(FlowArgs a) {
     if (L < pos[n - 1]) nodes_left(pos, n, L, kat);
     a.node_cnt[xi] = cnt;
     if (overflow) atomicOr(a.status, kStatusNodeOverflow);
-}
-
-// ------------------------------------------------------------------------------------
-// 3. two-particle vertex flow
-// ------------------------------------------------------------------------------------
-template <int SPT>
-struct Lane {
-    int site[SPT], isite[SPT], j[SPT];
-    bool valid[SPT];
-};
-
-template <int SPT>
-__device__ __forceinline__ void gather(const FlowArgs &a, const AB4 &ab, const Lane<SPT> &ln, float *vs, float *vd) {
-#pragma unroll
-    for (int k = 0; k < SPT; ++k) {
-        const int st = ab.exch ? ln.isite[k] : ln.site[k];
-        float gs = 0.0f, gd = 0.0f;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            gs += ab.w[q] * __ldg(a.ss + ab.off[q] + st);
-            gd += ab.sw[q] * __ldg(a.dd + ab.off[q] + st);
-        }
-        vs[k] = gs;
-        vd[k] = gd;
-    }
-}
-
-__device__ __forceinline__ void local_values(const FlowArgs &a, const AB4 &ab, float &vs, float &vd) {
-    float gs = 0.0f, gd = 0.0f;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        gs += ab.w[q] * __ldg(a.ss + ab.off[q]);
-        gd += ab.sw[q] * __ldg(a.dd + ab.off[q]);
-    }
-    vs = gs;
-    vd = gd;
-}
-
-struct Transfer {
-    float s, t, u, w1p, w1, w2p, w2;
-};
-
-// integralKernelS (SU2FrgCore.cpp:199-227)
-template <int SPT>
-__device__ __forceinline__ void kernel_s(const FlowArgs &a, const float *pos, const Transfer &f, float wp, const Lane<SPT> &ln,
-                                         float *rs, float *rd) {
-    AB4 ab;
-    float S0[SPT], S1[SPT], S2[SPT], S3[SPT], D0[SPT], D1[SPT], D2[SPT], D3[SPT];
-    access4<kS>(pos, a.n, a.nl, f.s, -f.w1 - wp, -f.w2 - wp, ab);
-    gather(a, ab, ln, S0, D0);
-    access4<kS>(pos, a.n, a.nl, f.s, f.w1p + wp, -f.w2p - wp, ab);
-    gather(a, ab, ln, S1, D1);
-    access4<kS>(pos, a.n, a.nl, f.s, f.w2 + wp, f.w1 + wp, ab);
-    gather(a, ab, ln, S2, D2);
-    access4<kS>(pos, a.n, a.nl, f.s, -f.w2p - wp, f.w1p + wp, ab);
-    gather(a, ab, ln, S3, D3);
-#pragma unroll
-    for (int k = 0; k < SPT; ++k) {
-        float x = 0.0f;
-        x -= 0.5f * S0[k] * S1[k];
-        x -= 0.5f * S2[k] * S3[k];
-        x += D0[k] * S1[k];
-        x += D2[k] * S3[k];
-        x += S0[k] * D1[k];
-        x += S2[k] * D3[k];
-        float y = 0.0f;
-        y += (3.0f / 16.0f) * S0[k] * S1[k];
-        y += (3.0f / 16.0f) * S2[k] * S3[k];
-        y += D0[k] * D1[k];
-        y += D2[k] * D3[k];
-        rs[k] = x;
-        rd[k] = y;
-    }
-}
-
-// integralKernelU (SU2FrgCore.cpp:305-334)
-template <int SPT>
-__device__ __forceinline__ void kernel_u(const FlowArgs &a, const float *pos, const Transfer &f, float wp, const Lane<SPT> &ln,
-                                         float *rs, float *rd) {
-    AB4 ab;
-    float S0[SPT], S1[SPT], S2[SPT], S3[SPT], D0[SPT], D1[SPT], D2[SPT], D3[SPT];
-    access4<kU>(pos, a.n, a.nl, f.w1 + wp, wp - f.w2p, f.u, ab);
-    gather(a, ab, ln, S0, D0);
-    access4<kU>(pos, a.n, a.nl, f.w1p + wp, f.w2 - wp, f.u, ab);
-    gather(a, ab, ln, S1, D1);
-    access4<kU>(pos, a.n, a.nl, f.w2p - wp, -f.w1 - wp, f.u, ab);
-    gather(a, ab, ln, S2, D2);
-    access4<kU>(pos, a.n, a.nl, f.w2 - wp, f.w1p + wp, f.u, ab);
-    gather(a, ab, ln, S3, D3);
-#pragma unroll
-    for (int k = 0; k < SPT; ++k) {
-        float x = 0.0f;
-        x += 0.5f * S0[k] * S1[k];
-        x += 0.5f * S2[k] * S3[k];
-        x += S0[k] * D1[k];
-        x += S2[k] * D3[k];
-        x += D0[k] * S1[k];
-        x += D2[k] * S3[k];
-        float y = 0.0f;
-        y += (3.0f / 16.0f) * S0[k] * S1[k];
-        y += (3.0f / 16.0f) * S2[k] * S3[k];
-        y += D0[k] * D1[k];
-        y += D2[k] * D3[k];
-        rs[k] = x;
-        rd[k] = y;
-    }
-}
-
-// integralKernelT (SU2FrgCore.cpp:229-303).  `xb` is this group's shared-memory exchange
-// area: four arrays of `stride` floats (spin A, spin B, density A, density B by site).
-template <int SPT>
-__device__ __forceinline__ void kernel_t(const FlowArgs &a, const float *pos, const Transfer &f, float wp, const Lane<SPT> &ln,
-                                         float *xb, int stride, float *rs, float *rd) {
-    AB4 ab;
-    float S0[SPT], S1[SPT], S2[SPT], S3[SPT], D0[SPT], D1[SPT], D2[SPT], D3[SPT];
-    access4<kT>(pos, a.n, a.nl, f.w1 - wp, f.t, f.w1p + wp, ab);
-    gather(a, ab, ln, S0, D0);
-    access4<kT>(pos, a.n, a.nl, f.w2p - wp, f.t, -f.w2 - wp, ab);
-    gather(a, ab, ln, S1, D1);
-    access4<kT>(pos, a.n, a.nl, f.w1p + wp, f.t, f.w1 - wp, ab);
-    gather(a, ab, ln, S2, D2);
-    access4<kT>(pos, a.n, a.nl, f.w2 + wp, f.t, wp - f.w2p, ab);
-    gather(a, ab, ln, S3, D3);
-#pragma unroll
-    for (int k = 0; k < SPT; ++k)
-        if (ln.valid[k]) {
-            const int j = ln.j[k];
-            xb[j] = S2[k];
-            xb[stride + j] = S3[k];
-            xb[2 * stride + j] = D2[k];
-            xb[3 * stride + j] = D3[k];
-        }
-    __syncwarp();
-    float cbs, cbd, icas, icad, cbs2, cbd2, icas2, icad2;
-    access4<kU>(pos, a.n, a.nl, f.w2p - wp, -f.w2 - wp, f.t, ab);
-    local_values(a, ab, cbs, cbd);
-    access4<kU>(pos, a.n, a.nl, f.w1 - wp, -f.w1p - wp, -f.t, ab);
-    local_values(a, ab, icas, icad);
-    access4<kU>(pos, a.n, a.nl, f.w2 + wp, wp - f.w2p, f.t, ab);
-    local_values(a, ab, cbs2, cbd2);
-    access4<kU>(pos, a.n, a.nl, f.w1p + wp, wp - f.w1, -f.t, ab);
-    local_values(a, ab, icas2, icad2);
-    const float s2 = 2.0f * a.spin, s8 = 8.0f * a.spin;
-#pragma unroll
-    for (int k = 0; k < SPT; ++k) {
-        float rpa_s = 0.0f, rpa_d = 0.0f;
-        if (ln.valid[k]) {
-            const int rid = ln.j[k];
-            const int i0 = __ldg(a.ov_ptr + rid), i1 = __ldg(a.ov_ptr + rid + 1);
-            for (int i = i0; i < i1; ++i) {
-                const int r1 = __ldg(a.ov_r1 + i), r2 = __ldg(a.ov_r2 + i);
-                rpa_s += xb[r1] * xb[stride + r2];
-                rpa_d += xb[2 * stride + r1] * xb[3 * stride + r2];
-            }
-        }
-        float x = 0.0f + s2 * rpa_s;
-        x -= cbd * S0[k];
-        x += (0.25f * cbs) * S0[k];
-        x -= icad * S1[k];
-        x += (0.25f * icas) * S1[k];
-        x -= cbd2 * S2[k];
-        x += (0.25f * cbs2) * S2[k];
-        x -= icad2 * S3[k];
-        x += (0.25f * icas2) * S3[k];
-        float y = 0.0f + s8 * rpa_d;
-        y -= cbd * D0[k];
-        y -= (0.75f * cbs) * D0[k];
-        y -= icad * D1[k];
-        y -= (0.75f * icas) * D1[k];
-        y -= cbd2 * D2[k];
-        y -= (0.75f * cbs2) * D2[k];
-        y -= icad2 * D3[k];
-        y -= (0.75f * icas2) * D3[k];
-        rs[k] = x;
-        rd[k] = y;
-    }
-    __syncwarp();
-}
-
-__device__ __forceinline__ void kahan_add(float &sum, float &comp, float v) {
-    const float y = v - comp;
-    const float t = sum + y;
-    comp = (t - sum) - y;
-    sum = t;
-}
-
-template <int CH, int SPT>
-__device__ __forceinline__ void channel_sum(const FlowArgs &a, const float *pos, const Transfer &f, int xi, int g, int G,
-                                            const Lane<SPT> &ln, float *xb, int stride, float *acc_s, float *cmp_s,
-                                            float *acc_d, float *cmp_d) {
-    const int cnt = __ldg(a.node_cnt + xi);
-    const float *nwp = a.node_wp + size_t(xi) * a.max_nodes;
-    const float *nc = a.node_c + size_t(xi) * a.max_nodes;
-    const int trips = (cnt + G - 1) / G;
-    for (int r = 0; r < trips; ++r) {
-        const int k = r * G + g;
-        const bool active = k < cnt;
-        const float wp = active ? __ldg(nwp + k) : 0.0f;
-        float c = active ? __ldg(nc + k) : 0.0f;
-        if (CH == kU) c = -c;
-        float rs[SPT], rd[SPT];
-        if (CH == kS) kernel_s<SPT>(a, pos, f, wp, ln, rs, rd);
-        else if (CH == kT) kernel_t<SPT>(a, pos, f, wp, ln, xb, stride, rs, rd);
-        else kernel_u<SPT>(a, pos, f, wp, ln, rs, rd);
-        if (active) {
-#pragma unroll
-            for (int q = 0; q < SPT; ++q) {
-                kahan_add(acc_s[q], cmp_s[q], c * rs[q]);
-                kahan_add(acc_d[q], cmp_d[q], c * rd[q]);
-            }
-        }
-    }
-}
-
-template <int SPT>
-__global__ void __launch_bounds__(kVertexThreads) su2_vertex_flow_kernel(FlowArgs a) {
-    extern __shared__ float smem[];
-    float *pos = smem;
-    for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
-    __syncthreads();
-
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int W = (SPT == 1) ? a.wsite : 32;
-    const int G = 32 / W;
-    const int g = lane / W, jl = lane - g * W;
-    const int stride = 32 * SPT;
-    float *xb = smem + kMaxFreq + warp * 4 * stride + (SPT == 1 ? g * W : 0);
-
-    Lane<SPT> ln;
-#pragma unroll
-    for (int k = 0; k < SPT; ++k) {
-        const int j = jl + k * W;
-        ln.j[k] = j;
-        ln.valid[k] = j < a.nl;
-        ln.site[k] = ln.valid[k] ? a.sites[j] : 0;
-        ln.isite[k] = ln.valid[k] ? a.inv_sites[j] : 0;
-    }
-    const float two_pi = 2.0f * float(kPiD);
-
-    for (;;) {
-        int it = 0;
-        if (lane == 0) it = atomicAdd(a.work_counter, 1);
-        it = __shfl_sync(0xffffffffu, it, 0);
-        if (it >= a.fn) break;
-        const int su = it / a.n, ti = it - su * a.n;
-        int si = int((sqrtf(8.0f * float(su) + 1.0f) - 1.0f) * 0.5f);
-        while (si * (si + 1) / 2 > su) --si;
-        while ((si + 1) * (si + 2) / 2 <= su) ++si;
-        const int ui = su - si * (si + 1) / 2;
-
-        Transfer f;
-        f.s = pos[si];
-        f.t = pos[ti];
-        f.u = pos[ui];
-        f.w1p = 0.5f * (f.s + f.t + f.u);
-        f.w1 = 0.5f * (f.s - f.t + f.u);
-        f.w2p = 0.5f * (f.s - f.t - f.u);
-        f.w2 = 0.5f * (f.s + f.t - f.u);
-
-        float acc_s[SPT], cmp_s[SPT], acc_d[SPT], cmp_d[SPT];
-#pragma unroll
-        for (int k = 0; k < SPT; ++k) acc_s[k] = cmp_s[k] = acc_d[k] = cmp_d[k] = 0.0f;
-        channel_sum<kS, SPT>(a, pos, f, si, g, G, ln, xb, stride, acc_s, cmp_s, acc_d, cmp_d);
-        channel_sum<kT, SPT>(a, pos, f, ti, g, G, ln, xb, stride, acc_s, cmp_s, acc_d, cmp_d);
-        channel_sum<kU, SPT>(a, pos, f, ui, g, G, ln, xb, stride, acc_s, cmp_s, acc_d, cmp_d);
-
-#pragma unroll
-        for (int k = 0; k < SPT; ++k) {
-            float vs = acc_s[k] - cmp_s[k], vd = acc_d[k] - cmp_d[k];
-            for (int o = W; o < 32; o <<= 1) {
-                vs += __shfl_xor_sync(0xffffffffu, vs, o);
-                vd += __shfl_xor_sync(0xffffffffu, vd, o);
-            }
-            if (g == 0 && ln.valid[k]) {
-                const float os = vs / two_pi, od = vd / two_pi;
-                const size_t idx = size_t(it) * a.nl + ln.j[k];
-                a.dss[idx] = os;
-                a.ddd[idx] = od;
-                if (isnan(os) || isnan(od)) atomicOr(a.status, kStatusNaN);
-            }
-        }
-    }
 }
 
 // ------------------------------------------------------------------------------------
@@ -494,7 +195,7 @@ __global__ void __launch_bounds__(128) su2_corr_inner_kernel(CorrArgs a) {
     const double dw = double(w) + sig(w);
     double acc_s[SPT], acc_d[SPT];
     for (int k = 0; k < SPT; ++k) acc_s[k] = acc_d[k] = 0.0;
-    const int groups = kVertexWarps * G;
+    const int groups = kCorrWarps * G;
     const int gid = warp * G + g;
     for (int b = gid; b < ncnt; b += groups) {
         const float wp = nwp[b];
@@ -537,7 +238,7 @@ __global__ void __launch_bounds__(128) su2_corr_inner_kernel(CorrArgs a) {
     __syncthreads();
     for (int j = threadIdx.x; j < nl; j += blockDim.x) {
         double s = 0.0, d = 0.0;
-        for (int q = 0; q < kVertexWarps; ++q) {
+        for (int q = 0; q < kCorrWarps; ++q) {
             s += red[q][0][j];
             d += red[q][1][j];
         }
@@ -645,6 +346,8 @@ struct spn_su2 {
     int *sites = nullptr, *inv_sites = nullptr, *ov_ptr = nullptr, *ov_r1 = nullptr, *ov_r2 = nullptr;
     int *range_rid = nullptr, *range_inv = nullptr, *corr_rid = nullptr;
     double *corr_partial = nullptr;
+    int *rpa_sched = nullptr, *rpa_count = nullptr, *rpa_slot_base = nullptr, *rpa_seg_ptr = nullptr;
+    int rpa_lanes = 0, rpa_n_seg = 0;
     bool profiling = false;
     std::vector<cudaEvent_t> ev_pool;
     std::vector<std::pair<int, int>> ev_vertex, ev_step;  // indices into ev_pool
@@ -678,6 +381,12 @@ struct spn_su2 {
         a.node_cnt = node_cnt;
         a.work_counter = work_counter;
         a.status = status;
+        a.rpa.sched = rpa_sched;
+        a.rpa.count = rpa_count;
+        a.rpa.slot_base = rpa_slot_base;
+        a.rpa.seg_ptr = rpa_seg_ptr;
+        a.rpa.lanes = rpa_lanes;
+        a.rpa.n_seg = rpa_n_seg;
         return a;
     }
 
@@ -692,8 +401,10 @@ struct spn_su2 {
         cudaSetDevice(device);
         for (auto e : ev_pool) cudaEventDestroy(e);
         ev_pool.clear();
-        void *ptrs[] = {freq, ss, dd, dss, ddd, v2, dv2, node_wp, node_c, corr_out, node_cnt, work_counter, status,
-                        sites, inv_sites, ov_ptr, ov_r1, ov_r2, range_rid, range_inv, corr_rid, corr_partial};
+        void *ptrs[] = {freq,      ss,        dd,        dss,       ddd,          v2,          dv2,
+                        node_wp,   node_c,    corr_out,  node_cnt,  work_counter, status,      sites,
+                        inv_sites, ov_ptr,    ov_r1,     ov_r2,     range_rid,    range_inv,   corr_rid,
+                        corr_partial, rpa_sched, rpa_count, rpa_slot_base, rpa_seg_ptr};
         for (void *p : ptrs)
             if (p) cudaFree(p);
         if (own_stream && stream) cudaStreamDestroy(stream);
@@ -714,16 +425,63 @@ void upload(T *dst, const T *src, size_t count, cudaStream_t s) {
     if (count) cuda_check(cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync H2D");
 }
 
-size_t vertex_smem_bytes(int spt) { return sizeof(float) * (kMaxFreq + kVertexWarps * 4 * 32 * spt); }
-
 void launch_vertex(spn_su2 *h) {
-    FlowArgs a = h->args();
-    const int spt = spt_for(h->nl);
-    const size_t smem = vertex_smem_bytes(spt);
-    if (spt == 1) su2_vertex_flow_kernel<1><<<h->vertex_grid, kVertexThreads, smem, h->stream>>>(a);
-    else if (spt == 2) su2_vertex_flow_kernel<2><<<h->vertex_grid, kVertexThreads, smem, h->stream>>>(a);
-    else su2_vertex_flow_kernel<4><<<h->vertex_grid, kVertexThreads, smem, h->stream>>>(a);
+    launch_vertex_flow(h->args(), h->vertex_grid, h->stream);
     cuda_check(cudaGetLastError(), "vertex flow launch");
+}
+
+// Lane-balanced RPA schedule (see RpaSchedule in su2_common.cuh) from the reference's
+// per-rid overlap pair lists (Lattice::getOverlap, src/Lattice.hpp:472).
+struct HostRpa {
+    std::vector<int> sched, count, slot_base, seg_ptr;
+    int lanes = 0, n_seg = 0;
+};
+
+HostRpa build_rpa_schedule(int nl, const int *ptr, const int *r1, const int *r2, int lanes) {
+    struct Pair {
+        int rid, a, b, m;
+    };
+    std::vector<Pair> pairs;
+    std::vector<int> mult(size_t(nl) * nl);
+    for (int r = 0; r < nl; ++r) {
+        std::fill(mult.begin(), mult.end(), 0);
+        for (int i = ptr[r]; i < ptr[r + 1]; ++i) ++mult[size_t(r1[i]) * nl + r2[i]];
+        for (int a = 0; a < nl; ++a)
+            for (int b = 0; b < nl; ++b) {
+                const int m = mult[size_t(a) * nl + b];
+                if (!m) continue;
+                if (m > 255) throw Error(ErrorType::Unsupported, "RPA pair multiplicity above 255");
+                pairs.push_back({r, a, b, m});
+            }
+    }
+    HostRpa s;
+    s.lanes = lanes;
+    const int P = int(pairs.size());
+    const int L = (P + lanes - 1) / lanes;
+    s.sched.assign(size_t(std::max(L, 1)) * lanes, 0);
+    s.count.assign(lanes, 0);
+    s.slot_base.assign(lanes, 0);
+    s.seg_ptr.assign(nl + 1, -1);
+    int seg = -1;
+    for (int l = 0; l < lanes; ++l) {
+        const int b0 = l * L, b1 = std::min(P, (l + 1) * L);
+        s.count[l] = std::max(0, b1 - b0);
+        s.slot_base[l] = seg + 1;
+        for (int i = b0; i < b1; ++i) {
+            const Pair &p = pairs[i];
+            if (i == b0 || pairs[i - 1].rid != p.rid) {
+                ++seg;
+                if (s.seg_ptr[p.rid] < 0) s.seg_ptr[p.rid] = seg;
+            }
+            const bool last = (i + 1 == b1) || pairs[i + 1].rid != p.rid;
+            s.sched[size_t(i - b0) * lanes + l] = p.a | (p.b << 7) | (p.m << 14) | (last ? (1 << 22) : 0);
+        }
+    }
+    s.n_seg = seg + 1;
+    s.seg_ptr[nl] = s.n_seg;
+    for (int r = nl - 1; r >= 0; --r)
+        if (s.seg_ptr[r] < 0) s.seg_ptr[r] = s.seg_ptr[r + 1];
+    return s;
 }
 
 void validate_desc(const spn_su2_desc *d) {
@@ -861,18 +619,25 @@ extern "C" int spn_su2_create(const spn_su2_desc *d, spn_su2 **out) {
             cuda_check(cudaMemsetAsync(h->v2, 0, h->n * sizeof(float), h->stream), "memset");
             cuda_check(cudaMemsetAsync(h->dv2, 0, h->n * sizeof(float), h->stream), "memset");
             cuda_check(cudaMemsetAsync(h->status, 0, sizeof(unsigned), h->stream), "memset");
+            // balanced RPA schedule for the lanes of one node group
+            const int lanes = spt_for(h->nl) == 1 ? wsite_for(h->nl) : 32;
+            HostRpa rpa = build_rpa_schedule(h->nl, d->overlap_ptr, d->overlap_rid1, d->overlap_rid2, lanes);
+            h->rpa_lanes = rpa.lanes;
+            h->rpa_n_seg = rpa.n_seg;
+            h->rpa_sched = dev_alloc<int>(rpa.sched.size(), "alloc rpa schedule");
+            h->rpa_count = dev_alloc<int>(rpa.count.size(), "alloc rpa schedule");
+            h->rpa_slot_base = dev_alloc<int>(rpa.slot_base.size(), "alloc rpa schedule");
+            h->rpa_seg_ptr = dev_alloc<int>(rpa.seg_ptr.size(), "alloc rpa schedule");
+            upload(h->rpa_sched, rpa.sched.data(), rpa.sched.size(), h->stream);
+            upload(h->rpa_count, rpa.count.data(), rpa.count.size(), h->stream);
+            upload(h->rpa_slot_base, rpa.slot_base.data(), rpa.slot_base.size(), h->stream);
+            upload(h->rpa_seg_ptr, rpa.seg_ptr.data(), rpa.seg_ptr.size(), h->stream);
             // persistent vertex grid: every SM filled to its occupancy limit
-            int sms = 0, per_sm = 0;
+            int sms = 0;
             cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device), "device attribute");
-            const int spt = spt_for(h->nl);
-            const size_t smem = vertex_smem_bytes(spt);
-            if (spt == 1)
-                cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, su2_vertex_flow_kernel<1>, kVertexThreads, smem), "occupancy");
-            else if (spt == 2)
-                cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, su2_vertex_flow_kernel<2>, kVertexThreads, smem), "occupancy");
-            else
-                cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, su2_vertex_flow_kernel<4>, kVertexThreads, smem), "occupancy");
-            h->vertex_grid = sms * (per_sm > 0 ? per_sm : 1);
+            const int per_sm = vertex_flow_blocks_per_sm(h->nl, h->rpa_n_seg);
+            if (per_sm < 1) throw Error(ErrorType::Unsupported, "vertex-flow kernel does not fit on this device");
+            h->vertex_grid = sms * per_sm;
             cuda_check(cudaStreamSynchronize(h->stream), "create sync");
         } catch (...) {
             h->release();

@@ -1,0 +1,409 @@
+// Two-particle vertex flow of the SU(2) pf-FRG right-hand side on sm_103a
+// (SU2FrgCore::_calculateVertexTwoParticle, src/SU2/SU2FrgCore.cpp:171-431).
+//
+// For one frequency triple (s,t,u) the flow is
+//   sum over channels X in {s,t,u} of sum over loop-frequency nodes (wp, c) of c * K_X(wp)
+// where the node lists (conventional terms at wp = +-Lambda and the trapezoid nodes of the
+// Katanin integrals, with propagators folded into c) depend only on the channel's transfer
+// frequency and are built per step by su2_node_table_kernel.
+//
+// Work distribution: a persistent grid; each warp pulls triples from a device atomic
+// counter.  For a triple and channel, nodes are handled in batches of 32:
+//   phase A, lane = node: the node's interpolation supports (access buffers: folding, mesh
+//            searches, weights) are computed once and written to shared memory as a
+//            NodeDesc; for the t channel the four site-local vertex values are gathered too;
+//   phase B, lane = (node group, site): each group of W lanes (W = next power of two >= Nl)
+//            takes one node at a time, reads its descriptor (broadcast), gathers the four
+//            interpolated vertex slabs for its sites (coalesced: a slab is Nl contiguous
+//            floats) and forms K_X; the t channel's RPA lattice sum
+//            sum_i A[rid1_i] B[rid2_i] runs over a lane-balanced schedule of the merged pair
+//            list (no divergent per-rid loops) with deterministic segment partials.
+// Accumulation over nodes is Kahan-compensated FP32; group partials are combined by shuffles.
+#include "su2_common.cuh"
+#include "su2_device.cuh"
+
+namespace spn {
+namespace {
+
+using namespace spn::dev;
+
+constexpr int kThreads = 128;
+constexpr int kWarps = kThreads / 32;
+constexpr int kBatch = 32;
+constexpr double kPi = 3.14159265358979323846;
+
+struct __align__(16) NodeDesc {
+    int4 off[4];
+    float4 w[4];
+    float4 sw[4];
+    int exch;  // bit i: buffer i reads the site-exchanged pairs (inverted sites)
+    float c;   // node coefficient, channel sign included
+    float lv[8];  // t channel: site-local values cbs, cbd, icas, icad, cbs2, cbd2, icas2, icad2
+    int pad[2];
+};
+static_assert(sizeof(NodeDesc) % 16 == 0, "NodeDesc must stay 16-byte aligned");
+
+template <int SPT>
+struct Lane {
+    int site[SPT], isite[SPT], j[SPT];
+    bool valid[SPT];
+};
+
+struct Transfer {
+    float s, t, u, w1p, w1, w2p, w2;
+};
+
+__device__ __forceinline__ void put_ab(NodeDesc &d, int i, const AB4 &ab) {
+    d.off[i] = make_int4(ab.off[0], ab.off[1], ab.off[2], ab.off[3]);
+    d.w[i] = make_float4(ab.w[0], ab.w[1], ab.w[2], ab.w[3]);
+    d.sw[i] = make_float4(ab.sw[0], ab.sw[1], ab.sw[2], ab.sw[3]);
+}
+
+__device__ __forceinline__ void local_pair(const FlowArgs &a, const AB4 &ab, float &vs, float &vd) {
+    float gs = 0.0f, gd = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        gs += ab.w[q] * __ldg(a.ss + ab.off[q]);
+        gd += ab.sw[q] * __ldg(a.dd + ab.off[q]);
+    }
+    vs = gs;
+    vd = gd;
+}
+
+// Phase A: descriptor of one node (lane = node).
+template <int CH>
+__device__ __forceinline__ void make_desc(const FlowArgs &a, const float *pos, const Transfer &f, float wp, float c,
+                                          NodeDesc &d) {
+    AB4 ab;
+    int exch = 0;
+    const int n = a.n, nl = a.nl;
+    if (CH == kS) {  // integralKernelS, SU2FrgCore.cpp:202-206
+        access4<kS>(pos, n, nl, f.s, -f.w1 - wp, -f.w2 - wp, ab); put_ab(d, 0, ab); exch |= ab.exch << 0;
+        access4<kS>(pos, n, nl, f.s, f.w1p + wp, -f.w2p - wp, ab); put_ab(d, 1, ab); exch |= ab.exch << 1;
+        access4<kS>(pos, n, nl, f.s, f.w2 + wp, f.w1 + wp, ab); put_ab(d, 2, ab); exch |= ab.exch << 2;
+        access4<kS>(pos, n, nl, f.s, -f.w2p - wp, f.w1p + wp, ab); put_ab(d, 3, ab); exch |= ab.exch << 3;
+    } else if (CH == kT) {  // integralKernelT, SU2FrgCore.cpp:233-239, 269-284
+        access4<kT>(pos, n, nl, f.w1 - wp, f.t, f.w1p + wp, ab); put_ab(d, 0, ab); exch |= ab.exch << 0;
+        access4<kT>(pos, n, nl, f.w2p - wp, f.t, -f.w2 - wp, ab); put_ab(d, 1, ab); exch |= ab.exch << 1;
+        access4<kT>(pos, n, nl, f.w1p + wp, f.t, f.w1 - wp, ab); put_ab(d, 2, ab); exch |= ab.exch << 2;
+        access4<kT>(pos, n, nl, f.w2 + wp, f.t, wp - f.w2p, ab); put_ab(d, 3, ab); exch |= ab.exch << 3;
+        float v0, v1;
+        access4<kU>(pos, n, nl, f.w2p - wp, -f.w2 - wp, f.t, ab); local_pair(a, ab, v0, v1); d.lv[0] = v0; d.lv[1] = v1;
+        access4<kU>(pos, n, nl, f.w1 - wp, -f.w1p - wp, -f.t, ab); local_pair(a, ab, v0, v1); d.lv[2] = v0; d.lv[3] = v1;
+        access4<kU>(pos, n, nl, f.w2 + wp, wp - f.w2p, f.t, ab); local_pair(a, ab, v0, v1); d.lv[4] = v0; d.lv[5] = v1;
+        access4<kU>(pos, n, nl, f.w1p + wp, wp - f.w1, -f.t, ab); local_pair(a, ab, v0, v1); d.lv[6] = v0; d.lv[7] = v1;
+    } else {  // integralKernelU, SU2FrgCore.cpp:309-313
+        access4<kU>(pos, n, nl, f.w1 + wp, wp - f.w2p, f.u, ab); put_ab(d, 0, ab); exch |= ab.exch << 0;
+        access4<kU>(pos, n, nl, f.w1p + wp, f.w2 - wp, f.u, ab); put_ab(d, 1, ab); exch |= ab.exch << 1;
+        access4<kU>(pos, n, nl, f.w2p - wp, -f.w1 - wp, f.u, ab); put_ab(d, 2, ab); exch |= ab.exch << 2;
+        access4<kU>(pos, n, nl, f.w2 - wp, f.w1p + wp, f.u, ab); put_ab(d, 3, ab); exch |= ab.exch << 3;
+    }
+    d.exch = exch;
+    d.c = c;
+}
+
+// Phase B: interpolated slab of buffer i for this lane's sites (getValueSuperbundle).
+template <int SPT>
+__device__ __forceinline__ void gather(const FlowArgs &a, const NodeDesc &d, int i, const Lane<SPT> &ln, float *vs,
+                                       float *vd) {
+    const int4 o = d.off[i];
+    const float4 w = d.w[i];
+    const float4 sw = d.sw[i];
+    const bool ex = (d.exch >> i) & 1;
+#pragma unroll
+    for (int k = 0; k < SPT; ++k) {
+        const int st = ex ? ln.isite[k] : ln.site[k];
+        float gs = 0.0f, gd = 0.0f;
+        gs += w.x * __ldg(a.ss + o.x + st);
+        gd += sw.x * __ldg(a.dd + o.x + st);
+        gs += w.y * __ldg(a.ss + o.y + st);
+        gd += sw.y * __ldg(a.dd + o.y + st);
+        gs += w.z * __ldg(a.ss + o.z + st);
+        gd += sw.z * __ldg(a.dd + o.z + st);
+        gs += w.w * __ldg(a.ss + o.w + st);
+        gd += sw.w * __ldg(a.dd + o.w + st);
+        vs[k] = gs;
+        vd[k] = gd;
+    }
+}
+
+__device__ __forceinline__ void kahan_add(float &sum, float &comp, float v) {
+    const float y = v - comp;
+    const float t = sum + y;
+    comp = (t - sum) - y;
+    sum = t;
+}
+
+// Per-group shared-memory exchange area of the t channel.
+struct TExchange {
+    float2 *A;      // [sites] (spin, density) of the third slab
+    float2 *B;      // [sites] (spin, density) of the fourth slab
+    float2 *slots;  // [n_seg] RPA segment partials
+};
+
+template <int CH, int SPT>
+__device__ __forceinline__ void node_term(const FlowArgs &a, const NodeDesc &d, const Lane<SPT> &ln, int jl,
+                                          const TExchange &tx, float *rs, float *rd) {
+    float S0[SPT], S1[SPT], S2[SPT], S3[SPT], D0[SPT], D1[SPT], D2[SPT], D3[SPT];
+    gather<SPT>(a, d, 0, ln, S0, D0);
+    gather<SPT>(a, d, 1, ln, S1, D1);
+    gather<SPT>(a, d, 2, ln, S2, D2);
+    gather<SPT>(a, d, 3, ln, S3, D3);
+    if (CH == kS || CH == kU) {
+#pragma unroll
+        for (int k = 0; k < SPT; ++k) {
+            float x = 0.0f, y = 0.0f;
+            if (CH == kS) {  // SU2FrgCore.cpp:216-226
+                x -= 0.5f * S0[k] * S1[k];
+                x -= 0.5f * S2[k] * S3[k];
+                x += D0[k] * S1[k];
+                x += D2[k] * S3[k];
+                x += S0[k] * D1[k];
+                x += S2[k] * D3[k];
+            } else {  // SU2FrgCore.cpp:323-328
+                x += 0.5f * S0[k] * S1[k];
+                x += 0.5f * S2[k] * S3[k];
+                x += S0[k] * D1[k];
+                x += S2[k] * D3[k];
+                x += D0[k] * S1[k];
+                x += D2[k] * S3[k];
+            }
+            y += (3.0f / 16.0f) * S0[k] * S1[k];
+            y += (3.0f / 16.0f) * S2[k] * S3[k];
+            y += D0[k] * D1[k];
+            y += D2[k] * D3[k];
+            rs[k] = x;
+            rd[k] = y;
+        }
+        return;
+    }
+    // t channel: RPA lattice sum (SU2FrgCore.cpp:249-266) over the balanced schedule
+#pragma unroll
+    for (int k = 0; k < SPT; ++k)
+        if (ln.valid[k]) {
+            tx.A[ln.j[k]] = make_float2(S2[k], D2[k]);
+            tx.B[ln.j[k]] = make_float2(S3[k], D3[k]);
+        }
+    __syncwarp();
+    {
+        const int lanes = a.rpa.lanes;
+        const int cnt = __ldg(a.rpa.count + jl);
+        int slot = __ldg(a.rpa.slot_base + jl);
+        float acc_s = 0.0f, acc_d = 0.0f;
+        const int *sched = a.rpa.sched + jl;
+        for (int i = 0; i < cnt; ++i) {
+            const int e = __ldg(sched + i * lanes);
+            const float m = float((e >> 14) & 0xff);
+            const float2 A = tx.A[e & 0x7f];
+            const float2 B = tx.B[(e >> 7) & 0x7f];
+            acc_s = fmaf(A.x * m, B.x, acc_s);
+            acc_d = fmaf(A.y * m, B.y, acc_d);
+            if (e & (1 << 22)) {
+                tx.slots[slot++] = make_float2(acc_s, acc_d);
+                acc_s = 0.0f;
+                acc_d = 0.0f;
+            }
+        }
+    }
+    __syncwarp();
+    const float s2 = 2.0f * a.spin, s8 = 8.0f * a.spin;
+    const float cbs = d.lv[0], cbd = d.lv[1], icas = d.lv[2], icad = d.lv[3];
+    const float cbs2 = d.lv[4], cbd2 = d.lv[5], icas2 = d.lv[6], icad2 = d.lv[7];
+#pragma unroll
+    for (int k = 0; k < SPT; ++k) {
+        float rpa_s = 0.0f, rpa_d = 0.0f;
+        if (ln.valid[k]) {
+            const int r = ln.j[k];
+            const int s0 = __ldg(a.rpa.seg_ptr + r), s1 = __ldg(a.rpa.seg_ptr + r + 1);
+            for (int q = s0; q < s1; ++q) {
+                const float2 p = tx.slots[q];
+                rpa_s += p.x;
+                rpa_d += p.y;
+            }
+        }
+        float x = 0.0f + s2 * rpa_s;  // SU2FrgCore.cpp:265, 286-293
+        x -= cbd * S0[k];
+        x += (0.25f * cbs) * S0[k];
+        x -= icad * S1[k];
+        x += (0.25f * icas) * S1[k];
+        x -= cbd2 * S2[k];
+        x += (0.25f * cbs2) * S2[k];
+        x -= icad2 * S3[k];
+        x += (0.25f * icas2) * S3[k];
+        float y = 0.0f + s8 * rpa_d;  // SU2FrgCore.cpp:266, 295-302
+        y -= cbd * D0[k];
+        y -= (0.75f * cbs) * D0[k];
+        y -= icad * D1[k];
+        y -= (0.75f * icas) * D1[k];
+        y -= cbd2 * D2[k];
+        y -= (0.75f * cbs2) * D2[k];
+        y -= icad2 * D3[k];
+        y -= (0.75f * icas2) * D3[k];
+        rs[k] = x;
+        rd[k] = y;
+    }
+    __syncwarp();
+}
+
+template <int CH, int SPT>
+__device__ __forceinline__ void channel_sum(const FlowArgs &a, const float *pos, const Transfer &f, int xi, int lane, int g,
+                                            int G, int jl, const Lane<SPT> &ln, NodeDesc *desc, const TExchange &tx,
+                                            float *acc_s, float *cmp_s, float *acc_d, float *cmp_d) {
+    const int cnt = __ldg(a.node_cnt + xi);
+    const float *nwp = a.node_wp + size_t(xi) * a.max_nodes;
+    const float *nc = a.node_c + size_t(xi) * a.max_nodes;
+    for (int b0 = 0; b0 < cnt; b0 += kBatch) {
+        const int nb = min(kBatch, cnt - b0);
+        if (lane < nb) {
+            const float wp = __ldg(nwp + b0 + lane);
+            float c = __ldg(nc + b0 + lane);
+            if (CH == kU) c = -c;
+            make_desc<CH>(a, pos, f, wp, c, desc[lane]);
+        }
+        __syncwarp();
+        const int trips = (nb + G - 1) / G;
+        for (int r = 0; r < trips; ++r) {
+            const int k = r * G + g;
+            const bool active = k < nb;
+            const NodeDesc &d = desc[active ? k : 0];
+            float rs[SPT], rd[SPT];
+            node_term<CH, SPT>(a, d, ln, jl, tx, rs, rd);
+            if (active) {
+                const float c = d.c;
+#pragma unroll
+                for (int q = 0; q < SPT; ++q) {
+                    kahan_add(acc_s[q], cmp_s[q], c * rs[q]);
+                    kahan_add(acc_d[q], cmp_d[q], c * rd[q]);
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Shared memory: frequency mesh, then per warp: 32 node descriptors and, per node group,
+// the t-channel exchange area (A, B of W*SPT sites, n_seg slots).
+__host__ __device__ inline size_t warp_bytes(int wsite, int spt, int n_seg) {
+    const int G = 32 / wsite;
+    const size_t per_group = sizeof(float2) * (2 * size_t(wsite) * spt + n_seg);
+    return kBatch * sizeof(NodeDesc) + G * ((per_group + 15) / 16 * 16);
+}
+
+template <int SPT>
+__global__ void __launch_bounds__(kThreads) su2_vertex_flow_kernel(FlowArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *pos = reinterpret_cast<float *>(smem_raw);
+    for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int W = (SPT == 1) ? a.wsite : 32;
+    const int G = 32 / W;
+    const int g = lane / W, jl = lane - g * W;
+    const int n_seg = a.rpa.n_seg;
+    const size_t wb = warp_bytes(W, SPT, n_seg);
+    unsigned char *wbase = smem_raw + kMaxFreq * sizeof(float) + warp * wb;
+    NodeDesc *desc = reinterpret_cast<NodeDesc *>(wbase);
+    const size_t per_group = (sizeof(float2) * (2 * size_t(W) * SPT + n_seg) + 15) / 16 * 16;
+    float2 *gx = reinterpret_cast<float2 *>(wbase + kBatch * sizeof(NodeDesc) + g * per_group);
+    TExchange tx{gx, gx + W * SPT, gx + 2 * W * SPT};
+    __syncthreads();
+
+    Lane<SPT> ln;
+#pragma unroll
+    for (int k = 0; k < SPT; ++k) {
+        const int j = jl + k * W;
+        ln.j[k] = j;
+        ln.valid[k] = j < a.nl;
+        ln.site[k] = ln.valid[k] ? a.sites[j] : 0;
+        ln.isite[k] = ln.valid[k] ? a.inv_sites[j] : 0;
+    }
+    const float two_pi = 2.0f * float(kPi);
+
+    for (;;) {
+        int it = 0;
+        if (lane == 0) it = atomicAdd(a.work_counter, 1);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= a.fn) break;
+        const int su = it / a.n, ti = it - su * a.n;
+        int si = int((sqrtf(8.0f * float(su) + 1.0f) - 1.0f) * 0.5f);
+        while (si * (si + 1) / 2 > su) --si;
+        while ((si + 1) * (si + 2) / 2 <= su) ++si;
+        const int ui = su - si * (si + 1) / 2;
+
+        Transfer f;
+        f.s = pos[si];
+        f.t = pos[ti];
+        f.u = pos[ui];
+        f.w1p = 0.5f * (f.s + f.t + f.u);
+        f.w1 = 0.5f * (f.s - f.t + f.u);
+        f.w2p = 0.5f * (f.s - f.t - f.u);
+        f.w2 = 0.5f * (f.s + f.t - f.u);
+
+        float acc_s[SPT], cmp_s[SPT], acc_d[SPT], cmp_d[SPT];
+#pragma unroll
+        for (int k = 0; k < SPT; ++k) acc_s[k] = cmp_s[k] = acc_d[k] = cmp_d[k] = 0.0f;
+        channel_sum<kS, SPT>(a, pos, f, si, lane, g, G, jl, ln, desc, tx, acc_s, cmp_s, acc_d, cmp_d);
+        channel_sum<kT, SPT>(a, pos, f, ti, lane, g, G, jl, ln, desc, tx, acc_s, cmp_s, acc_d, cmp_d);
+        channel_sum<kU, SPT>(a, pos, f, ui, lane, g, G, jl, ln, desc, tx, acc_s, cmp_s, acc_d, cmp_d);
+
+#pragma unroll
+        for (int k = 0; k < SPT; ++k) {
+            float vs = acc_s[k] - cmp_s[k], vd = acc_d[k] - cmp_d[k];
+            for (int o = W; o < 32; o <<= 1) {
+                vs += __shfl_xor_sync(0xffffffffu, vs, o);
+                vd += __shfl_xor_sync(0xffffffffu, vd, o);
+            }
+            if (g == 0 && ln.valid[k]) {
+                const float os = vs / two_pi, od = vd / two_pi;
+                const size_t idx = size_t(it) * a.nl + ln.j[k];
+                a.dss[idx] = os;
+                a.ddd[idx] = od;
+                if (isnan(os) || isnan(od)) atomicOr(a.status, kStatusNaN);
+            }
+        }
+    }
+}
+
+int spt_of(int nl) { return nl <= 32 ? 1 : (nl <= 64 ? 2 : 4); }
+
+int wsite_of(int nl) {
+    if (nl > 32) return 32;
+    int w = 1;
+    while (w < nl) w <<= 1;
+    return w;
+}
+
+}  // namespace
+
+size_t vertex_flow_smem_bytes(int nl, int n_seg) {
+    const int spt = spt_of(nl);
+    return kMaxFreq * sizeof(float) + kWarps * warp_bytes(spt == 1 ? wsite_of(nl) : 32, spt, n_seg);
+}
+
+int vertex_flow_blocks_per_sm(int nl, int n_seg) {
+    const size_t smem = vertex_flow_smem_bytes(nl, n_seg);
+    const int spt = spt_of(nl);
+    int per_sm = 0;
+    cudaError_t e;
+    if (spt == 1) {
+        cudaFuncSetAttribute(su2_vertex_flow_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, su2_vertex_flow_kernel<1>, kThreads, smem);
+    } else if (spt == 2) {
+        cudaFuncSetAttribute(su2_vertex_flow_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, su2_vertex_flow_kernel<2>, kThreads, smem);
+    } else {
+        cudaFuncSetAttribute(su2_vertex_flow_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, su2_vertex_flow_kernel<4>, kThreads, smem);
+    }
+    return e == cudaSuccess ? per_sm : -1;
+}
+
+void launch_vertex_flow(const FlowArgs &a, int grid, cudaStream_t stream) {
+    const size_t smem = vertex_flow_smem_bytes(a.nl, a.rpa.n_seg);
+    const int spt = spt_of(a.nl);
+    if (spt == 1) su2_vertex_flow_kernel<1><<<grid, kThreads, smem, stream>>>(a);
+    else if (spt == 2) su2_vertex_flow_kernel<2><<<grid, kThreads, smem, stream>>>(a);
+    else su2_vertex_flow_kernel<4><<<grid, kThreads, smem, stream>>>(a);
+}
+
+}  // namespace spn
