@@ -264,6 +264,11 @@ def main():
     torch.cuda.synchronize()
     if flow.is_diverged():
         raise SystemExit("flow diverged during warm-up")
+    # pick the vertex-flow kernel variant on a mid-flow cutoff (work grows as the cutoff falls)
+    c_keep = flow.get_state()[0]
+    flow.set_cutoff(float(cut[len(cut) // 2]))
+    variant = flow.autotune(3)
+    flow.set_cutoff(c_keep)
 
     schedule = sampled_steps(len(cut), args.warmup, args.steps)
     starts = [torch.cuda.Event(enable_timing=True) for _ in schedule]
@@ -372,6 +377,7 @@ def main():
                      "achieved_evaluated": achieved_eval, "frac_evaluated": achieved_eval / fp32_peak,
                      "peak_source": "measured in-run: pure-FFMA kernel on this GPU (MEASURED_PEAKS.json has no "
                                     "FP32 CUDA-core figure)", "fp32_clock_ghz_implied": clk},
+        "vertex_variant": variant,
         "gpu_launches": KERNELS_PER_STEP * len(schedule),
         "clocks": clocks,
         "full_flow": full,

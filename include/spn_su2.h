@@ -172,6 +172,17 @@ int spn_su2_get_node_counts(spn_su2 *h, int *counts);
  * two-particle vertex flow, into the device-resident flow buffers.  Asynchronous. */
 int spn_su2_compute_step(spn_su2 *h);
 
+/* Picks the vertex-flow kernel variant for this flow by timing the candidates on the current
+ * state (`reps` launches each): nodes a site group evaluates per iteration (1 or 2) and
+ * whether the RPA schedule is staged in shared memory.  Leaves the state unchanged; reports
+ * the choice and the persistent grid size.  Replaces the reference LoadManager's throughput
+ * model (src/lib/LoadManager.hpp:796-852) as the tuning step of the work distribution. */
+int spn_su2_autotune(spn_su2 *h, int reps, int *npi, int *sched_in_smem, int *grid);
+
+/* Selects a vertex-flow variant explicitly (npi = 1 or 2; schedule in shared memory or not).
+ * SPN_E_UNSUPPORTED if it does not fit for this lattice. */
+int spn_su2_set_variant(spn_su2 *h, int npi, int sched_in_smem);
+
 /* Copies the flow computed by the last compute_step: dv2[N], dv4ss/dv4dd[F_N*Nl]. */
 int spn_su2_get_flow(spn_su2 *h, float *dv2, float *dv4ss, float *dv4dd);
 

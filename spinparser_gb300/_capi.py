@@ -75,6 +75,8 @@ SIGNATURES = {
     "spn_su2_set_cutoff": (C.c_int, [C.c_void_p, C.c_float]),
     "spn_su2_get_node_counts": (C.c_int, [C.c_void_p, c_int_p]),
     "spn_su2_compute_step": (C.c_int, [C.c_void_p]),
+    "spn_su2_autotune": (C.c_int, [C.c_void_p, C.c_int, c_int_p, c_int_p, c_int_p]),
+    "spn_su2_set_variant": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "spn_su2_get_flow": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p]),
     "spn_su2_finalize_step": (C.c_int, [C.c_void_p, C.c_float]),
     "spn_su2_measure_correlation": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p, c_float_p]),

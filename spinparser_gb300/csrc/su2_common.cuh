@@ -21,7 +21,14 @@ struct RpaSchedule {
     const int *slot_base;  // [lanes]
     const int *seg_ptr;    // [Nl + 1]
     int lanes, n_seg;
+    int len;       // entries per lane (sched holds len * lanes ints)
+    int in_smem;   // the kernel stages the schedule in shared memory
 };
+
+// Shared-memory words of a staged schedule (sched, count, slot_base, seg_ptr).
+__host__ __device__ inline int rpa_smem_ints(const RpaSchedule &r, int nl) {
+    return r.len * r.lanes + 2 * r.lanes + nl + 1;
+}
 
 struct FlowArgs {
     int n, nl, fn, wsite, max_nodes, n_range;
@@ -41,8 +48,13 @@ struct FlowArgs {
 
 // Vertex-flow kernel (su2_vertex.cu): dynamic shared memory per block, the number of blocks
 // per SM it achieves, and the launch.
-size_t vertex_flow_smem_bytes(int nl, int n_seg);
-int vertex_flow_blocks_per_sm(int nl, int n_seg);
-void launch_vertex_flow(const FlowArgs &a, int grid, cudaStream_t stream);
+// `npi`: loop-frequency nodes a site group evaluates per iteration (1 or 2); whether the RPA
+// schedule is staged in shared memory is a.rpa.in_smem.  Both are chosen per flow by timing.
+size_t vertex_flow_smem_bytes(int nl, const RpaSchedule &rpa, int npi);
+int vertex_flow_blocks_per_sm(int nl, const RpaSchedule &rpa, int npi);
+void launch_vertex_flow(const FlowArgs &a, int npi, int grid, cudaStream_t stream);
+
+// Largest schedule staged in shared memory; larger ones are read from global memory.
+constexpr int kRpaSmemMaxInts = 8192;
 
 }  // namespace spn

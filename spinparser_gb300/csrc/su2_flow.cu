@@ -19,6 +19,7 @@
 // The T-channel RPA lattice sum exchanges the per-site bubble values through shared memory.
 // Accumulation over loop frequencies is Kahan-compensated FP32.
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -347,7 +348,9 @@ struct spn_su2 {
     int *range_rid = nullptr, *range_inv = nullptr, *corr_rid = nullptr;
     double *corr_partial = nullptr;
     int *rpa_sched = nullptr, *rpa_count = nullptr, *rpa_slot_base = nullptr, *rpa_seg_ptr = nullptr;
-    int rpa_lanes = 0, rpa_n_seg = 0;
+    int rpa_lanes = 0, rpa_n_seg = 0, rpa_len = 0, rpa_in_smem = 0;
+    int vertex_npi = 1;       // loop-frequency nodes per site-group iteration
+    int sms = 0;
     bool profiling = false;
     std::vector<cudaEvent_t> ev_pool;
     std::vector<std::pair<int, int>> ev_vertex, ev_step;  // indices into ev_pool
@@ -387,6 +390,8 @@ struct spn_su2 {
         a.rpa.seg_ptr = rpa_seg_ptr;
         a.rpa.lanes = rpa_lanes;
         a.rpa.n_seg = rpa_n_seg;
+        a.rpa.len = rpa_len;
+        a.rpa.in_smem = rpa_in_smem;
         return a;
     }
 
@@ -426,8 +431,28 @@ void upload(T *dst, const T *src, size_t count, cudaStream_t s) {
 }
 
 void launch_vertex(spn_su2 *h) {
-    launch_vertex_flow(h->args(), h->vertex_grid, h->stream);
+    launch_vertex_flow(h->args(), h->vertex_npi, h->vertex_grid, h->stream);
     cuda_check(cudaGetLastError(), "vertex flow launch");
+}
+
+// Selects a vertex-flow variant: nodes per iteration and where the RPA schedule lives; the
+// persistent grid fills every SM to the variant's occupancy.  Returns false if it cannot run.
+bool select_variant(spn_su2 *h, int npi, int in_smem) {
+    if (in_smem) {
+        RpaSchedule r = h->args().rpa;
+        if (rpa_smem_ints(r, h->nl) > kRpaSmemMaxInts) return false;
+    }
+    const int old_smem = h->rpa_in_smem;
+    h->rpa_in_smem = in_smem;
+    const int per_sm = vertex_flow_blocks_per_sm(h->nl, h->args().rpa, npi);
+    cudaGetLastError();
+    if (per_sm < 1) {
+        h->rpa_in_smem = old_smem;
+        return false;
+    }
+    h->vertex_npi = npi;
+    h->vertex_grid = h->sms * per_sm;
+    return true;
 }
 
 // Lane-balanced RPA schedule (see RpaSchedule in su2_common.cuh) from the reference's
@@ -624,6 +649,7 @@ extern "C" int spn_su2_create(const spn_su2_desc *d, spn_su2 **out) {
             HostRpa rpa = build_rpa_schedule(h->nl, d->overlap_ptr, d->overlap_rid1, d->overlap_rid2, lanes);
             h->rpa_lanes = rpa.lanes;
             h->rpa_n_seg = rpa.n_seg;
+            h->rpa_len = int(rpa.sched.size()) / rpa.lanes;
             h->rpa_sched = dev_alloc<int>(rpa.sched.size(), "alloc rpa schedule");
             h->rpa_count = dev_alloc<int>(rpa.count.size(), "alloc rpa schedule");
             h->rpa_slot_base = dev_alloc<int>(rpa.slot_base.size(), "alloc rpa schedule");
@@ -635,9 +661,10 @@ extern "C" int spn_su2_create(const spn_su2_desc *d, spn_su2 **out) {
             // persistent vertex grid: every SM filled to its occupancy limit
             int sms = 0;
             cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device), "device attribute");
-            const int per_sm = vertex_flow_blocks_per_sm(h->nl, h->rpa_n_seg);
-            if (per_sm < 1) throw Error(ErrorType::Unsupported, "vertex-flow kernel does not fit on this device");
-            h->vertex_grid = sms * per_sm;
+            h->sms = sms;
+            // default variant; spn_su2_autotune can pick a faster one for this flow
+            if (!select_variant(h, 1, 0) && !select_variant(h, 1, 1))
+                throw Error(ErrorType::Unsupported, "vertex-flow kernel does not fit on this device");
             cuda_check(cudaStreamSynchronize(h->stream), "create sync");
         } catch (...) {
             h->release();
@@ -751,6 +778,69 @@ extern "C" int spn_su2_compute_step(spn_su2 *h) {
             h->ev_vertex.emplace_back(e1, e2);
             h->ev_step.emplace_back(e0, e2);
         }
+    });
+}
+
+extern "C" int spn_su2_set_variant(spn_su2 *h, int npi, int sched_in_smem) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        if (npi != 1 && npi != 2) throw Error(ErrorType::Argument, "nodes per iteration must be 1 or 2");
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        if (!select_variant(h, npi, sched_in_smem ? 1 : 0))
+            throw Error(ErrorType::Unsupported, "vertex-flow variant does not fit on this device for this lattice");
+    });
+}
+
+extern "C" int spn_su2_autotune(spn_su2 *h, int reps, int *npi, int *sched_in_smem, int *grid) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        reps = std::max(1, std::min(reps, 16));
+        cudaEvent_t e0, e1;
+        cuda_check(cudaEventCreate(&e0), "event");
+        cuda_check(cudaEventCreate(&e1), "event");
+        const bool prof = h->profiling;
+        h->profiling = false;
+        float best = 0.0f;
+        int best_npi = h->vertex_npi, best_smem = h->rpa_in_smem;
+        try {
+            // the node tables of the current cutoff (compute_step leaves the state untouched)
+            cuda_check(spn_su2_compute_step(h) == 0 ? cudaSuccess : cudaErrorUnknown, "autotune step");
+            for (int npi = 1; npi <= 2; ++npi)
+                for (int sm = 0; sm <= 1; ++sm) {
+                    if (!select_variant(h, npi, sm)) continue;
+                    std::vector<float> ms;
+                    for (int r = 0; r <= reps; ++r) {
+                        cuda_check(cudaMemsetAsync(h->work_counter, 0, sizeof(int), h->stream), "memset counter");
+                        cuda_check(cudaEventRecord(e0, h->stream), "record");
+                        launch_vertex(h);
+                        cuda_check(cudaEventRecord(e1, h->stream), "record");
+                        cuda_check(cudaEventSynchronize(e1), "sync");
+                        float t = 0.0f;
+                        cuda_check(cudaEventElapsedTime(&t, e0, e1), "elapsed");
+                        if (r > 0) ms.push_back(t);  // first launch warms caches
+                    }
+                    std::sort(ms.begin(), ms.end());
+                    const float med = ms[ms.size() / 2];
+                    if (best == 0.0f || med < best) {
+                        best = med;
+                        best_npi = npi;
+                        best_smem = sm;
+                    }
+                }
+        } catch (...) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            h->profiling = prof;
+            throw;
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        h->profiling = prof;
+        if (!select_variant(h, best_npi, best_smem)) throw Error(ErrorType::Internal, "autotune: chosen variant unavailable");
+        if (npi) *npi = h->vertex_npi;
+        if (sched_in_smem) *sched_in_smem = h->rpa_in_smem;
+        if (grid) *grid = h->vertex_grid;
     });
 }
 

@@ -134,120 +134,147 @@ __device__ __forceinline__ void kahan_add(float &sum, float &comp, float v) {
     sum = t;
 }
 
-// Per-group shared-memory exchange area of the t channel.
+// Per-group shared-memory exchange area of the t channel.  Spin and density values are kept
+// in separate 32-bit arrays: with Nl <= 32 every element sits in its own bank, so the RPA
+// gathers A[rid1], B[rid2] of a warp never conflict.
 struct TExchange {
-    float2 *A;      // [sites] (spin, density) of the third slab
-    float2 *B;      // [sites] (spin, density) of the fourth slab
-    float2 *slots;  // [n_seg] RPA segment partials
+    float *As, *Ad;  // [sites] spin / density of the third slab
+    float *Bs, *Bd;  // [sites] spin / density of the fourth slab
+    float2 *slots;   // [n_seg] RPA segment partials
+    const int *sched, *count, *slot_base, *seg_ptr;  // RPA schedule (shared or global memory)
 };
 
-template <int CH, int SPT>
-__device__ __forceinline__ void node_term(const FlowArgs &a, const NodeDesc &d, const Lane<SPT> &ln, int jl,
-                                          const TExchange &tx, float *rs, float *rd) {
-    float S0[SPT], S1[SPT], S2[SPT], S3[SPT], D0[SPT], D1[SPT], D2[SPT], D3[SPT];
-    gather<SPT>(a, d, 0, ln, S0, D0);
-    gather<SPT>(a, d, 1, ln, S1, D1);
-    gather<SPT>(a, d, 2, ln, S2, D2);
-    gather<SPT>(a, d, 3, ln, S3, D3);
+// K_X at NPI nodes for this lane's sites (one group evaluates NPI nodes per iteration so that
+// the t channel decodes each RPA schedule entry once for all of them).
+template <int CH, int SPT, int NPI>
+__device__ __forceinline__ void node_term(const FlowArgs &a, const NodeDesc *const *d, const Lane<SPT> &ln, int jl,
+                                          const TExchange *tx, float (*rs)[SPT], float (*rd)[SPT]) {
+    float S0[NPI][SPT], S1[NPI][SPT], S2[NPI][SPT], S3[NPI][SPT], D0[NPI][SPT], D1[NPI][SPT], D2[NPI][SPT],
+        D3[NPI][SPT];
+#pragma unroll
+    for (int n = 0; n < NPI; ++n) {
+        gather<SPT>(a, *d[n], 0, ln, S0[n], D0[n]);
+        gather<SPT>(a, *d[n], 1, ln, S1[n], D1[n]);
+        gather<SPT>(a, *d[n], 2, ln, S2[n], D2[n]);
+        gather<SPT>(a, *d[n], 3, ln, S3[n], D3[n]);
+    }
     if (CH == kS || CH == kU) {
 #pragma unroll
-        for (int k = 0; k < SPT; ++k) {
-            float x = 0.0f, y = 0.0f;
-            if (CH == kS) {  // SU2FrgCore.cpp:216-226
-                x -= 0.5f * S0[k] * S1[k];
-                x -= 0.5f * S2[k] * S3[k];
-                x += D0[k] * S1[k];
-                x += D2[k] * S3[k];
-                x += S0[k] * D1[k];
-                x += S2[k] * D3[k];
-            } else {  // SU2FrgCore.cpp:323-328
-                x += 0.5f * S0[k] * S1[k];
-                x += 0.5f * S2[k] * S3[k];
-                x += S0[k] * D1[k];
-                x += S2[k] * D3[k];
-                x += D0[k] * S1[k];
-                x += D2[k] * S3[k];
+        for (int n = 0; n < NPI; ++n)
+#pragma unroll
+            for (int k = 0; k < SPT; ++k) {
+                float x = 0.0f, y = 0.0f;
+                if (CH == kS) {  // SU2FrgCore.cpp:216-226
+                    x -= 0.5f * S0[n][k] * S1[n][k];
+                    x -= 0.5f * S2[n][k] * S3[n][k];
+                    x += D0[n][k] * S1[n][k];
+                    x += D2[n][k] * S3[n][k];
+                    x += S0[n][k] * D1[n][k];
+                    x += S2[n][k] * D3[n][k];
+                } else {  // SU2FrgCore.cpp:323-328
+                    x += 0.5f * S0[n][k] * S1[n][k];
+                    x += 0.5f * S2[n][k] * S3[n][k];
+                    x += S0[n][k] * D1[n][k];
+                    x += S2[n][k] * D3[n][k];
+                    x += D0[n][k] * S1[n][k];
+                    x += D2[n][k] * S3[n][k];
+                }
+                y += (3.0f / 16.0f) * S0[n][k] * S1[n][k];
+                y += (3.0f / 16.0f) * S2[n][k] * S3[n][k];
+                y += D0[n][k] * D1[n][k];
+                y += D2[n][k] * D3[n][k];
+                rs[n][k] = x;
+                rd[n][k] = y;
             }
-            y += (3.0f / 16.0f) * S0[k] * S1[k];
-            y += (3.0f / 16.0f) * S2[k] * S3[k];
-            y += D0[k] * D1[k];
-            y += D2[k] * D3[k];
-            rs[k] = x;
-            rd[k] = y;
-        }
         return;
     }
     // t channel: RPA lattice sum (SU2FrgCore.cpp:249-266) over the balanced schedule
 #pragma unroll
-    for (int k = 0; k < SPT; ++k)
-        if (ln.valid[k]) {
-            tx.A[ln.j[k]] = make_float2(S2[k], D2[k]);
-            tx.B[ln.j[k]] = make_float2(S3[k], D3[k]);
-        }
+    for (int n = 0; n < NPI; ++n)
+#pragma unroll
+        for (int k = 0; k < SPT; ++k)
+            if (ln.valid[k]) {
+                const int j = ln.j[k];
+                tx[n].As[j] = S2[n][k];
+                tx[n].Ad[j] = D2[n][k];
+                tx[n].Bs[j] = S3[n][k];
+                tx[n].Bd[j] = D3[n][k];
+            }
     __syncwarp();
     {
         const int lanes = a.rpa.lanes;
-        const int cnt = __ldg(a.rpa.count + jl);
-        int slot = __ldg(a.rpa.slot_base + jl);
-        float acc_s = 0.0f, acc_d = 0.0f;
-        const int *sched = a.rpa.sched + jl;
+        const int cnt = tx[0].count[jl];
+        int slot = tx[0].slot_base[jl];
+        float acc_s[NPI], acc_d[NPI];
+#pragma unroll
+        for (int n = 0; n < NPI; ++n) acc_s[n] = acc_d[n] = 0.0f;
+        const int *sched = tx[0].sched + jl;
         for (int i = 0; i < cnt; ++i) {
-            const int e = __ldg(sched + i * lanes);
+            const int e = sched[i * lanes];
             const float m = float((e >> 14) & 0xff);
-            const float2 A = tx.A[e & 0x7f];
-            const float2 B = tx.B[(e >> 7) & 0x7f];
-            acc_s = fmaf(A.x * m, B.x, acc_s);
-            acc_d = fmaf(A.y * m, B.y, acc_d);
+            const int ra = e & 0x7f, rb = (e >> 7) & 0x7f;
+#pragma unroll
+            for (int n = 0; n < NPI; ++n) {
+                acc_s[n] = fmaf(tx[n].As[ra] * m, tx[n].Bs[rb], acc_s[n]);
+                acc_d[n] = fmaf(tx[n].Ad[ra] * m, tx[n].Bd[rb], acc_d[n]);
+            }
             if (e & (1 << 22)) {
-                tx.slots[slot++] = make_float2(acc_s, acc_d);
-                acc_s = 0.0f;
-                acc_d = 0.0f;
+#pragma unroll
+                for (int n = 0; n < NPI; ++n) {
+                    tx[n].slots[slot] = make_float2(acc_s[n], acc_d[n]);
+                    acc_s[n] = 0.0f;
+                    acc_d[n] = 0.0f;
+                }
+                ++slot;
             }
         }
     }
     __syncwarp();
     const float s2 = 2.0f * a.spin, s8 = 8.0f * a.spin;
-    const float cbs = d.lv[0], cbd = d.lv[1], icas = d.lv[2], icad = d.lv[3];
-    const float cbs2 = d.lv[4], cbd2 = d.lv[5], icas2 = d.lv[6], icad2 = d.lv[7];
 #pragma unroll
-    for (int k = 0; k < SPT; ++k) {
-        float rpa_s = 0.0f, rpa_d = 0.0f;
-        if (ln.valid[k]) {
-            const int r = ln.j[k];
-            const int s0 = __ldg(a.rpa.seg_ptr + r), s1 = __ldg(a.rpa.seg_ptr + r + 1);
-            for (int q = s0; q < s1; ++q) {
-                const float2 p = tx.slots[q];
-                rpa_s += p.x;
-                rpa_d += p.y;
+    for (int n = 0; n < NPI; ++n) {
+        const float cbs = d[n]->lv[0], cbd = d[n]->lv[1], icas = d[n]->lv[2], icad = d[n]->lv[3];
+        const float cbs2 = d[n]->lv[4], cbd2 = d[n]->lv[5], icas2 = d[n]->lv[6], icad2 = d[n]->lv[7];
+#pragma unroll
+        for (int k = 0; k < SPT; ++k) {
+            float rpa_s = 0.0f, rpa_d = 0.0f;
+            if (ln.valid[k]) {
+                const int r = ln.j[k];
+                const int s0 = tx[0].seg_ptr[r], s1 = tx[0].seg_ptr[r + 1];
+                for (int q = s0; q < s1; ++q) {
+                    const float2 p = tx[n].slots[q];
+                    rpa_s += p.x;
+                    rpa_d += p.y;
+                }
             }
+            float x = 0.0f + s2 * rpa_s;  // SU2FrgCore.cpp:265, 286-293
+            x -= cbd * S0[n][k];
+            x += (0.25f * cbs) * S0[n][k];
+            x -= icad * S1[n][k];
+            x += (0.25f * icas) * S1[n][k];
+            x -= cbd2 * S2[n][k];
+            x += (0.25f * cbs2) * S2[n][k];
+            x -= icad2 * S3[n][k];
+            x += (0.25f * icas2) * S3[n][k];
+            float y = 0.0f + s8 * rpa_d;  // SU2FrgCore.cpp:266, 295-302
+            y -= cbd * D0[n][k];
+            y -= (0.75f * cbs) * D0[n][k];
+            y -= icad * D1[n][k];
+            y -= (0.75f * icas) * D1[n][k];
+            y -= cbd2 * D2[n][k];
+            y -= (0.75f * cbs2) * D2[n][k];
+            y -= icad2 * D3[n][k];
+            y -= (0.75f * icas2) * D3[n][k];
+            rs[n][k] = x;
+            rd[n][k] = y;
         }
-        float x = 0.0f + s2 * rpa_s;  // SU2FrgCore.cpp:265, 286-293
-        x -= cbd * S0[k];
-        x += (0.25f * cbs) * S0[k];
-        x -= icad * S1[k];
-        x += (0.25f * icas) * S1[k];
-        x -= cbd2 * S2[k];
-        x += (0.25f * cbs2) * S2[k];
-        x -= icad2 * S3[k];
-        x += (0.25f * icas2) * S3[k];
-        float y = 0.0f + s8 * rpa_d;  // SU2FrgCore.cpp:266, 295-302
-        y -= cbd * D0[k];
-        y -= (0.75f * cbs) * D0[k];
-        y -= icad * D1[k];
-        y -= (0.75f * icas) * D1[k];
-        y -= cbd2 * D2[k];
-        y -= (0.75f * cbs2) * D2[k];
-        y -= icad2 * D3[k];
-        y -= (0.75f * icas2) * D3[k];
-        rs[k] = x;
-        rd[k] = y;
     }
     __syncwarp();
 }
 
-template <int CH, int SPT>
+template <int CH, int SPT, int NPI>
 __device__ __forceinline__ void channel_sum(const FlowArgs &a, const float *pos, const Transfer &f, int xi, int lane, int g,
-                                            int G, int jl, const Lane<SPT> &ln, NodeDesc *desc, const TExchange &tx,
+                                            int G, int jl, const Lane<SPT> &ln, NodeDesc *desc, const TExchange *tx,
                                             float *acc_s, float *cmp_s, float *acc_d, float *cmp_d) {
     const int cnt = __ldg(a.node_cnt + xi);
     const float *nwp = a.node_wp + size_t(xi) * a.max_nodes;
@@ -261,35 +288,47 @@ __device__ __forceinline__ void channel_sum(const FlowArgs &a, const float *pos,
             make_desc<CH>(a, pos, f, wp, c, desc[lane]);
         }
         __syncwarp();
-        const int trips = (nb + G - 1) / G;
+        const int trips = (nb + G * NPI - 1) / (G * NPI);
         for (int r = 0; r < trips; ++r) {
-            const int k = r * G + g;
-            const bool active = k < nb;
-            const NodeDesc &d = desc[active ? k : 0];
-            float rs[SPT], rd[SPT];
-            node_term<CH, SPT>(a, d, ln, jl, tx, rs, rd);
-            if (active) {
-                const float c = d.c;
+            const NodeDesc *d[NPI];
+            bool active[NPI];
 #pragma unroll
-                for (int q = 0; q < SPT; ++q) {
-                    kahan_add(acc_s[q], cmp_s[q], c * rs[q]);
-                    kahan_add(acc_d[q], cmp_d[q], c * rd[q]);
-                }
+            for (int n = 0; n < NPI; ++n) {
+                const int k = (r * G + g) * NPI + n;
+                active[n] = k < nb;
+                d[n] = &desc[active[n] ? k : 0];
             }
+            float rs[NPI][SPT], rd[NPI][SPT];
+            node_term<CH, SPT, NPI>(a, d, ln, jl, tx, rs, rd);
+#pragma unroll
+            for (int n = 0; n < NPI; ++n)
+                if (active[n]) {
+                    const float c = d[n]->c;
+#pragma unroll
+                    for (int q = 0; q < SPT; ++q) {
+                        kahan_add(acc_s[q], cmp_s[q], c * rs[n][q]);
+                        kahan_add(acc_d[q], cmp_d[q], c * rd[n][q]);
+                    }
+                }
         }
         __syncwarp();
     }
 }
 
-// Shared memory: frequency mesh, then per warp: 32 node descriptors and, per node group,
-// the t-channel exchange area (A, B of W*SPT sites, n_seg slots).
-__host__ __device__ inline size_t warp_bytes(int wsite, int spt, int n_seg) {
-    const int G = 32 / wsite;
-    const size_t per_group = sizeof(float2) * (2 * size_t(wsite) * spt + n_seg);
-    return kBatch * sizeof(NodeDesc) + G * ((per_group + 15) / 16 * 16);
+// Shared memory: frequency mesh; the RPA schedule when it is staged; then per warp: 32 node
+// descriptors and, per node group, NPI t-channel exchange areas (four arrays of W*SPT sites
+// and n_seg slots each).
+__host__ __device__ inline size_t node_area_bytes(int wsite, int spt, int n_seg) {
+    return (sizeof(float) * 4 * size_t(wsite) * spt + sizeof(float2) * n_seg + 15) / 16 * 16;
+}
+__host__ __device__ inline size_t warp_bytes(int wsite, int spt, int npi, int n_seg) {
+    return kBatch * sizeof(NodeDesc) + (32 / wsite) * npi * node_area_bytes(wsite, spt, n_seg);
+}
+__host__ __device__ inline size_t sched_bytes(const RpaSchedule &r, int nl) {
+    return r.in_smem ? (sizeof(int) * size_t(rpa_smem_ints(r, nl)) + 15) / 16 * 16 : 0;
 }
 
-template <int SPT>
+template <int SPT, int NPI>
 __global__ void __launch_bounds__(kThreads) su2_vertex_flow_kernel(FlowArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *pos = reinterpret_cast<float *>(smem_raw);
@@ -300,12 +339,46 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_flow_kernel(FlowArgs a) {
     const int G = 32 / W;
     const int g = lane / W, jl = lane - g * W;
     const int n_seg = a.rpa.n_seg;
-    const size_t wb = warp_bytes(W, SPT, n_seg);
-    unsigned char *wbase = smem_raw + kMaxFreq * sizeof(float) + warp * wb;
+    unsigned char *sbase = smem_raw + kMaxFreq * sizeof(float);
+    const int *sched, *count, *slot_base, *seg_ptr;
+    if (a.rpa.in_smem) {
+        int *s = reinterpret_cast<int *>(sbase);
+        const int ns = a.rpa.len * a.rpa.lanes, nc = a.rpa.lanes;
+        for (int i = threadIdx.x; i < ns; i += blockDim.x) s[i] = __ldg(a.rpa.sched + i);
+        for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+            s[ns + i] = __ldg(a.rpa.count + i);
+            s[ns + nc + i] = __ldg(a.rpa.slot_base + i);
+        }
+        for (int i = threadIdx.x; i <= a.nl; i += blockDim.x) s[ns + 2 * nc + i] = __ldg(a.rpa.seg_ptr + i);
+        sched = s;
+        count = s + ns;
+        slot_base = s + ns + nc;
+        seg_ptr = s + ns + 2 * nc;
+    } else {
+        sched = a.rpa.sched;
+        count = a.rpa.count;
+        slot_base = a.rpa.slot_base;
+        seg_ptr = a.rpa.seg_ptr;
+    }
+    unsigned char *wbase = sbase + sched_bytes(a.rpa, a.nl) + warp * warp_bytes(W, SPT, NPI, n_seg);
     NodeDesc *desc = reinterpret_cast<NodeDesc *>(wbase);
-    const size_t per_group = (sizeof(float2) * (2 * size_t(W) * SPT + n_seg) + 15) / 16 * 16;
-    float2 *gx = reinterpret_cast<float2 *>(wbase + kBatch * sizeof(NodeDesc) + g * per_group);
-    TExchange tx{gx, gx + W * SPT, gx + 2 * W * SPT};
+    const size_t nab = node_area_bytes(W, SPT, n_seg);
+    unsigned char *gbase = wbase + kBatch * sizeof(NodeDesc) + size_t(g) * NPI * nab;
+    const int ws = W * SPT;
+    TExchange tx[NPI];
+#pragma unroll
+    for (int n = 0; n < NPI; ++n) {
+        float *gx = reinterpret_cast<float *>(gbase + n * nab);
+        tx[n].As = gx;
+        tx[n].Ad = gx + ws;
+        tx[n].Bs = gx + 2 * ws;
+        tx[n].Bd = gx + 3 * ws;
+        tx[n].slots = reinterpret_cast<float2 *>(gx + 4 * ws);
+        tx[n].sched = sched;
+        tx[n].count = count;
+        tx[n].slot_base = slot_base;
+        tx[n].seg_ptr = seg_ptr;
+    }
     __syncthreads();
 
     Lane<SPT> ln;
@@ -342,9 +415,9 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_flow_kernel(FlowArgs a) {
         float acc_s[SPT], cmp_s[SPT], acc_d[SPT], cmp_d[SPT];
 #pragma unroll
         for (int k = 0; k < SPT; ++k) acc_s[k] = cmp_s[k] = acc_d[k] = cmp_d[k] = 0.0f;
-        channel_sum<kS, SPT>(a, pos, f, si, lane, g, G, jl, ln, desc, tx, acc_s, cmp_s, acc_d, cmp_d);
-        channel_sum<kT, SPT>(a, pos, f, ti, lane, g, G, jl, ln, desc, tx, acc_s, cmp_s, acc_d, cmp_d);
-        channel_sum<kU, SPT>(a, pos, f, ui, lane, g, G, jl, ln, desc, tx, acc_s, cmp_s, acc_d, cmp_d);
+        channel_sum<kS, SPT, NPI>(a, pos, f, si, lane, g, G, jl, ln, desc, tx, acc_s, cmp_s, acc_d, cmp_d);
+        channel_sum<kT, SPT, NPI>(a, pos, f, ti, lane, g, G, jl, ln, desc, tx, acc_s, cmp_s, acc_d, cmp_d);
+        channel_sum<kU, SPT, NPI>(a, pos, f, ui, lane, g, G, jl, ln, desc, tx, acc_s, cmp_s, acc_d, cmp_d);
 
 #pragma unroll
         for (int k = 0; k < SPT; ++k) {
@@ -375,35 +448,35 @@ int wsite_of(int nl) {
 
 }  // namespace
 
-size_t vertex_flow_smem_bytes(int nl, int n_seg) {
+size_t vertex_flow_smem_bytes(int nl, const RpaSchedule &rpa, int npi) {
     const int spt = spt_of(nl);
-    return kMaxFreq * sizeof(float) + kWarps * warp_bytes(spt == 1 ? wsite_of(nl) : 32, spt, n_seg);
+    return kMaxFreq * sizeof(float) + sched_bytes(rpa, nl) +
+           kWarps * warp_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, rpa.n_seg);
 }
 
-int vertex_flow_blocks_per_sm(int nl, int n_seg) {
-    const size_t smem = vertex_flow_smem_bytes(nl, n_seg);
-    const int spt = spt_of(nl);
+namespace {
+using VertexKernel = void (*)(FlowArgs);
+VertexKernel vertex_kernel(int spt, int npi) {
+    if (spt == 1) return npi == 1 ? su2_vertex_flow_kernel<1, 1> : su2_vertex_flow_kernel<1, 2>;
+    if (spt == 2) return npi == 1 ? su2_vertex_flow_kernel<2, 1> : su2_vertex_flow_kernel<2, 2>;
+    return npi == 1 ? su2_vertex_flow_kernel<4, 1> : su2_vertex_flow_kernel<4, 2>;
+}
+}  // namespace
+
+int vertex_flow_blocks_per_sm(int nl, const RpaSchedule &rpa, int npi) {
+    const size_t smem = vertex_flow_smem_bytes(nl, rpa, npi);
+    VertexKernel k = vertex_kernel(spt_of(nl), npi);
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess) return -1;
     int per_sm = 0;
-    cudaError_t e;
-    if (spt == 1) {
-        cudaFuncSetAttribute(su2_vertex_flow_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, su2_vertex_flow_kernel<1>, kThreads, smem);
-    } else if (spt == 2) {
-        cudaFuncSetAttribute(su2_vertex_flow_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, su2_vertex_flow_kernel<2>, kThreads, smem);
-    } else {
-        cudaFuncSetAttribute(su2_vertex_flow_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, su2_vertex_flow_kernel<4>, kThreads, smem);
-    }
-    return e == cudaSuccess ? per_sm : -1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, smem) != cudaSuccess) return -1;
+    return per_sm;
 }
 
-void launch_vertex_flow(const FlowArgs &a, int grid, cudaStream_t stream) {
-    const size_t smem = vertex_flow_smem_bytes(a.nl, a.rpa.n_seg);
-    const int spt = spt_of(a.nl);
-    if (spt == 1) su2_vertex_flow_kernel<1><<<grid, kThreads, smem, stream>>>(a);
-    else if (spt == 2) su2_vertex_flow_kernel<2><<<grid, kThreads, smem, stream>>>(a);
-    else su2_vertex_flow_kernel<4><<<grid, kThreads, smem, stream>>>(a);
+void launch_vertex_flow(const FlowArgs &a, int npi, int grid, cudaStream_t stream) {
+    const size_t smem = vertex_flow_smem_bytes(a.nl, a.rpa, npi);
+    VertexKernel k = vertex_kernel(spt_of(a.nl), npi);
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    k<<<grid, kThreads, smem, stream>>>(a);
 }
 
 }  // namespace spn

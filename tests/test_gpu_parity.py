@@ -66,6 +66,35 @@ def test_rhs_square_r3_n32_matches_oracle(square_r3):
     assert not flow.is_diverged()
 
 
+@pytest.mark.parametrize("lattice,rng,model,params", [
+    ("square", 3, "square-heisenberg", {"j": "1.0"}),
+    ("cubic", 3, "cubic-j1j2heisenberg", {"j1": "1.0", "j2": "0.25"}),
+])
+def test_every_vertex_variant_matches_oracle(lattice, rng, model, params):
+    """Each kernel variant the autotuner may pick (1 or 2 nodes per site-group iteration, RPA
+    schedule in shared or global memory) reproduces the oracle; autotune keeps parity."""
+    tab = spn.Lattice(lattice, rng, model, params).tables()
+    freq = spn.frequency_exponential(0.01, 30.0, 14)
+    orc = Oracle(tab, freq)
+    cut = np.array([3.0, 2.0, 1.0, 0.4], np.float32)
+    c, v2, ss, dd = oracle_state(orc, cut, *tab.initial_state(14), steps=2)
+    r2, rss, rdd = orc.rhs(c, v2, ss, dd)
+    flow = spn.Su2Flow(tab, freq)
+    flow.set_state(float(c), v2, ss, dd)
+    for npi in (1, 2):
+        for sm in (False, True):
+            flow.set_variant(npi, sm)
+            flow.compute_step()
+            g2, gss, gdd = flow.get_flow()
+            assert normwise(gss, rss) <= RHS_TOL, (npi, sm)
+            assert normwise(gdd, rdd) <= RHS_TOL, (npi, sm)
+    choice = flow.autotune(2)
+    assert choice["nodes_per_iteration"] in (1, 2) and choice["grid"] > 0
+    flow.compute_step()
+    _, gss, gdd = flow.get_flow()
+    assert normwise(gss, rss) <= RHS_TOL and normwise(gdd, rdd) <= RHS_TOL
+
+
 def test_rhs_small_mesh_late_cutoff(square_r3):
     """Small cutoff (below the smallest frequency) exercises the clamped interpolation and
     all three Katanin ranges."""
