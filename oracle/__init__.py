@@ -52,6 +52,7 @@ def _lib():
         lib.oracle_su2_euler_f32.argtypes = [f, f, C.c_longlong, fp, fp]
         lib.oracle_su2_euler_f32.restype = None
         lib.oracle_su2_flow_f32.argtypes = [dsc, fp, i, fp, fp, fp, fp, fp, i]
+        lib.oracle_su2_flow_f64.argtypes = [dsc, fp, i, dp, dp, dp, dp, dp, i]
         _LIB = lib
     return _LIB
 
@@ -138,14 +139,17 @@ class Oracle:
         assert fn(C.byref(self.desc), cutoff, _p(v2, ct), _p(ss, ct), _p(dd, ct), _p(cs, ct), _p(cd, ct)) == 0
         return cs, cd
 
-    def flow(self, cutoffs, v2, ss, dd, threads: int = 0):
-        """Whole flow; returns (n_measured, chi_s[n_cut, Nl], chi_d[n_cut, Nl], final state)."""
+    def flow(self, cutoffs, v2, ss, dd, threads: int = 0, fp64: bool = False):
+        """Whole flow; returns (n_measured, chi_s[n_cut, Nl], chi_d[n_cut, Nl], final state).
+        fp64=True runs every operation in double precision (the FP64 oracle)."""
         cut = np.ascontiguousarray(cutoffs, np.float32)
-        v2, ss, dd = (np.array(x, np.float32).reshape(-1) for x in (v2, ss, dd))
-        cs = np.zeros((len(cut), self.nl), np.float32)
-        cd = np.zeros((len(cut), self.nl), np.float32)
-        f = C.c_float
-        n = self.lib.oracle_su2_flow_f32(C.byref(self.desc), _p(cut, f), len(cut), _p(v2, f), _p(ss, f), _p(dd, f),
-                                         _p(cs, f), _p(cd, f), threads)
+        t = np.float64 if fp64 else np.float32
+        ct = C.c_double if fp64 else C.c_float
+        v2, ss, dd = (np.array(x, t).reshape(-1) for x in (v2, ss, dd))
+        cs = np.zeros((len(cut), self.nl), t)
+        cd = np.zeros((len(cut), self.nl), t)
+        fn = self.lib.oracle_su2_flow_f64 if fp64 else self.lib.oracle_su2_flow_f32
+        n = fn(C.byref(self.desc), _p(cut, C.c_float), len(cut), _p(v2, ct), _p(ss, ct), _p(dd, ct), _p(cs, ct),
+               _p(cd, ct), threads)
         assert n > 0
         return n, cs, cd, (v2, ss, dd)

@@ -719,4 +719,34 @@ int oracle_su2_flow_f32(const OracleDesc *d, const float *cutoffs, int n_cutoffs
     return k + 1;
 }
 
+// The same flow entirely in double precision (the FP64 oracle of the precision study): the
+// cutoff list is the float list of the task, every operation after that is FP64.
+int oracle_su2_flow_f64(const OracleDesc *d, const float *cutoffs, int n_cutoffs, double *v2, double *ss, double *dd,
+                        double *chi_s, double *chi_d, int nthreads) {
+    if (!d || n_cutoffs < 2) return -2;
+    const int N = d->n_freq, Nl = d->n_sites;
+    const long long size = (long long)N * N * (N + 1) / 2 * Nl;
+    std::vector<double> dv2(N), dss(size), ddd(size);
+    int k = 0;
+    double cutoff = cutoffs[0];
+    auto euler = [](double step, long long n, double *x, const double *dx) {
+        for (long long i = 0; i < n; ++i) x[i] += step * dx[i];
+    };
+    for (; k < n_cutoffs - 1; ++k) {
+        rhs_impl<double>(d, cutoff, v2, ss, dd, dv2.data(), dss.data(), ddd.data(), nthreads);
+        oracle_su2_correlation_f64(d, cutoff, v2, ss, dd, chi_s + (long long)k * Nl, chi_d + (long long)k * Nl);
+        bool nan = false;
+        for (int i = 0; i < N && !nan; ++i) nan = std::isnan(dv2[i]);
+        for (long long i = 0; i < size && !nan; ++i) nan = std::isnan(dss[i]) || std::isnan(ddd[i]);
+        if (nan) break;
+        const double next = cutoffs[k + 1];
+        euler(next - cutoff, N, v2, dv2.data());
+        euler(next - cutoff, size, dd, ddd.data());
+        euler(next - cutoff, size, ss, dss.data());
+        cutoff = next;
+    }
+    oracle_su2_correlation_f64(d, cutoff, v2, ss, dd, chi_s + (long long)k * Nl, chi_d + (long long)k * Nl);
+    return k + 1;
+}
+
 }  // extern "C"

@@ -38,6 +38,9 @@ struct FlowArgs {
     float *dss, *ddd;      // flow
     const float *v2;       // self-energy state
     float *dv2;            // self-energy flow
+    const double *v2d;     // FP64 self-energy state (used when fp64_sigma)
+    double *dv2d;          // FP64 self-energy flow
+    int fp64_sigma;
     const int *sites, *inv_sites, *ov_ptr, *ov_r1, *ov_r2, *range_rid, *range_inv;
     float *node_wp, *node_c;
     int *node_cnt;

@@ -67,9 +67,11 @@ __global__ void __launch_bounds__(128) su2_self_energy_kernel(FlowArgs a) {
                        double(value_none(pos, a.n, a.nl, a.ss, false, 0, 0, wml, wpl, 0.0f)));
         val += (double(value_none(pos, a.n, a.nl, a.dd, true, 0, 0, wpl, wml, 0.0f)) -
                 double(value_none(pos, a.n, a.nl, a.dd, true, 0, 0, wml, wpl, 0.0f)));
-        val /= (2.0 * kPiD * (double(L) + odd_interp(pos, a.n, a.v2, L)));
+        const double sig = a.fp64_sigma ? odd_interp(pos, a.n, a.v2d, L) : odd_interp(pos, a.n, a.v2, L);
+        val /= (2.0 * kPiD * (double(L) + sig));
         float out = float(val);
         a.dv2[i] = out;
+        if (a.fp64_sigma) a.dv2d[i] = val;
         if (isnan(out)) atomicOr(a.status, kStatusNaN);
     }
 }
@@ -98,11 +100,12 @@ __global__ void su2_node_table_kernel(FlowArgs a) {
             overflow = true;
         }
     };
-    auto sig = [&](float w) { return odd_interp(pos, n, a.v2, w); };
+    auto sig = [&](float w) { return a.fp64_sigma ? odd_interp(pos, n, a.v2d, w) : odd_interp(pos, n, a.v2, w); };
+    auto dsig = [&](float w) { return a.fp64_sigma ? odd_interp(pos, n, a.dv2d, w) : odd_interp(pos, n, a.dv2, w); };
     auto p = [&](float w1, float w2) { return 1.0 / ((double(w1) + sig(w1)) * (double(w2) + sig(w2))); };
     auto pk = [&](float w1, float w2) {
         double d1 = double(w1) + sig(w1);
-        return odd_interp(pos, n, a.dv2, w1) / (d1 * d1 * (double(w2) + sig(w2)));
+        return dsig(w1) / (d1 * d1 * (double(w2) + sig(w2)));
     };
     // conventional contribution (SU2FrgCore.cpp:351-371)
     put(L, p(L, L + x));
@@ -135,6 +138,16 @@ __global__ void su2_euler_kernel(float *__restrict__ x, const float *__restrict_
         x[i] = __fadd_rn(x[i], __fmul_rn(step, dx[i]));
 }
 
+// FP64 self-energy Euler step; keeps the FP32 mirror (what get_state returns) in sync.
+__global__ void su2_euler_f64_kernel(double *__restrict__ x, const double *__restrict__ dx, float *__restrict__ xf, int n,
+                                     float step) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double v = x[i] + double(step) * dx[i];
+        x[i] = v;
+        xf[i] = float(v);
+    }
+}
+
 // ------------------------------------------------------------------------------------
 // correlation measurement (nu = 0), SU2MeasurementCorrelation.cpp:77-177
 // ------------------------------------------------------------------------------------
@@ -142,11 +155,16 @@ struct CorrArgs {
     int n, nl, n_corr;
     float cutoff, spin;
     const float *freq, *ss, *dd, *v2;
+    const double *v2d;  // FP64 self-energy, read instead of v2 when not NULL
     const int *sites, *inv_sites, *corr_rid;
     double *partial;  // [max_nodes][2][nl]
     float *out;       // zz[n_corr], dd[n_corr], chi_s[nl], chi_d[nl]
     int wsite;
 };
+
+__device__ __forceinline__ double corr_sigma(const CorrArgs &a, const float *pos, float w) {
+    return a.v2d ? odd_interp(pos, a.n, a.v2d, w) : odd_interp(pos, a.n, a.v2, w);
+}
 
 // Loop-frequency nodes of the measurement's trapezoid rules at nu = 0 (outer and inner
 // integrals use the same ranges): (-inf, -cutoff] and [cutoff, inf).
@@ -192,7 +210,7 @@ __global__ void __launch_bounds__(128) su2_corr_inner_kernel(CorrArgs a) {
         isite[k] = valid[k] ? a.inv_sites[j] : 0;
     }
     const double S = a.spin;
-    auto sig = [&](float x) { return odd_interp(pos, a.n, a.v2, x); };
+    auto sig = [&](float x) { return corr_sigma(a, pos, x); };
     const double dw = double(w) + sig(w);
     double acc_s[SPT], acc_d[SPT];
     for (int k = 0; k < SPT; ++k) acc_s[k] = acc_d[k] = 0.0;
@@ -266,7 +284,7 @@ __global__ void su2_corr_final_kernel(CorrArgs a) {
             double ld = a.partial[(size_t(ia) * 2 + 1) * a.nl + j];
             if (j == 0) {
                 const float w = nwp[ia];
-                const double dw = double(w) + odd_interp(pos, a.n, a.v2, w);
+                const double dw = double(w) + corr_sigma(a, pos, w);
                 const double t1 = 1.0 / (dw * dw);
                 ls += S * t1 / (2.0 * kPiD);
                 ld += 2.0 * S * t1 / kPiD;
@@ -347,6 +365,7 @@ struct spn_su2 {
     int *sites = nullptr, *inv_sites = nullptr, *ov_ptr = nullptr, *ov_r1 = nullptr, *ov_r2 = nullptr;
     int *range_rid = nullptr, *range_inv = nullptr, *corr_rid = nullptr;
     double *corr_partial = nullptr;
+    double *v2d = nullptr, *dv2d = nullptr;  // FP64 self-energy (SPN_SU2_FP64_SELF_ENERGY)
     int *rpa_sched = nullptr, *rpa_count = nullptr, *rpa_slot_base = nullptr, *rpa_seg_ptr = nullptr;
     int rpa_lanes = 0, rpa_n_seg = 0, rpa_len = 0, rpa_in_smem = 0;
     int vertex_npi = 1;       // loop-frequency nodes per site-group iteration
@@ -372,6 +391,9 @@ struct spn_su2 {
         a.ddd = ddd;
         a.v2 = v2;
         a.dv2 = dv2;
+        a.v2d = v2d;
+        a.dv2d = dv2d;
+        a.fp64_sigma = (flags & SPN_SU2_FP64_SELF_ENERGY) ? 1 : 0;
         a.sites = sites;
         a.inv_sites = inv_sites;
         a.ov_ptr = ov_ptr;
@@ -409,7 +431,7 @@ struct spn_su2 {
         void *ptrs[] = {freq,      ss,        dd,        dss,       ddd,          v2,          dv2,
                         node_wp,   node_c,    corr_out,  node_cnt,  work_counter, status,      sites,
                         inv_sites, ov_ptr,    ov_r1,     ov_r2,     range_rid,    range_inv,   corr_rid,
-                        corr_partial, rpa_sched, rpa_count, rpa_slot_base, rpa_seg_ptr};
+                        corr_partial, rpa_sched, rpa_count, rpa_slot_base, rpa_seg_ptr, v2d, dv2d};
         for (void *p : ptrs)
             if (p) cudaFree(p);
         if (own_stream && stream) cudaStreamDestroy(stream);
@@ -613,6 +635,8 @@ extern "C" int spn_su2_create(const spn_su2_desc *d, spn_su2 **out) {
             h->ddd = dev_alloc<float>(vsz, "alloc dv4dd");
             h->v2 = dev_alloc<float>(h->n, "alloc v2");
             h->dv2 = dev_alloc<float>(h->n, "alloc dv2");
+            h->v2d = dev_alloc<double>(h->n, "alloc v2 (fp64)");
+            h->dv2d = dev_alloc<double>(h->n, "alloc dv2 (fp64)");
             h->node_wp = dev_alloc<float>(size_t(h->n) * h->max_nodes, "alloc node table");
             h->node_c = dev_alloc<float>(size_t(h->n) * h->max_nodes, "alloc node table");
             h->node_cnt = dev_alloc<int>(h->n, "alloc node counts");
@@ -643,6 +667,8 @@ extern "C" int spn_su2_create(const spn_su2_desc *d, spn_su2 **out) {
             cuda_check(cudaMemsetAsync(h->ddd, 0, vsz * sizeof(float), h->stream), "memset");
             cuda_check(cudaMemsetAsync(h->v2, 0, h->n * sizeof(float), h->stream), "memset");
             cuda_check(cudaMemsetAsync(h->dv2, 0, h->n * sizeof(float), h->stream), "memset");
+            cuda_check(cudaMemsetAsync(h->v2d, 0, h->n * sizeof(double), h->stream), "memset");
+            cuda_check(cudaMemsetAsync(h->dv2d, 0, h->n * sizeof(double), h->stream), "memset");
             cuda_check(cudaMemsetAsync(h->status, 0, sizeof(unsigned), h->stream), "memset");
             // balanced RPA schedule for the lanes of one node group
             const int lanes = spt_for(h->nl) == 1 ? wsite_for(h->nl) : 32;
@@ -717,6 +743,8 @@ extern "C" int spn_su2_set_state(spn_su2 *h, float cutoff, const float *v2, cons
         upload(h->v2, v2, h->n, h->stream);
         upload(h->ss, v4ss, vsz, h->stream);
         upload(h->dd, v4dd, vsz, h->stream);
+        std::vector<double> v2d(v2, v2 + h->n);  // the FP64 self-energy starts from the given values
+        upload(h->v2d, v2d.data(), h->n, h->stream);
         h->cutoff = cutoff;
         cuda_check(cudaStreamSynchronize(h->stream), "set_state sync");
     });
@@ -862,7 +890,10 @@ extern "C" int spn_su2_finalize_step(spn_su2 *h, float new_cutoff) {
         cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
         const float step = new_cutoff - h->cutoff;
         const long long vsz = h->fn * h->nl;
-        su2_euler_kernel<<<1, 64, 0, h->stream>>>(h->v2, h->dv2, h->n, step);
+        if (h->flags & SPN_SU2_FP64_SELF_ENERGY)
+            su2_euler_f64_kernel<<<1, 64, 0, h->stream>>>(h->v2d, h->dv2d, h->v2, h->n, step);
+        else
+            su2_euler_kernel<<<1, 64, 0, h->stream>>>(h->v2, h->dv2, h->n, step);
         const int grid = int(std::min<long long>((vsz / 4 + 255) / 256 + 1, 4096));
         su2_euler_kernel<<<grid, 256, 0, h->stream>>>(h->dd, h->ddd, vsz, step);
         su2_euler_kernel<<<grid, 256, 0, h->stream>>>(h->ss, h->dss, vsz, step);
@@ -884,6 +915,7 @@ void launch_correlation(spn_su2 *h) {
         a.ss = h->ss;
         a.dd = h->dd;
         a.v2 = h->v2;
+        a.v2d = (h->flags & SPN_SU2_FP64_SELF_ENERGY) ? h->v2d : nullptr;
         a.sites = h->sites;
         a.inv_sites = h->inv_sites;
         a.corr_rid = h->corr_rid;
@@ -1062,6 +1094,7 @@ extern "C" int spn_su2_correlation_noalloc(int n_freq, const float *freq, int n_
         a.ss = v4ss;
         a.dd = v4dd;
         a.v2 = v2;
+        a.v2d = nullptr;
         a.sites = sites_rid;
         a.inv_sites = inv_sites_rid;
         a.corr_rid = corr_rid;
