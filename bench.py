@@ -303,10 +303,11 @@ def main():
         flow.set_cutoff(float(cut[k]))
         flow.compute_step()
         flops_eval += flops_evaluated(tab, n, flow.node_counts())
-    if dist:
-        t = torch.tensor([total_ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    # replicas: every rank ran its own flow; units summed, slowest rank's time
+    from spinparser_gb300 import replicas
+
+    job = replicas.aggregate(len(schedule), total_ms * 1e-3)
+    total_ms = job.seconds * 1e3
 
     # end to end through the C ABI with pinned host buffers
     fn_nl = flow.fn * flow.nl
@@ -358,7 +359,7 @@ def main():
         if dist:
             dist.destroy_process_group()
         return
-    value = world * len(schedule) / (total_ms * 1e-3)
+    value = job.throughput
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": len(schedule),
         "warmup": args.warmup, "ms_per_step": total_ms / len(schedule), "higher_is_better": True, "scaling": "weak",
