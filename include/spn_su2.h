@@ -232,6 +232,65 @@ int spn_su2_set_profiling(spn_su2 *h, int enable);
  * and of the whole compute_step (self-energy + tables + vertex). */
 int spn_su2_get_profile(spn_su2 *h, double *vertex_ms, int *vertex_launches, double *step_ms, int *steps);
 
+/* ------------------------------------------------------------------------------------
+ * Files: checkpoints and observables in the reference's HDF5 layout.  Host only.
+ * ------------------------------------------------------------------------------------ */
+
+/* SU2EffectiveAction::writeCheckpoint (src/SU2/SU2EffectiveAction.hpp:79-147): group
+ * "checkpoint_<id>" with attribute "cutoff" and datasets cutoff[1], v2[n_v2], v4dd[n_v4],
+ * v4ss[n_v4].  append != 0 adds to an existing file (a new file otherwise); *checkpoint_id
+ * receives the new id, or -1 when the file already holds a checkpoint at this cutoff (nothing
+ * is written then). */
+int spn_su2_write_checkpoint(const char *path, int append, float cutoff, int n_v2, const float *v2, long long n_v4,
+                             const float *v4ss, const float *v4dd, int *checkpoint_id);
+
+/* SU2EffectiveAction::readCheckpoint (src/SU2/SU2EffectiveAction.hpp:149-200): reads group
+ * "checkpoint_<checkpoint_id>", or with checkpoint_id < 0 the checkpoint named after the
+ * index of the last group.  *found = 0 when that group or one of its datasets is missing.
+ * SPN_E_IO if the file cannot be read; SPN_E_ARGUMENT if its sizes differ from n_v2 / n_v4. */
+int spn_su2_read_checkpoint(const char *path, int checkpoint_id, float *cutoff, int n_v2, float *v2, long long n_v4,
+                            float *v4ss, float *v4dd, int *found);
+
+/* SU2MeasurementCorrelation::takeMeasurement's file output (src/SU2/SU2MeasurementCorrelation.cpp:179-355):
+ * adds zz and dd ([n_basis][n_range] of the lattice) as measurement groups of "SU2CorZZ" and
+ * "SU2CorDD" in the observable file, writing the "meta" group (lattice vectors, basis,
+ * sites) where it is missing.  *written = 0 when a measurement at this cutoff exists (it is
+ * kept and the new one discarded, as the reference does). */
+int spn_su2_write_correlation(const char *path, const spn_lattice *lat, float cutoff, const float *zz, const float *dd,
+                              int *written);
+
+/* ------------------------------------------------------------------------------------
+ * Task driver: SpinParser::run / runCore (src/SpinParser.cpp:53-210) for SU(2) tasks on
+ * one GPU.  Parses the task file (src/TaskFileParser.cpp), builds the lattice, writes the
+ * .ldf, runs the cutoff loop on the device with checkpoints, measurements, deferred
+ * measurements and the post-processing stage, and writes the calculation status back into
+ * the task file.  Output files sit beside the task file (.obs, .checkpoint, .data, .ldf).
+ * ------------------------------------------------------------------------------------ */
+typedef struct {
+    const char *resource_path; /* directory with the lattice / model XML files; NULL = the package's res/ */
+    int checkpoint_time;       /* seconds between checkpoints (--checkpointTime, default 3600) */
+    int force_restart;         /* --forceRestart */
+    int defer;                 /* --defer: archive the vertex for all measurements */
+    int debug_lattice;         /* --debugLattice: stop after the lattice (no GPU needed) */
+    int verbose;               /* -1 errors and warnings only, 0 progress, 1 debug (--verbose) */
+    int device;                /* CUDA device ordinal */
+    int flags;                 /* spn_su2_desc flags */
+    int autotune;              /* pick the vertex-flow variant by timing before the loop */
+} spn_run_options;
+
+typedef struct {
+    int status;            /* final calculation status: 0 new, 1 running, 2 postprocessing, 3 finished */
+    int steps;             /* flow steps computed (compute_step + finalize_step) */
+    int measurements;      /* correlation measurements evaluated on the device */
+    int diverged;          /* the flow stopped on a NaN */
+    double flow_seconds;   /* wall time of the cutoff loop */
+} spn_run_result;
+
+/* Fills o with the reference's defaults (checkpoint_time 3600, all switches off, device 0). */
+int spn_run_options_default(spn_run_options *o);
+/* Runs a task file; result may be NULL. */
+int spn_run_task(const char *task_path, const spn_run_options *o, spn_run_result *result);
+
 #ifdef __cplusplus
 }
 #endif

@@ -49,6 +49,30 @@ class Su2Desc(C.Structure):
     ]
 
 
+class RunOptions(C.Structure):
+    _fields_ = [
+        ("resource_path", C.c_char_p),
+        ("checkpoint_time", C.c_int),
+        ("force_restart", C.c_int),
+        ("defer", C.c_int),
+        ("debug_lattice", C.c_int),
+        ("verbose", C.c_int),
+        ("device", C.c_int),
+        ("flags", C.c_int),
+        ("autotune", C.c_int),
+    ]
+
+
+class RunResult(C.Structure):
+    _fields_ = [
+        ("status", C.c_int),
+        ("steps", C.c_int),
+        ("measurements", C.c_int),
+        ("diverged", C.c_int),
+        ("flow_seconds", C.c_double),
+    ]
+
+
 # name -> (restype, argtypes); every function declared in include/spn_su2.h
 SIGNATURES = {
     "spn_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
@@ -89,6 +113,13 @@ SIGNATURES = {
     "spn_su2_synchronize": (C.c_int, [C.c_void_p]),
     "spn_su2_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "spn_su2_get_profile": (C.c_int, [C.c_void_p, c_double_p, c_int_p, c_double_p, c_int_p]),
+    "spn_su2_write_checkpoint": (C.c_int, [C.c_char_p, C.c_int, C.c_float, C.c_int, c_float_p, C.c_longlong,
+                                           c_float_p, c_float_p, c_int_p]),
+    "spn_su2_read_checkpoint": (C.c_int, [C.c_char_p, C.c_int, c_float_p, C.c_int, c_float_p, C.c_longlong,
+                                          c_float_p, c_float_p, c_int_p]),
+    "spn_su2_write_correlation": (C.c_int, [C.c_char_p, C.c_void_p, C.c_float, c_float_p, c_float_p, c_int_p]),
+    "spn_run_options_default": (C.c_int, [C.POINTER(RunOptions)]),
+    "spn_run_task": (C.c_int, [C.c_char_p, C.POINTER(RunOptions), C.POINTER(RunResult)]),
 }
 
 

@@ -1,9 +1,13 @@
 // Host half of the C ABI (include/spn_su2.h): error reporting, lattice construction,
 // discretisations and the initial state.  None of these touch the GPU.
 #include "capi_common.hpp"
-#include "lattice.hpp"
+#include "lattice_handle.hpp"
+#include "log.hpp"
 #include "../../../include/spn_su2.h"
+#include <atomic>
 #include <cmath>
+#include <cstdio>
+#include <ctime>
 #include <cstring>
 #include <map>
 #include <string>
@@ -11,15 +15,24 @@
 namespace spn {
 namespace {
 thread_local std::string g_last_error;
+std::atomic<int> g_log_level{int(LogLevel::Info)};
 }
 void set_last_error(const std::string &msg) { g_last_error = msg; }
-}  // namespace spn
 
-struct spn_lattice {
-    spn::LatticeUnitCell uc;
-    spn::SpinModelUnitCell model;
-    spn::Lattice lat;
-};
+void set_log_level(LogLevel display) { g_log_level = int(display); }
+
+void log(LogLevel level, const std::string &msg) {
+    if (int(level) < g_log_level) return;
+    static const char *names[] = {"Debug", "Info", "Warning", "Error"};
+    std::time_t t = std::time(nullptr);
+    std::tm tm{};
+    localtime_r(&t, &tm);
+    char stamp[32];
+    std::strftime(stamp, sizeof(stamp), "%Y-%m-%d %H:%M:%S", &tm);
+    std::printf("[%s] %s: %s\n", stamp, names[int(level)], msg.c_str());
+    std::fflush(stdout);
+}
+}  // namespace spn
 
 extern "C" int spn_last_error(char *buf, size_t len) {
     const std::string &m = spn::g_last_error;

@@ -1,0 +1,377 @@
+// Task driver: SpinParser::run and SpinParser::runCore (src/SpinParser.cpp:53-210) with the
+// SU(2) flow resident on one GPU.
+//
+// The host side keeps the reference's control flow: parse the task file, build the lattice
+// (and always write the .ldf), create the core, then one of three stages depending on the
+// recorded calculation status --
+//   new / running:   [resume from the .checkpoint] -> cutoff loop {compute_step,
+//                    measurements, divergence check, Euler step, periodic checkpoint}
+//                    -> final measurement -> final checkpoint + status;
+//   postprocessing:  deferred measurements on every archived vertex of the .data file;
+//   finished:        nothing to do.
+// Measurements follow FrgCore::takeMeasurements (src/FrgCore.hpp:36-67): in the loop only the
+// non-deferred ones run, and with any deferred measurement (or --defer) the vertex of every
+// cutoff is appended to the .data file for the post-processing stage.
+//
+// All flow arithmetic runs on the device through the C ABI of this library (spn_su2_*); the
+// host only moves the state for checkpoints and writes files.  Observable files are kept in
+// memory and written whole at every checkpoint, at the end and at least every few seconds;
+// measurements after the last checkpoint are recomputed on resume (and duplicates
+// discarded), so the files after a resumed run equal those of an uninterrupted one.
+#include "capi_common.hpp"
+#include "error.hpp"
+#include "lattice_handle.hpp"
+#include "log.hpp"
+#include "su2_files.hpp"
+#include "task.hpp"
+#include "../../../include/spn_su2.h"
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <ctime>
+#include <dlfcn.h>
+#include <memory>
+#include <sstream>
+
+namespace spn {
+
+namespace {
+
+constexpr std::time_t kObsFlushSeconds = 10;
+
+void check(int rc) {
+    if (rc == 0) return;
+    char buf[2048];
+    spn_last_error(buf, sizeof(buf));
+    ErrorType t = (rc <= int(ErrorType::Argument) && rc >= int(ErrorType::Unsupported)) ? ErrorType(rc) : ErrorType::Internal;
+    throw Error(t, buf);
+}
+
+// The package's res/ directory: the library lives in <package>/_build/<machine>/.
+std::string default_resource_path() {
+    Dl_info info;
+    if (dladdr(reinterpret_cast<void *>(&spn_run_task), &info) && info.dli_fname) {
+        std::string p = info.dli_fname;
+        for (int i = 0; i < 3; ++i) {
+            size_t s = p.find_last_of('/');
+            if (s == std::string::npos) {
+                p.clear();
+                break;
+            }
+            p = p.substr(0, s);
+        }
+        if (!p.empty()) return p + "/res";
+    }
+    throw Error(ErrorType::Argument, "no resource path given and the library location is unknown");
+}
+
+std::string fixed6(double v) {
+    char b[64];
+    std::snprintf(b, sizeof(b), "%.6f", v);
+    return b;
+}
+
+struct FlowDeleter {
+    void operator()(spn_su2 *h) const { spn_su2_destroy(h); }
+};
+
+class Driver {
+public:
+    Driver(Task &task, const spn_run_options &o, spn_run_result &res) : task_(task), o_(o), res_(res) {}
+
+    void build(const std::string &resdir) {
+        lat_.reset(new spn_lattice);
+        lat_->uc = read_unit_cell(resdir, task_.lattice);
+        lat_->model = read_spin_model(resdir, task_.model, task_.model_options);
+        lat_->lat = build_lattice(lat_->uc, lat_->model, task_.range);
+        write_ldf(lat_->lat, lat_->uc, lat_->model, task_.files.ldf);
+        log(LogLevel::Info, "Generated lattice model.");
+
+        for (const MeasurementSpec &m : task_.measurements) {
+            if (m.name != "correlation") throw Error(ErrorType::Initialization, "Measurement: Unknown measurement type '" + m.name + "'.");
+            if (!m.options.empty())
+                throw Error(ErrorType::Initialization, "Measurement [correlation]: unknown option '" + m.options[0].first + "'.");
+            any_deferred_ = any_deferred_ || m.defer;
+        }
+        if (task_.symmetry == "XYZ" || task_.symmetry == "TRI")
+            throw Error(ErrorType::Unsupported, "Spin model identifier '" + task_.symmetry + "': only the SU2 core runs on the GPU in this build.");
+        if (task_.symmetry != "SU2") throw Error(ErrorType::Argument, "Spin model identifier '" + task_.symmetry + "' does not exist.");
+        // core options: model options that are not interaction parameters (src/TaskFileParser.cpp:310-317,
+        // src/SU2/SU2FrgCore.cpp:19-29)
+        for (const auto &kv : task_.model_options) {
+            if (lat_->model.parameters.count(kv.first)) continue;
+            if (kv.first == "spin") spin_ = float(parse_number(kv.second));
+            else if (kv.first == "normalization") normalization_ = float(parse_number(kv.second));
+            else throw Error(ErrorType::Initialization, "Unknown spin model option '" + kv.first + "'.");
+        }
+        if (std::isnan(normalization_)) normalization_ = 2.0f * spin_;
+        meta_ = make_obs_meta(lat_->lat);
+    }
+
+    void print_lattice() const {
+        const Lattice &L = lat_->lat;
+        log(LogLevel::Info, "Printing lattice debug information.");
+        log(LogLevel::Info, "\tNumber of basis sites per unit cell: " + std::to_string(L.basis.size()));
+        log(LogLevel::Info, "\tNumber of allocated sites: " + std::to_string(L.n_sites()) + " (" + std::to_string(L.n_sites() * sizeof(int)) + " bytes)");
+        log(LogLevel::Info, "\tNumber of sites within range of origin: " + std::to_string(L.range_ids[0].size()));
+        log(LogLevel::Info, "\tNumber of parametrized sites: " + std::to_string(L.size));
+        log(LogLevel::Info, "\tParametrization is as follows: ");
+        log(LogLevel::Info, "\t\tid: (a0, a1, a2, b)");
+        for (int i = 0; i < L.size; ++i) {
+            const LatticeSite &s = L.sites[i];
+            log(LogLevel::Info, "\t\t" + std::to_string(i) + ": (" + std::to_string(s.a0) + ", " + std::to_string(s.a1) + ", " +
+                                    std::to_string(s.a2) + ", " + std::to_string(s.b) + ")");
+        }
+    }
+
+    void create_core() {
+        spn_lattice_info info;
+        check(spn_lattice_get_info(lat_.get(), &info));
+        nl_ = info.n_sites;
+        n_corr_ = int64_t(info.n_basis) * info.n_range;
+        std::vector<int> srid(nl_), irid(nl_), optr(nl_ + 1), o1(info.n_overlap), o2(info.n_overlap), rr(info.n_range),
+            ri(info.n_range), cr(n_corr_);
+        check(spn_lattice_get_tables(lat_.get(), srid.data(), irid.data(), optr.data(), o1.data(), o2.data(), rr.data(),
+                                     ri.data(), cr.data(), nullptr, nullptr, nullptr));
+        const std::vector<float> &freq = task_.frequencies;
+        spn_su2_desc d{};
+        d.n_freq = int(freq.size());
+        d.freq = freq.data();
+        d.n_sites = nl_;
+        d.sites_rid = srid.data();
+        d.inv_sites_rid = irid.data();
+        d.overlap_ptr = optr.data();
+        d.overlap_rid1 = o1.data();
+        d.overlap_rid2 = o2.data();
+        d.n_range = info.n_range;
+        d.range_rid = rr.data();
+        d.range_inv_rid = ri.data();
+        d.n_corr = int(n_corr_);
+        d.corr_rid = cr.data();
+        d.spin_length = spin_;
+        d.device = o_.device;
+        d.flags = o_.flags;
+        spn_su2 *h = nullptr;
+        check(spn_su2_create(&d, &h));
+        flow_.reset(h);
+        int nf = 0, ns = 0;
+        long long nt = 0;
+        check(spn_su2_get_sizes(h, &nf, &ns, &nt));
+        n_v2_ = nf;
+        n_v4_ = int64_t(nt) * ns;
+        v2_.resize(n_v2_);
+        ss_.resize(n_v4_);
+        dd_.resize(n_v4_);
+        zz_.resize(n_corr_);
+        cdd_.resize(n_corr_);
+        // SU2EffectiveAction at the first cutoff (src/SU2/SU2EffectiveAction.hpp:38-60)
+        check(spn_su2_initial_state(lat_.get(), nf, normalization_, v2_.data(), ss_.data(), dd_.data()));
+        set_state(task_.cutoffs.front());
+        log(LogLevel::Info, "Generated FRG core with identifier SU2.");
+    }
+
+    void run() {
+        ComputationStatus cs = task_.status;
+        const std::vector<float> &cut = task_.cutoffs;
+        if (cs.status == CalcStatus::New || cs.status == CalcStatus::Running) {
+            size_t k = 0;
+            if (cs.status == CalcStatus::Running) {
+                float c = 0;
+                if (!read_checkpoint(task_.files.checkpoint, -1, c, v2_.data(), n_v2_, ss_.data(), dd_.data(), n_v4_))
+                    throw Error(ErrorType::IO, "Could not read checkpoint from [" + task_.files.checkpoint + "].");
+                set_state(c);
+                k = cut.size();
+                for (size_t i = 0; i < cut.size(); ++i)
+                    if (cut[i] == c) {
+                        k = i;
+                        break;
+                    }
+                if (k == cut.size())
+                    throw Error(ErrorType::Initialization, "Checkpoint cutoff " + fixed6(c) + " is not a value of the cutoff discretization.");
+                log(LogLevel::Info, "Resuming calculation from checkpoint at cutoff " + fixed6(c) + ".");
+            }
+            if (cs.status == CalcStatus::New) cs.start_time = std::time(nullptr);
+            cs.checkpoint_time = std::time(nullptr);
+            if (o_.autotune && k + 1 < cut.size()) autotune(cut[k + (cut.size() - k) / 2]);
+
+            auto t0 = std::chrono::steady_clock::now();
+            while (k + 1 < cut.size()) {
+                log(LogLevel::Debug, "Begin computation of flow.");
+                check(spn_su2_compute_step(flow_.get()));
+                log(LogLevel::Debug, "Begin computation of measurements.");
+                take_measurements(false);
+                int div = 0;
+                check(spn_su2_is_diverged(flow_.get(), &div));
+                if (div) {
+                    log(LogLevel::Info, "Vertex has diverged. Stopping calculation.");
+                    res_.diverged = 1;
+                    break;
+                }
+                ++k;
+                check(spn_su2_finalize_step(flow_.get(), cut[k]));
+                cutoff_ = cut[k];
+                ++res_.steps;
+                log(LogLevel::Info, "Current cutoff is at " + fixed6(cutoff_));
+                std::time_t now = std::time(nullptr);
+                if (now - cs.checkpoint_time > o_.checkpoint_time) {
+                    cs.checkpoint_time = now;
+                    cs.status = CalcStatus::Running;
+                    write_checkpoint_and_status(cs);
+                }
+                maybe_flush_obs();
+            }
+            take_measurements(false);
+            check(spn_su2_synchronize(flow_.get()));
+            res_.flow_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+
+            if (o_.defer || any_deferred_) {
+                cs.status = CalcStatus::Postprocessing;
+            } else {
+                cs.end_time = std::time(nullptr);
+                cs.status = CalcStatus::Finished;
+            }
+            cs.checkpoint_time = std::time(nullptr);
+            write_checkpoint_and_status(cs);
+        } else if (cs.status == CalcStatus::Postprocessing) {
+            log(LogLevel::Info, "Entering post-processing stage.");
+            int n = 0;
+            float c = 0;
+            while (read_checkpoint(task_.files.data, n++, c, v2_.data(), n_v2_, ss_.data(), dd_.data(), n_v4_)) {
+                set_state(c);
+                log(LogLevel::Info, "Post-processing measurements at cutoff " + std::to_string(c));
+                take_measurements(true);
+            }
+            obs_.flush();
+            cs.end_time = std::time(nullptr);
+            cs.status = CalcStatus::Finished;
+            write_task(task_, cs);
+            log(LogLevel::Info, "Post-processing done.");
+        } else {
+            log(LogLevel::Info, "Nothing left to do. Task had been finished already.");
+        }
+        obs_.flush();
+        res_.status = int(cs.status);
+    }
+
+private:
+    void set_state(float c) {
+        check(spn_su2_set_state(flow_.get(), c, v2_.data(), ss_.data(), dd_.data()));
+        cutoff_ = c;
+    }
+
+    void autotune(float at) {
+        int npi = 0, smem = 0, grid = 0;
+        check(spn_su2_set_cutoff(flow_.get(), at));
+        check(spn_su2_autotune(flow_.get(), 3, &npi, &smem, &grid));
+        check(spn_su2_set_cutoff(flow_.get(), cutoff_));
+        log(LogLevel::Debug, "Vertex flow variant: " + std::to_string(npi) + " node(s) per iteration, schedule in " +
+                                 (smem ? "shared" : "global") + " memory, grid " + std::to_string(grid));
+    }
+
+    void take_measurements(bool postprocessing) {
+        for (const MeasurementSpec &m : task_.measurements) {
+            if (!(cutoff_ <= m.max_cutoff && cutoff_ >= m.min_cutoff)) continue;
+            bool deferred = o_.defer || m.defer;
+            if (deferred != postprocessing) continue;
+            if (measured_cutoff_ != cutoff_) {
+                check(spn_su2_measure_correlation(flow_.get(), zz_.data(), cdd_.data(), nullptr, nullptr));
+                measured_cutoff_ = cutoff_;
+                ++res_.measurements;
+            }
+            obs_.add(m.output, "SU2CorZZ", meta_, cutoff_, zz_.data());
+            obs_.add(m.output, "SU2CorDD", meta_, cutoff_, cdd_.data());
+        }
+        if (!postprocessing && (o_.defer || any_deferred_)) {
+            float c = 0;
+            check(spn_su2_get_state(flow_.get(), &c, v2_.data(), ss_.data(), dd_.data()));
+            write_checkpoint(task_.files.data, true, c, v2_.data(), n_v2_, ss_.data(), dd_.data(), n_v4_);
+        }
+    }
+
+    // SpinParser::writeCheckpoint (src/SpinParser.cpp:212-220)
+    void write_checkpoint_and_status(const ComputationStatus &cs) {
+        log(LogLevel::Info, "Writing checkpoint.");
+        float c = 0;
+        check(spn_su2_get_state(flow_.get(), &c, v2_.data(), ss_.data(), dd_.data()));
+        write_checkpoint(task_.files.checkpoint, false, c, v2_.data(), n_v2_, ss_.data(), dd_.data(), n_v4_);
+        obs_.flush();
+        last_flush_ = std::time(nullptr);
+        write_task(task_, cs);
+    }
+
+    void maybe_flush_obs() {
+        std::time_t now = std::time(nullptr);
+        if (now - last_flush_ >= kObsFlushSeconds) {
+            obs_.flush();
+            last_flush_ = now;
+        }
+    }
+
+    Task &task_;
+    const spn_run_options &o_;
+    spn_run_result &res_;
+    std::unique_ptr<spn_lattice> lat_;
+    std::unique_ptr<spn_su2, FlowDeleter> flow_;
+    ObsMeta meta_;
+    ObsStore obs_;
+    float spin_ = 0.5f, normalization_ = NAN;
+    bool any_deferred_ = false;
+    int nl_ = 0;
+    int64_t n_corr_ = 0, n_v2_ = 0, n_v4_ = 0;
+    std::vector<float> v2_, ss_, dd_, zz_, cdd_;
+    float cutoff_ = 0, measured_cutoff_ = -1.0f;
+    std::time_t last_flush_ = std::time(nullptr);
+};
+
+}  // namespace
+
+void run_task(const std::string &task_path, const spn_run_options &o, spn_run_result &res) {
+    set_log_level(o.verbose < 0 ? LogLevel::Warning : (o.verbose > 0 ? LogLevel::Debug : LogLevel::Info));
+    const std::string resdir = o.resource_path ? std::string(o.resource_path) : default_resource_path();
+    Task task = parse_task(task_path, o.force_restart != 0);
+    log(LogLevel::Info, "Task file [" + task_path + "]: " + std::to_string(task.frequencies.size()) + " frequencies, " +
+                            std::to_string(task.cutoffs.size()) + " cutoff values.");
+    Driver drv(task, o, res);
+    drv.build(resdir);
+    res.status = int(task.status.status);
+    if (o.debug_lattice) {
+        drv.print_lattice();
+        log(LogLevel::Info, "Lattice debug output complete. Shutting down.");
+        return;
+    }
+    // a finished task needs no device: the reference builds its core anyway, then does nothing
+    if (task.status.status != CalcStatus::Finished) drv.create_core();
+    log(LogLevel::Info, "Launching FRG numerics core");
+    auto t0 = std::chrono::steady_clock::now();
+    drv.run();
+    log(LogLevel::Info, "Shutting down core. Computation took " +
+                            fixed6(std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count()) + " seconds. ");
+}
+
+}  // namespace spn
+
+extern "C" int spn_run_options_default(spn_run_options *o) {
+    return spn::guarded([&] {
+        if (!o) throw spn::Error(spn::ErrorType::Argument, "spn_run_options_default: null argument");
+        *o = spn_run_options{};
+        o->checkpoint_time = 3600;
+    });
+}
+
+extern "C" int spn_run_task(const char *task_path, const spn_run_options *o, spn_run_result *result) {
+    return spn::guarded([&] {
+        if (!task_path) throw spn::Error(spn::ErrorType::Argument, "spn_run_task: null task path");
+        spn_run_options opts;
+        if (o) opts = *o;
+        else spn_run_options_default(&opts);
+        spn_run_result r{};
+        try {
+            spn::run_task(task_path, opts, r);
+        } catch (const spn::Error &e) {
+            spn::log(spn::LogLevel::Error, std::string("Caught exception: ") + e.what());
+            if (result) *result = r;
+            throw;
+        }
+        if (result) *result = r;
+    });
+}

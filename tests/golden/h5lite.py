@@ -244,3 +244,90 @@ def read_correlations(path: str, group: str):
     cut = np.array([float(g[n].attrs["cutoff"].reshape(-1)[0]) for n in names], np.float32)
     data = np.stack([g[n + "/data"].read() for n in names])
     return cut, data
+
+
+def walk(path: str) -> dict:
+    """Every object of a file: {"/a/b": {"kind": "group"|"dataset", "attrs": {...},
+    "data": array (datasets only)}}."""
+    out = {}
+
+    def rec(node: Node, p: str):
+        entry = {"kind": "group" if node.is_group else "dataset",
+                 "attrs": {k: np.array(v) for k, v in node.attrs.items()}}
+        if node.is_group:
+            out[p] = entry
+            for k in node.keys():
+                rec(node[k], p.rstrip("/") + "/" + k)
+        else:
+            entry["data"] = node.read()
+            out[p] = entry
+
+    rec(open_file(path), "/")
+    return out
+
+
+def skeleton(path: str) -> list:
+    """Structure without values: [path, kind, sorted attribute names, shape] per object."""
+    return [[p, e["kind"], sorted(e["attrs"]), list(e["data"].shape) if "data" in e else None]
+            for p, e in sorted(walk(path).items())]
+
+
+def compare(path_a: str, path_b: str, tolerance: float = 1e-5) -> None:
+    """Recursive comparison of two files with the rules of the reference's test evaluator
+    (test/scripted/assets/test_eval.py: same members and attributes, max abs deviation below
+    the tolerance); raises AssertionError on the first difference."""
+    a, b = walk(path_a), walk(path_b)
+    assert sorted(a) == sorted(b), f"members differ: {sorted(set(a) ^ set(b))[:10]}"
+    for p in a:
+        ea, eb = a[p], b[p]
+        assert ea["kind"] == eb["kind"], p
+        assert sorted(ea["attrs"]) == sorted(eb["attrs"]), f"attributes differ in {p}"
+        for k in ea["attrs"]:
+            eps = float(np.max(np.abs(ea["attrs"][k] - eb["attrs"][k])))
+            assert eps < tolerance, f"deviation in attribute {p}/{k}: {eps}"
+        if "data" in ea:
+            assert ea["data"].shape == eb["data"].shape, p
+            eps = float(np.max(np.abs(ea["data"] - eb["data"]))) if ea["data"].size else 0.0
+            assert eps < tolerance, f"deviation in dataset {p}: {eps}"
+
+
+def layout_fingerprint(path: str) -> dict:
+    """Encoding choices of a file, independent of its values: superblock versions and B-tree
+    K values, and per object kind the set of header messages with the bytes that encode
+    datatypes, fill values, layout classes and dataspace / attribute headers.  Continuation
+    and NIL messages (how a writer grew a header) are left out."""
+    with open(path, "rb") as f:
+        r = _Reader(f.read())
+    kinds: dict[str, set] = {}
+
+    def key(mtype, body, size):
+        raw = r.b[body:body + size]
+        if mtype in (0x03, 0x05):
+            return raw.hex()
+        if mtype == 0x08:
+            return raw[:2].hex()
+        if mtype == 0x01:
+            return raw[:3].hex()
+        if mtype == 0x0C:
+            nlen = r.u(body + 2, 2)
+            tlen = r.u(body + 4, 2)
+            p = body + 8 + ((nlen + 7) & ~7)
+            return raw[:2].hex() + ":" + r.b[p:p + tlen].hex()
+        if mtype == 0x12:
+            return raw[:1].hex()
+        return ""
+
+    def rec(addr):
+        msgs = [(t, key(t, b, s)) for t, b, s in r.messages(addr) if t not in (0x00, 0x10)]
+        info = r.node(addr)
+        if "group" in info:
+            kind = "group"
+        else:
+            kind = "dataset_" + ("array" if info["dtype"].shape else "scalar")
+        kinds.setdefault(kind, set()).update(f"{t:#06x}:{k}" for t, k in msgs)
+        if "group" in info:
+            for _, child in r.group_children(*info["group"]):
+                rec(child)
+
+    rec(r.root["header"])
+    return {"superblock": r.b[8:24].hex(), "objects": {k: sorted(v) for k, v in sorted(kinds.items())}}

@@ -12,6 +12,10 @@ Outputs (committed, so the tests need no reference tree at run time):
                           factory from the reference's res/ unit cell and model
   python_obs_honeycomb.json  the numeric expectations of test/scripted/assets/test_python_obs.py
                           (honeycomb r=3 SU(2) run of test_pythonObs.sh) and the task parameters
+  reference1_layout.json  member structure and HDF5 encoding fingerprint of test_reference1.ref
+  res_hyperkagome/        the hyperkagome unit cell and Heisenberg model of the reference's
+                          res/ files (the input of test_reference1), so that the task-file
+                          driver can run that task end to end
 """
 from __future__ import annotations
 
@@ -62,6 +66,30 @@ def lattice_kats(src: str) -> dict:
     return out
 
 
+def extract_resource(ref_root: str, kind: str, tag: str, name: str) -> str:
+    """The <tag name="name">...</tag> element of res/<kind>.xml, verbatim."""
+    src = open(os.path.join(ref_root, "res", kind + ".xml")).read()
+    m = re.search(r'<%s name="%s">.*?</%s>' % (tag, re.escape(name), tag), src, re.S)
+    return m.group(0)
+
+
+def write_hyperkagome_resources(ref_root: str) -> None:
+    out = os.path.join(HERE, "res_hyperkagome")
+    os.makedirs(out, exist_ok=True)
+    head = '<?xml version="1.0" encoding="utf-8"?>\n'
+    with open(os.path.join(out, "lattices.xml"), "w") as f:
+        f.write(head + extract_resource(ref_root, "lattices", "unitcell", "hyperkagome") + "\n")
+    with open(os.path.join(out, "models.xml"), "w") as f:
+        f.write(head + extract_resource(ref_root, "models", "model", "hyperkagome-heisenberg") + "\n")
+
+
+def write_reference1_layout(ref: str) -> None:
+    """Structure (members, attributes, shapes) and encoding fingerprint of the libhdf5-written
+    test_reference1.ref, for checking the package's .obs writer without the file itself."""
+    with open(os.path.join(HERE, "reference1_layout.json"), "w") as f:
+        json.dump({"fingerprint": h5lite.layout_fingerprint(ref), "skeleton": h5lite.skeleton(ref)}, f, indent=0)
+
+
 def main(ref_root: str) -> None:
     import spinparser_gb300 as spn
 
@@ -86,6 +114,8 @@ def main(ref_root: str) -> None:
     lat = spn.Lattice(p1["lattice"], p1["range"], p1["model"], {"j": str(p1["j"])},
                       resource_dir=os.path.join(ref_root, "res"))
     lat.tables().to_npz(os.path.join(HERE, "hyperkagome_r3_tables.npz"))
+    write_hyperkagome_resources(ref_root)
+    write_reference1_layout(ref)
 
     # --- test_pythonObs: honeycomb expectations ---
     p2 = task_parameters(open(os.path.join(scripted, "test_pythonObs.sh")).read())

@@ -1,0 +1,163 @@
+"""Task files run end to end on the GPU through the driver (SpinParser::run), with the
+reference's scripted tests as the model (test/scripted/test_*.sh):
+
+  * test_reference1 / test_referenceFail: the hyperkagome task reproduces the golden .obs
+    of the reference (structure exact, values within the evaluator's 1e-5), and J = -1 does not;
+  * test_pythonObs: the honeycomb task's .obs answers the reference's obs.py queries;
+  * test_checkpoint: a calculation stopped at a larger cutoff and resumed from its checkpoint
+    with an extended cutoff list writes the same .obs as an uninterrupted run;
+  * test_defer: deferred measurements (method="defer" or --defer), evaluated in the
+    post-processing stage from the .data archive, write the same .obs as direct ones.
+"""
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+from spinparser_gb300 import task
+from taskfiles import exponential_cutoffs, manual_frequencies, write
+
+import h5lite
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+REF_RES = os.path.join(GOLDEN, "res_hyperkagome")
+HONEYCOMB = dict(lattice="honeycomb", rng=3, model="honeycomb-heisenberg")
+
+
+def reference1_task(tmp_path, j="1.0", name="r1.xml"):
+    g = np.load(os.path.join(GOLDEN, "reference1_su2.npz"))
+    cmax, cmin, step = (float(x) for x in g["cutoff_spec"])
+    return write(tmp_path, name, lattice="hyperkagome", rng=3, model="hyperkagome-heisenberg", params=f"<j>{j}</j>",
+                 freq=manual_frequencies(), cutoff=exponential_cutoffs(f"{cmax:g}", f"{cmin:g}", f"{step:g}")), g
+
+
+def status_of(task_path):
+    m = re.search(r'status="(\w+)"', open(task_path).read())
+    return m.group(1) if m else None
+
+
+def test_reference1_task_reproduces_golden_obs(tmp_path):
+    p, g = reference1_task(tmp_path)
+    s = task.run_task(p, resource_path=REF_RES, verbose=-1)
+    assert s.status == "finished" and not s.diverged and s.steps == len(g["cutoffs"]) - 1
+    assert status_of(p) == "finished"
+    obs = str(tmp_path / "r1.obs")
+    layout = json.load(open(os.path.join(GOLDEN, "reference1_layout.json")))
+    assert h5lite.skeleton(obs) == layout["skeleton"]
+    assert h5lite.layout_fingerprint(obs) == layout["fingerprint"]
+    for group, key in (("SU2CorZZ", "zz"), ("SU2CorDD", "dd")):
+        cut, data = h5lite.read_correlations(obs, group)
+        assert np.array_equal(cut, g["cutoffs"])
+        assert float(np.abs(data - g[key]).max()) < 1e-5, group
+        meta = h5lite.open_file(obs)[group + "/meta"]
+        assert float(np.abs(meta["sites"].read() - g["sites"]).max()) < 1e-5
+        assert float(np.abs(meta["basis"].read() - g["basis"]).max()) < 1e-5
+        assert float(np.abs(meta["latticeVectors"].read() - g["lattice_vectors"]).max()) < 1e-5
+    # a finished task has nothing left to do
+    assert task.run_task(p, resource_path=REF_RES, verbose=-1).steps == 0
+
+
+def test_reference_fail_task_differs_from_golden(tmp_path):
+    p, g = reference1_task(tmp_path, j="-1.0")
+    task.run_task(p, resource_path=REF_RES, verbose=-1)
+    cut, zz = h5lite.read_correlations(str(tmp_path / "r1.obs"), "SU2CorZZ")
+    n = min(len(cut), len(g["cutoffs"]))
+    assert float(np.abs(zz[:n] - g["zz"][:n]).max()) > 1e-5
+
+
+def test_python_obs_task(tmp_path):
+    """test_pythonObs.sh: honeycomb r3 through the driver; the .obs answers obs.py's queries."""
+    import spinparser_gb300 as spn
+    from obs_queries import evaluate_query
+
+    spec = json.load(open(os.path.join(GOLDEN, "python_obs_honeycomb.json")))
+    t = spec["task"]
+    p = write(tmp_path, "po.xml", lattice=t["lattice"], rng=t["range"], model=t["model"], params=f"<j>{t['j']}</j>",
+              freq=manual_frequencies(t["frequencies"]),
+              cutoff=exponential_cutoffs(t["cutoff_max"], t["cutoff_min"], t["cutoff_step"]))
+    task.run_task(p, verbose=-1)
+    cut, zz = h5lite.read_correlations(str(tmp_path / "po.obs"), "SU2CorZZ")
+    tab = spn.Lattice(t["lattice"], t["range"], t["model"], {"j": str(t["j"])}).tables()
+    for q in spec["queries"]:
+        got = evaluate_query(q, cut, zz, tab)
+        atol = 1e-16
+        if q["what"] == "structure_factor":
+            atol = 1e-5 * float(np.max(evaluate_query(q, cut, np.abs(zz), tab)))
+        assert np.isclose(got, np.array(q["expect"]), rtol=1e-5, atol=atol).all(), q["what"]
+
+
+def test_checkpoint_resume_equals_uninterrupted_run(tmp_path):
+    """test_checkpoint.sh: run to cutoff 0.5, then resume (status running) down to 0.3."""
+    full = write(tmp_path, "full.xml", cutoff=exponential_cutoffs(10, 0.3, 0.9), freq=manual_frequencies(), **HONEYCOMB)
+    part = write(tmp_path, "part.xml", cutoff=exponential_cutoffs(10, 0.5, 0.9), freq=manual_frequencies(), **HONEYCOMB)
+    task.run_task(full, force_restart=True, verbose=-1)
+    first = task.run_task(part, force_restart=True, verbose=-1)
+    assert first.status == "finished"
+    # rewrite the task with the longer cutoff list and a "running" calculation log
+    write(tmp_path, "part.xml", cutoff=exponential_cutoffs(10, 0.3, 0.9), freq=manual_frequencies(), **HONEYCOMB,
+          extra='<calculation status="running" startTime="1970-Jan-01 00:00:00" checkpointTime="1970-Jan-01 00:00:00" />')
+    second = task.run_task(part, verbose=-1)
+    assert second.status == "finished" and 0 < second.steps < first.steps
+    assert status_of(part) == "finished"
+    a, b = str(tmp_path / "full.obs"), str(tmp_path / "part.obs")
+    h5lite.compare(a, b, tolerance=1e-5)
+    # the device arithmetic is deterministic: the resumed run is bit-identical
+    for group in ("SU2CorZZ", "SU2CorDD"):
+        ca, da = h5lite.read_correlations(a, group)
+        cb, db = h5lite.read_correlations(b, group)
+        assert np.array_equal(ca, cb) and np.array_equal(da, db)
+    # the final checkpoint holds the state at the last cutoff
+    ck = h5lite.open_file(str(tmp_path / "part.checkpoint"))
+    assert ck.keys() == ["checkpoint_0"]
+    cut = np.float32(10.0)
+    while np.float32(cut * np.float32(0.9)) > np.float32(0.3):
+        cut = np.float32(cut * np.float32(0.9))
+    assert float(ck["checkpoint_0"].attrs["cutoff"][0]) == float(cut)
+
+
+def test_periodic_checkpoints_keep_status_running(tmp_path):
+    """--checkpointTime 0 writes a checkpoint (and a 'running' status) whenever a second
+    has passed; the end of the run records 'finished' and the final state."""
+    p = write(tmp_path, "pc.xml", cutoff=exponential_cutoffs(10, 0.3, 0.9), freq=manual_frequencies(), **HONEYCOMB)
+    s = task.run_task(p, checkpoint_time=0, verbose=-1)
+    assert s.status == "finished" and status_of(p) == "finished"
+    calc = re.search(r"<calculation[^>]*>", open(p).read()).group(0)
+    assert all(k in calc for k in ("startTime=", "checkpointTime=", "endTime="))
+
+
+@pytest.mark.parametrize("how", ["method", "option"])
+def test_deferred_measurements_equal_direct_ones(tmp_path, how):
+    """test_defer.sh: deferred measurements archive the vertex at every cutoff (.data) and
+    evaluate it in a second, post-processing run."""
+    direct = write(tmp_path, "nd.xml", freq=manual_frequencies(), **HONEYCOMB)
+    meas = '<measurements><measurement name="correlation" method="defer" /></measurements>'
+    deferred = write(tmp_path, "d.xml", freq=manual_frequencies(), **HONEYCOMB,
+                     measurements=meas if how == "method" else
+                     '<measurements><measurement name="correlation" /></measurements>')
+    task.run_task(direct, force_restart=True, verbose=-1)
+    s1 = task.run_task(deferred, force_restart=True, defer=(how == "option"), verbose=-1)
+    assert s1.status == "postprocessing" and s1.measurements == 0
+    assert status_of(deferred) == "postprocessing"
+    assert not os.path.exists(str(tmp_path / "d.obs"))
+    archive = h5lite.open_file(str(tmp_path / "d.data"))
+    assert len(archive.keys()) == s1.steps + 1
+    s2 = task.run_task(deferred, defer=(how == "option"), verbose=-1)
+    assert s2.status == "finished" and s2.steps == 0 and s2.measurements == s1.steps + 1
+    assert status_of(deferred) == "finished"
+    h5lite.compare(str(tmp_path / "nd.obs"), str(tmp_path / "d.obs"), tolerance=1e-5)
+    for group in ("SU2CorZZ", "SU2CorDD"):
+        ca, da = h5lite.read_correlations(str(tmp_path / "nd.obs"), group)
+        cb, db = h5lite.read_correlations(str(tmp_path / "d.obs"), group)
+        assert np.array_equal(ca, cb) and np.array_equal(da, db)
+
+
+def test_measurement_cutoff_window_and_fp64_self_energy(tmp_path):
+    meas = '<measurements><measurement name="correlation" minCutoff="1.0" maxCutoff="5.0" /></measurements>'
+    p = write(tmp_path, "w.xml", freq=manual_frequencies(), measurements=meas, **HONEYCOMB)
+    task.run_task(p, verbose=-1, fp64_self_energy=True)
+    cut, _ = h5lite.read_correlations(str(tmp_path / "w.obs"), "SU2CorZZ")
+    assert len(cut) > 0 and cut.max() <= 5.0 and cut.min() >= 1.0
