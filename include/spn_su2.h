@@ -233,6 +233,54 @@ int spn_su2_set_profiling(spn_su2 *h, int enable);
 int spn_su2_get_profile(spn_su2 *h, double *vertex_ms, int *vertex_launches, double *step_ms, int *steps);
 
 /* ------------------------------------------------------------------------------------
+ * Batches: many flows on one GPU advanced together.  No reference counterpart (the
+ * reference runs one flow per process); each flow follows SpinParser::runCore's cycle
+ * (compute, measure, divergence check, Euler step; final measurement at the last cutoff).
+ * A step launches every kernel once for all flows -- the vertex flow as one persistent launch
+ * over the ragged list of all flows' frequency triples -- and, by default, replays the step
+ * as a CUDA graph while the set of flows and their phases are unchanged.  Flows may be added
+ * and removed between steps (continuous batching); each flow's results are bit-identical to
+ * the same flow run alone with spn_su2_* and the same vertex-flow variant.
+ * ------------------------------------------------------------------------------------ */
+typedef struct spn_batch spn_batch;
+
+#define SPN_PHASE_FLOWING 0 /* computing its flow */
+#define SPN_PHASE_FINAL 1   /* at the last cutoff, final measurement pending */
+#define SPN_PHASE_DONE 2    /* finished (see flags) */
+#define SPN_FLOW_DIVERGED 0x1
+#define SPN_FLOW_NODE_OVERFLOW 0x2
+
+int spn_batch_create(int device, spn_batch **out);
+int spn_batch_destroy(spn_batch *b);
+/* Vertex-flow variant of the batch (npi = 1 or 2) and whether steps are replayed as graphs. */
+int spn_batch_set_variant(spn_batch *b, int npi, int use_graph);
+/* Device memory a flow takes in a batch (state, flow, tables, measurement history): the
+ * admission measure of a serving loop. */
+int spn_batch_footprint(const spn_su2_desc *desc, int n_cutoffs, long long *bytes);
+/* Admits a flow with its cutoff list (descending) and initial state at cutoffs[0]; returns its
+ * id.  desc->device must be the batch's device. */
+int spn_batch_add(spn_batch *b, const spn_su2_desc *desc, int n_cutoffs, const float *cutoffs, const float *v2,
+                  const float *v4ss, const float *v4dd, int *flow_id);
+/* Advances every unfinished flow by one step (asynchronous); *n_active receives the number of
+ * flows not yet done as far as the host knows (divergence is learnt one step later). */
+int spn_batch_step(spn_batch *b, int *n_active);
+/* Waits for all queued steps and refreshes the host's view of every flow. */
+int spn_batch_synchronize(spn_batch *b);
+/* Phase, cutoff index and SPN_FLOW_* flags of a flow as the host last saw them. */
+int spn_batch_poll(spn_batch *b, int flow_id, int *phase, int *step, int *flags);
+/* Measurements recorded so far (waits for queued work): *n_measured rows of cutoffs[k],
+ * zz/dd[k][n_corr] and chi_zz/chi_dd[k][Nl], the outputs of spn_su2_measure_correlation at
+ * every cutoff the flow reached.  Any output pointer may be NULL. */
+int spn_batch_get_result(spn_batch *b, int flow_id, int *n_measured, float *cutoffs, float *zz, float *dd,
+                         float *chi_zz, float *chi_dd);
+/* Current state of a flow (waits for queued work). */
+int spn_batch_get_state(spn_batch *b, int flow_id, float *cutoff, float *v2, float *v4ss, float *v4dd);
+/* Releases a flow's device memory; its id may be reused by a later spn_batch_add. */
+int spn_batch_remove(spn_batch *b, int flow_id);
+/* Steps run, CUDA graphs built, flows held. */
+int spn_batch_stats(spn_batch *b, long long *steps, long long *graph_builds, int *n_flows);
+
+/* ------------------------------------------------------------------------------------
  * Files: checkpoints and observables in the reference's HDF5 layout.  Host only.
  * ------------------------------------------------------------------------------------ */
 

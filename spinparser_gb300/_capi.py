@@ -113,6 +113,20 @@ SIGNATURES = {
     "spn_su2_synchronize": (C.c_int, [C.c_void_p]),
     "spn_su2_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "spn_su2_get_profile": (C.c_int, [C.c_void_p, c_double_p, c_int_p, c_double_p, c_int_p]),
+    "spn_batch_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    "spn_batch_destroy": (C.c_int, [C.c_void_p]),
+    "spn_batch_set_variant": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "spn_batch_footprint": (C.c_int, [C.POINTER(Su2Desc), C.c_int, c_ll_p]),
+    "spn_batch_add": (C.c_int, [C.c_void_p, C.POINTER(Su2Desc), C.c_int, c_float_p, c_float_p, c_float_p, c_float_p,
+                                c_int_p]),
+    "spn_batch_step": (C.c_int, [C.c_void_p, c_int_p]),
+    "spn_batch_synchronize": (C.c_int, [C.c_void_p]),
+    "spn_batch_poll": (C.c_int, [C.c_void_p, C.c_int, c_int_p, c_int_p, c_int_p]),
+    "spn_batch_get_result": (C.c_int, [C.c_void_p, C.c_int, c_int_p, c_float_p, c_float_p, c_float_p, c_float_p,
+                                       c_float_p]),
+    "spn_batch_get_state": (C.c_int, [C.c_void_p, C.c_int, c_float_p, c_float_p, c_float_p, c_float_p]),
+    "spn_batch_remove": (C.c_int, [C.c_void_p, C.c_int]),
+    "spn_batch_stats": (C.c_int, [C.c_void_p, c_ll_p, c_ll_p, c_int_p]),
     "spn_su2_write_checkpoint": (C.c_int, [C.c_char_p, C.c_int, C.c_float, C.c_int, c_float_p, C.c_longlong,
                                            c_float_p, c_float_p, c_int_p]),
     "spn_su2_read_checkpoint": (C.c_int, [C.c_char_p, C.c_int, c_float_p, C.c_int, c_float_p, C.c_longlong,

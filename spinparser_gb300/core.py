@@ -167,6 +167,30 @@ def measure_fp32_peak(device: int = 0):
     return t.value, g.value
 
 
+def make_desc(tables: LatticeTables, freq: np.ndarray, spin_length: float = 0.5, device: int = 0, flags: int = 0):
+    """The spn_su2_desc of a flow, and the arrays it points into (keep them alive while the
+    descriptor is used)."""
+    freq = np.ascontiguousarray(freq, dtype=np.float32)
+    keep = [freq] + [np.ascontiguousarray(x, dtype=np.int32) for x in
+                     (tables.sites_rid, tables.inv_sites_rid, tables.overlap_ptr, tables.overlap_rid1,
+                      tables.overlap_rid2, tables.range_rid, tables.range_inv_rid, tables.corr_rid)]
+    k = keep[1:]
+    d = Su2Desc()
+    d.n_freq = len(freq)
+    d.freq = _ptr(freq, C.c_float)
+    d.n_sites = tables.n_sites
+    d.sites_rid, d.inv_sites_rid, d.overlap_ptr = _ptr(k[0], C.c_int), _ptr(k[1], C.c_int), _ptr(k[2], C.c_int)
+    d.overlap_rid1, d.overlap_rid2 = _ptr(k[3], C.c_int), _ptr(k[4], C.c_int)
+    d.n_range = len(k[5])
+    d.range_rid, d.range_inv_rid = _ptr(k[5], C.c_int), _ptr(k[6], C.c_int)
+    d.n_corr = len(k[7])
+    d.corr_rid = _ptr(k[7], C.c_int)
+    d.spin_length = spin_length
+    d.device = device
+    d.flags = flags
+    return d, keep
+
+
 class Su2Flow:
     """One SU(2) flow resident on a GPU: the FrgCore::computeStep / finalizeStep cycle."""
 
@@ -179,23 +203,7 @@ class Su2Flow:
         self.n = len(self.freq)
         self.nl = tables.n_sites
         self.fn = self.n * self.n * (self.n + 1) // 2
-        self._keep = [np.ascontiguousarray(x, dtype=np.int32) for x in
-                      (tables.sites_rid, tables.inv_sites_rid, tables.overlap_ptr, tables.overlap_rid1,
-                       tables.overlap_rid2, tables.range_rid, tables.range_inv_rid, tables.corr_rid)]
-        k = self._keep
-        d = Su2Desc()
-        d.n_freq = self.n
-        d.freq = _ptr(self.freq, C.c_float)
-        d.n_sites = self.nl
-        d.sites_rid, d.inv_sites_rid, d.overlap_ptr = _ptr(k[0], C.c_int), _ptr(k[1], C.c_int), _ptr(k[2], C.c_int)
-        d.overlap_rid1, d.overlap_rid2 = _ptr(k[3], C.c_int), _ptr(k[4], C.c_int)
-        d.n_range = len(k[5])
-        d.range_rid, d.range_inv_rid = _ptr(k[5], C.c_int), _ptr(k[6], C.c_int)
-        d.n_corr = len(k[7])
-        d.corr_rid = _ptr(k[7], C.c_int)
-        d.spin_length = spin_length
-        d.device = device
-        d.flags = flags
+        d, self._keep = make_desc(tables, self.freq, spin_length, device, flags)
         h = C.c_void_p()
         check(lib.spn_su2_create(C.byref(d), C.byref(h)))
         self._h = h

@@ -1,0 +1,652 @@
+// Batched SU(2) flows on one GPU: many flows (different lattices, ranges, frequency counts,
+// cutoff lists) advanced together, each step one launch per kernel for all of them.
+//
+// Per step, for the flows still flowing:
+//   prepare      status words and work counters cleared
+//   self-energy  grid (frequency, flow)                    body: self_energy_body
+//   node tables  grid (frequency block, flow)              body: node_table_body
+//   vertex flow  one persistent launch per site class over the ragged (flow, triple) list
+//   correlation  grid (outer node, flow) + grid (flow)     bodies: corr_inner_body / corr_final_body
+//                (also for flows at their last cutoff, whose final measurement is due)
+//   Euler        grid (block, flow), skipped for a flow whose step produced a NaN
+//   advance      per flow: next cutoff, or final / done / diverged
+// Every per-step quantity (cutoff, step index, phase) lives in the flow's device record, so the
+// captured step (a CUDA graph) is replayed unchanged while the set of flows and their phases
+// stay the same; the host rebuilds the plan only when a flow joins, finishes or diverges.
+// The kernels evaluate each flow with the same device functions as the single-flow path, so
+// a flow's results do not depend on the other flows of the batch.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <vector>
+#include "su2_common.cuh"
+#include "su2_device.cuh"
+#include "su2_kernels.cuh"
+#include "su2_handle.cuh"
+
+using namespace spn;
+using namespace spn::dev;
+
+namespace {
+
+constexpr int kClasses = 3;  // sites per lane 1, 2, 4
+
+__global__ void batch_prepare_kernel(BatchFlow *flows, const int *list, int n, int *counters) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < kClasses && blockIdx.x == 0) counters[i] = 0;
+    if (i >= n) return;
+    BatchFlow &f = flows[list[i]];
+    if (f.phase != kPhaseDone) *f.a.status = 0u;
+}
+
+__global__ void __launch_bounds__(128) batch_self_energy_kernel(const BatchFlow *flows, const int *list) {
+    const BatchFlow &f = flows[list[blockIdx.y]];
+    if (f.phase != kPhaseFlowing) return;
+    const FlowArgs a = f.a;
+    if (int(blockIdx.x) >= a.n) return;
+    self_energy_body(a, blockIdx.x);
+}
+
+__global__ void batch_node_table_kernel(const BatchFlow *flows, const int *list) {
+    const BatchFlow &f = flows[list[blockIdx.y]];
+    if (f.phase != kPhaseFlowing) return;
+    const FlowArgs a = f.a;
+    if (int(blockIdx.x * blockDim.x) >= a.n) return;
+    node_table_body(a, blockIdx.x);
+}
+
+__device__ __forceinline__ CorrArgs batch_corr_args(const BatchFlow &f) {
+    CorrArgs c = f.c;
+    c.cutoff = f.a.cutoff;
+    c.out = f.hist + size_t(f.step) * (2 * size_t(c.n_corr) + 2 * c.nl);
+    return c;
+}
+
+template <int SPT>
+__global__ void __launch_bounds__(128) batch_corr_inner_kernel(const BatchFlow *flows, const int *list) {
+    const BatchFlow &f = flows[list[blockIdx.y]];
+    if (f.phase == kPhaseDone) return;
+    const CorrArgs c = batch_corr_args(f);
+    if (int(blockIdx.x) >= 2 * c.n + 4) return;
+    corr_inner_body<SPT>(c, blockIdx.x);
+}
+
+__global__ void batch_corr_final_kernel(const BatchFlow *flows, const int *list) {
+    const BatchFlow &f = flows[list[blockIdx.x]];
+    if (f.phase == kPhaseDone) return;
+    corr_final_body(batch_corr_args(f));
+}
+
+// Euler step of every flowing flow without a NaN in this step's flow (a flow whose step
+// produced a NaN stops before the update, as SpinParser::runCore does).
+__global__ void batch_euler_kernel(const BatchFlow *flows, const int *list) {
+    const BatchFlow &f = flows[list[blockIdx.y]];
+    if (f.phase != kPhaseFlowing || (*f.a.status & (kStatusNaN | kStatusNodeOverflow))) return;
+    const FlowArgs &a = f.a;
+    const float step = __fsub_rn(f.cutoffs[f.step + 1], f.cutoffs[f.step]);
+    const long long vsz = (long long)a.fn * a.nl;
+    const long long n4 = vsz / 4;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    float4 *s4 = reinterpret_cast<float4 *>(const_cast<float *>(a.ss));
+    float4 *d4 = reinterpret_cast<float4 *>(const_cast<float *>(a.dd));
+    const float4 *ds4 = reinterpret_cast<const float4 *>(a.dss);
+    const float4 *dd4 = reinterpret_cast<const float4 *>(a.ddd);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += stride) {
+        float4 v = s4[i], d = ds4[i];
+        v.x = euler_update(v.x, d.x, step);
+        v.y = euler_update(v.y, d.y, step);
+        v.z = euler_update(v.z, d.z, step);
+        v.w = euler_update(v.w, d.w, step);
+        s4[i] = v;
+        v = d4[i];
+        d = dd4[i];
+        v.x = euler_update(v.x, d.x, step);
+        v.y = euler_update(v.y, d.y, step);
+        v.z = euler_update(v.z, d.z, step);
+        v.w = euler_update(v.w, d.w, step);
+        d4[i] = v;
+    }
+    float *ss = const_cast<float *>(a.ss), *dd = const_cast<float *>(a.dd);
+    for (long long i = 4 * n4 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vsz; i += stride) {
+        ss[i] = euler_update(ss[i], a.dss[i], step);
+        dd[i] = euler_update(dd[i], a.ddd[i], step);
+    }
+    if (blockIdx.x == 0) {
+        float *v2 = const_cast<float *>(a.v2);
+        for (int i = threadIdx.x; i < a.n; i += blockDim.x) {
+            if (a.fp64_sigma) {
+                double *v2d = const_cast<double *>(a.v2d);
+                const double v = euler_update_f64(v2d[i], a.dv2d[i], step);
+                v2d[i] = v;
+                v2[i] = float(v);
+            } else {
+                v2[i] = euler_update(v2[i], a.dv2[i], step);
+            }
+        }
+    }
+}
+
+__global__ void batch_advance_kernel(BatchFlow *flows, const int *list, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    BatchFlow &f = flows[list[i]];
+    if (f.phase == kPhaseFinal) {
+        f.phase = kPhaseDone;
+    } else if (f.phase == kPhaseFlowing) {
+        const unsigned st = *f.a.status;
+        if (st & kStatusNodeOverflow) {
+            f.flags |= kFlagNodeOverflow;
+            f.phase = kPhaseDone;
+        } else if (st & kStatusNaN) {
+            f.flags |= kFlagDiverged;
+            f.phase = kPhaseDone;
+        } else {
+            f.step += 1;
+            f.a.cutoff = f.cutoffs[f.step];
+            if (f.step == f.n_cutoffs - 1) f.phase = kPhaseFinal;
+        }
+    }
+}
+
+template <class T>
+T *dalloc(size_t count, const char *what) {
+    void *p = nullptr;
+    cuda_check(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)), what);
+    return static_cast<T *>(p);
+}
+
+int class_of(int nl) {
+    const int spt = spt_for(nl);
+    return spt == 1 ? 0 : (spt == 2 ? 1 : 2);
+}
+
+}  // namespace
+
+struct spn_batch {
+    struct Flow {
+        spn_su2 *h = nullptr;
+        float *cutoffs = nullptr, *hist = nullptr;
+        std::vector<float> host_cutoffs;
+        int n_cutoffs = 0, step = 0, phase = kPhaseDone;
+        unsigned flags = 0;
+        bool used = false;
+        size_t hist_row = 0;
+    };
+    int device = 0, sms = 0, npi = 1;
+    bool use_graph = true;
+    cudaStream_t stream = nullptr;
+    std::vector<Flow> flows;
+    BatchFlow *d_flows = nullptr;
+    int capacity = 0;
+    int *d_lists = nullptr, *d_counters = nullptr;
+    size_t lists_cap = 0;
+    BatchFlow *h_status = nullptr;  // pinned: device records copied back after each step
+    cudaEvent_t status_ev = nullptr;
+    bool status_pending = false;
+    // plan
+    bool plan_valid = false;
+    std::vector<int> lists;  // flowing | measure | per-class measure | per-class vertex list | per-class prefix
+    int n_flowing = 0, n_measure = 0, n_max = 2;
+    int off_flowing = 0, off_measure = 0;
+    int off_cm[kClasses] = {}, n_cm[kClasses] = {};
+    int off_cv[kClasses] = {}, n_cv[kClasses] = {}, off_cp[kClasses] = {}, total_cv[kClasses] = {};
+    int warp_area[kClasses] = {}, nl_max = 1, vgrid[kClasses] = {};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long steps_run = 0, graph_builds = 0;
+
+    ~spn_batch() {
+        cudaSetDevice(device);
+        if (stream) cudaStreamSynchronize(stream);
+        for (auto &f : flows) release(f);
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (d_flows) cudaFree(d_flows);
+        if (d_lists) cudaFree(d_lists);
+        if (d_counters) cudaFree(d_counters);
+        if (h_status) cudaFreeHost(h_status);
+        if (status_ev) cudaEventDestroy(status_ev);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    static void release(Flow &f) {
+        if (f.h) {
+            f.h->release();
+            delete f.h;
+            f.h = nullptr;
+        }
+        if (f.cutoffs) cudaFree(f.cutoffs);
+        if (f.hist) cudaFree(f.hist);
+        f.cutoffs = f.hist = nullptr;
+        f.used = false;
+        f.phase = kPhaseDone;
+    }
+
+    void ensure_capacity(int n) {
+        if (n <= capacity) return;
+        int cap = std::max(16, capacity * 2);
+        while (cap < n) cap *= 2;
+        cuda_check(cudaStreamSynchronize(stream), "batch sync");
+        BatchFlow *nf = dalloc<BatchFlow>(cap, "alloc batch records");
+        BatchFlow *nh = nullptr;
+        cuda_check(cudaMallocHost(&nh, sizeof(BatchFlow) * cap), "alloc pinned batch records");
+        if (d_flows) {
+            cuda_check(cudaMemcpyAsync(nf, d_flows, sizeof(BatchFlow) * capacity, cudaMemcpyDeviceToDevice, stream), "copy records");
+            cuda_check(cudaStreamSynchronize(stream), "batch sync");
+            cudaFree(d_flows);
+        }
+        if (h_status) {
+            std::memcpy(nh, h_status, sizeof(BatchFlow) * capacity);
+            cudaFreeHost(h_status);
+        }
+        d_flows = nf;
+        h_status = nh;
+        capacity = cap;
+        plan_valid = false;
+    }
+
+    void ensure_lists(size_t n) {
+        if (n <= lists_cap) return;
+        if (d_lists) {
+            cuda_check(cudaStreamSynchronize(stream), "batch sync");
+            cudaFree(d_lists);
+        }
+        lists_cap = std::max<size_t>(n, 2 * lists_cap);
+        d_lists = dalloc<int>(lists_cap, "alloc batch lists");
+    }
+
+    // Reads the device records of the previous step (lagging one step behind the host) and
+    // takes over divergence and overflow, which only the device knows.
+    void absorb_status(bool wait) {
+        if (!status_pending) return;
+        if (!wait && cudaEventQuery(status_ev) == cudaErrorNotReady) return;
+        cuda_check(cudaEventSynchronize(status_ev), "batch status sync");
+        status_pending = false;
+        for (size_t i = 0; i < flows.size(); ++i) {
+            Flow &f = flows[i];
+            if (!f.used) continue;
+            const BatchFlow &r = h_status[i];
+            if (r.flags & ~f.flags) {
+                f.flags |= r.flags;
+                f.phase = kPhaseDone;
+                f.step = r.step;
+                plan_valid = false;
+            }
+        }
+    }
+
+    void build_plan() {
+        lists.clear();
+        n_max = 2;
+        nl_max = 1;
+        std::vector<int> flowing, measure, cm[kClasses], cv[kClasses];
+        for (size_t i = 0; i < flows.size(); ++i) {
+            const Flow &f = flows[i];
+            if (!f.used || f.phase == kPhaseDone) continue;
+            const int c = class_of(f.h->nl);
+            measure.push_back(int(i));
+            cm[c].push_back(int(i));
+            n_max = std::max(n_max, f.h->n);
+            nl_max = std::max(nl_max, f.h->nl);
+            if (f.phase == kPhaseFlowing) {
+                flowing.push_back(int(i));
+                cv[c].push_back(int(i));
+            }
+        }
+        auto put = [&](const std::vector<int> &v) {
+            const int off = int(lists.size());
+            lists.insert(lists.end(), v.begin(), v.end());
+            return off;
+        };
+        off_flowing = put(flowing);
+        n_flowing = int(flowing.size());
+        off_measure = put(measure);
+        n_measure = int(measure.size());
+        for (int c = 0; c < kClasses; ++c) {
+            off_cm[c] = put(cm[c]);
+            n_cm[c] = int(cm[c].size());
+            off_cv[c] = put(cv[c]);
+            n_cv[c] = int(cv[c].size());
+            std::vector<int> prefix(1, 0);
+            size_t area = 0;
+            for (int i : cv[c]) {
+                const spn_su2 *h = flows[i].h;
+                const long long next = prefix.back() + h->fn;
+                if (next >= (1ll << 31)) throw Error(ErrorType::Unsupported, "batch work list beyond 2^31 items");
+                prefix.push_back(int(next));
+                area = std::max(area, batch_vertex_warp_area(h->nl, h->rpa_n_seg, npi));
+            }
+            off_cp[c] = put(prefix);
+            total_cv[c] = prefix.back();
+            warp_area[c] = int((area + 15) / 16 * 16);
+            vgrid[c] = 0;
+            if (n_cv[c] > 0) {
+                const size_t smem = batch_vertex_smem_bytes(n_max, warp_area[c]);
+                const int per_sm = batch_vertex_blocks_per_sm(1 << c, npi, smem);
+                cudaGetLastError();
+                if (per_sm < 1) throw Error(ErrorType::Unsupported, "batched vertex-flow kernel does not fit for this batch");
+                vgrid[c] = sms * per_sm;
+            }
+        }
+        ensure_lists(lists.size());
+        cuda_check(cudaStreamSynchronize(stream), "batch sync");
+        if (!lists.empty())
+            cuda_check(cudaMemcpyAsync(d_lists, lists.data(), lists.size() * sizeof(int), cudaMemcpyHostToDevice, stream),
+                       "upload batch lists");
+        cuda_check(cudaStreamSynchronize(stream), "batch sync");
+        if (exec) {
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
+        }
+        if (graph) {
+            cudaGraphDestroy(graph);
+            graph = nullptr;
+        }
+        plan_valid = true;
+    }
+
+    void enqueue_step() {
+        const int *L = d_lists;
+        batch_prepare_kernel<<<(std::max(n_measure, kClasses) + 127) / 128, 128, 0, stream>>>(d_flows, L + off_measure, n_measure,
+                                                                                             d_counters);
+        if (n_flowing > 0) {
+            batch_self_energy_kernel<<<dim3(n_max, n_flowing), 128, 0, stream>>>(d_flows, L + off_flowing);
+            batch_node_table_kernel<<<dim3((n_max + 63) / 64, n_flowing), 64, 0, stream>>>(d_flows, L + off_flowing);
+            for (int c = 0; c < kClasses; ++c) {
+                if (n_cv[c] == 0) continue;
+                BatchVertexArgs b;
+                b.flows = d_flows;
+                b.list = L + off_cv[c];
+                b.prefix = L + off_cp[c];
+                b.n_list = n_cv[c];
+                b.total = total_cv[c];
+                b.n_max = n_max;
+                b.counter = d_counters + c;
+                b.warp_area = warp_area[c];
+                launch_batch_vertex(b, 1 << c, npi, vgrid[c], stream);
+            }
+        }
+        for (int c = 0; c < kClasses; ++c) {
+            if (n_cm[c] == 0) continue;
+            const dim3 g(2 * n_max + 4, n_cm[c]);
+            if (c == 0) batch_corr_inner_kernel<1><<<g, 128, 0, stream>>>(d_flows, L + off_cm[c]);
+            else if (c == 1) batch_corr_inner_kernel<2><<<g, 128, 0, stream>>>(d_flows, L + off_cm[c]);
+            else batch_corr_inner_kernel<4><<<g, 128, 0, stream>>>(d_flows, L + off_cm[c]);
+        }
+        if (n_measure > 0)
+            batch_corr_final_kernel<<<n_measure, 128, 2 * nl_max * sizeof(double), stream>>>(d_flows, L + off_measure);
+        if (n_flowing > 0) batch_euler_kernel<<<dim3(48, n_flowing), 256, 0, stream>>>(d_flows, L + off_flowing);
+        batch_advance_kernel<<<(std::max(n_measure, 1) + 127) / 128, 128, 0, stream>>>(d_flows, L + off_measure, n_measure);
+        cuda_check(cudaGetLastError(), "batch step launch");
+    }
+};
+
+namespace {
+
+size_t footprint_bytes(const spn_su2_desc *d, int n_cutoffs) {
+    const size_t n = size_t(d->n_freq), nl = size_t(d->n_sites);
+    const size_t fn = n * n * (n + 1) / 2;
+    const size_t nov = size_t(d->overlap_ptr ? d->overlap_ptr[d->n_sites] : 0);
+    size_t b = 4 * fn * nl * sizeof(float);                       // state and flow
+    b += n * (4 * sizeof(float) + 2 * sizeof(double));             // mesh, self-energy
+    b += n * (2 * n + 8) * 2 * sizeof(float) + n * sizeof(int);    // node tables
+    b += size_t(2 * n + 8) * 2 * nl * sizeof(double);              // correlation scratch
+    b += size_t(n_cutoffs) * (2 * size_t(d->n_corr) + 2 * nl) * sizeof(float);  // measurement history
+    b += (4 * nl + 3 * nov + 2 * size_t(d->n_range) + size_t(d->n_corr)) * sizeof(int);
+    return b;
+}
+
+}  // namespace
+
+extern "C" int spn_batch_create(int device, spn_batch **out) {
+    return guarded([&] {
+        if (!out) throw Error(ErrorType::Argument, "null output handle");
+        std::unique_ptr<spn_batch> b(new spn_batch);
+        b->device = device;
+        cuda_check(cudaSetDevice(device), "cudaSetDevice");
+        cuda_check(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device), "device attribute");
+        cuda_check(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        cuda_check(cudaEventCreateWithFlags(&b->status_ev, cudaEventDisableTiming), "cudaEventCreate");
+        b->d_counters = dalloc<int>(kClasses, "alloc batch counters");
+        b->ensure_capacity(16);
+        *out = b.release();
+    });
+}
+
+extern "C" int spn_batch_destroy(spn_batch *b) {
+    delete b;
+    return SPN_OK;
+}
+
+extern "C" int spn_batch_set_variant(spn_batch *b, int npi, int use_graph) {
+    return guarded([&] {
+        if (!b) throw Error(ErrorType::Argument, "null handle");
+        if (npi != 1 && npi != 2) throw Error(ErrorType::Argument, "nodes per iteration must be 1 or 2");
+        b->npi = npi;
+        b->use_graph = use_graph != 0;
+        b->plan_valid = false;
+    });
+}
+
+extern "C" int spn_batch_footprint(const spn_su2_desc *desc, int n_cutoffs, long long *bytes) {
+    return guarded([&] {
+        if (!desc || !bytes || n_cutoffs < 1) throw Error(ErrorType::Argument, "spn_batch_footprint: bad argument");
+        *bytes = (long long)footprint_bytes(desc, n_cutoffs);
+    });
+}
+
+extern "C" int spn_batch_add(spn_batch *b, const spn_su2_desc *desc, int n_cutoffs, const float *cutoffs, const float *v2,
+                             const float *v4ss, const float *v4dd, int *flow_id) {
+    return guarded([&] {
+        if (!b || !desc || !cutoffs || n_cutoffs < 1 || !v2 || !v4ss || !v4dd || !flow_id)
+            throw Error(ErrorType::Argument, "spn_batch_add: bad argument");
+        if (desc->device != b->device) throw Error(ErrorType::Argument, "spn_batch_add: flow device differs from the batch's");
+        for (int k = 1; k < n_cutoffs; ++k)
+            if (!(cutoffs[k] < cutoffs[k - 1])) throw Error(ErrorType::Argument, "spn_batch_add: cutoffs must descend");
+        cuda_check(cudaSetDevice(b->device), "cudaSetDevice");
+        b->absorb_status(true);
+        int slot = -1;
+        for (size_t i = 0; i < b->flows.size(); ++i)
+            if (!b->flows[i].used) {
+                slot = int(i);
+                break;
+            }
+        if (slot < 0) {
+            slot = int(b->flows.size());
+            b->flows.emplace_back();
+        }
+        b->ensure_capacity(slot + 1);
+        spn_batch::Flow &f = b->flows[slot];
+        try {
+            f.h = create_flow(desc, b->stream);
+            f.n_cutoffs = n_cutoffs;
+            f.host_cutoffs.assign(cutoffs, cutoffs + n_cutoffs);
+            f.cutoffs = dalloc<float>(n_cutoffs, "alloc batch cutoffs");
+            f.hist_row = 2 * size_t(f.h->n_corr) + 2 * f.h->nl;
+            f.hist = dalloc<float>(size_t(n_cutoffs) * f.hist_row, "alloc measurement history");
+            cuda_check(cudaMemcpyAsync(f.cutoffs, cutoffs, n_cutoffs * sizeof(float), cudaMemcpyHostToDevice, b->stream), "H2D");
+            const size_t vsz = size_t(f.h->fn) * f.h->nl;
+            cuda_check(cudaMemcpyAsync(f.h->v2, v2, f.h->n * sizeof(float), cudaMemcpyHostToDevice, b->stream), "H2D");
+            cuda_check(cudaMemcpyAsync(f.h->ss, v4ss, vsz * sizeof(float), cudaMemcpyHostToDevice, b->stream), "H2D");
+            cuda_check(cudaMemcpyAsync(f.h->dd, v4dd, vsz * sizeof(float), cudaMemcpyHostToDevice, b->stream), "H2D");
+            std::vector<double> v2d(v2, v2 + f.h->n);
+            cuda_check(cudaMemcpyAsync(f.h->v2d, v2d.data(), f.h->n * sizeof(double), cudaMemcpyHostToDevice, b->stream), "H2D");
+            f.h->cutoff = cutoffs[0];
+            BatchFlow r;
+            std::memset(&r, 0, sizeof(r));
+            r.a = f.h->args();
+            r.c = corr_args(f.h);
+            r.cutoffs = f.cutoffs;
+            r.hist = f.hist;
+            r.n_cutoffs = n_cutoffs;
+            r.step = 0;
+            r.phase = n_cutoffs > 1 ? kPhaseFlowing : kPhaseFinal;
+            r.flags = 0;
+            cuda_check(cudaMemcpyAsync(b->d_flows + slot, &r, sizeof(r), cudaMemcpyHostToDevice, b->stream), "H2D record");
+            cuda_check(cudaStreamSynchronize(b->stream), "batch add sync");
+            f.step = 0;
+            f.phase = r.phase;
+            f.flags = 0;
+            f.used = true;
+            b->h_status[slot] = r;
+        } catch (...) {
+            spn_batch::release(f);
+            throw;
+        }
+        b->plan_valid = false;
+        *flow_id = slot;
+    });
+}
+
+extern "C" int spn_batch_step(spn_batch *b, int *n_active) {
+    return guarded([&] {
+        if (!b) throw Error(ErrorType::Argument, "null handle");
+        cuda_check(cudaSetDevice(b->device), "cudaSetDevice");
+        b->absorb_status(false);
+        if (!b->plan_valid) b->build_plan();
+        if (b->n_measure > 0) {
+            if (b->use_graph) {
+                if (!b->exec) {
+                    cuda_check(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+                    b->enqueue_step();
+                    cuda_check(cudaStreamEndCapture(b->stream, &b->graph), "end capture");
+                    cuda_check(cudaGraphInstantiate(&b->exec, b->graph, 0), "graph instantiate");
+                    ++b->graph_builds;
+                }
+                cuda_check(cudaGraphLaunch(b->exec, b->stream), "graph launch");
+            } else {
+                b->enqueue_step();
+            }
+            ++b->steps_run;
+            // the host's view of every flow advances the same way the advance kernel does
+            for (auto &f : b->flows) {
+                if (!f.used) continue;
+                if (f.phase == kPhaseFinal) {
+                    f.phase = kPhaseDone;
+                    b->plan_valid = false;
+                } else if (f.phase == kPhaseFlowing) {
+                    ++f.step;
+                    if (f.step == f.n_cutoffs - 1) {
+                        f.phase = kPhaseFinal;
+                        b->plan_valid = false;
+                    }
+                }
+            }
+            if (!b->status_pending) {
+                cuda_check(cudaMemcpyAsync(b->h_status, b->d_flows, sizeof(BatchFlow) * b->flows.size(), cudaMemcpyDeviceToHost,
+                                           b->stream),
+                           "D2H records");
+                cuda_check(cudaEventRecord(b->status_ev, b->stream), "record");
+                b->status_pending = true;
+            }
+        }
+        if (n_active) {
+            int n = 0;
+            for (auto &f : b->flows) n += (f.used && f.phase != kPhaseDone);
+            *n_active = n;
+        }
+    });
+}
+
+extern "C" int spn_batch_synchronize(spn_batch *b) {
+    return guarded([&] {
+        if (!b) throw Error(ErrorType::Argument, "null handle");
+        cuda_check(cudaSetDevice(b->device), "cudaSetDevice");
+        cuda_check(cudaStreamSynchronize(b->stream), "batch sync");
+        b->absorb_status(true);
+        // a fresh copy of the records: the pending one may predate the last steps
+        cuda_check(cudaMemcpyAsync(b->h_status, b->d_flows, sizeof(BatchFlow) * b->flows.size(), cudaMemcpyDeviceToHost, b->stream),
+                   "D2H records");
+        cuda_check(cudaEventRecord(b->status_ev, b->stream), "record");
+        b->status_pending = true;
+        b->absorb_status(true);
+    });
+}
+
+extern "C" int spn_batch_poll(spn_batch *b, int flow_id, int *phase, int *step, int *flags) {
+    return guarded([&] {
+        if (!b || flow_id < 0 || flow_id >= int(b->flows.size()) || !b->flows[flow_id].used)
+            throw Error(ErrorType::Argument, "spn_batch_poll: unknown flow");
+        cuda_check(cudaSetDevice(b->device), "cudaSetDevice");
+        b->absorb_status(false);
+        const spn_batch::Flow &f = b->flows[flow_id];
+        if (phase) *phase = f.phase;
+        if (step) *step = f.step;
+        if (flags) *flags = int(f.flags);
+    });
+}
+
+extern "C" int spn_batch_get_result(spn_batch *b, int flow_id, int *n_measured, float *cutoffs, float *zz, float *dd,
+                                    float *chi_zz, float *chi_dd) {
+    return guarded([&] {
+        if (!b || flow_id < 0 || flow_id >= int(b->flows.size()) || !b->flows[flow_id].used)
+            throw Error(ErrorType::Argument, "spn_batch_get_result: unknown flow");
+        cuda_check(cudaSetDevice(b->device), "cudaSetDevice");
+        cuda_check(cudaStreamSynchronize(b->stream), "batch sync");
+        const spn_batch::Flow &f = b->flows[flow_id];
+        BatchFlow r;
+        cuda_check(cudaMemcpy(&r, b->d_flows + flow_id, sizeof(r), cudaMemcpyDeviceToHost), "D2H record");
+        // rows 0..step hold measurements; the row of the current step exists once measured
+        const int rows = (r.phase == kPhaseDone) ? r.step + 1 : r.step;
+        const int nc = f.h->n_corr, nl = f.h->nl;
+        std::vector<float> hist(size_t(std::max(rows, 0)) * f.hist_row);
+        if (rows > 0)
+            cuda_check(cudaMemcpy(hist.data(), f.hist, hist.size() * sizeof(float), cudaMemcpyDeviceToHost), "D2H history");
+        for (int k = 0; k < rows; ++k) {
+            const float *row = hist.data() + size_t(k) * f.hist_row;
+            if (cutoffs) cutoffs[k] = f.host_cutoffs[k];
+            if (zz) std::memcpy(zz + size_t(k) * nc, row, nc * sizeof(float));
+            if (dd) std::memcpy(dd + size_t(k) * nc, row + nc, nc * sizeof(float));
+            if (chi_zz) std::memcpy(chi_zz + size_t(k) * nl, row + 2 * nc, nl * sizeof(float));
+            if (chi_dd) std::memcpy(chi_dd + size_t(k) * nl, row + 2 * nc + nl, nl * sizeof(float));
+        }
+        if (n_measured) *n_measured = rows;
+    });
+}
+
+extern "C" int spn_batch_get_state(spn_batch *b, int flow_id, float *cutoff, float *v2, float *v4ss, float *v4dd) {
+    return guarded([&] {
+        if (!b || flow_id < 0 || flow_id >= int(b->flows.size()) || !b->flows[flow_id].used)
+            throw Error(ErrorType::Argument, "spn_batch_get_state: unknown flow");
+        cuda_check(cudaSetDevice(b->device), "cudaSetDevice");
+        cuda_check(cudaStreamSynchronize(b->stream), "batch sync");
+        const spn_batch::Flow &f = b->flows[flow_id];
+        BatchFlow r;
+        cuda_check(cudaMemcpy(&r, b->d_flows + flow_id, sizeof(r), cudaMemcpyDeviceToHost), "D2H record");
+        const size_t vsz = size_t(f.h->fn) * f.h->nl;
+        if (cutoff) *cutoff = r.a.cutoff;
+        if (v2) cuda_check(cudaMemcpy(v2, f.h->v2, f.h->n * sizeof(float), cudaMemcpyDeviceToHost), "D2H");
+        if (v4ss) cuda_check(cudaMemcpy(v4ss, f.h->ss, vsz * sizeof(float), cudaMemcpyDeviceToHost), "D2H");
+        if (v4dd) cuda_check(cudaMemcpy(v4dd, f.h->dd, vsz * sizeof(float), cudaMemcpyDeviceToHost), "D2H");
+    });
+}
+
+extern "C" int spn_batch_remove(spn_batch *b, int flow_id) {
+    return guarded([&] {
+        if (!b || flow_id < 0 || flow_id >= int(b->flows.size()) || !b->flows[flow_id].used)
+            throw Error(ErrorType::Argument, "spn_batch_remove: unknown flow");
+        cuda_check(cudaSetDevice(b->device), "cudaSetDevice");
+        cuda_check(cudaStreamSynchronize(b->stream), "batch sync");
+        b->absorb_status(true);
+        spn_batch::release(b->flows[flow_id]);
+        BatchFlow r;
+        std::memset(&r, 0, sizeof(r));
+        r.phase = kPhaseDone;
+        cuda_check(cudaMemcpy(b->d_flows + flow_id, &r, sizeof(r), cudaMemcpyHostToDevice), "H2D record");
+        b->plan_valid = false;
+    });
+}
+
+extern "C" int spn_batch_stats(spn_batch *b, long long *steps, long long *graph_builds, int *n_flows) {
+    return guarded([&] {
+        if (!b) throw Error(ErrorType::Argument, "null handle");
+        if (steps) *steps = b->steps_run;
+        if (graph_builds) *graph_builds = b->graph_builds;
+        if (n_flows) {
+            int n = 0;
+            for (auto &f : b->flows) n += f.used;
+            *n_flows = n;
+        }
+    });
+}

@@ -49,6 +49,43 @@ struct FlowArgs {
     RpaSchedule rpa;
 };
 
+// Correlation measurement (nu = 0) of one flow: the state it reads, the per-node partial
+// sums and the output zz[n_corr], dd[n_corr], chi_s[nl], chi_d[nl].
+struct CorrArgs {
+    int n, nl, n_corr;
+    float cutoff, spin;
+    const float *freq, *ss, *dd, *v2;
+    const double *v2d;  // FP64 self-energy, read instead of v2 when not NULL
+    const int *sites, *inv_sites, *corr_rid;
+    double *partial;  // [max_nodes][2][nl]
+    float *out;
+    int wsite;
+};
+
+// ------------------------------------------------------------------------------------
+// Batches: many flows advanced together (include/spn_su2.h, spn_batch_*).  Each flow has a
+// device-resident record; the batched kernels take the record array and a list of the flows
+// they work on, and read every per-step quantity (cutoff, step index, phase) from the record,
+// so a captured step can be replayed without the host.
+// ------------------------------------------------------------------------------------
+constexpr int kPhaseFlowing = 0;  // computes the flow, measures, steps to the next cutoff
+constexpr int kPhaseFinal = 1;    // at the last cutoff: only the final measurement is left
+constexpr int kPhaseDone = 2;     // finished (or diverged)
+
+constexpr unsigned kFlagDiverged = 1u;
+constexpr unsigned kFlagNodeOverflow = 2u;
+
+struct BatchFlow {
+    FlowArgs a;            // a.cutoff is the current cutoff, a.status the per-step status word
+    CorrArgs c;            // c.cutoff / c.out are derived per step from the fields below
+    const float *cutoffs;  // [n_cutoffs] descending
+    float *hist;           // [n_cutoffs][2 * n_corr + 2 * nl] measurement at every cutoff
+    int n_cutoffs;
+    int step;              // index of the current cutoff
+    int phase;
+    unsigned flags;
+};
+
 // Vertex-flow kernel (su2_vertex.cu): dynamic shared memory per block, the number of blocks
 // per SM it achieves, and the launch.
 // `npi`: loop-frequency nodes a site group evaluates per iteration (1 or 2); whether the RPA
@@ -59,5 +96,22 @@ void launch_vertex_flow(const FlowArgs &a, int npi, int grid, cudaStream_t strea
 
 // Largest schedule staged in shared memory; larger ones are read from global memory.
 constexpr int kRpaSmemMaxInts = 8192;
+
+// Batched vertex flow: one persistent launch over the ragged work list of all flows of one
+// site class (spt = 1, 2 or 4 sites per lane).  Work item w belongs to flow list[f] with
+// prefix[f] <= w < prefix[f+1] (prefix[f+1] - prefix[f] = that flow's triple count).
+// `warp_area` is the per-warp shared-memory bytes the largest flow of the list needs.
+struct BatchVertexArgs {
+    BatchFlow *flows;
+    const int *list, *prefix;
+    int n_list, total, n_max;
+    int *counter;
+    int warp_area;
+};
+size_t batch_vertex_warp_area(int nl, int n_seg, int npi);
+size_t batch_vertex_smem_bytes(int n_max, size_t warp_area);
+int batch_vertex_blocks_per_sm(int spt, int npi, size_t smem);
+void launch_batch_vertex(const BatchVertexArgs &b, int spt, int npi, int grid, cudaStream_t stream);
+int vertex_spt(int nl);  // sites per lane of a flow with nl sites
 
 }  // namespace spn

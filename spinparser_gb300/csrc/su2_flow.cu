@@ -27,6 +27,8 @@
 #include <vector>
 #include "su2_common.cuh"
 #include "su2_device.cuh"
+#include "su2_kernels.cuh"
+#include "su2_handle.cuh"
 #include "host/capi_common.hpp"
 #include "../../include/spn_su2.h"
 
@@ -35,89 +37,17 @@ using namespace spn::dev;
 
 namespace {
 
-constexpr double kPiD = 3.14159265358979323846;
-constexpr int kCorrWarps = 4;  // the correlation kernels run 128-thread blocks
+// ------------------------------------------------------------------------------------
+// single-flow kernels (bodies in su2_kernels.cuh)
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) su2_self_energy_kernel(FlowArgs a) { self_energy_body(a, blockIdx.x); }
 
-// ------------------------------------------------------------------------------------
-// 1. self-energy flow
-// ------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) su2_self_energy_kernel(FlowArgs a) {
-    __shared__ float pos[kMaxFreq];
-    __shared__ double red[4];
-    for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
-    __syncthreads();
-    const int i = blockIdx.x;
-    const float w = pos[i], L = a.cutoff;
-    const float wpl = w + L, wml = w - L;
-    double part = 0.0;
-    for (int j = threadIdx.x; j < a.n_range; j += blockDim.x) {
-        const int r12 = a.range_rid[j], r21 = a.range_inv[j];
-        float x1 = value_none(pos, a.n, a.nl, a.dd, true, r12, r21, wpl, 0.0f, wml);
-        float x2 = value_none(pos, a.n, a.nl, a.dd, true, r12, r21, wml, 0.0f, wpl);
-        part += double(x1) - double(x2);
-    }
-    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double sum = 0.0;
-        for (int k = 0; k < int(blockDim.x >> 5); ++k) sum += red[k];
-        double val = -4.0 * double(a.spin) * sum;
-        val += 0.75 * (double(value_none(pos, a.n, a.nl, a.ss, false, 0, 0, wpl, wml, 0.0f)) -
-                       double(value_none(pos, a.n, a.nl, a.ss, false, 0, 0, wml, wpl, 0.0f)));
-        val += (double(value_none(pos, a.n, a.nl, a.dd, true, 0, 0, wpl, wml, 0.0f)) -
-                double(value_none(pos, a.n, a.nl, a.dd, true, 0, 0, wml, wpl, 0.0f)));
-        const double sig = a.fp64_sigma ? odd_interp(pos, a.n, a.v2d, L) : odd_interp(pos, a.n, a.v2, L);
-        val /= (2.0 * kPiD * (double(L) + sig));
-        float out = float(val);
-        a.dv2[i] = out;
-        if (a.fp64_sigma) a.dv2d[i] = val;
-        if (isnan(out)) atomicOr(a.status, kStatusNaN);
-    }
-}
+__global__ void su2_node_table_kernel(FlowArgs a) { node_table_body(a, blockIdx.x); }
 
-// ------------------------------------------------------------------------------------
-// 2. loop-frequency node tables
-// ------------------------------------------------------------------------------------
-__global__ void su2_node_table_kernel(FlowArgs a) {
-    __shared__ float pos[kMaxFreq];
-    for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
-    __syncthreads();
-    const int xi = blockIdx.x * blockDim.x + threadIdx.x;
-    if (xi >= a.n) return;
-    const int n = a.n;
-    const float x = pos[xi], L = a.cutoff;
-    float *wp_out = a.node_wp + size_t(xi) * a.max_nodes;
-    float *c_out = a.node_c + size_t(xi) * a.max_nodes;
-    int cnt = 0;
-    bool overflow = false;
-    auto put = [&](float wp, double c) {
-        if (cnt < a.max_nodes) {
-            wp_out[cnt] = wp;
-            c_out[cnt] = float(c);
-            ++cnt;
-        } else {
-            overflow = true;
-        }
-    };
-    auto sig = [&](float w) { return a.fp64_sigma ? odd_interp(pos, n, a.v2d, w) : odd_interp(pos, n, a.v2, w); };
-    auto dsig = [&](float w) { return a.fp64_sigma ? odd_interp(pos, n, a.dv2d, w) : odd_interp(pos, n, a.dv2, w); };
-    auto p = [&](float w1, float w2) { return 1.0 / ((double(w1) + sig(w1)) * (double(w2) + sig(w2))); };
-    auto pk = [&](float w1, float w2) {
-        double d1 = double(w1) + sig(w1);
-        return dsig(w1) / (d1 * d1 * (double(w2) + sig(w2)));
-    };
-    // conventional contribution (SU2FrgCore.cpp:351-371)
-    put(L, p(L, L + x));
-    if (x > 2.0f * L) put(-L, p(L, L - x));
-    // Katanin contribution (SU2FrgCore.cpp:374-424)
-    auto kat = [&](float wp, double weight) { put(wp, weight * pk(wp, x + wp)); };
-    if (-(x + L) > -pos[n - 1]) nodes_right(pos, n, -(x + L), kat);
-    if (x - L > L) nodes_both(pos, n, L - x, -L, kat);
-    if (L < pos[n - 1]) nodes_left(pos, n, L, kat);
-    a.node_cnt[xi] = cnt;
-    if (overflow) atomicOr(a.status, kStatusNodeOverflow);
-}
+template <int SPT>
+__global__ void __launch_bounds__(128) su2_corr_inner_kernel(CorrArgs a) { corr_inner_body<SPT>(a, blockIdx.x); }
+
+__global__ void su2_corr_final_kernel(CorrArgs a) { corr_final_body(a); }
 
 // ------------------------------------------------------------------------------------
 // Euler step  x += step * dx  (rounded like the reference: product, then sum)
@@ -128,180 +58,23 @@ __global__ void su2_euler_kernel(float *__restrict__ x, const float *__restrict_
     const float4 *d4 = reinterpret_cast<const float4 *>(dx);
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += (long long)gridDim.x * blockDim.x) {
         float4 v = x4[i], d = __ldg(d4 + i);
-        v.x = __fadd_rn(v.x, __fmul_rn(step, d.x));
-        v.y = __fadd_rn(v.y, __fmul_rn(step, d.y));
-        v.z = __fadd_rn(v.z, __fmul_rn(step, d.z));
-        v.w = __fadd_rn(v.w, __fmul_rn(step, d.w));
+        v.x = euler_update(v.x, d.x, step);
+        v.y = euler_update(v.y, d.y, step);
+        v.z = euler_update(v.z, d.z, step);
+        v.w = euler_update(v.w, d.w, step);
         x4[i] = v;
     }
     for (long long i = 4 * n4 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        x[i] = __fadd_rn(x[i], __fmul_rn(step, dx[i]));
+        x[i] = euler_update(x[i], dx[i], step);
 }
 
 // FP64 self-energy Euler step; keeps the FP32 mirror (what get_state returns) in sync.
 __global__ void su2_euler_f64_kernel(double *__restrict__ x, const double *__restrict__ dx, float *__restrict__ xf, int n,
                                      float step) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const double v = x[i] + double(step) * dx[i];
+        const double v = euler_update_f64(x[i], dx[i], step);
         x[i] = v;
         xf[i] = float(v);
-    }
-}
-
-// ------------------------------------------------------------------------------------
-// correlation measurement (nu = 0), SU2MeasurementCorrelation.cpp:77-177
-// ------------------------------------------------------------------------------------
-struct CorrArgs {
-    int n, nl, n_corr;
-    float cutoff, spin;
-    const float *freq, *ss, *dd, *v2;
-    const double *v2d;  // FP64 self-energy, read instead of v2 when not NULL
-    const int *sites, *inv_sites, *corr_rid;
-    double *partial;  // [max_nodes][2][nl]
-    float *out;       // zz[n_corr], dd[n_corr], chi_s[nl], chi_d[nl]
-    int wsite;
-};
-
-__device__ __forceinline__ double corr_sigma(const CorrArgs &a, const float *pos, float w) {
-    return a.v2d ? odd_interp(pos, a.n, a.v2d, w) : odd_interp(pos, a.n, a.v2, w);
-}
-
-// Loop-frequency nodes of the measurement's trapezoid rules at nu = 0 (outer and inner
-// integrals use the same ranges): (-inf, -cutoff] and [cutoff, inf).
-__device__ int corr_nodes(const float *pos, int n, float cut, float *wp, double *w) {
-    int cnt = 0;
-    auto put = [&](float x, double c) {
-        wp[cnt] = x;
-        w[cnt] = c;
-        ++cnt;
-    };
-    if (-(0.0f + cut) > -pos[n - 1]) nodes_right(pos, n, -cut - 0.0f, put);
-    if (cut < pos[n - 1]) nodes_left(pos, n, cut, put);
-    return cnt;
-}
-
-constexpr int kMaxCorrNodes = 2 * kMaxFreq + 8;
-
-template <int SPT>
-__global__ void __launch_bounds__(128) su2_corr_inner_kernel(CorrArgs a) {
-    __shared__ float pos[kMaxFreq];
-    __shared__ float nwp[kMaxCorrNodes];
-    __shared__ double nw[kMaxCorrNodes];
-    __shared__ int ncnt;
-    __shared__ double red[4][2][32 * SPT];
-    for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
-    __syncthreads();
-    if (threadIdx.x == 0) ncnt = corr_nodes(pos, a.n, a.cutoff, nwp, nw);
-    __syncthreads();
-    const int ia = blockIdx.x;
-    if (ia >= ncnt) return;
-    const float w = nwp[ia];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int W = (SPT == 1) ? a.wsite : 32;
-    const int G = 32 / W;
-    const int g = lane / W, jl = lane - g * W;
-    const int nl = a.nl;
-    int site[SPT], isite[SPT];
-    bool valid[SPT];
-    for (int k = 0; k < SPT; ++k) {
-        const int j = jl + k * W;
-        valid[k] = j < nl;
-        site[k] = valid[k] ? a.sites[j] : 0;
-        isite[k] = valid[k] ? a.inv_sites[j] : 0;
-    }
-    const double S = a.spin;
-    auto sig = [&](float x) { return corr_sigma(a, pos, x); };
-    const double dw = double(w) + sig(w);
-    double acc_s[SPT], acc_d[SPT];
-    for (int k = 0; k < SPT; ++k) acc_s[k] = acc_d[k] = 0.0;
-    const int groups = kCorrWarps * G;
-    const int gid = warp * G + g;
-    for (int b = gid; b < ncnt; b += groups) {
-        const float wp = nwp[b];
-        AB8 ab;
-        access8(pos, a.n, nl, w + wp + 0.0f, 0.0f, w - wp, ab);
-        const float vs = value_none(pos, a.n, nl, a.ss, false, 0, 0, w + wp + 0.0f, w - wp, 0.0f);
-        const float vd = value_none(pos, a.n, nl, a.dd, true, 0, 0, w + wp + 0.0f, w - wp, 0.0f);
-        const double dwp = double(wp) + sig(wp);
-        const double norm = 1.0 / (dw * dw * dwp * dwp * (4.0 * kPiD * kPiD));
-        const double cw = nw[b] * norm;
-        for (int k = 0; k < SPT; ++k) {
-            const int st = ab.exch ? isite[k] : site[k];
-            float gs = 0.0f, gd = 0.0f;
-            for (int q = 0; q < 8; ++q) {
-                gs += ab.w[q] * __ldg(a.ss + ab.off[q] + st);
-                gd += ab.sw[q] * __ldg(a.dd + ab.off[q] + st);
-            }
-            double rs = -S * S * double(gs);
-            double rd = -16.0 * S * S * double(gd);
-            if (jl + k * W == 0) {
-                rs += S * (-double(vs) / 4.0 + double(vd));
-                rd += S * (3.0 * double(vs) + 4.0 * double(vd));
-            }
-            if (valid[k]) {
-                acc_s[k] += cw * rs;
-                acc_d[k] += cw * rd;
-            }
-        }
-    }
-    for (int k = 0; k < SPT; ++k) {
-        for (int o = W; o < 32; o <<= 1) {
-            acc_s[k] += __shfl_xor_sync(0xffffffffu, acc_s[k], o);
-            acc_d[k] += __shfl_xor_sync(0xffffffffu, acc_d[k], o);
-        }
-        if (g == 0) {
-            red[warp][0][jl + k * W] = acc_s[k];
-            red[warp][1][jl + k * W] = acc_d[k];
-        }
-    }
-    __syncthreads();
-    for (int j = threadIdx.x; j < nl; j += blockDim.x) {
-        double s = 0.0, d = 0.0;
-        for (int q = 0; q < kCorrWarps; ++q) {
-            s += red[q][0][j];
-            d += red[q][1][j];
-        }
-        a.partial[(size_t(ia) * 2 + 0) * nl + j] = s;
-        a.partial[(size_t(ia) * 2 + 1) * nl + j] = d;
-    }
-}
-
-__global__ void su2_corr_final_kernel(CorrArgs a) {
-    __shared__ float pos[kMaxFreq];
-    __shared__ float nwp[kMaxCorrNodes];
-    __shared__ double nw[kMaxCorrNodes];
-    __shared__ int ncnt;
-    extern __shared__ double chi[];  // [2][nl]
-    for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
-    __syncthreads();
-    if (threadIdx.x == 0) ncnt = corr_nodes(pos, a.n, a.cutoff, nwp, nw);
-    __syncthreads();
-    const double S = a.spin;
-    for (int j = threadIdx.x; j < a.nl; j += blockDim.x) {
-        double cs = 0.0, cd = 0.0;
-        for (int ia = 0; ia < ncnt; ++ia) {
-            double ls = a.partial[(size_t(ia) * 2 + 0) * a.nl + j];
-            double ld = a.partial[(size_t(ia) * 2 + 1) * a.nl + j];
-            if (j == 0) {
-                const float w = nwp[ia];
-                const double dw = double(w) + corr_sigma(a, pos, w);
-                const double t1 = 1.0 / (dw * dw);
-                ls += S * t1 / (2.0 * kPiD);
-                ld += 2.0 * S * t1 / kPiD;
-            }
-            cs += nw[ia] * ls;
-            cd += nw[ia] * ld;
-        }
-        chi[j] = cs;
-        chi[a.nl + j] = cd;
-        a.out[2 * a.n_corr + j] = float(cs);
-        a.out[2 * a.n_corr + a.nl + j] = float(cd);
-    }
-    __syncthreads();
-    for (int q = threadIdx.x; q < a.n_corr; q += blockDim.x) {
-        const int r = a.corr_rid[q];
-        a.out[q] = float(chi[r]);
-        a.out[a.n_corr + q] = float(chi[a.nl + r]);
     }
 }
 
@@ -327,9 +100,13 @@ __global__ void __launch_bounds__(256) fp32_peak_kernel(float *out, float seed) 
     if (s == 12345.678f) out[0] = s;  // keeps the chains live
 }
 
+}  // namespace
+
 // ------------------------------------------------------------------------------------
-// host helpers
+// host helpers (declared in su2_handle.cuh)
 // ------------------------------------------------------------------------------------
+namespace spn {
+
 void cuda_check(cudaError_t e, const char *what) {
     if (e != cudaSuccess) throw Error(ErrorType::Cuda, std::string(what) + ": " + cudaGetErrorString(e));
 }
@@ -343,100 +120,7 @@ int wsite_for(int nl) {
 
 int spt_for(int nl) { return nl <= 32 ? 1 : (nl <= 64 ? 2 : 4); }
 
-constexpr int kMaxSites = 128;
-
-}  // namespace
-
-// ------------------------------------------------------------------------------------
-// the flow handle
-// ------------------------------------------------------------------------------------
-struct spn_su2 {
-    int device = 0;
-    int n = 0, nl = 0, n_range = 0, n_corr = 0, max_nodes = 0, flags = 0, n_overlap = 0;
-    long long fn = 0;
-    float spin = 0.5f, cutoff = 0.0f;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    int vertex_grid = 0;
-    float *freq = nullptr, *ss = nullptr, *dd = nullptr, *dss = nullptr, *ddd = nullptr, *v2 = nullptr, *dv2 = nullptr;
-    float *node_wp = nullptr, *node_c = nullptr, *corr_out = nullptr;
-    int *node_cnt = nullptr, *work_counter = nullptr;
-    unsigned *status = nullptr;
-    int *sites = nullptr, *inv_sites = nullptr, *ov_ptr = nullptr, *ov_r1 = nullptr, *ov_r2 = nullptr;
-    int *range_rid = nullptr, *range_inv = nullptr, *corr_rid = nullptr;
-    double *corr_partial = nullptr;
-    double *v2d = nullptr, *dv2d = nullptr;  // FP64 self-energy (SPN_SU2_FP64_SELF_ENERGY)
-    int *rpa_sched = nullptr, *rpa_count = nullptr, *rpa_slot_base = nullptr, *rpa_seg_ptr = nullptr;
-    int rpa_lanes = 0, rpa_n_seg = 0, rpa_len = 0, rpa_in_smem = 0;
-    int vertex_npi = 1;       // loop-frequency nodes per site-group iteration
-    int sms = 0;
-    bool profiling = false;
-    std::vector<cudaEvent_t> ev_pool;
-    std::vector<std::pair<int, int>> ev_vertex, ev_step;  // indices into ev_pool
-
-    FlowArgs args() const {
-        FlowArgs a;
-        a.n = n;
-        a.nl = nl;
-        a.fn = int(fn);
-        a.wsite = wsite_for(nl);
-        a.max_nodes = max_nodes;
-        a.n_range = n_range;
-        a.cutoff = cutoff;
-        a.spin = spin;
-        a.freq = freq;
-        a.ss = ss;
-        a.dd = dd;
-        a.dss = dss;
-        a.ddd = ddd;
-        a.v2 = v2;
-        a.dv2 = dv2;
-        a.v2d = v2d;
-        a.dv2d = dv2d;
-        a.fp64_sigma = (flags & SPN_SU2_FP64_SELF_ENERGY) ? 1 : 0;
-        a.sites = sites;
-        a.inv_sites = inv_sites;
-        a.ov_ptr = ov_ptr;
-        a.ov_r1 = ov_r1;
-        a.ov_r2 = ov_r2;
-        a.range_rid = range_rid;
-        a.range_inv = range_inv;
-        a.node_wp = node_wp;
-        a.node_c = node_c;
-        a.node_cnt = node_cnt;
-        a.work_counter = work_counter;
-        a.status = status;
-        a.rpa.sched = rpa_sched;
-        a.rpa.count = rpa_count;
-        a.rpa.slot_base = rpa_slot_base;
-        a.rpa.seg_ptr = rpa_seg_ptr;
-        a.rpa.lanes = rpa_lanes;
-        a.rpa.n_seg = rpa_n_seg;
-        a.rpa.len = rpa_len;
-        a.rpa.in_smem = rpa_in_smem;
-        return a;
-    }
-
-    int event() {
-        cudaEvent_t e;
-        cuda_check(cudaEventCreate(&e), "cudaEventCreate");
-        ev_pool.push_back(e);
-        return int(ev_pool.size()) - 1;
-    }
-
-    void release() {
-        cudaSetDevice(device);
-        for (auto e : ev_pool) cudaEventDestroy(e);
-        ev_pool.clear();
-        void *ptrs[] = {freq,      ss,        dd,        dss,       ddd,          v2,          dv2,
-                        node_wp,   node_c,    corr_out,  node_cnt,  work_counter, status,      sites,
-                        inv_sites, ov_ptr,    ov_r1,     ov_r2,     range_rid,    range_inv,   corr_rid,
-                        corr_partial, rpa_sched, rpa_count, rpa_slot_base, rpa_seg_ptr, v2d, dv2d};
-        for (void *p : ptrs)
-            if (p) cudaFree(p);
-        if (own_stream && stream) cudaStreamDestroy(stream);
-    }
-};
+}  // namespace spn
 
 namespace {
 
@@ -608,9 +292,7 @@ extern "C" int spn_measure_fp32_peak(int device, double *tflops, double *sm_cloc
     });
 }
 
-extern "C" int spn_su2_create(const spn_su2_desc *d, spn_su2 **out) {
-    return guarded([&] {
-        if (!out) throw Error(ErrorType::Argument, "null output handle");
+spn_su2 *spn::create_flow(const spn_su2_desc *d, cudaStream_t stream) {
         validate_desc(d);
         auto *h = new spn_su2;
         try {
@@ -625,8 +307,13 @@ extern "C" int spn_su2_create(const spn_su2_desc *d, spn_su2 **out) {
             h->flags = d->flags;
             h->spin = d->spin_length;
             h->max_nodes = 2 * h->n + 8;
-            cuda_check(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "cudaStreamCreate");
-            h->own_stream = true;
+            if (stream) {
+                h->stream = stream;
+                h->own_stream = false;
+            } else {
+                cuda_check(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+                h->own_stream = true;
+            }
             const size_t vsz = size_t(h->fn) * h->nl;
             h->freq = dev_alloc<float>(h->n, "alloc freq");
             h->ss = dev_alloc<float>(vsz, "alloc v4ss");
@@ -697,7 +384,13 @@ extern "C" int spn_su2_create(const spn_su2_desc *d, spn_su2 **out) {
             delete h;
             throw;
         }
-        *out = h;
+        return h;
+}
+
+extern "C" int spn_su2_create(const spn_su2_desc *d, spn_su2 **out) {
+    return guarded([&] {
+        if (!out) throw Error(ErrorType::Argument, "null output handle");
+        *out = create_flow(d, nullptr);
     });
 }
 
@@ -904,7 +597,9 @@ extern "C" int spn_su2_finalize_step(spn_su2 *h, float new_cutoff) {
 
 namespace {
 
-void launch_correlation(spn_su2 *h) {
+}  // namespace
+
+CorrArgs spn::corr_args(const spn_su2 *h) {
         CorrArgs a;
         a.n = h->n;
         a.nl = h->nl;
@@ -922,6 +617,13 @@ void launch_correlation(spn_su2 *h) {
         a.partial = h->corr_partial;
         a.out = h->corr_out;
         a.wsite = wsite_for(h->nl);
+        return a;
+}
+
+namespace {
+
+void launch_correlation(spn_su2 *h) {
+        const CorrArgs a = corr_args(h);
         const int spt = spt_for(h->nl);
         const int blocks = 2 * h->n + 4;
         if (spt == 1) su2_corr_inner_kernel<1><<<blocks, 128, 0, h->stream>>>(a);

@@ -1,0 +1,119 @@
+// The flow handle of the C ABI (struct spn_su2) and the host helpers shared by the single-flow
+// entry points (su2_flow.cu) and the batch engine (su2_batch.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <string>
+#include <utility>
+#include <vector>
+#include "su2_common.cuh"
+#include "host/capi_common.hpp"
+#include "../../include/spn_su2.h"
+
+namespace spn {
+
+void cuda_check(cudaError_t e, const char *what);
+int wsite_for(int nl);  // lanes of a site group: next power of two >= nl (32 above 32 sites)
+int spt_for(int nl);    // sites per lane: 1, 2 or 4
+constexpr int kMaxSites = 128;
+
+}  // namespace spn
+
+struct spn_su2 {
+    int device = 0;
+    int n = 0, nl = 0, n_range = 0, n_corr = 0, max_nodes = 0, flags = 0, n_overlap = 0;
+    long long fn = 0;
+    float spin = 0.5f, cutoff = 0.0f;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int vertex_grid = 0;
+    float *freq = nullptr, *ss = nullptr, *dd = nullptr, *dss = nullptr, *ddd = nullptr, *v2 = nullptr, *dv2 = nullptr;
+    float *node_wp = nullptr, *node_c = nullptr, *corr_out = nullptr;
+    int *node_cnt = nullptr, *work_counter = nullptr;
+    unsigned *status = nullptr;
+    int *sites = nullptr, *inv_sites = nullptr, *ov_ptr = nullptr, *ov_r1 = nullptr, *ov_r2 = nullptr;
+    int *range_rid = nullptr, *range_inv = nullptr, *corr_rid = nullptr;
+    double *corr_partial = nullptr;
+    double *v2d = nullptr, *dv2d = nullptr;  // FP64 self-energy (SPN_SU2_FP64_SELF_ENERGY)
+    int *rpa_sched = nullptr, *rpa_count = nullptr, *rpa_slot_base = nullptr, *rpa_seg_ptr = nullptr;
+    int rpa_lanes = 0, rpa_n_seg = 0, rpa_len = 0, rpa_in_smem = 0;
+    int vertex_npi = 1;       // loop-frequency nodes per site-group iteration
+    int sms = 0;
+    bool profiling = false;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<int, int>> ev_vertex, ev_step;  // indices into ev_pool
+
+    spn::FlowArgs args() const {
+        spn::FlowArgs a;
+        a.n = n;
+        a.nl = nl;
+        a.fn = int(fn);
+        a.wsite = spn::wsite_for(nl);
+        a.max_nodes = max_nodes;
+        a.n_range = n_range;
+        a.cutoff = cutoff;
+        a.spin = spin;
+        a.freq = freq;
+        a.ss = ss;
+        a.dd = dd;
+        a.dss = dss;
+        a.ddd = ddd;
+        a.v2 = v2;
+        a.dv2 = dv2;
+        a.v2d = v2d;
+        a.dv2d = dv2d;
+        a.fp64_sigma = (flags & SPN_SU2_FP64_SELF_ENERGY) ? 1 : 0;
+        a.sites = sites;
+        a.inv_sites = inv_sites;
+        a.ov_ptr = ov_ptr;
+        a.ov_r1 = ov_r1;
+        a.ov_r2 = ov_r2;
+        a.range_rid = range_rid;
+        a.range_inv = range_inv;
+        a.node_wp = node_wp;
+        a.node_c = node_c;
+        a.node_cnt = node_cnt;
+        a.work_counter = work_counter;
+        a.status = status;
+        a.rpa.sched = rpa_sched;
+        a.rpa.count = rpa_count;
+        a.rpa.slot_base = rpa_slot_base;
+        a.rpa.seg_ptr = rpa_seg_ptr;
+        a.rpa.lanes = rpa_lanes;
+        a.rpa.n_seg = rpa_n_seg;
+        a.rpa.len = rpa_len;
+        a.rpa.in_smem = rpa_in_smem;
+        return a;
+    }
+
+    int event() {
+        cudaEvent_t e;
+        spn::cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+        ev_pool.push_back(e);
+        return int(ev_pool.size()) - 1;
+    }
+
+    void release() {
+        cudaSetDevice(device);
+        for (auto e : ev_pool) cudaEventDestroy(e);
+        ev_pool.clear();
+        void *ptrs[] = {freq,      ss,        dd,        dss,       ddd,          v2,          dv2,
+                        node_wp,   node_c,    corr_out,  node_cnt,  work_counter, status,      sites,
+                        inv_sites, ov_ptr,    ov_r1,     ov_r2,     range_rid,    range_inv,   corr_rid,
+                        corr_partial, rpa_sched, rpa_count, rpa_slot_base, rpa_seg_ptr, v2d, dv2d};
+        for (void *p : ptrs)
+            if (p) cudaFree(p);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+};
+
+
+namespace spn {
+
+// Allocates and initialises one flow (spn_su2_create); work is queued on `stream`, or on a
+// stream of its own when `stream` is NULL.
+spn_su2 *create_flow(const spn_su2_desc *d, cudaStream_t stream);
+// Argument block of the correlation measurement of a flow at its current cutoff.
+CorrArgs corr_args(const spn_su2 *h);
+// Builds the node tables and evaluates the vertex flow etc. of one flow: see su2_flow.cu.
+
+}  // namespace spn

@@ -315,17 +315,113 @@ __device__ __forceinline__ void channel_sum(const FlowArgs &a, const float *pos,
     }
 }
 
-// Shared memory: frequency mesh; the RPA schedule when it is staged; then per warp: 32 node
-// descriptors and, per node group, NPI t-channel exchange areas (four arrays of W*SPT sites
-// and n_seg slots each).
+// Shared memory of the single-flow kernel: frequency mesh; the RPA schedule when it is staged;
+// then per warp: 32 node descriptors and, per node group, NPI t-channel exchange areas (four
+// arrays of W*SPT sites and n_seg slots each).
 __host__ __device__ inline size_t node_area_bytes(int wsite, int spt, int n_seg) {
     return (sizeof(float) * 4 * size_t(wsite) * spt + sizeof(float2) * n_seg + 15) / 16 * 16;
 }
+__host__ __device__ inline size_t group_area_bytes(int wsite, int spt, int npi, int n_seg) {
+    return (32 / wsite) * npi * node_area_bytes(wsite, spt, n_seg);
+}
 __host__ __device__ inline size_t warp_bytes(int wsite, int spt, int npi, int n_seg) {
-    return kBatch * sizeof(NodeDesc) + (32 / wsite) * npi * node_area_bytes(wsite, spt, n_seg);
+    return kBatch * sizeof(NodeDesc) + group_area_bytes(wsite, spt, npi, n_seg);
 }
 __host__ __device__ inline size_t sched_bytes(const RpaSchedule &r, int nl) {
     return r.in_smem ? (sizeof(int) * size_t(rpa_smem_ints(r, nl)) + 15) / 16 * 16 : 0;
+}
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) / 16 * 16; }
+
+// What one warp needs to evaluate triples of one flow: lane roles, site indices and the
+// shared-memory areas.
+template <int SPT, int NPI>
+struct WarpCtx {
+    NodeDesc *desc;
+    TExchange tx[NPI];
+    Lane<SPT> ln;
+    int W, G, g, jl;
+};
+
+// `groups`: the warp's node-group areas; sched..seg_ptr: the RPA schedule (shared or global).
+template <int SPT, int NPI>
+__device__ __forceinline__ void setup_ctx(const FlowArgs &a, int lane, NodeDesc *desc, unsigned char *groups,
+                                          const int *sched, const int *count, const int *slot_base, const int *seg_ptr,
+                                          WarpCtx<SPT, NPI> &c) {
+    c.desc = desc;
+    c.W = (SPT == 1) ? a.wsite : 32;
+    c.G = 32 / c.W;
+    c.g = lane / c.W;
+    c.jl = lane - c.g * c.W;
+    const size_t nab = node_area_bytes(c.W, SPT, a.rpa.n_seg);
+    unsigned char *gbase = groups + size_t(c.g) * NPI * nab;
+    const int ws = c.W * SPT;
+#pragma unroll
+    for (int n = 0; n < NPI; ++n) {
+        float *gx = reinterpret_cast<float *>(gbase + n * nab);
+        c.tx[n].As = gx;
+        c.tx[n].Ad = gx + ws;
+        c.tx[n].Bs = gx + 2 * ws;
+        c.tx[n].Bd = gx + 3 * ws;
+        c.tx[n].slots = reinterpret_cast<float2 *>(gx + 4 * ws);
+        c.tx[n].sched = sched;
+        c.tx[n].count = count;
+        c.tx[n].slot_base = slot_base;
+        c.tx[n].seg_ptr = seg_ptr;
+    }
+#pragma unroll
+    for (int k = 0; k < SPT; ++k) {
+        const int j = c.jl + k * c.W;
+        c.ln.j[k] = j;
+        c.ln.valid[k] = j < a.nl;
+        c.ln.site[k] = c.ln.valid[k] ? a.sites[j] : 0;
+        c.ln.isite[k] = c.ln.valid[k] ? a.inv_sites[j] : 0;
+    }
+}
+
+// The flow of triple `it` of flow `a` (all lanes of the warp take part).  The single-flow and
+// the batched kernel both evaluate triples with this function, so a flow's result does not
+// depend on the kernel, the launch or the other flows of a batch.
+template <int SPT, int NPI>
+__device__ __forceinline__ void vertex_triple(const FlowArgs &a, const float *pos, int it, const WarpCtx<SPT, NPI> &c,
+                                              int lane) {
+    const float two_pi = 2.0f * float(kPi);
+    const int su = it / a.n, ti = it - su * a.n;
+    int si = int((sqrtf(8.0f * float(su) + 1.0f) - 1.0f) * 0.5f);
+    while (si * (si + 1) / 2 > su) --si;
+    while ((si + 1) * (si + 2) / 2 <= su) ++si;
+    const int ui = su - si * (si + 1) / 2;
+
+    Transfer f;
+    f.s = pos[si];
+    f.t = pos[ti];
+    f.u = pos[ui];
+    f.w1p = 0.5f * (f.s + f.t + f.u);
+    f.w1 = 0.5f * (f.s - f.t + f.u);
+    f.w2p = 0.5f * (f.s - f.t - f.u);
+    f.w2 = 0.5f * (f.s + f.t - f.u);
+
+    float acc_s[SPT], cmp_s[SPT], acc_d[SPT], cmp_d[SPT];
+#pragma unroll
+    for (int k = 0; k < SPT; ++k) acc_s[k] = cmp_s[k] = acc_d[k] = cmp_d[k] = 0.0f;
+    channel_sum<kS, SPT, NPI>(a, pos, f, si, lane, c.g, c.G, c.jl, c.ln, c.desc, c.tx, acc_s, cmp_s, acc_d, cmp_d);
+    channel_sum<kT, SPT, NPI>(a, pos, f, ti, lane, c.g, c.G, c.jl, c.ln, c.desc, c.tx, acc_s, cmp_s, acc_d, cmp_d);
+    channel_sum<kU, SPT, NPI>(a, pos, f, ui, lane, c.g, c.G, c.jl, c.ln, c.desc, c.tx, acc_s, cmp_s, acc_d, cmp_d);
+
+#pragma unroll
+    for (int k = 0; k < SPT; ++k) {
+        float vs = acc_s[k] - cmp_s[k], vd = acc_d[k] - cmp_d[k];
+        for (int o = c.W; o < 32; o <<= 1) {
+            vs += __shfl_xor_sync(0xffffffffu, vs, o);
+            vd += __shfl_xor_sync(0xffffffffu, vd, o);
+        }
+        if (c.g == 0 && c.ln.valid[k]) {
+            const float os = vs / two_pi, od = vd / two_pi;
+            const size_t idx = size_t(it) * a.nl + c.ln.j[k];
+            a.dss[idx] = os;
+            a.ddd[idx] = od;
+            if (isnan(os) || isnan(od)) atomicOr(a.status, kStatusNaN);
+        }
+    }
 }
 
 template <int SPT, int NPI>
@@ -336,8 +432,6 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_flow_kernel(FlowArgs a) {
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int W = (SPT == 1) ? a.wsite : 32;
-    const int G = 32 / W;
-    const int g = lane / W, jl = lane - g * W;
     const int n_seg = a.rpa.n_seg;
     unsigned char *sbase = smem_raw + kMaxFreq * sizeof(float);
     const int *sched, *count, *slot_base, *seg_ptr;
@@ -361,79 +455,67 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_flow_kernel(FlowArgs a) {
         seg_ptr = a.rpa.seg_ptr;
     }
     unsigned char *wbase = sbase + sched_bytes(a.rpa, a.nl) + warp * warp_bytes(W, SPT, NPI, n_seg);
-    NodeDesc *desc = reinterpret_cast<NodeDesc *>(wbase);
-    const size_t nab = node_area_bytes(W, SPT, n_seg);
-    unsigned char *gbase = wbase + kBatch * sizeof(NodeDesc) + size_t(g) * NPI * nab;
-    const int ws = W * SPT;
-    TExchange tx[NPI];
-#pragma unroll
-    for (int n = 0; n < NPI; ++n) {
-        float *gx = reinterpret_cast<float *>(gbase + n * nab);
-        tx[n].As = gx;
-        tx[n].Ad = gx + ws;
-        tx[n].Bs = gx + 2 * ws;
-        tx[n].Bd = gx + 3 * ws;
-        tx[n].slots = reinterpret_cast<float2 *>(gx + 4 * ws);
-        tx[n].sched = sched;
-        tx[n].count = count;
-        tx[n].slot_base = slot_base;
-        tx[n].seg_ptr = seg_ptr;
-    }
+    WarpCtx<SPT, NPI> c;
+    setup_ctx<SPT, NPI>(a, lane, reinterpret_cast<NodeDesc *>(wbase), wbase + kBatch * sizeof(NodeDesc), sched, count,
+                        slot_base, seg_ptr, c);
     __syncthreads();
-
-    Lane<SPT> ln;
-#pragma unroll
-    for (int k = 0; k < SPT; ++k) {
-        const int j = jl + k * W;
-        ln.j[k] = j;
-        ln.valid[k] = j < a.nl;
-        ln.site[k] = ln.valid[k] ? a.sites[j] : 0;
-        ln.isite[k] = ln.valid[k] ? a.inv_sites[j] : 0;
-    }
-    const float two_pi = 2.0f * float(kPi);
 
     for (;;) {
         int it = 0;
         if (lane == 0) it = atomicAdd(a.work_counter, 1);
         it = __shfl_sync(0xffffffffu, it, 0);
         if (it >= a.fn) break;
-        const int su = it / a.n, ti = it - su * a.n;
-        int si = int((sqrtf(8.0f * float(su) + 1.0f) - 1.0f) * 0.5f);
-        while (si * (si + 1) / 2 > su) --si;
-        while ((si + 1) * (si + 2) / 2 <= su) ++si;
-        const int ui = su - si * (si + 1) / 2;
+        vertex_triple<SPT, NPI>(a, pos, it, c, lane);
+    }
+}
 
-        Transfer f;
-        f.s = pos[si];
-        f.t = pos[ti];
-        f.u = pos[ui];
-        f.w1p = 0.5f * (f.s + f.t + f.u);
-        f.w1 = 0.5f * (f.s - f.t + f.u);
-        f.w2p = 0.5f * (f.s - f.t - f.u);
-        f.w2 = 0.5f * (f.s + f.t - f.u);
+// Batched vertex flow: a persistent grid over the ragged list of (flow, triple) items of all
+// flows of one site class.  A warp keeps the flow it works on (argument block, frequency
+// mesh, lane roles) in its own shared-memory area and reloads it only when an item of another
+// flow comes up; items are numbered flow by flow, so that happens rarely.  The RPA schedule
+// is read from global memory (it differs between flows).
+template <int SPT, int NPI>
+__global__ void __launch_bounds__(kThreads) su2_vertex_batch_kernel(BatchVertexArgs b) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const size_t fa_bytes = align16(sizeof(FlowArgs)), pos_bytes = align16(sizeof(float) * b.n_max);
+    unsigned char *wbase = smem_raw + size_t(warp) * (fa_bytes + pos_bytes + kBatch * sizeof(NodeDesc) + b.warp_area);
+    FlowArgs *fa = reinterpret_cast<FlowArgs *>(wbase);
+    float *pos = reinterpret_cast<float *>(wbase + fa_bytes);
+    NodeDesc *desc = reinterpret_cast<NodeDesc *>(wbase + fa_bytes + pos_bytes);
+    unsigned char *groups = wbase + fa_bytes + pos_bytes + kBatch * sizeof(NodeDesc);
 
-        float acc_s[SPT], cmp_s[SPT], acc_d[SPT], cmp_d[SPT];
-#pragma unroll
-        for (int k = 0; k < SPT; ++k) acc_s[k] = cmp_s[k] = acc_d[k] = cmp_d[k] = 0.0f;
-        channel_sum<kS, SPT, NPI>(a, pos, f, si, lane, g, G, jl, ln, desc, tx, acc_s, cmp_s, acc_d, cmp_d);
-        channel_sum<kT, SPT, NPI>(a, pos, f, ti, lane, g, G, jl, ln, desc, tx, acc_s, cmp_s, acc_d, cmp_d);
-        channel_sum<kU, SPT, NPI>(a, pos, f, ui, lane, g, G, jl, ln, desc, tx, acc_s, cmp_s, acc_d, cmp_d);
-
-#pragma unroll
-        for (int k = 0; k < SPT; ++k) {
-            float vs = acc_s[k] - cmp_s[k], vd = acc_d[k] - cmp_d[k];
-            for (int o = W; o < 32; o <<= 1) {
-                vs += __shfl_xor_sync(0xffffffffu, vs, o);
-                vd += __shfl_xor_sync(0xffffffffu, vd, o);
-            }
-            if (g == 0 && ln.valid[k]) {
-                const float os = vs / two_pi, od = vd / two_pi;
-                const size_t idx = size_t(it) * a.nl + ln.j[k];
-                a.dss[idx] = os;
-                a.ddd[idx] = od;
-                if (isnan(os) || isnan(od)) atomicOr(a.status, kStatusNaN);
-            }
+    WarpCtx<SPT, NPI> c;
+    int cur = -1, base = 0;
+    bool skip = false;
+    for (;;) {
+        int w = 0;
+        if (lane == 0) w = atomicAdd(b.counter, 1);
+        w = __shfl_sync(0xffffffffu, w, 0);
+        if (w >= b.total) break;
+        int lo = 0, hi = b.n_list - 1;  // last f with prefix[f] <= w
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(b.prefix + mid) <= w) lo = mid;
+            else hi = mid - 1;
         }
+        if (lo != cur) {
+            cur = lo;
+            base = __ldg(b.prefix + lo);
+            const BatchFlow *bf = b.flows + __ldg(b.list + lo);
+            __syncwarp();
+            const int *src = reinterpret_cast<const int *>(&bf->a);
+            int *dst = reinterpret_cast<int *>(fa);
+            for (int i = lane; i < int(sizeof(FlowArgs) / sizeof(int)); i += 32) dst[i] = src[i];
+            skip = bf->phase != kPhaseFlowing;
+            __syncwarp();
+            for (int i = lane; i < fa->n; i += 32) pos[i] = fa->freq[i];
+            setup_ctx<SPT, NPI>(*fa, lane, desc, groups, fa->rpa.sched, fa->rpa.count, fa->rpa.slot_base,
+                                fa->rpa.seg_ptr, c);
+            __syncwarp();
+        }
+        if (skip) continue;
+        vertex_triple<SPT, NPI>(*fa, pos, w - base, c, lane);
     }
 }
 
@@ -477,6 +559,41 @@ void launch_vertex_flow(const FlowArgs &a, int npi, int grid, cudaStream_t strea
     VertexKernel k = vertex_kernel(spt_of(a.nl), npi);
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     k<<<grid, kThreads, smem, stream>>>(a);
+}
+
+int vertex_spt(int nl) { return spt_of(nl); }
+
+size_t batch_vertex_warp_area(int nl, int n_seg, int npi) {
+    const int spt = spt_of(nl);
+    return group_area_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, n_seg);
+}
+
+size_t batch_vertex_smem_bytes(int n_max, size_t warp_area) {
+    return kWarps * (align16(sizeof(FlowArgs)) + align16(sizeof(float) * n_max) + kBatch * sizeof(NodeDesc) + warp_area);
+}
+
+namespace {
+using BatchKernel = void (*)(BatchVertexArgs);
+BatchKernel batch_kernel(int spt, int npi) {
+    if (spt == 1) return npi == 1 ? su2_vertex_batch_kernel<1, 1> : su2_vertex_batch_kernel<1, 2>;
+    if (spt == 2) return npi == 1 ? su2_vertex_batch_kernel<2, 1> : su2_vertex_batch_kernel<2, 2>;
+    return npi == 1 ? su2_vertex_batch_kernel<4, 1> : su2_vertex_batch_kernel<4, 2>;
+}
+}  // namespace
+
+int batch_vertex_blocks_per_sm(int spt, int npi, size_t smem) {
+    BatchKernel k = batch_kernel(spt, npi);
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess) return -1;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, smem) != cudaSuccess) return -1;
+    return per_sm;
+}
+
+// The kernel's shared-memory limit is raised by batch_vertex_blocks_per_sm when the plan is
+// built, so this launch can be captured into a graph.
+void launch_batch_vertex(const BatchVertexArgs &b, int spt, int npi, int grid, cudaStream_t stream) {
+    const size_t smem = batch_vertex_smem_bytes(b.n_max, size_t(b.warp_area));
+    batch_kernel(spt, npi)<<<grid, kThreads, smem, stream>>>(b);
 }
 
 }  // namespace spn
