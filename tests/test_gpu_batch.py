@@ -62,7 +62,7 @@ def assert_same(batch, fid, ref, name):
     assert r.diverged == ref["div"], name
     assert np.array_equal(r.cutoffs, ref["cut"]), name
     for key, got in (("zz", r.zz), ("dd", r.dd), ("cz", r.chi_zz), ("cd", r.chi_dd)):
-        assert np.array_equal(got, ref[key].reshape(got.shape)), (name, key)
+        assert np.array_equal(got, ref[key].reshape(got.shape), equal_nan=True), (name, key)
     if not ref["div"]:
         c, v2, ss, sd = batch.state(fid)
         rc, rv2, rss, rsd = ref["state"]
