@@ -53,6 +53,8 @@ WORKLOADS = {
                               n_freq=64, fmin=0.002, fmax=100.0, cmax=100.0, cmin=0.01, cstep=0.99),
 }
 DEFAULT_WORKLOAD = "cubic-j1j2-r6-n64"
+# multi-flow workloads (spinparser_gb300/workloads.py): the seeded scan and the serving stream
+MULTI_WORKLOADS = ("scan-square-j1j2-128", "serve-mixed")
 METRIC = "cutoff steps/s per flow"
 KERNELS_PER_STEP = 8  # self-energy, node tables, vertex flow, 2 x correlation, 3 x Euler
 
@@ -63,7 +65,10 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + list(MULTI_WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--flows", type=int, default=None, help="multi-flow workloads: number of flows / requests")
+    ap.add_argument("--rates", type=str, default="0.5,1,2,4,inf",
+                    help="serve-mixed: arrival rates as multiples of the sequential plain-GPU capacity")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU work budget of the baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -221,8 +226,143 @@ def run_reference(args, wl):
     print(json.dumps(line))
 
 
+def _plain_solve(spec):
+    """One request solved alone on the plain single-flow path (tables, flow, full cutoff loop)."""
+    import spinparser_gb300 as spn
+    from spinparser_gb300.driver import run_flow
+
+    tab, freq, cut = spec.build()
+    flow = spn.Su2Flow(tab, freq, flags=spec.flags)
+    meas, zz, dd, cz, cd, div = run_flow(flow, cut, tab.initial_state(len(freq)))
+    flow.close()
+    return meas, zz, dd, div
+
+
+def _cpu_flow_seconds(specs, budget_s):
+    """CPU oracle time of whole flows, per distinct (lattice, range, N): the per-step time from
+    a bounded triple sample at the four baseline cutoffs, times the flow's steps."""
+    classes = {}
+    for sp in specs:
+        classes.setdefault((sp.lattice, sp.range, sp.model, sp.n_freq), []).append(sp)
+    per_class = budget_s / max(1, len(classes))
+    total, samples = 0.0, []
+    for (lat, rng_, model, n), members in classes.items():
+        sp = members[0]
+        tab, freq, cut = sp.build()
+        b = cpu_baseline(tab, freq, baseline_cutoffs(cut), tab.initial_state(len(freq)), per_class)
+        t_step = 1.0 / b["value"]
+        total += t_step * (len(cut) - 1) * len(members)
+        samples.append(f"{lat} r{rng_} N{n}: {t_step:.2f} s/step x {len(members)}")
+    return total, samples, b["cores"]
+
+
+def _check_same(a, b):
+    """Largest absolute difference of two flows' correlations (0.0 = bit-identical)."""
+    am, azz, add_, _ = a
+    if len(am) != len(b.cutoffs) or not np.array_equal(am, b.cutoffs):
+        return float("inf")
+    return float(max(np.nanmax(np.abs(azz.reshape(b.zz.shape) - b.zz)), np.nanmax(np.abs(add_.reshape(b.dd.shape) - b.dd))))
+
+
+def run_multi(args):
+    """Multi-flow workloads: batched / served flows against sequential plain-GPU solves."""
+    import torch
+
+    from spinparser_gb300 import workloads
+    from spinparser_gb300.serve import FlowServer, time_to_result_stats
+
+    torch.cuda.set_device(0)
+    scan = args.workload.startswith("scan")
+    n = args.flows or (128 if scan else 24)
+    specs = workloads.scan_specs(n) if scan else workloads.serve_specs(n)
+    # warm-up (untimed): kernels loaded, caches warm, allocator primed
+    warm = [workloads.FlowSpec("square", 3, "square-j1j2heisenberg", (("j1", "1.0"), ("j2", "0.3")), 16,
+                               0.005, 50.0, 50.0, 5.0, 0.9)] * 3
+    for sp in warm:
+        _plain_solve(sp)
+    srv = FlowServer()
+    for sp in warm:
+        srv.submit(sp)
+    srv.drain()
+    srv.close()
+
+    sampler = ClockSampler(0)
+    sampler.start()
+    # sequential plain-GPU solves (FIFO, all requests present at t = 0)
+    plain, plain_done = [], []
+    t0 = time.perf_counter()
+    for sp in specs:
+        ts = time.perf_counter()
+        plain.append(_plain_solve(sp))
+        plain_done.append((time.perf_counter() - t0, time.perf_counter() - ts))
+    t_plain = time.perf_counter() - t0
+    service = np.array([d[1] for d in plain_done])
+    arms = {}
+    rates = [float("inf")] if scan else [float(x) * (1.0 / service.mean()) for x in args.rates.split(",")]
+    max_diff = 0.0
+    for rate in rates:
+        arrivals = workloads.poisson_arrivals(n, rate)
+        srv = FlowServer()
+        t0 = time.perf_counter()
+        tickets = []
+        i = 0
+        while True:
+            now = time.perf_counter() - t0
+            while i < n and arrivals[i] <= now:
+                tickets.append(srv.submit(specs[i], t_arrival=t0 + arrivals[i]))
+                i += 1
+            busy = srv.pump()
+            if busy == 0:
+                if i >= n:
+                    break
+                time.sleep(min(0.01, max(0.0, arrivals[i] - (time.perf_counter() - t0))))
+        makespan = time.perf_counter() - t0
+        for t in tickets:
+            max_diff = max(max_diff, _check_same(plain[t.id], t.result))
+        # the same arrivals served by the sequential plain path (FIFO queue of its service times)
+        free_at, plain_ttr = 0.0, []
+        for k in range(n):
+            start = max(free_at, arrivals[k])
+            free_at = start + service[k]
+            plain_ttr.append(free_at - arrivals[k])
+        arms["inf" if not np.isfinite(rate) else f"{rate:.4g}"] = {
+            "arrival_rate_per_s": None if not np.isfinite(rate) else rate,
+            "batched": {"flows_per_s": n / makespan, "makespan_s": makespan, "steps": srv.steps,
+                        **time_to_result_stats(tickets)},
+            "plain_gpu_fifo": {"flows_per_s": n / max(free_at, 1e-9), "makespan_s": free_at,
+                               "p50_s": float(np.percentile(plain_ttr, 50)), "p99_s": float(np.percentile(plain_ttr, 99))},
+        }
+        srv.close()
+    clocks = sampler.stop()
+    cpu_s, cpu_samples, cores = _cpu_flow_seconds(specs, args.cpu_seconds) if not args.no_cpu_baseline else (None, [], 0)
+    top = arms[list(arms)[-1]]
+    line = {
+        "metric": "scan flows/s" if scan else "served flows/s",
+        "value": top["batched"]["flows_per_s"], "unit": "flows/s", "n_gpus": 1,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "flows": n, "seed": workloads.SEED,
+                   "draws": "square J1-J2, J2 U[0,1], range U{3,5,7}, N U{32,48,64}, grid [0.005,50], cutoff 50->0.05 x0.98"
+                   if scan else "square/cubic/pyrochlore J1-J2, J2 U[-0.5,0.5], range U{3..7}, N U{32,48,64}, "
+                                "grid [0.005,50], cutoff 50->0.05 x0.98, Poisson arrivals"},
+        "plain_gpu_sequential": {"flows_per_s": n / t_plain, "seconds": t_plain,
+                                 "service_s_mean": float(service.mean()), "service_s_max": float(service.max())},
+        "speedup_vs_plain": top["batched"]["flows_per_s"] / (n / t_plain),
+        "arms": arms,
+        "max_abs_diff_vs_plain": max_diff,
+        "cpu_baseline": None if cpu_s is None else {
+            "value": n / cpu_s, "unit": "flows/s", "cores": cores, "kind": "port",
+            "sample": "per (lattice, range, N): oracle step time from a bounded triple sample at 4 cutoffs x steps; "
+                      + "; ".join(cpu_samples)},
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
 def main():
     args = parse_args()
+    if args.workload in MULTI_WORKLOADS:
+        run_multi(args)
+        return
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args, wl)

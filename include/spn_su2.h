@@ -40,6 +40,8 @@ int spn_last_error(char *buf, size_t len);
 
 /* Library / device information: number of CUDA devices visible (0 without a GPU). */
 int spn_device_count(int *count);
+/* Free and total device memory in bytes (the admission budget of a serving loop). */
+int spn_device_memory(int device, long long *free_bytes, long long *total_bytes);
 
 /* Measured FP32 FMA throughput of a device (TFLOP/s, best of several runs of a pure-FFMA
  * kernel) and the SM clock it implies.  The vertex-flow kernel runs on the FP32 CUDA cores;

@@ -31,6 +31,7 @@ using namespace spn::dev;
 namespace {
 
 constexpr int kClasses = 3;  // sites per lane 1, 2, 4
+constexpr int kBatchSchedMaxInts = 3072;  // per-warp staged RPA schedule (12 KB) at most
 
 __global__ void batch_prepare_kernel(BatchFlow *flows, const int *list, int n, int *counters) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -191,7 +192,7 @@ struct spn_batch {
     int off_flowing = 0, off_measure = 0;
     int off_cm[kClasses] = {}, n_cm[kClasses] = {};
     int off_cv[kClasses] = {}, n_cv[kClasses] = {}, off_cp[kClasses] = {}, total_cv[kClasses] = {};
-    int warp_area[kClasses] = {}, nl_max = 1, vgrid[kClasses] = {};
+    int warp_area[kClasses] = {}, nl_max = 1, vgrid[kClasses] = {}, sched_ints[kClasses] = {};
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     long long steps_run = 0, graph_builds = 0;
@@ -310,19 +311,23 @@ struct spn_batch {
             n_cv[c] = int(cv[c].size());
             std::vector<int> prefix(1, 0);
             size_t area = 0;
+            int sched = 0;
             for (int i : cv[c]) {
                 const spn_su2 *h = flows[i].h;
                 const long long next = prefix.back() + h->fn;
                 if (next >= (1ll << 31)) throw Error(ErrorType::Unsupported, "batch work list beyond 2^31 items");
                 prefix.push_back(int(next));
                 area = std::max(area, batch_vertex_warp_area(h->nl, h->rpa_n_seg, npi));
+                sched = std::max(sched, rpa_smem_ints(h->args().rpa, h->nl));
             }
             off_cp[c] = put(prefix);
             total_cv[c] = prefix.back();
             warp_area[c] = int((area + 15) / 16 * 16);
+            // each warp stages its flow's RPA schedule when the largest one is small
+            sched_ints[c] = sched <= kBatchSchedMaxInts ? sched : 0;
             vgrid[c] = 0;
             if (n_cv[c] > 0) {
-                const size_t smem = batch_vertex_smem_bytes(n_max, warp_area[c]);
+                const size_t smem = batch_vertex_smem_bytes(n_max, warp_area[c], sched_ints[c]);
                 const int per_sm = batch_vertex_blocks_per_sm(1 << c, npi, smem);
                 cudaGetLastError();
                 if (per_sm < 1) throw Error(ErrorType::Unsupported, "batched vertex-flow kernel does not fit for this batch");
@@ -364,6 +369,7 @@ struct spn_batch {
                 b.n_max = n_max;
                 b.counter = d_counters + c;
                 b.warp_area = warp_area[c];
+                b.sched_ints = sched_ints[c];
                 launch_batch_vertex(b, 1 << c, npi, vgrid[c], stream);
             }
         }

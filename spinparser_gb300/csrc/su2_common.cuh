@@ -101,15 +101,18 @@ constexpr int kRpaSmemMaxInts = 8192;
 // site class (spt = 1, 2 or 4 sites per lane).  Work item w belongs to flow list[f] with
 // prefix[f] <= w < prefix[f+1] (prefix[f+1] - prefix[f] = that flow's triple count).
 // `warp_area` is the per-warp shared-memory bytes the largest flow of the list needs.
+// `sched_ints` > 0: each warp stages the RPA schedule of its current flow in shared memory
+// (room for that many ints; every flow of the list must fit), else it reads global memory.
 struct BatchVertexArgs {
     BatchFlow *flows;
     const int *list, *prefix;
     int n_list, total, n_max;
     int *counter;
     int warp_area;
+    int sched_ints;
 };
 size_t batch_vertex_warp_area(int nl, int n_seg, int npi);
-size_t batch_vertex_smem_bytes(int n_max, size_t warp_area);
+size_t batch_vertex_smem_bytes(int n_max, size_t warp_area, int sched_ints);
 int batch_vertex_blocks_per_sm(int spt, int npi, size_t smem);
 void launch_batch_vertex(const BatchVertexArgs &b, int spt, int npi, int grid, cudaStream_t stream);
 int vertex_spt(int nl);  // sites per lane of a flow with nl sites

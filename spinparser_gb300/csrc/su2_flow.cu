@@ -260,6 +260,16 @@ extern "C" int spn_device_count(int *count) {
     });
 }
 
+extern "C" int spn_device_memory(int device, long long *free_bytes, long long *total_bytes) {
+    return guarded([&] {
+        cuda_check(cudaSetDevice(device), "cudaSetDevice");
+        size_t f = 0, t = 0;
+        cuda_check(cudaMemGetInfo(&f, &t), "cudaMemGetInfo");
+        if (free_bytes) *free_bytes = (long long)f;
+        if (total_bytes) *total_bytes = (long long)t;
+    });
+}
+
 extern "C" int spn_measure_fp32_peak(int device, double *tflops, double *sm_clock_ghz_est) {
     return guarded([&] {
         if (!tflops) throw Error(ErrorType::Argument, "null output");
@@ -375,8 +385,9 @@ spn_su2 *spn::create_flow(const spn_su2_desc *d, cudaStream_t stream) {
             int sms = 0;
             cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device), "device attribute");
             h->sms = sms;
-            // default variant; spn_su2_autotune can pick a faster one for this flow
-            if (!select_variant(h, 1, 0) && !select_variant(h, 1, 1))
+            // default variant (schedule staged in shared memory where it fits); spn_su2_autotune
+            // can pick a faster one for this flow
+            if (!select_variant(h, 1, 1) && !select_variant(h, 1, 0))
                 throw Error(ErrorType::Unsupported, "vertex-flow kernel does not fit on this device");
             cuda_check(cudaStreamSynchronize(h->stream), "create sync");
         } catch (...) {

@@ -479,11 +479,14 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_batch_kernel(BatchVertexA
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const size_t fa_bytes = align16(sizeof(FlowArgs)), pos_bytes = align16(sizeof(float) * b.n_max);
-    unsigned char *wbase = smem_raw + size_t(warp) * (fa_bytes + pos_bytes + kBatch * sizeof(NodeDesc) + b.warp_area);
+    const size_t sch_bytes = align16(sizeof(int) * size_t(b.sched_ints));
+    unsigned char *wbase =
+        smem_raw + size_t(warp) * (fa_bytes + pos_bytes + sch_bytes + kBatch * sizeof(NodeDesc) + b.warp_area);
     FlowArgs *fa = reinterpret_cast<FlowArgs *>(wbase);
     float *pos = reinterpret_cast<float *>(wbase + fa_bytes);
-    NodeDesc *desc = reinterpret_cast<NodeDesc *>(wbase + fa_bytes + pos_bytes);
-    unsigned char *groups = wbase + fa_bytes + pos_bytes + kBatch * sizeof(NodeDesc);
+    int *sch = reinterpret_cast<int *>(wbase + fa_bytes + pos_bytes);
+    NodeDesc *desc = reinterpret_cast<NodeDesc *>(wbase + fa_bytes + pos_bytes + sch_bytes);
+    unsigned char *groups = wbase + fa_bytes + pos_bytes + sch_bytes + kBatch * sizeof(NodeDesc);
 
     WarpCtx<SPT, NPI> c;
     int cur = -1, base = 0;
@@ -510,8 +513,20 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_batch_kernel(BatchVertexA
             skip = bf->phase != kPhaseFlowing;
             __syncwarp();
             for (int i = lane; i < fa->n; i += 32) pos[i] = fa->freq[i];
-            setup_ctx<SPT, NPI>(*fa, lane, desc, groups, fa->rpa.sched, fa->rpa.count, fa->rpa.slot_base,
-                                fa->rpa.seg_ptr, c);
+            if (b.sched_ints > 0) {  // the host checked that every flow's schedule fits
+                const RpaSchedule &r = fa->rpa;
+                const int ns = r.len * r.lanes, nc = r.lanes;
+                for (int i = lane; i < ns; i += 32) sch[i] = __ldg(r.sched + i);
+                for (int i = lane; i < nc; i += 32) {
+                    sch[ns + i] = __ldg(r.count + i);
+                    sch[ns + nc + i] = __ldg(r.slot_base + i);
+                }
+                for (int i = lane; i <= fa->nl; i += 32) sch[ns + 2 * nc + i] = __ldg(r.seg_ptr + i);
+                setup_ctx<SPT, NPI>(*fa, lane, desc, groups, sch, sch + ns, sch + ns + nc, sch + ns + 2 * nc, c);
+            } else {
+                setup_ctx<SPT, NPI>(*fa, lane, desc, groups, fa->rpa.sched, fa->rpa.count, fa->rpa.slot_base,
+                                    fa->rpa.seg_ptr, c);
+            }
             __syncwarp();
         }
         if (skip) continue;
@@ -568,8 +583,9 @@ size_t batch_vertex_warp_area(int nl, int n_seg, int npi) {
     return group_area_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, n_seg);
 }
 
-size_t batch_vertex_smem_bytes(int n_max, size_t warp_area) {
-    return kWarps * (align16(sizeof(FlowArgs)) + align16(sizeof(float) * n_max) + kBatch * sizeof(NodeDesc) + warp_area);
+size_t batch_vertex_smem_bytes(int n_max, size_t warp_area, int sched_ints) {
+    return kWarps * (align16(sizeof(FlowArgs)) + align16(sizeof(float) * n_max) + align16(sizeof(int) * size_t(sched_ints)) +
+                     kBatch * sizeof(NodeDesc) + warp_area);
 }
 
 namespace {
@@ -592,7 +608,7 @@ int batch_vertex_blocks_per_sm(int spt, int npi, size_t smem) {
 // The kernel's shared-memory limit is raised by batch_vertex_blocks_per_sm when the plan is
 // built, so this launch can be captured into a graph.
 void launch_batch_vertex(const BatchVertexArgs &b, int spt, int npi, int grid, cudaStream_t stream) {
-    const size_t smem = batch_vertex_smem_bytes(b.n_max, size_t(b.warp_area));
+    const size_t smem = batch_vertex_smem_bytes(b.n_max, size_t(b.warp_area), b.sched_ints);
     batch_kernel(spt, npi)<<<grid, kThreads, smem, stream>>>(b);
 }
 

@@ -1,0 +1,158 @@
+"""Serving SU(2) flows: continuous batching over one GPU (``Su2Batch``).
+
+Requests (``FlowSpec``: lattice, range, model, couplings, frequency grid, cutoff list) are
+queued as they arrive.  Between batch steps the server admits queued requests in arrival order
+while their device footprint fits the memory budget (and, optionally, a flow-count limit);
+every admitted flow keeps its vertex and self-energy state resident on the device until it
+finishes, and all resident flows advance together, one cutoff step per batch step.  Finished
+flows are retired at once (results copied out, memory released) so that waiting requests take
+their place.  Each ticket records its arrival, admission and completion time; the time to
+result is completion minus arrival.
+
+A flow's results do not depend on the company it keeps in the batch (the batch engine
+evaluates every flow with the single-flow device code), so serving changes when a result
+arrives, never what it is.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from ._capi import check, load_library
+from .batch import FLOW_DIVERGED, PHASE_DONE, BatchResult, Su2Batch
+from .core import Lattice, cutoff_exponential, frequency_exponential
+
+
+@dataclass(frozen=True)
+class FlowSpec:
+    """One flow as a task file describes it (exponential frequency and cutoff grids)."""
+    lattice: str
+    range: int
+    model: str
+    params: tuple          # ((name, value), ...) coupling parameters
+    n_freq: int
+    fmin: float
+    fmax: float
+    cmax: float
+    cmin: float
+    cstep: float
+    flags: int = 0
+
+    def build(self):
+        lat = Lattice(self.lattice, self.range, self.model, dict(self.params))
+        tab = lat.tables()
+        return tab, frequency_exponential(self.fmin, self.fmax, self.n_freq), cutoff_exponential(self.cmax, self.cmin, self.cstep)
+
+
+@dataclass
+class Ticket:
+    id: int
+    spec: FlowSpec
+    t_arrival: float
+    t_admit: float | None = None
+    t_done: float | None = None
+    flow_id: int | None = None
+    footprint: int = 0
+    result: BatchResult | None = None
+    _built: tuple | None = field(default=None, repr=False)
+
+    @property
+    def time_to_result(self) -> float | None:
+        return None if self.t_done is None else self.t_done - self.t_arrival
+
+
+def device_memory(device: int = 0):
+    """(free, total) device bytes."""
+    lib = load_library()
+    f, t = C.c_longlong(), C.c_longlong()
+    check(lib.spn_device_memory(device, C.byref(f), C.byref(t)))
+    return f.value, t.value
+
+
+class FlowServer:
+    def __init__(self, device: int = 0, memory_budget: int | None = None, max_flows: int | None = None,
+                 nodes_per_iteration: int = 1, use_graph: bool = True, clock=time.perf_counter):
+        self.batch = Su2Batch(device, nodes_per_iteration, use_graph)
+        if memory_budget is None:
+            free, _ = device_memory(device)
+            memory_budget = int(0.8 * free)
+        self.budget = memory_budget
+        self.max_flows = max_flows
+        self.clock = clock
+        self.queue: deque[Ticket] = deque()
+        self.active: dict[int, Ticket] = {}   # flow id -> ticket
+        self.finished: list[Ticket] = []
+        self.used = 0
+        self._next = 0
+        self.steps = 0
+
+    def submit(self, spec: FlowSpec, t_arrival: float | None = None) -> Ticket:
+        t = Ticket(self._next, spec, self.clock() if t_arrival is None else t_arrival)
+        self._next += 1
+        self.queue.append(t)
+        return t
+
+    def _admit(self) -> None:
+        while self.queue:
+            t = self.queue[0]
+            if self.max_flows is not None and len(self.active) >= self.max_flows:
+                return
+            if t._built is None:
+                t._built = t.spec.build()
+                tab, freq, cut = t._built
+                t.footprint = Su2Batch.footprint(tab, freq, len(cut))
+            if self.active and self.used + t.footprint > self.budget:
+                return
+            self.queue.popleft()
+            tab, freq, cut = t._built
+            t.flow_id = self.batch.add(tab, freq, cut, flags=t.spec.flags)
+            t.t_admit = self.clock()
+            self.used += t.footprint
+            self.active[t.flow_id] = t
+
+    def _retire(self) -> None:
+        for fid in list(self.active):
+            phase, _, _ = self.batch.poll(fid)
+            if phase != PHASE_DONE:
+                continue
+            t = self.active.pop(fid)
+            t.result = self.batch.result(fid)
+            t.t_done = self.clock()
+            self.batch.remove(fid)
+            self.used -= t.footprint
+            t._built = None
+            self.finished.append(t)
+
+    def pump(self) -> int:
+        """Admits what fits, advances every resident flow by one step and retires finished
+        flows.  Returns the number of flows resident or queued."""
+        self._admit()
+        if self.active:
+            self.batch.step()
+            self.steps += 1
+            self._retire()
+        return len(self.active) + len(self.queue)
+
+    def drain(self) -> None:
+        """Runs until every submitted request has its result."""
+        while self.pump():
+            pass
+
+    def close(self) -> None:
+        self.batch.close()
+
+
+def time_to_result_stats(tickets) -> dict:
+    ttr = np.array([t.time_to_result for t in tickets if t.time_to_result is not None])
+    if ttr.size == 0:
+        return {"n": 0}
+    return {"n": int(ttr.size), "p50_s": float(np.percentile(ttr, 50)), "p99_s": float(np.percentile(ttr, 99)),
+            "mean_s": float(ttr.mean()), "max_s": float(ttr.max())}
+
+
+def diverged(t: Ticket) -> bool:
+    return t.result is not None and t.result.diverged
