@@ -100,6 +100,15 @@ int spn_lattice_get_sites(const spn_lattice *lat, int *site_params, int *pair_ri
  * (row-major, 9 floats each).  SpinModel::interactions (src/SpinModel.hpp). */
 int spn_lattice_get_interactions(const spn_lattice *lat, int *rid, float *coupling);
 
+/* The RPA schedule the device uses for a lattice (diagnostics; host only): the merged pair
+ * lists of all rids cut into `lanes` balanced chunks, encoded as factors (products = 0,
+ * stride 1) or products (products = 1, Nl <= 32, stride 2); see csrc/host/rpa_schedule.hpp.
+ * info[4] = {entries per lane, segments, ints per entry, total ints of sched}.  With
+ * sched = NULL only info is filled; otherwise sched must hold info[3] ints, count and
+ * slot_base `lanes` ints and seg_ptr Nl + 1 ints. */
+int spn_rpa_schedule(int n_sites, const int *overlap_ptr, const int *overlap_rid1, const int *overlap_rid2, int lanes,
+                     int products, int *info, int *sched, int *count, int *slot_base, int *seg_ptr);
+
 /* Writes the lattice debug file (.ldf) as `--debugLattice`-free SpinParser always does. */
 int spn_lattice_write_ldf(const spn_lattice *lat, const char *path);
 

@@ -8,10 +8,11 @@ namespace spn {
 constexpr unsigned kStatusNaN = 1u;           // a NaN was written into the flow
 constexpr unsigned kStatusNodeOverflow = 2u;  // a loop-frequency node table overflowed
 
-// Lane-balanced RPA schedule: the RPA pair lists of all rids, merged into distinct
-// (rid1, rid2) pairs with their multiplicity, sorted by output rid, and cut into `lanes`
-// contiguous chunks.  Entry i of lane l is sched[i * lanes + l]:
-//   bits 0-6 rid1, bits 7-13 rid2, bits 14-21 multiplicity, bit 22 "last pair of a segment".
+// Lane-balanced RPA schedule (built by host/rpa_schedule.cpp): the RPA pair lists of all
+// rids merged into distinct (rid, rid1, rid2) with their multiplicity, sorted by rid and cut
+// into `lanes` contiguous chunks.  Entry i of lane l is at sched[(i * lanes + l) * stride]:
+//   stride 1 (factors, any Nl):  int  rid1 | rid2 << 7 | m << 14 | last << 22;
+//   stride 2 (products, Nl <= 32): int2 {rid1 * Nl + rid2 | last << 31, float m}.
 // A segment is a run of pairs of one output rid inside one chunk; its partial sum goes to the
 // next slot of the lane (slot_base[l], slot_base[l]+1, ...), and rid r sums the slots
 // seg_ptr[r] .. seg_ptr[r+1]-1 in order.
@@ -21,13 +22,14 @@ struct RpaSchedule {
     const int *slot_base;  // [lanes]
     const int *seg_ptr;    // [Nl + 1]
     int lanes, n_seg;
-    int len;       // entries per lane (sched holds len * lanes ints)
+    int len;       // entries per lane
+    int stride;    // ints per entry
     int in_smem;   // the kernel stages the schedule in shared memory
 };
 
 // Shared-memory words of a staged schedule (sched, count, slot_base, seg_ptr).
 __host__ __device__ inline int rpa_smem_ints(const RpaSchedule &r, int nl) {
-    return r.len * r.lanes + 2 * r.lanes + nl + 1;
+    return r.len * r.lanes * r.stride + 2 * r.lanes + nl + 1;
 }
 
 struct FlowArgs {

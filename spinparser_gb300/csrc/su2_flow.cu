@@ -29,6 +29,7 @@
 #include "su2_device.cuh"
 #include "su2_kernels.cuh"
 #include "su2_handle.cuh"
+#include "host/rpa_schedule.hpp"
 #include "host/capi_common.hpp"
 #include "../../include/spn_su2.h"
 
@@ -159,60 +160,6 @@ bool select_variant(spn_su2 *h, int npi, int in_smem) {
     h->vertex_npi = npi;
     h->vertex_grid = h->sms * per_sm;
     return true;
-}
-
-// Lane-balanced RPA schedule (see RpaSchedule in su2_common.cuh) from the reference's
-// per-rid overlap pair lists (Lattice::getOverlap, src/Lattice.hpp:472).
-struct HostRpa {
-    std::vector<int> sched, count, slot_base, seg_ptr;
-    int lanes = 0, n_seg = 0;
-};
-
-HostRpa build_rpa_schedule(int nl, const int *ptr, const int *r1, const int *r2, int lanes) {
-    struct Pair {
-        int rid, a, b, m;
-    };
-    std::vector<Pair> pairs;
-    std::vector<int> mult(size_t(nl) * nl);
-    for (int r = 0; r < nl; ++r) {
-        std::fill(mult.begin(), mult.end(), 0);
-        for (int i = ptr[r]; i < ptr[r + 1]; ++i) ++mult[size_t(r1[i]) * nl + r2[i]];
-        for (int a = 0; a < nl; ++a)
-            for (int b = 0; b < nl; ++b) {
-                const int m = mult[size_t(a) * nl + b];
-                if (!m) continue;
-                if (m > 255) throw Error(ErrorType::Unsupported, "RPA pair multiplicity above 255");
-                pairs.push_back({r, a, b, m});
-            }
-    }
-    HostRpa s;
-    s.lanes = lanes;
-    const int P = int(pairs.size());
-    const int L = (P + lanes - 1) / lanes;
-    s.sched.assign(size_t(std::max(L, 1)) * lanes, 0);
-    s.count.assign(lanes, 0);
-    s.slot_base.assign(lanes, 0);
-    s.seg_ptr.assign(nl + 1, -1);
-    int seg = -1;
-    for (int l = 0; l < lanes; ++l) {
-        const int b0 = l * L, b1 = std::min(P, (l + 1) * L);
-        s.count[l] = std::max(0, b1 - b0);
-        s.slot_base[l] = seg + 1;
-        for (int i = b0; i < b1; ++i) {
-            const Pair &p = pairs[i];
-            if (i == b0 || pairs[i - 1].rid != p.rid) {
-                ++seg;
-                if (s.seg_ptr[p.rid] < 0) s.seg_ptr[p.rid] = seg;
-            }
-            const bool last = (i + 1 == b1) || pairs[i + 1].rid != p.rid;
-            s.sched[size_t(i - b0) * lanes + l] = p.a | (p.b << 7) | (p.m << 14) | (last ? (1 << 22) : 0);
-        }
-    }
-    s.n_seg = seg + 1;
-    s.seg_ptr[nl] = s.n_seg;
-    for (int r = nl - 1; r >= 0; --r)
-        if (s.seg_ptr[r] < 0) s.seg_ptr[r] = s.seg_ptr[r + 1];
-    return s;
 }
 
 void validate_desc(const spn_su2_desc *d) {
@@ -369,10 +316,12 @@ spn_su2 *spn::create_flow(const spn_su2_desc *d, cudaStream_t stream) {
             cuda_check(cudaMemsetAsync(h->status, 0, sizeof(unsigned), h->stream), "memset");
             // balanced RPA schedule for the lanes of one node group
             const int lanes = spt_for(h->nl) == 1 ? wsite_for(h->nl) : 32;
-            HostRpa rpa = build_rpa_schedule(h->nl, d->overlap_ptr, d->overlap_rid1, d->overlap_rid2, lanes);
+            RpaHostSchedule rpa = build_rpa_schedule(h->nl, d->overlap_ptr, d->overlap_rid1, d->overlap_rid2, lanes,
+                                                     spt_for(h->nl) == 1);
             h->rpa_lanes = rpa.lanes;
             h->rpa_n_seg = rpa.n_seg;
-            h->rpa_len = int(rpa.sched.size()) / rpa.lanes;
+            h->rpa_len = rpa.len;
+            h->rpa_stride = rpa.stride;
             h->rpa_sched = dev_alloc<int>(rpa.sched.size(), "alloc rpa schedule");
             h->rpa_count = dev_alloc<int>(rpa.count.size(), "alloc rpa schedule");
             h->rpa_slot_base = dev_alloc<int>(rpa.slot_base.size(), "alloc rpa schedule");

@@ -35,7 +35,7 @@ struct spn_su2 {
     double *corr_partial = nullptr;
     double *v2d = nullptr, *dv2d = nullptr;  // FP64 self-energy (SPN_SU2_FP64_SELF_ENERGY)
     int *rpa_sched = nullptr, *rpa_count = nullptr, *rpa_slot_base = nullptr, *rpa_seg_ptr = nullptr;
-    int rpa_lanes = 0, rpa_n_seg = 0, rpa_len = 0, rpa_in_smem = 0;
+    int rpa_lanes = 0, rpa_n_seg = 0, rpa_len = 0, rpa_stride = 1, rpa_in_smem = 0;
     int vertex_npi = 1;       // loop-frequency nodes per site-group iteration
     int sms = 0;
     bool profiling = false;
@@ -81,6 +81,7 @@ struct spn_su2 {
         a.rpa.lanes = rpa_lanes;
         a.rpa.n_seg = rpa_n_seg;
         a.rpa.len = rpa_len;
+        a.rpa.stride = rpa_stride;
         a.rpa.in_smem = rpa_in_smem;
         return a;
     }

@@ -134,12 +134,16 @@ __device__ __forceinline__ void kahan_add(float &sum, float &comp, float v) {
     sum = t;
 }
 
-// Per-group shared-memory exchange area of the t channel.  Spin and density values are kept
-// in separate 32-bit arrays: with Nl <= 32 every element sits in its own bank, so the RPA
-// gathers A[rid1], B[rid2] of a warp never conflict.
+// Per-group shared-memory exchange area of the t channel.
+//   Nl <= 32 (one site per lane): A2/B2 hold (spin, density) of the third / fourth slab per
+//     site, P2[a * Nl + b] = A2[a] * B2[b] (both channels), then the RPA sums m * P2[ab] over
+//     the product-encoded schedule.
+//   Nl > 32: spin and density in separate 32-bit arrays As/Ad/Bs/Bd, and the RPA multiplies
+//     A[rid1] * m by B[rid2] over the factor-encoded schedule.
 struct TExchange {
-    float *As, *Ad;  // [sites] spin / density of the third slab
-    float *Bs, *Bd;  // [sites] spin / density of the fourth slab
+    float *As, *Ad;  // [sites] spin / density of the third slab   (Nl > 32)
+    float *Bs, *Bd;  // [sites] spin / density of the fourth slab  (Nl > 32)
+    float2 *A2, *B2, *P2;  // (Nl <= 32)
     float2 *slots;   // [n_seg] RPA segment partials
     const int *sched, *count, *slot_base, *seg_ptr;  // RPA schedule (shared or global memory)
 };
@@ -189,19 +193,71 @@ __device__ __forceinline__ void node_term(const FlowArgs &a, const NodeDesc *con
         return;
     }
     // t channel: RPA lattice sum (SU2FrgCore.cpp:249-266) over the balanced schedule
+    if (SPT == 1) {
+        if (ln.valid[0]) {
+            const int j = ln.j[0];
 #pragma unroll
-    for (int n = 0; n < NPI; ++n)
-#pragma unroll
-        for (int k = 0; k < SPT; ++k)
-            if (ln.valid[k]) {
-                const int j = ln.j[k];
-                tx[n].As[j] = S2[n][k];
-                tx[n].Ad[j] = D2[n][k];
-                tx[n].Bs[j] = S3[n][k];
-                tx[n].Bd[j] = D3[n][k];
+            for (int n = 0; n < NPI; ++n) {
+                tx[n].A2[j] = make_float2(S2[n][0], D2[n][0]);
+                tx[n].B2[j] = make_float2(S3[n][0], D3[n][0]);
             }
-    __syncwarp();
-    {
+        }
+        __syncwarp();
+        // products of both channels: lane jl forms column b = jl
+        const int nl = a.nl;
+        if (jl < nl) {
+#pragma unroll
+            for (int n = 0; n < NPI; ++n) {
+                const float2 bb = tx[n].B2[jl];
+                const float2 *A2 = tx[n].A2;
+                float2 *P2 = tx[n].P2 + jl;
+                for (int q = 0; q < nl; ++q) {
+                    const float2 av = A2[q];
+                    P2[q * nl] = make_float2(av.x * bb.x, av.y * bb.y);
+                }
+            }
+        }
+        __syncwarp();
+        const int lanes = a.rpa.lanes;
+        const int cnt = tx[0].count[jl];
+        int slot = tx[0].slot_base[jl];
+        float acc_s[NPI], acc_d[NPI];
+#pragma unroll
+        for (int n = 0; n < NPI; ++n) acc_s[n] = acc_d[n] = 0.0f;
+        const int2 *sched = reinterpret_cast<const int2 *>(tx[0].sched) + jl;
+        for (int i = 0; i < cnt; ++i) {
+            const int2 e = sched[i * lanes];
+            const float m = __int_as_float(e.y);
+            const int ab = e.x & 0x7fffffff;
+#pragma unroll
+            for (int n = 0; n < NPI; ++n) {
+                const float2 p = tx[n].P2[ab];
+                acc_s[n] = fmaf(m, p.x, acc_s[n]);
+                acc_d[n] = fmaf(m, p.y, acc_d[n]);
+            }
+            if (e.x < 0) {  // last pair of a segment
+#pragma unroll
+                for (int n = 0; n < NPI; ++n) {
+                    tx[n].slots[slot] = make_float2(acc_s[n], acc_d[n]);
+                    acc_s[n] = 0.0f;
+                    acc_d[n] = 0.0f;
+                }
+                ++slot;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int n = 0; n < NPI; ++n)
+#pragma unroll
+            for (int k = 0; k < SPT; ++k)
+                if (ln.valid[k]) {
+                    const int j = ln.j[k];
+                    tx[n].As[j] = S2[n][k];
+                    tx[n].Ad[j] = D2[n][k];
+                    tx[n].Bs[j] = S3[n][k];
+                    tx[n].Bd[j] = D3[n][k];
+                }
+        __syncwarp();
         const int lanes = a.rpa.lanes;
         const int cnt = tx[0].count[jl];
         int slot = tx[0].slot_base[jl];
@@ -318,14 +374,24 @@ __device__ __forceinline__ void channel_sum(const FlowArgs &a, const float *pos,
 // Shared memory of the single-flow kernel: frequency mesh; the RPA schedule when it is staged;
 // then per warp: 32 node descriptors and, per node group, NPI t-channel exchange areas (four
 // arrays of W*SPT sites and n_seg slots each).
-__host__ __device__ inline size_t node_area_bytes(int wsite, int spt, int n_seg) {
-    return (sizeof(float) * 4 * size_t(wsite) * spt + sizeof(float2) * n_seg + 15) / 16 * 16;
+// Bytes of one node's t-channel exchange area.  With one site per lane it holds A2, B2 (wsite
+// float2 each), P2 (Nl^2 float2) and the slots; its size is padded so that the groups sharing
+// a half-warp (stride npi * area) sit min(wsite, 16) 8-byte words apart modulo 16, which keeps
+// their product reads on different banks (the schedule spreads a group's reads over the
+// residues modulo min(wsite, 16)).
+__host__ __device__ inline size_t node_area_bytes(int wsite, int spt, int n_seg, int nl, int npi) {
+    if (spt != 1) return (sizeof(float) * 4 * size_t(wsite) * spt + sizeof(float2) * n_seg + 15) / 16 * 16;
+    size_t b = (sizeof(float2) * (2 * size_t(wsite) + size_t(nl) * nl + n_seg) + 15) / 16 * 16;
+    const int hw = wsite < 16 ? wsite : 16;
+    if (hw % 2 == 0)
+        for (int k = 0; k < 16 && (npi * b / 8) % 16 != size_t(hw % 16); ++k) b += 16;
+    return b;
 }
-__host__ __device__ inline size_t group_area_bytes(int wsite, int spt, int npi, int n_seg) {
-    return (32 / wsite) * npi * node_area_bytes(wsite, spt, n_seg);
+__host__ __device__ inline size_t group_area_bytes(int wsite, int spt, int npi, int n_seg, int nl) {
+    return (32 / wsite) * npi * node_area_bytes(wsite, spt, n_seg, nl, npi);
 }
-__host__ __device__ inline size_t warp_bytes(int wsite, int spt, int npi, int n_seg) {
-    return kBatch * sizeof(NodeDesc) + group_area_bytes(wsite, spt, npi, n_seg);
+__host__ __device__ inline size_t warp_bytes(int wsite, int spt, int npi, int n_seg, int nl) {
+    return kBatch * sizeof(NodeDesc) + group_area_bytes(wsite, spt, npi, n_seg, nl);
 }
 __host__ __device__ inline size_t sched_bytes(const RpaSchedule &r, int nl) {
     return r.in_smem ? (sizeof(int) * size_t(rpa_smem_ints(r, nl)) + 15) / 16 * 16 : 0;
@@ -352,17 +418,27 @@ __device__ __forceinline__ void setup_ctx(const FlowArgs &a, int lane, NodeDesc 
     c.G = 32 / c.W;
     c.g = lane / c.W;
     c.jl = lane - c.g * c.W;
-    const size_t nab = node_area_bytes(c.W, SPT, a.rpa.n_seg);
+    const size_t nab = node_area_bytes(c.W, SPT, a.rpa.n_seg, a.nl, NPI);
     unsigned char *gbase = groups + size_t(c.g) * NPI * nab;
     const int ws = c.W * SPT;
 #pragma unroll
     for (int n = 0; n < NPI; ++n) {
         float *gx = reinterpret_cast<float *>(gbase + n * nab);
-        c.tx[n].As = gx;
-        c.tx[n].Ad = gx + ws;
-        c.tx[n].Bs = gx + 2 * ws;
-        c.tx[n].Bd = gx + 3 * ws;
-        c.tx[n].slots = reinterpret_cast<float2 *>(gx + 4 * ws);
+        if (SPT == 1) {
+            float2 *g2 = reinterpret_cast<float2 *>(gx);
+            c.tx[n].A2 = g2;
+            c.tx[n].B2 = g2 + ws;
+            c.tx[n].P2 = g2 + 2 * ws;
+            c.tx[n].slots = g2 + 2 * ws + a.nl * a.nl;
+            c.tx[n].As = c.tx[n].Ad = c.tx[n].Bs = c.tx[n].Bd = nullptr;
+        } else {
+            c.tx[n].As = gx;
+            c.tx[n].Ad = gx + ws;
+            c.tx[n].Bs = gx + 2 * ws;
+            c.tx[n].Bd = gx + 3 * ws;
+            c.tx[n].slots = reinterpret_cast<float2 *>(gx + 4 * ws);
+            c.tx[n].A2 = c.tx[n].B2 = c.tx[n].P2 = nullptr;
+        }
         c.tx[n].sched = sched;
         c.tx[n].count = count;
         c.tx[n].slot_base = slot_base;
@@ -437,7 +513,7 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_flow_kernel(FlowArgs a) {
     const int *sched, *count, *slot_base, *seg_ptr;
     if (a.rpa.in_smem) {
         int *s = reinterpret_cast<int *>(sbase);
-        const int ns = a.rpa.len * a.rpa.lanes, nc = a.rpa.lanes;
+        const int ns = a.rpa.len * a.rpa.lanes * a.rpa.stride, nc = a.rpa.lanes;
         for (int i = threadIdx.x; i < ns; i += blockDim.x) s[i] = __ldg(a.rpa.sched + i);
         for (int i = threadIdx.x; i < nc; i += blockDim.x) {
             s[ns + i] = __ldg(a.rpa.count + i);
@@ -454,7 +530,7 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_flow_kernel(FlowArgs a) {
         slot_base = a.rpa.slot_base;
         seg_ptr = a.rpa.seg_ptr;
     }
-    unsigned char *wbase = sbase + sched_bytes(a.rpa, a.nl) + warp * warp_bytes(W, SPT, NPI, n_seg);
+    unsigned char *wbase = sbase + sched_bytes(a.rpa, a.nl) + warp * warp_bytes(W, SPT, NPI, n_seg, a.nl);
     WarpCtx<SPT, NPI> c;
     setup_ctx<SPT, NPI>(a, lane, reinterpret_cast<NodeDesc *>(wbase), wbase + kBatch * sizeof(NodeDesc), sched, count,
                         slot_base, seg_ptr, c);
@@ -515,7 +591,7 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_batch_kernel(BatchVertexA
             for (int i = lane; i < fa->n; i += 32) pos[i] = fa->freq[i];
             if (b.sched_ints > 0) {  // the host checked that every flow's schedule fits
                 const RpaSchedule &r = fa->rpa;
-                const int ns = r.len * r.lanes, nc = r.lanes;
+                const int ns = r.len * r.lanes * r.stride, nc = r.lanes;
                 for (int i = lane; i < ns; i += 32) sch[i] = __ldg(r.sched + i);
                 for (int i = lane; i < nc; i += 32) {
                     sch[ns + i] = __ldg(r.count + i);
@@ -548,7 +624,7 @@ int wsite_of(int nl) {
 size_t vertex_flow_smem_bytes(int nl, const RpaSchedule &rpa, int npi) {
     const int spt = spt_of(nl);
     return kMaxFreq * sizeof(float) + sched_bytes(rpa, nl) +
-           kWarps * warp_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, rpa.n_seg);
+           kWarps * warp_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, rpa.n_seg, nl);
 }
 
 namespace {
@@ -580,7 +656,7 @@ int vertex_spt(int nl) { return spt_of(nl); }
 
 size_t batch_vertex_warp_area(int nl, int n_seg, int npi) {
     const int spt = spt_of(nl);
-    return group_area_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, n_seg);
+    return group_area_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, n_seg, nl);
 }
 
 size_t batch_vertex_smem_bytes(int n_max, size_t warp_area, int sched_ints) {

@@ -129,8 +129,9 @@ def test_two_nodes_per_iteration_variant():
 
 
 def test_server_admits_by_footprint_and_results_do_not_change(reference):
-    """Continuous batching with a memory budget of about two flows: requests wait, are
-    admitted as others finish, and every result equals the flow alone."""
+    """Continuous batching under a memory budget (the largest flow plus a little) and under a
+    two-flow slot limit: requests wait, are admitted as others finish, and every result equals
+    the flow alone."""
     from spinparser_gb300.serve import FlowServer, FlowSpec
 
     def spec(name):
@@ -138,18 +139,20 @@ def test_server_admits_by_footprint_and_results_do_not_change(reference):
         return FlowSpec(lat, rng, model, tuple(params.items()), n, 0.05, 50.0, cmax, cmin, step, flags)
 
     names = list(CASES)
-    feet = [Su2Batch.footprint(*case(n)[:2], len(case(n)[2])) for n in names]
-    srv = FlowServer(memory_budget=int(2.5 * max(feet)))
-    tickets = {n: srv.submit(spec(n)) for n in names}
-    most = 0
-    while srv.pump():
-        most = max(most, len(srv.active))
-        assert srv.used <= srv.budget
-    assert 1 <= most <= 2
-    for n, t in tickets.items():
-        assert t.t_admit is not None and t.t_done is not None and t.time_to_result > 0
-        r = t.result
-        ref = reference[n]
-        assert r.diverged == ref["div"] and np.array_equal(r.cutoffs, ref["cut"])
-        assert np.array_equal(r.zz, ref["zz"].reshape(r.zz.shape)) and np.array_equal(r.dd, ref["dd"].reshape(r.dd.shape))
-    srv.close()
+    feet = sorted(Su2Batch.footprint(*case(n)[:2], len(case(n)[2])) for n in names)
+    for budget, slots in ((feet[-1] + feet[0] // 2, None), (10 * feet[-1], 2)):
+        srv = FlowServer(memory_budget=budget, max_flows=slots)
+        tickets = {n: srv.submit(spec(n)) for n in names}
+        most = 0
+        while srv.pump():
+            most = max(most, len(srv.active))
+            assert srv.used <= srv.budget
+            assert slots is None or len(srv.active) <= slots
+        assert 1 <= most < len(names)  # requests had to wait for memory / slots
+        for n, t in tickets.items():
+            assert t.t_admit is not None and t.t_done is not None and t.time_to_result > 0
+            r = t.result
+            ref = reference[n]
+            assert r.diverged == ref["div"] and np.array_equal(r.cutoffs, ref["cut"])
+            assert np.array_equal(r.zz, ref["zz"].reshape(r.zz.shape)) and np.array_equal(r.dd, ref["dd"].reshape(r.dd.shape))
+        srv.close()
