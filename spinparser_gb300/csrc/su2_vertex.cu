@@ -350,7 +350,7 @@ __device__ __forceinline__ void channel_sum(const FlowArgs &a, const float *pos,
             bool active[NPI];
 #pragma unroll
             for (int n = 0; n < NPI; ++n) {
-                const int k = (r * G + g) * NPI + n;
+                const int k = (r * NPI + n) * G + g;  // group g: nodes g, g+G, g+2G, ... for every NPI
                 active[n] = k < nb;
                 d[n] = &desc[active[n] ? k : 0];
             }
