@@ -234,7 +234,7 @@ extern "C" int spn_rpa_schedule(int n_sites, const int *overlap_ptr, const int *
         spn::RpaHostSchedule s = spn::build_rpa_schedule(n_sites, overlap_ptr, overlap_rid1, overlap_rid2, lanes, products != 0);
         info[0] = s.len;
         info[1] = s.n_seg;
-        info[2] = s.stride;
+        info[2] = products ? 1 : 0;
         info[3] = int(s.sched.size());
         if (!sched) return;
         std::memcpy(sched, s.sched.data(), s.sched.size() * sizeof(int));

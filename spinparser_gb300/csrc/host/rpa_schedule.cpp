@@ -13,6 +13,14 @@ struct Pair {
     int rid, a, b, m;
 };
 
+// IEEE binary16 bits of an integer 1 <= m <= 255 (exact).
+int half_bits(int m) {
+    int e = 0;
+    while ((m >> (e + 1)) != 0) ++e;
+    const int mant = ((m << 10) >> e) & 0x3ff;
+    return ((e + 15) << 10) | mant;
+}
+
 }  // namespace
 
 RpaHostSchedule build_rpa_schedule(int nl, const int *ptr, const int *r1, const int *r2, int lanes, bool products) {
@@ -33,11 +41,10 @@ RpaHostSchedule build_rpa_schedule(int nl, const int *ptr, const int *r1, const 
     }
     RpaHostSchedule s;
     s.lanes = lanes;
-    s.stride = products ? 2 : 1;
     const int P = int(pairs.size());
     const int L = std::max(1, (P + lanes - 1) / lanes);
     s.len = L;
-    s.sched.assign(size_t(L) * lanes * s.stride, 0);
+    s.sched.assign(size_t(L) * lanes, 0);
     s.count.assign(lanes, 0);
     s.slot_base.assign(lanes, 0);
     s.seg_ptr.assign(nl + 1, -1);
@@ -65,7 +72,7 @@ RpaHostSchedule build_rpa_schedule(int nl, const int *ptr, const int *r1, const 
     for (int r = nl - 1; r >= 0; --r)
         if (s.seg_ptr[r] < 0) s.seg_ptr[r] = s.seg_ptr[r + 1];
 
-    if (products) {
+    if (nl <= 32) {
         // Reorder inside segments: at step i the lanes that share a half-warp should read
         // P[ab] at distinct banks.  A lane group of `lanes` lanes fills min(lanes, 16) lanes of
         // a half-warp; its reads are conflict-free when the ab of those lanes differ modulo
@@ -123,13 +130,9 @@ RpaHostSchedule build_rpa_schedule(int nl, const int *ptr, const int *r1, const 
             const Pair &p = order[l][i];
             const bool last = (i + 1 == seg_end[l][si]);
             if (last) ++si;
-            const size_t at = (size_t(i) * lanes + l) * s.stride;
+            const size_t at = size_t(i) * lanes + l;
             if (products) {
-                const float m = float(p.m);
-                int mbits;
-                std::memcpy(&mbits, &m, sizeof(int));
-                s.sched[at] = (p.a * nl + p.b) | (last ? int(0x80000000u) : 0);
-                s.sched[at + 1] = mbits;
+                s.sched[at] = (p.a * nl + p.b) | (last ? (1 << 15) : 0) | int(unsigned(half_bits(p.m)) << 16);
             } else {
                 s.sched[at] = p.a | (p.b << 7) | (p.m << 14) | (last ? (1 << 22) : 0);
             }

@@ -21,6 +21,7 @@
 // Accumulation over nodes is Kahan-compensated FP32; group partials are combined by shuffles.
 #include "su2_common.cuh"
 #include "su2_device.cuh"
+#include <cuda_fp16.h>
 
 namespace spn {
 namespace {
@@ -29,7 +30,7 @@ using namespace spn::dev;
 
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
-constexpr int kBatch = 32;
+constexpr int kBatch = 16;  // nodes whose descriptors a warp builds at once (phase A)
 constexpr double kPi = 3.14159265358979323846;
 
 struct __align__(16) NodeDesc {
@@ -192,8 +193,9 @@ __device__ __forceinline__ void node_term(const FlowArgs &a, const NodeDesc *con
             }
         return;
     }
-    // t channel: RPA lattice sum (SU2FrgCore.cpp:249-266) over the balanced schedule
-    if (SPT == 1) {
+    // t channel: RPA lattice sum (SU2FrgCore.cpp:249-266) over the balanced schedule.  Both
+    // encodings accumulate acc += m * (A[rid1] * B[rid2]) in the schedule's order.
+    if (SPT == 1 && a.rpa.products) {
         if (ln.valid[0]) {
             const int j = ln.j[0];
 #pragma unroll
@@ -224,18 +226,18 @@ __device__ __forceinline__ void node_term(const FlowArgs &a, const NodeDesc *con
         float acc_s[NPI], acc_d[NPI];
 #pragma unroll
         for (int n = 0; n < NPI; ++n) acc_s[n] = acc_d[n] = 0.0f;
-        const int2 *sched = reinterpret_cast<const int2 *>(tx[0].sched) + jl;
+        const int *sched = tx[0].sched + jl;
         for (int i = 0; i < cnt; ++i) {
-            const int2 e = sched[i * lanes];
-            const float m = __int_as_float(e.y);
-            const int ab = e.x & 0x7fffffff;
+            const int e = sched[i * lanes];
+            const float m = __half2float(__ushort_as_half((unsigned short)((unsigned)e >> 16)));
+            const int ab = e & 0x7fff;
 #pragma unroll
             for (int n = 0; n < NPI; ++n) {
                 const float2 p = tx[n].P2[ab];
                 acc_s[n] = fmaf(m, p.x, acc_s[n]);
                 acc_d[n] = fmaf(m, p.y, acc_d[n]);
             }
-            if (e.x < 0) {  // last pair of a segment
+            if (e & (1 << 15)) {  // last pair of a segment
 #pragma unroll
                 for (int n = 0; n < NPI; ++n) {
                     tx[n].slots[slot] = make_float2(acc_s[n], acc_d[n]);
@@ -271,8 +273,8 @@ __device__ __forceinline__ void node_term(const FlowArgs &a, const NodeDesc *con
             const int ra = e & 0x7f, rb = (e >> 7) & 0x7f;
 #pragma unroll
             for (int n = 0; n < NPI; ++n) {
-                acc_s[n] = fmaf(tx[n].As[ra] * m, tx[n].Bs[rb], acc_s[n]);
-                acc_d[n] = fmaf(tx[n].Ad[ra] * m, tx[n].Bd[rb], acc_d[n]);
+                acc_s[n] = fmaf(m, tx[n].As[ra] * tx[n].Bs[rb], acc_s[n]);
+                acc_d[n] = fmaf(m, tx[n].Ad[ra] * tx[n].Bd[rb], acc_d[n]);
             }
             if (e & (1 << 22)) {
 #pragma unroll
@@ -379,19 +381,19 @@ __device__ __forceinline__ void channel_sum(const FlowArgs &a, const float *pos,
 // a half-warp (stride npi * area) sit min(wsite, 16) 8-byte words apart modulo 16, which keeps
 // their product reads on different banks (the schedule spreads a group's reads over the
 // residues modulo min(wsite, 16)).
-__host__ __device__ inline size_t node_area_bytes(int wsite, int spt, int n_seg, int nl, int npi) {
-    if (spt != 1) return (sizeof(float) * 4 * size_t(wsite) * spt + sizeof(float2) * n_seg + 15) / 16 * 16;
+__host__ __device__ inline size_t node_area_bytes(int wsite, int spt, int n_seg, int nl, int npi, int products) {
+    if (spt != 1 || !products) return (sizeof(float) * 4 * size_t(wsite) * spt + sizeof(float2) * n_seg + 15) / 16 * 16;
     size_t b = (sizeof(float2) * (2 * size_t(wsite) + size_t(nl) * nl + n_seg) + 15) / 16 * 16;
     const int hw = wsite < 16 ? wsite : 16;
     if (hw % 2 == 0)
         for (int k = 0; k < 16 && (npi * b / 8) % 16 != size_t(hw % 16); ++k) b += 16;
     return b;
 }
-__host__ __device__ inline size_t group_area_bytes(int wsite, int spt, int npi, int n_seg, int nl) {
-    return (32 / wsite) * npi * node_area_bytes(wsite, spt, n_seg, nl, npi);
+__host__ __device__ inline size_t group_area_bytes(int wsite, int spt, int npi, int n_seg, int nl, int products) {
+    return (32 / wsite) * npi * node_area_bytes(wsite, spt, n_seg, nl, npi, products);
 }
-__host__ __device__ inline size_t warp_bytes(int wsite, int spt, int npi, int n_seg, int nl) {
-    return kBatch * sizeof(NodeDesc) + group_area_bytes(wsite, spt, npi, n_seg, nl);
+__host__ __device__ inline size_t warp_bytes(int wsite, int spt, int npi, int n_seg, int nl, int products) {
+    return kBatch * sizeof(NodeDesc) + group_area_bytes(wsite, spt, npi, n_seg, nl, products);
 }
 __host__ __device__ inline size_t sched_bytes(const RpaSchedule &r, int nl) {
     return r.in_smem ? (sizeof(int) * size_t(rpa_smem_ints(r, nl)) + 15) / 16 * 16 : 0;
@@ -418,13 +420,13 @@ __device__ __forceinline__ void setup_ctx(const FlowArgs &a, int lane, NodeDesc 
     c.G = 32 / c.W;
     c.g = lane / c.W;
     c.jl = lane - c.g * c.W;
-    const size_t nab = node_area_bytes(c.W, SPT, a.rpa.n_seg, a.nl, NPI);
+    const size_t nab = node_area_bytes(c.W, SPT, a.rpa.n_seg, a.nl, NPI, a.rpa.products);
     unsigned char *gbase = groups + size_t(c.g) * NPI * nab;
     const int ws = c.W * SPT;
 #pragma unroll
     for (int n = 0; n < NPI; ++n) {
         float *gx = reinterpret_cast<float *>(gbase + n * nab);
-        if (SPT == 1) {
+        if (SPT == 1 && a.rpa.products) {
             float2 *g2 = reinterpret_cast<float2 *>(gx);
             c.tx[n].A2 = g2;
             c.tx[n].B2 = g2 + ws;
@@ -513,7 +515,7 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_flow_kernel(FlowArgs a) {
     const int *sched, *count, *slot_base, *seg_ptr;
     if (a.rpa.in_smem) {
         int *s = reinterpret_cast<int *>(sbase);
-        const int ns = a.rpa.len * a.rpa.lanes * a.rpa.stride, nc = a.rpa.lanes;
+        const int ns = a.rpa.len * a.rpa.lanes, nc = a.rpa.lanes;
         for (int i = threadIdx.x; i < ns; i += blockDim.x) s[i] = __ldg(a.rpa.sched + i);
         for (int i = threadIdx.x; i < nc; i += blockDim.x) {
             s[ns + i] = __ldg(a.rpa.count + i);
@@ -530,7 +532,7 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_flow_kernel(FlowArgs a) {
         slot_base = a.rpa.slot_base;
         seg_ptr = a.rpa.seg_ptr;
     }
-    unsigned char *wbase = sbase + sched_bytes(a.rpa, a.nl) + warp * warp_bytes(W, SPT, NPI, n_seg, a.nl);
+    unsigned char *wbase = sbase + sched_bytes(a.rpa, a.nl) + warp * warp_bytes(W, SPT, NPI, n_seg, a.nl, a.rpa.products);
     WarpCtx<SPT, NPI> c;
     setup_ctx<SPT, NPI>(a, lane, reinterpret_cast<NodeDesc *>(wbase), wbase + kBatch * sizeof(NodeDesc), sched, count,
                         slot_base, seg_ptr, c);
@@ -591,7 +593,7 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_batch_kernel(BatchVertexA
             for (int i = lane; i < fa->n; i += 32) pos[i] = fa->freq[i];
             if (b.sched_ints > 0) {  // the host checked that every flow's schedule fits
                 const RpaSchedule &r = fa->rpa;
-                const int ns = r.len * r.lanes * r.stride, nc = r.lanes;
+                const int ns = r.len * r.lanes, nc = r.lanes;
                 for (int i = lane; i < ns; i += 32) sch[i] = __ldg(r.sched + i);
                 for (int i = lane; i < nc; i += 32) {
                     sch[ns + i] = __ldg(r.count + i);
@@ -624,7 +626,7 @@ int wsite_of(int nl) {
 size_t vertex_flow_smem_bytes(int nl, const RpaSchedule &rpa, int npi) {
     const int spt = spt_of(nl);
     return kMaxFreq * sizeof(float) + sched_bytes(rpa, nl) +
-           kWarps * warp_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, rpa.n_seg, nl);
+           kWarps * warp_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, rpa.n_seg, nl, rpa.products);
 }
 
 namespace {
@@ -654,9 +656,9 @@ void launch_vertex_flow(const FlowArgs &a, int npi, int grid, cudaStream_t strea
 
 int vertex_spt(int nl) { return spt_of(nl); }
 
-size_t batch_vertex_warp_area(int nl, int n_seg, int npi) {
+size_t batch_vertex_warp_area(int nl, int n_seg, int npi, int products) {
     const int spt = spt_of(nl);
-    return group_area_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, n_seg, nl);
+    return group_area_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, n_seg, nl, products);
 }
 
 size_t batch_vertex_smem_bytes(int n_max, size_t warp_area, int sched_ints) {

@@ -43,20 +43,21 @@ def schedule(tab, lanes, products):
 def decode(tab, lanes, products, info, sched, count, base, seg, A, B):
     """The kernel's walk: per lane, accumulate m * A[a] * B[b], flush at segment ends."""
     nl = tab.n_sites
-    L, n_seg, stride = info[0], info[1], info[2]
+    L, n_seg = info[0], info[1]
+    assert info[2] == int(products) and info[3] == L * lanes
     slots = np.zeros(n_seg)
     for l in range(lanes):
         assert 0 <= count[l] <= L
         acc, slot = 0.0, base[l]
         for i in range(count[l]):
-            at = (i * lanes + l) * stride
+            at = i * lanes + l
             if products:
-                x = int(sched[at])
-                last = x < 0
-                ab = x & 0x7FFFFFFF
+                x = int(np.uint32(sched[at]))
+                last = bool(x & (1 << 15))
+                ab = x & 0x7FFF
                 assert ab < nl * nl
                 a, b = divmod(ab, nl)
-                m = float(np.frombuffer(np.int32(sched[at + 1]).tobytes(), np.float32)[0])
+                m = float(np.frombuffer(np.uint16(x >> 16).tobytes(), np.float16)[0])
             else:
                 e = int(sched[at])
                 a, b, m, last = e & 0x7F, (e >> 7) & 0x7F, float((e >> 14) & 0xFF), bool(e & (1 << 22))
@@ -88,15 +89,14 @@ def test_schedule_reproduces_rpa_sums(lat):
         np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-12)
 
 
-def _conflicts(tab, lanes, info, sched, count):
+def _conflicts(nl, lanes, L, ab, count):
     """Extra shared-memory wavefronts of the product reads: per step and half-warp, the
-    largest number of lanes on one bank pair minus one."""
-    nl, L = tab.n_sites, info[0]
+    largest number of lanes on one bank pair minus one.  ab[i * lanes + l] = product index."""
     hw = min(lanes, 16)
     extra = 0
     for i in range(L):
         for h0 in range(0, lanes, hw):
-            keys = [(int(sched[(i * lanes + l) * 2]) & 0x7FFFFFFF) % hw for l in range(h0, h0 + hw) if i < count[l]]
+            keys = [int(ab[i * lanes + l]) % hw for l in range(h0, h0 + hw) if i < count[l]]
             if keys:
                 extra += max(np.bincount(keys)) - 1
     return extra
@@ -107,15 +107,20 @@ def test_product_schedule_spreads_banks(lat):
     tab = spn.Lattice(*lat).tables()
     nl = tab.n_sites
     lanes = 1 << max(0, (nl - 1).bit_length())
-    s = schedule(tab, lanes, True)
-    ordered = _conflicts(tab, lanes, s[0], s[1], s[2])
-    # the same chunks in plain pair order: rebuild the unordered schedule from the factor encoding
-    f = schedule(tab, lanes, False)
-    naive = np.zeros_like(s[1])
-    for k, e in enumerate(f[1]):
-        a, b = e & 0x7F, (e >> 7) & 0x7F
-        naive[2 * k] = a * nl + b
-    baseline = _conflicts(tab, lanes, s[0], naive, s[2])
+    info, sched, count, _, _ = schedule(tab, lanes, True)
+    L = info[0]
+    ordered = _conflicts(nl, lanes, L, sched.view(np.uint32) & 0x7FFF, count)
+    # the factor encoding walks the pairs in the same order
+    f = schedule(tab, lanes, False)[1]
+    assert np.array_equal((f & 0x7F) * nl + ((f >> 7) & 0x7F), (sched.view(np.uint32) & 0x7FFF).astype(np.int64))
+    # the same chunks in plain (rid, rid1, rid2) order
+    ptr, r1, r2 = tab.overlap_ptr, tab.overlap_rid1, tab.overlap_rid2
+    pairs = sorted({(r, a, b) for r in range(nl) for a, b in zip(r1[ptr[r]:ptr[r + 1]], r2[ptr[r]:ptr[r + 1]])})
+    naive = np.zeros(L * lanes, np.int64)
+    for l in range(lanes):
+        for i, (_, a, b) in enumerate(pairs[l * L:(l + 1) * L]):
+            naive[i * lanes + l] = a * nl + b
+    baseline = _conflicts(nl, lanes, L, naive, count)
     print(f"{lat[0]} r{lat[1]}: extra wavefronts ordered {ordered} vs plain order {baseline}")
     assert ordered <= baseline
     if nl >= 8:
