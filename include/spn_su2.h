@@ -101,13 +101,12 @@ int spn_lattice_get_sites(const spn_lattice *lat, int *site_params, int *pair_ri
 int spn_lattice_get_interactions(const spn_lattice *lat, int *rid, float *coupling);
 
 /* The RPA schedule the device uses for a lattice (diagnostics; host only): the merged pair
- * lists of all rids cut into `lanes` balanced chunks, encoded as factors (products = 0) or
- * products (products = 1, Nl <= 32); see csrc/host/rpa_schedule.hpp.
- * info[4] = {entries per lane, segments, products, total ints of sched}.  With
- * sched = NULL only info is filled; otherwise sched must hold info[3] ints, count and
- * slot_base `lanes` ints and seg_ptr Nl + 1 ints. */
+ * lists of all rids cut into `lanes` balanced chunks (csrc/host/rpa_schedule.hpp).
+ * info[3] = {entries per lane, segments, total ints of sched}.  With sched = NULL only info
+ * is filled; otherwise sched must hold info[2] ints, count and slot_base `lanes` ints and
+ * seg_ptr Nl + 1 ints. */
 int spn_rpa_schedule(int n_sites, const int *overlap_ptr, const int *overlap_rid1, const int *overlap_rid2, int lanes,
-                     int products, int *info, int *sched, int *count, int *slot_base, int *seg_ptr);
+                     int *info, int *sched, int *count, int *slot_base, int *seg_ptr);
 
 /* Writes the lattice debug file (.ldf) as `--debugLattice`-free SpinParser always does. */
 int spn_lattice_write_ldf(const spn_lattice *lat, const char *path);
@@ -184,17 +183,16 @@ int spn_su2_get_node_counts(spn_su2 *h, int *counts);
 int spn_su2_compute_step(spn_su2 *h);
 
 /* Picks the vertex-flow kernel variant for this flow by timing the candidates on the current
- * state (`reps` launches each): nodes a site group evaluates per iteration (1 or 2), whether
- * the RPA schedule is staged in shared memory, and whether the RPA sum first forms the
- * products of the exchanged values (Nl <= 32).  All variants give identical results.  Leaves
- * the state unchanged; reports the choice and the persistent grid size.  Replaces the
+ * state (`reps` launches each): nodes a site group evaluates per iteration (1 or 2) and
+ * whether the RPA schedule is staged in shared memory.  All variants give identical results.
+ * Leaves the state unchanged; reports the choice and the persistent grid size.  Replaces the
  * reference LoadManager's throughput model (src/lib/LoadManager.hpp:796-852) as the tuning
  * step of the work distribution. */
-int spn_su2_autotune(spn_su2 *h, int reps, int *npi, int *sched_in_smem, int *rpa_products, int *grid);
+int spn_su2_autotune(spn_su2 *h, int reps, int *npi, int *sched_in_smem, int *grid);
 
-/* Selects a vertex-flow variant explicitly (npi = 1 or 2; schedule in shared memory or not;
- * product-form RPA or not).  SPN_E_UNSUPPORTED if it does not fit for this lattice. */
-int spn_su2_set_variant(spn_su2 *h, int npi, int sched_in_smem, int rpa_products);
+/* Selects a vertex-flow variant explicitly (npi = 1 or 2; schedule in shared memory or not).
+ * SPN_E_UNSUPPORTED if it does not fit for this lattice. */
+int spn_su2_set_variant(spn_su2 *h, int npi, int sched_in_smem);
 
 /* Copies the flow computed by the last compute_step: dv2[N], dv4ss/dv4dd[F_N*Nl]. */
 int spn_su2_get_flow(spn_su2 *h, float *dv2, float *dv4ss, float *dv4dd);
@@ -265,10 +263,9 @@ typedef struct spn_batch spn_batch;
 
 int spn_batch_create(int device, spn_batch **out);
 int spn_batch_destroy(spn_batch *b);
-/* Vertex-flow variant of the batch (npi = 1 or 2; product-form RPA for flows of <= 32 sites,
- * applied to flows added afterwards) and whether steps are replayed as graphs.  Variants do
- * not change results. */
-int spn_batch_set_variant(spn_batch *b, int npi, int use_graph, int rpa_products);
+/* Vertex-flow variant of the batch (npi = 1 or 2) and whether steps are replayed as graphs.
+ * Variants do not change results. */
+int spn_batch_set_variant(spn_batch *b, int npi, int use_graph);
 /* Device memory a flow takes in a batch (state, flow, tables, measurement history): the
  * admission measure of a serving loop. */
 int spn_batch_footprint(const spn_su2_desc *desc, int n_cutoffs, long long *bytes);

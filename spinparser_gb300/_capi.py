@@ -88,8 +88,8 @@ SIGNATURES = {
     "spn_lattice_get_sites": (C.c_int, [C.c_void_p, c_int_p, c_int_p]),
     "spn_lattice_get_interactions": (C.c_int, [C.c_void_p, c_int_p, c_float_p]),
     "spn_lattice_write_ldf": (C.c_int, [C.c_void_p, C.c_char_p]),
-    "spn_rpa_schedule": (C.c_int, [C.c_int, c_int_p, c_int_p, c_int_p, C.c_int, C.c_int, c_int_p, c_int_p, c_int_p,
-                                   c_int_p, c_int_p]),
+    "spn_rpa_schedule": (C.c_int, [C.c_int, c_int_p, c_int_p, c_int_p, C.c_int, c_int_p, c_int_p, c_int_p, c_int_p,
+                                   c_int_p]),
     "spn_frequency_exponential": (C.c_int, [C.c_float, C.c_float, C.c_int, c_float_p]),
     "spn_cutoff_exponential": (C.c_int, [C.c_float, C.c_float, C.c_float, c_float_p, C.c_int, c_int_p]),
     "spn_su2_initial_state": (C.c_int, [C.c_void_p, C.c_int, C.c_float, c_float_p, c_float_p, c_float_p]),
@@ -102,8 +102,8 @@ SIGNATURES = {
     "spn_su2_set_cutoff": (C.c_int, [C.c_void_p, C.c_float]),
     "spn_su2_get_node_counts": (C.c_int, [C.c_void_p, c_int_p]),
     "spn_su2_compute_step": (C.c_int, [C.c_void_p]),
-    "spn_su2_autotune": (C.c_int, [C.c_void_p, C.c_int, c_int_p, c_int_p, c_int_p, c_int_p]),
-    "spn_su2_set_variant": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "spn_su2_autotune": (C.c_int, [C.c_void_p, C.c_int, c_int_p, c_int_p, c_int_p]),
+    "spn_su2_set_variant": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "spn_su2_get_flow": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p]),
     "spn_su2_finalize_step": (C.c_int, [C.c_void_p, C.c_float]),
     "spn_su2_measure_correlation": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p, c_float_p]),
@@ -118,7 +118,7 @@ SIGNATURES = {
     "spn_su2_get_profile": (C.c_int, [C.c_void_p, c_double_p, c_int_p, c_double_p, c_int_p]),
     "spn_batch_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
     "spn_batch_destroy": (C.c_int, [C.c_void_p]),
-    "spn_batch_set_variant": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "spn_batch_set_variant": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "spn_batch_footprint": (C.c_int, [C.POINTER(Su2Desc), C.c_int, c_ll_p]),
     "spn_batch_add": (C.c_int, [C.c_void_p, C.POINTER(Su2Desc), C.c_int, c_float_p, c_float_p, c_float_p, c_float_p,
                                 c_int_p]),

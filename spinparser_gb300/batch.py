@@ -32,14 +32,14 @@ class BatchResult:
 
 
 class Su2Batch:
-    def __init__(self, device: int = 0, nodes_per_iteration: int = 1, use_graph: bool = True, rpa_products: bool = False):
+    def __init__(self, device: int = 0, nodes_per_iteration: int = 1, use_graph: bool = True):
         lib = load_library()
         self._lib = lib
         self.device = device
         h = C.c_void_p()
         check(lib.spn_batch_create(device, C.byref(h)))
         self._h = h
-        check(lib.spn_batch_set_variant(h, nodes_per_iteration, int(use_graph), int(rpa_products)))
+        check(lib.spn_batch_set_variant(h, nodes_per_iteration, int(use_graph)))
         self._flows = {}
 
     def close(self) -> None:
@@ -50,9 +50,9 @@ class Su2Batch:
     def __del__(self):
         self.close()
 
-    def set_variant(self, nodes_per_iteration: int = 1, use_graph: bool = True, rpa_products: bool = False) -> None:
-        """Kernel variant for flows added from now on, and graph replay; results do not change."""
-        check(self._lib.spn_batch_set_variant(self._h, nodes_per_iteration, int(use_graph), int(rpa_products)))
+    def set_variant(self, nodes_per_iteration: int = 1, use_graph: bool = True) -> None:
+        """Kernel variant and graph replay; results do not change."""
+        check(self._lib.spn_batch_set_variant(self._h, nodes_per_iteration, int(use_graph)))
 
     @staticmethod
     def footprint(tables: LatticeTables, freq, n_cutoffs: int) -> int:

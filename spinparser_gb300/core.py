@@ -254,14 +254,13 @@ class Su2Flow:
 
     def autotune(self, reps: int = 3) -> dict:
         """Times the vertex-flow kernel variants on the current state and keeps the fastest."""
-        npi, sm, prod, grid = C.c_int(), C.c_int(), C.c_int(), C.c_int()
-        check(self._lib.spn_su2_autotune(self._h, reps, C.byref(npi), C.byref(sm), C.byref(prod), C.byref(grid)))
-        return {"nodes_per_iteration": npi.value, "schedule_in_smem": bool(sm.value), "rpa_products": bool(prod.value),
-                "grid": grid.value}
+        npi, sm, grid = C.c_int(), C.c_int(), C.c_int()
+        check(self._lib.spn_su2_autotune(self._h, reps, C.byref(npi), C.byref(sm), C.byref(grid)))
+        return {"nodes_per_iteration": npi.value, "schedule_in_smem": bool(sm.value), "grid": grid.value}
 
-    def set_variant(self, nodes_per_iteration: int, schedule_in_smem: bool, rpa_products: bool = False) -> None:
+    def set_variant(self, nodes_per_iteration: int, schedule_in_smem: bool) -> None:
         """Kernel variant (all variants give identical results)."""
-        check(self._lib.spn_su2_set_variant(self._h, nodes_per_iteration, int(schedule_in_smem), int(rpa_products)))
+        check(self._lib.spn_su2_set_variant(self._h, nodes_per_iteration, int(schedule_in_smem)))
 
     def get_flow(self):
         v2 = np.empty(self.n, np.float32)

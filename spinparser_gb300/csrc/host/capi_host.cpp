@@ -221,9 +221,9 @@ extern "C" int spn_su2_initial_state(const spn_lattice *lat, int n_freq, float n
 }
 
 extern "C" int spn_rpa_schedule(int n_sites, const int *overlap_ptr, const int *overlap_rid1, const int *overlap_rid2,
-                                int lanes, int products, int *info, int *sched, int *count, int *slot_base, int *seg_ptr) {
+                                int lanes, int *info, int *sched, int *count, int *slot_base, int *seg_ptr) {
     return spn::guarded([&] {
-        if (n_sites < 1 || n_sites > 128 || !overlap_ptr || !info || lanes < 1 || lanes > 32 || (products && n_sites > 32))
+        if (n_sites < 1 || n_sites > 128 || !overlap_ptr || !info || lanes < 1 || lanes > 32)
             throw spn::Error(spn::ErrorType::Argument, "spn_rpa_schedule: bad argument");
         const int nov = overlap_ptr[n_sites];
         for (int r = 0; r < n_sites; ++r)
@@ -231,11 +231,10 @@ extern "C" int spn_rpa_schedule(int n_sites, const int *overlap_ptr, const int *
         for (int i = 0; i < nov; ++i)
             if (overlap_rid1[i] < 0 || overlap_rid1[i] >= n_sites || overlap_rid2[i] < 0 || overlap_rid2[i] >= n_sites)
                 throw spn::Error(spn::ErrorType::Argument, "overlap entry out of range");
-        spn::RpaHostSchedule s = spn::build_rpa_schedule(n_sites, overlap_ptr, overlap_rid1, overlap_rid2, lanes, products != 0);
+        spn::RpaHostSchedule s = spn::build_rpa_schedule(n_sites, overlap_ptr, overlap_rid1, overlap_rid2, lanes);
         info[0] = s.len;
         info[1] = s.n_seg;
-        info[2] = products ? 1 : 0;
-        info[3] = int(s.sched.size());
+        info[2] = int(s.sched.size());
         if (!sched) return;
         std::memcpy(sched, s.sched.data(), s.sched.size() * sizeof(int));
         if (count) std::memcpy(count, s.count.data(), s.count.size() * sizeof(int));

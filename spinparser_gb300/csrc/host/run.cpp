@@ -260,13 +260,12 @@ private:
     }
 
     void autotune(float at) {
-        int npi = 0, smem = 0, prod = 0, grid = 0;
+        int npi = 0, smem = 0, grid = 0;
         check(spn_su2_set_cutoff(flow_.get(), at));
-        check(spn_su2_autotune(flow_.get(), 3, &npi, &smem, &prod, &grid));
+        check(spn_su2_autotune(flow_.get(), 3, &npi, &smem, &grid));
         check(spn_su2_set_cutoff(flow_.get(), cutoff_));
         log(LogLevel::Debug, "Vertex flow variant: " + std::to_string(npi) + " node(s) per iteration, schedule in " +
-                                 (smem ? "shared" : "global") + " memory, " + (prod ? "product" : "factor") +
-                                 "-form RPA, grid " + std::to_string(grid));
+                                 (smem ? "shared" : "global") + " memory, grid " + std::to_string(grid));
     }
 
     void take_measurements(bool postprocessing) {

@@ -174,7 +174,7 @@ struct spn_batch {
         bool used = false;
         size_t hist_row = 0;
     };
-    int device = 0, sms = 0, npi = 1, rpa_products = 0;
+    int device = 0, sms = 0, npi = 1;
     bool use_graph = true;
     cudaStream_t stream = nullptr;
     std::vector<Flow> flows;
@@ -317,7 +317,7 @@ struct spn_batch {
                 const long long next = prefix.back() + h->fn;
                 if (next >= (1ll << 31)) throw Error(ErrorType::Unsupported, "batch work list beyond 2^31 items");
                 prefix.push_back(int(next));
-                area = std::max(area, batch_vertex_warp_area(h->nl, h->rpa_n_seg, npi, h->rpa_products));
+                area = std::max(area, batch_vertex_warp_area(h->nl, h->rpa_n_seg, npi));
                 sched = std::max(sched, rpa_smem_ints(h->args().rpa, h->nl));
             }
             off_cp[c] = put(prefix);
@@ -425,12 +425,11 @@ extern "C" int spn_batch_destroy(spn_batch *b) {
     return SPN_OK;
 }
 
-extern "C" int spn_batch_set_variant(spn_batch *b, int npi, int use_graph, int rpa_products) {
+extern "C" int spn_batch_set_variant(spn_batch *b, int npi, int use_graph) {
     return guarded([&] {
         if (!b) throw Error(ErrorType::Argument, "null handle");
         if (npi != 1 && npi != 2) throw Error(ErrorType::Argument, "nodes per iteration must be 1 or 2");
         b->npi = npi;
-        b->rpa_products = rpa_products ? 1 : 0;
         b->use_graph = use_graph != 0;
         b->plan_valid = false;
     });
@@ -467,7 +466,6 @@ extern "C" int spn_batch_add(spn_batch *b, const spn_su2_desc *desc, int n_cutof
         spn_batch::Flow &f = b->flows[slot];
         try {
             f.h = create_flow(desc, b->stream);
-            f.h->rpa_products = (b->rpa_products && f.h->rpa_sched_p) ? 1 : 0;
             f.n_cutoffs = n_cutoffs;
             f.host_cutoffs.assign(cutoffs, cutoffs + n_cutoffs);
             f.cutoffs = dalloc<float>(n_cutoffs, "alloc batch cutoffs");

@@ -11,9 +11,7 @@ constexpr unsigned kStatusNodeOverflow = 2u;  // a loop-frequency node table ove
 // Lane-balanced RPA schedule (built by host/rpa_schedule.cpp): the RPA pair lists of all
 // rids merged into distinct (rid, rid1, rid2) with their multiplicity, sorted by rid and cut
 // into `lanes` contiguous chunks.  Entry i of lane l is sched[i * lanes + l]:
-//   factors (any Nl):     rid1 | rid2 << 7 | m << 14 | last << 22;
-//   products (Nl <= 32):  rid1 * Nl + rid2 | last << 15 | fp16(m) << 16.
-// Both encodings accumulate m * (A[rid1] * B[rid2]) in the same order (same bits).
+//   bits 0-6 rid1, bits 7-13 rid2, bits 14-21 multiplicity, bit 22 "last pair of a segment".
 // A segment is a run of pairs of one output rid inside one chunk; its partial sum goes to the
 // next slot of the lane (slot_base[l], slot_base[l]+1, ...), and rid r sums the slots
 // seg_ptr[r] .. seg_ptr[r+1]-1 in order.
@@ -24,7 +22,6 @@ struct RpaSchedule {
     const int *seg_ptr;    // [Nl + 1]
     int lanes, n_seg;
     int len;       // entries per lane
-    int products;  // product encoding (the kernel forms A * B products first)
     int in_smem;   // the kernel stages the schedule in shared memory
 };
 
@@ -93,7 +90,7 @@ struct BatchFlow {
 // per SM it achieves, and the launch.
 // `npi`: loop-frequency nodes a site group evaluates per iteration (1 or 2); whether the RPA
 // schedule is staged in shared memory is a.rpa.in_smem.  Both are chosen per flow by timing.
-size_t vertex_flow_smem_bytes(int nl, const RpaSchedule &rpa, int npi);  // rpa.products and rpa.in_smem count
+size_t vertex_flow_smem_bytes(int nl, const RpaSchedule &rpa, int npi);
 int vertex_flow_blocks_per_sm(int nl, const RpaSchedule &rpa, int npi);
 void launch_vertex_flow(const FlowArgs &a, int npi, int grid, cudaStream_t stream);
 
@@ -114,7 +111,7 @@ struct BatchVertexArgs {
     int warp_area;
     int sched_ints;
 };
-size_t batch_vertex_warp_area(int nl, int n_seg, int npi, int products);
+size_t batch_vertex_warp_area(int nl, int n_seg, int npi);
 size_t batch_vertex_smem_bytes(int n_max, size_t warp_area, int sched_ints);
 int batch_vertex_blocks_per_sm(int spt, int npi, size_t smem);
 void launch_batch_vertex(const BatchVertexArgs &b, int spt, int npi, int grid, cudaStream_t stream);

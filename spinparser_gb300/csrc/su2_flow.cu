@@ -142,23 +142,20 @@ void launch_vertex(spn_su2 *h) {
     cuda_check(cudaGetLastError(), "vertex flow launch");
 }
 
-// Selects a vertex-flow variant: nodes per iteration, where the RPA schedule lives and its
-// encoding (all variants give the same bits); the persistent grid fills every SM to the
-// variant's occupancy.  Returns false if it cannot run.
-bool select_variant(spn_su2 *h, int npi, int in_smem, int products) {
-    if (products && !h->rpa_sched_p) return false;
+// Selects a vertex-flow variant: nodes per iteration and where the RPA schedule lives (all
+// variants give the same bits); the persistent grid fills every SM to the variant's
+// occupancy.  Returns false if it cannot run.
+bool select_variant(spn_su2 *h, int npi, int in_smem) {
     if (in_smem) {
         RpaSchedule r = h->args().rpa;
         if (rpa_smem_ints(r, h->nl) > kRpaSmemMaxInts) return false;
     }
-    const int old_smem = h->rpa_in_smem, old_products = h->rpa_products;
+    const int old_smem = h->rpa_in_smem;
     h->rpa_in_smem = in_smem;
-    h->rpa_products = products;
     const int per_sm = vertex_flow_blocks_per_sm(h->nl, h->args().rpa, npi);
     cudaGetLastError();
     if (per_sm < 1) {
         h->rpa_in_smem = old_smem;
-        h->rpa_products = old_products;
         return false;
     }
     h->vertex_npi = npi;
@@ -320,16 +317,10 @@ spn_su2 *spn::create_flow(const spn_su2_desc *d, cudaStream_t stream) {
             cuda_check(cudaMemsetAsync(h->status, 0, sizeof(unsigned), h->stream), "memset");
             // balanced RPA schedule for the lanes of one node group
             const int lanes = spt_for(h->nl) == 1 ? wsite_for(h->nl) : 32;
-            RpaHostSchedule rpa = build_rpa_schedule(h->nl, d->overlap_ptr, d->overlap_rid1, d->overlap_rid2, lanes, false);
+            RpaHostSchedule rpa = build_rpa_schedule(h->nl, d->overlap_ptr, d->overlap_rid1, d->overlap_rid2, lanes);
             h->rpa_lanes = rpa.lanes;
             h->rpa_n_seg = rpa.n_seg;
             h->rpa_len = rpa.len;
-            if (spt_for(h->nl) == 1) {  // the product encoding of the same schedule
-                RpaHostSchedule rp =
-                    build_rpa_schedule(h->nl, d->overlap_ptr, d->overlap_rid1, d->overlap_rid2, lanes, true);
-                h->rpa_sched_p = dev_alloc<int>(rp.sched.size(), "alloc rpa schedule");
-                upload(h->rpa_sched_p, rp.sched.data(), rp.sched.size(), h->stream);
-            }
             h->rpa_sched = dev_alloc<int>(rpa.sched.size(), "alloc rpa schedule");
             h->rpa_count = dev_alloc<int>(rpa.count.size(), "alloc rpa schedule");
             h->rpa_slot_base = dev_alloc<int>(rpa.slot_base.size(), "alloc rpa schedule");
@@ -344,7 +335,7 @@ spn_su2 *spn::create_flow(const spn_su2_desc *d, cudaStream_t stream) {
             h->sms = sms;
             // default variant (schedule staged in shared memory where it fits); spn_su2_autotune
             // can pick a faster one for this flow
-            if (!select_variant(h, 1, 1, 0) && !select_variant(h, 1, 0, 0))
+            if (!select_variant(h, 1, 1) && !select_variant(h, 1, 0))
                 throw Error(ErrorType::Unsupported, "vertex-flow kernel does not fit on this device");
             cuda_check(cudaStreamSynchronize(h->stream), "create sync");
         } catch (...) {
@@ -470,17 +461,17 @@ extern "C" int spn_su2_compute_step(spn_su2 *h) {
     });
 }
 
-extern "C" int spn_su2_set_variant(spn_su2 *h, int npi, int sched_in_smem, int rpa_products) {
+extern "C" int spn_su2_set_variant(spn_su2 *h, int npi, int sched_in_smem) {
     return guarded([&] {
         if (!h) throw Error(ErrorType::Argument, "null handle");
         if (npi != 1 && npi != 2) throw Error(ErrorType::Argument, "nodes per iteration must be 1 or 2");
         cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
-        if (!select_variant(h, npi, sched_in_smem ? 1 : 0, rpa_products ? 1 : 0))
+        if (!select_variant(h, npi, sched_in_smem ? 1 : 0))
             throw Error(ErrorType::Unsupported, "vertex-flow variant does not fit on this device for this lattice");
     });
 }
 
-extern "C" int spn_su2_autotune(spn_su2 *h, int reps, int *npi, int *sched_in_smem, int *rpa_products, int *grid) {
+extern "C" int spn_su2_autotune(spn_su2 *h, int reps, int *npi, int *sched_in_smem, int *grid) {
     return guarded([&] {
         if (!h) throw Error(ErrorType::Argument, "null handle");
         cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
@@ -491,14 +482,13 @@ extern "C" int spn_su2_autotune(spn_su2 *h, int reps, int *npi, int *sched_in_sm
         const bool prof = h->profiling;
         h->profiling = false;
         float best = 0.0f;
-        int best_npi = h->vertex_npi, best_smem = h->rpa_in_smem, best_prod = h->rpa_products;
+        int best_npi = h->vertex_npi, best_smem = h->rpa_in_smem;
         try {
             // the node tables of the current cutoff (compute_step leaves the state untouched)
             cuda_check(spn_su2_compute_step(h) == 0 ? cudaSuccess : cudaErrorUnknown, "autotune step");
-            for (int prod = 0; prod <= 1; ++prod)
             for (int npi = 1; npi <= 2; ++npi)
                 for (int sm = 0; sm <= 1; ++sm) {
-                    if (!select_variant(h, npi, sm, prod)) continue;
+                    if (!select_variant(h, npi, sm)) continue;
                     std::vector<float> ms;
                     for (int r = 0; r <= reps; ++r) {
                         cuda_check(cudaMemsetAsync(h->work_counter, 0, sizeof(int), h->stream), "memset counter");
@@ -516,7 +506,6 @@ extern "C" int spn_su2_autotune(spn_su2 *h, int reps, int *npi, int *sched_in_sm
                         best = med;
                         best_npi = npi;
                         best_smem = sm;
-                        best_prod = prod;
                     }
                 }
         } catch (...) {
@@ -528,11 +517,9 @@ extern "C" int spn_su2_autotune(spn_su2 *h, int reps, int *npi, int *sched_in_sm
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         h->profiling = prof;
-        if (!select_variant(h, best_npi, best_smem, best_prod))
-            throw Error(ErrorType::Internal, "autotune: chosen variant unavailable");
+        if (!select_variant(h, best_npi, best_smem)) throw Error(ErrorType::Internal, "autotune: chosen variant unavailable");
         if (npi) *npi = h->vertex_npi;
         if (sched_in_smem) *sched_in_smem = h->rpa_in_smem;
-        if (rpa_products) *rpa_products = h->rpa_products;
         if (grid) *grid = h->vertex_grid;
     });
 }

@@ -35,8 +35,7 @@ struct spn_su2 {
     double *corr_partial = nullptr;
     double *v2d = nullptr, *dv2d = nullptr;  // FP64 self-energy (SPN_SU2_FP64_SELF_ENERGY)
     int *rpa_sched = nullptr, *rpa_count = nullptr, *rpa_slot_base = nullptr, *rpa_seg_ptr = nullptr;
-    int rpa_lanes = 0, rpa_n_seg = 0, rpa_len = 0, rpa_products = 0, rpa_in_smem = 0;
-    int *rpa_sched_p = nullptr;  // product encoding (Nl <= 32), same order as rpa_sched
+    int rpa_lanes = 0, rpa_n_seg = 0, rpa_len = 0, rpa_in_smem = 0;
     int vertex_npi = 1;       // loop-frequency nodes per site-group iteration
     int sms = 0;
     bool profiling = false;
@@ -82,8 +81,6 @@ struct spn_su2 {
         a.rpa.lanes = rpa_lanes;
         a.rpa.n_seg = rpa_n_seg;
         a.rpa.len = rpa_len;
-        a.rpa.products = rpa_products;
-        if (rpa_products) a.rpa.sched = rpa_sched_p;
         a.rpa.in_smem = rpa_in_smem;
         return a;
     }
@@ -102,7 +99,7 @@ struct spn_su2 {
         void *ptrs[] = {freq,      ss,        dd,        dss,       ddd,          v2,          dv2,
                         node_wp,   node_c,    corr_out,  node_cnt,  work_counter, status,      sites,
                         inv_sites, ov_ptr,    ov_r1,     ov_r2,     range_rid,    range_inv,   corr_rid,
-                        corr_partial, rpa_sched, rpa_count, rpa_slot_base, rpa_seg_ptr, v2d, dv2d, rpa_sched_p};
+                        corr_partial, rpa_sched, rpa_count, rpa_slot_base, rpa_seg_ptr, v2d, dv2d};
         for (void *p : ptrs)
             if (p) cudaFree(p);
         if (own_stream && stream) cudaStreamDestroy(stream);

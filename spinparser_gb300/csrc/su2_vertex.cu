@@ -21,7 +21,6 @@
 // Accumulation over nodes is Kahan-compensated FP32; group partials are combined by shuffles.
 #include "su2_common.cuh"
 #include "su2_device.cuh"
-#include <cuda_fp16.h>
 
 namespace spn {
 namespace {
@@ -30,7 +29,7 @@ using namespace spn::dev;
 
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
-constexpr int kBatch = 16;  // nodes whose descriptors a warp builds at once (phase A)
+constexpr int kBatch = 32;  // nodes whose descriptors a warp builds at once (phase A)
 constexpr double kPi = 3.14159265358979323846;
 
 struct __align__(16) NodeDesc {
@@ -135,16 +134,12 @@ __device__ __forceinline__ void kahan_add(float &sum, float &comp, float v) {
     sum = t;
 }
 
-// Per-group shared-memory exchange area of the t channel.
-//   Nl <= 32 (one site per lane): A2/B2 hold (spin, density) of the third / fourth slab per
-//     site, P2[a * Nl + b] = A2[a] * B2[b] (both channels), then the RPA sums m * P2[ab] over
-//     the product-encoded schedule.
-//   Nl > 32: spin and density in separate 32-bit arrays As/Ad/Bs/Bd, and the RPA multiplies
-//     A[rid1] * m by B[rid2] over the factor-encoded schedule.
+// Per-group shared-memory exchange area of the t channel.  Spin and density values are kept
+// in separate 32-bit arrays: with Nl <= 32 every element sits in its own bank, so the RPA
+// gathers A[rid1], B[rid2] of a warp never conflict.
 struct TExchange {
-    float *As, *Ad;  // [sites] spin / density of the third slab   (Nl > 32)
-    float *Bs, *Bd;  // [sites] spin / density of the fourth slab  (Nl > 32)
-    float2 *A2, *B2, *P2;  // (Nl <= 32)
+    float *As, *Ad;  // [sites] spin / density of the third slab
+    float *Bs, *Bd;  // [sites] spin / density of the fourth slab
     float2 *slots;   // [n_seg] RPA segment partials
     const int *sched, *count, *slot_base, *seg_ptr;  // RPA schedule (shared or global memory)
 };
@@ -193,61 +188,8 @@ __device__ __forceinline__ void node_term(const FlowArgs &a, const NodeDesc *con
             }
         return;
     }
-    // t channel: RPA lattice sum (SU2FrgCore.cpp:249-266) over the balanced schedule.  Both
-    // encodings accumulate acc += m * (A[rid1] * B[rid2]) in the schedule's order.
-    if (SPT == 1 && a.rpa.products) {
-        if (ln.valid[0]) {
-            const int j = ln.j[0];
-#pragma unroll
-            for (int n = 0; n < NPI; ++n) {
-                tx[n].A2[j] = make_float2(S2[n][0], D2[n][0]);
-                tx[n].B2[j] = make_float2(S3[n][0], D3[n][0]);
-            }
-        }
-        __syncwarp();
-        // products of both channels: lane jl forms column b = jl
-        const int nl = a.nl;
-        if (jl < nl) {
-#pragma unroll
-            for (int n = 0; n < NPI; ++n) {
-                const float2 bb = tx[n].B2[jl];
-                const float2 *A2 = tx[n].A2;
-                float2 *P2 = tx[n].P2 + jl;
-                for (int q = 0; q < nl; ++q) {
-                    const float2 av = A2[q];
-                    P2[q * nl] = make_float2(av.x * bb.x, av.y * bb.y);
-                }
-            }
-        }
-        __syncwarp();
-        const int lanes = a.rpa.lanes;
-        const int cnt = tx[0].count[jl];
-        int slot = tx[0].slot_base[jl];
-        float acc_s[NPI], acc_d[NPI];
-#pragma unroll
-        for (int n = 0; n < NPI; ++n) acc_s[n] = acc_d[n] = 0.0f;
-        const int *sched = tx[0].sched + jl;
-        for (int i = 0; i < cnt; ++i) {
-            const int e = sched[i * lanes];
-            const float m = __half2float(__ushort_as_half((unsigned short)((unsigned)e >> 16)));
-            const int ab = e & 0x7fff;
-#pragma unroll
-            for (int n = 0; n < NPI; ++n) {
-                const float2 p = tx[n].P2[ab];
-                acc_s[n] = fmaf(m, p.x, acc_s[n]);
-                acc_d[n] = fmaf(m, p.y, acc_d[n]);
-            }
-            if (e & (1 << 15)) {  // last pair of a segment
-#pragma unroll
-                for (int n = 0; n < NPI; ++n) {
-                    tx[n].slots[slot] = make_float2(acc_s[n], acc_d[n]);
-                    acc_s[n] = 0.0f;
-                    acc_d[n] = 0.0f;
-                }
-                ++slot;
-            }
-        }
-    } else {
+    // t channel: RPA lattice sum (SU2FrgCore.cpp:249-266) over the balanced schedule
+    {
 #pragma unroll
         for (int n = 0; n < NPI; ++n)
 #pragma unroll
@@ -273,8 +215,8 @@ __device__ __forceinline__ void node_term(const FlowArgs &a, const NodeDesc *con
             const int ra = e & 0x7f, rb = (e >> 7) & 0x7f;
 #pragma unroll
             for (int n = 0; n < NPI; ++n) {
-                acc_s[n] = fmaf(m, tx[n].As[ra] * tx[n].Bs[rb], acc_s[n]);
-                acc_d[n] = fmaf(m, tx[n].Ad[ra] * tx[n].Bd[rb], acc_d[n]);
+                acc_s[n] = fmaf(tx[n].As[ra] * m, tx[n].Bs[rb], acc_s[n]);
+                acc_d[n] = fmaf(tx[n].Ad[ra] * m, tx[n].Bd[rb], acc_d[n]);
             }
             if (e & (1 << 22)) {
 #pragma unroll
@@ -376,24 +318,14 @@ __device__ __forceinline__ void channel_sum(const FlowArgs &a, const float *pos,
 // Shared memory of the single-flow kernel: frequency mesh; the RPA schedule when it is staged;
 // then per warp: 32 node descriptors and, per node group, NPI t-channel exchange areas (four
 // arrays of W*SPT sites and n_seg slots each).
-// Bytes of one node's t-channel exchange area.  With one site per lane it holds A2, B2 (wsite
-// float2 each), P2 (Nl^2 float2) and the slots; its size is padded so that the groups sharing
-// a half-warp (stride npi * area) sit min(wsite, 16) 8-byte words apart modulo 16, which keeps
-// their product reads on different banks (the schedule spreads a group's reads over the
-// residues modulo min(wsite, 16)).
-__host__ __device__ inline size_t node_area_bytes(int wsite, int spt, int n_seg, int nl, int npi, int products) {
-    if (spt != 1 || !products) return (sizeof(float) * 4 * size_t(wsite) * spt + sizeof(float2) * n_seg + 15) / 16 * 16;
-    size_t b = (sizeof(float2) * (2 * size_t(wsite) + size_t(nl) * nl + n_seg) + 15) / 16 * 16;
-    const int hw = wsite < 16 ? wsite : 16;
-    if (hw % 2 == 0)
-        for (int k = 0; k < 16 && (npi * b / 8) % 16 != size_t(hw % 16); ++k) b += 16;
-    return b;
+__host__ __device__ inline size_t node_area_bytes(int wsite, int spt, int n_seg) {
+    return (sizeof(float) * 4 * size_t(wsite) * spt + sizeof(float2) * n_seg + 15) / 16 * 16;
 }
-__host__ __device__ inline size_t group_area_bytes(int wsite, int spt, int npi, int n_seg, int nl, int products) {
-    return (32 / wsite) * npi * node_area_bytes(wsite, spt, n_seg, nl, npi, products);
+__host__ __device__ inline size_t group_area_bytes(int wsite, int spt, int npi, int n_seg) {
+    return (32 / wsite) * npi * node_area_bytes(wsite, spt, n_seg);
 }
-__host__ __device__ inline size_t warp_bytes(int wsite, int spt, int npi, int n_seg, int nl, int products) {
-    return kBatch * sizeof(NodeDesc) + group_area_bytes(wsite, spt, npi, n_seg, nl, products);
+__host__ __device__ inline size_t warp_bytes(int wsite, int spt, int npi, int n_seg) {
+    return kBatch * sizeof(NodeDesc) + group_area_bytes(wsite, spt, npi, n_seg);
 }
 __host__ __device__ inline size_t sched_bytes(const RpaSchedule &r, int nl) {
     return r.in_smem ? (sizeof(int) * size_t(rpa_smem_ints(r, nl)) + 15) / 16 * 16 : 0;
@@ -420,27 +352,17 @@ __device__ __forceinline__ void setup_ctx(const FlowArgs &a, int lane, NodeDesc 
     c.G = 32 / c.W;
     c.g = lane / c.W;
     c.jl = lane - c.g * c.W;
-    const size_t nab = node_area_bytes(c.W, SPT, a.rpa.n_seg, a.nl, NPI, a.rpa.products);
+    const size_t nab = node_area_bytes(c.W, SPT, a.rpa.n_seg);
     unsigned char *gbase = groups + size_t(c.g) * NPI * nab;
     const int ws = c.W * SPT;
 #pragma unroll
     for (int n = 0; n < NPI; ++n) {
         float *gx = reinterpret_cast<float *>(gbase + n * nab);
-        if (SPT == 1 && a.rpa.products) {
-            float2 *g2 = reinterpret_cast<float2 *>(gx);
-            c.tx[n].A2 = g2;
-            c.tx[n].B2 = g2 + ws;
-            c.tx[n].P2 = g2 + 2 * ws;
-            c.tx[n].slots = g2 + 2 * ws + a.nl * a.nl;
-            c.tx[n].As = c.tx[n].Ad = c.tx[n].Bs = c.tx[n].Bd = nullptr;
-        } else {
-            c.tx[n].As = gx;
-            c.tx[n].Ad = gx + ws;
-            c.tx[n].Bs = gx + 2 * ws;
-            c.tx[n].Bd = gx + 3 * ws;
-            c.tx[n].slots = reinterpret_cast<float2 *>(gx + 4 * ws);
-            c.tx[n].A2 = c.tx[n].B2 = c.tx[n].P2 = nullptr;
-        }
+        c.tx[n].As = gx;
+        c.tx[n].Ad = gx + ws;
+        c.tx[n].Bs = gx + 2 * ws;
+        c.tx[n].Bd = gx + 3 * ws;
+        c.tx[n].slots = reinterpret_cast<float2 *>(gx + 4 * ws);
         c.tx[n].sched = sched;
         c.tx[n].count = count;
         c.tx[n].slot_base = slot_base;
@@ -532,7 +454,7 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_flow_kernel(FlowArgs a) {
         slot_base = a.rpa.slot_base;
         seg_ptr = a.rpa.seg_ptr;
     }
-    unsigned char *wbase = sbase + sched_bytes(a.rpa, a.nl) + warp * warp_bytes(W, SPT, NPI, n_seg, a.nl, a.rpa.products);
+    unsigned char *wbase = sbase + sched_bytes(a.rpa, a.nl) + warp * warp_bytes(W, SPT, NPI, n_seg);
     WarpCtx<SPT, NPI> c;
     setup_ctx<SPT, NPI>(a, lane, reinterpret_cast<NodeDesc *>(wbase), wbase + kBatch * sizeof(NodeDesc), sched, count,
                         slot_base, seg_ptr, c);
@@ -626,7 +548,7 @@ int wsite_of(int nl) {
 size_t vertex_flow_smem_bytes(int nl, const RpaSchedule &rpa, int npi) {
     const int spt = spt_of(nl);
     return kMaxFreq * sizeof(float) + sched_bytes(rpa, nl) +
-           kWarps * warp_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, rpa.n_seg, nl, rpa.products);
+           kWarps * warp_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, rpa.n_seg);
 }
 
 namespace {
@@ -656,9 +578,9 @@ void launch_vertex_flow(const FlowArgs &a, int npi, int grid, cudaStream_t strea
 
 int vertex_spt(int nl) { return spt_of(nl); }
 
-size_t batch_vertex_warp_area(int nl, int n_seg, int npi, int products) {
+size_t batch_vertex_warp_area(int nl, int n_seg, int npi) {
     const int spt = spt_of(nl);
-    return group_area_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, n_seg, nl, products);
+    return group_area_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, n_seg);
 }
 
 size_t batch_vertex_smem_bytes(int n_max, size_t warp_area, int sched_ints) {

@@ -75,9 +75,8 @@ def device_memory(device: int = 0):
 
 class FlowServer:
     def __init__(self, device: int = 0, memory_budget: int | None = None, max_flows: int | None = None,
-                 nodes_per_iteration: int = 1, use_graph: bool = True, rpa_products: bool = False,
-                 clock=time.perf_counter):
-        self.batch = Su2Batch(device, nodes_per_iteration, use_graph, rpa_products)
+                 nodes_per_iteration: int = 1, use_graph: bool = True, clock=time.perf_counter):
+        self.batch = Su2Batch(device, nodes_per_iteration, use_graph)
         if memory_budget is None:
             free, _ = device_memory(device)
             memory_budget = int(0.8 * free)

@@ -118,12 +118,11 @@ def test_diverging_flow_does_not_disturb_its_neighbours(reference):
     assert_same(b, good, reference["square-r3"], "square-r3")
 
 
-@pytest.mark.parametrize("npi,products", [(2, False), (1, True), (2, True)])
-def test_other_variants_give_the_same_bits(reference, npi, products):
-    """Batches with other kernel variants (2 nodes per iteration, product-form RPA) against
-    the flows run alone with the default variant."""
+def test_other_variant_gives_the_same_bits(reference):
+    """A batch with the other kernel variant (2 nodes per iteration) against the flows run
+    alone with the default variant."""
     names = ("square-r3", "square-r11", "pyrochlore-r2", "cubic-r3-fp64")
-    b = Su2Batch(nodes_per_iteration=npi, rpa_products=products)
+    b = Su2Batch(nodes_per_iteration=2)
     ids = {n: add(b, n) for n in names}
     b.run()
     for n, fid in ids.items():
