@@ -61,13 +61,18 @@ RpaHostSchedule build_rpa_schedule(int nl, const int *ptr, const int *r1, const 
     for (int r = nl - 1; r >= 0; --r)
         if (s.seg_ptr[r] < 0) s.seg_ptr[r] = s.seg_ptr[r + 1];
 
+    s.packed = nl <= 32;
+    const unsigned scale = nl <= 16 ? 8u : 4u;
+
     for (int l = 0; l < lanes; ++l) {
         size_t si = 0;
         for (int i = 0; i < s.count[l]; ++i) {
             const Pair &p = order[l][i];
             const bool last = (i + 1 == seg_end[l][si]);
             if (last) ++si;
-            s.sched[size_t(i) * lanes + l] = p.a | (p.b << 7) | (p.m << 14) | (last ? (1 << 22) : 0);
+            s.sched[size_t(i) * lanes + l] =
+                s.packed ? int(scale * p.a | (scale * p.b) << 8 | unsigned(p.m) << 16 | (last ? 0x80000000u : 0u))
+                         : p.a | (p.b << 7) | (p.m << 14) | (last ? (1 << 22) : 0);
         }
     }
     return s;

@@ -134,15 +134,36 @@ __device__ __forceinline__ void kahan_add(float &sum, float &comp, float v) {
     sum = t;
 }
 
-// Per-group shared-memory exchange area of the t channel.  Spin and density values are kept
-// in separate 32-bit arrays: with Nl <= 32 every element sits in its own bank, so the RPA
-// gathers A[rid1], B[rid2] of a warp never conflict.
+// Per-group shared-memory exchange area of the t channel: the (spin, density) values of the
+// third and fourth slab per site, then the RPA segment partials.
+//   Nl <= 16: interleaved float2 pairs A2, B2 (every element its own 8-byte bank pair), one
+//     64-bit load each;
+//   otherwise: separate 32-bit arrays As, Ad, Bs, Bd (every element its own bank for Nl <= 32).
+// With one site per lane the spin and density sums run as packed f32x2 arithmetic.
 struct TExchange {
-    float *As, *Ad;  // [sites] spin / density of the third slab
-    float *Bs, *Bd;  // [sites] spin / density of the fourth slab
+    float *As, *Ad;  // [sites] spin / density of the third slab   (Nl > 32)
+    float *Bs, *Bd;  // [sites] spin / density of the fourth slab  (Nl > 32)
+    float2 *A2, *B2;  // [sites] (spin, density) of the third / fourth slab (Nl <= 16)
     float2 *slots;   // [n_seg] RPA segment partials
     const int *sched, *count, *slot_base, *seg_ptr;  // RPA schedule (shared or global memory)
 };
+
+// Packed single-precision pairs (fma.rn.f32x2 / mul.rn.f32x2): per element the same IEEE
+// round-to-nearest results as fmaf and a * b.
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 x, y, z;\n\tmov.b64 x, {%2, %3};\n\tmov.b64 y, {%4, %5};\n\t"
+        "mul.rn.f32x2 z, x, y;\n\tmov.b64 {%0, %1}, z;\n}"
+        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    float2 d;
+    asm("{\n\t.reg .b64 x, y, z, w;\n\tmov.b64 x, {%2, %3};\n\tmov.b64 y, {%4, %5};\n\tmov.b64 z, {%6, %7};\n\t"
+        "fma.rn.f32x2 w, x, y, z;\n\tmov.b64 {%0, %1}, w;\n}"
+        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
 
 // K_X at NPI nodes for this lane's sites (one group evaluates NPI nodes per iteration so that
 // the t channel decodes each RPA schedule entry once for all of them).
@@ -188,8 +209,84 @@ __device__ __forceinline__ void node_term(const FlowArgs &a, const NodeDesc *con
             }
         return;
     }
-    // t channel: RPA lattice sum (SU2FrgCore.cpp:249-266) over the balanced schedule
-    {
+    // t channel: RPA lattice sum (SU2FrgCore.cpp:249-266) over the balanced schedule; both
+    // forms accumulate acc += (A[rid1] * m) * B[rid2] per channel in schedule order
+    if (SPT == 1) {
+        const bool pairs = a.nl <= 16;  // interleaved (spin, density) pairs, else separate arrays
+        if (ln.valid[0]) {
+            const int j = ln.j[0];
+#pragma unroll
+            for (int n = 0; n < NPI; ++n) {
+                if (pairs) {
+                    tx[n].A2[j] = make_float2(S2[n][0], D2[n][0]);
+                    tx[n].B2[j] = make_float2(S3[n][0], D3[n][0]);
+                } else {
+                    tx[n].As[j] = S2[n][0];
+                    tx[n].Ad[j] = D2[n][0];
+                    tx[n].Bs[j] = S3[n][0];
+                    tx[n].Bd[j] = D3[n][0];
+                }
+            }
+        }
+        __syncwarp();
+        const int lanes = a.rpa.lanes;
+        const int cnt = tx[0].count[jl];
+        int slot = tx[0].slot_base[jl];
+        float2 acc[NPI];
+#pragma unroll
+        for (int n = 0; n < NPI; ++n) acc[n] = make_float2(0.0f, 0.0f);
+        const int *sched = tx[0].sched + jl;
+        // exchanged (spin, density) values of entry e for node n
+        auto fetch = [&](int e, int n, float2 &av, float2 &bv) {
+            const unsigned oa = unsigned(e) & 0xffu, ob = (unsigned(e) >> 8) & 0xffu;  // byte offsets
+            if (pairs) {
+                av = *reinterpret_cast<const float2 *>(reinterpret_cast<const char *>(tx[n].A2) + oa);
+                bv = *reinterpret_cast<const float2 *>(reinterpret_cast<const char *>(tx[n].B2) + ob);
+            } else {
+                av.x = *reinterpret_cast<const float *>(reinterpret_cast<const char *>(tx[n].As) + oa);
+                av.y = *reinterpret_cast<const float *>(reinterpret_cast<const char *>(tx[n].Ad) + oa);
+                bv.x = *reinterpret_cast<const float *>(reinterpret_cast<const char *>(tx[n].Bs) + ob);
+                bv.y = *reinterpret_cast<const float *>(reinterpret_cast<const char *>(tx[n].Bd) + ob);
+            }
+        };
+        auto accumulate = [&](int e, const float2 *av, const float2 *bv) {
+            const float m = float((e >> 16) & 0xff);
+            const float2 m2 = make_float2(m, m);
+#pragma unroll
+            for (int n = 0; n < NPI; ++n) acc[n] = fma2(mul2(av[n], m2), bv[n], acc[n]);
+            if (e < 0) {  // last pair of a segment
+#pragma unroll
+                for (int n = 0; n < NPI; ++n) {
+                    tx[n].slots[slot] = acc[n];
+                    acc[n] = make_float2(0.0f, 0.0f);
+                }
+                ++slot;
+            }
+        };
+        // four entries at a time: their schedule words and values are loaded before the
+        // accumulations (which stay in schedule order), so the loads overlap
+        constexpr int kU = 4;
+        int i = 0;
+        for (; i + kU <= cnt; i += kU) {
+            int e[kU];
+            float2 av[kU][NPI], bv[kU][NPI];
+#pragma unroll
+            for (int u = 0; u < kU; ++u) e[u] = sched[(i + u) * lanes];
+#pragma unroll
+            for (int u = 0; u < kU; ++u)
+#pragma unroll
+                for (int n = 0; n < NPI; ++n) fetch(e[u], n, av[u][n], bv[u][n]);
+#pragma unroll
+            for (int u = 0; u < kU; ++u) accumulate(e[u], av[u], bv[u]);
+        }
+        for (; i < cnt; ++i) {
+            const int e = sched[i * lanes];
+            float2 av[NPI], bv[NPI];
+#pragma unroll
+            for (int n = 0; n < NPI; ++n) fetch(e, n, av[n], bv[n]);
+            accumulate(e, av, bv);
+        }
+    } else {
 #pragma unroll
         for (int n = 0; n < NPI; ++n)
 #pragma unroll
@@ -362,6 +459,8 @@ __device__ __forceinline__ void setup_ctx(const FlowArgs &a, int lane, NodeDesc 
         c.tx[n].Ad = gx + ws;
         c.tx[n].Bs = gx + 2 * ws;
         c.tx[n].Bd = gx + 3 * ws;
+        c.tx[n].A2 = reinterpret_cast<float2 *>(gx);       // same bytes, used when Nl <= 16
+        c.tx[n].B2 = reinterpret_cast<float2 *>(gx) + ws;
         c.tx[n].slots = reinterpret_cast<float2 *>(gx + 4 * ws);
         c.tx[n].sched = sched;
         c.tx[n].count = count;

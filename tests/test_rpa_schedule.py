@@ -26,7 +26,7 @@ def schedule(tab, lanes):
     lib = load_library()
     ip = C.POINTER(C.c_int)
     ptr, r1, r2 = (np.ascontiguousarray(x, np.int32) for x in (tab.overlap_ptr, tab.overlap_rid1, tab.overlap_rid2))
-    info = np.zeros(3, np.int32)
+    info = np.zeros(4, np.int32)
     args = (tab.n_sites, ptr.ctypes.data_as(ip), r1.ctypes.data_as(ip), r2.ctypes.data_as(ip), lanes)
     check(lib.spn_rpa_schedule(*args, info.ctypes.data_as(ip), None, None, None, None))
     sched = np.zeros(info[2], np.int32)
@@ -40,15 +40,21 @@ def schedule(tab, lanes):
 
 def decode(nl, lanes, info, sched, count, base, seg, A, B):
     """The kernel's walk: per lane, accumulate (A[a] * m) * B[b], flush at segment ends."""
-    L, n_seg = info[0], info[1]
-    assert info[2] == L * lanes
+    L, n_seg, packed = info[0], info[1], bool(info[3])
+    assert info[2] == L * lanes and packed == (nl <= 32)
     slots = np.zeros(n_seg)
     for l in range(lanes):
         assert 0 <= count[l] <= L
         acc, slot = 0.0, base[l]
         for i in range(count[l]):
-            e = int(sched[i * lanes + l])
-            a, b, m, last = e & 0x7F, (e >> 7) & 0x7F, float((e >> 14) & 0xFF), bool(e & (1 << 22))
+            e = int(np.uint32(sched[i * lanes + l]))
+            if packed:  # byte offsets: float2 arrays up to 16 sites, float arrays above
+                scale = 8 if nl <= 16 else 4
+                oa, ob = e & 0xFF, (e >> 8) & 0xFF
+                assert oa % scale == 0 and ob % scale == 0
+                a, b, m, last = oa // scale, ob // scale, float((e >> 16) & 0xFF), bool(e >> 31)
+            else:
+                a, b, m, last = e & 0x7F, (e >> 7) & 0x7F, float((e >> 14) & 0xFF), bool(e & (1 << 22))
             assert a < nl and b < nl and m >= 1
             acc += A[a] * m * B[b]
             if last:
@@ -73,3 +79,4 @@ def test_schedule_reproduces_rpa_sums(lat):
     np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-12)
     # merging repeated pairs shortens the walk
     assert schedule(tab, lanes)[0][0] * lanes < ptr[-1] + lanes
+
