@@ -7,6 +7,8 @@ namespace spn {
 
 constexpr unsigned kStatusNaN = 1u;           // a NaN was written into the flow
 constexpr unsigned kStatusNodeOverflow = 2u;  // a loop-frequency node table overflowed
+constexpr unsigned kStatusStageTimeout = 4u;  // a bulk copy to shared memory did not complete in
+                                              // time; the kernel read global memory instead
 
 // Lane-balanced RPA schedule (built by host/rpa_schedule.cpp): the RPA pair lists of all
 // rids merged into distinct (rid, rid1, rid2) with their multiplicity, sorted by rid and cut
@@ -23,6 +25,8 @@ struct RpaSchedule {
     int lanes, n_seg;
     int len;       // entries per lane
     int in_smem;   // the kernel stages the schedule in shared memory
+    const int *image;  // sched | count | slot_base | seg_ptr contiguous, as staged (16-byte aligned)
+    int image_bytes;   // multiple of 16
 };
 
 // Shared-memory words of a staged schedule (sched, count, slot_base, seg_ptr).

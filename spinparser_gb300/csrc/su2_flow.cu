@@ -321,14 +321,20 @@ spn_su2 *spn::create_flow(const spn_su2_desc *d, cudaStream_t stream) {
             h->rpa_lanes = rpa.lanes;
             h->rpa_n_seg = rpa.n_seg;
             h->rpa_len = rpa.len;
-            h->rpa_sched = dev_alloc<int>(rpa.sched.size(), "alloc rpa schedule");
-            h->rpa_count = dev_alloc<int>(rpa.count.size(), "alloc rpa schedule");
-            h->rpa_slot_base = dev_alloc<int>(rpa.slot_base.size(), "alloc rpa schedule");
-            h->rpa_seg_ptr = dev_alloc<int>(rpa.seg_ptr.size(), "alloc rpa schedule");
-            upload(h->rpa_sched, rpa.sched.data(), rpa.sched.size(), h->stream);
-            upload(h->rpa_count, rpa.count.data(), rpa.count.size(), h->stream);
-            upload(h->rpa_slot_base, rpa.slot_base.data(), rpa.slot_base.size(), h->stream);
-            upload(h->rpa_seg_ptr, rpa.seg_ptr.data(), rpa.seg_ptr.size(), h->stream);
+            // one image in the staged layout (what the kernel copies to shared memory in one bulk
+            // transfer), padded to 16 bytes
+            std::vector<int> image(rpa.sched);
+            image.insert(image.end(), rpa.count.begin(), rpa.count.end());
+            image.insert(image.end(), rpa.slot_base.begin(), rpa.slot_base.end());
+            image.insert(image.end(), rpa.seg_ptr.begin(), rpa.seg_ptr.end());
+            image.resize((image.size() + 3) / 4 * 4, 0);
+            h->rpa_image = dev_alloc<int>(image.size(), "alloc rpa schedule");
+            upload(h->rpa_image, image.data(), image.size(), h->stream);
+            h->rpa_image_bytes = int(image.size() * sizeof(int));
+            h->rpa_sched = h->rpa_image;
+            h->rpa_count = h->rpa_sched + rpa.sched.size();
+            h->rpa_slot_base = h->rpa_count + rpa.count.size();
+            h->rpa_seg_ptr = h->rpa_slot_base + rpa.slot_base.size();
             // persistent vertex grid: every SM filled to its occupancy limit
             int sms = 0;
             cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device), "device attribute");

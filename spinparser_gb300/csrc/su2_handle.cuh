@@ -34,7 +34,9 @@ struct spn_su2 {
     int *range_rid = nullptr, *range_inv = nullptr, *corr_rid = nullptr;
     double *corr_partial = nullptr;
     double *v2d = nullptr, *dv2d = nullptr;  // FP64 self-energy (SPN_SU2_FP64_SELF_ENERGY)
-    int *rpa_sched = nullptr, *rpa_count = nullptr, *rpa_slot_base = nullptr, *rpa_seg_ptr = nullptr;
+    int *rpa_image = nullptr;  // sched | count | slot_base | seg_ptr in one allocation (the staged layout)
+    int *rpa_sched = nullptr, *rpa_count = nullptr, *rpa_slot_base = nullptr, *rpa_seg_ptr = nullptr;  // into rpa_image
+    int rpa_image_bytes = 0;
     int rpa_lanes = 0, rpa_n_seg = 0, rpa_len = 0, rpa_in_smem = 0;
     int vertex_npi = 1;       // loop-frequency nodes per site-group iteration
     int sms = 0;
@@ -78,6 +80,8 @@ struct spn_su2 {
         a.rpa.count = rpa_count;
         a.rpa.slot_base = rpa_slot_base;
         a.rpa.seg_ptr = rpa_seg_ptr;
+        a.rpa.image = rpa_image;
+        a.rpa.image_bytes = rpa_image_bytes;
         a.rpa.lanes = rpa_lanes;
         a.rpa.n_seg = rpa_n_seg;
         a.rpa.len = rpa_len;
@@ -99,7 +103,7 @@ struct spn_su2 {
         void *ptrs[] = {freq,      ss,        dd,        dss,       ddd,          v2,          dv2,
                         node_wp,   node_c,    corr_out,  node_cnt,  work_counter, status,      sites,
                         inv_sites, ov_ptr,    ov_r1,     ov_r2,     range_rid,    range_inv,   corr_rid,
-                        corr_partial, rpa_sched, rpa_count, rpa_slot_base, rpa_seg_ptr, v2d, dv2d};
+                        corr_partial, rpa_image, v2d, dv2d};
         for (void *p : ptrs)
             if (p) cudaFree(p);
         if (own_stream && stream) cudaStreamDestroy(stream);

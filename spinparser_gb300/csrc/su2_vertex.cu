@@ -412,6 +412,42 @@ __device__ __forceinline__ void channel_sum(const FlowArgs &a, const float *pos,
     }
 }
 
+// ------------------------------------------------------------------------------------
+// Bulk copies global -> shared through the copy engine (cp.async.bulk) completing on an
+// mbarrier.  Addresses and sizes are multiples of 16 bytes.
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return unsigned(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Waits for phase `parity` of the barrier to complete, at most kStageSpin polls; false on timeout.
+constexpr int kStageSpin = 1 << 20;
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
+    for (int i = 0; i < kStageSpin; ++i) {
+        unsigned done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.b32 %0, 1, 0, p;\n}"
+                     : "=r"(done)
+                     : "r"(smem_u32(bar)), "r"(parity)
+                     : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
 // Shared memory of the single-flow kernel: frequency mesh; the RPA schedule when it is staged;
 // then per warp: 32 node descriptors and, per node group, NPI t-channel exchange areas (four
 // arrays of W*SPT sites and n_seg slots each).
@@ -526,23 +562,36 @@ __device__ __forceinline__ void vertex_triple(const FlowArgs &a, const float *po
 template <int SPT, int NPI>
 __global__ void __launch_bounds__(kThreads) su2_vertex_flow_kernel(FlowArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float *pos = reinterpret_cast<float *>(smem_raw);
-    for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
-
+    __shared__ __align__(8) unsigned long long stage_bar;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int W = (SPT == 1) ? a.wsite : 32;
     const int n_seg = a.rpa.n_seg;
     unsigned char *sbase = smem_raw + kMaxFreq * sizeof(float);
+
+    // Stage the frequency mesh and (if selected) the RPA schedule image in shared memory with
+    // the bulk-copy engine: one thread arms an mbarrier with the byte count and issues the
+    // copies; every thread waits on the barrier (bounded; on timeout the kernel records
+    // kStatusStageTimeout and reads the global copies instead).
+    const unsigned pos_bytes = (unsigned(a.n) * sizeof(float) + 15u) & ~15u;
+    const unsigned img_bytes = a.rpa.in_smem ? unsigned(a.rpa.image_bytes) : 0u;
+    if (threadIdx.x == 0) {
+        mbar_init(&stage_bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_arrive_expect_tx(&stage_bar, pos_bytes + img_bytes);
+        bulk_copy_g2s(smem_raw, a.freq, pos_bytes, &stage_bar);
+        if (img_bytes) bulk_copy_g2s(sbase, a.rpa.image, img_bytes, &stage_bar);
+    }
+    const bool staged = mbar_wait(&stage_bar, 0);
+    if (!staged) atomicOr(a.status, kStatusStageTimeout);
+
+    const float *pos = staged ? reinterpret_cast<const float *>(smem_raw) : a.freq;
     const int *sched, *count, *slot_base, *seg_ptr;
-    if (a.rpa.in_smem) {
-        int *s = reinterpret_cast<int *>(sbase);
+    if (a.rpa.in_smem && staged) {
+        const int *s = reinterpret_cast<const int *>(sbase);
         const int ns = a.rpa.len * a.rpa.lanes, nc = a.rpa.lanes;
-        for (int i = threadIdx.x; i < ns; i += blockDim.x) s[i] = __ldg(a.rpa.sched + i);
-        for (int i = threadIdx.x; i < nc; i += blockDim.x) {
-            s[ns + i] = __ldg(a.rpa.count + i);
-            s[ns + nc + i] = __ldg(a.rpa.slot_base + i);
-        }
-        for (int i = threadIdx.x; i <= a.nl; i += blockDim.x) s[ns + 2 * nc + i] = __ldg(a.rpa.seg_ptr + i);
         sched = s;
         count = s + ns;
         slot_base = s + ns + nc;
@@ -566,6 +615,8 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_flow_kernel(FlowArgs a) {
         if (it >= a.fn) break;
         vertex_triple<SPT, NPI>(a, pos, it, c, lane);
     }
+    // a copy that timed out must still land before the block's shared memory is released
+    if (!staged && threadIdx.x == 0) mbar_wait(&stage_bar, 0);
 }
 
 // Batched vertex flow: a persistent grid over the ragged list of (flow, triple) items of all
