@@ -153,6 +153,13 @@ typedef struct {
 /* Self-energy and its flow are kept in FP64 on the device (plain mode keeps FP32, the
  * reference's type). */
 #define SPN_SU2_FP64_SELF_ENERGY 0x1
+/* The whole flow in FP64 on the device: state, flow, loop-frequency nodes, every integrand
+ * and the measurement (the precision reference for FP32 flows of the same task; the cutoff
+ * list and the frequency mesh keep the task's float values).  The float entry points convert
+ * on the host; the _f64 entry points below move the double arrays themselves.  Such a flow is
+ * evaluated by a plain FP64 kernel (one warp per frequency triple): correct, not fast.  Not
+ * accepted by spn_batch_add. */
+#define SPN_SU2_FP64 0x2
 
 /* Creates a flow (allocates its device memory).  State starts at zero, cutoff 0.
  * Replaces SU2FrgCore's constructor (src/SU2/SU2FrgCore.cpp:17-81). */
@@ -210,6 +217,13 @@ int spn_su2_measure_correlation(spn_su2 *h, float *zz, float *dd, float *chi_zz,
  * copy-out of the last launched measurement (synchronises). */
 int spn_su2_launch_correlation(spn_su2 *h);
 int spn_su2_get_correlation(spn_su2 *h, float *zz, float *dd, float *chi_zz, float *chi_dd);
+
+/* Double-precision state, flow and measurement of a flow created with SPN_SU2_FP64
+ * (SPN_E_UNSUPPORTED for other flows); same layouts and meaning as the float calls above. */
+int spn_su2_set_state_f64(spn_su2 *h, float cutoff, const double *v2, const double *v4ss, const double *v4dd);
+int spn_su2_get_state_f64(spn_su2 *h, float *cutoff, double *v2, double *v4ss, double *v4dd);
+int spn_su2_get_flow_f64(spn_su2 *h, double *dv2, double *dv4ss, double *dv4dd);
+int spn_su2_measure_correlation_f64(spn_su2 *h, double *zz, double *dd, double *chi_zz, double *chi_dd);
 
 /* Correlation measurement that allocates no device memory.  No counterpart in the reference:
  * it exists for callers that cannot allocate device memory when they measure, such as a host

@@ -6,10 +6,10 @@ spinparser_gb300._build``).
 """
 from ._capi import SpnError, load_library
 from .batch import Su2Batch
-from .core import (FP64_SELF_ENERGY, RES_DIR, Lattice, LatticeTables, Su2Flow, cutoff_exponential, device_count,
+from .core import (FP64, FP64_SELF_ENERGY, RES_DIR, Lattice, LatticeTables, Su2Flow, cutoff_exponential, device_count,
                    frequency_exponential, measure_fp32_peak)
 
 __all__ = [
     "SpnError", "load_library", "Lattice", "LatticeTables", "Su2Flow", "frequency_exponential", "cutoff_exponential",
-    "device_count", "measure_fp32_peak", "RES_DIR", "FP64_SELF_ENERGY", "Su2Batch",
+    "device_count", "measure_fp32_peak", "RES_DIR", "FP64", "FP64_SELF_ENERGY", "Su2Batch",
 ]

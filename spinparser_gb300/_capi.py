@@ -108,6 +108,10 @@ SIGNATURES = {
     "spn_su2_finalize_step": (C.c_int, [C.c_void_p, C.c_float]),
     "spn_su2_measure_correlation": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p, c_float_p]),
     "spn_su2_launch_correlation": (C.c_int, [C.c_void_p]),
+    "spn_su2_set_state_f64": (C.c_int, [C.c_void_p, C.c_float, c_double_p, c_double_p, c_double_p]),
+    "spn_su2_get_state_f64": (C.c_int, [C.c_void_p, c_float_p, c_double_p, c_double_p, c_double_p]),
+    "spn_su2_get_flow_f64": (C.c_int, [C.c_void_p, c_double_p, c_double_p, c_double_p]),
+    "spn_su2_measure_correlation_f64": (C.c_int, [C.c_void_p, c_double_p, c_double_p, c_double_p, c_double_p]),
     "spn_su2_get_correlation": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p, c_float_p]),
     "spn_su2_correlation_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                               C.c_void_p, C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p,

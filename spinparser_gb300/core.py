@@ -19,6 +19,7 @@ from ._capi import LatticeInfo, Su2Desc, check, load_library
 RES_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "res")
 
 FP64_SELF_ENERGY = 0x1
+FP64 = 0x2  # the whole flow in double precision (precision reference; plain FP64 kernel)
 
 
 def _ptr(a: np.ndarray | None, ctype):
@@ -208,6 +209,7 @@ class Su2Flow:
         check(lib.spn_su2_create(C.byref(d), C.byref(h)))
         self._h = h
         self.n_corr = d.n_corr
+        self.fp64 = bool(flags & FP64)
 
     def close(self) -> None:
         if getattr(self, "_h", None):
@@ -289,6 +291,42 @@ class Su2Flow:
         dd = np.empty(self.n_corr, np.float32) if dd is None else dd
         check(self._lib.spn_su2_get_correlation(self._h, _ptr(zz, C.c_float), _ptr(dd, C.c_float), None, None))
         return zz, dd
+
+    # ---- double-precision data of an FP64 flow (flags=FP64) ----
+    def set_state_f64(self, cutoff: float, v2: np.ndarray, v4ss: np.ndarray, v4dd: np.ndarray) -> None:
+        v2 = np.ascontiguousarray(v2, np.float64)
+        v4ss = np.ascontiguousarray(v4ss, np.float64).reshape(-1)
+        v4dd = np.ascontiguousarray(v4dd, np.float64).reshape(-1)
+        if v2.size != self.n or v4ss.size != self.fn * self.nl or v4dd.size != self.fn * self.nl:
+            raise ValueError("state arrays have the wrong size")
+        check(self._lib.spn_su2_set_state_f64(self._h, cutoff, _ptr(v2, C.c_double), _ptr(v4ss, C.c_double),
+                                              _ptr(v4dd, C.c_double)))
+
+    def get_state_f64(self):
+        v2 = np.empty(self.n, np.float64)
+        ss = np.empty(self.fn * self.nl, np.float64)
+        dd = np.empty(self.fn * self.nl, np.float64)
+        c = C.c_float()
+        check(self._lib.spn_su2_get_state_f64(self._h, C.byref(c), _ptr(v2, C.c_double), _ptr(ss, C.c_double),
+                                              _ptr(dd, C.c_double)))
+        return c.value, v2, ss, dd
+
+    def get_flow_f64(self):
+        v2 = np.empty(self.n, np.float64)
+        ss = np.empty(self.fn * self.nl, np.float64)
+        dd = np.empty(self.fn * self.nl, np.float64)
+        check(self._lib.spn_su2_get_flow_f64(self._h, _ptr(v2, C.c_double), _ptr(ss, C.c_double),
+                                             _ptr(dd, C.c_double)))
+        return v2, ss, dd
+
+    def measure_correlation_f64(self):
+        zz = np.empty(self.n_corr, np.float64)
+        dd = np.empty(self.n_corr, np.float64)
+        cz = np.empty(self.nl, np.float64)
+        cd = np.empty(self.nl, np.float64)
+        check(self._lib.spn_su2_measure_correlation_f64(self._h, _ptr(zz, C.c_double), _ptr(dd, C.c_double),
+                                                        _ptr(cz, C.c_double), _ptr(cd, C.c_double)))
+        return zz, dd, cz, cd
 
     def is_diverged(self) -> bool:
         v = C.c_int(0)

@@ -448,6 +448,7 @@ extern "C" int spn_batch_add(spn_batch *b, const spn_su2_desc *desc, int n_cutof
         if (!b || !desc || !cutoffs || n_cutoffs < 1 || !v2 || !v4ss || !v4dd || !flow_id)
             throw Error(ErrorType::Argument, "spn_batch_add: bad argument");
         if (desc->device != b->device) throw Error(ErrorType::Argument, "spn_batch_add: flow device differs from the batch's");
+        if (desc->flags & SPN_SU2_FP64) throw Error(ErrorType::Unsupported, "spn_batch_add: FP64 flows run alone (spn_su2_create)");
         for (int k = 1; k < n_cutoffs; ++k)
             if (!(cutoffs[k] < cutoffs[k - 1])) throw Error(ErrorType::Argument, "spn_batch_add: cutoffs must descend");
         cuda_check(cudaSetDevice(b->device), "cudaSetDevice");

@@ -34,37 +34,43 @@ __host__ __device__ inline int rpa_smem_ints(const RpaSchedule &r, int nl) {
     return r.len * r.lanes + 2 * r.lanes + nl + 1;
 }
 
-struct FlowArgs {
+// Argument block of one flow in working precision T (float: the reference's types; double:
+// the FP64 flow, SPN_SU2_FP64).  The cutoff list is float in both (the task file's values).
+template <class T>
+struct FlowArgsT {
     int n, nl, fn, wsite, max_nodes, n_range;
     float cutoff, spin;
-    const float *freq;
-    const float *ss, *dd;  // state
-    float *dss, *ddd;      // flow
-    const float *v2;       // self-energy state
-    float *dv2;            // self-energy flow
+    const T *freq;
+    const T *ss, *dd;      // state
+    T *dss, *ddd;          // flow
+    const T *v2;           // self-energy state
+    T *dv2;                // self-energy flow
     const double *v2d;     // FP64 self-energy state (used when fp64_sigma)
     double *dv2d;          // FP64 self-energy flow
     int fp64_sigma;
     const int *sites, *inv_sites, *ov_ptr, *ov_r1, *ov_r2, *range_rid, *range_inv;
-    float *node_wp, *node_c;
+    T *node_wp, *node_c;
     int *node_cnt;
     int *work_counter;
     unsigned *status;
     RpaSchedule rpa;
 };
+using FlowArgs = FlowArgsT<float>;
 
 // Correlation measurement (nu = 0) of one flow: the state it reads, the per-node partial
 // sums and the output zz[n_corr], dd[n_corr], chi_s[nl], chi_d[nl].
-struct CorrArgs {
+template <class T>
+struct CorrArgsT {
     int n, nl, n_corr;
     float cutoff, spin;
-    const float *freq, *ss, *dd, *v2;
+    const T *freq, *ss, *dd, *v2;
     const double *v2d;  // FP64 self-energy, read instead of v2 when not NULL
     const int *sites, *inv_sites, *corr_rid;
     double *partial;  // [max_nodes][2][nl]
-    float *out;
+    T *out;
     int wsite;
 };
+using CorrArgs = CorrArgsT<float>;
 
 // ------------------------------------------------------------------------------------
 // Batches: many flows advanced together (include/spn_su2.h, spn_batch_*).  Each flow has a
@@ -97,6 +103,9 @@ struct BatchFlow {
 size_t vertex_flow_smem_bytes(int nl, const RpaSchedule &rpa, int npi);
 int vertex_flow_blocks_per_sm(int nl, const RpaSchedule &rpa, int npi);
 void launch_vertex_flow(const FlowArgs &a, int npi, int grid, cudaStream_t stream);
+// FP64 flow (su2_vertex64.cu): one warp per triple over a persistent grid.
+void launch_vertex_flow_f64(const FlowArgsT<double> &a, int grid, cudaStream_t stream);
+int vertex_flow_f64_blocks_per_sm(int nl);
 
 // Largest schedule staged in shared memory; larger ones are read from global memory.
 constexpr int kRpaSmemMaxInts = 8192;

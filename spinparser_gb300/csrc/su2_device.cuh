@@ -14,8 +14,20 @@ namespace dev {
 
 constexpr int kMaxFreq = 256;  // largest supported N (positive frequencies)
 
+// Single IEEE operations rounded to nearest in the working precision T (float: the
+// reference's types; double: the FP64 flow).
+__device__ __forceinline__ float rn_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double rn_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float rn_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double rn_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float rn_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double rn_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float rn_div(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double rn_div(double a, double b) { return __ddiv_rn(a, b); }
+
 // First index i in [1, n) with pos[i] > w; n if none (also for NaN w).
-__device__ __forceinline__ int first_greater(const float *pos, int n, float w) {
+template <class T>
+__device__ __forceinline__ int first_greater(const T *pos, int n, T w) {
     int lo = 1, hi = n;
     while (lo < hi) {
         int mid = (lo + hi) >> 1;
@@ -26,7 +38,8 @@ __device__ __forceinline__ int first_greater(const float *pos, int n, float w) {
 }
 
 // First index i in [1, n) with pos[i] >= w; n if none.
-__device__ __forceinline__ int first_geq(const float *pos, int n, float w) {
+template <class T>
+__device__ __forceinline__ int first_geq(const T *pos, int n, T w) {
     int lo = 1, hi = n;
     while (lo < hi) {
         int mid = (lo + hi) >> 1;
@@ -37,85 +50,97 @@ __device__ __forceinline__ int first_geq(const float *pos, int n, float w) {
 }
 
 // FrequencyDiscretization::offset (w >= 0): index of the mesh point equal to w.
-__device__ __forceinline__ int mesh_offset(const float *pos, int n, float w) {
+template <class T>
+__device__ __forceinline__ int mesh_offset(const T *pos, int n, T w) {
     if (w <= pos[0]) return 0;
     int i = first_geq(pos, n, w);
     return i < n ? i : n - 1;
 }
 
 // FrequencyDiscretization::interpolateOffset (w >= 0).
-__device__ __forceinline__ void mesh_interp(const float *pos, int n, float w, int &lo, int &hi, float &bias) {
+template <class T>
+__device__ __forceinline__ void mesh_interp(const T *pos, int n, T w, int &lo, int &hi, T &bias) {
     if (w <= pos[0]) {
         lo = hi = 0;
-        bias = 0.0f;
+        bias = T(0);
         return;
     }
     int i = first_greater(pos, n, w);
     if (i < n) {
         hi = i;
         lo = i - 1;
-        bias = __fdiv_rn(__fsub_rn(w, pos[lo]), __fsub_rn(pos[hi], pos[lo]));
+        bias = rn_div(rn_sub(w, pos[lo]), rn_sub(pos[hi], pos[lo]));
     } else {
         lo = hi = n - 1;
-        bias = 0.0f;
+        bias = T(0);
     }
 }
 
 // Index into the symmetric mesh -w[n-1] .. -w[0], w[0] .. w[n-1] (0 .. 2n-1).
-__device__ __forceinline__ float full_value(const float *pos, int n, int k) { return k < n ? -pos[n - 1 - k] : pos[k - n]; }
+template <class T>
+__device__ __forceinline__ T full_value(const T *pos, int n, int k) { return k < n ? -pos[n - 1 - k] : pos[k - n]; }
 
-__device__ __forceinline__ int pos_lesser(const float *pos, int n, float w) {  // w >= 0, returns positive index
+template <class T>
+__device__ __forceinline__ int pos_lesser(const T *pos, int n, T w) {  // w >= 0, returns positive index
     if (w <= pos[0]) return 0;
     int i = first_greater(pos, n, w);
     return i < n ? i - 1 : n - 1;
 }
-__device__ __forceinline__ int pos_greater(const float *pos, int n, float w) {  // w >= 0
+template <class T>
+__device__ __forceinline__ int pos_greater(const T *pos, int n, T w) {  // w >= 0
     if (w <= pos[0]) return 0;
     int i = first_greater(pos, n, w);
     return i < n ? i : n - 1;
 }
 // FrequencyDiscretization::lesser / greater on the full mesh (full index).
-__device__ __forceinline__ int full_lesser(const float *pos, int n, float w) {
+template <class T>
+__device__ __forceinline__ int full_lesser(const T *pos, int n, T w) {
     if (w < 0) return n - 1 - pos_greater(pos, n, -w);
     return n + pos_lesser(pos, n, w);
 }
-__device__ __forceinline__ int full_greater(const float *pos, int n, float w) {
+template <class T>
+__device__ __forceinline__ int full_greater(const T *pos, int n, T w) {
     if (w < 0) return n - 1 - pos_lesser(pos, n, -w);
     return n + pos_greater(pos, n, w);
 }
 
 // Linear interpolation of a function stored on the positive mesh and odd in w
 // (SU2VertexSingleParticle::getValue, src/SU2/SU2VertexSingleParticle.hpp:73-87).
-template <class T>
-__device__ __forceinline__ double odd_interp(const float *pos, int n, const T *data, float w) {
+template <class P, class T>
+__device__ __forceinline__ double odd_interp(const P *pos, int n, const T *data, P w) {
     double sign = 1.0;
     if (w < 0) {
         w = -w;
         sign = -1.0;
     }
     int lo, hi;
-    float b;
+    P b;
     mesh_interp(pos, n, w, lo, hi, b);
     return sign * ((1.0 - double(b)) * double(data[lo]) + double(b) * double(data[hi]));
 }
 
 // Access buffer with four interpolation supports (SU2VertexTwoParticleAccessBuffer<4>).
-struct AB4 {
+template <class T>
+struct AB4T {
     int off[4];    // element offset of the (s,t,u) slab start; add the site index
-    float w[4];    // interpolation weight
-    float sw[4];   // sign * weight (density channel)
+    T w[4];        // interpolation weight
+    T sw[4];       // sign * weight (density channel)
     bool exch;     // read the site-exchanged pair
 };
 
-struct AB8 {
+template <class T>
+struct AB8T {
     int off[8];
-    float w[8];
-    float sw[8];
+    T w[8];
+    T sw[8];
     bool exch;
 };
+using AB4 = AB4T<float>;
+using AB8 = AB8T<float>;
 
 // _generateAccessBufferOffset: storage keeps s >= u; a swapped pair flips the density sign.
-__device__ __forceinline__ void slab(int si, int ti, int ui, int stepT, int nl, int &off, float w, float &wout, float &swout) {
+template <class T>
+__device__ __forceinline__ void slab(int si, int ti, int ui, int stepT, int nl, int &off, T w, T &wout, T &swout) {
     if (si < ui) {
         off = (ui * (ui + 1) / 2 + si) * stepT + ti * nl;
         wout = w;
@@ -128,7 +153,8 @@ __device__ __forceinline__ void slab(int si, int ti, int ui, int stepT, int nl, 
 }
 
 // Frequency folding into the stored sector (SU2VertexTwoParticle.hpp:405-427).
-__device__ __forceinline__ bool fold(float &s, float &t, float &u) {
+template <class T>
+__device__ __forceinline__ bool fold(T &s, T &t, T &u) {
     bool exch = false;
     if (s < 0 && u < 0) {
         s = -s;
@@ -150,12 +176,12 @@ enum Channel { kS = 0, kT = 1, kU = 2 };
 
 // generateAccessBuffer(s, t, u, channel) for channel in {S, T, U}
 // (src/SU2/SU2VertexTwoParticle.hpp:399-490).
-template <int CH>
-__device__ __forceinline__ void access4(const float *pos, int n, int nl, float s, float t, float u, AB4 &ab) {
+template <int CH, class T>
+__device__ __forceinline__ void access4(const T *pos, int n, int nl, T s, T t, T u, AB4T<T> &ab) {
     ab.exch = fold(s, t, u);
     const int stepT = n * nl;
     int e, la, ua, lb, ub;
-    float ba, bb;
+    T ba, bb;
     if (CH == kS) {
         e = mesh_offset(pos, n, s);
         mesh_interp(pos, n, t, la, ua, ba);
@@ -169,8 +195,8 @@ __device__ __forceinline__ void access4(const float *pos, int n, int nl, float s
         mesh_interp(pos, n, s, la, ua, ba);
         mesh_interp(pos, n, t, lb, ub, bb);
     }
-    const float na = __fsub_rn(1.0f, ba), nb = __fsub_rn(1.0f, bb);
-    const float w0 = __fmul_rn(nb, na), w1 = __fmul_rn(nb, ba), w2 = __fmul_rn(bb, na), w3 = __fmul_rn(bb, ba);
+    const T na = rn_sub(T(1), ba), nb = rn_sub(T(1), bb);
+    const T w0 = rn_mul(nb, na), w1 = rn_mul(nb, ba), w2 = rn_mul(bb, na), w3 = rn_mul(bb, ba);
     if (CH == kS) {
         slab(e, la, lb, stepT, nl, ab.off[0], w0, ab.w[0], ab.sw[0]);
         slab(e, ua, lb, stepT, nl, ab.off[1], w1, ab.w[1], ab.sw[1]);
@@ -190,42 +216,45 @@ __device__ __forceinline__ void access4(const float *pos, int n, int nl, float s
 }
 
 // generateAccessBuffer(s, t, u): trilinear, eight supports (SU2VertexTwoParticle.hpp:500-557).
-__device__ __forceinline__ void access8(const float *pos, int n, int nl, float s, float t, float u, AB8 &ab) {
+template <class T>
+__device__ __forceinline__ void access8(const T *pos, int n, int nl, T s, T t, T u, AB8T<T> &ab) {
     ab.exch = fold(s, t, u);
     const int stepT = n * nl;
     int ls, us, lt, ut, lu, uu;
-    float bs, bt, bu;
+    T bs, bt, bu;
     mesh_interp(pos, n, s, ls, us, bs);
     mesh_interp(pos, n, t, lt, ut, bt);
     mesh_interp(pos, n, u, lu, uu, bu);
-    const float ns = __fsub_rn(1.0f, bs), nt = __fsub_rn(1.0f, bt), nu = __fsub_rn(1.0f, bu);
-    slab(ls, lt, lu, stepT, nl, ab.off[0], __fmul_rn(__fmul_rn(nt, ns), nu), ab.w[0], ab.sw[0]);
-    slab(us, lt, lu, stepT, nl, ab.off[1], __fmul_rn(__fmul_rn(nt, bs), nu), ab.w[1], ab.sw[1]);
-    slab(ls, ut, lu, stepT, nl, ab.off[2], __fmul_rn(__fmul_rn(bt, ns), nu), ab.w[2], ab.sw[2]);
-    slab(us, ut, lu, stepT, nl, ab.off[3], __fmul_rn(__fmul_rn(bt, bs), nu), ab.w[3], ab.sw[3]);
-    slab(ls, lt, uu, stepT, nl, ab.off[4], __fmul_rn(__fmul_rn(nt, ns), bu), ab.w[4], ab.sw[4]);
-    slab(us, lt, uu, stepT, nl, ab.off[5], __fmul_rn(__fmul_rn(nt, bs), bu), ab.w[5], ab.sw[5]);
-    slab(ls, ut, uu, stepT, nl, ab.off[6], __fmul_rn(__fmul_rn(bt, ns), bu), ab.w[6], ab.sw[6]);
-    slab(us, ut, uu, stepT, nl, ab.off[7], __fmul_rn(__fmul_rn(bt, bs), bu), ab.w[7], ab.sw[7]);
+    const T ns = rn_sub(T(1), bs), nt = rn_sub(T(1), bt), nu = rn_sub(T(1), bu);
+    slab(ls, lt, lu, stepT, nl, ab.off[0], rn_mul(rn_mul(nt, ns), nu), ab.w[0], ab.sw[0]);
+    slab(us, lt, lu, stepT, nl, ab.off[1], rn_mul(rn_mul(nt, bs), nu), ab.w[1], ab.sw[1]);
+    slab(ls, ut, lu, stepT, nl, ab.off[2], rn_mul(rn_mul(bt, ns), nu), ab.w[2], ab.sw[2]);
+    slab(us, ut, lu, stepT, nl, ab.off[3], rn_mul(rn_mul(bt, bs), nu), ab.w[3], ab.sw[3]);
+    slab(ls, lt, uu, stepT, nl, ab.off[4], rn_mul(rn_mul(nt, ns), bu), ab.w[4], ab.sw[4]);
+    slab(us, lt, uu, stepT, nl, ab.off[5], rn_mul(rn_mul(nt, bs), bu), ab.w[5], ab.sw[5]);
+    slab(ls, ut, uu, stepT, nl, ab.off[6], rn_mul(rn_mul(bt, ns), bu), ab.w[6], ab.sw[6]);
+    slab(us, ut, uu, stepT, nl, ab.off[7], rn_mul(rn_mul(bt, bs), bu), ab.w[7], ab.sw[7]);
 }
 
 // SU2VertexTwoParticle::_directAccessMapFrequencyExchange for one site.
-__device__ __forceinline__ float direct(const float *__restrict__ v, int si, int ti, int ui, int site, int stepT, int nl,
-                                        bool density) {
+template <class T>
+__device__ __forceinline__ T direct(const T *__restrict__ v, int si, int ti, int ui, int site, int stepT, int nl,
+                                    bool density) {
     if (si >= ui) return v[(si * (si + 1) / 2 + ui) * stepT + ti * nl + site];
-    float x = v[(ui * (ui + 1) / 2 + si) * stepT + ti * nl + site];
+    T x = v[(ui * (ui + 1) / 2 + si) * stepT + ti * nl + site];
     return density ? -x : x;
 }
 
 // getValue(i1, i2, s, t, u, symmetry, FrequencyChannel::None) where the site pair enters
 // through its rid (rid12) and the rid of the exchanged pair (rid21).
-__device__ __forceinline__ float value_none(const float *pos, int n, int nl, const float *__restrict__ v, bool density,
-                                            int rid12, int rid21, float s, float t, float u) {
+template <class T>
+__device__ __forceinline__ T value_none(const T *pos, int n, int nl, const T *__restrict__ v, bool density, int rid12,
+                                        int rid21, T s, T t, T u) {
     bool exch = fold(s, t, u);
     const int site = exch ? rid21 : rid12;
     const int stepT = n * nl;
     int ls, us, lt, ut, lu, uu;
-    float bs, bt, bu;
+    T bs, bt, bu;
     mesh_interp(pos, n, s, ls, us, bs);
     mesh_interp(pos, n, t, lt, ut, bt);
     mesh_interp(pos, n, u, lu, uu, bu);
@@ -239,59 +268,59 @@ __device__ __forceinline__ float value_none(const float *pos, int n, int nl, con
 // same order, with weight = 0.5 * (the float node spacing the reference multiplies by).
 
 // integrateWithObscureLeftBoundary(min, last)
-template <class Emit>
-__device__ void nodes_left(const float *pos, int n, float min, Emit &&emit) {
+template <class T, class Emit>
+__device__ void nodes_left(const T *pos, int n, T min, Emit &&emit) {
     const int maxi = 2 * n - 1;
     int um = full_greater(pos, n, min);
     if (um != maxi) {
-        emit(min, 0.5 * double(__fsub_rn(full_value(pos, n, um), min)));
-        emit(full_value(pos, n, um), 0.5 * double(__fsub_rn(full_value(pos, n, um + 1), min)));
+        emit(min, 0.5 * double(rn_sub(full_value(pos, n, um), min)));
+        emit(full_value(pos, n, um), 0.5 * double(rn_sub(full_value(pos, n, um + 1), min)));
         while (++um != maxi)
-            emit(full_value(pos, n, um), 0.5 * double(__fsub_rn(full_value(pos, n, um + 1), full_value(pos, n, um - 1))));
-        emit(full_value(pos, n, um), 0.5 * double(__fsub_rn(full_value(pos, n, um), full_value(pos, n, um - 1))));
+            emit(full_value(pos, n, um), 0.5 * double(rn_sub(full_value(pos, n, um + 1), full_value(pos, n, um - 1))));
+        emit(full_value(pos, n, um), 0.5 * double(rn_sub(full_value(pos, n, um), full_value(pos, n, um - 1))));
     } else {
-        const double w = double(__fmul_rn(0.5f, __fsub_rn(full_value(pos, n, um), min)));
+        const double w = double(rn_mul(T(0.5), rn_sub(full_value(pos, n, um), min)));
         emit(min, w);
         emit(full_value(pos, n, um), w);
     }
 }
 
 // integrateWithObscureRightBoundary(beginNegative, max)
-template <class Emit>
-__device__ void nodes_right(const float *pos, int n, float max, Emit &&emit) {
+template <class T, class Emit>
+__device__ void nodes_right(const T *pos, int n, T max, Emit &&emit) {
     int um = 0;
     const int ux = full_lesser(pos, n, max);
     if (um != ux) {
-        emit(full_value(pos, n, um), 0.5 * double(__fsub_rn(full_value(pos, n, um + 1), full_value(pos, n, um))));
+        emit(full_value(pos, n, um), 0.5 * double(rn_sub(full_value(pos, n, um + 1), full_value(pos, n, um))));
         while (++um != ux)
-            emit(full_value(pos, n, um), 0.5 * double(__fsub_rn(full_value(pos, n, um + 1), full_value(pos, n, um - 1))));
-        emit(full_value(pos, n, um), 0.5 * double(__fsub_rn(max, full_value(pos, n, um - 1))));
-        emit(max, 0.5 * double(__fsub_rn(max, full_value(pos, n, um))));
+            emit(full_value(pos, n, um), 0.5 * double(rn_sub(full_value(pos, n, um + 1), full_value(pos, n, um - 1))));
+        emit(full_value(pos, n, um), 0.5 * double(rn_sub(max, full_value(pos, n, um - 1))));
+        emit(max, 0.5 * double(rn_sub(max, full_value(pos, n, um))));
     } else {
-        const double w = double(__fmul_rn(0.5f, __fsub_rn(max, full_value(pos, n, um))));
+        const double w = double(rn_mul(T(0.5), rn_sub(max, full_value(pos, n, um))));
         emit(max, w);
         emit(full_value(pos, n, um), w);
     }
 }
 
 // integrateWithObscureBoundaries(min, max)
-template <class Emit>
-__device__ void nodes_both(const float *pos, int n, float min, float max, Emit &&emit) {
+template <class T, class Emit>
+__device__ void nodes_both(const T *pos, int n, T min, T max, Emit &&emit) {
     int um = full_greater(pos, n, min);
     const int ux = full_lesser(pos, n, max);
     if (ux >= um) {
-        emit(min, 0.5 * double(__fsub_rn(full_value(pos, n, um), min)));
+        emit(min, 0.5 * double(rn_sub(full_value(pos, n, um), min)));
         if (ux != um) {
-            emit(full_value(pos, n, um), 0.5 * double(__fsub_rn(full_value(pos, n, um + 1), min)));
+            emit(full_value(pos, n, um), 0.5 * double(rn_sub(full_value(pos, n, um + 1), min)));
             while (++um != ux)
-                emit(full_value(pos, n, um), 0.5 * double(__fsub_rn(full_value(pos, n, um + 1), full_value(pos, n, um - 1))));
-            emit(full_value(pos, n, um), 0.5 * double(__fsub_rn(max, full_value(pos, n, um - 1))));
+                emit(full_value(pos, n, um), 0.5 * double(rn_sub(full_value(pos, n, um + 1), full_value(pos, n, um - 1))));
+            emit(full_value(pos, n, um), 0.5 * double(rn_sub(max, full_value(pos, n, um - 1))));
         } else {
-            emit(full_value(pos, n, um), 0.5 * double(__fsub_rn(max, min)));
+            emit(full_value(pos, n, um), 0.5 * double(rn_sub(max, min)));
         }
-        emit(max, 0.5 * double(__fsub_rn(max, full_value(pos, n, um))));
+        emit(max, 0.5 * double(rn_sub(max, full_value(pos, n, um))));
     } else {
-        const double w = double(__fmul_rn(0.5f, __fsub_rn(max, min)));
+        const double w = double(rn_mul(T(0.5), rn_sub(max, min)));
         emit(max, w);
         emit(min, w);
     }

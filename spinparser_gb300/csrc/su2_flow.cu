@@ -50,6 +50,16 @@ __global__ void __launch_bounds__(128) su2_corr_inner_kernel(CorrArgs a) { corr_
 
 __global__ void su2_corr_final_kernel(CorrArgs a) { corr_final_body(a); }
 
+// FP64 flow (SPN_SU2_FP64): the same bodies in double
+__global__ void __launch_bounds__(128) su2_self_energy_f64_kernel(FlowArgsT<double> a) { self_energy_body(a, blockIdx.x); }
+
+__global__ void su2_node_table_f64_kernel(FlowArgsT<double> a) { node_table_body(a, blockIdx.x); }
+
+template <int SPT>
+__global__ void __launch_bounds__(128) su2_corr_inner_f64_kernel(CorrArgsT<double> a) { corr_inner_body<SPT>(a, blockIdx.x); }
+
+__global__ void su2_corr_final_f64_kernel(CorrArgsT<double> a) { corr_final_body(a); }
+
 // ------------------------------------------------------------------------------------
 // Euler step  x += step * dx  (rounded like the reference: product, then sum)
 // ------------------------------------------------------------------------------------
@@ -77,6 +87,13 @@ __global__ void su2_euler_f64_kernel(double *__restrict__ x, const double *__res
         x[i] = v;
         xf[i] = float(v);
     }
+}
+
+// Euler step of an FP64 flow: x += step * dx in double, step = new - old cutoff in double
+// (the float cutoffs widened first).
+__global__ void su2_euler_flow_f64_kernel(double *__restrict__ x, const double *__restrict__ dx, long long n, double step) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        x[i] = euler_update_f64(x[i], dx[i], step);
 }
 
 // ------------------------------------------------------------------------------------
@@ -138,14 +155,45 @@ void upload(T *dst, const T *src, size_t count, cudaStream_t s) {
 }
 
 void launch_vertex(spn_su2 *h) {
-    launch_vertex_flow(h->args(), h->vertex_npi, h->vertex_grid, h->stream);
+    if (h->fp64()) launch_vertex_flow_f64(h->args64(), h->vertex_grid, h->stream);
+    else launch_vertex_flow(h->args(), h->vertex_npi, h->vertex_grid, h->stream);
     cuda_check(cudaGetLastError(), "vertex flow launch");
+}
+
+template <class T>
+std::vector<T> download(const T *src, size_t count, cudaStream_t s) {
+    std::vector<T> v(count);
+    if (count) cuda_check(cudaMemcpyAsync(v.data(), src, count * sizeof(T), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync D2H");
+    cuda_check(cudaStreamSynchronize(s), "D2H sync");
+    return v;
+}
+
+// Copies n doubles from the device into float `out` (the float entry points of an FP64 flow).
+void download_as_float(float *out, const double *src, size_t count, cudaStream_t s) {
+    if (!out) return;
+    std::vector<double> v = download(src, count, s);
+    for (size_t i = 0; i < count; ++i) out[i] = float(v[i]);
+}
+
+void upload_as_double(double *dst, const float *src, size_t count, cudaStream_t s) {
+    std::vector<double> v(src, src + count);
+    upload(dst, v.data(), count, s);
+    cuda_check(cudaStreamSynchronize(s), "H2D sync");
 }
 
 // Selects a vertex-flow variant: nodes per iteration and where the RPA schedule lives (all
 // variants give the same bits); the persistent grid fills every SM to the variant's
 // occupancy.  Returns false if it cannot run.
 bool select_variant(spn_su2 *h, int npi, int in_smem) {
+    if (h->fp64()) {  // one FP64 kernel
+        const int per_sm = vertex_flow_f64_blocks_per_sm(h->nl);
+        cudaGetLastError();
+        if (per_sm < 1 || npi != 1 || in_smem) return false;
+        h->vertex_npi = 1;
+        h->rpa_in_smem = 0;
+        h->vertex_grid = h->sms * per_sm;
+        return true;
+    }
     if (in_smem) {
         RpaSchedule r = h->args().rpa;
         if (rpa_smem_ints(r, h->nl) > kRpaSmemMaxInts) return false;
@@ -273,17 +321,40 @@ spn_su2 *spn::create_flow(const spn_su2_desc *d, cudaStream_t stream) {
                 h->own_stream = true;
             }
             const size_t vsz = size_t(h->fn) * h->nl;
+            const bool f64 = h->fp64();
             h->freq = dev_alloc<float>(h->n, "alloc freq");
-            h->ss = dev_alloc<float>(vsz, "alloc v4ss");
-            h->dd = dev_alloc<float>(vsz, "alloc v4dd");
-            h->dss = dev_alloc<float>(vsz, "alloc dv4ss");
-            h->ddd = dev_alloc<float>(vsz, "alloc dv4dd");
             h->v2 = dev_alloc<float>(h->n, "alloc v2");
             h->dv2 = dev_alloc<float>(h->n, "alloc dv2");
             h->v2d = dev_alloc<double>(h->n, "alloc v2 (fp64)");
             h->dv2d = dev_alloc<double>(h->n, "alloc dv2 (fp64)");
-            h->node_wp = dev_alloc<float>(size_t(h->n) * h->max_nodes, "alloc node table");
-            h->node_c = dev_alloc<float>(size_t(h->n) * h->max_nodes, "alloc node table");
+            if (f64) {
+                h->freq64 = dev_alloc<double>(h->n, "alloc freq (fp64)");
+                h->ss64 = dev_alloc<double>(vsz, "alloc v4ss (fp64)");
+                h->dd64 = dev_alloc<double>(vsz, "alloc v4dd (fp64)");
+                h->dss64 = dev_alloc<double>(vsz, "alloc dv4ss (fp64)");
+                h->ddd64 = dev_alloc<double>(vsz, "alloc dv4dd (fp64)");
+                h->node_wp64 = dev_alloc<double>(size_t(h->n) * h->max_nodes, "alloc node table (fp64)");
+                h->node_c64 = dev_alloc<double>(size_t(h->n) * h->max_nodes, "alloc node table (fp64)");
+                h->corr_out64 = dev_alloc<double>(2 * size_t(h->n_corr) + 2 * h->nl, "alloc corr out (fp64)");
+                std::vector<double> f(d->freq, d->freq + h->n);
+                upload(h->freq64, f.data(), h->n, h->stream);
+                cuda_check(cudaMemsetAsync(h->ss64, 0, vsz * sizeof(double), h->stream), "memset");
+                cuda_check(cudaMemsetAsync(h->dd64, 0, vsz * sizeof(double), h->stream), "memset");
+                cuda_check(cudaMemsetAsync(h->dss64, 0, vsz * sizeof(double), h->stream), "memset");
+                cuda_check(cudaMemsetAsync(h->ddd64, 0, vsz * sizeof(double), h->stream), "memset");
+                cuda_check(cudaStreamSynchronize(h->stream), "create sync");  // f leaves scope
+            } else {
+                h->ss = dev_alloc<float>(vsz, "alloc v4ss");
+                h->dd = dev_alloc<float>(vsz, "alloc v4dd");
+                h->dss = dev_alloc<float>(vsz, "alloc dv4ss");
+                h->ddd = dev_alloc<float>(vsz, "alloc dv4dd");
+                h->node_wp = dev_alloc<float>(size_t(h->n) * h->max_nodes, "alloc node table");
+                h->node_c = dev_alloc<float>(size_t(h->n) * h->max_nodes, "alloc node table");
+                cuda_check(cudaMemsetAsync(h->ss, 0, vsz * sizeof(float), h->stream), "memset");
+                cuda_check(cudaMemsetAsync(h->dd, 0, vsz * sizeof(float), h->stream), "memset");
+                cuda_check(cudaMemsetAsync(h->dss, 0, vsz * sizeof(float), h->stream), "memset");
+                cuda_check(cudaMemsetAsync(h->ddd, 0, vsz * sizeof(float), h->stream), "memset");
+            }
             h->node_cnt = dev_alloc<int>(h->n, "alloc node counts");
             h->work_counter = dev_alloc<int>(1, "alloc work counter");
             h->status = dev_alloc<unsigned>(1, "alloc status");
@@ -296,7 +367,7 @@ spn_su2 *spn::create_flow(const spn_su2_desc *d, cudaStream_t stream) {
             h->range_inv = dev_alloc<int>(h->n_range + 1, "alloc range");
             h->corr_rid = dev_alloc<int>(h->n_corr + 1, "alloc corr map");
             h->corr_partial = dev_alloc<double>(size_t(kMaxCorrNodes) * 2 * h->nl, "alloc corr scratch");
-            h->corr_out = dev_alloc<float>(2 * size_t(h->n_corr) + 2 * h->nl, "alloc corr out");
+            if (!f64) h->corr_out = dev_alloc<float>(2 * size_t(h->n_corr) + 2 * h->nl, "alloc corr out");
             upload(h->freq, d->freq, h->n, h->stream);
             upload(h->sites, d->sites_rid, h->nl, h->stream);
             upload(h->inv_sites, d->inv_sites_rid, h->nl, h->stream);
@@ -306,10 +377,6 @@ spn_su2 *spn::create_flow(const spn_su2_desc *d, cudaStream_t stream) {
             upload(h->range_rid, d->range_rid, h->n_range, h->stream);
             upload(h->range_inv, d->range_inv_rid, h->n_range, h->stream);
             upload(h->corr_rid, d->corr_rid, h->n_corr, h->stream);
-            cuda_check(cudaMemsetAsync(h->ss, 0, vsz * sizeof(float), h->stream), "memset");
-            cuda_check(cudaMemsetAsync(h->dd, 0, vsz * sizeof(float), h->stream), "memset");
-            cuda_check(cudaMemsetAsync(h->dss, 0, vsz * sizeof(float), h->stream), "memset");
-            cuda_check(cudaMemsetAsync(h->ddd, 0, vsz * sizeof(float), h->stream), "memset");
             cuda_check(cudaMemsetAsync(h->v2, 0, h->n * sizeof(float), h->stream), "memset");
             cuda_check(cudaMemsetAsync(h->dv2, 0, h->n * sizeof(float), h->stream), "memset");
             cuda_check(cudaMemsetAsync(h->v2d, 0, h->n * sizeof(double), h->stream), "memset");
@@ -341,7 +408,7 @@ spn_su2 *spn::create_flow(const spn_su2_desc *d, cudaStream_t stream) {
             h->sms = sms;
             // default variant (schedule staged in shared memory where it fits); spn_su2_autotune
             // can pick a faster one for this flow
-            if (!select_variant(h, 1, 1) && !select_variant(h, 1, 0))
+            if (!select_variant(h, 1, f64 ? 0 : 1) && !select_variant(h, 1, 0))
                 throw Error(ErrorType::Unsupported, "vertex-flow kernel does not fit on this device");
             cuda_check(cudaStreamSynchronize(h->stream), "create sync");
         } catch (...) {
@@ -399,8 +466,13 @@ extern "C" int spn_su2_set_state(spn_su2 *h, float cutoff, const float *v2, cons
         cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
         const size_t vsz = size_t(h->fn) * h->nl;
         upload(h->v2, v2, h->n, h->stream);
-        upload(h->ss, v4ss, vsz, h->stream);
-        upload(h->dd, v4dd, vsz, h->stream);
+        if (h->fp64()) {
+            upload_as_double(h->ss64, v4ss, vsz, h->stream);
+            upload_as_double(h->dd64, v4dd, vsz, h->stream);
+        } else {
+            upload(h->ss, v4ss, vsz, h->stream);
+            upload(h->dd, v4dd, vsz, h->stream);
+        }
         std::vector<double> v2d(v2, v2 + h->n);  // the FP64 self-energy starts from the given values
         upload(h->v2d, v2d.data(), h->n, h->stream);
         h->cutoff = cutoff;
@@ -414,6 +486,12 @@ extern "C" int spn_su2_get_state(spn_su2 *h, float *cutoff, float *v2, float *v4
         cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
         const size_t vsz = size_t(h->fn) * h->nl;
         if (cutoff) *cutoff = h->cutoff;
+        if (h->fp64()) {
+            download_as_float(v2, h->v2d, h->n, h->stream);
+            download_as_float(v4ss, h->ss64, vsz, h->stream);
+            download_as_float(v4dd, h->dd64, vsz, h->stream);
+            return;
+        }
         if (v2) cuda_check(cudaMemcpyAsync(v2, h->v2, h->n * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
         if (v4ss) cuda_check(cudaMemcpyAsync(v4ss, h->ss, vsz * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
         if (v4dd) cuda_check(cudaMemcpyAsync(v4dd, h->dd, vsz * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
@@ -448,11 +526,19 @@ extern "C" int spn_su2_compute_step(spn_su2 *h) {
         }
         cuda_check(cudaMemsetAsync(h->status, 0, sizeof(unsigned), h->stream), "memset status");
         cuda_check(cudaMemsetAsync(h->work_counter, 0, sizeof(int), h->stream), "memset counter");
-        FlowArgs a = h->args();
-        su2_self_energy_kernel<<<h->n, 128, 0, h->stream>>>(a);
-        cuda_check(cudaGetLastError(), "self-energy launch");
-        su2_node_table_kernel<<<(h->n + 63) / 64, 64, 0, h->stream>>>(a);
-        cuda_check(cudaGetLastError(), "node table launch");
+        if (h->fp64()) {
+            const FlowArgsT<double> a = h->args64();
+            su2_self_energy_f64_kernel<<<h->n, 128, 0, h->stream>>>(a);
+            cuda_check(cudaGetLastError(), "self-energy launch");
+            su2_node_table_f64_kernel<<<(h->n + 63) / 64, 64, 0, h->stream>>>(a);
+            cuda_check(cudaGetLastError(), "node table launch");
+        } else {
+            const FlowArgs a = h->args();
+            su2_self_energy_kernel<<<h->n, 128, 0, h->stream>>>(a);
+            cuda_check(cudaGetLastError(), "self-energy launch");
+            su2_node_table_kernel<<<(h->n + 63) / 64, 64, 0, h->stream>>>(a);
+            cuda_check(cudaGetLastError(), "node table launch");
+        }
         if (h->profiling) {
             e1 = h->event();
             cuda_check(cudaEventRecord(h->ev_pool[e1], h->stream), "event record");
@@ -472,6 +558,8 @@ extern "C" int spn_su2_set_variant(spn_su2 *h, int npi, int sched_in_smem) {
         if (!h) throw Error(ErrorType::Argument, "null handle");
         if (npi != 1 && npi != 2) throw Error(ErrorType::Argument, "nodes per iteration must be 1 or 2");
         cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        if (h->fp64() && (npi != 1 || sched_in_smem))
+            throw Error(ErrorType::Unsupported, "an FP64 flow has one vertex-flow kernel (npi 1, schedule in global memory)");
         if (!select_variant(h, npi, sched_in_smem ? 1 : 0))
             throw Error(ErrorType::Unsupported, "vertex-flow variant does not fit on this device for this lattice");
     });
@@ -482,6 +570,12 @@ extern "C" int spn_su2_autotune(spn_su2 *h, int reps, int *npi, int *sched_in_sm
         if (!h) throw Error(ErrorType::Argument, "null handle");
         cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
         reps = std::max(1, std::min(reps, 16));
+        if (h->fp64()) {  // nothing to choose
+            if (npi) *npi = h->vertex_npi;
+            if (sched_in_smem) *sched_in_smem = h->rpa_in_smem;
+            if (grid) *grid = h->vertex_grid;
+            return;
+        }
         cudaEvent_t e0, e1;
         cuda_check(cudaEventCreate(&e0), "event");
         cuda_check(cudaEventCreate(&e1), "event");
@@ -535,6 +629,12 @@ extern "C" int spn_su2_get_flow(spn_su2 *h, float *dv2, float *dv4ss, float *dv4
         if (!h) throw Error(ErrorType::Argument, "null handle");
         cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
         const size_t vsz = size_t(h->fn) * h->nl;
+        if (h->fp64()) {
+            download_as_float(dv2, h->dv2d, h->n, h->stream);
+            download_as_float(dv4ss, h->dss64, vsz, h->stream);
+            download_as_float(dv4dd, h->ddd64, vsz, h->stream);
+            return;
+        }
         if (dv2) cuda_check(cudaMemcpyAsync(dv2, h->dv2, h->n * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
         if (dv4ss) cuda_check(cudaMemcpyAsync(dv4ss, h->dss, vsz * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
         if (dv4dd) cuda_check(cudaMemcpyAsync(dv4dd, h->ddd, vsz * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
@@ -548,6 +648,16 @@ extern "C" int spn_su2_finalize_step(spn_su2 *h, float new_cutoff) {
         cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
         const float step = new_cutoff - h->cutoff;
         const long long vsz = h->fn * h->nl;
+        if (h->fp64()) {
+            const double step64 = double(new_cutoff) - double(h->cutoff);
+            const int grid = int(std::min<long long>((vsz + 255) / 256, 4096));
+            su2_euler_flow_f64_kernel<<<1, 64, 0, h->stream>>>(h->v2d, h->dv2d, h->n, step64);
+            su2_euler_flow_f64_kernel<<<grid, 256, 0, h->stream>>>(h->dd64, h->ddd64, vsz, step64);
+            su2_euler_flow_f64_kernel<<<grid, 256, 0, h->stream>>>(h->ss64, h->dss64, vsz, step64);
+            cuda_check(cudaGetLastError(), "euler launch");
+            h->cutoff = new_cutoff;
+            return;
+        }
         if (h->flags & SPN_SU2_FP64_SELF_ENERGY)
             su2_euler_f64_kernel<<<1, 64, 0, h->stream>>>(h->v2d, h->dv2d, h->v2, h->n, step);
         else
@@ -587,7 +697,41 @@ CorrArgs spn::corr_args(const spn_su2 *h) {
 
 namespace {
 
+CorrArgsT<double> corr_args64(const spn_su2 *h) {
+        const CorrArgs f = corr_args(h);
+        CorrArgsT<double> a;
+        a.n = f.n;
+        a.nl = f.nl;
+        a.n_corr = f.n_corr;
+        a.cutoff = f.cutoff;
+        a.spin = f.spin;
+        a.freq = h->freq64;
+        a.ss = h->ss64;
+        a.dd = h->dd64;
+        a.v2 = h->v2d;
+        a.v2d = nullptr;
+        a.sites = f.sites;
+        a.inv_sites = f.inv_sites;
+        a.corr_rid = f.corr_rid;
+        a.partial = f.partial;
+        a.out = h->corr_out64;
+        a.wsite = f.wsite;
+        return a;
+}
+
 void launch_correlation(spn_su2 *h) {
+        if (h->fp64()) {
+            const CorrArgsT<double> a = corr_args64(h);
+            const int spt = spt_for(h->nl);
+            const int blocks = 2 * h->n + 4;
+            if (spt == 1) su2_corr_inner_f64_kernel<1><<<blocks, 128, 0, h->stream>>>(a);
+            else if (spt == 2) su2_corr_inner_f64_kernel<2><<<blocks, 128, 0, h->stream>>>(a);
+            else su2_corr_inner_f64_kernel<4><<<blocks, 128, 0, h->stream>>>(a);
+            cuda_check(cudaGetLastError(), "correlation launch");
+            su2_corr_final_f64_kernel<<<1, 128, 2 * h->nl * sizeof(double), h->stream>>>(a);
+            cuda_check(cudaGetLastError(), "correlation final launch");
+            return;
+        }
         const CorrArgs a = corr_args(h);
         const int spt = spt_for(h->nl);
         const int blocks = 2 * h->n + 4;
@@ -600,6 +744,18 @@ void launch_correlation(spn_su2 *h) {
 }
 
 void copy_correlation(spn_su2 *h, float *zz, float *dd, float *chi_zz, float *chi_dd) {
+        if (h->fp64()) {
+            const std::vector<double> v = download(h->corr_out64, 2 * size_t(h->n_corr) + 2 * h->nl, h->stream);
+            auto put = [&](float *out, size_t off, int cnt) {
+                if (out)
+                    for (int i = 0; i < cnt; ++i) out[i] = float(v[off + i]);
+            };
+            put(zz, 0, h->n_corr);
+            put(dd, h->n_corr, h->n_corr);
+            put(chi_zz, 2 * size_t(h->n_corr), h->nl);
+            put(chi_dd, 2 * size_t(h->n_corr) + h->nl, h->nl);
+            return;
+        }
         if (zz) cuda_check(cudaMemcpyAsync(zz, h->corr_out, h->n_corr * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
         if (dd)
             cuda_check(cudaMemcpyAsync(dd, h->corr_out + h->n_corr, h->n_corr * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
@@ -619,6 +775,69 @@ extern "C" int spn_su2_measure_correlation(spn_su2 *h, float *zz, float *dd, flo
         cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
         launch_correlation(h);
         copy_correlation(h, zz, dd, chi_zz, chi_dd);
+    });
+}
+
+// ---- double-precision data movement of an FP64 flow ----
+namespace {
+void require_fp64(const spn_su2 *h) {
+    if (!h) throw Error(ErrorType::Argument, "null handle");
+    if (!h->fp64()) throw Error(ErrorType::Unsupported, "the flow was not created with SPN_SU2_FP64");
+}
+}  // namespace
+
+extern "C" int spn_su2_set_state_f64(spn_su2 *h, float cutoff, const double *v2, const double *v4ss, const double *v4dd) {
+    return guarded([&] {
+        require_fp64(h);
+        if (!v2 || !v4ss || !v4dd) throw Error(ErrorType::Argument, "null argument");
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        const size_t vsz = size_t(h->fn) * h->nl;
+        upload(h->v2d, v2, h->n, h->stream);
+        upload(h->ss64, v4ss, vsz, h->stream);
+        upload(h->dd64, v4dd, vsz, h->stream);
+        h->cutoff = cutoff;
+        cuda_check(cudaStreamSynchronize(h->stream), "set_state sync");
+    });
+}
+
+extern "C" int spn_su2_get_state_f64(spn_su2 *h, float *cutoff, double *v2, double *v4ss, double *v4dd) {
+    return guarded([&] {
+        require_fp64(h);
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        const size_t vsz = size_t(h->fn) * h->nl;
+        if (cutoff) *cutoff = h->cutoff;
+        if (v2) cuda_check(cudaMemcpyAsync(v2, h->v2d, h->n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        if (v4ss) cuda_check(cudaMemcpyAsync(v4ss, h->ss64, vsz * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        if (v4dd) cuda_check(cudaMemcpyAsync(v4dd, h->dd64, vsz * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        cuda_check(cudaStreamSynchronize(h->stream), "get_state sync");
+    });
+}
+
+extern "C" int spn_su2_get_flow_f64(spn_su2 *h, double *dv2, double *dv4ss, double *dv4dd) {
+    return guarded([&] {
+        require_fp64(h);
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        const size_t vsz = size_t(h->fn) * h->nl;
+        if (dv2) cuda_check(cudaMemcpyAsync(dv2, h->dv2d, h->n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        if (dv4ss) cuda_check(cudaMemcpyAsync(dv4ss, h->dss64, vsz * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        if (dv4dd) cuda_check(cudaMemcpyAsync(dv4dd, h->ddd64, vsz * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        cuda_check(cudaStreamSynchronize(h->stream), "get_flow sync");
+    });
+}
+
+extern "C" int spn_su2_measure_correlation_f64(spn_su2 *h, double *zz, double *dd, double *chi_zz, double *chi_dd) {
+    return guarded([&] {
+        require_fp64(h);
+        cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
+        launch_correlation(h);
+        const std::vector<double> v = download(h->corr_out64, 2 * size_t(h->n_corr) + 2 * h->nl, h->stream);
+        auto put = [&](double *out, size_t off, int cnt) {
+            if (out) std::copy(v.begin() + off, v.begin() + off + cnt, out);
+        };
+        put(zz, 0, h->n_corr);
+        put(dd, h->n_corr, h->n_corr);
+        put(chi_zz, 2 * size_t(h->n_corr), h->nl);
+        put(chi_dd, 2 * size_t(h->n_corr) + h->nl, h->nl);
     });
 }
 

@@ -34,6 +34,10 @@ struct spn_su2 {
     int *range_rid = nullptr, *range_inv = nullptr, *corr_rid = nullptr;
     double *corr_partial = nullptr;
     double *v2d = nullptr, *dv2d = nullptr;  // FP64 self-energy (SPN_SU2_FP64_SELF_ENERGY)
+    // FP64 flow (SPN_SU2_FP64): state, flow, node tables and measurement output in double;
+    // the float arrays above other than v2/dv2 stay unallocated.
+    double *freq64 = nullptr, *ss64 = nullptr, *dd64 = nullptr, *dss64 = nullptr, *ddd64 = nullptr;
+    double *node_wp64 = nullptr, *node_c64 = nullptr, *corr_out64 = nullptr;
     int *rpa_image = nullptr;  // sched | count | slot_base | seg_ptr in one allocation (the staged layout)
     int *rpa_sched = nullptr, *rpa_count = nullptr, *rpa_slot_base = nullptr, *rpa_seg_ptr = nullptr;  // into rpa_image
     int rpa_image_bytes = 0;
@@ -89,6 +93,46 @@ struct spn_su2 {
         return a;
     }
 
+    bool fp64() const { return (flags & SPN_SU2_FP64) != 0; }
+
+    // Argument block of an FP64 flow: every array in double, the self-energy in v2d/dv2d.
+    spn::FlowArgsT<double> args64() const {
+        const spn::FlowArgs f = args();
+        spn::FlowArgsT<double> a;
+        a.n = f.n;
+        a.nl = f.nl;
+        a.fn = f.fn;
+        a.wsite = f.wsite;
+        a.max_nodes = f.max_nodes;
+        a.n_range = f.n_range;
+        a.cutoff = f.cutoff;
+        a.spin = f.spin;
+        a.freq = freq64;
+        a.ss = ss64;
+        a.dd = dd64;
+        a.dss = dss64;
+        a.ddd = ddd64;
+        a.v2 = v2d;
+        a.dv2 = dv2d;
+        a.v2d = v2d;
+        a.dv2d = dv2d;
+        a.fp64_sigma = 0;
+        a.sites = f.sites;
+        a.inv_sites = f.inv_sites;
+        a.ov_ptr = f.ov_ptr;
+        a.ov_r1 = f.ov_r1;
+        a.ov_r2 = f.ov_r2;
+        a.range_rid = f.range_rid;
+        a.range_inv = f.range_inv;
+        a.node_wp = node_wp64;
+        a.node_c = node_c64;
+        a.node_cnt = f.node_cnt;
+        a.work_counter = f.work_counter;
+        a.status = f.status;
+        a.rpa = f.rpa;
+        return a;
+    }
+
     int event() {
         cudaEvent_t e;
         spn::cuda_check(cudaEventCreate(&e), "cudaEventCreate");
@@ -103,7 +147,8 @@ struct spn_su2 {
         void *ptrs[] = {freq,      ss,        dd,        dss,       ddd,          v2,          dv2,
                         node_wp,   node_c,    corr_out,  node_cnt,  work_counter, status,      sites,
                         inv_sites, ov_ptr,    ov_r1,     ov_r2,     range_rid,    range_inv,   corr_rid,
-                        corr_partial, rpa_image, v2d, dv2d};
+                        corr_partial, rpa_image, v2d, dv2d, freq64, ss64, dd64, dss64, ddd64,
+                        node_wp64, node_c64, corr_out64};
         for (void *p : ptrs)
             if (p) cudaFree(p);
         if (own_stream && stream) cudaStreamDestroy(stream);

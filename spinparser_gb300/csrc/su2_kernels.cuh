@@ -15,19 +15,20 @@ constexpr int kCorrWarps = 4;  // the correlation kernels run 128-thread blocks
 // ------------------------------------------------------------------------------------
 // 1. self-energy flow
 // ------------------------------------------------------------------------------------
-__device__ __forceinline__ void self_energy_body(const FlowArgs &a, int blk) {
-    __shared__ float pos[kMaxFreq];
+template <class T>
+__device__ __forceinline__ void self_energy_body(const FlowArgsT<T> &a, int blk) {
+    __shared__ T pos[kMaxFreq];
     __shared__ double red[4];
     for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
     __syncthreads();
     const int i = blk;
-    const float w = pos[i], L = a.cutoff;
-    const float wpl = w + L, wml = w - L;
+    const T w = pos[i], L = T(a.cutoff);
+    const T wpl = w + L, wml = w - L;
     double part = 0.0;
     for (int j = threadIdx.x; j < a.n_range; j += blockDim.x) {
         const int r12 = a.range_rid[j], r21 = a.range_inv[j];
-        float x1 = value_none(pos, a.n, a.nl, a.dd, true, r12, r21, wpl, 0.0f, wml);
-        float x2 = value_none(pos, a.n, a.nl, a.dd, true, r12, r21, wml, 0.0f, wpl);
+        T x1 = value_none(pos, a.n, a.nl, a.dd, true, r12, r21, wpl, T(0), wml);
+        T x2 = value_none(pos, a.n, a.nl, a.dd, true, r12, r21, wml, T(0), wpl);
         part += double(x1) - double(x2);
     }
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
@@ -37,13 +38,13 @@ __device__ __forceinline__ void self_energy_body(const FlowArgs &a, int blk) {
         double sum = 0.0;
         for (int k = 0; k < int(blockDim.x >> 5); ++k) sum += red[k];
         double val = -4.0 * double(a.spin) * sum;
-        val += 0.75 * (double(value_none(pos, a.n, a.nl, a.ss, false, 0, 0, wpl, wml, 0.0f)) -
-                       double(value_none(pos, a.n, a.nl, a.ss, false, 0, 0, wml, wpl, 0.0f)));
-        val += (double(value_none(pos, a.n, a.nl, a.dd, true, 0, 0, wpl, wml, 0.0f)) -
-                double(value_none(pos, a.n, a.nl, a.dd, true, 0, 0, wml, wpl, 0.0f)));
+        val += 0.75 * (double(value_none(pos, a.n, a.nl, a.ss, false, 0, 0, wpl, wml, T(0))) -
+                       double(value_none(pos, a.n, a.nl, a.ss, false, 0, 0, wml, wpl, T(0))));
+        val += (double(value_none(pos, a.n, a.nl, a.dd, true, 0, 0, wpl, wml, T(0))) -
+                double(value_none(pos, a.n, a.nl, a.dd, true, 0, 0, wml, wpl, T(0))));
         const double sig = a.fp64_sigma ? odd_interp(pos, a.n, a.v2d, L) : odd_interp(pos, a.n, a.v2, L);
         val /= (2.0 * kPiD * (double(L) + sig));
-        float out = float(val);
+        T out = T(val);
         a.dv2[i] = out;
         if (a.fp64_sigma) a.dv2d[i] = val;
         if (isnan(out)) atomicOr(a.status, kStatusNaN);
@@ -53,39 +54,40 @@ __device__ __forceinline__ void self_energy_body(const FlowArgs &a, int blk) {
 // ------------------------------------------------------------------------------------
 // 2. loop-frequency node tables
 // ------------------------------------------------------------------------------------
-__device__ __forceinline__ void node_table_body(const FlowArgs &a, int blk) {
-    __shared__ float pos[kMaxFreq];
+template <class T>
+__device__ __forceinline__ void node_table_body(const FlowArgsT<T> &a, int blk) {
+    __shared__ T pos[kMaxFreq];
     for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
     __syncthreads();
     const int xi = blk * blockDim.x + threadIdx.x;
     if (xi >= a.n) return;
     const int n = a.n;
-    const float x = pos[xi], L = a.cutoff;
-    float *wp_out = a.node_wp + size_t(xi) * a.max_nodes;
-    float *c_out = a.node_c + size_t(xi) * a.max_nodes;
+    const T x = pos[xi], L = T(a.cutoff);
+    T *wp_out = a.node_wp + size_t(xi) * a.max_nodes;
+    T *c_out = a.node_c + size_t(xi) * a.max_nodes;
     int cnt = 0;
     bool overflow = false;
-    auto put = [&](float wp, double c) {
+    auto put = [&](T wp, double c) {
         if (cnt < a.max_nodes) {
             wp_out[cnt] = wp;
-            c_out[cnt] = float(c);
+            c_out[cnt] = T(c);
             ++cnt;
         } else {
             overflow = true;
         }
     };
-    auto sig = [&](float w) { return a.fp64_sigma ? odd_interp(pos, n, a.v2d, w) : odd_interp(pos, n, a.v2, w); };
-    auto dsig = [&](float w) { return a.fp64_sigma ? odd_interp(pos, n, a.dv2d, w) : odd_interp(pos, n, a.dv2, w); };
-    auto p = [&](float w1, float w2) { return 1.0 / ((double(w1) + sig(w1)) * (double(w2) + sig(w2))); };
-    auto pk = [&](float w1, float w2) {
+    auto sig = [&](T w) { return a.fp64_sigma ? odd_interp(pos, n, a.v2d, w) : odd_interp(pos, n, a.v2, w); };
+    auto dsig = [&](T w) { return a.fp64_sigma ? odd_interp(pos, n, a.dv2d, w) : odd_interp(pos, n, a.dv2, w); };
+    auto p = [&](T w1, T w2) { return 1.0 / ((double(w1) + sig(w1)) * (double(w2) + sig(w2))); };
+    auto pk = [&](T w1, T w2) {
         double d1 = double(w1) + sig(w1);
         return dsig(w1) / (d1 * d1 * (double(w2) + sig(w2)));
     };
     // conventional contribution (SU2FrgCore.cpp:351-371)
     put(L, p(L, L + x));
-    if (x > 2.0f * L) put(-L, p(L, L - x));
+    if (x > T(2) * L) put(-L, p(L, L - x));
     // Katanin contribution (SU2FrgCore.cpp:374-424)
-    auto kat = [&](float wp, double weight) { put(wp, weight * pk(wp, x + wp)); };
+    auto kat = [&](T wp, double weight) { put(wp, weight * pk(wp, x + wp)); };
     if (-(x + L) > -pos[n - 1]) nodes_right(pos, n, -(x + L), kat);
     if (x - L > L) nodes_both(pos, n, L - x, -L, kat);
     if (L < pos[n - 1]) nodes_left(pos, n, L, kat);
@@ -98,48 +100,50 @@ __device__ __forceinline__ void node_table_body(const FlowArgs &a, int blk) {
 // SU2FrgCore.cpp:111-137)
 // ------------------------------------------------------------------------------------
 __device__ __forceinline__ float euler_update(float x, float dx, float step) { return __fadd_rn(x, __fmul_rn(step, dx)); }
-// FP64 self-energy (SPN_SU2_FP64_SELF_ENERGY): the same update in double precision.
-__device__ __forceinline__ double euler_update_f64(double x, double dx, float step) {
-    return __dadd_rn(x, __dmul_rn(double(step), dx));
+// FP64 self-energy (SPN_SU2_FP64_SELF_ENERGY) and the FP64 flow: the same update in double.
+__device__ __forceinline__ double euler_update_f64(double x, double dx, double step) {
+    return __dadd_rn(x, __dmul_rn(step, dx));
 }
 
 // ------------------------------------------------------------------------------------
 // correlation measurement (nu = 0), SU2MeasurementCorrelation.cpp:77-177
 // ------------------------------------------------------------------------------------
-__device__ __forceinline__ double corr_sigma(const CorrArgs &a, const float *pos, float w) {
+template <class T>
+__device__ __forceinline__ double corr_sigma(const CorrArgsT<T> &a, const T *pos, T w) {
     return a.v2d ? odd_interp(pos, a.n, a.v2d, w) : odd_interp(pos, a.n, a.v2, w);
 }
 
 // Loop-frequency nodes of the measurement's trapezoid rules at nu = 0 (outer and inner
 // integrals use the same ranges): (-inf, -cutoff] and [cutoff, inf).
-__device__ inline int corr_nodes(const float *pos, int n, float cut, float *wp, double *w) {
+template <class T>
+__device__ inline int corr_nodes(const T *pos, int n, T cut, T *wp, double *w) {
     int cnt = 0;
-    auto put = [&](float x, double c) {
+    auto put = [&](T x, double c) {
         wp[cnt] = x;
         w[cnt] = c;
         ++cnt;
     };
-    if (-(0.0f + cut) > -pos[n - 1]) nodes_right(pos, n, -cut - 0.0f, put);
+    if (-(T(0) + cut) > -pos[n - 1]) nodes_right(pos, n, -cut - T(0), put);
     if (cut < pos[n - 1]) nodes_left(pos, n, cut, put);
     return cnt;
 }
 
 constexpr int kMaxCorrNodes = 2 * kMaxFreq + 8;
 
-template <int SPT>
-__device__ __forceinline__ void corr_inner_body(const CorrArgs &a, int blk) {
-    __shared__ float pos[kMaxFreq];
-    __shared__ float nwp[kMaxCorrNodes];
+template <int SPT, class T>
+__device__ __forceinline__ void corr_inner_body(const CorrArgsT<T> &a, int blk) {
+    __shared__ T pos[kMaxFreq];
+    __shared__ T nwp[kMaxCorrNodes];
     __shared__ double nw[kMaxCorrNodes];
     __shared__ int ncnt;
     __shared__ double red[4][2][32 * SPT];
     for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
     __syncthreads();
-    if (threadIdx.x == 0) ncnt = corr_nodes(pos, a.n, a.cutoff, nwp, nw);
+    if (threadIdx.x == 0) ncnt = corr_nodes(pos, a.n, T(a.cutoff), nwp, nw);
     __syncthreads();
     const int ia = blk;
     if (ia >= ncnt) return;
-    const float w = nwp[ia];
+    const T w = nwp[ia];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int W = (SPT == 1) ? a.wsite : 32;
     const int G = 32 / W;
@@ -154,24 +158,24 @@ __device__ __forceinline__ void corr_inner_body(const CorrArgs &a, int blk) {
         isite[k] = valid[k] ? a.inv_sites[j] : 0;
     }
     const double S = a.spin;
-    auto sig = [&](float x) { return corr_sigma(a, pos, x); };
+    auto sig = [&](T x) { return corr_sigma(a, pos, x); };
     const double dw = double(w) + sig(w);
     double acc_s[SPT], acc_d[SPT];
     for (int k = 0; k < SPT; ++k) acc_s[k] = acc_d[k] = 0.0;
     const int groups = kCorrWarps * G;
     const int gid = warp * G + g;
     for (int b = gid; b < ncnt; b += groups) {
-        const float wp = nwp[b];
-        AB8 ab;
-        access8(pos, a.n, nl, w + wp + 0.0f, 0.0f, w - wp, ab);
-        const float vs = value_none(pos, a.n, nl, a.ss, false, 0, 0, w + wp + 0.0f, w - wp, 0.0f);
-        const float vd = value_none(pos, a.n, nl, a.dd, true, 0, 0, w + wp + 0.0f, w - wp, 0.0f);
+        const T wp = nwp[b];
+        AB8T<T> ab;
+        access8(pos, a.n, nl, w + wp + T(0), T(0), w - wp, ab);
+        const T vs = value_none(pos, a.n, nl, a.ss, false, 0, 0, w + wp + T(0), w - wp, T(0));
+        const T vd = value_none(pos, a.n, nl, a.dd, true, 0, 0, w + wp + T(0), w - wp, T(0));
         const double dwp = double(wp) + sig(wp);
         const double norm = 1.0 / (dw * dw * dwp * dwp * (4.0 * kPiD * kPiD));
         const double cw = nw[b] * norm;
         for (int k = 0; k < SPT; ++k) {
             const int st = ab.exch ? isite[k] : site[k];
-            float gs = 0.0f, gd = 0.0f;
+            T gs = T(0), gd = T(0);
             for (int q = 0; q < 8; ++q) {
                 gs += ab.w[q] * __ldg(a.ss + ab.off[q] + st);
                 gd += ab.sw[q] * __ldg(a.dd + ab.off[q] + st);
@@ -210,15 +214,16 @@ __device__ __forceinline__ void corr_inner_body(const CorrArgs &a, int blk) {
     }
 }
 
-__device__ __forceinline__ void corr_final_body(const CorrArgs &a) {
-    __shared__ float pos[kMaxFreq];
-    __shared__ float nwp[kMaxCorrNodes];
+template <class T>
+__device__ __forceinline__ void corr_final_body(const CorrArgsT<T> &a) {
+    __shared__ T pos[kMaxFreq];
+    __shared__ T nwp[kMaxCorrNodes];
     __shared__ double nw[kMaxCorrNodes];
     __shared__ int ncnt;
     extern __shared__ double chi[];  // [2][nl]
     for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
     __syncthreads();
-    if (threadIdx.x == 0) ncnt = corr_nodes(pos, a.n, a.cutoff, nwp, nw);
+    if (threadIdx.x == 0) ncnt = corr_nodes(pos, a.n, T(a.cutoff), nwp, nw);
     __syncthreads();
     const double S = a.spin;
     for (int j = threadIdx.x; j < a.nl; j += blockDim.x) {
@@ -227,7 +232,7 @@ __device__ __forceinline__ void corr_final_body(const CorrArgs &a) {
             double ls = a.partial[(size_t(ia) * 2 + 0) * a.nl + j];
             double ld = a.partial[(size_t(ia) * 2 + 1) * a.nl + j];
             if (j == 0) {
-                const float w = nwp[ia];
+                const T w = nwp[ia];
                 const double dw = double(w) + corr_sigma(a, pos, w);
                 const double t1 = 1.0 / (dw * dw);
                 ls += S * t1 / (2.0 * kPiD);
@@ -238,14 +243,14 @@ __device__ __forceinline__ void corr_final_body(const CorrArgs &a) {
         }
         chi[j] = cs;
         chi[a.nl + j] = cd;
-        a.out[2 * a.n_corr + j] = float(cs);
-        a.out[2 * a.n_corr + a.nl + j] = float(cd);
+        a.out[2 * a.n_corr + j] = T(cs);
+        a.out[2 * a.n_corr + a.nl + j] = T(cd);
     }
     __syncthreads();
     for (int q = threadIdx.x; q < a.n_corr; q += blockDim.x) {
         const int r = a.corr_rid[q];
-        a.out[q] = float(chi[r]);
-        a.out[a.n_corr + q] = float(chi[a.nl + r]);
+        a.out[q] = T(chi[r]);
+        a.out[a.n_corr + q] = T(chi[a.nl + r]);
     }
 }
 
