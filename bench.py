@@ -55,6 +55,9 @@ WORKLOADS = {
 DEFAULT_WORKLOAD = "cubic-j1j2-r6-n64"
 # multi-flow workloads (spinparser_gb300/workloads.py): the seeded scan and the serving stream
 MULTI_WORKLOADS = ("scan-square-j1j2-128", "serve-mixed")
+# precision study: the single-flow workload run to the end in FP32 forms and in FP64 on the GPU
+PRECISION_WORKLOADS = {"precision-cubic-j1j2-r6-n64": "cubic-j1j2-r6-n64",
+                       "precision-pyrochlore-r5-n64": "pyrochlore-r5-n64"}
 METRIC = "cutoff steps/s per flow"
 KERNELS_PER_STEP = 8  # self-energy, node tables, vertex flow, 2 x correlation, 3 x Euler
 
@@ -65,7 +68,8 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + list(MULTI_WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + list(MULTI_WORKLOADS) + list(PRECISION_WORKLOADS),
+                    default=DEFAULT_WORKLOAD)
     ap.add_argument("--flows", type=int, default=None, help="multi-flow workloads: number of flows / requests")
     ap.add_argument("--rates", type=str, default="0.5,1,2,4,inf",
                     help="serve-mixed: arrival rates as multiples of the sequential plain-GPU capacity")
@@ -358,10 +362,102 @@ def run_multi(args):
     print(json.dumps(line))
 
 
+def _flow_history(flow, cut, fp64):
+    """Runs a flow over the whole cutoff list as the task driver does (measure, then step) and
+    returns (chi_zz[k, Nl], zz[k, n_corr], seconds, steps measured); stops at a divergence."""
+    import spinparser_gb300 as spn  # noqa: F401
+
+    chi = np.full((len(cut), flow.nl), np.nan)
+    zz = np.full((len(cut), flow.n_corr), np.nan)
+    t0 = time.perf_counter()
+    k = 0
+    for k in range(len(cut)):
+        if fp64:
+            z, _, c, _ = flow.measure_correlation_f64()
+        else:
+            z, _, c, _ = flow.measure_correlation()
+        chi[k], zz[k] = c, z
+        if k + 1 == len(cut):
+            break
+        flow.compute_step()
+        flow.finalize_step(float(cut[k + 1]))
+        if flow.is_diverged():
+            break
+    flow.synchronize()
+    return chi, zz, time.perf_counter() - t0, k + 1
+
+
+def run_precision(args):
+    """Error of the FP32 flows against the FP64 flow of the same task, both on the GPU.
+
+    Three flows from the same initial condition over the whole cutoff list, each measured at
+    every cutoff: the FP64 flow (SPN_SU2_FP64: every operation in double), the precision form
+    (FP32 vertex with Kahan-compensated loop-frequency sums, FP64 self-energy state, quadrature
+    weights and measurement accumulation: SPN_SU2_FP64_SELF_ENERGY) and the plain FP32 flow.
+    The error at cutoff k is normwise, max_rid |chi32 - chi64| / max_rid |chi64| of the static
+    spin susceptibility (and the same for the correlation entries zz)."""
+    import torch
+
+    import spinparser_gb300 as spn
+
+    torch.cuda.set_device(0)
+    name = PRECISION_WORKLOADS[args.workload]
+    wl = WORKLOADS[name]
+    tab, freq, cut = setup(wl)
+    init = tab.initial_state(len(freq))
+    sampler = ClockSampler(0)
+    sampler.start()
+    arms = {}
+    for label, flags in (("fp64", spn.FP64), ("fp32_fp64_self_energy", spn.FP64_SELF_ENERGY), ("fp32_plain", 0)):
+        flow = spn.Su2Flow(tab, freq, flags=flags)
+        flow.set_state(float(cut[0]), *init)
+        if flags != spn.FP64:
+            flow.autotune()
+        arms[label] = _flow_history(flow, cut, flags == spn.FP64)
+        flow.close()
+    clocks = sampler.stop()
+    chi64, zz64, t64, n64 = arms["fp64"]
+
+    def err(a, b):
+        return float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-300))
+
+    report = {}
+    for label in ("fp32_fp64_self_energy", "fp32_plain"):
+        chi, zz, secs, nk = arms[label]
+        n = min(nk, n64)
+        e_chi = np.array([err(chi[k], chi64[k]) for k in range(n)])
+        e_zz = np.array([err(zz[k], zz64[k]) for k in range(n)])
+        idx = sorted(set(np.linspace(0, n - 1, 12).astype(int).tolist()))
+        report[label] = {
+            "final_rel_err_chi": float(e_chi[n - 1]), "final_rel_err_zz": float(e_zz[n - 1]),
+            "max_rel_err_chi": float(e_chi.max()), "max_rel_err_zz": float(e_zz.max()),
+            "growth": [{"step": k, "cutoff": float(cut[k]), "rel_err_chi": float(e_chi[k]),
+                        "rel_err_zz": float(e_zz[k])} for k in idx],
+            "steps_measured": nk, "flow_seconds": secs, "steps_per_s": (nk - 1) / secs,
+        }
+    main_arm = report["fp32_fp64_self_energy"]
+    line = {
+        "metric": "final correlation rel. error vs FP64 GPU flow", "value": main_arm["final_rel_err_chi"],
+        "unit": "relative", "n_gpus": 1, "higher_is_better": False, "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (model initial condition, advanced by the flow)", "tolerance": 1e-4,
+        "within_tolerance": bool(main_arm["final_rel_err_chi"] <= 1e-4 and main_arm["final_rel_err_zz"] <= 1e-4),
+        "config": {"workload": args.workload, "lattice": wl["lattice"], "range": wl["range"], "model": wl["model"],
+                   "params": wl["params"], "n_freq": len(freq), "freq_range": [wl["fmin"], wl["fmax"]],
+                   "cutoff": [wl["cmax"], wl["cmin"], wl["cstep"]], "n_cutoffs": len(cut), "n_sites": tab.n_sites},
+        "fp64_flow": {"steps_measured": n64, "flow_seconds": t64, "steps_per_s": (n64 - 1) / t64},
+        "arms": report,
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
 def main():
     args = parse_args()
     if args.workload in MULTI_WORKLOADS:
         run_multi(args)
+        return
+    if args.workload in PRECISION_WORKLOADS:
+        run_precision(args)
         return
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":

@@ -102,7 +102,8 @@ int spn_lattice_get_interactions(const spn_lattice *lat, int *rid, float *coupli
 
 /* The RPA schedule the device uses for a lattice (diagnostics; host only): the merged pair
  * lists of all rids cut into `lanes` balanced chunks (csrc/host/rpa_schedule.hpp).
- * info[4] = {entries per lane, segments, total ints of sched, packed encoding (Nl <= 32)}.
+ * info[5] = {entries per lane, segments, total ints of sched, packed encoding (Nl <= 32),
+ * row width of the outer-product matrix the packed entries index (0 otherwise)}.
  * With sched = NULL only info is filled; otherwise sched must hold info[2] ints, count and
  * slot_base `lanes` ints and seg_ptr Nl + 1 ints. */
 int spn_rpa_schedule(int n_sites, const int *overlap_ptr, const int *overlap_rid1, const int *overlap_rid2, int lanes,

@@ -236,6 +236,7 @@ extern "C" int spn_rpa_schedule(int n_sites, const int *overlap_ptr, const int *
         info[1] = s.n_seg;
         info[2] = int(s.sched.size());
         info[3] = s.packed ? 1 : 0;
+        info[4] = s.width;
         if (!sched) return;
         std::memcpy(sched, s.sched.data(), s.sched.size() * sizeof(int));
         if (count) std::memcpy(count, s.count.data(), s.count.size() * sizeof(int));

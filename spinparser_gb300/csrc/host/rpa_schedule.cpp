@@ -62,7 +62,7 @@ RpaHostSchedule build_rpa_schedule(int nl, const int *ptr, const int *r1, const 
         if (s.seg_ptr[r] < 0) s.seg_ptr[r] = s.seg_ptr[r + 1];
 
     s.packed = nl <= 32;
-    const unsigned scale = nl <= 16 ? 8u : 4u;
+    s.width = s.packed ? rpa_outer_width(nl) : 0;
 
     for (int l = 0; l < lanes; ++l) {
         size_t si = 0;
@@ -71,7 +71,7 @@ RpaHostSchedule build_rpa_schedule(int nl, const int *ptr, const int *r1, const 
             const bool last = (i + 1 == seg_end[l][si]);
             if (last) ++si;
             s.sched[size_t(i) * lanes + l] =
-                s.packed ? int(scale * p.a | (scale * p.b) << 8 | unsigned(p.m) << 16 | (last ? 0x80000000u : 0u))
+                s.packed ? int(unsigned(p.a * s.width + p.b) * 8u | unsigned(p.m) << 16 | (last ? 0x80000000u : 0u))
                          : p.a | (p.b << 7) | (p.m << 14) | (last ? (1 << 22) : 0);
         }
     }

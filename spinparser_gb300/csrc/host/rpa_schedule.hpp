@@ -5,20 +5,33 @@
 // into `lanes` contiguous chunks of equal length; a run of one rid inside a chunk is a
 // segment, whose partial sum goes to the lane's next slot (slot_base[l], +1, ...); rid r sums
 // the slots seg_ptr[r] .. seg_ptr[r+1]-1 in order.  Entry i of lane l is sched[i * lanes + l].
-// The kernel accumulates acc += (A[rid1] * m) * B[rid2] for spin and density.  Entries:
-//   Nl <= 32 ("packed"): off1 | off2 << 8 | m << 16 | last << 31 with byte offsets of the
-//            exchanged values -- 8 rid (interleaved (spin, density) float2 arrays) for Nl <= 16,
-//            where every element has its own 8-byte bank pair, and 4 rid (separate 32-bit
-//            arrays, conflict-free) for 16 < Nl <= 32;
-//   Nl > 32: rid1 | rid2 << 7 | m << 14 | last << 22.
+// Entries:
+//   Nl <= 32 ("packed", outer-product form): off | m << 16 | last << 31, off = the byte offset
+//            (rid1 * W + rid2) * 8 of the (spin, density) float2 element M[rid1][rid2] of a
+//            row-major W x W matrix, W = rpa_outer_width(Nl).  The kernel accumulates
+//            M = sum over nodes of (c A) x B first and walks the schedule once per triple:
+//            acc += m * M[rid1][rid2];
+//   Nl > 32: rid1 | rid2 << 7 | m << 14 | last << 22; the kernel accumulates
+//            acc += (A[rid1] * m) * B[rid2] per node.
 #pragma once
 #include <vector>
 
+#ifdef __CUDACC__
+#define SPN_HD __host__ __device__
+#else
+#define SPN_HD
+#endif
+
 namespace spn {
+
+// Row width of the outer-product RPA matrix of a lattice with nl <= 32 sites: 8 x the rows of
+// M one lane accumulates (the warp's 32 lanes form an 8 x 4 grid of blocks of w/8 x w/4).
+SPN_HD inline int rpa_outer_width(int nl) { return nl <= 8 ? 8 : (nl <= 16 ? 16 : (nl <= 24 ? 24 : 32)); }
 
 struct RpaHostSchedule {
     std::vector<int> sched, count, slot_base, seg_ptr;
     int lanes = 0, n_seg = 0, len = 0;
+    int width = 0;  // outer-product matrix row width (packed form)
     bool packed = false;
 };
 

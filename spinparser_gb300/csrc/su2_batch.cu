@@ -30,12 +30,12 @@ using namespace spn::dev;
 
 namespace {
 
-constexpr int kClasses = 3;  // sites per lane 1, 2, 4
+constexpr int kClasses = 3;  // measurement classes: sites per lane 1, 2, 4
 constexpr int kBatchSchedMaxInts = 3072;  // per-warp staged RPA schedule (12 KB) at most
 
 __global__ void batch_prepare_kernel(BatchFlow *flows, const int *list, int n, int *counters) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < kClasses && blockIdx.x == 0) counters[i] = 0;
+    if (i < kVertexClasses && blockIdx.x == 0) counters[i] = 0;
     if (i >= n) return;
     BatchFlow &f = flows[list[i]];
     if (f.phase != kPhaseDone) *f.a.status = 0u;
@@ -190,9 +190,10 @@ struct spn_batch {
     std::vector<int> lists;  // flowing | measure | per-class measure | per-class vertex list | per-class prefix
     int n_flowing = 0, n_measure = 0, n_max = 2;
     int off_flowing = 0, off_measure = 0;
-    int off_cm[kClasses] = {}, n_cm[kClasses] = {};
-    int off_cv[kClasses] = {}, n_cv[kClasses] = {}, off_cp[kClasses] = {}, total_cv[kClasses] = {};
-    int warp_area[kClasses] = {}, nl_max = 1, vgrid[kClasses] = {}, sched_ints[kClasses] = {};
+    int off_cm[kClasses] = {}, n_cm[kClasses] = {};  // per measurement class
+    // per vertex class (vertex_class): work lists, prefixes, shared memory, grid
+    int off_cv[kVertexClasses] = {}, n_cv[kVertexClasses] = {}, off_cp[kVertexClasses] = {}, total_cv[kVertexClasses] = {};
+    int warp_area[kVertexClasses] = {}, nl_max = 1, vgrid[kVertexClasses] = {}, sched_ints[kVertexClasses] = {};
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     long long steps_run = 0, graph_builds = 0;
@@ -281,18 +282,19 @@ struct spn_batch {
         lists.clear();
         n_max = 2;
         nl_max = 1;
-        std::vector<int> flowing, measure, cm[kClasses], cv[kClasses];
+        std::vector<int> flowing, measure, cm[kClasses], cv[kVertexClasses];
         for (size_t i = 0; i < flows.size(); ++i) {
             const Flow &f = flows[i];
             if (!f.used || f.phase == kPhaseDone) continue;
             const int c = class_of(f.h->nl);
             measure.push_back(int(i));
             cm[c].push_back(int(i));
+            const int vc = vertex_class(f.h->nl);
             n_max = std::max(n_max, f.h->n);
             nl_max = std::max(nl_max, f.h->nl);
             if (f.phase == kPhaseFlowing) {
                 flowing.push_back(int(i));
-                cv[c].push_back(int(i));
+                cv[vc].push_back(int(i));
             }
         }
         auto put = [&](const std::vector<int> &v) {
@@ -307,6 +309,8 @@ struct spn_batch {
         for (int c = 0; c < kClasses; ++c) {
             off_cm[c] = put(cm[c]);
             n_cm[c] = int(cm[c].size());
+        }
+        for (int c = 0; c < kVertexClasses; ++c) {
             off_cv[c] = put(cv[c]);
             n_cv[c] = int(cv[c].size());
             std::vector<int> prefix(1, 0);
@@ -328,7 +332,7 @@ struct spn_batch {
             vgrid[c] = 0;
             if (n_cv[c] > 0) {
                 const size_t smem = batch_vertex_smem_bytes(n_max, warp_area[c], sched_ints[c]);
-                const int per_sm = batch_vertex_blocks_per_sm(1 << c, npi, smem);
+                const int per_sm = batch_vertex_blocks_per_sm(c, npi, smem);
                 cudaGetLastError();
                 if (per_sm < 1) throw Error(ErrorType::Unsupported, "batched vertex-flow kernel does not fit for this batch");
                 vgrid[c] = sms * per_sm;
@@ -353,12 +357,12 @@ struct spn_batch {
 
     void enqueue_step() {
         const int *L = d_lists;
-        batch_prepare_kernel<<<(std::max(n_measure, kClasses) + 127) / 128, 128, 0, stream>>>(d_flows, L + off_measure, n_measure,
+        batch_prepare_kernel<<<(std::max(n_measure, kVertexClasses) + 127) / 128, 128, 0, stream>>>(d_flows, L + off_measure, n_measure,
                                                                                              d_counters);
         if (n_flowing > 0) {
             batch_self_energy_kernel<<<dim3(n_max, n_flowing), 128, 0, stream>>>(d_flows, L + off_flowing);
             batch_node_table_kernel<<<dim3((n_max + 63) / 64, n_flowing), 64, 0, stream>>>(d_flows, L + off_flowing);
-            for (int c = 0; c < kClasses; ++c) {
+            for (int c = 0; c < kVertexClasses; ++c) {
                 if (n_cv[c] == 0) continue;
                 BatchVertexArgs b;
                 b.flows = d_flows;
@@ -370,7 +374,7 @@ struct spn_batch {
                 b.counter = d_counters + c;
                 b.warp_area = warp_area[c];
                 b.sched_ints = sched_ints[c];
-                launch_batch_vertex(b, 1 << c, npi, vgrid[c], stream);
+                launch_batch_vertex(b, c, npi, vgrid[c], stream);
             }
         }
         for (int c = 0; c < kClasses; ++c) {
@@ -414,7 +418,7 @@ extern "C" int spn_batch_create(int device, spn_batch **out) {
         cuda_check(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device), "device attribute");
         cuda_check(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
         cuda_check(cudaEventCreateWithFlags(&b->status_ev, cudaEventDisableTiming), "cudaEventCreate");
-        b->d_counters = dalloc<int>(kClasses, "alloc batch counters");
+        b->d_counters = dalloc<int>(kVertexClasses, "alloc batch counters");
         b->ensure_capacity(16);
         *out = b.release();
     });

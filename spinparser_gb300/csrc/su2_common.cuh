@@ -2,6 +2,7 @@
 // the launch interface of the vertex-flow kernel.
 #pragma once
 #include <cuda_runtime.h>
+#include "host/rpa_schedule.hpp"
 
 namespace spn {
 
@@ -12,11 +13,10 @@ constexpr unsigned kStatusStageTimeout = 4u;  // a bulk copy to shared memory di
 
 // Lane-balanced RPA schedule (built by host/rpa_schedule.cpp): the RPA pair lists of all
 // rids merged into distinct (rid, rid1, rid2) with their multiplicity, sorted by rid and cut
-// into `lanes` contiguous chunks.  Entry i of lane l is sched[i * lanes + l]:
-//   bits 0-6 rid1, bits 7-13 rid2, bits 14-21 multiplicity, bit 22 "last pair of a segment".
-// A segment is a run of pairs of one output rid inside one chunk; its partial sum goes to the
-// next slot of the lane (slot_base[l], slot_base[l]+1, ...), and rid r sums the slots
-// seg_ptr[r] .. seg_ptr[r+1]-1 in order.
+// into `lanes` (32) contiguous chunks.  Entry i of lane l is sched[i * lanes + l]; the entry
+// encodings are described in host/rpa_schedule.hpp.  A segment is a run of pairs of one output
+// rid inside one chunk; its partial sum goes to the next slot of the lane (slot_base[l],
+// slot_base[l]+1, ...), and rid r sums the slots seg_ptr[r] .. seg_ptr[r+1]-1 in order.
 struct RpaSchedule {
     const int *sched;
     const int *count;      // [lanes] entries of each lane
@@ -111,7 +111,7 @@ int vertex_flow_f64_blocks_per_sm(int nl);
 constexpr int kRpaSmemMaxInts = 8192;
 
 // Batched vertex flow: one persistent launch over the ragged work list of all flows of one
-// site class (spt = 1, 2 or 4 sites per lane).  Work item w belongs to flow list[f] with
+// vertex class (vertex_class below).  Work item w belongs to flow list[f] with
 // prefix[f] <= w < prefix[f+1] (prefix[f+1] - prefix[f] = that flow's triple count).
 // `warp_area` is the per-warp shared-memory bytes the largest flow of the list needs.
 // `sched_ints` > 0: each warp stages the RPA schedule of its current flow in shared memory
@@ -126,8 +126,12 @@ struct BatchVertexArgs {
 };
 size_t batch_vertex_warp_area(int nl, int n_seg, int npi);
 size_t batch_vertex_smem_bytes(int n_max, size_t warp_area, int sched_ints);
-int batch_vertex_blocks_per_sm(int spt, int npi, size_t smem);
-void launch_batch_vertex(const BatchVertexArgs &b, int spt, int npi, int grid, cudaStream_t stream);
+int batch_vertex_blocks_per_sm(int cls, int npi, size_t smem);
+void launch_batch_vertex(const BatchVertexArgs &b, int cls, int npi, int grid, cudaStream_t stream);
 int vertex_spt(int nl);  // sites per lane of a flow with nl sites
+// Vertex-kernel class of a flow (one kernel instance per class): 0-3 for nl <= 32 (outer-product
+// RPA with w = 8, 16, 24, 32), 4 for 2 sites per lane, 5 for 4.
+constexpr int kVertexClasses = 6;
+int vertex_class(int nl);
 
 }  // namespace spn

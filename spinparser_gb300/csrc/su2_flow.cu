@@ -382,9 +382,8 @@ spn_su2 *spn::create_flow(const spn_su2_desc *d, cudaStream_t stream) {
             cuda_check(cudaMemsetAsync(h->v2d, 0, h->n * sizeof(double), h->stream), "memset");
             cuda_check(cudaMemsetAsync(h->dv2d, 0, h->n * sizeof(double), h->stream), "memset");
             cuda_check(cudaMemsetAsync(h->status, 0, sizeof(unsigned), h->stream), "memset");
-            // balanced RPA schedule for the lanes of one node group
-            const int lanes = spt_for(h->nl) == 1 ? wsite_for(h->nl) : 32;
-            RpaHostSchedule rpa = build_rpa_schedule(h->nl, d->overlap_ptr, d->overlap_rid1, d->overlap_rid2, lanes);
+            // RPA schedule balanced over the 32 lanes of a warp
+            RpaHostSchedule rpa = build_rpa_schedule(h->nl, d->overlap_ptr, d->overlap_rid1, d->overlap_rid2, 32);
             h->rpa_lanes = rpa.lanes;
             h->rpa_n_seg = rpa.n_seg;
             h->rpa_len = rpa.len;

@@ -15,10 +15,17 @@
 //   phase B, lane = (node group, site): each group of W lanes (W = next power of two >= Nl)
 //            takes one node at a time, reads its descriptor (broadcast), gathers the four
 //            interpolated vertex slabs for its sites (coalesced: a slab is Nl contiguous
-//            floats) and forms K_X; the t channel's RPA lattice sum
-//            sum_i A[rid1_i] B[rid2_i] runs over a lane-balanced schedule of the merged pair
-//            list (no divergent per-rid loops) with deterministic segment partials.
-// Accumulation over nodes is Kahan-compensated FP32; group partials are combined by shuffles.
+//            floats) and forms K_X.
+// The t channel's RPA lattice sum sum_i A[rid1_i] B[rid2_i] (A, B: the third and fourth slab
+// of the node) is linear in the node, so for Nl <= 32 the warp first accumulates the matrix
+//   M = sum over the channel's nodes of (c A) x B        (Nl x Nl, spin and density)
+// in registers -- the 32 lanes own an 8 x 4 grid of blocks, updated with packed f32x2 FMAs
+// from a per-node shared-memory panel -- and then walks the merged pair list once per triple,
+// sum m M[rid1][rid2] per rid (every (rid1, rid2) occurs: the pair matrix is dense).  For
+// Nl > 32 each node walks the merged pair list itself.  Both walks follow a lane-balanced
+// schedule with deterministic segment partials (no divergent per-rid loops).
+// Accumulation over nodes is Kahan-compensated FP32 for the local terms (the RPA matrix sums
+// are plain FP32); group partials are combined by shuffles.
 #include "su2_common.cuh"
 #include "su2_device.cuh"
 
@@ -134,29 +141,30 @@ __device__ __forceinline__ void kahan_add(float &sum, float &comp, float v) {
     sum = t;
 }
 
-// Per-group shared-memory exchange area of the t channel: the (spin, density) values of the
-// third and fourth slab per site, then the RPA segment partials.
-//   Nl <= 16: interleaved float2 pairs A2, B2 (every element its own 8-byte bank pair), one
-//     64-bit load each;
-//   otherwise: separate 32-bit arrays As, Ad, Bs, Bd (every element its own bank for Nl <= 32).
-// With one site per lane the spin and density sums run as packed f32x2 arithmetic.
+// Per-group shared-memory exchange area of the t channel.
+//   Nl <= 32: the node's panel, A2[w] = c * (spin, density) of the third slab and B2[w] =
+//     (spin, density) of the fourth slab per site (w = rpa_outer_width(Nl)); the warp adds the
+//     outer products of the panels of a trip to its M accumulators;
+//   Nl > 32: separate 32-bit arrays As, Ad, Bs, Bd of the third and fourth slab, then the RPA
+//     segment partials of the node's own walk.
 struct TExchange {
     float *As, *Ad;  // [sites] spin / density of the third slab   (Nl > 32)
     float *Bs, *Bd;  // [sites] spin / density of the fourth slab  (Nl > 32)
-    float2 *A2, *B2;  // [sites] (spin, density) of the third / fourth slab (Nl <= 16)
-    float2 *slots;   // [n_seg] RPA segment partials
+    float2 *A2, *B2;  // [w] panel (Nl <= 32)
+    float2 *slots;   // [n_seg] RPA segment partials (Nl > 32)
     const int *sched, *count, *slot_base, *seg_ptr;  // RPA schedule (shared or global memory)
 };
 
-// Packed single-precision pairs (fma.rn.f32x2 / mul.rn.f32x2): per element the same IEEE
-// round-to-nearest results as fmaf and a * b.
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
-    float2 d;
-    asm("{\n\t.reg .b64 x, y, z;\n\tmov.b64 x, {%2, %3};\n\tmov.b64 y, {%4, %5};\n\t"
-        "mul.rn.f32x2 z, x, y;\n\tmov.b64 {%0, %1}, z;\n}"
-        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return d;
-}
+// Outer-product RPA accumulators of one lane (Nl <= 32): an MB x 2MB block of the
+// (8 MB) x (8 MB) matrix M, (spin, density) per element.  Lane l owns rows (l >> 2) * MB ...
+// and columns (l & 3) * 2MB ...
+template <int MB>
+struct OuterAcc {
+    float2 m[MB > 0 ? MB : 1][MB > 0 ? 2 * MB : 1];
+};
+
+// Packed single-precision pairs (fma.rn.f32x2): per element the same IEEE round-to-nearest
+// result as fmaf.
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
     float2 d;
     asm("{\n\t.reg .b64 x, y, z, w;\n\tmov.b64 x, {%2, %3};\n\tmov.b64 y, {%4, %5};\n\tmov.b64 z, {%6, %7};\n\t"
@@ -209,82 +217,18 @@ __device__ __forceinline__ void node_term(const FlowArgs &a, const NodeDesc *con
             }
         return;
     }
-    // t channel: RPA lattice sum (SU2FrgCore.cpp:249-266) over the balanced schedule; both
-    // forms accumulate acc += (A[rid1] * m) * B[rid2] per channel in schedule order
+    // t channel: RPA lattice sum (SU2FrgCore.cpp:249-266)
     if (SPT == 1) {
-        const bool pairs = a.nl <= 16;  // interleaved (spin, density) pairs, else separate arrays
+        // outer-product form: the node's panel (c * third slab, fourth slab); channel_sum adds
+        // the panels' outer products to the warp's M accumulators after the trip
         if (ln.valid[0]) {
             const int j = ln.j[0];
 #pragma unroll
             for (int n = 0; n < NPI; ++n) {
-                if (pairs) {
-                    tx[n].A2[j] = make_float2(S2[n][0], D2[n][0]);
-                    tx[n].B2[j] = make_float2(S3[n][0], D3[n][0]);
-                } else {
-                    tx[n].As[j] = S2[n][0];
-                    tx[n].Ad[j] = D2[n][0];
-                    tx[n].Bs[j] = S3[n][0];
-                    tx[n].Bd[j] = D3[n][0];
-                }
+                const float c = d[n]->c;
+                tx[n].A2[j] = make_float2(c * S2[n][0], c * D2[n][0]);
+                tx[n].B2[j] = make_float2(S3[n][0], D3[n][0]);
             }
-        }
-        __syncwarp();
-        const int lanes = a.rpa.lanes;
-        const int cnt = tx[0].count[jl];
-        int slot = tx[0].slot_base[jl];
-        float2 acc[NPI];
-#pragma unroll
-        for (int n = 0; n < NPI; ++n) acc[n] = make_float2(0.0f, 0.0f);
-        const int *sched = tx[0].sched + jl;
-        // exchanged (spin, density) values of entry e for node n
-        auto fetch = [&](int e, int n, float2 &av, float2 &bv) {
-            const unsigned oa = unsigned(e) & 0xffu, ob = (unsigned(e) >> 8) & 0xffu;  // byte offsets
-            if (pairs) {
-                av = *reinterpret_cast<const float2 *>(reinterpret_cast<const char *>(tx[n].A2) + oa);
-                bv = *reinterpret_cast<const float2 *>(reinterpret_cast<const char *>(tx[n].B2) + ob);
-            } else {
-                av.x = *reinterpret_cast<const float *>(reinterpret_cast<const char *>(tx[n].As) + oa);
-                av.y = *reinterpret_cast<const float *>(reinterpret_cast<const char *>(tx[n].Ad) + oa);
-                bv.x = *reinterpret_cast<const float *>(reinterpret_cast<const char *>(tx[n].Bs) + ob);
-                bv.y = *reinterpret_cast<const float *>(reinterpret_cast<const char *>(tx[n].Bd) + ob);
-            }
-        };
-        auto accumulate = [&](int e, const float2 *av, const float2 *bv) {
-            const float m = float((e >> 16) & 0xff);
-            const float2 m2 = make_float2(m, m);
-#pragma unroll
-            for (int n = 0; n < NPI; ++n) acc[n] = fma2(mul2(av[n], m2), bv[n], acc[n]);
-            if (e < 0) {  // last pair of a segment
-#pragma unroll
-                for (int n = 0; n < NPI; ++n) {
-                    tx[n].slots[slot] = acc[n];
-                    acc[n] = make_float2(0.0f, 0.0f);
-                }
-                ++slot;
-            }
-        };
-        // four entries at a time: their schedule words and values are loaded before the
-        // accumulations (which stay in schedule order), so the loads overlap
-        constexpr int kU = 4;
-        int i = 0;
-        for (; i + kU <= cnt; i += kU) {
-            int e[kU];
-            float2 av[kU][NPI], bv[kU][NPI];
-#pragma unroll
-            for (int u = 0; u < kU; ++u) e[u] = sched[(i + u) * lanes];
-#pragma unroll
-            for (int u = 0; u < kU; ++u)
-#pragma unroll
-                for (int n = 0; n < NPI; ++n) fetch(e[u], n, av[u][n], bv[u][n]);
-#pragma unroll
-            for (int u = 0; u < kU; ++u) accumulate(e[u], av[u], bv[u]);
-        }
-        for (; i < cnt; ++i) {
-            const int e = sched[i * lanes];
-            float2 av[NPI], bv[NPI];
-#pragma unroll
-            for (int n = 0; n < NPI; ++n) fetch(e, n, av[n], bv[n]);
-            accumulate(e, av, bv);
         }
     } else {
 #pragma unroll
@@ -325,8 +269,8 @@ __device__ __forceinline__ void node_term(const FlowArgs &a, const NodeDesc *con
                 ++slot;
             }
         }
+        __syncwarp();
     }
-    __syncwarp();
     const float s2 = 2.0f * a.spin, s8 = 8.0f * a.spin;
 #pragma unroll
     for (int n = 0; n < NPI; ++n) {
@@ -335,7 +279,7 @@ __device__ __forceinline__ void node_term(const FlowArgs &a, const NodeDesc *con
 #pragma unroll
         for (int k = 0; k < SPT; ++k) {
             float rpa_s = 0.0f, rpa_d = 0.0f;
-            if (ln.valid[k]) {
+            if (SPT != 1 && ln.valid[k]) {  // Nl <= 32: the RPA term enters once per triple
                 const int r = ln.j[k];
                 const int s0 = tx[0].seg_ptr[r], s1 = tx[0].seg_ptr[r + 1];
                 for (int q = s0; q < s1; ++q) {
@@ -366,12 +310,40 @@ __device__ __forceinline__ void node_term(const FlowArgs &a, const NodeDesc *con
             rd[n][k] = y;
         }
     }
-    __syncwarp();
+    if (SPT != 1) __syncwarp();
 }
 
-template <int CH, int SPT, int NPI>
+// Adds the outer products of the panels of nodes k = (r*NPI+n)*G+gg < nb (ascending k) to the
+// lane's block of M.  `pan`: the warp's first panel; panel (gg, n) starts pstride float2 later
+// per step of gg * NPI + n.
+template <int NPI, int MB>
+__device__ __forceinline__ void outer_update(const float2 *pan, int pstride, int lane, int r, int G, int nb,
+                                             OuterAcc<MB> &M) {
+    constexpr int W = 8 * MB;
+    const int rb = lane >> 2, cb = lane & 3;
+#pragma unroll
+    for (int n = 0; n < NPI; ++n)
+        for (int gg = 0; gg < G; ++gg) {
+            const int k = (r * NPI + n) * G + gg;
+            if (k >= nb) break;
+            const float2 *A = pan + (gg * NPI + n) * pstride + rb * MB;
+            const float2 *B = pan + (gg * NPI + n) * pstride + W + cb * 2 * MB;
+            float2 av[MB], bv[2 * MB];
+#pragma unroll
+            for (int i = 0; i < MB; ++i) av[i] = A[i];
+#pragma unroll
+            for (int j = 0; j < 2 * MB; ++j) bv[j] = B[j];
+#pragma unroll
+            for (int i = 0; i < MB; ++i)
+#pragma unroll
+                for (int j = 0; j < 2 * MB; ++j) M.m[i][j] = fma2(av[i], bv[j], M.m[i][j]);
+        }
+}
+
+template <int CH, int SPT, int NPI, int MB>
 __device__ __forceinline__ void channel_sum(const FlowArgs &a, const float *pos, const Transfer &f, int xi, int lane, int g,
                                             int G, int jl, const Lane<SPT> &ln, NodeDesc *desc, const TExchange *tx,
+                                            const float2 *pan, int pstride, OuterAcc<MB> &M,
                                             float *acc_s, float *cmp_s, float *acc_d, float *cmp_d) {
     const int cnt = __ldg(a.node_cnt + xi);
     const float *nwp = a.node_wp + size_t(xi) * a.max_nodes;
@@ -407,6 +379,11 @@ __device__ __forceinline__ void channel_sum(const FlowArgs &a, const float *pos,
                         kahan_add(acc_d[q], cmp_d[q], c * rd[n][q]);
                     }
                 }
+            if constexpr (CH == kT && SPT == 1) {
+                __syncwarp();  // panels written
+                outer_update<NPI, MB>(pan, pstride, lane, r, G, nb, M);
+                __syncwarp();  // panels read
+            }
         }
         __syncwarp();
     }
@@ -449,16 +426,25 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
 }
 
 // Shared memory of the single-flow kernel: frequency mesh; the RPA schedule when it is staged;
-// then per warp: 32 node descriptors and, per node group, NPI t-channel exchange areas (four
-// arrays of W*SPT sites and n_seg slots each).
-__host__ __device__ inline size_t node_area_bytes(int wsite, int spt, int n_seg) {
+// then per warp: 32 node descriptors and, per node group, NPI t-channel exchange areas (Nl <=
+// 32: a panel of 2 w float2; otherwise four arrays of W*SPT sites and n_seg slots).  For Nl <=
+// 32 the same warp area holds, between the t and the u channel, the matrix M (w x w float2)
+// and the n_seg segment partials of the pair walk.
+__host__ __device__ inline size_t node_area_bytes(int wsite, int spt, int n_seg, int w) {
+    if (spt == 1) return sizeof(float2) * 2 * size_t(w);  // w is a multiple of 8: 16-byte aligned
     return (sizeof(float) * 4 * size_t(wsite) * spt + sizeof(float2) * n_seg + 15) / 16 * 16;
 }
-__host__ __device__ inline size_t group_area_bytes(int wsite, int spt, int npi, int n_seg) {
-    return (32 / wsite) * npi * node_area_bytes(wsite, spt, n_seg);
+__host__ __device__ inline size_t group_area_bytes(int wsite, int spt, int npi, int n_seg, int w) {
+    return (32 / wsite) * npi * node_area_bytes(wsite, spt, n_seg, w);
 }
-__host__ __device__ inline size_t warp_bytes(int wsite, int spt, int npi, int n_seg) {
-    return kBatch * sizeof(NodeDesc) + group_area_bytes(wsite, spt, npi, n_seg);
+__host__ __device__ inline size_t outer_stage_bytes(int w, int n_seg) {
+    return (sizeof(float2) * (size_t(w) * w + n_seg) + 15) / 16 * 16;
+}
+__host__ __device__ inline size_t warp_bytes(int wsite, int spt, int npi, int n_seg, int w) {
+    const size_t main = kBatch * sizeof(NodeDesc) + group_area_bytes(wsite, spt, npi, n_seg, w);
+    if (spt != 1) return main;
+    const size_t st = outer_stage_bytes(w, n_seg);
+    return main > st ? main : st;
 }
 __host__ __device__ inline size_t sched_bytes(const RpaSchedule &r, int nl) {
     return r.in_smem ? (sizeof(int) * size_t(rpa_smem_ints(r, nl)) + 15) / 16 * 16 : 0;
@@ -473,10 +459,12 @@ struct WarpCtx {
     TExchange tx[NPI];
     Lane<SPT> ln;
     int W, G, g, jl;
+    float2 *panel;  // Nl <= 32: first t-channel panel of the warp
+    int pstride;    // float2 from one panel to the next
 };
 
 // `groups`: the warp's node-group areas; sched..seg_ptr: the RPA schedule (shared or global).
-template <int SPT, int NPI>
+template <int SPT, int NPI, int MB>
 __device__ __forceinline__ void setup_ctx(const FlowArgs &a, int lane, NodeDesc *desc, unsigned char *groups,
                                           const int *sched, const int *count, const int *slot_base, const int *seg_ptr,
                                           WarpCtx<SPT, NPI> &c) {
@@ -485,7 +473,15 @@ __device__ __forceinline__ void setup_ctx(const FlowArgs &a, int lane, NodeDesc 
     c.G = 32 / c.W;
     c.g = lane / c.W;
     c.jl = lane - c.g * c.W;
-    const size_t nab = node_area_bytes(c.W, SPT, a.rpa.n_seg);
+    const size_t nab = node_area_bytes(c.W, SPT, a.rpa.n_seg, 8 * MB);
+    c.panel = reinterpret_cast<float2 *>(groups);
+    c.pstride = int(nab / sizeof(float2));
+    if (SPT == 1) {  // panel entries of sites >= Nl stay zero
+        float4 *z = reinterpret_cast<float4 *>(groups);
+        const int n16 = int(c.G * NPI * nab / 16);
+        for (int i = lane; i < n16; i += 32) z[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        __syncwarp();
+    }
     unsigned char *gbase = groups + size_t(c.g) * NPI * nab;
     const int ws = c.W * SPT;
 #pragma unroll
@@ -495,8 +491,8 @@ __device__ __forceinline__ void setup_ctx(const FlowArgs &a, int lane, NodeDesc 
         c.tx[n].Ad = gx + ws;
         c.tx[n].Bs = gx + 2 * ws;
         c.tx[n].Bd = gx + 3 * ws;
-        c.tx[n].A2 = reinterpret_cast<float2 *>(gx);       // same bytes, used when Nl <= 16
-        c.tx[n].B2 = reinterpret_cast<float2 *>(gx) + ws;
+        c.tx[n].A2 = reinterpret_cast<float2 *>(gx);       // same bytes, used when Nl <= 32
+        c.tx[n].B2 = reinterpret_cast<float2 *>(gx) + 8 * MB;
         c.tx[n].slots = reinterpret_cast<float2 *>(gx + 4 * ws);
         c.tx[n].sched = sched;
         c.tx[n].count = count;
@@ -516,7 +512,68 @@ __device__ __forceinline__ void setup_ctx(const FlowArgs &a, int lane, NodeDesc 
 // The flow of triple `it` of flow `a` (all lanes of the warp take part).  The single-flow and
 // the batched kernel both evaluate triples with this function, so a flow's result does not
 // depend on the kernel, the launch or the other flows of a batch.
-template <int SPT, int NPI>
+// Nl <= 32, after the t channel: the lane's block of M goes to the warp area, the warp walks
+// the merged pair list once (segment partials after M), and group 0 adds its rid's sum
+// s2 * sum m M[rid1][rid2] (spin) and s8 * ... (density) to its accumulators.
+template <int SPT, int NPI, int MB>
+__device__ __forceinline__ void outer_gather(const FlowArgs &a, const WarpCtx<SPT, NPI> &c, int lane,
+                                             const OuterAcc<MB> &M, float *acc_s, float *cmp_s, float *acc_d,
+                                             float *cmp_d) {
+    constexpr int W = 8 * MB;
+    float2 *Ms = reinterpret_cast<float2 *>(c.desc);  // descriptors and panels are free here
+    float2 *slots = Ms + W * W;
+    const int rb = lane >> 2, cb = lane & 3;
+#pragma unroll
+    for (int i = 0; i < MB; ++i)
+#pragma unroll
+        for (int j = 0; j < 2 * MB; ++j) Ms[(rb * MB + i) * W + cb * 2 * MB + j] = M.m[i][j];
+    __syncwarp();
+    const int lanes = a.rpa.lanes;
+    const int cnt = c.tx[0].count[lane];
+    int slot = c.tx[0].slot_base[lane];
+    const int *sched = c.tx[0].sched + lane;
+    const char *mb = reinterpret_cast<const char *>(Ms);
+    float2 acc = make_float2(0.0f, 0.0f);
+    auto step = [&](int e, float2 v) {
+        const float m = float((e >> 16) & 0xff);
+        acc = fma2(make_float2(m, m), v, acc);
+        if (e < 0) {  // last pair of a segment
+            slots[slot++] = acc;
+            acc = make_float2(0.0f, 0.0f);
+        }
+    };
+    constexpr int kU = 4;
+    int i = 0;
+    for (; i + kU <= cnt; i += kU) {
+        int e[kU];
+        float2 v[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) e[u] = sched[(i + u) * lanes];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) v[u] = *reinterpret_cast<const float2 *>(mb + (e[u] & 0xffff));
+#pragma unroll
+        for (int u = 0; u < kU; ++u) step(e[u], v[u]);
+    }
+    for (; i < cnt; ++i) {
+        const int e = sched[i * lanes];
+        step(e, *reinterpret_cast<const float2 *>(mb + (e & 0xffff)));
+    }
+    __syncwarp();
+    if (c.g == 0 && c.ln.valid[0]) {
+        const int r = c.ln.j[0];
+        float os = 0.0f, od = 0.0f;
+        for (int q = c.tx[0].seg_ptr[r]; q < c.tx[0].seg_ptr[r + 1]; ++q) {
+            const float2 p = slots[q];
+            os += p.x;
+            od += p.y;
+        }
+        kahan_add(acc_s[0], cmp_s[0], (2.0f * a.spin) * os);  // SU2FrgCore.cpp:265-266
+        kahan_add(acc_d[0], cmp_d[0], (8.0f * a.spin) * od);
+    }
+    __syncwarp();
+}
+
+template <int SPT, int NPI, int MB>
 __device__ __forceinline__ void vertex_triple(const FlowArgs &a, const float *pos, int it, const WarpCtx<SPT, NPI> &c,
                                               int lane) {
     const float two_pi = 2.0f * float(kPi);
@@ -538,9 +595,18 @@ __device__ __forceinline__ void vertex_triple(const FlowArgs &a, const float *po
     float acc_s[SPT], cmp_s[SPT], acc_d[SPT], cmp_d[SPT];
 #pragma unroll
     for (int k = 0; k < SPT; ++k) acc_s[k] = cmp_s[k] = acc_d[k] = cmp_d[k] = 0.0f;
-    channel_sum<kS, SPT, NPI>(a, pos, f, si, lane, c.g, c.G, c.jl, c.ln, c.desc, c.tx, acc_s, cmp_s, acc_d, cmp_d);
-    channel_sum<kT, SPT, NPI>(a, pos, f, ti, lane, c.g, c.G, c.jl, c.ln, c.desc, c.tx, acc_s, cmp_s, acc_d, cmp_d);
-    channel_sum<kU, SPT, NPI>(a, pos, f, ui, lane, c.g, c.G, c.jl, c.ln, c.desc, c.tx, acc_s, cmp_s, acc_d, cmp_d);
+    OuterAcc<MB> M;
+#pragma unroll
+    for (int i = 0; i < (MB > 0 ? MB : 1); ++i)
+#pragma unroll
+        for (int j = 0; j < (MB > 0 ? 2 * MB : 1); ++j) M.m[i][j] = make_float2(0.0f, 0.0f);
+    channel_sum<kS, SPT, NPI, MB>(a, pos, f, si, lane, c.g, c.G, c.jl, c.ln, c.desc, c.tx, c.panel, c.pstride, M, acc_s,
+                                  cmp_s, acc_d, cmp_d);
+    channel_sum<kT, SPT, NPI, MB>(a, pos, f, ti, lane, c.g, c.G, c.jl, c.ln, c.desc, c.tx, c.panel, c.pstride, M, acc_s,
+                                  cmp_s, acc_d, cmp_d);
+    if constexpr (SPT == 1) outer_gather<SPT, NPI, MB>(a, c, lane, M, acc_s, cmp_s, acc_d, cmp_d);
+    channel_sum<kU, SPT, NPI, MB>(a, pos, f, ui, lane, c.g, c.G, c.jl, c.ln, c.desc, c.tx, c.panel, c.pstride, M, acc_s,
+                                  cmp_s, acc_d, cmp_d);
 
 #pragma unroll
     for (int k = 0; k < SPT; ++k) {
@@ -559,7 +625,7 @@ __device__ __forceinline__ void vertex_triple(const FlowArgs &a, const float *po
     }
 }
 
-template <int SPT, int NPI>
+template <int SPT, int NPI, int MB>
 __global__ void __launch_bounds__(kThreads) su2_vertex_flow_kernel(FlowArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ __align__(8) unsigned long long stage_bar;
@@ -602,10 +668,10 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_flow_kernel(FlowArgs a) {
         slot_base = a.rpa.slot_base;
         seg_ptr = a.rpa.seg_ptr;
     }
-    unsigned char *wbase = sbase + sched_bytes(a.rpa, a.nl) + warp * warp_bytes(W, SPT, NPI, n_seg);
+    unsigned char *wbase = sbase + sched_bytes(a.rpa, a.nl) + warp * warp_bytes(W, SPT, NPI, n_seg, 8 * MB);
     WarpCtx<SPT, NPI> c;
-    setup_ctx<SPT, NPI>(a, lane, reinterpret_cast<NodeDesc *>(wbase), wbase + kBatch * sizeof(NodeDesc), sched, count,
-                        slot_base, seg_ptr, c);
+    setup_ctx<SPT, NPI, MB>(a, lane, reinterpret_cast<NodeDesc *>(wbase), wbase + kBatch * sizeof(NodeDesc), sched, count,
+                            slot_base, seg_ptr, c);
     __syncthreads();
 
     for (;;) {
@@ -613,7 +679,7 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_flow_kernel(FlowArgs a) {
         if (lane == 0) it = atomicAdd(a.work_counter, 1);
         it = __shfl_sync(0xffffffffu, it, 0);
         if (it >= a.fn) break;
-        vertex_triple<SPT, NPI>(a, pos, it, c, lane);
+        vertex_triple<SPT, NPI, MB>(a, pos, it, c, lane);
     }
     // a copy that timed out must still land before the block's shared memory is released
     if (!staged && threadIdx.x == 0) mbar_wait(&stage_bar, 0);
@@ -624,7 +690,7 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_flow_kernel(FlowArgs a) {
 // mesh, lane roles) in its own shared-memory area and reloads it only when an item of another
 // flow comes up; items are numbered flow by flow, so that happens rarely.  The RPA schedule
 // is read from global memory (it differs between flows).
-template <int SPT, int NPI>
+template <int SPT, int NPI, int MB>
 __global__ void __launch_bounds__(kThreads) su2_vertex_batch_kernel(BatchVertexArgs b) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -672,15 +738,15 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_batch_kernel(BatchVertexA
                     sch[ns + nc + i] = __ldg(r.slot_base + i);
                 }
                 for (int i = lane; i <= fa->nl; i += 32) sch[ns + 2 * nc + i] = __ldg(r.seg_ptr + i);
-                setup_ctx<SPT, NPI>(*fa, lane, desc, groups, sch, sch + ns, sch + ns + nc, sch + ns + 2 * nc, c);
+                setup_ctx<SPT, NPI, MB>(*fa, lane, desc, groups, sch, sch + ns, sch + ns + nc, sch + ns + 2 * nc, c);
             } else {
-                setup_ctx<SPT, NPI>(*fa, lane, desc, groups, fa->rpa.sched, fa->rpa.count, fa->rpa.slot_base,
-                                    fa->rpa.seg_ptr, c);
+                setup_ctx<SPT, NPI, MB>(*fa, lane, desc, groups, fa->rpa.sched, fa->rpa.count, fa->rpa.slot_base,
+                                        fa->rpa.seg_ptr, c);
             }
             __syncwarp();
         }
         if (skip) continue;
-        vertex_triple<SPT, NPI>(*fa, pos, w - base, c, lane);
+        vertex_triple<SPT, NPI, MB>(*fa, pos, w - base, c, lane);
     }
 }
 
@@ -693,26 +759,42 @@ int wsite_of(int nl) {
     return w;
 }
 
+int outer_w_of(int nl) { return nl <= 32 ? rpa_outer_width(nl) : 0; }
+
 }  // namespace
+
+int vertex_class(int nl) {
+    if (nl > 32) return nl <= 64 ? 4 : 5;
+    return rpa_outer_width(nl) / 8 - 1;  // 0..3: outer-product blocks of 1..4 rows
+}
 
 size_t vertex_flow_smem_bytes(int nl, const RpaSchedule &rpa, int npi) {
     const int spt = spt_of(nl);
     return kMaxFreq * sizeof(float) + sched_bytes(rpa, nl) +
-           kWarps * warp_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, rpa.n_seg);
+           kWarps * warp_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, rpa.n_seg, outer_w_of(nl));
 }
 
 namespace {
 using VertexKernel = void (*)(FlowArgs);
-VertexKernel vertex_kernel(int spt, int npi) {
-    if (spt == 1) return npi == 1 ? su2_vertex_flow_kernel<1, 1> : su2_vertex_flow_kernel<1, 2>;
-    if (spt == 2) return npi == 1 ? su2_vertex_flow_kernel<2, 1> : su2_vertex_flow_kernel<2, 2>;
-    return npi == 1 ? su2_vertex_flow_kernel<4, 1> : su2_vertex_flow_kernel<4, 2>;
+template <int SPT, int MB>
+VertexKernel vertex_kernel_npi(int npi) {
+    return npi == 1 ? su2_vertex_flow_kernel<SPT, 1, MB> : su2_vertex_flow_kernel<SPT, 2, MB>;
+}
+VertexKernel vertex_kernel(int cls, int npi) {
+    switch (cls) {
+        case 0: return vertex_kernel_npi<1, 1>(npi);
+        case 1: return vertex_kernel_npi<1, 2>(npi);
+        case 2: return vertex_kernel_npi<1, 3>(npi);
+        case 3: return vertex_kernel_npi<1, 4>(npi);
+        case 4: return vertex_kernel_npi<2, 0>(npi);
+        default: return vertex_kernel_npi<4, 0>(npi);
+    }
 }
 }  // namespace
 
 int vertex_flow_blocks_per_sm(int nl, const RpaSchedule &rpa, int npi) {
     const size_t smem = vertex_flow_smem_bytes(nl, rpa, npi);
-    VertexKernel k = vertex_kernel(spt_of(nl), npi);
+    VertexKernel k = vertex_kernel(vertex_class(nl), npi);
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess) return -1;
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, smem) != cudaSuccess) return -1;
@@ -721,7 +803,7 @@ int vertex_flow_blocks_per_sm(int nl, const RpaSchedule &rpa, int npi) {
 
 void launch_vertex_flow(const FlowArgs &a, int npi, int grid, cudaStream_t stream) {
     const size_t smem = vertex_flow_smem_bytes(a.nl, a.rpa, npi);
-    VertexKernel k = vertex_kernel(spt_of(a.nl), npi);
+    VertexKernel k = vertex_kernel(vertex_class(a.nl), npi);
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     k<<<grid, kThreads, smem, stream>>>(a);
 }
@@ -730,7 +812,8 @@ int vertex_spt(int nl) { return spt_of(nl); }
 
 size_t batch_vertex_warp_area(int nl, int n_seg, int npi) {
     const int spt = spt_of(nl);
-    return group_area_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, n_seg);
+    // everything after the descriptors: the group areas, or the outer-product stage
+    return warp_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, n_seg, outer_w_of(nl)) - kBatch * sizeof(NodeDesc);
 }
 
 size_t batch_vertex_smem_bytes(int n_max, size_t warp_area, int sched_ints) {
@@ -740,15 +823,24 @@ size_t batch_vertex_smem_bytes(int n_max, size_t warp_area, int sched_ints) {
 
 namespace {
 using BatchKernel = void (*)(BatchVertexArgs);
-BatchKernel batch_kernel(int spt, int npi) {
-    if (spt == 1) return npi == 1 ? su2_vertex_batch_kernel<1, 1> : su2_vertex_batch_kernel<1, 2>;
-    if (spt == 2) return npi == 1 ? su2_vertex_batch_kernel<2, 1> : su2_vertex_batch_kernel<2, 2>;
-    return npi == 1 ? su2_vertex_batch_kernel<4, 1> : su2_vertex_batch_kernel<4, 2>;
+template <int SPT, int MB>
+BatchKernel batch_kernel_npi(int npi) {
+    return npi == 1 ? su2_vertex_batch_kernel<SPT, 1, MB> : su2_vertex_batch_kernel<SPT, 2, MB>;
+}
+BatchKernel batch_kernel(int cls, int npi) {
+    switch (cls) {
+        case 0: return batch_kernel_npi<1, 1>(npi);
+        case 1: return batch_kernel_npi<1, 2>(npi);
+        case 2: return batch_kernel_npi<1, 3>(npi);
+        case 3: return batch_kernel_npi<1, 4>(npi);
+        case 4: return batch_kernel_npi<2, 0>(npi);
+        default: return batch_kernel_npi<4, 0>(npi);
+    }
 }
 }  // namespace
 
-int batch_vertex_blocks_per_sm(int spt, int npi, size_t smem) {
-    BatchKernel k = batch_kernel(spt, npi);
+int batch_vertex_blocks_per_sm(int cls, int npi, size_t smem) {
+    BatchKernel k = batch_kernel(cls, npi);
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess) return -1;
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, smem) != cudaSuccess) return -1;
@@ -757,9 +849,9 @@ int batch_vertex_blocks_per_sm(int spt, int npi, size_t smem) {
 
 // The kernel's shared-memory limit is raised by batch_vertex_blocks_per_sm when the plan is
 // built, so this launch can be captured into a graph.
-void launch_batch_vertex(const BatchVertexArgs &b, int spt, int npi, int grid, cudaStream_t stream) {
+void launch_batch_vertex(const BatchVertexArgs &b, int cls, int npi, int grid, cudaStream_t stream) {
     const size_t smem = batch_vertex_smem_bytes(b.n_max, size_t(b.warp_area), b.sched_ints);
-    batch_kernel(spt, npi)<<<grid, kThreads, smem, stream>>>(b);
+    batch_kernel(cls, npi)<<<grid, kThreads, smem, stream>>>(b);
 }
 
 }  // namespace spn

@@ -26,7 +26,7 @@ def schedule(tab, lanes):
     lib = load_library()
     ip = C.POINTER(C.c_int)
     ptr, r1, r2 = (np.ascontiguousarray(x, np.int32) for x in (tab.overlap_ptr, tab.overlap_rid1, tab.overlap_rid2))
-    info = np.zeros(4, np.int32)
+    info = np.zeros(5, np.int32)
     args = (tab.n_sites, ptr.ctypes.data_as(ip), r1.ctypes.data_as(ip), r2.ctypes.data_as(ip), lanes)
     check(lib.spn_rpa_schedule(*args, info.ctypes.data_as(ip), None, None, None, None))
     sched = np.zeros(info[2], np.int32)
@@ -39,8 +39,9 @@ def schedule(tab, lanes):
 
 
 def decode(nl, lanes, info, sched, count, base, seg, A, B):
-    """The kernel's walk: per lane, accumulate (A[a] * m) * B[b], flush at segment ends."""
-    L, n_seg, packed = info[0], info[1], bool(info[3])
+    """The kernel's walk: per lane, accumulate m * M[a][b] (M = outer(A, B), Nl <= 32) or
+    (A[a] * m) * B[b] (Nl > 32), flush at segment ends."""
+    L, n_seg, packed, width = info[0], info[1], bool(info[3]), int(info[4])
     assert info[2] == L * lanes and packed == (nl <= 32)
     slots = np.zeros(n_seg)
     for l in range(lanes):
@@ -48,11 +49,13 @@ def decode(nl, lanes, info, sched, count, base, seg, A, B):
         acc, slot = 0.0, base[l]
         for i in range(count[l]):
             e = int(np.uint32(sched[i * lanes + l]))
-            if packed:  # byte offsets: float2 arrays up to 16 sites, float arrays above
-                scale = 8 if nl <= 16 else 4
-                oa, ob = e & 0xFF, (e >> 8) & 0xFF
-                assert oa % scale == 0 and ob % scale == 0
-                a, b, m, last = oa // scale, ob // scale, float((e >> 16) & 0xFF), bool(e >> 31)
+            if packed:  # byte offset of the float2 element M[a][b] of a width x width matrix
+                assert width >= nl and width % 8 == 0
+                off = e & 0xFFFF
+                assert off % 8 == 0 and off < width * width * 8
+                a, b = divmod(off // 8, width)
+                m, last = float((e >> 16) & 0xFF), bool(e >> 31)
+                assert (e >> 24) & 0x7F == 0
             else:
                 a, b, m, last = e & 0x7F, (e >> 7) & 0x7F, float((e >> 14) & 0xFF), bool(e & (1 << 22))
             assert a < nl and b < nl and m >= 1
@@ -74,7 +77,7 @@ def test_schedule_reproduces_rpa_sums(lat):
     A, B = rng.standard_normal(nl), rng.standard_normal(nl)
     ptr, r1, r2 = tab.overlap_ptr, tab.overlap_rid1, tab.overlap_rid2
     want = np.array([np.sum(A[r1[ptr[r]:ptr[r + 1]]] * B[r2[ptr[r]:ptr[r + 1]]]) for r in range(nl)])
-    lanes = (1 << max(0, (nl - 1).bit_length())) if nl <= 32 else 32
+    lanes = 32
     got = decode(nl, lanes, *schedule(tab, lanes), A, B)
     np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-12)
     # merging repeated pairs shortens the walk
