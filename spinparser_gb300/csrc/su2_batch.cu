@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(128) batch_corr_inner_kernel(const BatchFlow *
     if (f.phase == kPhaseDone) return;
     const CorrArgs c = batch_corr_args(f);
     if (int(blockIdx.x) >= 2 * c.n + 4) return;
-    corr_inner_body<SPT>(c, blockIdx.x);
+    corr_inner_body<SPT>(c, PairedState<float>{c.sd}, blockIdx.x);
 }
 
 __global__ void batch_corr_final_kernel(const BatchFlow *flows, const int *list) {
@@ -86,32 +86,17 @@ __global__ void batch_euler_kernel(const BatchFlow *flows, const int *list) {
     if (f.phase != kPhaseFlowing || (*f.a.status & (kStatusNaN | kStatusNodeOverflow))) return;
     const FlowArgs &a = f.a;
     const float step = __fsub_rn(f.cutoffs[f.step + 1], f.cutoffs[f.step]);
-    const long long vsz = (long long)a.fn * a.nl;
-    const long long n4 = vsz / 4;
+    // the (spin, density) state is one array of 2 F_N Nl floats (F_N Nl float2, 8-byte aligned)
+    const long long n2 = (long long)a.fn * a.nl;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    float4 *s4 = reinterpret_cast<float4 *>(const_cast<float *>(a.ss));
-    float4 *d4 = reinterpret_cast<float4 *>(const_cast<float *>(a.dd));
-    const float4 *ds4 = reinterpret_cast<const float4 *>(a.dss);
-    const float4 *dd4 = reinterpret_cast<const float4 *>(a.ddd);
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += stride) {
-        float4 v = s4[i], d = ds4[i];
+    float2 *x = const_cast<float2 *>(a.sd);
+    const float2 *dx = a.dsd;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n2; i += stride) {
+        float2 v = x[i];
+        const float2 d = dx[i];
         v.x = euler_update(v.x, d.x, step);
         v.y = euler_update(v.y, d.y, step);
-        v.z = euler_update(v.z, d.z, step);
-        v.w = euler_update(v.w, d.w, step);
-        s4[i] = v;
-        v = d4[i];
-        d = dd4[i];
-        v.x = euler_update(v.x, d.x, step);
-        v.y = euler_update(v.y, d.y, step);
-        v.z = euler_update(v.z, d.z, step);
-        v.w = euler_update(v.w, d.w, step);
-        d4[i] = v;
-    }
-    float *ss = const_cast<float *>(a.ss), *dd = const_cast<float *>(a.dd);
-    for (long long i = 4 * n4 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < vsz; i += stride) {
-        ss[i] = euler_update(ss[i], a.dss[i], step);
-        dd[i] = euler_update(dd[i], a.ddd[i], step);
+        x[i] = v;
     }
     if (blockIdx.x == 0) {
         float *v2 = const_cast<float *>(a.v2);
@@ -479,8 +464,8 @@ extern "C" int spn_batch_add(spn_batch *b, const spn_su2_desc *desc, int n_cutof
             cuda_check(cudaMemcpyAsync(f.cutoffs, cutoffs, n_cutoffs * sizeof(float), cudaMemcpyHostToDevice, b->stream), "H2D");
             const size_t vsz = size_t(f.h->fn) * f.h->nl;
             cuda_check(cudaMemcpyAsync(f.h->v2, v2, f.h->n * sizeof(float), cudaMemcpyHostToDevice, b->stream), "H2D");
-            cuda_check(cudaMemcpyAsync(f.h->ss, v4ss, vsz * sizeof(float), cudaMemcpyHostToDevice, b->stream), "H2D");
-            cuda_check(cudaMemcpyAsync(f.h->dd, v4dd, vsz * sizeof(float), cudaMemcpyHostToDevice, b->stream), "H2D");
+            // staged through the new flow's (still unused) flow buffer
+            upload_state(f.h, v4ss, v4dd, reinterpret_cast<float *>(f.h->dsd), b->stream);
             std::vector<double> v2d(v2, v2 + f.h->n);
             cuda_check(cudaMemcpyAsync(f.h->v2d, v2d.data(), f.h->n * sizeof(double), cudaMemcpyHostToDevice, b->stream), "H2D");
             f.h->cutoff = cutoffs[0];
@@ -628,8 +613,9 @@ extern "C" int spn_batch_get_state(spn_batch *b, int flow_id, float *cutoff, flo
         const size_t vsz = size_t(f.h->fn) * f.h->nl;
         if (cutoff) *cutoff = r.a.cutoff;
         if (v2) cuda_check(cudaMemcpy(v2, f.h->v2, f.h->n * sizeof(float), cudaMemcpyDeviceToHost), "D2H");
-        if (v4ss) cuda_check(cudaMemcpy(v4ss, f.h->ss, vsz * sizeof(float), cudaMemcpyDeviceToHost), "D2H");
-        if (v4dd) cuda_check(cudaMemcpy(v4dd, f.h->dd, vsz * sizeof(float), cudaMemcpyDeviceToHost), "D2H");
+        // staged through the flow buffer: between batch steps it holds nothing that is used again
+        download_state(f.h, f.h->sd, v4ss, v4dd, reinterpret_cast<float *>(f.h->dsd), b->stream);
+        cuda_check(cudaStreamSynchronize(b->stream), "batch get_state sync");
     });
 }
 

@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include "host/rpa_schedule.hpp"
+#include "su2_device.cuh"
 
 namespace spn {
 
@@ -36,13 +37,14 @@ __host__ __device__ inline int rpa_smem_ints(const RpaSchedule &r, int nl) {
 
 // Argument block of one flow in working precision T (float: the reference's types; double:
 // the FP64 flow, SPN_SU2_FP64).  The cutoff list is float in both (the task file's values).
+// Vertex arrays hold (spin, density) pairs per element, index ((s(s+1)/2+u)*N + t)*Nl + rid.
 template <class T>
 struct FlowArgsT {
     int n, nl, fn, wsite, max_nodes, n_range;
     float cutoff, spin;
     const T *freq;
-    const T *ss, *dd;      // state
-    T *dss, *ddd;          // flow
+    const dev::pair_t<T> *sd;  // state
+    dev::pair_t<T> *dsd;       // flow
     const T *v2;           // self-energy state
     T *dv2;                // self-energy flow
     const double *v2d;     // FP64 self-energy state (used when fp64_sigma)
@@ -57,13 +59,16 @@ struct FlowArgsT {
 };
 using FlowArgs = FlowArgsT<float>;
 
-// Correlation measurement (nu = 0) of one flow: the state it reads, the per-node partial
-// sums and the output zz[n_corr], dd[n_corr], chi_s[nl], chi_d[nl].
+// Correlation measurement (nu = 0) of one flow: the state it reads (sd, or the separate
+// arrays ss/dd of a caller of the allocation-free measurement), the per-node partial sums and
+// the output zz[n_corr], dd[n_corr], chi_s[nl], chi_d[nl].
 template <class T>
 struct CorrArgsT {
     int n, nl, n_corr;
     float cutoff, spin;
-    const T *freq, *ss, *dd, *v2;
+    const T *freq, *v2;
+    const dev::pair_t<T> *sd;
+    const T *ss, *dd;
     const double *v2d;  // FP64 self-energy, read instead of v2 when not NULL
     const int *sites, *inv_sites, *corr_rid;
     double *partial;  // [max_nodes][2][nl]

@@ -7,12 +7,51 @@
 // divisions).  The searches are binary searches over the ascending positive mesh with the
 // tie rules of the reference's linear scans (src/FrequencyDiscretization.hpp:253-356).
 #pragma once
+#include <cuda_runtime.h>
 #include <cstdint>
 
 namespace spn {
 namespace dev {
 
 constexpr int kMaxFreq = 256;  // largest supported N (positive frequencies)
+
+// (spin, density) pair of the working precision: the element type of a device vertex array.
+template <class T>
+struct pair_of;
+template <>
+struct pair_of<float> {
+    using type = float2;
+};
+template <>
+struct pair_of<double> {
+    using type = double2;
+};
+template <class T>
+using pair_t = typename pair_of<T>::type;
+
+// Read access to a vertex state by element index ((s(s+1)/2+u)*N + t)*Nl + rid.
+// PairedState: the device layout, (spin, density) interleaved per element;
+// SplitState: two separate arrays (the reference's layout, as callers of the allocation-free
+// measurement hold it).
+template <class T>
+struct PairedState {
+    const pair_t<T> *v;
+    __device__ __forceinline__ T spin(int i) const { return __ldg(reinterpret_cast<const T *>(v) + 2 * i); }
+    __device__ __forceinline__ T density(int i) const { return __ldg(reinterpret_cast<const T *>(v) + 2 * i + 1); }
+    __device__ __forceinline__ pair_t<T> both(int i) const { return __ldg(v + i); }
+};
+template <class T>
+struct SplitState {
+    const T *ss, *dd;
+    __device__ __forceinline__ T spin(int i) const { return __ldg(ss + i); }
+    __device__ __forceinline__ T density(int i) const { return __ldg(dd + i); }
+    __device__ __forceinline__ pair_t<T> both(int i) const {
+        pair_t<T> p;
+        p.x = __ldg(ss + i);
+        p.y = __ldg(dd + i);
+        return p;
+    }
+};
 
 // Single IEEE operations rounded to nearest in the working precision T (float: the
 // reference's types; double: the FP64 flow).
@@ -236,20 +275,23 @@ __device__ __forceinline__ void access8(const T *pos, int n, int nl, T s, T t, T
     slab(us, ut, uu, stepT, nl, ab.off[7], rn_mul(rn_mul(bt, bs), bu), ab.w[7], ab.sw[7]);
 }
 
-// SU2VertexTwoParticle::_directAccessMapFrequencyExchange for one site.
-template <class T>
-__device__ __forceinline__ T direct(const T *__restrict__ v, int si, int ti, int ui, int site, int stepT, int nl,
-                                    bool density) {
-    if (si >= ui) return v[(si * (si + 1) / 2 + ui) * stepT + ti * nl + site];
-    T x = v[(ui * (ui + 1) / 2 + si) * stepT + ti * nl + site];
-    return density ? -x : x;
+// SU2VertexTwoParticle::_directAccessMapFrequencyExchange for one site (density: the density
+// channel, whose sign flips when the stored sector swaps s and u; else the spin channel).
+template <class T, class S>
+__device__ __forceinline__ T direct(const S &v, int si, int ti, int ui, int site, int stepT, int nl, bool density) {
+    if (si >= ui) {
+        const int i = (si * (si + 1) / 2 + ui) * stepT + ti * nl + site;
+        return density ? v.density(i) : v.spin(i);
+    }
+    const int i = (ui * (ui + 1) / 2 + si) * stepT + ti * nl + site;
+    return density ? -v.density(i) : v.spin(i);
 }
 
 // getValue(i1, i2, s, t, u, symmetry, FrequencyChannel::None) where the site pair enters
 // through its rid (rid12) and the rid of the exchanged pair (rid21).
-template <class T>
-__device__ __forceinline__ T value_none(const T *pos, int n, int nl, const T *__restrict__ v, bool density, int rid12,
-                                        int rid21, T s, T t, T u) {
+template <class T, class S>
+__device__ __forceinline__ T value_none(const T *pos, int n, int nl, const S &v, bool density, int rid12, int rid21,
+                                        T s, T t, T u) {
     bool exch = fold(s, t, u);
     const int site = exch ? rid21 : rid12;
     const int stepT = n * nl;
@@ -258,7 +300,7 @@ __device__ __forceinline__ T value_none(const T *pos, int n, int nl, const T *__
     mesh_interp(pos, n, s, ls, us, bs);
     mesh_interp(pos, n, t, lt, ut, bt);
     mesh_interp(pos, n, u, lu, uu, bu);
-    auto D = [&](int a, int b, int c) { return direct(v, a, b, c, site, stepT, nl, density); };
+    auto D = [&](int a, int b, int c) { return direct<T>(v, a, b, c, site, stepT, nl, density); };
     return (1 - bu) * ((1 - bt) * ((1 - bs) * D(ls, lt, lu) + bs * D(us, lt, lu)) + bt * ((1 - bs) * D(ls, ut, lu) + bs * D(us, ut, lu))) +
            bu * ((1 - bt) * ((1 - bs) * D(ls, lt, uu) + bs * D(us, lt, uu)) + bt * ((1 - bs) * D(ls, ut, uu) + bs * D(us, ut, uu)));
 }

@@ -46,7 +46,15 @@ __global__ void __launch_bounds__(128) su2_self_energy_kernel(FlowArgs a) { self
 __global__ void su2_node_table_kernel(FlowArgs a) { node_table_body(a, blockIdx.x); }
 
 template <int SPT>
-__global__ void __launch_bounds__(128) su2_corr_inner_kernel(CorrArgs a) { corr_inner_body<SPT>(a, blockIdx.x); }
+__global__ void __launch_bounds__(128) su2_corr_inner_kernel(CorrArgs a) {
+    corr_inner_body<SPT>(a, PairedState<float>{a.sd}, blockIdx.x);
+}
+
+// the allocation-free measurement: the caller's separate spin and density arrays
+template <int SPT>
+__global__ void __launch_bounds__(128) su2_corr_inner_split_kernel(CorrArgs a) {
+    corr_inner_body<SPT>(a, SplitState<float>{a.ss, a.dd}, blockIdx.x);
+}
 
 __global__ void su2_corr_final_kernel(CorrArgs a) { corr_final_body(a); }
 
@@ -56,7 +64,9 @@ __global__ void __launch_bounds__(128) su2_self_energy_f64_kernel(FlowArgsT<doub
 __global__ void su2_node_table_f64_kernel(FlowArgsT<double> a) { node_table_body(a, blockIdx.x); }
 
 template <int SPT>
-__global__ void __launch_bounds__(128) su2_corr_inner_f64_kernel(CorrArgsT<double> a) { corr_inner_body<SPT>(a, blockIdx.x); }
+__global__ void __launch_bounds__(128) su2_corr_inner_f64_kernel(CorrArgsT<double> a) {
+    corr_inner_body<SPT>(a, PairedState<double>{a.sd}, blockIdx.x);
+}
 
 __global__ void su2_corr_final_f64_kernel(CorrArgsT<double> a) { corr_final_body(a); }
 
@@ -86,6 +96,20 @@ __global__ void su2_euler_f64_kernel(double *__restrict__ x, const double *__res
         const double v = euler_update_f64(x[i], dx[i], step);
         x[i] = v;
         xf[i] = float(v);
+    }
+}
+
+// State copies between the reference layout (two arrays: stage[0, n) spin, stage[n, 2n)
+// density) and the device layout ((spin, density) per element).
+__global__ void su2_pair_kernel(const float *__restrict__ stage, float2 *__restrict__ sd, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        sd[i] = make_float2(stage[i], stage[n + i]);
+}
+__global__ void su2_split_kernel(const float2 *__restrict__ sd, float *__restrict__ stage, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float2 v = sd[i];
+        stage[i] = v.x;
+        stage[n + i] = v.y;
     }
 }
 
@@ -154,6 +178,13 @@ void upload(T *dst, const T *src, size_t count, cudaStream_t s) {
     if (count) cuda_check(cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync H2D");
 }
 
+float *stage_of(spn_su2 *h) {
+    if (!h->stage) h->stage = dev_alloc<float>(2 * size_t(h->fn) * h->nl, "alloc state stage");
+    return h->stage;
+}
+
+int copy_grid(long long n) { return int(std::min<long long>((n + 255) / 256, 4096)); }
+
 void launch_vertex(spn_su2 *h) {
     if (h->fp64()) launch_vertex_flow_f64(h->args64(), h->vertex_grid, h->stream);
     else launch_vertex_flow(h->args(), h->vertex_npi, h->vertex_grid, h->stream);
@@ -175,10 +206,22 @@ void download_as_float(float *out, const double *src, size_t count, cudaStream_t
     for (size_t i = 0; i < count; ++i) out[i] = float(v[i]);
 }
 
-void upload_as_double(double *dst, const float *src, size_t count, cudaStream_t s) {
-    std::vector<double> v(src, src + count);
+// FP64 flows: (spin, density) pairs from / into separate host arrays (converted on the host).
+template <class S>
+void upload_pairs64(double2 *dst, const S *ss, const S *dd, size_t count, cudaStream_t s) {
+    std::vector<double2> v(count);
+    for (size_t i = 0; i < count; ++i) v[i] = make_double2(double(ss[i]), double(dd[i]));
     upload(dst, v.data(), count, s);
     cuda_check(cudaStreamSynchronize(s), "H2D sync");
+}
+template <class S>
+void download_pairs64(S *ss, S *dd, const double2 *src, size_t count, cudaStream_t s) {
+    if (!ss && !dd) return;
+    const std::vector<double2> v = download(src, count, s);
+    for (size_t i = 0; i < count; ++i) {
+        if (ss) ss[i] = S(v[i].x);
+        if (dd) dd[i] = S(v[i].y);
+    }
 }
 
 // Selects a vertex-flow variant: nodes per iteration and where the RPA schedule lives (all
@@ -329,31 +372,23 @@ spn_su2 *spn::create_flow(const spn_su2_desc *d, cudaStream_t stream) {
             h->dv2d = dev_alloc<double>(h->n, "alloc dv2 (fp64)");
             if (f64) {
                 h->freq64 = dev_alloc<double>(h->n, "alloc freq (fp64)");
-                h->ss64 = dev_alloc<double>(vsz, "alloc v4ss (fp64)");
-                h->dd64 = dev_alloc<double>(vsz, "alloc v4dd (fp64)");
-                h->dss64 = dev_alloc<double>(vsz, "alloc dv4ss (fp64)");
-                h->ddd64 = dev_alloc<double>(vsz, "alloc dv4dd (fp64)");
+                h->sd64 = dev_alloc<double2>(vsz, "alloc vertex state (fp64)");
+                h->dsd64 = dev_alloc<double2>(vsz, "alloc vertex flow (fp64)");
                 h->node_wp64 = dev_alloc<double>(size_t(h->n) * h->max_nodes, "alloc node table (fp64)");
                 h->node_c64 = dev_alloc<double>(size_t(h->n) * h->max_nodes, "alloc node table (fp64)");
                 h->corr_out64 = dev_alloc<double>(2 * size_t(h->n_corr) + 2 * h->nl, "alloc corr out (fp64)");
                 std::vector<double> f(d->freq, d->freq + h->n);
                 upload(h->freq64, f.data(), h->n, h->stream);
-                cuda_check(cudaMemsetAsync(h->ss64, 0, vsz * sizeof(double), h->stream), "memset");
-                cuda_check(cudaMemsetAsync(h->dd64, 0, vsz * sizeof(double), h->stream), "memset");
-                cuda_check(cudaMemsetAsync(h->dss64, 0, vsz * sizeof(double), h->stream), "memset");
-                cuda_check(cudaMemsetAsync(h->ddd64, 0, vsz * sizeof(double), h->stream), "memset");
+                cuda_check(cudaMemsetAsync(h->sd64, 0, vsz * sizeof(double2), h->stream), "memset");
+                cuda_check(cudaMemsetAsync(h->dsd64, 0, vsz * sizeof(double2), h->stream), "memset");
                 cuda_check(cudaStreamSynchronize(h->stream), "create sync");  // f leaves scope
             } else {
-                h->ss = dev_alloc<float>(vsz, "alloc v4ss");
-                h->dd = dev_alloc<float>(vsz, "alloc v4dd");
-                h->dss = dev_alloc<float>(vsz, "alloc dv4ss");
-                h->ddd = dev_alloc<float>(vsz, "alloc dv4dd");
+                h->sd = dev_alloc<float2>(vsz, "alloc vertex state");
+                h->dsd = dev_alloc<float2>(vsz, "alloc vertex flow");
                 h->node_wp = dev_alloc<float>(size_t(h->n) * h->max_nodes, "alloc node table");
                 h->node_c = dev_alloc<float>(size_t(h->n) * h->max_nodes, "alloc node table");
-                cuda_check(cudaMemsetAsync(h->ss, 0, vsz * sizeof(float), h->stream), "memset");
-                cuda_check(cudaMemsetAsync(h->dd, 0, vsz * sizeof(float), h->stream), "memset");
-                cuda_check(cudaMemsetAsync(h->dss, 0, vsz * sizeof(float), h->stream), "memset");
-                cuda_check(cudaMemsetAsync(h->ddd, 0, vsz * sizeof(float), h->stream), "memset");
+                cuda_check(cudaMemsetAsync(h->sd, 0, vsz * sizeof(float2), h->stream), "memset");
+                cuda_check(cudaMemsetAsync(h->dsd, 0, vsz * sizeof(float2), h->stream), "memset");
             }
             h->node_cnt = dev_alloc<int>(h->n, "alloc node counts");
             h->work_counter = dev_alloc<int>(1, "alloc work counter");
@@ -465,13 +500,8 @@ extern "C" int spn_su2_set_state(spn_su2 *h, float cutoff, const float *v2, cons
         cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
         const size_t vsz = size_t(h->fn) * h->nl;
         upload(h->v2, v2, h->n, h->stream);
-        if (h->fp64()) {
-            upload_as_double(h->ss64, v4ss, vsz, h->stream);
-            upload_as_double(h->dd64, v4dd, vsz, h->stream);
-        } else {
-            upload(h->ss, v4ss, vsz, h->stream);
-            upload(h->dd, v4dd, vsz, h->stream);
-        }
+        if (h->fp64()) upload_pairs64(h->sd64, v4ss, v4dd, vsz, h->stream);
+        else upload_state(h, v4ss, v4dd, stage_of(h), h->stream);
         std::vector<double> v2d(v2, v2 + h->n);  // the FP64 self-energy starts from the given values
         upload(h->v2d, v2d.data(), h->n, h->stream);
         h->cutoff = cutoff;
@@ -487,13 +517,11 @@ extern "C" int spn_su2_get_state(spn_su2 *h, float *cutoff, float *v2, float *v4
         if (cutoff) *cutoff = h->cutoff;
         if (h->fp64()) {
             download_as_float(v2, h->v2d, h->n, h->stream);
-            download_as_float(v4ss, h->ss64, vsz, h->stream);
-            download_as_float(v4dd, h->dd64, vsz, h->stream);
+            download_pairs64(v4ss, v4dd, h->sd64, vsz, h->stream);
             return;
         }
         if (v2) cuda_check(cudaMemcpyAsync(v2, h->v2, h->n * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
-        if (v4ss) cuda_check(cudaMemcpyAsync(v4ss, h->ss, vsz * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
-        if (v4dd) cuda_check(cudaMemcpyAsync(v4dd, h->dd, vsz * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        download_state(h, h->sd, v4ss, v4dd, stage_of(h), h->stream);
         cuda_check(cudaStreamSynchronize(h->stream), "get_state sync");
     });
 }
@@ -630,13 +658,11 @@ extern "C" int spn_su2_get_flow(spn_su2 *h, float *dv2, float *dv4ss, float *dv4
         const size_t vsz = size_t(h->fn) * h->nl;
         if (h->fp64()) {
             download_as_float(dv2, h->dv2d, h->n, h->stream);
-            download_as_float(dv4ss, h->dss64, vsz, h->stream);
-            download_as_float(dv4dd, h->ddd64, vsz, h->stream);
+            download_pairs64(dv4ss, dv4dd, h->dsd64, vsz, h->stream);
             return;
         }
         if (dv2) cuda_check(cudaMemcpyAsync(dv2, h->dv2, h->n * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
-        if (dv4ss) cuda_check(cudaMemcpyAsync(dv4ss, h->dss, vsz * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
-        if (dv4dd) cuda_check(cudaMemcpyAsync(dv4dd, h->ddd, vsz * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        download_state(h, h->dsd, dv4ss, dv4dd, stage_of(h), h->stream);
         cuda_check(cudaStreamSynchronize(h->stream), "get_flow sync");
     });
 }
@@ -649,10 +675,9 @@ extern "C" int spn_su2_finalize_step(spn_su2 *h, float new_cutoff) {
         const long long vsz = h->fn * h->nl;
         if (h->fp64()) {
             const double step64 = double(new_cutoff) - double(h->cutoff);
-            const int grid = int(std::min<long long>((vsz + 255) / 256, 4096));
             su2_euler_flow_f64_kernel<<<1, 64, 0, h->stream>>>(h->v2d, h->dv2d, h->n, step64);
-            su2_euler_flow_f64_kernel<<<grid, 256, 0, h->stream>>>(h->dd64, h->ddd64, vsz, step64);
-            su2_euler_flow_f64_kernel<<<grid, 256, 0, h->stream>>>(h->ss64, h->dss64, vsz, step64);
+            su2_euler_flow_f64_kernel<<<copy_grid(2 * vsz), 256, 0, h->stream>>>(
+                reinterpret_cast<double *>(h->sd64), reinterpret_cast<const double *>(h->dsd64), 2 * vsz, step64);
             cuda_check(cudaGetLastError(), "euler launch");
             h->cutoff = new_cutoff;
             return;
@@ -661,9 +686,10 @@ extern "C" int spn_su2_finalize_step(spn_su2 *h, float new_cutoff) {
             su2_euler_f64_kernel<<<1, 64, 0, h->stream>>>(h->v2d, h->dv2d, h->v2, h->n, step);
         else
             su2_euler_kernel<<<1, 64, 0, h->stream>>>(h->v2, h->dv2, h->n, step);
-        const int grid = int(std::min<long long>((vsz / 4 + 255) / 256 + 1, 4096));
-        su2_euler_kernel<<<grid, 256, 0, h->stream>>>(h->dd, h->ddd, vsz, step);
-        su2_euler_kernel<<<grid, 256, 0, h->stream>>>(h->ss, h->dss, vsz, step);
+        // the (spin, density) arrays are updated as one array of 2 F_N Nl floats
+        const int grid = int(std::min<long long>((2 * vsz / 4 + 255) / 256 + 1, 4096));
+        su2_euler_kernel<<<grid, 256, 0, h->stream>>>(reinterpret_cast<float *>(h->sd), reinterpret_cast<const float *>(h->dsd),
+                                                      2 * vsz, step);
         cuda_check(cudaGetLastError(), "euler launch");
         h->cutoff = new_cutoff;
     });
@@ -673,6 +699,23 @@ namespace {
 
 }  // namespace
 
+void spn::upload_state(spn_su2 *h, const float *v4ss, const float *v4dd, float *stage, cudaStream_t stream) {
+    const size_t vsz = size_t(h->fn) * h->nl;
+    upload(stage, v4ss, vsz, stream);
+    upload(stage + vsz, v4dd, vsz, stream);
+    su2_pair_kernel<<<copy_grid((long long)vsz), 256, 0, stream>>>(stage, h->sd, (long long)vsz);
+    cuda_check(cudaGetLastError(), "state pair launch");
+}
+
+void spn::download_state(const spn_su2 *h, const float2 *src, float *v4ss, float *v4dd, float *stage, cudaStream_t stream) {
+    if (!v4ss && !v4dd) return;
+    const size_t vsz = size_t(h->fn) * h->nl;
+    su2_split_kernel<<<copy_grid((long long)vsz), 256, 0, stream>>>(src, stage, (long long)vsz);
+    cuda_check(cudaGetLastError(), "state split launch");
+    if (v4ss) cuda_check(cudaMemcpyAsync(v4ss, stage, vsz * sizeof(float), cudaMemcpyDeviceToHost, stream), "D2H");
+    if (v4dd) cuda_check(cudaMemcpyAsync(v4dd, stage + vsz, vsz * sizeof(float), cudaMemcpyDeviceToHost, stream), "D2H");
+}
+
 CorrArgs spn::corr_args(const spn_su2 *h) {
         CorrArgs a;
         a.n = h->n;
@@ -681,8 +724,9 @@ CorrArgs spn::corr_args(const spn_su2 *h) {
         a.cutoff = h->cutoff;
         a.spin = h->spin;
         a.freq = h->freq;
-        a.ss = h->ss;
-        a.dd = h->dd;
+        a.sd = h->sd;
+        a.ss = nullptr;
+        a.dd = nullptr;
         a.v2 = h->v2;
         a.v2d = (h->flags & SPN_SU2_FP64_SELF_ENERGY) ? h->v2d : nullptr;
         a.sites = h->sites;
@@ -705,8 +749,9 @@ CorrArgsT<double> corr_args64(const spn_su2 *h) {
         a.cutoff = f.cutoff;
         a.spin = f.spin;
         a.freq = h->freq64;
-        a.ss = h->ss64;
-        a.dd = h->dd64;
+        a.sd = h->sd64;
+        a.ss = nullptr;
+        a.dd = nullptr;
         a.v2 = h->v2d;
         a.v2d = nullptr;
         a.sites = f.sites;
@@ -792,8 +837,7 @@ extern "C" int spn_su2_set_state_f64(spn_su2 *h, float cutoff, const double *v2,
         cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
         const size_t vsz = size_t(h->fn) * h->nl;
         upload(h->v2d, v2, h->n, h->stream);
-        upload(h->ss64, v4ss, vsz, h->stream);
-        upload(h->dd64, v4dd, vsz, h->stream);
+        upload_pairs64(h->sd64, v4ss, v4dd, vsz, h->stream);
         h->cutoff = cutoff;
         cuda_check(cudaStreamSynchronize(h->stream), "set_state sync");
     });
@@ -806,8 +850,7 @@ extern "C" int spn_su2_get_state_f64(spn_su2 *h, float *cutoff, double *v2, doub
         const size_t vsz = size_t(h->fn) * h->nl;
         if (cutoff) *cutoff = h->cutoff;
         if (v2) cuda_check(cudaMemcpyAsync(v2, h->v2d, h->n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H");
-        if (v4ss) cuda_check(cudaMemcpyAsync(v4ss, h->ss64, vsz * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H");
-        if (v4dd) cuda_check(cudaMemcpyAsync(v4dd, h->dd64, vsz * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        download_pairs64(v4ss, v4dd, h->sd64, vsz, h->stream);
         cuda_check(cudaStreamSynchronize(h->stream), "get_state sync");
     });
 }
@@ -818,8 +861,7 @@ extern "C" int spn_su2_get_flow_f64(spn_su2 *h, double *dv2, double *dv4ss, doub
         cuda_check(cudaSetDevice(h->device), "cudaSetDevice");
         const size_t vsz = size_t(h->fn) * h->nl;
         if (dv2) cuda_check(cudaMemcpyAsync(dv2, h->dv2d, h->n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H");
-        if (dv4ss) cuda_check(cudaMemcpyAsync(dv4ss, h->dss64, vsz * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H");
-        if (dv4dd) cuda_check(cudaMemcpyAsync(dv4dd, h->ddd64, vsz * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        download_pairs64(dv4ss, dv4dd, h->dsd64, vsz, h->stream);
         cuda_check(cudaStreamSynchronize(h->stream), "get_flow sync");
     });
 }
@@ -976,6 +1018,7 @@ extern "C" int spn_su2_correlation_noalloc(int n_freq, const float *freq, int n_
         a.cutoff = cutoff;
         a.spin = spin_length;
         a.freq = freq;
+        a.sd = nullptr;
         a.ss = v4ss;
         a.dd = v4dd;
         a.v2 = v2;
@@ -989,9 +1032,9 @@ extern "C" int spn_su2_correlation_noalloc(int n_freq, const float *freq, int n_
         cudaStream_t s = static_cast<cudaStream_t>(stream);
         const int spt = spt_for(n_sites);
         const int blocks = 2 * n_freq + 4;
-        if (spt == 1) su2_corr_inner_kernel<1><<<blocks, 128, 0, s>>>(a);
-        else if (spt == 2) su2_corr_inner_kernel<2><<<blocks, 128, 0, s>>>(a);
-        else su2_corr_inner_kernel<4><<<blocks, 128, 0, s>>>(a);
+        if (spt == 1) su2_corr_inner_split_kernel<1><<<blocks, 128, 0, s>>>(a);
+        else if (spt == 2) su2_corr_inner_split_kernel<2><<<blocks, 128, 0, s>>>(a);
+        else su2_corr_inner_split_kernel<4><<<blocks, 128, 0, s>>>(a);
         cuda_check(cudaGetLastError(), "correlation launch");
         su2_corr_final_kernel<<<1, 128, 2 * n_sites * sizeof(double), s>>>(a);
         cuda_check(cudaGetLastError(), "correlation final launch");

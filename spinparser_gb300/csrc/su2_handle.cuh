@@ -26,7 +26,9 @@ struct spn_su2 {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int vertex_grid = 0;
-    float *freq = nullptr, *ss = nullptr, *dd = nullptr, *dss = nullptr, *ddd = nullptr, *v2 = nullptr, *dv2 = nullptr;
+    float *freq = nullptr, *v2 = nullptr, *dv2 = nullptr;
+    float2 *sd = nullptr, *dsd = nullptr;  // vertex state and flow, (spin, density) per element
+    float *stage = nullptr;  // 2 F_N Nl floats for state copies in the reference layout (on first use)
     float *node_wp = nullptr, *node_c = nullptr, *corr_out = nullptr;
     int *node_cnt = nullptr, *work_counter = nullptr;
     unsigned *status = nullptr;
@@ -36,7 +38,8 @@ struct spn_su2 {
     double *v2d = nullptr, *dv2d = nullptr;  // FP64 self-energy (SPN_SU2_FP64_SELF_ENERGY)
     // FP64 flow (SPN_SU2_FP64): state, flow, node tables and measurement output in double;
     // the float arrays above other than v2/dv2 stay unallocated.
-    double *freq64 = nullptr, *ss64 = nullptr, *dd64 = nullptr, *dss64 = nullptr, *ddd64 = nullptr;
+    double *freq64 = nullptr;
+    double2 *sd64 = nullptr, *dsd64 = nullptr;
     double *node_wp64 = nullptr, *node_c64 = nullptr, *corr_out64 = nullptr;
     int *rpa_image = nullptr;  // sched | count | slot_base | seg_ptr in one allocation (the staged layout)
     int *rpa_sched = nullptr, *rpa_count = nullptr, *rpa_slot_base = nullptr, *rpa_seg_ptr = nullptr;  // into rpa_image
@@ -59,10 +62,8 @@ struct spn_su2 {
         a.cutoff = cutoff;
         a.spin = spin;
         a.freq = freq;
-        a.ss = ss;
-        a.dd = dd;
-        a.dss = dss;
-        a.ddd = ddd;
+        a.sd = sd;
+        a.dsd = dsd;
         a.v2 = v2;
         a.dv2 = dv2;
         a.v2d = v2d;
@@ -108,10 +109,8 @@ struct spn_su2 {
         a.cutoff = f.cutoff;
         a.spin = f.spin;
         a.freq = freq64;
-        a.ss = ss64;
-        a.dd = dd64;
-        a.dss = dss64;
-        a.ddd = ddd64;
+        a.sd = sd64;
+        a.dsd = dsd64;
         a.v2 = v2d;
         a.dv2 = dv2d;
         a.v2d = v2d;
@@ -144,11 +143,10 @@ struct spn_su2 {
         cudaSetDevice(device);
         for (auto e : ev_pool) cudaEventDestroy(e);
         ev_pool.clear();
-        void *ptrs[] = {freq,      ss,        dd,        dss,       ddd,          v2,          dv2,
-                        node_wp,   node_c,    corr_out,  node_cnt,  work_counter, status,      sites,
-                        inv_sites, ov_ptr,    ov_r1,     ov_r2,     range_rid,    range_inv,   corr_rid,
-                        corr_partial, rpa_image, v2d, dv2d, freq64, ss64, dd64, dss64, ddd64,
-                        node_wp64, node_c64, corr_out64};
+        void *ptrs[] = {freq,      sd,     dsd,       stage,     v2,           dv2,       node_wp,  node_c,
+                        corr_out,  node_cnt, work_counter, status, sites,     inv_sites,    ov_ptr,    ov_r1,
+                        ov_r2,     range_rid, range_inv, corr_rid, corr_partial, rpa_image, v2d,      dv2d,
+                        freq64,    sd64,   dsd64,     node_wp64, node_c64,  corr_out64};
         for (void *p : ptrs)
             if (p) cudaFree(p);
         if (own_stream && stream) cudaStreamDestroy(stream);
@@ -163,6 +161,12 @@ namespace spn {
 spn_su2 *create_flow(const spn_su2_desc *d, cudaStream_t stream);
 // Argument block of the correlation measurement of a flow at its current cutoff.
 CorrArgs corr_args(const spn_su2 *h);
+// State movement in the reference layout (separate spin and density arrays of F_N*Nl floats)
+// for an FP32 flow, through `stage` (2 F_N Nl device floats): the two halves are copied and
+// interleaved into the flow's state, or the state is split into them and copied out.  Queued
+// on `stream`; the host arrays must stay valid until it is synchronised.
+void upload_state(spn_su2 *h, const float *v4ss, const float *v4dd, float *stage, cudaStream_t stream);
+void download_state(const spn_su2 *h, const float2 *src, float *v4ss, float *v4dd, float *stage, cudaStream_t stream);
 // Builds the node tables and evaluates the vertex flow etc. of one flow: see su2_flow.cu.
 
 }  // namespace spn

@@ -24,11 +24,12 @@ __device__ __forceinline__ void self_energy_body(const FlowArgsT<T> &a, int blk)
     const int i = blk;
     const T w = pos[i], L = T(a.cutoff);
     const T wpl = w + L, wml = w - L;
+    const PairedState<T> st{a.sd};
     double part = 0.0;
     for (int j = threadIdx.x; j < a.n_range; j += blockDim.x) {
         const int r12 = a.range_rid[j], r21 = a.range_inv[j];
-        T x1 = value_none(pos, a.n, a.nl, a.dd, true, r12, r21, wpl, T(0), wml);
-        T x2 = value_none(pos, a.n, a.nl, a.dd, true, r12, r21, wml, T(0), wpl);
+        T x1 = value_none(pos, a.n, a.nl, st, true, r12, r21, wpl, T(0), wml);
+        T x2 = value_none(pos, a.n, a.nl, st, true, r12, r21, wml, T(0), wpl);
         part += double(x1) - double(x2);
     }
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
@@ -38,10 +39,10 @@ __device__ __forceinline__ void self_energy_body(const FlowArgsT<T> &a, int blk)
         double sum = 0.0;
         for (int k = 0; k < int(blockDim.x >> 5); ++k) sum += red[k];
         double val = -4.0 * double(a.spin) * sum;
-        val += 0.75 * (double(value_none(pos, a.n, a.nl, a.ss, false, 0, 0, wpl, wml, T(0))) -
-                       double(value_none(pos, a.n, a.nl, a.ss, false, 0, 0, wml, wpl, T(0))));
-        val += (double(value_none(pos, a.n, a.nl, a.dd, true, 0, 0, wpl, wml, T(0))) -
-                double(value_none(pos, a.n, a.nl, a.dd, true, 0, 0, wml, wpl, T(0))));
+        val += 0.75 * (double(value_none(pos, a.n, a.nl, st, false, 0, 0, wpl, wml, T(0))) -
+                       double(value_none(pos, a.n, a.nl, st, false, 0, 0, wml, wpl, T(0))));
+        val += (double(value_none(pos, a.n, a.nl, st, true, 0, 0, wpl, wml, T(0))) -
+                double(value_none(pos, a.n, a.nl, st, true, 0, 0, wml, wpl, T(0))));
         const double sig = a.fp64_sigma ? odd_interp(pos, a.n, a.v2d, L) : odd_interp(pos, a.n, a.v2, L);
         val /= (2.0 * kPiD * (double(L) + sig));
         T out = T(val);
@@ -130,8 +131,9 @@ __device__ inline int corr_nodes(const T *pos, int n, T cut, T *wp, double *w) {
 
 constexpr int kMaxCorrNodes = 2 * kMaxFreq + 8;
 
-template <int SPT, class T>
-__device__ __forceinline__ void corr_inner_body(const CorrArgsT<T> &a, int blk) {
+// `st`: the state (PairedState of a flow, or SplitState of an allocation-free call).
+template <int SPT, class T, class View>
+__device__ __forceinline__ void corr_inner_body(const CorrArgsT<T> &a, const View &st, int blk) {
     __shared__ T pos[kMaxFreq];
     __shared__ T nwp[kMaxCorrNodes];
     __shared__ double nw[kMaxCorrNodes];
@@ -168,17 +170,18 @@ __device__ __forceinline__ void corr_inner_body(const CorrArgsT<T> &a, int blk) 
         const T wp = nwp[b];
         AB8T<T> ab;
         access8(pos, a.n, nl, w + wp + T(0), T(0), w - wp, ab);
-        const T vs = value_none(pos, a.n, nl, a.ss, false, 0, 0, w + wp + T(0), w - wp, T(0));
-        const T vd = value_none(pos, a.n, nl, a.dd, true, 0, 0, w + wp + T(0), w - wp, T(0));
+        const T vs = value_none(pos, a.n, nl, st, false, 0, 0, w + wp + T(0), w - wp, T(0));
+        const T vd = value_none(pos, a.n, nl, st, true, 0, 0, w + wp + T(0), w - wp, T(0));
         const double dwp = double(wp) + sig(wp);
         const double norm = 1.0 / (dw * dw * dwp * dwp * (4.0 * kPiD * kPiD));
         const double cw = nw[b] * norm;
         for (int k = 0; k < SPT; ++k) {
-            const int st = ab.exch ? isite[k] : site[k];
+            const int site_k = ab.exch ? isite[k] : site[k];
             T gs = T(0), gd = T(0);
             for (int q = 0; q < 8; ++q) {
-                gs += ab.w[q] * __ldg(a.ss + ab.off[q] + st);
-                gd += ab.sw[q] * __ldg(a.dd + ab.off[q] + st);
+                const pair_t<T> p = st.both(ab.off[q] + site_k);
+                gs += ab.w[q] * p.x;
+                gd += ab.sw[q] * p.y;
             }
             double rs = -S * S * double(gs);
             double rd = -16.0 * S * S * double(gd);

@@ -41,8 +41,7 @@ constexpr double kPi = 3.14159265358979323846;
 
 struct __align__(16) NodeDesc {
     int4 off[4];
-    float4 w[4];
-    float4 sw[4];
+    float4 ws[4][2];  // per buffer: (w0, sw0, w1, sw1), (w2, sw2, w3, sw3): weight, sign * weight
     int exch;  // bit i: buffer i reads the site-exchanged pairs (inverted sites)
     float c;   // node coefficient, channel sign included
     float lv[8];  // t channel: site-local values cbs, cbd, icas, icad, cbs2, cbd2, icas2, icad2
@@ -60,21 +59,30 @@ struct Transfer {
     float s, t, u, w1p, w1, w2p, w2;
 };
 
-__device__ __forceinline__ void put_ab(NodeDesc &d, int i, const AB4 &ab) {
-    d.off[i] = make_int4(ab.off[0], ab.off[1], ab.off[2], ab.off[3]);
-    d.w[i] = make_float4(ab.w[0], ab.w[1], ab.w[2], ab.w[3]);
-    d.sw[i] = make_float4(ab.sw[0], ab.sw[1], ab.sw[2], ab.sw[3]);
+// Packed single-precision pairs (fma.rn.f32x2): per element the same IEEE round-to-nearest
+// result as fmaf.
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    float2 d;
+    asm("{\n\t.reg .b64 x, y, z, w;\n\tmov.b64 x, {%2, %3};\n\tmov.b64 y, {%4, %5};\n\tmov.b64 z, {%6, %7};\n\t"
+        "fma.rn.f32x2 w, x, y, z;\n\tmov.b64 {%0, %1}, w;\n}"
+        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
 }
 
+__device__ __forceinline__ void put_ab(NodeDesc &d, int i, const AB4 &ab) {
+    d.off[i] = make_int4(ab.off[0], ab.off[1], ab.off[2], ab.off[3]);
+    d.ws[i][0] = make_float4(ab.w[0], ab.sw[0], ab.w[1], ab.sw[1]);
+    d.ws[i][1] = make_float4(ab.w[2], ab.sw[2], ab.w[3], ab.sw[3]);
+}
+
+// Site-local (rid 0) (spin, density) value of an access buffer: spin sum w * ss, density sum
+// (sign * w) * dd, one packed FMA per support.
 __device__ __forceinline__ void local_pair(const FlowArgs &a, const AB4 &ab, float &vs, float &vd) {
-    float gs = 0.0f, gd = 0.0f;
+    float2 g = make_float2(0.0f, 0.0f);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        gs += ab.w[q] * __ldg(a.ss + ab.off[q]);
-        gd += ab.sw[q] * __ldg(a.dd + ab.off[q]);
-    }
-    vs = gs;
-    vd = gd;
+    for (int q = 0; q < 4; ++q) g = fma2(make_float2(ab.w[q], ab.sw[q]), __ldg(a.sd + ab.off[q]), g);
+    vs = g.x;
+    vd = g.y;
 }
 
 // Phase A: descriptor of one node (lane = node).
@@ -109,28 +117,24 @@ __device__ __forceinline__ void make_desc(const FlowArgs &a, const float *pos, c
     d.c = c;
 }
 
-// Phase B: interpolated slab of buffer i for this lane's sites (getValueSuperbundle).
+// Phase B: interpolated slab of buffer i for this lane's sites (getValueSuperbundle): per
+// support one 64-bit load of the (spin, density) element and one packed FMA.
 template <int SPT>
 __device__ __forceinline__ void gather(const FlowArgs &a, const NodeDesc &d, int i, const Lane<SPT> &ln, float *vs,
                                        float *vd) {
     const int4 o = d.off[i];
-    const float4 w = d.w[i];
-    const float4 sw = d.sw[i];
+    const float4 p0 = d.ws[i][0], p1 = d.ws[i][1];
     const bool ex = (d.exch >> i) & 1;
 #pragma unroll
     for (int k = 0; k < SPT; ++k) {
-        const int st = ex ? ln.isite[k] : ln.site[k];
-        float gs = 0.0f, gd = 0.0f;
-        gs += w.x * __ldg(a.ss + o.x + st);
-        gd += sw.x * __ldg(a.dd + o.x + st);
-        gs += w.y * __ldg(a.ss + o.y + st);
-        gd += sw.y * __ldg(a.dd + o.y + st);
-        gs += w.z * __ldg(a.ss + o.z + st);
-        gd += sw.z * __ldg(a.dd + o.z + st);
-        gs += w.w * __ldg(a.ss + o.w + st);
-        gd += sw.w * __ldg(a.dd + o.w + st);
-        vs[k] = gs;
-        vd[k] = gd;
+        const float2 *v = a.sd + (ex ? ln.isite[k] : ln.site[k]);
+        float2 g = make_float2(0.0f, 0.0f);
+        g = fma2(make_float2(p0.x, p0.y), __ldg(v + o.x), g);
+        g = fma2(make_float2(p0.z, p0.w), __ldg(v + o.y), g);
+        g = fma2(make_float2(p1.x, p1.y), __ldg(v + o.z), g);
+        g = fma2(make_float2(p1.z, p1.w), __ldg(v + o.w), g);
+        vs[k] = g.x;
+        vd[k] = g.y;
     }
 }
 
@@ -162,16 +166,6 @@ template <int MB>
 struct OuterAcc {
     float2 m[MB > 0 ? MB : 1][MB > 0 ? 2 * MB : 1];
 };
-
-// Packed single-precision pairs (fma.rn.f32x2): per element the same IEEE round-to-nearest
-// result as fmaf.
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
-    float2 d;
-    asm("{\n\t.reg .b64 x, y, z, w;\n\tmov.b64 x, {%2, %3};\n\tmov.b64 y, {%4, %5};\n\tmov.b64 z, {%6, %7};\n\t"
-        "fma.rn.f32x2 w, x, y, z;\n\tmov.b64 {%0, %1}, w;\n}"
-        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
-    return d;
-}
 
 // K_X at NPI nodes for this lane's sites (one group evaluates NPI nodes per iteration so that
 // the t channel decodes each RPA schedule entry once for all of them).
@@ -617,9 +611,7 @@ __device__ __forceinline__ void vertex_triple(const FlowArgs &a, const float *po
         }
         if (c.g == 0 && c.ln.valid[k]) {
             const float os = vs / two_pi, od = vd / two_pi;
-            const size_t idx = size_t(it) * a.nl + c.ln.j[k];
-            a.dss[idx] = os;
-            a.ddd[idx] = od;
+            a.dsd[size_t(it) * a.nl + c.ln.j[k]] = make_float2(os, od);
             if (isnan(os) || isnan(od)) atomicOr(a.status, kStatusNaN);
         }
     }

@@ -37,8 +37,9 @@ __device__ __forceinline__ void gather64(const FlowArgsT<double> &a, const AB4T<
             const int st = ab.exch ? isite[k] : site[k];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                gs += ab.w[q] * a.ss[ab.off[q] + st];
-                gd += ab.sw[q] * a.dd[ab.off[q] + st];
+                const double2 p = a.sd[ab.off[q] + st];
+                gs += ab.w[q] * p.x;
+                gd += ab.sw[q] * p.y;
             }
         }
         vs[k] = gs;
@@ -51,8 +52,9 @@ __device__ __forceinline__ void local64(const FlowArgsT<double> &a, const AB4T<d
     double gs = 0.0, gd = 0.0;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-        gs += ab.w[q] * a.ss[ab.off[q]];
-        gd += ab.sw[q] * a.dd[ab.off[q]];
+        const double2 p = a.sd[ab.off[q]];
+        gs += ab.w[q] * p.x;
+        gd += ab.sw[q] * p.y;
     }
     vs = gs;
     vd = gd;
@@ -221,9 +223,7 @@ __global__ void __launch_bounds__(kThreads64) su2_vertex_flow_f64_kernel(FlowArg
         for (int k = 0; k < kSitesPerLane64; ++k)
             if (valid[k]) {
                 const double os = acc_s[k] / (2.0 * kPi64), od = acc_d[k] / (2.0 * kPi64);
-                const size_t idx = size_t(it) * nl + jj[k];
-                a.dss[idx] = os;
-                a.ddd[idx] = od;
+                a.dsd[size_t(it) * nl + jj[k]] = make_double2(os, od);
                 if (isnan(os) || isnan(od)) atomicOr(a.status, kStatusNaN);
             }
     }
