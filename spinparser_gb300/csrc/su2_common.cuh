@@ -43,6 +43,9 @@ struct FlowArgsT {
     int n, nl, fn, wsite, max_nodes, n_range;
     float cutoff, spin;
     const T *freq;
+    const unsigned short *mesh_lo;  // bucket index of the mesh (dev::MeshIndex; FP32 flows)
+    unsigned mesh_base;
+    int mesh_shift;
     const dev::pair_t<T> *sd;  // state
     dev::pair_t<T> *dsd;       // flow
     const T *v2;           // self-energy state

@@ -115,6 +115,73 @@ __device__ __forceinline__ void mesh_interp(const T *pos, int n, T w, int &lo, i
     }
 }
 
+// Bucket index over the float bit patterns of the positive mesh (FP32 flows; built on the
+// host by build_mesh_index): bucket b covers the patterns [base + (b << shift), base +
+// (b+1 << shift)), and lo[b] is the first i >= 1 with pos[i] at or above the bucket's start.
+// Every i below lo[bucket(w)] has pos[i] < w, so the searches start there and finish with the
+// same comparisons as the binary searches above (identical results, NaN included); for a
+// mesh whose buckets hold at most a point or two that is one table read and a step or two.
+constexpr int kMeshBuckets = 512;
+
+struct MeshIndex {
+    const float *pos;
+    int n;
+    const unsigned short *lo;  // [kMeshBuckets]
+    unsigned base;
+    int shift;
+    __device__ __forceinline__ int start(float w) const {
+        const unsigned key = __float_as_uint(w);
+        unsigned b = key >= base ? (key - base) >> shift : 0u;
+        if (b >= unsigned(kMeshBuckets)) b = kMeshBuckets - 1;
+        return __ldg(lo + b);
+    }
+    __device__ __forceinline__ int first_greater(float w) const {  // as first_greater(pos, n, w)
+        int i = start(w);
+        while (i < n && !(pos[i] > w)) ++i;
+        return i;
+    }
+    __device__ __forceinline__ int first_geq(float w) const {  // as first_geq(pos, n, w)
+        int i = start(w);
+        while (i < n && !(pos[i] >= w)) ++i;
+        return i;
+    }
+};
+
+// The two mesh lookups an access buffer needs, by binary search (MeshSearch) or through a
+// bucket index (MeshIndex); w >= 0.
+template <class T>
+struct MeshSearch {
+    const T *pos;
+    int n;
+    __device__ __forceinline__ int first_greater(T w) const { return dev::first_greater(pos, n, w); }
+    __device__ __forceinline__ int first_geq(T w) const { return dev::first_geq(pos, n, w); }
+};
+
+template <class T, class M>
+__device__ __forceinline__ int mesh_offset_m(const M &m, T w) {
+    if (w <= m.pos[0]) return 0;
+    int i = m.first_geq(w);
+    return i < m.n ? i : m.n - 1;
+}
+
+template <class T, class M>
+__device__ __forceinline__ void mesh_interp_m(const M &m, T w, int &lo, int &hi, T &bias) {
+    if (w <= m.pos[0]) {
+        lo = hi = 0;
+        bias = T(0);
+        return;
+    }
+    int i = m.first_greater(w);
+    if (i < m.n) {
+        hi = i;
+        lo = i - 1;
+        bias = rn_div(rn_sub(w, m.pos[lo]), rn_sub(m.pos[hi], m.pos[lo]));
+    } else {
+        lo = hi = m.n - 1;
+        bias = T(0);
+    }
+}
+
 // Index into the symmetric mesh -w[n-1] .. -w[0], w[0] .. w[n-1] (0 .. 2n-1).
 template <class T>
 __device__ __forceinline__ T full_value(const T *pos, int n, int k) { return k < n ? -pos[n - 1 - k] : pos[k - n]; }
@@ -214,25 +281,25 @@ __device__ __forceinline__ bool fold(T &s, T &t, T &u) {
 enum Channel { kS = 0, kT = 1, kU = 2 };
 
 // generateAccessBuffer(s, t, u, channel) for channel in {S, T, U}
-// (src/SU2/SU2VertexTwoParticle.hpp:399-490).
-template <int CH, class T>
-__device__ __forceinline__ void access4(const T *pos, int n, int nl, T s, T t, T u, AB4T<T> &ab) {
+// (src/SU2/SU2VertexTwoParticle.hpp:399-490); `m` looks up the positive mesh.
+template <int CH, class T, class M>
+__device__ __forceinline__ void access4m(const M &m, int nl, T s, T t, T u, AB4T<T> &ab) {
     ab.exch = fold(s, t, u);
-    const int stepT = n * nl;
+    const int stepT = m.n * nl;
     int e, la, ua, lb, ub;
     T ba, bb;
     if (CH == kS) {
-        e = mesh_offset(pos, n, s);
-        mesh_interp(pos, n, t, la, ua, ba);
-        mesh_interp(pos, n, u, lb, ub, bb);
+        e = mesh_offset_m(m, s);
+        mesh_interp_m(m, t, la, ua, ba);
+        mesh_interp_m(m, u, lb, ub, bb);
     } else if (CH == kT) {
-        e = mesh_offset(pos, n, t);
-        mesh_interp(pos, n, s, la, ua, ba);
-        mesh_interp(pos, n, u, lb, ub, bb);
+        e = mesh_offset_m(m, t);
+        mesh_interp_m(m, s, la, ua, ba);
+        mesh_interp_m(m, u, lb, ub, bb);
     } else {
-        e = mesh_offset(pos, n, u);
-        mesh_interp(pos, n, s, la, ua, ba);
-        mesh_interp(pos, n, t, lb, ub, bb);
+        e = mesh_offset_m(m, u);
+        mesh_interp_m(m, s, la, ua, ba);
+        mesh_interp_m(m, t, lb, ub, bb);
     }
     const T na = rn_sub(T(1), ba), nb = rn_sub(T(1), bb);
     const T w0 = rn_mul(nb, na), w1 = rn_mul(nb, ba), w2 = rn_mul(bb, na), w3 = rn_mul(bb, ba);
@@ -252,6 +319,11 @@ __device__ __forceinline__ void access4(const T *pos, int n, int nl, T s, T t, T
         slab(la, ub, e, stepT, nl, ab.off[2], w2, ab.w[2], ab.sw[2]);
         slab(ua, ub, e, stepT, nl, ab.off[3], w3, ab.w[3], ab.sw[3]);
     }
+}
+
+template <int CH, class T>
+__device__ __forceinline__ void access4(const T *pos, int n, int nl, T s, T t, T u, AB4T<T> &ab) {
+    access4m<CH>(MeshSearch<T>{pos, n}, nl, s, t, u, ab);
 }
 
 // generateAccessBuffer(s, t, u): trilinear, eight supports (SU2VertexTwoParticle.hpp:500-557).

@@ -404,6 +404,27 @@ spn_su2 *spn::create_flow(const spn_su2_desc *d, cudaStream_t stream) {
             h->corr_partial = dev_alloc<double>(size_t(kMaxCorrNodes) * 2 * h->nl, "alloc corr scratch");
             if (!f64) h->corr_out = dev_alloc<float>(2 * size_t(h->n_corr) + 2 * h->nl, "alloc corr out");
             upload(h->freq, d->freq, h->n, h->stream);
+            // bucket index of the mesh (dev::MeshIndex): the smallest shift that puts the bit
+            // patterns of freq[0] .. freq[n-1] into kMeshBuckets buckets, and per bucket the
+            // first index >= 1 whose mesh value lies at or above the bucket's start
+            {
+                auto bits = [](float x) { unsigned u; std::memcpy(&u, &x, sizeof u); return u; };
+                const unsigned base = bits(d->freq[0]), span = bits(d->freq[h->n - 1]) - base;
+                int shift = 0;
+                while ((span >> shift) >= unsigned(kMeshBuckets)) ++shift;
+                std::vector<unsigned short> lo(kMeshBuckets);
+                int i = 0;
+                for (int b = 0; b < kMeshBuckets; ++b) {
+                    const unsigned long long start = (unsigned long long)base + ((unsigned long long)b << shift);
+                    while (i < h->n && (unsigned long long)bits(d->freq[i]) < start) ++i;
+                    lo[b] = (unsigned short)std::max(1, i);
+                }
+                h->mesh_lo = dev_alloc<unsigned short>(kMeshBuckets, "alloc mesh index");
+                upload(h->mesh_lo, lo.data(), kMeshBuckets, h->stream);
+                h->mesh_base = base;
+                h->mesh_shift = shift;
+                cuda_check(cudaStreamSynchronize(h->stream), "mesh index sync");  // lo leaves scope
+            }
             upload(h->sites, d->sites_rid, h->nl, h->stream);
             upload(h->inv_sites, d->inv_sites_rid, h->nl, h->stream);
             upload(h->ov_ptr, d->overlap_ptr, h->nl + 1, h->stream);

@@ -29,6 +29,9 @@ struct spn_su2 {
     float *freq = nullptr, *v2 = nullptr, *dv2 = nullptr;
     float2 *sd = nullptr, *dsd = nullptr;  // vertex state and flow, (spin, density) per element
     float *stage = nullptr;  // 2 F_N Nl floats for state copies in the reference layout (on first use)
+    unsigned short *mesh_lo = nullptr;  // bucket index of the frequency mesh
+    unsigned mesh_base = 0;
+    int mesh_shift = 0;
     float *node_wp = nullptr, *node_c = nullptr, *corr_out = nullptr;
     int *node_cnt = nullptr, *work_counter = nullptr;
     unsigned *status = nullptr;
@@ -62,6 +65,9 @@ struct spn_su2 {
         a.cutoff = cutoff;
         a.spin = spin;
         a.freq = freq;
+        a.mesh_lo = mesh_lo;
+        a.mesh_base = mesh_base;
+        a.mesh_shift = mesh_shift;
         a.sd = sd;
         a.dsd = dsd;
         a.v2 = v2;
@@ -109,6 +115,9 @@ struct spn_su2 {
         a.cutoff = f.cutoff;
         a.spin = f.spin;
         a.freq = freq64;
+        a.mesh_lo = mesh_lo;
+        a.mesh_base = mesh_base;
+        a.mesh_shift = mesh_shift;
         a.sd = sd64;
         a.dsd = dsd64;
         a.v2 = v2d;
@@ -146,7 +155,7 @@ struct spn_su2 {
         void *ptrs[] = {freq,      sd,     dsd,       stage,     v2,           dv2,       node_wp,  node_c,
                         corr_out,  node_cnt, work_counter, status, sites,     inv_sites,    ov_ptr,    ov_r1,
                         ov_r2,     range_rid, range_inv, corr_rid, corr_partial, rpa_image, v2d,      dv2d,
-                        freq64,    sd64,   dsd64,     node_wp64, node_c64,  corr_out64};
+                        freq64,    sd64,   dsd64,     node_wp64, node_c64,  corr_out64, mesh_lo};
         for (void *p : ptrs)
             if (p) cudaFree(p);
         if (own_stream && stream) cudaStreamDestroy(stream);

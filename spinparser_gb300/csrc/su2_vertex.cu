@@ -91,27 +91,28 @@ __device__ __forceinline__ void make_desc(const FlowArgs &a, const float *pos, c
                                           NodeDesc &d) {
     AB4 ab;
     int exch = 0;
-    const int n = a.n, nl = a.nl;
+    const int nl = a.nl;
+    const MeshIndex m{pos, a.n, a.mesh_lo, a.mesh_base, a.mesh_shift};
     if (CH == kS) {  // integralKernelS, SU2FrgCore.cpp:202-206
-        access4<kS>(pos, n, nl, f.s, -f.w1 - wp, -f.w2 - wp, ab); put_ab(d, 0, ab); exch |= ab.exch << 0;
-        access4<kS>(pos, n, nl, f.s, f.w1p + wp, -f.w2p - wp, ab); put_ab(d, 1, ab); exch |= ab.exch << 1;
-        access4<kS>(pos, n, nl, f.s, f.w2 + wp, f.w1 + wp, ab); put_ab(d, 2, ab); exch |= ab.exch << 2;
-        access4<kS>(pos, n, nl, f.s, -f.w2p - wp, f.w1p + wp, ab); put_ab(d, 3, ab); exch |= ab.exch << 3;
+        access4m<kS>(m, nl, f.s, -f.w1 - wp, -f.w2 - wp, ab); put_ab(d, 0, ab); exch |= ab.exch << 0;
+        access4m<kS>(m, nl, f.s, f.w1p + wp, -f.w2p - wp, ab); put_ab(d, 1, ab); exch |= ab.exch << 1;
+        access4m<kS>(m, nl, f.s, f.w2 + wp, f.w1 + wp, ab); put_ab(d, 2, ab); exch |= ab.exch << 2;
+        access4m<kS>(m, nl, f.s, -f.w2p - wp, f.w1p + wp, ab); put_ab(d, 3, ab); exch |= ab.exch << 3;
     } else if (CH == kT) {  // integralKernelT, SU2FrgCore.cpp:233-239, 269-284
-        access4<kT>(pos, n, nl, f.w1 - wp, f.t, f.w1p + wp, ab); put_ab(d, 0, ab); exch |= ab.exch << 0;
-        access4<kT>(pos, n, nl, f.w2p - wp, f.t, -f.w2 - wp, ab); put_ab(d, 1, ab); exch |= ab.exch << 1;
-        access4<kT>(pos, n, nl, f.w1p + wp, f.t, f.w1 - wp, ab); put_ab(d, 2, ab); exch |= ab.exch << 2;
-        access4<kT>(pos, n, nl, f.w2 + wp, f.t, wp - f.w2p, ab); put_ab(d, 3, ab); exch |= ab.exch << 3;
+        access4m<kT>(m, nl, f.w1 - wp, f.t, f.w1p + wp, ab); put_ab(d, 0, ab); exch |= ab.exch << 0;
+        access4m<kT>(m, nl, f.w2p - wp, f.t, -f.w2 - wp, ab); put_ab(d, 1, ab); exch |= ab.exch << 1;
+        access4m<kT>(m, nl, f.w1p + wp, f.t, f.w1 - wp, ab); put_ab(d, 2, ab); exch |= ab.exch << 2;
+        access4m<kT>(m, nl, f.w2 + wp, f.t, wp - f.w2p, ab); put_ab(d, 3, ab); exch |= ab.exch << 3;
         float v0, v1;
-        access4<kU>(pos, n, nl, f.w2p - wp, -f.w2 - wp, f.t, ab); local_pair(a, ab, v0, v1); d.lv[0] = v0; d.lv[1] = v1;
-        access4<kU>(pos, n, nl, f.w1 - wp, -f.w1p - wp, -f.t, ab); local_pair(a, ab, v0, v1); d.lv[2] = v0; d.lv[3] = v1;
-        access4<kU>(pos, n, nl, f.w2 + wp, wp - f.w2p, f.t, ab); local_pair(a, ab, v0, v1); d.lv[4] = v0; d.lv[5] = v1;
-        access4<kU>(pos, n, nl, f.w1p + wp, wp - f.w1, -f.t, ab); local_pair(a, ab, v0, v1); d.lv[6] = v0; d.lv[7] = v1;
+        access4m<kU>(m, nl, f.w2p - wp, -f.w2 - wp, f.t, ab); local_pair(a, ab, v0, v1); d.lv[0] = v0; d.lv[1] = v1;
+        access4m<kU>(m, nl, f.w1 - wp, -f.w1p - wp, -f.t, ab); local_pair(a, ab, v0, v1); d.lv[2] = v0; d.lv[3] = v1;
+        access4m<kU>(m, nl, f.w2 + wp, wp - f.w2p, f.t, ab); local_pair(a, ab, v0, v1); d.lv[4] = v0; d.lv[5] = v1;
+        access4m<kU>(m, nl, f.w1p + wp, wp - f.w1, -f.t, ab); local_pair(a, ab, v0, v1); d.lv[6] = v0; d.lv[7] = v1;
     } else {  // integralKernelU, SU2FrgCore.cpp:309-313
-        access4<kU>(pos, n, nl, f.w1 + wp, wp - f.w2p, f.u, ab); put_ab(d, 0, ab); exch |= ab.exch << 0;
-        access4<kU>(pos, n, nl, f.w1p + wp, f.w2 - wp, f.u, ab); put_ab(d, 1, ab); exch |= ab.exch << 1;
-        access4<kU>(pos, n, nl, f.w2p - wp, -f.w1 - wp, f.u, ab); put_ab(d, 2, ab); exch |= ab.exch << 2;
-        access4<kU>(pos, n, nl, f.w2 - wp, f.w1p + wp, f.u, ab); put_ab(d, 3, ab); exch |= ab.exch << 3;
+        access4m<kU>(m, nl, f.w1 + wp, wp - f.w2p, f.u, ab); put_ab(d, 0, ab); exch |= ab.exch << 0;
+        access4m<kU>(m, nl, f.w1p + wp, f.w2 - wp, f.u, ab); put_ab(d, 1, ab); exch |= ab.exch << 1;
+        access4m<kU>(m, nl, f.w2p - wp, -f.w1 - wp, f.u, ab); put_ab(d, 2, ab); exch |= ab.exch << 2;
+        access4m<kU>(m, nl, f.w2 - wp, f.w1p + wp, f.u, ab); put_ab(d, 3, ab); exch |= ab.exch << 3;
     }
     d.exch = exch;
     d.c = c;
