@@ -281,23 +281,25 @@ __device__ __forceinline__ bool fold(T &s, T &t, T &u) {
 enum Channel { kS = 0, kT = 1, kU = 2 };
 
 // generateAccessBuffer(s, t, u, channel) for channel in {S, T, U}
-// (src/SU2/SU2VertexTwoParticle.hpp:399-490); `m` looks up the positive mesh.
+// (src/SU2/SU2VertexTwoParticle.hpp:399-490); `m` looks up the positive mesh.  `e_known` >= 0:
+// the exact mesh index of the channel's own coordinate, which the caller knows when that
+// coordinate is (up to sign) a mesh value (offset(w_i) = i on a strictly ascending mesh).
 template <int CH, class T, class M>
-__device__ __forceinline__ void access4m(const M &m, int nl, T s, T t, T u, AB4T<T> &ab) {
+__device__ __forceinline__ void access4m(const M &m, int nl, T s, T t, T u, AB4T<T> &ab, int e_known = -1) {
     ab.exch = fold(s, t, u);
     const int stepT = m.n * nl;
     int e, la, ua, lb, ub;
     T ba, bb;
     if (CH == kS) {
-        e = mesh_offset_m(m, s);
+        e = e_known >= 0 ? e_known : mesh_offset_m(m, s);
         mesh_interp_m(m, t, la, ua, ba);
         mesh_interp_m(m, u, lb, ub, bb);
     } else if (CH == kT) {
-        e = mesh_offset_m(m, t);
+        e = e_known >= 0 ? e_known : mesh_offset_m(m, t);
         mesh_interp_m(m, s, la, ua, ba);
         mesh_interp_m(m, u, lb, ub, bb);
     } else {
-        e = mesh_offset_m(m, u);
+        e = e_known >= 0 ? e_known : mesh_offset_m(m, u);
         mesh_interp_m(m, s, la, ua, ba);
         mesh_interp_m(m, t, lb, ub, bb);
     }

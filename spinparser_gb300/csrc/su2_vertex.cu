@@ -57,6 +57,7 @@ struct Lane {
 
 struct Transfer {
     float s, t, u, w1p, w1, w2p, w2;
+    int si, ti, ui;  // mesh indices of s, t, u: the channel coordinate's offset in every buffer
 };
 
 // Packed single-precision pairs (fma.rn.f32x2): per element the same IEEE round-to-nearest
@@ -94,25 +95,25 @@ __device__ __forceinline__ void make_desc(const FlowArgs &a, const float *pos, c
     const int nl = a.nl;
     const MeshIndex m{pos, a.n, a.mesh_lo, a.mesh_base, a.mesh_shift};
     if (CH == kS) {  // integralKernelS, SU2FrgCore.cpp:202-206
-        access4m<kS>(m, nl, f.s, -f.w1 - wp, -f.w2 - wp, ab); put_ab(d, 0, ab); exch |= ab.exch << 0;
-        access4m<kS>(m, nl, f.s, f.w1p + wp, -f.w2p - wp, ab); put_ab(d, 1, ab); exch |= ab.exch << 1;
-        access4m<kS>(m, nl, f.s, f.w2 + wp, f.w1 + wp, ab); put_ab(d, 2, ab); exch |= ab.exch << 2;
-        access4m<kS>(m, nl, f.s, -f.w2p - wp, f.w1p + wp, ab); put_ab(d, 3, ab); exch |= ab.exch << 3;
+        access4m<kS>(m, nl, f.s, -f.w1 - wp, -f.w2 - wp, ab, f.si); put_ab(d, 0, ab); exch |= ab.exch << 0;
+        access4m<kS>(m, nl, f.s, f.w1p + wp, -f.w2p - wp, ab, f.si); put_ab(d, 1, ab); exch |= ab.exch << 1;
+        access4m<kS>(m, nl, f.s, f.w2 + wp, f.w1 + wp, ab, f.si); put_ab(d, 2, ab); exch |= ab.exch << 2;
+        access4m<kS>(m, nl, f.s, -f.w2p - wp, f.w1p + wp, ab, f.si); put_ab(d, 3, ab); exch |= ab.exch << 3;
     } else if (CH == kT) {  // integralKernelT, SU2FrgCore.cpp:233-239, 269-284
-        access4m<kT>(m, nl, f.w1 - wp, f.t, f.w1p + wp, ab); put_ab(d, 0, ab); exch |= ab.exch << 0;
-        access4m<kT>(m, nl, f.w2p - wp, f.t, -f.w2 - wp, ab); put_ab(d, 1, ab); exch |= ab.exch << 1;
-        access4m<kT>(m, nl, f.w1p + wp, f.t, f.w1 - wp, ab); put_ab(d, 2, ab); exch |= ab.exch << 2;
-        access4m<kT>(m, nl, f.w2 + wp, f.t, wp - f.w2p, ab); put_ab(d, 3, ab); exch |= ab.exch << 3;
+        access4m<kT>(m, nl, f.w1 - wp, f.t, f.w1p + wp, ab, f.ti); put_ab(d, 0, ab); exch |= ab.exch << 0;
+        access4m<kT>(m, nl, f.w2p - wp, f.t, -f.w2 - wp, ab, f.ti); put_ab(d, 1, ab); exch |= ab.exch << 1;
+        access4m<kT>(m, nl, f.w1p + wp, f.t, f.w1 - wp, ab, f.ti); put_ab(d, 2, ab); exch |= ab.exch << 2;
+        access4m<kT>(m, nl, f.w2 + wp, f.t, wp - f.w2p, ab, f.ti); put_ab(d, 3, ab); exch |= ab.exch << 3;
         float v0, v1;
-        access4m<kU>(m, nl, f.w2p - wp, -f.w2 - wp, f.t, ab); local_pair(a, ab, v0, v1); d.lv[0] = v0; d.lv[1] = v1;
-        access4m<kU>(m, nl, f.w1 - wp, -f.w1p - wp, -f.t, ab); local_pair(a, ab, v0, v1); d.lv[2] = v0; d.lv[3] = v1;
-        access4m<kU>(m, nl, f.w2 + wp, wp - f.w2p, f.t, ab); local_pair(a, ab, v0, v1); d.lv[4] = v0; d.lv[5] = v1;
-        access4m<kU>(m, nl, f.w1p + wp, wp - f.w1, -f.t, ab); local_pair(a, ab, v0, v1); d.lv[6] = v0; d.lv[7] = v1;
+        access4m<kU>(m, nl, f.w2p - wp, -f.w2 - wp, f.t, ab, f.ti); local_pair(a, ab, v0, v1); d.lv[0] = v0; d.lv[1] = v1;
+        access4m<kU>(m, nl, f.w1 - wp, -f.w1p - wp, -f.t, ab, f.ti); local_pair(a, ab, v0, v1); d.lv[2] = v0; d.lv[3] = v1;
+        access4m<kU>(m, nl, f.w2 + wp, wp - f.w2p, f.t, ab, f.ti); local_pair(a, ab, v0, v1); d.lv[4] = v0; d.lv[5] = v1;
+        access4m<kU>(m, nl, f.w1p + wp, wp - f.w1, -f.t, ab, f.ti); local_pair(a, ab, v0, v1); d.lv[6] = v0; d.lv[7] = v1;
     } else {  // integralKernelU, SU2FrgCore.cpp:309-313
-        access4m<kU>(m, nl, f.w1 + wp, wp - f.w2p, f.u, ab); put_ab(d, 0, ab); exch |= ab.exch << 0;
-        access4m<kU>(m, nl, f.w1p + wp, f.w2 - wp, f.u, ab); put_ab(d, 1, ab); exch |= ab.exch << 1;
-        access4m<kU>(m, nl, f.w2p - wp, -f.w1 - wp, f.u, ab); put_ab(d, 2, ab); exch |= ab.exch << 2;
-        access4m<kU>(m, nl, f.w2 - wp, f.w1p + wp, f.u, ab); put_ab(d, 3, ab); exch |= ab.exch << 3;
+        access4m<kU>(m, nl, f.w1 + wp, wp - f.w2p, f.u, ab, f.ui); put_ab(d, 0, ab); exch |= ab.exch << 0;
+        access4m<kU>(m, nl, f.w1p + wp, f.w2 - wp, f.u, ab, f.ui); put_ab(d, 1, ab); exch |= ab.exch << 1;
+        access4m<kU>(m, nl, f.w2p - wp, -f.w1 - wp, f.u, ab, f.ui); put_ab(d, 2, ab); exch |= ab.exch << 2;
+        access4m<kU>(m, nl, f.w2 - wp, f.w1p + wp, f.u, ab, f.ui); put_ab(d, 3, ab); exch |= ab.exch << 3;
     }
     d.exch = exch;
     d.c = c;
@@ -586,6 +587,9 @@ __device__ __forceinline__ void vertex_triple(const FlowArgs &a, const float *po
     f.w1 = 0.5f * (f.s - f.t + f.u);
     f.w2p = 0.5f * (f.s - f.t - f.u);
     f.w2 = 0.5f * (f.s + f.t - f.u);
+    f.si = si;
+    f.ti = ti;
+    f.ui = ui;
 
     float acc_s[SPT], cmp_s[SPT], acc_d[SPT], cmp_d[SPT];
 #pragma unroll
