@@ -90,6 +90,17 @@ int spn_lattice_get_tables(const spn_lattice *lat, int *sites_rid, int *inv_site
                            int *overlap_rid1, int *overlap_rid2, int *range_rid, int *range_inv_rid, int *corr_rid,
                            double *site_pos, double *basis_pos, double *lattice_vectors);
 
+/* Spin permutations of the same tables, for cores without SU(2) symmetry (XYZ): each entry is
+ * an index p into the permutations (X,Y,Z) (X,Z,Y) (Y,X,Z) (Y,Z,X) (Z,X,Y) (Z,Y,X); component c
+ * (0 = X, 1 = Y, 2 = Z) of a pair is component perm[p][c] of its representative
+ * (LatticeSiteDescriptor::spinPermutation, src/Lattice.hpp:36-44, built in
+ * LatticeModelFactory.cpp:833-870).  Arrays as in spn_lattice_get_tables: sites_perm and
+ * inv_sites_perm [Nl], overlap_perm1 / overlap_perm2 [overlap_ptr[Nl]] (the pairs (0,j) and
+ * (j,rid)), range_perm / range_inv_perm [n_range], corr_perm [n_basis * n_range].  For a model
+ * whose couplings need no spin permutation every entry is 0. */
+int spn_lattice_get_spin_tables(const spn_lattice *lat, int *sites_perm, int *inv_sites_perm, int *overlap_perm1,
+                                int *overlap_perm2, int *range_perm, int *range_inv_perm, int *corr_perm);
+
 /* All stored sites (Lattice::getSiteParameters, src/Lattice.hpp:397): site_params[4*i..] =
  * (a0, a1, a2, basis) of site id i, i < n_sites_total; and, if pair_rid is not NULL, the
  * full symmetry table pair_rid[i1*n_sites_total + i2] = symmetryTransform(i1, i2)

@@ -153,3 +153,108 @@ class Oracle:
                _p(cd, ct), threads)
         assert n > 0
         return n, cs, cd, (v2, ss, dd)
+
+
+# ---------------------------------------------------------------------------------------
+# XYZ core (oracle/xyz_oracle.cpp): models with diagonal couplings (Kitaev, XXZ, ...)
+# ---------------------------------------------------------------------------------------
+class XyzOracleDesc(C.Structure):
+    _fields_ = [
+        ("n_freq", C.c_int), ("freq", C.POINTER(C.c_float)), ("n_sites", C.c_int),
+        ("sites_rid", C.POINTER(C.c_int)), ("sites_perm", C.POINTER(C.c_int)),
+        ("inv_sites_rid", C.POINTER(C.c_int)), ("inv_sites_perm", C.POINTER(C.c_int)),
+        ("overlap_ptr", C.POINTER(C.c_int)), ("overlap_rid1", C.POINTER(C.c_int)),
+        ("overlap_rid2", C.POINTER(C.c_int)), ("overlap_perm1", C.POINTER(C.c_int)),
+        ("overlap_perm2", C.POINTER(C.c_int)), ("n_range", C.c_int), ("range_rid", C.POINTER(C.c_int)),
+        ("range_inv_rid", C.POINTER(C.c_int)),
+    ]
+
+
+SPIN_PERMUTATIONS = np.array([[0, 1, 2], [0, 2, 1], [1, 0, 2], [1, 2, 0], [2, 0, 1], [2, 1, 0]], np.int32)
+
+
+def xyz_initial_state(tables, n_freq: int, normalization: float = 1.0):
+    """XYZEffectiveAction initial condition (src/XYZ/XYZEffectiveAction.hpp:38-60):
+    v4[c][it*Nl + rid] += 0.25 J^cc(rid) / normalization for c = X, Y, Z; density and
+    self-energy zero."""
+    fn = n_freq * n_freq * (n_freq + 1) // 2
+    v2 = np.zeros(n_freq, np.float32)
+    v4 = np.zeros((4, fn, tables.n_sites), np.float32)
+    for rid, J in zip(tables.interaction_rid, tables.interaction_J):
+        for c in range(3):
+            v4[c, :, rid] += (np.float32(0.25) * np.float32(J[c, c])) / np.float32(normalization)
+    return v2, v4.reshape(4, -1)
+
+
+def xyz_scatter(chi, tables, spin):
+    """Correlations per (basis, site in range) of chi[4][Nl] (XYZMeasurementCorrelation.cpp:
+    166-184): component c of entry (b, j) reads component perm[c] of its representative."""
+    rid = tables.corr_rid.reshape(tables.n_basis, tables.n_range)
+    perm = spin.corr_perm.reshape(tables.n_basis, tables.n_range)
+    out = np.empty((4, tables.n_basis, tables.n_range), chi.dtype)
+    for c in range(3):
+        out[c] = chi[SPIN_PERMUTATIONS[perm, c], rid]
+    out[3] = chi[3, rid]
+    return out
+
+
+class XyzOracle:
+    """CPU restatement of the reference XYZ core for one lattice + frequency mesh."""
+
+    def __init__(self, tables, spin, freq):
+        lib = _lib()
+        self.lib = lib
+        fp, i4 = C.POINTER(C.c_float), C.c_int
+        pp = C.POINTER(C.POINTER(C.c_float))
+        dsc = C.POINTER(XyzOracleDesc)
+        lib.oracle_xyz_rhs_f32.argtypes = [dsc, C.c_float, fp, pp, fp, pp, i4]
+        lib.oracle_xyz_correlation_f32.argtypes = [dsc, C.c_float, fp, pp, pp]
+        lib.oracle_xyz_flow_f32.argtypes = [dsc, fp, i4, fp, pp, pp, i4]
+        self.freq = np.ascontiguousarray(freq, np.float32)
+        self.n = len(self.freq)
+        self.nl = int(tables.n_sites)
+        self.fn = self.n * self.n * (self.n + 1) // 2
+        arrs = [tables.sites_rid, spin.sites_perm, tables.inv_sites_rid, spin.inv_sites_perm, tables.overlap_ptr,
+                tables.overlap_rid1, tables.overlap_rid2, spin.overlap_perm1, spin.overlap_perm2, tables.range_rid,
+                tables.range_inv_rid]
+        self._keep = [np.ascontiguousarray(a, np.int32) for a in arrs]
+        k = [_p(a, C.c_int) for a in self._keep]
+        d = XyzOracleDesc()
+        d.n_freq, d.freq, d.n_sites = self.n, _p(self.freq, C.c_float), self.nl
+        (d.sites_rid, d.sites_perm, d.inv_sites_rid, d.inv_sites_perm, d.overlap_ptr, d.overlap_rid1, d.overlap_rid2,
+         d.overlap_perm1, d.overlap_perm2) = k[:9]
+        d.n_range, d.range_rid, d.range_inv_rid = len(self._keep[9]), k[9], k[10]
+        self.desc = d
+
+    @staticmethod
+    def _pp(arrs):
+        return (C.POINTER(C.c_float) * len(arrs))(*[_p(a, C.c_float) for a in arrs])
+
+    def rhs(self, cutoff, v2, v4, threads: int = 0):
+        """(dv2[N], dv4[4][F_N*Nl]) of the state (v2[N], v4[4][F_N*Nl])."""
+        v2 = np.ascontiguousarray(v2, np.float32)
+        v4 = [np.ascontiguousarray(x, np.float32).reshape(-1) for x in v4]
+        dv2 = np.empty(self.n, np.float32)
+        dv4 = [np.empty(self.fn * self.nl, np.float32) for _ in range(4)]
+        assert self.lib.oracle_xyz_rhs_f32(C.byref(self.desc), cutoff, _p(v2, C.c_float), self._pp(v4), _p(dv2, C.c_float),
+                                           self._pp(dv4), threads) == 0
+        return dv2, np.stack(dv4)
+
+    def correlation(self, cutoff, v2, v4):
+        v2 = np.ascontiguousarray(v2, np.float32)
+        v4 = [np.ascontiguousarray(x, np.float32).reshape(-1) for x in v4]
+        chi = [np.empty(self.nl, np.float32) for _ in range(4)]
+        assert self.lib.oracle_xyz_correlation_f32(C.byref(self.desc), cutoff, _p(v2, C.c_float), self._pp(v4),
+                                                   self._pp(chi)) == 0
+        return np.stack(chi)
+
+    def flow(self, cutoffs, v2, v4, threads: int = 0):
+        """Whole flow; returns (n_measured, chi[n_cut, 4, Nl], final (v2, v4))."""
+        cut = np.ascontiguousarray(cutoffs, np.float32)
+        v2 = np.array(v2, np.float32)
+        v4 = [np.array(x, np.float32).reshape(-1) for x in v4]
+        chi = [np.zeros(len(cut) * self.nl, np.float32) for _ in range(4)]
+        n = self.lib.oracle_xyz_flow_f32(C.byref(self.desc), _p(cut, C.c_float), len(cut), _p(v2, C.c_float),
+                                         self._pp(v4), self._pp(chi), threads)
+        assert n > 0
+        return n, np.stack(chi).reshape(4, len(cut), self.nl).transpose(1, 0, 2), (v2, np.stack(v4))

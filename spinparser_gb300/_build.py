@@ -102,9 +102,9 @@ def build_oracle(force: bool = False) -> str:
     """Compiles the CPU oracle (test infrastructure) into oracle/_build/<machine>/."""
     out = oracle_library_path()
     os.makedirs(os.path.dirname(out), exist_ok=True)
-    src = os.path.join(ORACLE_DIR, "su2_oracle.cpp")
-    if force or _stale(out, [src]):
-        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp", src, "-o", out])
+    srcs = [os.path.join(ORACLE_DIR, f) for f in ("su2_oracle.cpp", "xyz_oracle.cpp")]
+    if force or _stale(out, srcs):
+        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp", *srcs, "-o", out])
     return out
 
 

@@ -88,6 +88,8 @@ SIGNATURES = {
     "spn_lattice_get_sites": (C.c_int, [C.c_void_p, c_int_p, c_int_p]),
     "spn_lattice_get_interactions": (C.c_int, [C.c_void_p, c_int_p, c_float_p]),
     "spn_lattice_write_ldf": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "spn_lattice_get_spin_tables": (C.c_int, [C.c_void_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p,
+                                              c_int_p]),
     "spn_rpa_schedule": (C.c_int, [C.c_int, c_int_p, c_int_p, c_int_p, C.c_int, c_int_p, c_int_p, c_int_p, c_int_p,
                                    c_int_p]),
     "spn_frequency_exponential": (C.c_int, [C.c_float, C.c_float, C.c_int, c_float_p]),

@@ -91,6 +91,31 @@ class LatticeTables:
         return v2, ss.reshape(-1), dd.reshape(-1)
 
 
+# The six spin-component permutations of the lattice tables (index -> images of X, Y, Z).
+SPIN_PERMUTATIONS = np.array([[0, 1, 2], [0, 2, 1], [1, 0, 2], [1, 2, 0], [2, 0, 1], [2, 1, 0]], np.int32)
+
+
+@dataclass
+class SpinTables:
+    """Spin permutations that accompany the symmetry maps of a lattice (indices into
+    SPIN_PERMUTATIONS), parallel to the LatticeTables arrays of the same names."""
+    sites_perm: np.ndarray
+    inv_sites_perm: np.ndarray
+    overlap_perm1: np.ndarray
+    overlap_perm2: np.ndarray
+    range_perm: np.ndarray
+    range_inv_perm: np.ndarray
+    corr_perm: np.ndarray
+
+    def to_npz(self, path: str) -> None:
+        np.savez_compressed(path, **{k: np.asarray(v) for k, v in self.__dict__.items()})
+
+    @classmethod
+    def from_npz(cls, path: str) -> "SpinTables":
+        z = np.load(path)
+        return cls(**{k: z[k] for k in cls.__dataclass_fields__})
+
+
 class Lattice:
     """Symmetry-reduced lattice + spin model built by the library's host factory."""
 
@@ -142,6 +167,15 @@ class Lattice:
         check(self._lib.spn_lattice_get_interactions(self._h, _ptr(irid, I), _ptr(iJ, C.c_float)))
         return LatticeTables(nl, nb, nr, sites, inv, optr, r1[:no], r2[:no], rr, ri, corr, spos, bpos, lv,
                              irid[:ni], iJ[:ni])
+
+    def spin_tables(self) -> SpinTables:
+        i = self.info
+        nl, nr, nb, no = i.n_sites, i.n_range, i.n_basis, i.n_overlap
+        a = [np.empty(nl, np.int32), np.empty(nl, np.int32), np.empty(max(no, 1), np.int32),
+             np.empty(max(no, 1), np.int32), np.empty(nr, np.int32), np.empty(nr, np.int32),
+             np.empty(nb * nr, np.int32)]
+        check(self._lib.spn_lattice_get_spin_tables(self._h, *[_ptr(x, C.c_int) for x in a]))
+        return SpinTables(a[0], a[1], a[2][:no], a[3][:no], a[4], a[5], a[6])
 
     def sites(self, with_pairs: bool = False):
         """(site_params[n_total, 4], pair_rid[n_total, n_total] or None)."""

@@ -88,6 +88,35 @@ extern "C" int spn_lattice_get_info(const spn_lattice *lat, spn_lattice_info *in
     });
 }
 
+extern "C" int spn_lattice_get_spin_tables(const spn_lattice *lat, int *sites_perm, int *inv_sites_perm,
+                                           int *overlap_perm1, int *overlap_perm2, int *range_perm, int *range_inv_perm,
+                                           int *corr_perm) {
+    return spn::guarded([&] {
+        if (!lat) throw spn::Error(spn::ErrorType::Argument, "spn_lattice_get_spin_tables: null lattice");
+        const spn::Lattice &L = lat->lat;
+        const int nb = int(L.basis.size());
+        const int nr = int(L.range_ids[0].size());
+        if (sites_perm) {
+            auto v = L.sites_perm();
+            std::memcpy(sites_perm, v.data(), v.size() * sizeof(int));
+        }
+        if (inv_sites_perm) {
+            auto v = L.inverted_sites_perm();
+            std::memcpy(inv_sites_perm, v.data(), v.size() * sizeof(int));
+        }
+        if (overlap_perm1) std::memcpy(overlap_perm1, L.overlap_perm1.data(), L.overlap_perm1.size() * sizeof(int));
+        if (overlap_perm2) std::memcpy(overlap_perm2, L.overlap_perm2.data(), L.overlap_perm2.size() * sizeof(int));
+        for (int n = 0; n < nr; ++n) {
+            int j = L.range_ids[0][n];
+            if (range_perm) range_perm[n] = L.perm(0, j);
+            if (range_inv_perm) range_inv_perm[n] = L.perm(j, 0);
+        }
+        for (int b = 0; b < nb; ++b)
+            for (int n = 0; n < nr; ++n)
+                if (corr_perm) corr_perm[b * nr + n] = L.perm(L.basis_ids[b], L.range_ids[b][n]);
+    });
+}
+
 extern "C" int spn_lattice_get_tables(const spn_lattice *lat, int *sites_rid, int *inv_sites_rid, int *overlap_ptr,
                                       int *overlap_rid1, int *overlap_rid2, int *range_rid, int *range_inv_rid,
                                       int *corr_rid, double *site_pos, double *basis_pos, double *lattice_vectors) {

@@ -279,6 +279,16 @@ std::vector<std::pair<LatticeSite, int>> orbit(const LatticeUnitCell &uc, const 
     return out;
 }
 
+// compose(p, q)[c] = kSpinPerm[p][kSpinPerm[q][c]]: the spin permutation of a map q followed
+// by the representative's own p (LatticeModelFactory.cpp:863-865).
+int compose_perm(int p, int q) {
+    int r[3];
+    for (int c = 0; c < 3; ++c) r[c] = kSpinPerm[p][kSpinPerm[q][c]];
+    for (int k = 0; k < 6; ++k)
+        if (kSpinPerm[k][0] == r[0] && kSpinPerm[k][1] == r[1] && kSpinPerm[k][2] == r[2]) return k;
+    return 0;
+}
+
 int inverse_perm(int p) {
     int inv[3];
     for (int k = 0; k < 3; ++k) inv[kSpinPerm[p][k]] = k;
@@ -313,6 +323,18 @@ std::vector<int> Lattice::sites_rid() const {
 std::vector<int> Lattice::inverted_sites_rid() const {
     std::vector<int> r(size);
     for (int j = 0; j < size; ++j) r[j] = transform(j, 0);
+    return r;
+}
+
+std::vector<int> Lattice::sites_perm() const {
+    std::vector<int> r(size);
+    for (int j = 0; j < size; ++j) r[j] = perm(0, j);
+    return r;
+}
+
+std::vector<int> Lattice::inverted_sites_perm() const {
+    std::vector<int> r(size);
+    for (int j = 0; j < size; ++j) r[j] = perm(j, 0);
     return r;
 }
 
@@ -516,7 +538,11 @@ Lattice build_lattice(const LatticeUnitCell &uc, const SpinModelUnitCell &model,
         for (const auto &s : hood[b].v) lat.range_ids[b].push_back(sites.index_of(s));
 
     lat.sym_rid.assign(size_t(ns) * ns, -1);
-    for (int n = 0; n < n0; ++n) lat.sym_rid[n] = cls[n];
+    lat.sym_perm.assign(size_t(ns) * ns, 0);
+    for (int n = 0; n < n0; ++n) {
+        lat.sym_rid[n] = cls[n];
+        lat.sym_perm[n] = (unsigned char)cls_perm[n];
+    }
     for (int b = 1; b < nb; ++b) {
         const std::vector<Automorphism> to_origin = lattice_automorphisms(uc, model, loc, LatticeSite(0, 0, 0, b), true);
         const int bid = lat.basis_ids[b];
@@ -527,6 +553,7 @@ Lattice build_lattice(const LatticeUnitCell &uc, const SpinModelUnitCell &model,
             int nid = sites.index_of(n), eid = sites.index_of(img);
             if (eid < 0 || eid >= n0) throw Error(ErrorType::Initialization, "Could not build lattice. Could not find enough symmetries");
             lat.sym_rid[size_t(bid) * ns + nid] = lat.sym_rid[eid];
+            lat.sym_perm[size_t(bid) * ns + nid] = (unsigned char)compose_perm(lat.sym_perm[eid], to_origin[0].perm);
         }
     }
     // translate every pair (s1, s2) within range to (basis(s1), s2 - s1)
@@ -539,6 +566,7 @@ Lattice build_lattice(const LatticeUnitCell &uc, const SpinModelUnitCell &model,
             if (!hood[x.b].contains(d)) continue;
             int s2p = sites.index_of(d);
             lat.sym_rid[size_t(s1) * ns + s2] = lat.sym_rid[size_t(s1p) * ns + s2p];
+            lat.sym_perm[size_t(s1) * ns + s2] = lat.sym_perm[size_t(s1p) * ns + s2p];
         }
     }
 
@@ -555,6 +583,8 @@ Lattice build_lattice(const LatticeUnitCell &uc, const SpinModelUnitCell &model,
             if (r1 < 0 || r2 < 0) throw Error(ErrorType::Internal, "Lattice overlap references an unset symmetry entry.");
             lat.overlap_rid1.push_back(r1);
             lat.overlap_rid2.push_back(r2);
+            lat.overlap_perm1.push_back(lat.perm(0, j));
+            lat.overlap_perm2.push_back(lat.perm(j, r));
         }
         lat.overlap_ptr.push_back(int(lat.overlap_rid1.size()));
     }

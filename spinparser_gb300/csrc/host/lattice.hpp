@@ -61,16 +61,26 @@ struct Lattice {
     std::vector<int> basis_ids;                // site id of (0,0,0,b)
     std::vector<std::vector<int>> range_ids;   // [b] site ids in range of (0,0,0,b), reference order
     std::vector<int> sym_rid;                  // [id1 * n_sites + id2] -> rid of the pair, -1 if unset
+    // [id1 * n_sites + id2] -> spin permutation that accompanies the map of the pair onto its
+    // representative, an index into the six permutations (X,Y,Z) (X,Z,Y) (Y,X,Z) (Y,Z,X)
+    // (Z,X,Y) (Z,Y,X): component c of the pair is component kSpinPerm[p][c] of the
+    // representative (LatticeSiteDescriptor::spinPermutation, src/Lattice.hpp)
+    std::vector<unsigned char> sym_perm;
     std::vector<int> overlap_ptr;              // CSR over rid: [size + 1]
     std::vector<int> overlap_rid1, overlap_rid2;
+    std::vector<int> overlap_perm1, overlap_perm2;  // permutations of (0, j) and (j, rid) per pair
     std::vector<RidInteraction> interactions;  // SpinModel::interactions (src/SpinModel.hpp)
 
     int n_sites() const { return int(sites.size()); }
     int transform(int id1, int id2) const { return sym_rid[size_t(id1) * sites.size() + id2]; }
+    int perm(int id1, int id2) const { return sym_perm[size_t(id1) * sites.size() + id2]; }
     Vec3 position(int id) const;
     // Lattice::getSites()[j].rid and getInvertedSites()[j].rid
     std::vector<int> sites_rid() const;
     std::vector<int> inverted_sites_rid() const;
+    // spin permutations of getSites()[j] and getInvertedSites()[j]
+    std::vector<int> sites_perm() const;
+    std::vector<int> inverted_sites_perm() const;
 };
 
 // Parses numbers the way InputParser::stringToDouble does (src/lib/InputParser.hpp:24-56):

@@ -16,6 +16,15 @@ Outputs (committed, so the tests need no reference tree at run time):
   res_hyperkagome/        the hyperkagome unit cell and Heisenberg model of the reference's
                           res/ files (the input of test_reference1), so that the task-file
                           driver can run that task end to end
+  reference2_xyz.npz      golden XYZ-core correlations of test/scripted/test_reference2.sh
+                          (hyperhoneycomb r=3 Heisenberg-Kitaev j=0.1, k=-1, 14 manual
+                          frequencies, cutoff 10 -> 0.3 x0.9), read from
+                          test/scripted/assets/test_reference2.ref (XYZCorXX/YY/ZZ/DD)
+  res_hyperhoneycomb/     the hyperhoneycomb unit cell and Heisenberg-Kitaev model of the
+                          reference's res/ files (the input of test_reference2)
+
+`python tests/golden/make_fixtures.py <reference root> reference2` regenerates only the
+test_reference2 fixtures.
 """
 from __future__ import annotations
 
@@ -83,6 +92,36 @@ def write_hyperkagome_resources(ref_root: str) -> None:
         f.write(head + extract_resource(ref_root, "models", "model", "hyperkagome-heisenberg") + "\n")
 
 
+def write_reference2(ref_root: str) -> None:
+    """XYZ golden of test_reference2 (the XYZ task of the script's XYZ/TRI pair) and its
+    resource files."""
+    scripted = os.path.join(ref_root, "test", "scripted")
+    script = open(os.path.join(scripted, "test_reference2.sh")).read()
+    p = task_parameters(script.replace("${CORE}", "XYZ"))
+    k = float(re.search(r"<k>([-0-9.]+)</k>", script).group(1))
+    ref = os.path.join(scripted, "assets", "test_reference2.ref")
+    comps = {}
+    cut = None
+    for c in ("XX", "YY", "ZZ", "DD"):
+        cc, v = h5lite.read_correlations(ref, "XYZCor" + c)
+        assert cut is None or np.array_equal(cut, cc)
+        cut = cc
+        comps[c.lower()] = v
+    meta = h5lite.open_file(ref)["XYZCorXX/meta"]
+    np.savez_compressed(os.path.join(HERE, "reference2_xyz.npz"), cutoffs=cut, **comps,
+                        frequencies=np.array(p["frequencies"], np.float32),
+                        cutoff_spec=np.array([p["cutoff_max"], p["cutoff_min"], p["cutoff_step"]], np.float32),
+                        j=np.float32(p["j"]), k=np.float32(k), sites=meta["sites"].read(), basis=meta["basis"].read(),
+                        lattice_vectors=meta["latticeVectors"].read())
+    out = os.path.join(HERE, "res_hyperhoneycomb")
+    os.makedirs(out, exist_ok=True)
+    head = '<?xml version="1.0" encoding="utf-8"?>\n'
+    with open(os.path.join(out, "lattices.xml"), "w") as f:
+        f.write(head + extract_resource(ref_root, "lattices", "unitcell", p["lattice"]) + "\n")
+    with open(os.path.join(out, "models.xml"), "w") as f:
+        f.write(head + extract_resource(ref_root, "models", "model", p["model"]) + "\n")
+
+
 def write_reference1_layout(ref: str) -> None:
     """Structure (members, attributes, shapes) and encoding fingerprint of the libhdf5-written
     test_reference1.ref, for checking the package's .obs writer without the file itself."""
@@ -142,4 +181,9 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) > 2 and sys.argv[2] == "reference2":
+        write_reference2(root)
+    else:
+        main(root)
+        write_reference2(root)
