@@ -65,10 +65,11 @@ def test_xyz_oracle_fails_on_sign_flipped_kitaev():
                       resource_dir=os.path.join(GOLDEN, "res_hyperhoneycomb"))
     tab, st = lat.tables(), lat.spin_tables()
     freq = np.sort(z["frequencies"])
-    cut = z["cutoffs"][:6]
+    cut = z["cutoffs"][:16]
     orc = XyzOracle(tab, st, freq)
     n, chi, _ = orc.flow(cut, *xyz_initial_state(tab, len(freq)))
     corr = xyz_scatter(chi[n - 1], tab, st)
+    # the reference's comparator (1e-5 absolute) rejects it well before the end of the flow
     assert np.abs(corr[0] - z["xx"][n - 1]).max() > 1e-3
 
 
