@@ -377,6 +377,53 @@ int spn_run_options_default(spn_run_options *o);
 /* Runs a task file; result may be NULL. */
 int spn_run_task(const char *task_path, const spn_run_options *o, spn_run_result *result);
 
+/* ------------------------------------------------------------------------------------
+ * XYZ core: models with diagonal, possibly anisotropic couplings (Heisenberg-Kitaev, XXZ, ...)
+ * on the same skeleton, with four vertex components X, Y, Z and density D
+ * (src/XYZ/XYZFrgCore.cpp, XYZVertexTwoParticle.hpp, XYZMeasurementCorrelation.cpp).
+ * Arrays in the reference layout: v2[N], v4xx/v4yy/v4zz/v4dd[F_N*Nl].
+ * ------------------------------------------------------------------------------------ */
+typedef struct spn_xyz spn_xyz;
+
+typedef struct {
+    int n_freq;                 /* N */
+    const float *freq;          /* [N] ascending, positive */
+    int n_sites;                /* Nl <= 128 */
+    const int *sites_rid, *sites_perm;         /* [Nl] getSites(): rid and spin permutation */
+    const int *inv_sites_rid, *inv_sites_perm; /* [Nl] getInvertedSites() */
+    const int *overlap_ptr;     /* [Nl+1] */
+    const int *overlap_rid1, *overlap_rid2;    /* [overlap_ptr[Nl]] */
+    const int *overlap_perm1, *overlap_perm2;  /* [overlap_ptr[Nl]] permutations of (0,j), (j,rid) */
+    int n_range;
+    const int *range_rid, *range_inv_rid;      /* [n_range] */
+    int n_corr;                 /* n_basis * n_range */
+    const int *corr_rid, *corr_perm;           /* [n_corr] */
+    int device;
+    int flags;                  /* reserved, 0 */
+} spn_xyz_desc;
+/* Permutation indices are those of spn_lattice_get_spin_tables. */
+
+/* XYZEffectiveAction initial condition (src/XYZ/XYZEffectiveAction.hpp:38-60): zeros, then
+ * v4cc[it*Nl + rid] += 0.25 J^cc(rid) / normalization for c = x, y, z. */
+int spn_xyz_initial_state(const spn_lattice *lat, int n_freq, float normalization, float *v2, float *v4xx,
+                          float *v4yy, float *v4zz, float *v4dd);
+
+/* The flow cycle, as the spn_su2_* calls (XYZFrgCore::computeStep / finalizeStep,
+ * XYZFrgCore.cpp:109-159). */
+int spn_xyz_create(const spn_xyz_desc *desc, spn_xyz **out);
+int spn_xyz_destroy(spn_xyz *h);
+int spn_xyz_set_state(spn_xyz *h, float cutoff, const float *v2, const float *v4xx, const float *v4yy,
+                      const float *v4zz, const float *v4dd);
+int spn_xyz_get_state(spn_xyz *h, float *cutoff, float *v2, float *v4xx, float *v4yy, float *v4zz, float *v4dd);
+int spn_xyz_compute_step(spn_xyz *h);
+int spn_xyz_get_flow(spn_xyz *h, float *dv2, float *v4xx, float *v4yy, float *v4zz, float *v4dd);
+int spn_xyz_finalize_step(spn_xyz *h, float new_cutoff);
+/* Correlations xx/yy/zz/dd[n_corr] in the (basis, site-in-range) order of XYZCorXX etc.
+ * (XYZMeasurementCorrelation.cpp:166-184) and chi[4][Nl] per representative; any pointer may be
+ * NULL. */
+int spn_xyz_measure_correlation(spn_xyz *h, float *xx, float *yy, float *zz, float *dd, float *chi);
+int spn_xyz_is_diverged(spn_xyz *h, int *diverged);
+
 #ifdef __cplusplus
 }
 #endif

@@ -6,10 +6,12 @@ spinparser_gb300._build``).
 """
 from ._capi import SpnError, load_library
 from .batch import Su2Batch
-from .core import (FP64, FP64_SELF_ENERGY, RES_DIR, Lattice, LatticeTables, Su2Flow, cutoff_exponential, device_count,
-                   frequency_exponential, measure_fp32_peak)
+from .core import (FP64, FP64_SELF_ENERGY, RES_DIR, Lattice, LatticeTables, SpinTables, Su2Flow, cutoff_exponential,
+                   device_count, frequency_exponential, measure_fp32_peak)
+from .xyz import XyzFlow, xyz_initial_state
 
 __all__ = [
     "SpnError", "load_library", "Lattice", "LatticeTables", "Su2Flow", "frequency_exponential", "cutoff_exponential",
-    "device_count", "measure_fp32_peak", "RES_DIR", "FP64", "FP64_SELF_ENERGY", "Su2Batch",
+    "device_count", "measure_fp32_peak", "RES_DIR", "FP64", "FP64_SELF_ENERGY", "Su2Batch", "SpinTables", "XyzFlow",
+    "xyz_initial_state",
 ]

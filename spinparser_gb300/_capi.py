@@ -28,6 +28,16 @@ class LatticeInfo(C.Structure):
     ]
 
 
+class XyzDesc(C.Structure):
+    _fields_ = [
+        ("n_freq", C.c_int), ("freq", c_float_p), ("n_sites", C.c_int),
+        ("sites_rid", c_int_p), ("sites_perm", c_int_p), ("inv_sites_rid", c_int_p), ("inv_sites_perm", c_int_p),
+        ("overlap_ptr", c_int_p), ("overlap_rid1", c_int_p), ("overlap_rid2", c_int_p), ("overlap_perm1", c_int_p),
+        ("overlap_perm2", c_int_p), ("n_range", C.c_int), ("range_rid", c_int_p), ("range_inv_rid", c_int_p),
+        ("n_corr", C.c_int), ("corr_rid", c_int_p), ("corr_perm", c_int_p), ("device", C.c_int), ("flags", C.c_int),
+    ]
+
+
 class Su2Desc(C.Structure):
     _fields_ = [
         ("n_freq", C.c_int),
@@ -110,6 +120,17 @@ SIGNATURES = {
     "spn_su2_finalize_step": (C.c_int, [C.c_void_p, C.c_float]),
     "spn_su2_measure_correlation": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p, c_float_p]),
     "spn_su2_launch_correlation": (C.c_int, [C.c_void_p]),
+    "spn_xyz_initial_state": (C.c_int, [C.c_void_p, C.c_int, C.c_float, c_float_p, c_float_p, c_float_p, c_float_p,
+                                        c_float_p]),
+    "spn_xyz_create": (C.c_int, [C.POINTER(XyzDesc), C.POINTER(C.c_void_p)]),
+    "spn_xyz_destroy": (C.c_int, [C.c_void_p]),
+    "spn_xyz_set_state": (C.c_int, [C.c_void_p, C.c_float, c_float_p, c_float_p, c_float_p, c_float_p, c_float_p]),
+    "spn_xyz_get_state": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p, c_float_p, c_float_p, c_float_p]),
+    "spn_xyz_compute_step": (C.c_int, [C.c_void_p]),
+    "spn_xyz_get_flow": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p, c_float_p, c_float_p]),
+    "spn_xyz_finalize_step": (C.c_int, [C.c_void_p, C.c_float]),
+    "spn_xyz_measure_correlation": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p, c_float_p, c_float_p]),
+    "spn_xyz_is_diverged": (C.c_int, [C.c_void_p, c_int_p]),
     "spn_su2_set_state_f64": (C.c_int, [C.c_void_p, C.c_float, c_double_p, c_double_p, c_double_p]),
     "spn_su2_get_state_f64": (C.c_int, [C.c_void_p, c_float_p, c_double_p, c_double_p, c_double_p]),
     "spn_su2_get_flow_f64": (C.c_int, [C.c_void_p, c_double_p, c_double_p, c_double_p]),

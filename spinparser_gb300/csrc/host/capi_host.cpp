@@ -249,6 +249,25 @@ extern "C" int spn_su2_initial_state(const spn_lattice *lat, int n_freq, float n
     });
 }
 
+extern "C" int spn_xyz_initial_state(const spn_lattice *lat, int n_freq, float normalization, float *v2, float *v4xx,
+                                     float *v4yy, float *v4zz, float *v4dd) {
+    return spn::guarded([&] {
+        if (!lat || n_freq < 2) throw spn::Error(spn::ErrorType::Argument, "spn_xyz_initial_state: bad argument");
+        const spn::Lattice &L = lat->lat;
+        const long long nl = L.size;
+        const long long fn = (long long)n_freq * n_freq * (n_freq + 1) / 2;
+        if (v2) std::memset(v2, 0, sizeof(float) * n_freq);
+        if (v4dd) std::memset(v4dd, 0, sizeof(float) * size_t(fn * nl));
+        float *comp[3] = {v4xx, v4yy, v4zz};
+        for (int c = 0; c < 3; ++c) {
+            if (!comp[c]) continue;
+            std::memset(comp[c], 0, sizeof(float) * size_t(fn * nl));
+            for (long long it = 0; it < fn; ++it)
+                for (const auto &ia : L.interactions) comp[c][it * nl + ia.rid] += 0.25f * ia.J[c][c] / normalization;
+        }
+    });
+}
+
 extern "C" int spn_rpa_schedule(int n_sites, const int *overlap_ptr, const int *overlap_rid1, const int *overlap_rid2,
                                 int lanes, int *info, int *sched, int *count, int *slot_base, int *seg_ptr) {
     return spn::guarded([&] {

@@ -1,0 +1,845 @@
+// GB300 kernels of the XYZ pf-FRG flow right-hand side (models with diagonal, possibly
+// anisotropic couplings: Heisenberg-Kitaev, XXZ, ...) and the device half of the spn_xyz_* C
+// ABI in include/spn_su2.h.  Restates XYZFrgCore (src/XYZ/XYZFrgCore.cpp:161-570), the XYZ
+// vertex access (src/XYZ/XYZVertexTwoParticle.hpp:185-612) and XYZMeasurementCorrelation
+// (src/XYZ/XYZMeasurementCorrelation.cpp:98-184).
+//
+// The vertex has four components per element, X, Y, Z and density D, stored as one float4
+// per element ((s(s+1)/2+u)*N + t)*Nl + rid, so an interpolation support is one 16-byte load.
+// A lattice symmetry map may permute X, Y, Z: site j of the superbundle reads component
+// perm[p_j][c] of its representative, and each RPA pair carries the permutations of its two
+// factors (spn_lattice_get_spin_tables).
+//
+// A step: the self-energy flow (one CTA per frequency), the loop-frequency node tables (the
+// SU(2) core's, shared), the vertex flow and the Euler update.  The vertex-flow kernel runs a
+// persistent grid whose warps take one (s,t,u) triple at a time from a device counter; the
+// lanes hold the sites (up to four each), the channel's nodes are visited in order, and the t
+// channel's RPA sum exchanges the first two slabs of a node through shared memory.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "su2_common.cuh"
+#include "su2_device.cuh"
+#include "su2_kernels.cuh"
+#include "host/capi_common.hpp"
+#include "../../include/spn_su2.h"
+
+using namespace spn;
+using namespace spn::dev;
+
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kWarps = kThreads / 32;
+constexpr int kSpt = 4;  // sites per lane (Nl <= 128)
+constexpr int X = 0, Y = 1, Z = 2, D = 3;
+
+// The six spin permutations (X,Y,Z) (X,Z,Y) (Y,X,Z) (Y,Z,X) (Z,X,Y) (Z,Y,X): 2 bits per image
+// component, 6 bits per permutation.
+constexpr unsigned long long kPermBits =
+    36ull | (24ull << 6) | (33ull << 12) | (9ull << 18) | (18ull << 24) | (6ull << 30);
+__host__ __device__ __forceinline__ int perm_c(int p, int c) { return int((kPermBits >> (6 * p + 2 * c)) & 3ull); }
+
+__device__ __forceinline__ float comp_of(const float4 &v, int c) { return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w)); }
+
+struct XyzArgs {
+    int n, nl, fn, max_nodes, n_range, n_corr;
+    float cutoff;
+    const float *freq;
+    const float4 *sd;  // state
+    float4 *dsd;       // flow
+    const float *v2;
+    float *dv2;
+    const int *sites, *sites_perm, *inv_sites, *inv_sites_perm;
+    const int *ov_ptr, *ov_r1, *ov_r2, *ov_p1, *ov_p2;
+    const int *range_rid, *range_inv;
+    const float *node_wp, *node_c;
+    const int *node_cnt;
+    int *work_counter;
+    unsigned *status;
+    const int *corr_rid, *corr_perm;
+    double *partial;  // [kMaxCorrNodes][4][nl]
+    float *out;       // [4][n_corr] correlations, then chi [4][nl]
+};
+
+// One component of the state for value_none (su2_device.cuh): c < 3 reads X, Y or Z (its
+// "spin" accessor), c == 3 the density (with the density's sign on an s <-> u swap).
+struct QuadComp {
+    const float4 *v;
+    int c;
+    __device__ __forceinline__ float spin(int i) const { return comp_of(__ldg(v + i), c); }
+    __device__ __forceinline__ float density(int i) const { return __ldg(v + i).w; }
+};
+
+__device__ __forceinline__ float value4(const float *pos, const XyzArgs &a, int c, int rid12, int rid21, float s, float t,
+                                        float u) {
+    return value_none(pos, a.n, a.nl, QuadComp{a.sd, c}, c == D, rid12, rid21, s, t, u);
+}
+
+// ------------------------------------------------------------------------------------
+// self-energy flow, one CTA per frequency (XYZFrgCore.cpp:161-194)
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) xyz_self_energy_kernel(XyzArgs a) {
+    __shared__ float pos[kMaxFreq];
+    __shared__ double red[4];
+    for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
+    __syncthreads();
+    const int i = blockIdx.x;
+    const float w = pos[i], L = a.cutoff;
+    const float wpl = w + L, wml = w - L;
+    double part = 0.0;
+    for (int j = threadIdx.x; j < a.n_range; j += blockDim.x) {
+        const int r12 = a.range_rid[j], r21 = a.range_inv[j];
+        part += double(value4(pos, a, D, r12, r21, wpl, 0.0f, wml)) - double(value4(pos, a, D, r12, r21, wml, 0.0f, wpl));
+    }
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sum = 0.0;
+        for (int k = 0; k < int(blockDim.x >> 5); ++k) sum += red[k];
+        double val = -2.0 * sum;
+        for (int c = 0; c < 4; ++c)
+            val += double(value4(pos, a, c, 0, 0, wpl, wml, 0.0f)) - double(value4(pos, a, c, 0, 0, wml, wpl, 0.0f));
+        val /= (2.0 * kPiD * (double(L) + odd_interp(pos, a.n, a.v2, L)));
+        const float outv = float(val);
+        a.dv2[i] = outv;
+        if (isnan(outv)) atomicOr(a.status, kStatusNaN);
+    }
+}
+
+// Loop-frequency node tables: the SU(2) core's body on an argument block of this flow.
+__global__ void xyz_node_table_kernel(FlowArgs f) { node_table_body(f, blockIdx.x); }
+
+// ------------------------------------------------------------------------------------
+// vertex flow
+// ------------------------------------------------------------------------------------
+struct Lane4 {
+    int j[kSpt], rid[kSpt], prm[kSpt], irid[kSpt], iprm[kSpt];
+    bool valid[kSpt];
+};
+
+// Interpolated slab of one access buffer for the lane's sites (getValueSuperbundle): X, Y, Z
+// of site j read the permuted components of its representative, D the signed density.
+__device__ __forceinline__ void gather4(const XyzArgs &a, const AB4 &ab, const Lane4 &ln, float4 *out) {
+#pragma unroll
+    for (int k = 0; k < kSpt; ++k) {
+        float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (ln.valid[k]) {
+            const int r = ab.exch ? ln.irid[k] : ln.rid[k];
+            const int p = ab.exch ? ln.iprm[k] : ln.prm[k];
+            const int c0 = perm_c(p, 0), c1 = perm_c(p, 1), c2 = perm_c(p, 2);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float4 v = __ldg(a.sd + ab.off[q] + r);
+                g.x += ab.w[q] * comp_of(v, c0);
+                g.y += ab.w[q] * comp_of(v, c1);
+                g.z += ab.w[q] * comp_of(v, c2);
+                g.w += ab.sw[q] * v.w;
+            }
+        }
+        out[k] = g;
+    }
+}
+
+// getValueLocal of the four components at rid 0 (identity permutation).
+__device__ __forceinline__ float4 local4(const XyzArgs &a, const AB4 &ab) {
+    float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const float4 v = __ldg(a.sd + ab.off[q]);
+        g.x += ab.w[q] * v.x;
+        g.y += ab.w[q] * v.y;
+        g.z += ab.w[q] * v.z;
+        g.w += ab.sw[q] * v.w;
+    }
+    return g;
+}
+
+// The products of a pair of slabs (a, b) in the s integrand: per component (D,c) and (c,D)
+// added, the two others crossed and subtracted (XYZFrgCore.cpp:230-261).
+__device__ __forceinline__ float4 s_terms(const float4 &a, const float4 &b) {
+    float4 r;
+    r.x = a.w * b.x + a.x * b.w - a.z * b.y - a.y * b.z;
+    r.y = a.w * b.y + a.y * b.w - a.z * b.x - a.x * b.z;
+    r.z = a.w * b.z + a.z * b.w - a.x * b.y - a.y * b.x;
+    r.w = a.w * b.w + a.x * b.x + a.y * b.y + a.z * b.z;
+    return r;
+}
+
+// The u integrand subtracts all four products of every component (XYZFrgCore.cpp:436-469):
+// the cross terms keep the sign of the others, unlike the s integrand.
+__device__ __forceinline__ float4 u_terms(const float4 &a, const float4 &b) {
+    float4 r;
+    r.x = -(a.w * b.x + a.x * b.w + a.z * b.y + a.y * b.z);
+    r.y = -(a.w * b.y + a.y * b.w + a.z * b.x + a.x * b.z);
+    r.z = -(a.w * b.z + a.z * b.w + a.x * b.y + a.y * b.x);
+    r.w = -(a.w * b.w + a.x * b.x + a.y * b.y + a.z * b.z);
+    return r;
+}
+
+__global__ void __launch_bounds__(kThreads) xyz_vertex_kernel(XyzArgs a) {
+    __shared__ float pos[kMaxFreq];
+    extern __shared__ float4 xs[];  // per warp: A[kSpt*32], B[kSpt*32] (first two t slabs)
+    for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int n = a.n, nl = a.nl;
+    float4 *As = xs + size_t(warp) * 2 * kSpt * 32, *Bs = As + kSpt * 32;
+    Lane4 ln;
+#pragma unroll
+    for (int k = 0; k < kSpt; ++k) {
+        const int j = lane + 32 * k;
+        ln.j[k] = j;
+        ln.valid[k] = j < nl;
+        ln.rid[k] = ln.valid[k] ? a.sites[j] : 0;
+        ln.prm[k] = ln.valid[k] ? a.sites_perm[j] : 0;
+        ln.irid[k] = ln.valid[k] ? a.inv_sites[j] : 0;
+        ln.iprm[k] = ln.valid[k] ? a.inv_sites_perm[j] : 0;
+    }
+    const float two_pi = 2.0f * float(kPiD);
+
+    for (;;) {
+        int it = 0;
+        if (lane == 0) it = atomicAdd(a.work_counter, 1);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= a.fn) break;
+        const int su = it / n, ti = it - su * n;
+        int si = int((sqrtf(8.0f * float(su) + 1.0f) - 1.0f) * 0.5f);
+        while (si * (si + 1) / 2 > su) --si;
+        while ((si + 1) * (si + 2) / 2 <= su) ++si;
+        const int ui = su - si * (si + 1) / 2;
+        const float s = pos[si], t = pos[ti], u = pos[ui];
+        const float w1p = 0.5f * (s + t + u), w1 = 0.5f * (s - t + u), w2p = 0.5f * (s - t - u), w2 = 0.5f * (s + t - u);
+
+        float4 acc[kSpt];
+#pragma unroll
+        for (int k = 0; k < kSpt; ++k) acc[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        for (int ch = 0; ch < 3; ++ch) {
+            const int xi = ch == 0 ? si : (ch == 1 ? ti : ui);
+            const int cnt = a.node_cnt[xi];
+            const float *nwp = a.node_wp + size_t(xi) * a.max_nodes;
+            const float *nc = a.node_c + size_t(xi) * a.max_nodes;
+            for (int b = 0; b < cnt; ++b) {
+                const float wp = nwp[b], c = nc[b];
+                AB4 ab;
+                float4 S0[kSpt], S1[kSpt], S2[kSpt], S3[kSpt], r[kSpt];
+                if (ch == 0) {  // integralKernelS, XYZFrgCore.cpp:215-262
+                    access4<kS>(pos, n, nl, s, -w1 - wp, -w2 - wp, ab); gather4(a, ab, ln, S0);
+                    access4<kS>(pos, n, nl, s, w1p + wp, -w2p - wp, ab); gather4(a, ab, ln, S1);
+                    access4<kS>(pos, n, nl, s, w2 + wp, w1 + wp, ab); gather4(a, ab, ln, S2);
+                    access4<kS>(pos, n, nl, s, -w2p - wp, w1p + wp, ab); gather4(a, ab, ln, S3);
+#pragma unroll
+                    for (int k = 0; k < kSpt; ++k) {
+                        const float4 p = s_terms(S0[k], S1[k]), q = s_terms(S2[k], S3[k]);
+                        r[k] = make_float4(p.x + q.x, p.y + q.y, p.z + q.z, p.w + q.w);
+                    }
+                } else if (ch == 2) {  // integralKernelU, XYZFrgCore.cpp:420-470
+                    access4<kU>(pos, n, nl, w1 + wp, wp - w2p, u, ab); gather4(a, ab, ln, S0);
+                    access4<kU>(pos, n, nl, w1p + wp, w2 - wp, u, ab); gather4(a, ab, ln, S1);
+                    access4<kU>(pos, n, nl, w2p - wp, -w1 - wp, u, ab); gather4(a, ab, ln, S2);
+                    access4<kU>(pos, n, nl, w2 - wp, w1p + wp, u, ab); gather4(a, ab, ln, S3);
+#pragma unroll
+                    for (int k = 0; k < kSpt; ++k) {
+                        const float4 p = u_terms(S0[k], S1[k]), q = u_terms(S2[k], S3[k]);
+                        r[k] = make_float4(p.x + q.x, p.y + q.y, p.z + q.z, p.w + q.w);
+                    }
+                } else {  // integralKernelT, XYZFrgCore.cpp:264-418
+                    access4<kT>(pos, n, nl, w1 - wp, t, w1p + wp, ab); gather4(a, ab, ln, S0);
+                    access4<kT>(pos, n, nl, w2p - wp, t, -w2 - wp, ab); gather4(a, ab, ln, S1);
+                    access4<kT>(pos, n, nl, w1p + wp, t, w1 - wp, ab); gather4(a, ab, ln, S2);
+                    access4<kT>(pos, n, nl, w2 + wp, t, wp - w2p, ab); gather4(a, ab, ln, S3);
+                    // RPA: the first two slabs of all sites through shared memory
+#pragma unroll
+                    for (int k = 0; k < kSpt; ++k)
+                        if (ln.valid[k]) {
+                            As[ln.j[k]] = S0[k];
+                            Bs[ln.j[k]] = S1[k];
+                        }
+                    __syncwarp();
+                    float4 cb, ica, cb2, ica2;
+                    access4<kU>(pos, n, nl, w2p - wp, -w2 - wp, t, ab); cb = local4(a, ab);
+                    access4<kU>(pos, n, nl, w1 - wp, -w1p - wp, -t, ab); ica = local4(a, ab);
+                    access4<kU>(pos, n, nl, w2 + wp, wp - w2p, t, ab); cb2 = local4(a, ab);
+                    access4<kU>(pos, n, nl, w1p + wp, wp - w1, -t, ab); ica2 = local4(a, ab);
+                    const float cbv[4] = {cb.x, cb.y, cb.z, cb.w}, icav[4] = {ica.x, ica.y, ica.z, ica.w};
+                    const float cb2v[4] = {cb2.x, cb2.y, cb2.z, cb2.w}, ica2v[4] = {ica2.x, ica2.y, ica2.z, ica2.w};
+#pragma unroll
+                    for (int k = 0; k < kSpt; ++k) {
+                        float rp[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                        if (ln.valid[k]) {
+                            const int rid = ln.j[k];
+                            for (int i = a.ov_ptr[rid]; i < a.ov_ptr[rid + 1]; ++i) {
+                                const float4 x1 = As[a.ov_r1[i]], x2 = Bs[a.ov_r2[i]];
+                                const int p1 = a.ov_p1[i], p2 = a.ov_p2[i];
+#pragma unroll
+                                for (int cc = 0; cc < 3; ++cc) rp[cc] += comp_of(x1, perm_c(p1, cc)) * comp_of(x2, perm_c(p2, cc));
+                                rp[3] += x1.w * x2.w;
+                            }
+                        }
+                        const float a0[4] = {S0[k].x, S0[k].y, S0[k].z, S0[k].w}, a1[4] = {S1[k].x, S1[k].y, S1[k].z, S1[k].w};
+                        const float a2[4] = {S2[k].x, S2[k].y, S2[k].z, S2[k].w}, a3[4] = {S3[k].x, S3[k].y, S3[k].z, S3[k].w};
+                        float rv[4];
+#pragma unroll
+                        for (int cc = 0; cc < 3; ++cc) {  // XYZFrgCore.cpp:347-401
+                            const int pA = cc == X ? Y : X, pB = cc == Z ? Y : Z;
+                            const int qA = cc == Z ? X : Z, qB = cc == X ? Y : (cc == Y ? X : Y);
+                            float v = 4.0f * rp[cc];
+                            v -= a0[cc] * cbv[D];
+                            v += a0[cc] * cbv[pA];
+                            v += a0[cc] * cbv[pB];
+                            v -= a0[cc] * cbv[cc];
+                            v -= icav[D] * a1[cc];
+                            v += icav[qA] * a1[cc];
+                            v += icav[qB] * a1[cc];
+                            v -= icav[cc] * a1[cc];
+                            v -= a2[cc] * cb2v[D];
+                            v += a2[cc] * cb2v[pA];
+                            v += a2[cc] * cb2v[pB];
+                            v -= a2[cc] * cb2v[cc];
+                            v -= ica2v[D] * a3[cc];
+                            v += ica2v[qA] * a3[cc];
+                            v += ica2v[qB] * a3[cc];
+                            v -= ica2v[cc] * a3[cc];
+                            rv[cc] = v;
+                        }
+                        {  // XYZFrgCore.cpp:402-417
+                            float v = 4.0f * rp[D];
+                            v -= a0[D] * cbv[D];
+                            v -= a0[D] * cbv[X];
+                            v -= a0[D] * cbv[Y];
+                            v -= a0[D] * cbv[Z];
+                            v -= icav[D] * a1[D];
+                            v -= icav[X] * a1[D];
+                            v -= icav[Y] * a1[D];
+                            v -= icav[Z] * a1[D];
+                            v -= a2[D] * cb2v[D];
+                            v -= a2[D] * cb2v[X];
+                            v -= a2[D] * cb2v[Y];
+                            v -= a2[D] * cb2v[Z];
+                            v -= ica2v[D] * a3[D];
+                            v -= ica2v[X] * a3[D];
+                            v -= ica2v[Y] * a3[D];
+                            v -= ica2v[Z] * a3[D];
+                            rv[D] = v;
+                        }
+                        r[k] = make_float4(rv[0], rv[1], rv[2], rv[3]);
+                    }
+                    __syncwarp();
+                }
+#pragma unroll
+                for (int k = 0; k < kSpt; ++k) {
+                    acc[k].x += c * r[k].x;
+                    acc[k].y += c * r[k].y;
+                    acc[k].z += c * r[k].z;
+                    acc[k].w += c * r[k].w;
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kSpt; ++k)
+            if (ln.valid[k]) {
+                const float4 o = make_float4(acc[k].x / two_pi, acc[k].y / two_pi, acc[k].z / two_pi, acc[k].w / two_pi);
+                a.dsd[size_t(it) * nl + ln.j[k]] = o;
+                if (isnan(o.x) || isnan(o.y) || isnan(o.z) || isnan(o.w)) atomicOr(a.status, kStatusNaN);
+            }
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// correlation measurement at nu = 0 (XYZMeasurementCorrelation.cpp:98-184): one CTA per
+// outer node accumulates the inner integral per site in FP64, a final CTA adds the outer
+// weights and the on-site term and scatters to (basis, site in range) entries.
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) xyz_corr_inner_kernel(XyzArgs a) {
+    __shared__ float pos[kMaxFreq];
+    __shared__ float nwp[kMaxCorrNodes];
+    __shared__ double nw[kMaxCorrNodes];
+    __shared__ int ncnt;
+    __shared__ double red[kWarps][4][32 * kSpt];
+    for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
+    __syncthreads();
+    if (threadIdx.x == 0) ncnt = corr_nodes(pos, a.n, a.cutoff, nwp, nw);
+    __syncthreads();
+    const int ia = blockIdx.x;
+    if (ia >= ncnt) return;
+    const float w = nwp[ia];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nl = a.nl;
+    Lane4 ln;
+#pragma unroll
+    for (int k = 0; k < kSpt; ++k) {
+        const int j = lane + 32 * k;
+        ln.j[k] = j;
+        ln.valid[k] = j < nl;
+        ln.rid[k] = ln.valid[k] ? a.sites[j] : 0;
+        ln.prm[k] = ln.valid[k] ? a.sites_perm[j] : 0;
+        ln.irid[k] = ln.valid[k] ? a.inv_sites[j] : 0;
+        ln.iprm[k] = ln.valid[k] ? a.inv_sites_perm[j] : 0;
+    }
+    const double dw = double(w) + odd_interp(pos, a.n, a.v2, w);
+    double acc[kSpt][4];
+#pragma unroll
+    for (int k = 0; k < kSpt; ++k)
+        for (int c = 0; c < 4; ++c) acc[k][c] = 0.0;
+    for (int b = warp; b < ncnt; b += kWarps) {
+        const float wp = nwp[b];
+        AB8 ab;
+        access8(pos, a.n, nl, w + wp + 0.0f, 0.0f, w - wp, ab);
+        float vv[4];
+        for (int c = 0; c < 4; ++c) vv[c] = value4(pos, a, c, 0, 0, w + wp + 0.0f, w - wp, 0.0f);
+        const double dwp = double(wp) + odd_interp(pos, a.n, a.v2, wp);
+        const double cw = nw[b] / (dw * dw * dwp * dwp * (4.0 * kPiD * kPiD));
+#pragma unroll
+        for (int k = 0; k < kSpt; ++k) {
+            if (!ln.valid[k]) continue;
+            const int r = ab.exch ? ln.irid[k] : ln.rid[k];
+            const int p = ab.exch ? ln.iprm[k] : ln.prm[k];
+            float g[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            for (int q = 0; q < 8; ++q) {
+                const float4 v = __ldg(a.sd + ab.off[q] + r);
+                for (int c = 0; c < 3; ++c) g[c] += ab.w[q] * comp_of(v, perm_c(p, c));
+                g[3] += ab.sw[q] * v.w;
+            }
+            double rr[4] = {-double(g[0]), -double(g[1]), -double(g[2]), -4.0 * double(g[3])};  // dumbbell
+            if (ln.j[k] == 0) {  // egg diagram
+                rr[0] += 0.5 * (double(vv[0]) - vv[1] - vv[2] + vv[3]);
+                rr[1] += 0.5 * (-double(vv[0]) + vv[1] - vv[2] + vv[3]);
+                rr[2] += 0.5 * (-double(vv[0]) - vv[1] + vv[2] + vv[3]);
+                rr[3] += 2.0 * (double(vv[0]) + vv[1] + vv[2] + vv[3]);
+            }
+            for (int c = 0; c < 4; ++c) acc[k][c] += cw * rr[c];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kSpt; ++k)
+        for (int c = 0; c < 4; ++c) red[warp][c][lane + 32 * k] = acc[k][c];
+    __syncthreads();
+    for (int e = threadIdx.x; e < 4 * nl; e += blockDim.x) {
+        const int c = e / nl, j = e - c * nl;
+        double sum = 0.0;
+        for (int q = 0; q < kWarps; ++q) sum += red[q][c][j];
+        a.partial[(size_t(ia) * 4 + c) * nl + j] = sum;
+    }
+}
+
+__global__ void xyz_corr_final_kernel(XyzArgs a) {
+    __shared__ float pos[kMaxFreq];
+    __shared__ float nwp[kMaxCorrNodes];
+    __shared__ double nw[kMaxCorrNodes];
+    __shared__ int ncnt;
+    extern __shared__ double chi[];  // [4][nl]
+    for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
+    __syncthreads();
+    if (threadIdx.x == 0) ncnt = corr_nodes(pos, a.n, a.cutoff, nwp, nw);
+    __syncthreads();
+    const int nl = a.nl;
+    for (int e = threadIdx.x; e < 4 * nl; e += blockDim.x) {
+        const int c = e / nl, j = e - c * nl;
+        double sum = 0.0;
+        for (int ia = 0; ia < ncnt; ++ia) {
+            double v = a.partial[(size_t(ia) * 4 + c) * nl + j];
+            if (j == 0) {  // on-site term
+                const float w = nwp[ia];
+                const double dw = double(w) + odd_interp(pos, a.n, a.v2, w);
+                const double t1 = 1.0 / (dw * dw);
+                v += c == D ? t1 / kPiD : t1 / (4.0 * kPiD);
+            }
+            sum += nw[ia] * v;
+        }
+        chi[e] = sum;
+        a.out[4 * size_t(a.n_corr) + e] = float(sum);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < a.n_corr; q += blockDim.x) {
+        const int r = a.corr_rid[q], p = a.corr_perm[q];
+        for (int c = 0; c < 3; ++c) a.out[size_t(c) * a.n_corr + q] = float(chi[perm_c(p, c) * nl + r]);
+        a.out[3 * size_t(a.n_corr) + q] = float(chi[3 * nl + r]);
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// Euler step, state layout changes
+// ------------------------------------------------------------------------------------
+__global__ void xyz_euler_kernel(float *__restrict__ x, const float *__restrict__ dx, long long n, float step) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        x[i] = __fadd_rn(x[i], __fmul_rn(step, dx[i]));
+}
+
+// stage[c * n + i] (four arrays in the reference layout) <-> v[i] (one float4 per element)
+__global__ void xyz_pack_kernel(const float *__restrict__ stage, float4 *__restrict__ v, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        v[i] = make_float4(stage[i], stage[n + i], stage[2 * n + i], stage[3 * n + i]);
+}
+__global__ void xyz_unpack_kernel(const float4 *__restrict__ v, float *__restrict__ stage, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float4 e = v[i];
+        stage[i] = e.x;
+        stage[n + i] = e.y;
+        stage[2 * n + i] = e.z;
+        stage[3 * n + i] = e.w;
+    }
+}
+
+void check_cuda(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) throw Error(ErrorType::Cuda, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <class T>
+T *dalloc(size_t count, const char *what) {
+    void *p = nullptr;
+    check_cuda(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T) + 16), what);
+    return static_cast<T *>(p);
+}
+
+template <class T>
+void h2d(T *dst, const T *src, size_t count, cudaStream_t s) {
+    if (count) check_cuda(cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync H2D");
+}
+
+int copy_grid(long long n) { return int(std::min<long long>((n + 255) / 256, 4096)); }
+
+}  // namespace
+
+struct spn_xyz {
+    int device = 0, n = 0, nl = 0, n_range = 0, n_corr = 0, n_overlap = 0, max_nodes = 0, sms = 0, grid = 0;
+    long long fn = 0;
+    float cutoff = 0.0f;
+    cudaStream_t stream = nullptr;
+    float *freq = nullptr, *v2 = nullptr, *dv2 = nullptr, *stage = nullptr, *node_wp = nullptr, *node_c = nullptr,
+          *corr_out = nullptr;
+    float4 *sd = nullptr, *dsd = nullptr;
+    int *ints = nullptr;  // all integer tables in one allocation
+    int *sites, *sites_perm, *inv_sites, *inv_sites_perm, *ov_ptr, *ov_r1, *ov_r2, *ov_p1, *ov_p2, *range_rid,
+        *range_inv, *corr_rid, *corr_perm, *node_cnt, *work_counter;
+    unsigned *status = nullptr;
+    double *partial = nullptr;
+
+    XyzArgs args() const {
+        XyzArgs a;
+        a.n = n;
+        a.nl = nl;
+        a.fn = int(fn);
+        a.max_nodes = max_nodes;
+        a.n_range = n_range;
+        a.n_corr = n_corr;
+        a.cutoff = cutoff;
+        a.freq = freq;
+        a.sd = sd;
+        a.dsd = dsd;
+        a.v2 = v2;
+        a.dv2 = dv2;
+        a.sites = sites;
+        a.sites_perm = sites_perm;
+        a.inv_sites = inv_sites;
+        a.inv_sites_perm = inv_sites_perm;
+        a.ov_ptr = ov_ptr;
+        a.ov_r1 = ov_r1;
+        a.ov_r2 = ov_r2;
+        a.ov_p1 = ov_p1;
+        a.ov_p2 = ov_p2;
+        a.range_rid = range_rid;
+        a.range_inv = range_inv;
+        a.node_wp = node_wp;
+        a.node_c = node_c;
+        a.node_cnt = node_cnt;
+        a.work_counter = work_counter;
+        a.status = status;
+        a.corr_rid = corr_rid;
+        a.corr_perm = corr_perm;
+        a.partial = partial;
+        a.out = corr_out;
+        return a;
+    }
+
+    // argument block of the SU(2) node-table body (self-energy, mesh, node tables only)
+    FlowArgs node_args() const {
+        FlowArgs f;
+        std::memset(&f, 0, sizeof(f));
+        f.n = n;
+        f.nl = nl;
+        f.max_nodes = max_nodes;
+        f.cutoff = cutoff;
+        f.freq = freq;
+        f.v2 = v2;
+        f.dv2 = dv2;
+        f.fp64_sigma = 0;
+        f.node_wp = node_wp;
+        f.node_c = node_c;
+        f.node_cnt = node_cnt;
+        f.status = status;
+        return f;
+    }
+
+    void release() {
+        cudaSetDevice(device);
+        void *ptrs[] = {freq, v2, dv2, stage, node_wp, node_c, corr_out, sd, dsd, ints, status, partial};
+        for (void *p : ptrs)
+            if (p) cudaFree(p);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+void validate(const spn_xyz_desc *d) {
+    if (!d) throw Error(ErrorType::Argument, "null descriptor");
+    if (d->n_freq < 2 || d->n_freq > kMaxFreq)
+        throw Error(ErrorType::Unsupported, "n_freq must be in [2, " + std::to_string(kMaxFreq) + "]");
+    if (d->n_sites < 1 || d->n_sites > 32 * kSpt)
+        throw Error(ErrorType::Unsupported, "n_sites must be in [1, " + std::to_string(32 * kSpt) + "]");
+    if (!d->freq || !d->sites_rid || !d->sites_perm || !d->inv_sites_rid || !d->inv_sites_perm || !d->overlap_ptr ||
+        (d->n_range > 0 && (!d->range_rid || !d->range_inv_rid)) || (d->n_corr > 0 && (!d->corr_rid || !d->corr_perm)))
+        throw Error(ErrorType::Argument, "descriptor table pointer is NULL");
+    for (int i = 0; i < d->n_freq; ++i) {
+        if (!(d->freq[i] > 0.0f)) throw Error(ErrorType::Argument, "frequencies must be positive");
+        if (i > 0 && !(d->freq[i] > d->freq[i - 1])) throw Error(ErrorType::Argument, "frequencies must be strictly ascending");
+    }
+    const long long fn = (long long)d->n_freq * d->n_freq * (d->n_freq + 1) / 2;
+    if (fn * d->n_sites >= (1ll << 31)) throw Error(ErrorType::Unsupported, "vertex larger than 2^31 elements");
+    const int nl = d->n_sites;
+    auto in_range = [&](const int *v, int cnt, int hi, const char *what) {
+        for (int i = 0; i < cnt; ++i)
+            if (v[i] < 0 || v[i] >= hi) throw Error(ErrorType::Argument, std::string(what) + " entry out of range");
+    };
+    in_range(d->sites_rid, nl, nl, "sites_rid");
+    in_range(d->inv_sites_rid, nl, nl, "inv_sites_rid");
+    in_range(d->sites_perm, nl, 6, "sites_perm");
+    in_range(d->inv_sites_perm, nl, 6, "inv_sites_perm");
+    if (d->overlap_ptr[0] != 0) throw Error(ErrorType::Argument, "overlap_ptr[0] must be 0");
+    for (int r = 0; r < nl; ++r)
+        if (d->overlap_ptr[r + 1] < d->overlap_ptr[r]) throw Error(ErrorType::Argument, "overlap_ptr must be non-decreasing");
+    const int nov = d->overlap_ptr[nl];
+    if (nov > 0 && (!d->overlap_rid1 || !d->overlap_rid2 || !d->overlap_perm1 || !d->overlap_perm2))
+        throw Error(ErrorType::Argument, "overlap pair table is NULL");
+    in_range(d->overlap_rid1, nov, nl, "overlap_rid1");
+    in_range(d->overlap_rid2, nov, nl, "overlap_rid2");
+    in_range(d->overlap_perm1, nov, 6, "overlap_perm1");
+    in_range(d->overlap_perm2, nov, 6, "overlap_perm2");
+    in_range(d->range_rid, d->n_range, nl, "range_rid");
+    in_range(d->range_inv_rid, d->n_range, nl, "range_inv_rid");
+    in_range(d->corr_rid, d->n_corr, nl, "corr_rid");
+    in_range(d->corr_perm, d->n_corr, 6, "corr_perm");
+}
+
+size_t vertex_smem() { return size_t(kWarps) * 2 * kSpt * 32 * sizeof(float4); }
+
+void launch_correlation(spn_xyz *h) {
+    const XyzArgs a = h->args();
+    xyz_corr_inner_kernel<<<2 * h->n + 4, 128, 0, h->stream>>>(a);
+    check_cuda(cudaGetLastError(), "correlation launch");
+    xyz_corr_final_kernel<<<1, 128, 4 * h->nl * sizeof(double), h->stream>>>(a);
+    check_cuda(cudaGetLastError(), "correlation final launch");
+}
+
+}  // namespace
+
+extern "C" int spn_xyz_create(const spn_xyz_desc *d, spn_xyz **out) {
+    return guarded([&] {
+        if (!out) throw Error(ErrorType::Argument, "null output handle");
+        validate(d);
+        auto *h = new spn_xyz;
+        try {
+            h->device = d->device;
+            check_cuda(cudaSetDevice(h->device), "cudaSetDevice");
+            h->n = d->n_freq;
+            h->nl = d->n_sites;
+            h->fn = (long long)h->n * h->n * (h->n + 1) / 2;
+            h->n_range = d->n_range;
+            h->n_corr = d->n_corr;
+            h->n_overlap = d->overlap_ptr[d->n_sites];
+            h->max_nodes = 2 * h->n + 8;
+            check_cuda(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+            const size_t vsz = size_t(h->fn) * h->nl;
+            h->freq = dalloc<float>(h->n, "alloc freq");
+            h->v2 = dalloc<float>(h->n, "alloc v2");
+            h->dv2 = dalloc<float>(h->n, "alloc dv2");
+            h->sd = dalloc<float4>(vsz, "alloc vertex state");
+            h->dsd = dalloc<float4>(vsz, "alloc vertex flow");
+            h->node_wp = dalloc<float>(size_t(h->n) * h->max_nodes, "alloc node table");
+            h->node_c = dalloc<float>(size_t(h->n) * h->max_nodes, "alloc node table");
+            h->corr_out = dalloc<float>(4 * size_t(h->n_corr) + 4 * h->nl, "alloc correlation output");
+            h->partial = dalloc<double>(size_t(kMaxCorrNodes) * 4 * h->nl, "alloc correlation scratch");
+            h->status = dalloc<unsigned>(1, "alloc status");
+            // integer tables, one allocation
+            const int nl = h->nl, nov = h->n_overlap, nr = h->n_range, nc = h->n_corr;
+            std::vector<int> img;
+            std::vector<size_t> at;
+            auto put = [&](const int *src, int cnt) {
+                at.push_back(img.size());
+                if (src) img.insert(img.end(), src, src + cnt);
+                else img.insert(img.end(), size_t(cnt), 0);
+            };
+            put(d->sites_rid, nl);
+            put(d->sites_perm, nl);
+            put(d->inv_sites_rid, nl);
+            put(d->inv_sites_perm, nl);
+            put(d->overlap_ptr, nl + 1);
+            put(d->overlap_rid1, nov);
+            put(d->overlap_rid2, nov);
+            put(d->overlap_perm1, nov);
+            put(d->overlap_perm2, nov);
+            put(d->range_rid, nr);
+            put(d->range_inv_rid, nr);
+            put(d->corr_rid, nc);
+            put(d->corr_perm, nc);
+            put(nullptr, h->n);  // node counts
+            put(nullptr, 1);     // work counter
+            h->ints = dalloc<int>(img.size(), "alloc lattice tables");
+            h2d(h->ints, img.data(), img.size(), h->stream);
+            int **fields[] = {&h->sites, &h->sites_perm, &h->inv_sites, &h->inv_sites_perm, &h->ov_ptr, &h->ov_r1,
+                              &h->ov_r2, &h->ov_p1, &h->ov_p2, &h->range_rid, &h->range_inv, &h->corr_rid,
+                              &h->corr_perm, &h->node_cnt, &h->work_counter};
+            for (size_t k = 0; k < at.size(); ++k) *fields[k] = h->ints + at[k];
+            h2d(h->freq, d->freq, h->n, h->stream);
+            check_cuda(cudaMemsetAsync(h->sd, 0, vsz * sizeof(float4), h->stream), "memset");
+            check_cuda(cudaMemsetAsync(h->dsd, 0, vsz * sizeof(float4), h->stream), "memset");
+            check_cuda(cudaMemsetAsync(h->v2, 0, h->n * sizeof(float), h->stream), "memset");
+            check_cuda(cudaMemsetAsync(h->dv2, 0, h->n * sizeof(float), h->stream), "memset");
+            check_cuda(cudaMemsetAsync(h->status, 0, sizeof(unsigned), h->stream), "memset");
+            check_cuda(cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device), "device attribute");
+            int per_sm = 0;
+            check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, xyz_vertex_kernel, kThreads, vertex_smem()),
+                       "occupancy");
+            if (per_sm < 1) throw Error(ErrorType::Unsupported, "XYZ vertex-flow kernel does not fit on this device");
+            h->grid = h->sms * per_sm;
+            check_cuda(cudaStreamSynchronize(h->stream), "create sync");
+        } catch (...) {
+            h->release();
+            delete h;
+            throw;
+        }
+        *out = h;
+    });
+}
+
+extern "C" int spn_xyz_destroy(spn_xyz *h) {
+    if (!h) return SPN_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    h->release();
+    delete h;
+    return SPN_OK;
+}
+
+namespace {
+float *stage_of(spn_xyz *h) {
+    if (!h->stage) h->stage = dalloc<float>(4 * size_t(h->fn) * h->nl, "alloc state stage");
+    return h->stage;
+}
+}  // namespace
+
+extern "C" int spn_xyz_set_state(spn_xyz *h, float cutoff, const float *v2, const float *xx, const float *yy, const float *zz,
+                                 const float *dd) {
+    return guarded([&] {
+        if (!h || !v2 || !xx || !yy || !zz || !dd) throw Error(ErrorType::Argument, "null argument");
+        check_cuda(cudaSetDevice(h->device), "cudaSetDevice");
+        const size_t vsz = size_t(h->fn) * h->nl;
+        float *st = stage_of(h);
+        const float *src[4] = {xx, yy, zz, dd};
+        for (int c = 0; c < 4; ++c) h2d(st + c * vsz, src[c], vsz, h->stream);
+        xyz_pack_kernel<<<copy_grid((long long)vsz), 256, 0, h->stream>>>(st, h->sd, (long long)vsz);
+        check_cuda(cudaGetLastError(), "pack launch");
+        h2d(h->v2, v2, h->n, h->stream);
+        h->cutoff = cutoff;
+        check_cuda(cudaStreamSynchronize(h->stream), "set_state sync");
+    });
+}
+
+namespace {
+void copy_out(spn_xyz *h, const float4 *src, float *const dst[4]) {
+    const size_t vsz = size_t(h->fn) * h->nl;
+    float *st = stage_of(h);
+    xyz_unpack_kernel<<<copy_grid((long long)vsz), 256, 0, h->stream>>>(src, st, (long long)vsz);
+    check_cuda(cudaGetLastError(), "unpack launch");
+    for (int c = 0; c < 4; ++c)
+        if (dst[c])
+            check_cuda(cudaMemcpyAsync(dst[c], st + c * vsz, vsz * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
+}
+}  // namespace
+
+extern "C" int spn_xyz_get_state(spn_xyz *h, float *cutoff, float *v2, float *xx, float *yy, float *zz, float *dd) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        check_cuda(cudaSetDevice(h->device), "cudaSetDevice");
+        if (cutoff) *cutoff = h->cutoff;
+        if (v2) check_cuda(cudaMemcpyAsync(v2, h->v2, h->n * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        float *const dst[4] = {xx, yy, zz, dd};
+        copy_out(h, h->sd, dst);
+        check_cuda(cudaStreamSynchronize(h->stream), "get_state sync");
+    });
+}
+
+extern "C" int spn_xyz_get_flow(spn_xyz *h, float *dv2, float *xx, float *yy, float *zz, float *dd) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        check_cuda(cudaSetDevice(h->device), "cudaSetDevice");
+        if (dv2) check_cuda(cudaMemcpyAsync(dv2, h->dv2, h->n * sizeof(float), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        float *const dst[4] = {xx, yy, zz, dd};
+        copy_out(h, h->dsd, dst);
+        check_cuda(cudaStreamSynchronize(h->stream), "get_flow sync");
+    });
+}
+
+extern "C" int spn_xyz_compute_step(spn_xyz *h) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        check_cuda(cudaSetDevice(h->device), "cudaSetDevice");
+        check_cuda(cudaMemsetAsync(h->status, 0, sizeof(unsigned), h->stream), "memset status");
+        check_cuda(cudaMemsetAsync(h->work_counter, 0, sizeof(int), h->stream), "memset counter");
+        const XyzArgs a = h->args();
+        xyz_self_energy_kernel<<<h->n, 128, 0, h->stream>>>(a);
+        check_cuda(cudaGetLastError(), "self-energy launch");
+        xyz_node_table_kernel<<<(h->n + 63) / 64, 64, 0, h->stream>>>(h->node_args());
+        check_cuda(cudaGetLastError(), "node table launch");
+        xyz_vertex_kernel<<<h->grid, kThreads, vertex_smem(), h->stream>>>(a);
+        check_cuda(cudaGetLastError(), "vertex flow launch");
+    });
+}
+
+extern "C" int spn_xyz_finalize_step(spn_xyz *h, float new_cutoff) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        check_cuda(cudaSetDevice(h->device), "cudaSetDevice");
+        const float step = new_cutoff - h->cutoff;
+        const long long n4 = 4 * h->fn * h->nl;
+        xyz_euler_kernel<<<1, 64, 0, h->stream>>>(h->v2, h->dv2, h->n, step);
+        xyz_euler_kernel<<<copy_grid(n4), 256, 0, h->stream>>>(reinterpret_cast<float *>(h->sd),
+                                                              reinterpret_cast<const float *>(h->dsd), n4, step);
+        check_cuda(cudaGetLastError(), "euler launch");
+        h->cutoff = new_cutoff;
+    });
+}
+
+extern "C" int spn_xyz_measure_correlation(spn_xyz *h, float *xx, float *yy, float *zz, float *dd, float *chi) {
+    return guarded([&] {
+        if (!h) throw Error(ErrorType::Argument, "null handle");
+        check_cuda(cudaSetDevice(h->device), "cudaSetDevice");
+        launch_correlation(h);
+        float *const dst[4] = {xx, yy, zz, dd};
+        for (int c = 0; c < 4; ++c)
+            if (dst[c])
+                check_cuda(cudaMemcpyAsync(dst[c], h->corr_out + size_t(c) * h->n_corr, h->n_corr * sizeof(float),
+                                           cudaMemcpyDeviceToHost, h->stream),
+                           "D2H");
+        if (chi)
+            check_cuda(cudaMemcpyAsync(chi, h->corr_out + 4 * size_t(h->n_corr), 4 * h->nl * sizeof(float),
+                                       cudaMemcpyDeviceToHost, h->stream),
+                       "D2H");
+        check_cuda(cudaStreamSynchronize(h->stream), "correlation sync");
+    });
+}
+
+extern "C" int spn_xyz_is_diverged(spn_xyz *h, int *diverged) {
+    return guarded([&] {
+        if (!h || !diverged) throw Error(ErrorType::Argument, "null argument");
+        check_cuda(cudaSetDevice(h->device), "cudaSetDevice");
+        unsigned st = 0;
+        check_cuda(cudaMemcpyAsync(&st, h->status, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        check_cuda(cudaStreamSynchronize(h->stream), "status sync");
+        if (st & kStatusNodeOverflow) throw Error(ErrorType::Device, "loop-frequency node table overflow");
+        *diverged = (st & kStatusNaN) ? 1 : 0;
+    });
+}
