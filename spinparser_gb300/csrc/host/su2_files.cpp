@@ -45,8 +45,8 @@ std::string fmt_cutoff(float c) { return std::to_string(c); }
 
 }  // namespace
 
-int write_checkpoint(const std::string &path, bool append, float cutoff, const float *v2, int64_t n_v2,
-                     const float *v4ss, const float *v4dd, int64_t n_v4) {
+int write_checkpoint_arrays(const std::string &path, bool append, float cutoff, const float *v2, int64_t n_v2,
+                            const std::vector<std::pair<std::string, const float *>> &v4, int64_t n_v4) {
     const bool existing = append && h5::File::is_hdf5(path);
     h5::File file;
     if (existing) file = h5::File::open(path);
@@ -59,15 +59,14 @@ int write_checkpoint(const std::string &path, bool append, float cutoff, const f
     g.attrs.push_back(cutoff_attr(cutoff));
     g.datasets.push_back(vector_dataset("cutoff", &cutoff, 1));
     g.datasets.push_back(vector_dataset("v2", v2, n_v2));
-    g.datasets.push_back(vector_dataset("v4dd", v4dd, n_v4));
-    g.datasets.push_back(vector_dataset("v4ss", v4ss, n_v4));
+    for (const auto &a : v4) g.datasets.push_back(vector_dataset(a.first, a.second, n_v4));
     if (existing) h5::append_file(file, file.root);
     else h5::write_file(path, file.root);
     return id;
 }
 
-bool read_checkpoint(const std::string &path, int id, float &cutoff, float *v2, int64_t n_v2, float *v4ss,
-                     float *v4dd, int64_t n_v4) {
+bool read_checkpoint_arrays(const std::string &path, int id, float &cutoff, float *v2, int64_t n_v2,
+                            const std::vector<std::pair<std::string, float *>> &v4, int64_t n_v4) {
     if (!h5::File::is_hdf5(path)) throw Error(ErrorType::IO, "Could not open data file for reading");
     h5::File file = h5::File::open(path);
     std::string name;
@@ -83,14 +82,15 @@ bool read_checkpoint(const std::string &path, int id, float &cutoff, float *v2, 
     }
     h5::Group *g = file.root.group(name);
     if (!g) return false;
-    struct Want { const char *name; float *dst; int64_t n; };
+    struct Want { std::string name; float *dst; int64_t n; };
     float c = 0;
-    const Want wants[] = {{"cutoff", &c, 1}, {"v2", v2, n_v2}, {"v4dd", v4dd, n_v4}, {"v4ss", v4ss, n_v4}};
+    std::vector<Want> wants = {{"cutoff", &c, 1}, {"v2", v2, n_v2}};
+    for (const auto &a : v4) wants.push_back({a.first, a.second, n_v4});
     for (const Want &w : wants) {
         h5::Dataset *d = g->dataset(w.name);
         if (!d) return false;
         if (int64_t(d->count()) != w.n)
-            throw Error(ErrorType::Argument, std::string("checkpoint dataset '") + w.name + "' holds " + std::to_string(d->count()) +
+            throw Error(ErrorType::Argument, "checkpoint dataset '" + w.name + "' holds " + std::to_string(d->count()) +
                                                  " values, the flow has " + std::to_string(w.n));
     }
     for (const Want &w : wants) {
@@ -100,6 +100,17 @@ bool read_checkpoint(const std::string &path, int id, float &cutoff, float *v2, 
     }
     cutoff = c;
     return true;
+}
+
+// SU2EffectiveAction::writeCheckpoint writes v2, v4dd, v4ss (src/SU2/SU2EffectiveAction.hpp:141-144)
+int write_checkpoint(const std::string &path, bool append, float cutoff, const float *v2, int64_t n_v2,
+                     const float *v4ss, const float *v4dd, int64_t n_v4) {
+    return write_checkpoint_arrays(path, append, cutoff, v2, n_v2, {{"v4dd", v4dd}, {"v4ss", v4ss}}, n_v4);
+}
+
+bool read_checkpoint(const std::string &path, int id, float &cutoff, float *v2, int64_t n_v2, float *v4ss,
+                     float *v4dd, int64_t n_v4) {
+    return read_checkpoint_arrays(path, id, cutoff, v2, n_v2, {{"v4dd", v4dd}, {"v4ss", v4ss}}, n_v4);
 }
 
 ObsMeta make_obs_meta(const Lattice &L) {

@@ -1,4 +1,4 @@
-// SU(2) checkpoints and observable files in the reference's HDF5 layout.
+// Checkpoints and observable files of the SU(2) and XYZ cores in the reference's HDF5 layout.
 //
 // Checkpoints: SU2EffectiveAction::writeCheckpoint / readCheckpoint
 // (src/SU2/SU2EffectiveAction.hpp:79-200).  Observables: SU2MeasurementCorrelation's
@@ -7,12 +7,21 @@
 #include <cstdint>
 #include <map>
 #include <string>
+#include <utility>
 #include <vector>
 #include "h5.hpp"
 
 namespace spn {
 
 struct Lattice;
+
+// A checkpoint group holds "cutoff", "v2" and the named vertex arrays in the given order
+// (SU(2): v4dd, v4ss; XYZ: v4dd, v4xx, v4yy, v4zz -- XYZEffectiveAction.hpp:144-149).
+// Returns the checkpoint id written, or -1 if the file holds a checkpoint at `cutoff`.
+int write_checkpoint_arrays(const std::string &path, bool append, float cutoff, const float *v2, int64_t n_v2,
+                            const std::vector<std::pair<std::string, const float *>> &v4, int64_t n_v4);
+bool read_checkpoint_arrays(const std::string &path, int id, float &cutoff, float *v2, int64_t n_v2,
+                            const std::vector<std::pair<std::string, float *>> &v4, int64_t n_v4);
 
 // Returns the checkpoint id written, or -1 if the file holds a checkpoint at `cutoff`.
 int write_checkpoint(const std::string &path, bool append, float cutoff, const float *v2, int64_t n_v2,

@@ -20,6 +20,7 @@ Outputs (committed, so the tests need no reference tree at run time):
                           (hyperhoneycomb r=3 Heisenberg-Kitaev j=0.1, k=-1, 14 manual
                           frequencies, cutoff 10 -> 0.3 x0.9), read from
                           test/scripted/assets/test_reference2.ref (XYZCorXX/YY/ZZ/DD)
+  reference2_layout.json  member structure and HDF5 encoding fingerprint of test_reference2.ref
   res_hyperhoneycomb/     the hyperhoneycomb unit cell and Heisenberg-Kitaev model of the
                           reference's res/ files (the input of test_reference2)
 
@@ -113,6 +114,8 @@ def write_reference2(ref_root: str) -> None:
                         cutoff_spec=np.array([p["cutoff_max"], p["cutoff_min"], p["cutoff_step"]], np.float32),
                         j=np.float32(p["j"]), k=np.float32(k), sites=meta["sites"].read(), basis=meta["basis"].read(),
                         lattice_vectors=meta["latticeVectors"].read())
+    with open(os.path.join(HERE, "reference2_layout.json"), "w") as f:
+        json.dump({"fingerprint": h5lite.layout_fingerprint(ref), "skeleton": h5lite.skeleton(ref)}, f, indent=0)
     out = os.path.join(HERE, "res_hyperhoneycomb")
     os.makedirs(out, exist_ok=True)
     head = '<?xml version="1.0" encoding="utf-8"?>\n'

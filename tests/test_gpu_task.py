@@ -161,3 +161,63 @@ def test_measurement_cutoff_window_and_fp64_self_energy(tmp_path):
     task.run_task(p, verbose=-1, fp64_self_energy=True)
     cut, _ = h5lite.read_correlations(str(tmp_path / "w.obs"), "SU2CorZZ")
     assert len(cut) > 0 and cut.max() <= 5.0 and cut.min() >= 1.0
+
+
+# ---------------------------------------------------------------------------------------
+# XYZ core through the driver (test_reference2.sh, XYZ task)
+# ---------------------------------------------------------------------------------------
+REF2_RES = os.path.join(GOLDEN, "res_hyperhoneycomb")
+
+
+def reference2_task(tmp_path, name="r2.xml", cutoff=None, extra=""):
+    g = np.load(os.path.join(GOLDEN, "reference2_xyz.npz"))
+    cmax, cmin, step = (float(x) for x in g["cutoff_spec"])
+    cut = cutoff or exponential_cutoffs(f"{cmax:g}", f"{cmin:g}", f"{step:g}")
+    return write(tmp_path, name, lattice="hyperhoneycomb", rng=3, model="hyperhoneycomb-kitaev", symmetry="XYZ",
+                 params=f"<j>{float(g['j']):g}</j><k>{float(g['k']):g}</k>", freq=manual_frequencies(), cutoff=cut,
+                 extra=extra), g
+
+
+def test_reference2_xyz_task_reproduces_golden_obs(tmp_path):
+    p, g = reference2_task(tmp_path)
+    s = task.run_task(p, resource_path=REF2_RES, verbose=-1)
+    assert s.status == "finished" and not s.diverged and s.steps == len(g["cutoffs"]) - 1
+    obs = str(tmp_path / "r2.obs")
+    layout = json.load(open(os.path.join(GOLDEN, "reference2_layout.json")))
+    assert h5lite.skeleton(obs) == layout["skeleton"]
+    assert h5lite.layout_fingerprint(obs) == layout["fingerprint"]
+    for group, key in (("XYZCorXX", "xx"), ("XYZCorYY", "yy"), ("XYZCorZZ", "zz"), ("XYZCorDD", "dd")):
+        cut, data = h5lite.read_correlations(obs, group)
+        assert np.array_equal(cut, g["cutoffs"])
+        assert float(np.abs(data - g[key]).max()) < 1e-5, group
+    # the checkpoint holds the XYZ arrays in the reference's order
+    ck = h5lite.open_file(str(tmp_path / "r2.checkpoint"))["checkpoint_0"]
+    assert ck.keys() == ["cutoff", "v2", "v4dd", "v4xx", "v4yy", "v4zz"]
+
+
+def test_reference2_xyz_sign_flip_fails_golden(tmp_path):
+    """test_referenceFail.sh in XYZ form: k -> -k must not reproduce the golden values."""
+    g = np.load(os.path.join(GOLDEN, "reference2_xyz.npz"))
+    p = write(tmp_path, "f.xml", lattice="hyperhoneycomb", rng=3, model="hyperhoneycomb-kitaev", symmetry="XYZ",
+              params=f"<j>{float(g['j']):g}</j><k>{-float(g['k']):g}</k>", freq=manual_frequencies(),
+              cutoff=exponential_cutoffs("10", "0.3", "0.9"))
+    task.run_task(p, resource_path=REF2_RES, verbose=-1)
+    _, data = h5lite.read_correlations(str(tmp_path / "f.obs"), "XYZCorXX")
+    assert float(np.abs(data - g["xx"]).max()) > 1e-3
+
+
+def test_xyz_checkpoint_resume_equals_uninterrupted_run(tmp_path):
+    full, _ = reference2_task(tmp_path, "full.xml")
+    part, _ = reference2_task(tmp_path, "part.xml", cutoff=exponential_cutoffs("10", "0.5", "0.9"))
+    task.run_task(full, resource_path=REF2_RES, force_restart=True, verbose=-1)
+    first = task.run_task(part, resource_path=REF2_RES, force_restart=True, verbose=-1)
+    assert first.status == "finished"
+    reference2_task(tmp_path, "part.xml", extra='<calculation status="running" startTime="1970-Jan-01 00:00:00" '
+                                                'checkpointTime="1970-Jan-01 00:00:00" />')
+    second = task.run_task(part, resource_path=REF2_RES, verbose=-1)
+    assert second.status == "finished" and 0 < second.steps < first.steps
+    a, b = str(tmp_path / "full.obs"), str(tmp_path / "part.obs")
+    for group in ("XYZCorXX", "XYZCorYY", "XYZCorZZ", "XYZCorDD"):
+        ca, da = h5lite.read_correlations(a, group)
+        cb, db = h5lite.read_correlations(b, group)
+        assert np.array_equal(ca, cb) and np.array_equal(da, db)

@@ -61,7 +61,7 @@ def test_cli_debug_lattice(tmp_path, capfd):
     (dict(params="<j>1.0</j><colour>red</colour>"), -3, "Unknown spin model option 'colour'."),
     (dict(params=""), -3, "Interaction parameter 'j' is not defined in the taskfile"),
     (dict(symmetry="U1"), -2, "Spin model identifier 'U1' does not exist."),
-    (dict(symmetry="XYZ"), -8, "only the SU2 core runs on the GPU"),
+    (dict(symmetry="TRI"), -8, "the TRI core is not part of this build"),
     (dict(lattice="nonexistent"), -3, "nonexistent"),
 ])
 def test_task_validation_errors(tmp_path, kw, code, message):
