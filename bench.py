@@ -58,6 +58,12 @@ MULTI_WORKLOADS = ("scan-square-j1j2-128", "serve-mixed")
 # precision study: the single-flow workload run to the end in FP32 forms and in FP64 on the GPU
 PRECISION_WORKLOADS = {"precision-cubic-j1j2-r6-n64": "cubic-j1j2-r6-n64",
                        "precision-pyrochlore-r5-n64": "pyrochlore-r5-n64"}
+# the XYZ core (models with diagonal couplings): a Heisenberg-Kitaev flow
+XYZ_WORKLOADS = {
+    "xyz-honeycomb-kitaev-r9-n48": dict(lattice="honeycomb", range=9, model="honeycomb-kitaev",
+                                        params={"j": "0.1", "k": "-1.0"}, n_freq=48, fmin=0.005, fmax=50.0,
+                                        cmax=50.0, cmin=0.05, cstep=0.98),
+}
 METRIC = "cutoff steps/s per flow"
 KERNELS_PER_STEP = 8  # self-energy, node tables, vertex flow, 2 x correlation, 3 x Euler
 
@@ -68,8 +74,8 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + list(MULTI_WORKLOADS) + list(PRECISION_WORKLOADS),
-                    default=DEFAULT_WORKLOAD)
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + list(MULTI_WORKLOADS) + list(PRECISION_WORKLOADS) +
+                    list(XYZ_WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--flows", type=int, default=None, help="multi-flow workloads: number of flows / requests")
     ap.add_argument("--rates", type=str, default="0.5,1,2,4,inf",
                     help="serve-mixed: arrival rates as multiples of the sequential plain-GPU capacity")
@@ -451,8 +457,68 @@ def run_precision(args):
     print(json.dumps(line))
 
 
+def run_xyz(args):
+    """The XYZ core: one whole flow on the GPU (device-resident state, measurement at every
+    cutoff, as the driver runs it), against the XYZ oracle on the host cores (two right-hand
+    sides at cutoffs a third and two thirds into the flow, extrapolated to the flow)."""
+    import torch
+
+    import spinparser_gb300 as spn
+
+    torch.cuda.set_device(0)
+    wl = XYZ_WORKLOADS[args.workload]
+    lat = spn.Lattice(wl["lattice"], wl["range"], wl["model"], wl["params"])
+    tab, st = lat.tables(), lat.spin_tables()
+    freq = spn.frequency_exponential(wl["fmin"], wl["fmax"], wl["n_freq"])
+    cut = spn.cutoff_exponential(wl["cmax"], wl["cmin"], wl["cstep"])
+    init = spn.xyz_initial_state(lat, len(freq))
+    flow = spn.XyzFlow(tab, st, freq)
+    warm = max(args.warmup, 3)
+    flow.run(cut[:warm + 1], *init)  # untimed warm-up
+    sampler = ClockSampler(0)
+    sampler.start()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    measured, corr, diverged = flow.run(cut, *init)
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
+    clocks = sampler.stop()
+    steps = len(measured) - 1
+    line = {
+        "metric": "cutoff steps/s per flow (XYZ core)", "value": steps / secs, "unit": "steps/s", "n_gpus": 1,
+        "steps": steps, "warmup": warm, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (model initial condition, advanced by the flow)",
+        "config": {"workload": args.workload, **{k: wl[k] for k in ("lattice", "range", "model", "params", "n_freq")},
+                   "cutoff": [wl["cmax"], wl["cmin"], wl["cstep"]], "n_cutoffs": len(cut), "n_sites": tab.n_sites,
+                   "n_overlap": tab.n_overlap, "timed": "the whole flow, measurement at every cutoff"},
+        "diverged": diverged, "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        from oracle import XyzOracle
+
+        orc = XyzOracle(tab, st, freq)
+        _, v2, v4 = flow.get_state()
+        threads = os.cpu_count() or 1
+        samples = []
+        for frac in (1 / 3, 2 / 3):
+            c = float(cut[int(frac * (len(cut) - 1))])
+            t1 = time.perf_counter()
+            orc.rhs(c, v2, v4, threads=threads)
+            samples.append(time.perf_counter() - t1)
+        per_step = float(np.mean(samples))
+        line["cpu_baseline"] = {"value": 1.0 / per_step, "unit": "steps/s", "cores": threads, "kind": "port",
+                                "sample": "two full right-hand sides of the XYZ oracle at the final state, cutoffs a "
+                                          "third and two thirds into the list; %.2f s per step" % per_step}
+    print(json.dumps(line))
+    flow.close()
+
+
 def main():
     args = parse_args()
+    if args.workload in XYZ_WORKLOADS:
+        run_xyz(args)
+        return
     if args.workload in MULTI_WORKLOADS:
         run_multi(args)
         return

@@ -12,9 +12,12 @@
 //
 // A step: the self-energy flow (one CTA per frequency), the loop-frequency node tables (the
 // SU(2) core's, shared), the vertex flow and the Euler update.  The vertex-flow kernel runs a
-// persistent grid whose warps take one (s,t,u) triple at a time from a device counter; the
-// lanes hold the sites (up to four each), the channel's nodes are visited in order, and the t
-// channel's RPA sum exchanges the first two slabs of a node through shared memory.
+// persistent grid whose warps take one (s,t,u) triple at a time from a device counter.  Per
+// channel, nodes go in batches of 32: first each lane builds one node's access buffers (and
+// the t channel's site-local values) into a shared-memory descriptor, then the lanes hold
+// the sites (up to four each) and walk the batch's nodes in order.  The t channel's RPA sum
+// exchanges the first two slabs of a node through shared memory in all six spin
+// permutations, so a pair (rid1, rid2, perm1, perm2) is two 16-byte loads and four FMAs.
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cstring>
@@ -54,6 +57,7 @@ struct XyzArgs {
     float *dv2;
     const int *sites, *sites_perm, *inv_sites, *inv_sites_perm;
     const int *ov_ptr, *ov_r1, *ov_r2, *ov_p1, *ov_p2;
+    const int *ov_pk;  // rid1 | rid2 << 7 | perm1 << 14 | perm2 << 17 per pair
     const int *range_rid, *range_inv;
     const float *node_wp, *node_c;
     const int *node_cnt;
@@ -180,14 +184,89 @@ __device__ __forceinline__ float4 u_terms(const float4 &a, const float4 &b) {
     return r;
 }
 
+// v with X, Y, Z replaced by components perm[p][0..2] of v (density unchanged).
+template <int P>
+__device__ __forceinline__ float4 permuted(const float4 &v) {
+    constexpr int c0 = int((kPermBits >> (6 * P)) & 3ull), c1 = int((kPermBits >> (6 * P + 2)) & 3ull),
+                  c2 = int((kPermBits >> (6 * P + 4)) & 3ull);
+    return make_float4(comp_of(v, c0), comp_of(v, c1), comp_of(v, c2), v.w);
+}
+
+// Node descriptor (lane = node in phase A): the four access buffers of the node and, for the
+// t channel, the four site-local values (getValueLocal of ab4..ab7, four components each).
+struct __align__(16) XDesc {
+    int4 off[4];
+    float4 w[4], sw[4];
+    float4 lv[4];
+    int exch;  // bit i: buffer i reads the site-exchanged pairs
+    float c;   // node coefficient
+    int pad[2];
+};
+
+__device__ __forceinline__ void put_desc(XDesc &d, int i, const AB4 &ab) {
+    d.off[i] = make_int4(ab.off[0], ab.off[1], ab.off[2], ab.off[3]);
+    d.w[i] = make_float4(ab.w[0], ab.w[1], ab.w[2], ab.w[3]);
+    d.sw[i] = make_float4(ab.sw[0], ab.sw[1], ab.sw[2], ab.sw[3]);
+}
+
+// Phase A: the descriptor of one node of channel ch (0 = s, 1 = t, 2 = u).  The channel's own
+// coordinate is a mesh value, so its offset is the triple's index e.
+__device__ __forceinline__ void make_xdesc(const XyzArgs &a, const float *pos, int ch, int e, float s, float t, float u,
+                                           float w1p, float w1, float w2p, float w2, float wp, float c, XDesc &d) {
+    const MeshSearch<float> m{pos, a.n};
+    const int nl = a.nl;
+    AB4 ab;
+    int ex = 0;
+    if (ch == 0) {  // integralKernelS, XYZFrgCore.cpp:218-224
+        access4m<kS>(m, nl, s, -w1 - wp, -w2 - wp, ab, e); put_desc(d, 0, ab); ex |= ab.exch << 0;
+        access4m<kS>(m, nl, s, w1p + wp, -w2p - wp, ab, e); put_desc(d, 1, ab); ex |= ab.exch << 1;
+        access4m<kS>(m, nl, s, w2 + wp, w1 + wp, ab, e); put_desc(d, 2, ab); ex |= ab.exch << 2;
+        access4m<kS>(m, nl, s, -w2p - wp, w1p + wp, ab, e); put_desc(d, 3, ab); ex |= ab.exch << 3;
+    } else if (ch == 1) {  // integralKernelT, XYZFrgCore.cpp:268-276, 323-345
+        access4m<kT>(m, nl, w1 - wp, t, w1p + wp, ab, e); put_desc(d, 0, ab); ex |= ab.exch << 0;
+        access4m<kT>(m, nl, w2p - wp, t, -w2 - wp, ab, e); put_desc(d, 1, ab); ex |= ab.exch << 1;
+        access4m<kT>(m, nl, w1p + wp, t, w1 - wp, ab, e); put_desc(d, 2, ab); ex |= ab.exch << 2;
+        access4m<kT>(m, nl, w2 + wp, t, wp - w2p, ab, e); put_desc(d, 3, ab); ex |= ab.exch << 3;
+        access4m<kU>(m, nl, w2p - wp, -w2 - wp, t, ab, e); d.lv[0] = local4(a, ab);
+        access4m<kU>(m, nl, w1 - wp, -w1p - wp, -t, ab, e); d.lv[1] = local4(a, ab);
+        access4m<kU>(m, nl, w2 + wp, wp - w2p, t, ab, e); d.lv[2] = local4(a, ab);
+        access4m<kU>(m, nl, w1p + wp, wp - w1, -t, ab, e); d.lv[3] = local4(a, ab);
+    } else {  // integralKernelU, XYZFrgCore.cpp:424-430
+        access4m<kU>(m, nl, w1 + wp, wp - w2p, u, ab, e); put_desc(d, 0, ab); ex |= ab.exch << 0;
+        access4m<kU>(m, nl, w1p + wp, w2 - wp, u, ab, e); put_desc(d, 1, ab); ex |= ab.exch << 1;
+        access4m<kU>(m, nl, w2p - wp, -w1 - wp, u, ab, e); put_desc(d, 2, ab); ex |= ab.exch << 2;
+        access4m<kU>(m, nl, w2 - wp, w1p + wp, u, ab, e); put_desc(d, 3, ab); ex |= ab.exch << 3;
+    }
+    d.exch = ex;
+    d.c = c;
+}
+
+// Phase B gather of buffer i of a descriptor (see gather4).
+__device__ __forceinline__ void gather_desc(const XyzArgs &a, const XDesc &d, int i, const Lane4 &ln, float4 *out) {
+    AB4 ab;
+    const int4 o = d.off[i];
+    const float4 w = d.w[i], sw = d.sw[i];
+    ab.off[0] = o.x; ab.off[1] = o.y; ab.off[2] = o.z; ab.off[3] = o.w;
+    ab.w[0] = w.x; ab.w[1] = w.y; ab.w[2] = w.z; ab.w[3] = w.w;
+    ab.sw[0] = sw.x; ab.sw[1] = sw.y; ab.sw[2] = sw.z; ab.sw[3] = sw.w;
+    ab.exch = (d.exch >> i) & 1;
+    gather4(a, ab, ln, out);
+}
+
+constexpr int kXBatch = 32;  // nodes whose descriptors a warp builds at once
+
 __global__ void __launch_bounds__(kThreads) xyz_vertex_kernel(XyzArgs a) {
     __shared__ float pos[kMaxFreq];
-    extern __shared__ float4 xs[];  // per warp: A[kSpt*32], B[kSpt*32] (first two t slabs)
+    // per warp: kXBatch node descriptors, then the first two t slabs of every site in all six
+    // spin permutations, A6[p][nl] and B6[p][nl]
+    extern __shared__ float4 xs[];
     for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int n = a.n, nl = a.nl;
-    float4 *As = xs + size_t(warp) * 2 * kSpt * 32, *Bs = As + kSpt * 32;
+    const int warp_f4 = kXBatch * int(sizeof(XDesc) / sizeof(float4)) + 12 * nl;
+    XDesc *desc = reinterpret_cast<XDesc *>(xs + size_t(warp) * warp_f4);
+    float4 *A6 = xs + size_t(warp) * warp_f4 + kXBatch * (sizeof(XDesc) / sizeof(float4)), *B6 = A6 + 6 * nl;
     Lane4 ln;
 #pragma unroll
     for (int k = 0; k < kSpt; ++k) {
@@ -222,120 +301,129 @@ __global__ void __launch_bounds__(kThreads) xyz_vertex_kernel(XyzArgs a) {
             const int cnt = a.node_cnt[xi];
             const float *nwp = a.node_wp + size_t(xi) * a.max_nodes;
             const float *nc = a.node_c + size_t(xi) * a.max_nodes;
-            for (int b = 0; b < cnt; ++b) {
-                const float wp = nwp[b], c = nc[b];
-                AB4 ab;
-                float4 S0[kSpt], S1[kSpt], S2[kSpt], S3[kSpt], r[kSpt];
-                if (ch == 0) {  // integralKernelS, XYZFrgCore.cpp:215-262
-                    access4<kS>(pos, n, nl, s, -w1 - wp, -w2 - wp, ab); gather4(a, ab, ln, S0);
-                    access4<kS>(pos, n, nl, s, w1p + wp, -w2p - wp, ab); gather4(a, ab, ln, S1);
-                    access4<kS>(pos, n, nl, s, w2 + wp, w1 + wp, ab); gather4(a, ab, ln, S2);
-                    access4<kS>(pos, n, nl, s, -w2p - wp, w1p + wp, ab); gather4(a, ab, ln, S3);
+            for (int b0 = 0; b0 < cnt; b0 += kXBatch) {
+                const int nb = min(kXBatch, cnt - b0);
+                if (lane < nb)  // phase A: lane = node
+                    make_xdesc(a, pos, ch, xi, s, t, u, w1p, w1, w2p, w2, nwp[b0 + lane], nc[b0 + lane], desc[lane]);
+                __syncwarp();
+                for (int b = 0; b < nb; ++b) {  // phase B: lane = site
+                    const XDesc &d = desc[b];
+                    float4 S0[kSpt], S1[kSpt], S2[kSpt], S3[kSpt], r[kSpt];
+                    gather_desc(a, d, 0, ln, S0);
+                    gather_desc(a, d, 1, ln, S1);
+                    gather_desc(a, d, 2, ln, S2);
+                    gather_desc(a, d, 3, ln, S3);
+                    if (ch == 0) {  // XYZFrgCore.cpp:229-261
 #pragma unroll
-                    for (int k = 0; k < kSpt; ++k) {
-                        const float4 p = s_terms(S0[k], S1[k]), q = s_terms(S2[k], S3[k]);
-                        r[k] = make_float4(p.x + q.x, p.y + q.y, p.z + q.z, p.w + q.w);
-                    }
-                } else if (ch == 2) {  // integralKernelU, XYZFrgCore.cpp:420-470
-                    access4<kU>(pos, n, nl, w1 + wp, wp - w2p, u, ab); gather4(a, ab, ln, S0);
-                    access4<kU>(pos, n, nl, w1p + wp, w2 - wp, u, ab); gather4(a, ab, ln, S1);
-                    access4<kU>(pos, n, nl, w2p - wp, -w1 - wp, u, ab); gather4(a, ab, ln, S2);
-                    access4<kU>(pos, n, nl, w2 - wp, w1p + wp, u, ab); gather4(a, ab, ln, S3);
-#pragma unroll
-                    for (int k = 0; k < kSpt; ++k) {
-                        const float4 p = u_terms(S0[k], S1[k]), q = u_terms(S2[k], S3[k]);
-                        r[k] = make_float4(p.x + q.x, p.y + q.y, p.z + q.z, p.w + q.w);
-                    }
-                } else {  // integralKernelT, XYZFrgCore.cpp:264-418
-                    access4<kT>(pos, n, nl, w1 - wp, t, w1p + wp, ab); gather4(a, ab, ln, S0);
-                    access4<kT>(pos, n, nl, w2p - wp, t, -w2 - wp, ab); gather4(a, ab, ln, S1);
-                    access4<kT>(pos, n, nl, w1p + wp, t, w1 - wp, ab); gather4(a, ab, ln, S2);
-                    access4<kT>(pos, n, nl, w2 + wp, t, wp - w2p, ab); gather4(a, ab, ln, S3);
-                    // RPA: the first two slabs of all sites through shared memory
-#pragma unroll
-                    for (int k = 0; k < kSpt; ++k)
-                        if (ln.valid[k]) {
-                            As[ln.j[k]] = S0[k];
-                            Bs[ln.j[k]] = S1[k];
+                        for (int k = 0; k < kSpt; ++k) {
+                            const float4 p = s_terms(S0[k], S1[k]), q = s_terms(S2[k], S3[k]);
+                            r[k] = make_float4(p.x + q.x, p.y + q.y, p.z + q.z, p.w + q.w);
                         }
-                    __syncwarp();
-                    float4 cb, ica, cb2, ica2;
-                    access4<kU>(pos, n, nl, w2p - wp, -w2 - wp, t, ab); cb = local4(a, ab);
-                    access4<kU>(pos, n, nl, w1 - wp, -w1p - wp, -t, ab); ica = local4(a, ab);
-                    access4<kU>(pos, n, nl, w2 + wp, wp - w2p, t, ab); cb2 = local4(a, ab);
-                    access4<kU>(pos, n, nl, w1p + wp, wp - w1, -t, ab); ica2 = local4(a, ab);
-                    const float cbv[4] = {cb.x, cb.y, cb.z, cb.w}, icav[4] = {ica.x, ica.y, ica.z, ica.w};
-                    const float cb2v[4] = {cb2.x, cb2.y, cb2.z, cb2.w}, ica2v[4] = {ica2.x, ica2.y, ica2.z, ica2.w};
+                    } else if (ch == 2) {  // XYZFrgCore.cpp:436-469
 #pragma unroll
-                    for (int k = 0; k < kSpt; ++k) {
-                        float rp[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-                        if (ln.valid[k]) {
-                            const int rid = ln.j[k];
-                            for (int i = a.ov_ptr[rid]; i < a.ov_ptr[rid + 1]; ++i) {
-                                const float4 x1 = As[a.ov_r1[i]], x2 = Bs[a.ov_r2[i]];
-                                const int p1 = a.ov_p1[i], p2 = a.ov_p2[i];
+                        for (int k = 0; k < kSpt; ++k) {
+                            const float4 p = u_terms(S0[k], S1[k]), q = u_terms(S2[k], S3[k]);
+                            r[k] = make_float4(p.x + q.x, p.y + q.y, p.z + q.z, p.w + q.w);
+                        }
+                    } else {  // t channel: RPA over the first two slabs of all sites, then local terms
 #pragma unroll
-                                for (int cc = 0; cc < 3; ++cc) rp[cc] += comp_of(x1, perm_c(p1, cc)) * comp_of(x2, perm_c(p2, cc));
-                                rp[3] += x1.w * x2.w;
+                        for (int k = 0; k < kSpt; ++k)
+                            if (ln.valid[k]) {
+                                const int j = ln.j[k];
+                                A6[0 * nl + j] = permuted<0>(S0[k]);
+                                A6[1 * nl + j] = permuted<1>(S0[k]);
+                                A6[2 * nl + j] = permuted<2>(S0[k]);
+                                A6[3 * nl + j] = permuted<3>(S0[k]);
+                                A6[4 * nl + j] = permuted<4>(S0[k]);
+                                A6[5 * nl + j] = permuted<5>(S0[k]);
+                                B6[0 * nl + j] = permuted<0>(S1[k]);
+                                B6[1 * nl + j] = permuted<1>(S1[k]);
+                                B6[2 * nl + j] = permuted<2>(S1[k]);
+                                B6[3 * nl + j] = permuted<3>(S1[k]);
+                                B6[4 * nl + j] = permuted<4>(S1[k]);
+                                B6[5 * nl + j] = permuted<5>(S1[k]);
                             }
-                        }
-                        const float a0[4] = {S0[k].x, S0[k].y, S0[k].z, S0[k].w}, a1[4] = {S1[k].x, S1[k].y, S1[k].z, S1[k].w};
-                        const float a2[4] = {S2[k].x, S2[k].y, S2[k].z, S2[k].w}, a3[4] = {S3[k].x, S3[k].y, S3[k].z, S3[k].w};
-                        float rv[4];
+                        __syncwarp();
+                        const float4 cb = d.lv[0], ica = d.lv[1], cb2 = d.lv[2], ica2 = d.lv[3];
+                        const float cbv[4] = {cb.x, cb.y, cb.z, cb.w}, icav[4] = {ica.x, ica.y, ica.z, ica.w};
+                        const float cb2v[4] = {cb2.x, cb2.y, cb2.z, cb2.w}, ica2v[4] = {ica2.x, ica2.y, ica2.z, ica2.w};
 #pragma unroll
-                        for (int cc = 0; cc < 3; ++cc) {  // XYZFrgCore.cpp:347-401
-                            const int pA = cc == X ? Y : X, pB = cc == Z ? Y : Z;
-                            const int qA = cc == Z ? X : Z, qB = cc == X ? Y : (cc == Y ? X : Y);
-                            float v = 4.0f * rp[cc];
-                            v -= a0[cc] * cbv[D];
-                            v += a0[cc] * cbv[pA];
-                            v += a0[cc] * cbv[pB];
-                            v -= a0[cc] * cbv[cc];
-                            v -= icav[D] * a1[cc];
-                            v += icav[qA] * a1[cc];
-                            v += icav[qB] * a1[cc];
-                            v -= icav[cc] * a1[cc];
-                            v -= a2[cc] * cb2v[D];
-                            v += a2[cc] * cb2v[pA];
-                            v += a2[cc] * cb2v[pB];
-                            v -= a2[cc] * cb2v[cc];
-                            v -= ica2v[D] * a3[cc];
-                            v += ica2v[qA] * a3[cc];
-                            v += ica2v[qB] * a3[cc];
-                            v -= ica2v[cc] * a3[cc];
-                            rv[cc] = v;
+                        for (int k = 0; k < kSpt; ++k) {
+                            float rp[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                            if (ln.valid[k]) {  // XYZFrgCore.cpp:282-305
+                                const int rid = ln.j[k];
+                                for (int i = a.ov_ptr[rid]; i < a.ov_ptr[rid + 1]; ++i) {
+                                    const int e = __ldg(a.ov_pk + i);
+                                    const float4 x1 = A6[((e >> 14) & 7) * nl + (e & 127)];
+                                    const float4 x2 = B6[((e >> 17) & 7) * nl + ((e >> 7) & 127)];
+                                    rp[0] += x1.x * x2.x;
+                                    rp[1] += x1.y * x2.y;
+                                    rp[2] += x1.z * x2.z;
+                                    rp[3] += x1.w * x2.w;
+                                }
+                            }
+                            const float a0[4] = {S0[k].x, S0[k].y, S0[k].z, S0[k].w};
+                            const float a1[4] = {S1[k].x, S1[k].y, S1[k].z, S1[k].w};
+                            const float a2[4] = {S2[k].x, S2[k].y, S2[k].z, S2[k].w};
+                            const float a3[4] = {S3[k].x, S3[k].y, S3[k].z, S3[k].w};
+                            float rv[4];
+#pragma unroll
+                            for (int cc = 0; cc < 3; ++cc) {  // XYZFrgCore.cpp:347-401
+                                const int pA = cc == X ? Y : X, pB = cc == Z ? Y : Z;
+                                const int qA = cc == Z ? X : Z, qB = cc == X ? Y : (cc == Y ? X : Y);
+                                float v = 4.0f * rp[cc];
+                                v -= a0[cc] * cbv[D];
+                                v += a0[cc] * cbv[pA];
+                                v += a0[cc] * cbv[pB];
+                                v -= a0[cc] * cbv[cc];
+                                v -= icav[D] * a1[cc];
+                                v += icav[qA] * a1[cc];
+                                v += icav[qB] * a1[cc];
+                                v -= icav[cc] * a1[cc];
+                                v -= a2[cc] * cb2v[D];
+                                v += a2[cc] * cb2v[pA];
+                                v += a2[cc] * cb2v[pB];
+                                v -= a2[cc] * cb2v[cc];
+                                v -= ica2v[D] * a3[cc];
+                                v += ica2v[qA] * a3[cc];
+                                v += ica2v[qB] * a3[cc];
+                                v -= ica2v[cc] * a3[cc];
+                                rv[cc] = v;
+                            }
+                            {  // XYZFrgCore.cpp:402-417
+                                float v = 4.0f * rp[D];
+                                v -= a0[D] * cbv[D];
+                                v -= a0[D] * cbv[X];
+                                v -= a0[D] * cbv[Y];
+                                v -= a0[D] * cbv[Z];
+                                v -= icav[D] * a1[D];
+                                v -= icav[X] * a1[D];
+                                v -= icav[Y] * a1[D];
+                                v -= icav[Z] * a1[D];
+                                v -= a2[D] * cb2v[D];
+                                v -= a2[D] * cb2v[X];
+                                v -= a2[D] * cb2v[Y];
+                                v -= a2[D] * cb2v[Z];
+                                v -= ica2v[D] * a3[D];
+                                v -= ica2v[X] * a3[D];
+                                v -= ica2v[Y] * a3[D];
+                                v -= ica2v[Z] * a3[D];
+                                rv[D] = v;
+                            }
+                            r[k] = make_float4(rv[0], rv[1], rv[2], rv[3]);
                         }
-                        {  // XYZFrgCore.cpp:402-417
-                            float v = 4.0f * rp[D];
-                            v -= a0[D] * cbv[D];
-                            v -= a0[D] * cbv[X];
-                            v -= a0[D] * cbv[Y];
-                            v -= a0[D] * cbv[Z];
-                            v -= icav[D] * a1[D];
-                            v -= icav[X] * a1[D];
-                            v -= icav[Y] * a1[D];
-                            v -= icav[Z] * a1[D];
-                            v -= a2[D] * cb2v[D];
-                            v -= a2[D] * cb2v[X];
-                            v -= a2[D] * cb2v[Y];
-                            v -= a2[D] * cb2v[Z];
-                            v -= ica2v[D] * a3[D];
-                            v -= ica2v[X] * a3[D];
-                            v -= ica2v[Y] * a3[D];
-                            v -= ica2v[Z] * a3[D];
-                            rv[D] = v;
-                        }
-                        r[k] = make_float4(rv[0], rv[1], rv[2], rv[3]);
+                        __syncwarp();
                     }
-                    __syncwarp();
-                }
+                    const float c = d.c;
 #pragma unroll
-                for (int k = 0; k < kSpt; ++k) {
-                    acc[k].x += c * r[k].x;
-                    acc[k].y += c * r[k].y;
-                    acc[k].z += c * r[k].z;
-                    acc[k].w += c * r[k].w;
+                    for (int k = 0; k < kSpt; ++k) {
+                        acc[k].x += c * r[k].x;
+                        acc[k].y += c * r[k].y;
+                        acc[k].z += c * r[k].z;
+                        acc[k].w += c * r[k].w;
+                    }
                 }
+                __syncwarp();
             }
         }
 #pragma unroll
@@ -512,8 +600,8 @@ struct spn_xyz {
           *corr_out = nullptr;
     float4 *sd = nullptr, *dsd = nullptr;
     int *ints = nullptr;  // all integer tables in one allocation
-    int *sites, *sites_perm, *inv_sites, *inv_sites_perm, *ov_ptr, *ov_r1, *ov_r2, *ov_p1, *ov_p2, *range_rid,
-        *range_inv, *corr_rid, *corr_perm, *node_cnt, *work_counter;
+    int *sites, *sites_perm, *inv_sites, *inv_sites_perm, *ov_ptr, *ov_r1, *ov_r2, *ov_p1, *ov_p2, *ov_pk,
+        *range_rid, *range_inv, *corr_rid, *corr_perm, *node_cnt, *work_counter;
     unsigned *status = nullptr;
     double *partial = nullptr;
 
@@ -540,6 +628,7 @@ struct spn_xyz {
         a.ov_r2 = ov_r2;
         a.ov_p1 = ov_p1;
         a.ov_p2 = ov_p2;
+        a.ov_pk = ov_pk;
         a.range_rid = range_rid;
         a.range_inv = range_inv;
         a.node_wp = node_wp;
@@ -624,7 +713,7 @@ void validate(const spn_xyz_desc *d) {
     in_range(d->corr_perm, d->n_corr, 6, "corr_perm");
 }
 
-size_t vertex_smem() { return size_t(kWarps) * 2 * kSpt * 32 * sizeof(float4); }
+size_t vertex_smem(int nl) { return size_t(kWarps) * (kXBatch * sizeof(XDesc) + 12 * size_t(nl) * sizeof(float4)); }
 
 void launch_correlation(spn_xyz *h) {
     const XyzArgs a = h->args();
@@ -681,6 +770,10 @@ extern "C" int spn_xyz_create(const spn_xyz_desc *d, spn_xyz **out) {
             put(d->overlap_rid2, nov);
             put(d->overlap_perm1, nov);
             put(d->overlap_perm2, nov);
+            std::vector<int> packed(nov);
+            for (int i = 0; i < nov; ++i)
+                packed[i] = d->overlap_rid1[i] | d->overlap_rid2[i] << 7 | d->overlap_perm1[i] << 14 | d->overlap_perm2[i] << 17;
+            put(packed.data(), nov);
             put(d->range_rid, nr);
             put(d->range_inv_rid, nr);
             put(d->corr_rid, nc);
@@ -690,8 +783,8 @@ extern "C" int spn_xyz_create(const spn_xyz_desc *d, spn_xyz **out) {
             h->ints = dalloc<int>(img.size(), "alloc lattice tables");
             h2d(h->ints, img.data(), img.size(), h->stream);
             int **fields[] = {&h->sites, &h->sites_perm, &h->inv_sites, &h->inv_sites_perm, &h->ov_ptr, &h->ov_r1,
-                              &h->ov_r2, &h->ov_p1, &h->ov_p2, &h->range_rid, &h->range_inv, &h->corr_rid,
-                              &h->corr_perm, &h->node_cnt, &h->work_counter};
+                              &h->ov_r2, &h->ov_p1, &h->ov_p2, &h->ov_pk, &h->range_rid, &h->range_inv,
+                              &h->corr_rid, &h->corr_perm, &h->node_cnt, &h->work_counter};
             for (size_t k = 0; k < at.size(); ++k) *fields[k] = h->ints + at[k];
             h2d(h->freq, d->freq, h->n, h->stream);
             check_cuda(cudaMemsetAsync(h->sd, 0, vsz * sizeof(float4), h->stream), "memset");
@@ -701,7 +794,10 @@ extern "C" int spn_xyz_create(const spn_xyz_desc *d, spn_xyz **out) {
             check_cuda(cudaMemsetAsync(h->status, 0, sizeof(unsigned), h->stream), "memset");
             check_cuda(cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device), "device attribute");
             int per_sm = 0;
-            check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, xyz_vertex_kernel, kThreads, vertex_smem()),
+            check_cuda(cudaFuncSetAttribute(xyz_vertex_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            int(vertex_smem(h->nl))),
+                       "shared memory limit");
+            check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, xyz_vertex_kernel, kThreads, vertex_smem(h->nl)),
                        "occupancy");
             if (per_sm < 1) throw Error(ErrorType::Unsupported, "XYZ vertex-flow kernel does not fit on this device");
             h->grid = h->sms * per_sm;
@@ -794,7 +890,9 @@ extern "C" int spn_xyz_compute_step(spn_xyz *h) {
         check_cuda(cudaGetLastError(), "self-energy launch");
         xyz_node_table_kernel<<<(h->n + 63) / 64, 64, 0, h->stream>>>(h->node_args());
         check_cuda(cudaGetLastError(), "node table launch");
-        xyz_vertex_kernel<<<h->grid, kThreads, vertex_smem(), h->stream>>>(a);
+        check_cuda(cudaFuncSetAttribute(xyz_vertex_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(vertex_smem(h->nl))),
+                   "shared memory limit");
+        xyz_vertex_kernel<<<h->grid, kThreads, vertex_smem(h->nl), h->stream>>>(a);
         check_cuda(cudaGetLastError(), "vertex flow launch");
     });
 }
