@@ -79,6 +79,8 @@ def parse_args():
     ap.add_argument("--flows", type=int, default=None, help="multi-flow workloads: number of flows / requests")
     ap.add_argument("--rates", type=str, default="0.5,1,2,4,inf",
                     help="serve-mixed: arrival rates as multiples of the sequential plain-GPU capacity")
+    ap.add_argument("--policy", type=str, default="fifo",
+                    help="serve-mixed: admission policies to run at every rate, comma separated (fifo, sjf)")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU work budget of the baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -310,25 +312,31 @@ def run_multi(args):
     arms = {}
     rates = [float("inf")] if scan else [float(x) * (1.0 / service.mean()) for x in args.rates.split(",")]
     max_diff = 0.0
+    policies = ["fifo"] if scan else args.policy.split(",")
     for rate in rates:
         arrivals = workloads.poisson_arrivals(n, rate)
-        srv = FlowServer()
-        t0 = time.perf_counter()
-        tickets = []
-        i = 0
-        while True:
-            now = time.perf_counter() - t0
-            while i < n and arrivals[i] <= now:
-                tickets.append(srv.submit(specs[i], t_arrival=t0 + arrivals[i]))
-                i += 1
-            busy = srv.pump()
-            if busy == 0:
-                if i >= n:
-                    break
-                time.sleep(min(0.01, max(0.0, arrivals[i] - (time.perf_counter() - t0))))
-        makespan = time.perf_counter() - t0
-        for t in tickets:
-            max_diff = max(max_diff, _check_same(plain[t.id], t.result))
+        served = {}
+        for policy in policies:
+            srv = FlowServer(policy=policy)
+            t0 = time.perf_counter()
+            tickets = []
+            i = 0
+            while True:
+                now = time.perf_counter() - t0
+                while i < n and arrivals[i] <= now:
+                    tickets.append(srv.submit(specs[i], t_arrival=t0 + arrivals[i]))
+                    i += 1
+                busy = srv.pump()
+                if busy == 0:
+                    if i >= n:
+                        break
+                    time.sleep(min(0.01, max(0.0, arrivals[i] - (time.perf_counter() - t0))))
+            makespan = time.perf_counter() - t0
+            for t in tickets:
+                max_diff = max(max_diff, _check_same(plain[t.id], t.result))
+            served[policy] = {"flows_per_s": n / makespan, "makespan_s": makespan, "steps": srv.steps,
+                              **time_to_result_stats(tickets)}
+            srv.close()
         # the same arrivals served by the sequential plain path (FIFO queue of its service times)
         free_at, plain_ttr = 0.0, []
         for k in range(n):
@@ -337,12 +345,11 @@ def run_multi(args):
             plain_ttr.append(free_at - arrivals[k])
         arms["inf" if not np.isfinite(rate) else f"{rate:.4g}"] = {
             "arrival_rate_per_s": None if not np.isfinite(rate) else rate,
-            "batched": {"flows_per_s": n / makespan, "makespan_s": makespan, "steps": srv.steps,
-                        **time_to_result_stats(tickets)},
+            "batched": served[policies[0]],
+            **({"batched_by_policy": served} if len(policies) > 1 else {}),
             "plain_gpu_fifo": {"flows_per_s": n / max(free_at, 1e-9), "makespan_s": free_at,
                                "p50_s": float(np.percentile(plain_ttr, 50)), "p99_s": float(np.percentile(plain_ttr, 99))},
         }
-        srv.close()
     clocks = sampler.stop()
     cpu_s, cpu_samples, cores = _cpu_flow_seconds(specs, args.cpu_seconds) if not args.no_cpu_baseline else (None, [], 0)
     top = arms[list(arms)[-1]]

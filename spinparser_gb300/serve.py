@@ -1,8 +1,10 @@
 """Serving SU(2) flows: continuous batching over one GPU (``Su2Batch``).
 
 Requests (``FlowSpec``: lattice, range, model, couplings, frequency grid, cutoff list) are
-queued as they arrive.  Between batch steps the server admits queued requests in arrival order
-while their device footprint fits the memory budget (and, optionally, a flow-count limit);
+queued as they arrive.  Between batch steps the server admits queued requests -- in arrival
+order ("fifo") or smallest expected work first ("sjf": the flow's nominal work per step times
+its number of steps) -- while their device footprint fits the memory budget (and, optionally,
+a flow-count limit);
 every admitted flow keeps its vertex and self-energy state resident on the device until it
 finishes, and all resident flows advance together, one cutoff step per batch step.  Finished
 flows are retired at once (results copied out, memory released) so that waiting requests take
@@ -57,6 +59,7 @@ class Ticket:
     t_done: float | None = None
     flow_id: int | None = None
     footprint: int = 0
+    work: float = 0.0  # expected work of the whole flow (nominal flops), for "sjf" admission
     result: BatchResult | None = None
     _built: tuple | None = field(default=None, repr=False)
 
@@ -73,9 +76,39 @@ def device_memory(device: int = 0):
     return f.value, t.value
 
 
+def expected_work(tab, freq, cut) -> float:
+    """Nominal work of a flow: F_N (2N+8)(3*100*Nl + 4*sum O) flops per step times its steps."""
+    n = len(freq)
+    fn = n * n * (n + 1) // 2
+    return float(fn) * (2 * n + 8) * (300.0 * tab.n_sites + 4.0 * tab.n_overlap) * max(len(cut) - 1, 1)
+
+
+def prepare(t: Ticket) -> None:
+    """Build a queued request's tables once; fills its device footprint and expected work."""
+    if t._built is None:
+        t._built = t.spec.build()
+        tab, freq, cut = t._built
+        t.footprint = Su2Batch.footprint(tab, freq, len(cut))
+        t.work = expected_work(tab, freq, cut)
+
+
+def next_ticket(queue, policy: str) -> Ticket:
+    """The request a server admits next: the oldest ("fifo") or the one with the least expected
+    work, ties to the oldest ("sjf")."""
+    if policy == "sjf":
+        for q in queue:
+            prepare(q)
+        return min(queue, key=lambda q: (q.work, q.id))
+    prepare(queue[0])
+    return queue[0]
+
+
 class FlowServer:
     def __init__(self, device: int = 0, memory_budget: int | None = None, max_flows: int | None = None,
-                 nodes_per_iteration: int = 1, use_graph: bool = True, clock=time.perf_counter):
+                 nodes_per_iteration: int = 1, use_graph: bool = True, clock=time.perf_counter, policy: str = "fifo"):
+        if policy not in ("fifo", "sjf"):
+            raise ValueError("policy must be 'fifo' or 'sjf'")
+        self.policy = policy
         self.batch = Su2Batch(device, nodes_per_iteration, use_graph)
         if memory_budget is None:
             free, _ = device_memory(device)
@@ -98,16 +131,12 @@ class FlowServer:
 
     def _admit(self) -> None:
         while self.queue:
-            t = self.queue[0]
             if self.max_flows is not None and len(self.active) >= self.max_flows:
                 return
-            if t._built is None:
-                t._built = t.spec.build()
-                tab, freq, cut = t._built
-                t.footprint = Su2Batch.footprint(tab, freq, len(cut))
+            t = next_ticket(self.queue, self.policy)
             if self.active and self.used + t.footprint > self.budget:
                 return
-            self.queue.popleft()
+            self.queue.remove(t)
             tab, freq, cut = t._built
             t.flow_id = self.batch.add(tab, freq, cut, flags=t.spec.flags)
             t.t_admit = self.clock()

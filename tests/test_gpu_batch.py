@@ -131,8 +131,8 @@ def test_other_variant_gives_the_same_bits(reference):
 
 def test_server_admits_by_footprint_and_results_do_not_change(reference):
     """Continuous batching under a memory budget (the largest flow plus a little) and under a
-    two-flow slot limit: requests wait, are admitted as others finish, and every result equals
-    the flow alone."""
+    two-flow slot limit (arrival order and least work first): requests wait, are admitted as
+    others finish, and every result equals the flow alone."""
     from spinparser_gb300.serve import FlowServer, FlowSpec
 
     def spec(name):
@@ -141,8 +141,9 @@ def test_server_admits_by_footprint_and_results_do_not_change(reference):
 
     names = list(CASES)
     feet = sorted(Su2Batch.footprint(*case(n)[:2], len(case(n)[2])) for n in names)
-    for budget, slots in ((feet[-1] + feet[0] // 2, None), (10 * feet[-1], 2)):
-        srv = FlowServer(memory_budget=budget, max_flows=slots)
+    for budget, slots, policy in ((feet[-1] + feet[0] // 2, None, "fifo"), (10 * feet[-1], 2, "fifo"),
+                                  (10 * feet[-1], 2, "sjf")):
+        srv = FlowServer(memory_budget=budget, max_flows=slots, policy=policy)
         tickets = {n: srv.submit(spec(n)) for n in names}
         most = 0
         while srv.pump():

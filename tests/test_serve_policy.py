@@ -1,0 +1,44 @@
+"""Admission order of the flow server (host logic, no GPU): arrival order for "fifo", least
+expected work first for "sjf", ties to the oldest request."""
+import pytest
+
+from spinparser_gb300.serve import FlowSpec, Ticket, expected_work, next_ticket
+
+
+def spec(rng, n):
+    return FlowSpec("square", rng, "square-j1j2heisenberg", (("j1", "1.0"), ("j2", "0.3")), n, 0.005, 50.0,
+                    50.0, 0.5, 0.9)
+
+
+def queue(*specs):
+    return [Ticket(i, s, float(i)) for i, s in enumerate(specs)]
+
+
+def test_fifo_takes_the_oldest():
+    q = queue(spec(5, 16), spec(3, 8))
+    assert next_ticket(q, "fifo") is q[0]
+    assert q[0].footprint > 0 and q[0].work > 0
+    assert q[1]._built is None  # fifo builds only the head
+
+
+def test_sjf_takes_the_least_work_and_ties_to_the_oldest():
+    q = queue(spec(5, 16), spec(3, 16), spec(3, 8), spec(3, 8))
+    t = next_ticket(q, "sjf")
+    assert t is q[2]
+    works = [x.work for x in q]
+    assert works[2] == works[3] < works[1] < works[0]
+    q.remove(t)
+    assert next_ticket(q, "sjf").id == 3  # the remaining (3, 8) request
+
+
+def test_expected_work_scales_with_the_steps():
+    q = queue(spec(3, 8))
+    next_ticket(q, "fifo")
+    tab, freq, cut = q[0]._built
+    assert expected_work(tab, freq, cut[:11]) == pytest.approx(q[0].work * 10 / (len(cut) - 1))
+
+
+def test_unknown_policy_is_rejected():
+    from spinparser_gb300.serve import FlowServer
+    with pytest.raises(ValueError):
+        FlowServer(policy="lifo")
