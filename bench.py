@@ -80,7 +80,8 @@ def parse_args():
     ap.add_argument("--rates", type=str, default="0.5,1,2,4,inf",
                     help="serve-mixed: arrival rates as multiples of the sequential plain-GPU capacity")
     ap.add_argument("--policy", type=str, default="fifo",
-                    help="serve-mixed: admission policies to run at every rate, comma separated (fifo, sjf)")
+                    help="serve-mixed: server arms to run at every rate, comma separated: fifo or sjf, "
+                         "optionally @k for a k-flow slot limit (e.g. fifo,sjf@2)")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU work budget of the baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -317,7 +318,8 @@ def run_multi(args):
         arrivals = workloads.poisson_arrivals(n, rate)
         served = {}
         for policy in policies:
-            srv = FlowServer(policy=policy)
+            name, _, slots = policy.partition("@")
+            srv = FlowServer(policy=name, max_flows=int(slots) if slots else None)
             t0 = time.perf_counter()
             tickets = []
             i = 0

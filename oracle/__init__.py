@@ -258,3 +258,110 @@ class XyzOracle:
                                          self._pp(v4), self._pp(chi), threads)
         assert n > 0
         return n, np.stack(chi).reshape(4, len(cut), self.nl).transpose(1, 0, 2), (v2, np.stack(v4))
+
+
+# ---------------------------------------------------------------------------------------
+# TRI core (oracle/tri_oracle.cpp): time-reversal-invariant models with general couplings
+# (Heisenberg-Kitaev-Gamma, ...).  The vertex has 16 components (a, b), a, b in X, Y, Z,
+# density, stored as v4[F_N][16][Nl] (component 4a + b), the reference's own layout.
+# ---------------------------------------------------------------------------------------
+TRI_COMPONENTS = ("xx", "xy", "xz", "yx", "yy", "yz", "zx", "zy", "zz", "dd")
+
+
+def tri_initial_state(tables, n_freq: int, normalization: float = 1.0):
+    """TRIEffectiveAction initial condition (src/TRI/TRIEffectiveAction.hpp:38-62):
+    v4[it][a][b][rid] += 0.25 J^ab(rid) / normalization for spin components a, b; every
+    component with a density index and the self-energy start at zero."""
+    fn = n_freq * n_freq * (n_freq + 1) // 2
+    v2 = np.zeros(n_freq, np.float32)
+    v4 = np.zeros((fn, 4, 4, tables.n_sites), np.float32)
+    for rid, J in zip(tables.interaction_rid, tables.interaction_J):
+        for a in range(3):
+            for b in range(3):
+                v4[:, a, b, rid] += (np.float32(0.25) * np.float32(J[a, b])) / np.float32(normalization)
+    return v2, v4.reshape(-1)
+
+
+def tri_scatter(chi, tables, spin):
+    """Correlations per (basis, site in range) of chi[16][Nl] (TRIMeasurementCorrelation.cpp:
+    262-284): entry (b, j) of component (a, c) reads component (P a, P c) of its representative,
+    P the entry's spin permutation; returns [10, n_basis, n_range] in TRI_COMPONENTS order."""
+    chi = np.asarray(chi).reshape(16, -1)
+    rid = tables.corr_rid.reshape(tables.n_basis, tables.n_range)
+    perm = SPIN_PERMUTATIONS[spin.corr_perm.reshape(tables.n_basis, tables.n_range)]
+    out = np.empty((10, tables.n_basis, tables.n_range), chi.dtype)
+    q = 0
+    for a in range(3):
+        for c in range(3):
+            out[q] = chi[4 * perm[..., a] + perm[..., c], rid]
+            q += 1
+    out[9] = chi[15, rid]
+    return out
+
+
+class TriOracle:
+    """CPU restatement of the reference TRI core for one lattice + frequency mesh."""
+
+    def __init__(self, tables, spin, freq):
+        lib = _lib()
+        self.lib = lib
+        fp, i4 = C.POINTER(C.c_float), C.c_int
+        dsc = C.POINTER(XyzOracleDesc)
+        lib.oracle_tri_rhs_f32.argtypes = [dsc, C.c_float, fp, fp, fp, fp, i4]
+        lib.oracle_tri_correlation_f32.argtypes = [dsc, C.c_float, fp, fp, fp]
+        lib.oracle_tri_flow_f32.argtypes = [dsc, fp, i4, fp, fp, fp, i4]
+        lib.oracle_tri_tables.argtypes = [C.POINTER(C.c_int)]
+        self.freq = np.ascontiguousarray(freq, np.float32)
+        self.n = len(self.freq)
+        self.nl = int(tables.n_sites)
+        self.fn = self.n * self.n * (self.n + 1) // 2
+        self.size = self.fn * 16 * self.nl
+        arrs = [tables.sites_rid, spin.sites_perm, tables.inv_sites_rid, spin.inv_sites_perm, tables.overlap_ptr,
+                tables.overlap_rid1, tables.overlap_rid2, spin.overlap_perm1, spin.overlap_perm2, tables.range_rid,
+                tables.range_inv_rid]
+        self._keep = [np.ascontiguousarray(a, np.int32) for a in arrs]
+        k = [_p(a, C.c_int) for a in self._keep]
+        d = XyzOracleDesc()
+        d.n_freq, d.freq, d.n_sites = self.n, _p(self.freq, C.c_float), self.nl
+        (d.sites_rid, d.sites_perm, d.inv_sites_rid, d.inv_sites_perm, d.overlap_ptr, d.overlap_rid1, d.overlap_rid2,
+         d.overlap_perm1, d.overlap_perm2) = k[:9]
+        d.n_range, d.range_rid, d.range_inv_rid = len(self._keep[9]), k[9], k[10]
+        self.desc = d
+
+    def tables(self):
+        """The coefficient tables as rows (table, output, n, a, b, sign)."""
+        rows = np.zeros(6 * 16 * 72, np.int32)
+        n = self.lib.oracle_tri_tables(_p(rows, C.c_int))
+        assert n > 0
+        return rows[:6 * n].reshape(n, 6)
+
+    def rhs(self, cutoff, v2, v4, threads: int = 0):
+        """(dv2[N], dv4[F_N*16*Nl]) of the state (v2[N], v4[F_N*16*Nl])."""
+        v2 = np.ascontiguousarray(v2, np.float32)
+        v4 = np.ascontiguousarray(v4, np.float32).reshape(-1)
+        assert v4.size == self.size
+        dv2 = np.empty(self.n, np.float32)
+        dv4 = np.empty(self.size, np.float32)
+        assert self.lib.oracle_tri_rhs_f32(C.byref(self.desc), cutoff, _p(v2, C.c_float), _p(v4, C.c_float),
+                                           _p(dv2, C.c_float), _p(dv4, C.c_float), threads) == 0
+        return dv2, dv4
+
+    def correlation(self, cutoff, v2, v4):
+        """chi[16][Nl] at the state (the mixed spin/density components are zero)."""
+        v2 = np.ascontiguousarray(v2, np.float32)
+        v4 = np.ascontiguousarray(v4, np.float32).reshape(-1)
+        chi = np.empty(16 * self.nl, np.float32)
+        assert self.lib.oracle_tri_correlation_f32(C.byref(self.desc), cutoff, _p(v2, C.c_float), _p(v4, C.c_float),
+                                                   _p(chi, C.c_float)) == 0
+        return chi.reshape(16, self.nl)
+
+    def flow(self, cutoffs, v2, v4, threads: int = 0):
+        """Whole flow; returns (n_measured, chi[n_cut, 16, Nl], final (v2, v4))."""
+        cut = np.ascontiguousarray(cutoffs, np.float32)
+        v2 = np.array(v2, np.float32)
+        v4 = np.array(v4, np.float32).reshape(-1)
+        chi = np.zeros(len(cut) * 16 * self.nl, np.float32)
+        n = self.lib.oracle_tri_flow_f32(C.byref(self.desc), _p(cut, C.c_float), len(cut), _p(v2, C.c_float),
+                                         _p(v4, C.c_float), _p(chi, C.c_float), threads)
+        assert n > 0
+        return n, chi.reshape(len(cut), 16, self.nl), (v2, v4)

@@ -102,7 +102,7 @@ def build_oracle(force: bool = False) -> str:
     """Compiles the CPU oracle (test infrastructure) into oracle/_build/<machine>/."""
     out = oracle_library_path()
     os.makedirs(os.path.dirname(out), exist_ok=True)
-    srcs = [os.path.join(ORACLE_DIR, f) for f in ("su2_oracle.cpp", "xyz_oracle.cpp")]
+    srcs = [os.path.join(ORACLE_DIR, f) for f in ("su2_oracle.cpp", "xyz_oracle.cpp", "tri_oracle.cpp")]
     if force or _stale(out, srcs):
         _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp", *srcs, "-o", out])
     return out

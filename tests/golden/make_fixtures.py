@@ -24,8 +24,16 @@ Outputs (committed, so the tests need no reference tree at run time):
   res_hyperhoneycomb/     the hyperhoneycomb unit cell and Heisenberg-Kitaev model of the
                           reference's res/ files (the input of test_reference2)
 
-`python tests/golden/make_fixtures.py <reference root> reference2` regenerates only the
-test_reference2 fixtures.
+  reference3_tri.npz      golden TRI-core correlations of test/scripted/test_reference3.sh
+                          (honeycomb r=3 Heisenberg-Kitaev-Gamma j=0.2, k=1, g=-0.1, 14 manual
+                          frequencies, cutoff 10 -> 0.3 x0.9), read from
+                          test/scripted/assets/test_reference3.ref (TRICorXX ... TRICorDD)
+  reference3_layout.json  member structure and HDF5 encoding fingerprint of test_reference3.ref
+  res_honeycomb/          the honeycomb unit cell and Heisenberg-Kitaev-Gamma model of the
+                          reference's res/ files (the input of test_reference3)
+
+`python tests/golden/make_fixtures.py <reference root> reference2` (or `reference3`)
+regenerates only the fixtures of that script.
 """
 from __future__ import annotations
 
@@ -125,6 +133,42 @@ def write_reference2(ref_root: str) -> None:
         f.write(head + extract_resource(ref_root, "models", "model", p["model"]) + "\n")
 
 
+TRI_COMPONENTS = ("XX", "XY", "XZ", "YX", "YY", "YZ", "ZX", "ZY", "ZZ", "DD")
+
+
+def write_reference3(ref_root: str) -> None:
+    """TRI golden of test_reference3 (Heisenberg-Kitaev-Gamma on the honeycomb lattice) and its
+    resource files."""
+    scripted = os.path.join(ref_root, "test", "scripted")
+    script = open(os.path.join(scripted, "test_reference3.sh")).read()
+    p = task_parameters(script)
+    k = float(re.search(r"<k>([-0-9.]+)</k>", script).group(1))
+    g = float(re.search(r"<g>([-0-9.]+)</g>", script).group(1))
+    ref = os.path.join(scripted, "assets", "test_reference3.ref")
+    comps = {}
+    cut = None
+    for c in TRI_COMPONENTS:
+        cc, v = h5lite.read_correlations(ref, "TRICor" + c)
+        assert cut is None or np.array_equal(cut, cc)
+        cut = cc
+        comps[c.lower()] = v
+    meta = h5lite.open_file(ref)["TRICorXX/meta"]
+    np.savez_compressed(os.path.join(HERE, "reference3_tri.npz"), cutoffs=cut, **comps,
+                        frequencies=np.array(p["frequencies"], np.float32),
+                        cutoff_spec=np.array([p["cutoff_max"], p["cutoff_min"], p["cutoff_step"]], np.float32),
+                        j=np.float32(p["j"]), k=np.float32(k), g=np.float32(g), sites=meta["sites"].read(),
+                        basis=meta["basis"].read(), lattice_vectors=meta["latticeVectors"].read())
+    with open(os.path.join(HERE, "reference3_layout.json"), "w") as f:
+        json.dump({"fingerprint": h5lite.layout_fingerprint(ref), "skeleton": h5lite.skeleton(ref)}, f, indent=0)
+    out = os.path.join(HERE, "res_honeycomb")
+    os.makedirs(out, exist_ok=True)
+    head = '<?xml version="1.0" encoding="utf-8"?>\n'
+    with open(os.path.join(out, "lattices.xml"), "w") as f:
+        f.write(head + extract_resource(ref_root, "lattices", "unitcell", p["lattice"]) + "\n")
+    with open(os.path.join(out, "models.xml"), "w") as f:
+        f.write(head + extract_resource(ref_root, "models", "model", p["model"]) + "\n")
+
+
 def write_reference1_layout(ref: str) -> None:
     """Structure (members, attributes, shapes) and encoding fingerprint of the libhdf5-written
     test_reference1.ref, for checking the package's .obs writer without the file itself."""
@@ -187,6 +231,9 @@ if __name__ == "__main__":
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     if len(sys.argv) > 2 and sys.argv[2] == "reference2":
         write_reference2(root)
+    elif len(sys.argv) > 2 and sys.argv[2] == "reference3":
+        write_reference3(root)
     else:
         main(root)
         write_reference2(root)
+        write_reference3(root)
