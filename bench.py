@@ -64,6 +64,13 @@ XYZ_WORKLOADS = {
                                         params={"j": "0.1", "k": "-1.0"}, n_freq=48, fmin=0.005, fmax=50.0,
                                         cmax=50.0, cmin=0.05, cstep=0.98),
 }
+# the TRI core (time-reversal-invariant models with off-diagonal couplings): a
+# Heisenberg-Kitaev-Gamma flow; the first --steps cutoffs of the list are timed
+TRI_WORKLOADS = {
+    "tri-honeycomb-kitaev-gamma-r9-n32": dict(lattice="honeycomb", range=9, model="honeycomb-kitaev-gamma",
+                                              params={"j": "0.2", "k": "1.0", "g": "-0.1"}, n_freq=32, fmin=0.005,
+                                              fmax=50.0, cmax=50.0, cmin=0.05, cstep=0.98),
+}
 METRIC = "cutoff steps/s per flow"
 KERNELS_PER_STEP = 8  # self-energy, node tables, vertex flow, 2 x correlation, 3 x Euler
 
@@ -75,7 +82,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + list(MULTI_WORKLOADS) + list(PRECISION_WORKLOADS) +
-                    list(XYZ_WORKLOADS), default=DEFAULT_WORKLOAD)
+                    list(XYZ_WORKLOADS) + list(TRI_WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--flows", type=int, default=None, help="multi-flow workloads: number of flows / requests")
     ap.add_argument("--rates", type=str, default="0.5,1,2,4,inf",
                     help="serve-mixed: arrival rates as multiples of the sequential plain-GPU capacity")
@@ -467,21 +474,29 @@ def run_precision(args):
 
 
 def run_xyz(args):
-    """The XYZ core: one whole flow on the GPU (device-resident state, measurement at every
-    cutoff, as the driver runs it), against the XYZ oracle on the host cores (two right-hand
-    sides at cutoffs a third and two thirds into the flow, extrapolated to the flow)."""
+    """The XYZ or TRI core: one flow on the GPU (device-resident state, measurement at every
+    cutoff, as the driver runs it; XYZ the whole cutoff list, TRI its first --steps cutoffs),
+    against the core's oracle on the host cores (two right-hand sides at cutoffs a third and two
+    thirds into the timed list)."""
     import torch
 
     import spinparser_gb300 as spn
 
     torch.cuda.set_device(0)
-    wl = XYZ_WORKLOADS[args.workload]
+    tri = args.workload in TRI_WORKLOADS
+    wl = (TRI_WORKLOADS if tri else XYZ_WORKLOADS)[args.workload]
     lat = spn.Lattice(wl["lattice"], wl["range"], wl["model"], wl["params"])
     tab, st = lat.tables(), lat.spin_tables()
     freq = spn.frequency_exponential(wl["fmin"], wl["fmax"], wl["n_freq"])
     cut = spn.cutoff_exponential(wl["cmax"], wl["cmin"], wl["cstep"])
-    init = spn.xyz_initial_state(lat, len(freq))
-    flow = spn.XyzFlow(tab, st, freq)
+    n_cut = len(cut)
+    if tri:
+        cut = cut[:args.steps + 1]
+        init = spn.tri_initial_state(lat, len(freq))
+        flow = spn.TriFlow(tab, st, freq)
+    else:
+        init = spn.xyz_initial_state(lat, len(freq))
+        flow = spn.XyzFlow(tab, st, freq)
     warm = max(args.warmup, 3)
     flow.run(cut[:warm + 1], *init)  # untimed warm-up
     sampler = ClockSampler(0)
@@ -494,19 +509,22 @@ def run_xyz(args):
     clocks = sampler.stop()
     steps = len(measured) - 1
     line = {
-        "metric": "cutoff steps/s per flow (XYZ core)", "value": steps / secs, "unit": "steps/s", "n_gpus": 1,
+        "metric": "cutoff steps/s per flow (%s core)" % ("TRI" if tri else "XYZ"), "value": steps / secs,
+        "unit": "steps/s", "n_gpus": 1,
         "steps": steps, "warmup": warm, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (model initial condition, advanced by the flow)",
         "config": {"workload": args.workload, **{k: wl[k] for k in ("lattice", "range", "model", "params", "n_freq")},
-                   "cutoff": [wl["cmax"], wl["cmin"], wl["cstep"]], "n_cutoffs": len(cut), "n_sites": tab.n_sites,
-                   "n_overlap": tab.n_overlap, "timed": "the whole flow, measurement at every cutoff"},
+                   "cutoff": [wl["cmax"], wl["cmin"], wl["cstep"]], "n_cutoffs": n_cut, "n_sites": tab.n_sites,
+                   "n_overlap": tab.n_overlap,
+                   "timed": ("the first %d cutoff steps" % steps if tri else "the whole flow") +
+                            ", measurement at every cutoff"},
         "diverged": diverged, "clocks": clocks,
     }
     if not args.no_cpu_baseline:
-        from oracle import XyzOracle
+        from oracle import TriOracle, XyzOracle
 
-        orc = XyzOracle(tab, st, freq)
+        orc = (TriOracle if tri else XyzOracle)(tab, st, freq)
         _, v2, v4 = flow.get_state()
         threads = os.cpu_count() or 1
         samples = []
@@ -517,7 +535,8 @@ def run_xyz(args):
             samples.append(time.perf_counter() - t1)
         per_step = float(np.mean(samples))
         line["cpu_baseline"] = {"value": 1.0 / per_step, "unit": "steps/s", "cores": threads, "kind": "port",
-                                "sample": "two full right-hand sides of the XYZ oracle at the final state, cutoffs a "
+                                "sample": "two full right-hand sides of the %s oracle at the final state, cutoffs a "
+                                          % ("TRI" if tri else "XYZ") +
                                           "third and two thirds into the list; %.2f s per step" % per_step}
     print(json.dumps(line))
     flow.close()
@@ -525,7 +544,7 @@ def run_xyz(args):
 
 def main():
     args = parse_args()
-    if args.workload in XYZ_WORKLOADS:
+    if args.workload in XYZ_WORKLOADS or args.workload in TRI_WORKLOADS:
         run_xyz(args)
         return
     if args.workload in MULTI_WORKLOADS:

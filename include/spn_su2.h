@@ -424,6 +424,40 @@ int spn_xyz_finalize_step(spn_xyz *h, float new_cutoff);
 int spn_xyz_measure_correlation(spn_xyz *h, float *xx, float *yy, float *zz, float *dd, float *chi);
 int spn_xyz_is_diverged(spn_xyz *h, int *diverged);
 
+/* ------------------------------------------------------------------------------------
+ * TRI core: time-reversal-invariant models with general, also off-diagonal, couplings
+ * (Heisenberg-Kitaev-Gamma, ...), 16 vertex components (a, b), a, b in X, Y, Z, density
+ * (src/TRI/TRIFrgCore.cpp, TRIVertexTwoParticle.hpp, TRIMeasurementCorrelation.cpp).
+ * Arrays in the reference layout: v2[N], v4[F_N][16][Nl] (component 4a + b), the checkpoint
+ * dataset "v4" of TRIEffectiveAction (TRIEffectiveAction.hpp:147-148).
+ * ------------------------------------------------------------------------------------ */
+typedef struct spn_tri spn_tri;
+typedef spn_xyz_desc spn_tri_desc; /* the same lattice and spin-permutation tables */
+
+/* TRIEffectiveAction initial condition (src/TRI/TRIEffectiveAction.hpp:38-62): zeros, then
+ * v4[it][a][b][rid] += 0.25 J^ab(rid) / normalization for spin components a, b. */
+int spn_tri_initial_state(const spn_lattice *lat, int n_freq, float normalization, float *v2, float *v4);
+
+/* The flow cycle (TRIFrgCore::computeStep / finalizeStep, TRIFrgCore.cpp:76-120). */
+int spn_tri_create(const spn_tri_desc *desc, spn_tri **out);
+int spn_tri_destroy(spn_tri *h);
+int spn_tri_set_state(spn_tri *h, float cutoff, const float *v2, const float *v4);
+int spn_tri_get_state(spn_tri *h, float *cutoff, float *v2, float *v4);
+int spn_tri_compute_step(spn_tri *h);
+int spn_tri_get_flow(spn_tri *h, float *dv2, float *dv4);
+int spn_tri_finalize_step(spn_tri *h, float new_cutoff);
+/* Correlations corr[10][n_corr] in the order XX XY XZ YX YY YZ ZX ZY ZZ DD, each in the
+ * (basis, site-in-range) order of TRICorXX etc. (TRIMeasurementCorrelation.cpp:255-283), and
+ * chi[16][Nl] per representative (the mixed spin/density components are zero); either
+ * pointer may be NULL. */
+int spn_tri_measure_correlation(spn_tri *h, float *corr, float *chi);
+int spn_tri_is_diverged(spn_tri *h, int *diverged);
+
+/* The coefficient tables the TRI kernels evaluate, as rows (table, output, n, a, b, sign):
+ * table 0 particle-particle ladder, 1 particle-hole ladder, 2 RPA, 3 chalice, 4 inverse
+ * chalice, 5 egg diagram; 1152 rows of 6 ints.  Host only (no device needed). */
+int spn_tri_tables(int *rows);
+
 #ifdef __cplusplus
 }
 #endif

@@ -144,7 +144,8 @@ Tables build_tables() {
             pauli(c1, lam, r, k);
             pauli(r, c2, r2, k2);
             pauli(r2, rho, r3, k3);
-            const int s = r3 == D ? real_sign(k + k2 + k3 + eta(lam, rho)) : 0;
+            // imaginary (odd power) only for the mixed outputs, which the measurement skips
+            const int s = r3 == D && real_sign(k + k2 + k3 + eta(lam, rho)) != -2 ? real_sign(k + k2 + k3 + eta(lam, rho)) : 0;
             T.egg[c][n] = {(signed char)(4 * lam + rho), 0, (signed char)s};
         }
     }
@@ -718,7 +719,7 @@ extern "C" {
 
 // The coefficient tables as (table, output, n, a, b, sign) rows, for inspection by the tests.
 // Tables: 0 = s ladder, 1 = u ladder, 2 = RPA, 3 = chalice, 4 = inverse chalice, 5 = egg.
-// Returns the number of rows (at most 6 * 256), or -1 if the algebra gave an imaginary
+// Returns the number of rows (1152), or -1 if the algebra gave an imaginary
 // coefficient or an inconsistent product.
 int oracle_tri_tables(int *rows) {
     const Tables &T = tables();

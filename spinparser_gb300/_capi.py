@@ -131,6 +131,17 @@ SIGNATURES = {
     "spn_xyz_finalize_step": (C.c_int, [C.c_void_p, C.c_float]),
     "spn_xyz_measure_correlation": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p, c_float_p, c_float_p]),
     "spn_xyz_is_diverged": (C.c_int, [C.c_void_p, c_int_p]),
+    "spn_tri_initial_state": (C.c_int, [C.c_void_p, C.c_int, C.c_float, c_float_p, c_float_p]),
+    "spn_tri_create": (C.c_int, [C.POINTER(XyzDesc), C.POINTER(C.c_void_p)]),
+    "spn_tri_destroy": (C.c_int, [C.c_void_p]),
+    "spn_tri_set_state": (C.c_int, [C.c_void_p, C.c_float, c_float_p, c_float_p]),
+    "spn_tri_get_state": (C.c_int, [C.c_void_p, c_float_p, c_float_p, c_float_p]),
+    "spn_tri_compute_step": (C.c_int, [C.c_void_p]),
+    "spn_tri_get_flow": (C.c_int, [C.c_void_p, c_float_p, c_float_p]),
+    "spn_tri_finalize_step": (C.c_int, [C.c_void_p, C.c_float]),
+    "spn_tri_measure_correlation": (C.c_int, [C.c_void_p, c_float_p, c_float_p]),
+    "spn_tri_is_diverged": (C.c_int, [C.c_void_p, c_int_p]),
+    "spn_tri_tables": (C.c_int, [c_int_p]),
     "spn_su2_set_state_f64": (C.c_int, [C.c_void_p, C.c_float, c_double_p, c_double_p, c_double_p]),
     "spn_su2_get_state_f64": (C.c_int, [C.c_void_p, c_float_p, c_double_p, c_double_p, c_double_p]),
     "spn_su2_get_flow_f64": (C.c_int, [C.c_void_p, c_double_p, c_double_p, c_double_p]),

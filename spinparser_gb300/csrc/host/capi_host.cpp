@@ -4,6 +4,7 @@
 #include "lattice_handle.hpp"
 #include "log.hpp"
 #include "rpa_schedule.hpp"
+#include "../tri_algebra.hpp"
 #include "../../../include/spn_su2.h"
 #include <atomic>
 #include <cmath>
@@ -264,6 +265,52 @@ extern "C" int spn_xyz_initial_state(const spn_lattice *lat, int n_freq, float n
             std::memset(comp[c], 0, sizeof(float) * size_t(fn * nl));
             for (long long it = 0; it < fn; ++it)
                 for (const auto &ia : L.interactions) comp[c][it * nl + ia.rid] += 0.25f * ia.J[c][c] / normalization;
+        }
+    });
+}
+
+extern "C" int spn_tri_initial_state(const spn_lattice *lat, int n_freq, float normalization, float *v2, float *v4) {
+    return spn::guarded([&] {
+        if (!lat || n_freq < 2 || !v4) throw spn::Error(spn::ErrorType::Argument, "spn_tri_initial_state: bad argument");
+        const spn::Lattice &L = lat->lat;
+        const long long nl = L.size;
+        const long long fn = (long long)n_freq * n_freq * (n_freq + 1) / 2;
+        if (v2) std::memset(v2, 0, sizeof(float) * n_freq);
+        std::memset(v4, 0, sizeof(float) * size_t(16 * fn * nl));
+        for (long long it = 0; it < fn; ++it)
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b)
+                    for (const auto &ia : L.interactions)
+                        v4[(it * 16 + 4 * a + b) * nl + ia.rid] += 0.25f * ia.J[a][b] / normalization;
+    });
+}
+
+extern "C" int spn_tri_tables(int *rows) {
+    return spn::guarded([&] {
+        if (!rows) throw spn::Error(spn::ErrorType::Argument, "spn_tri_tables: null argument");
+        namespace T = spn::tri;
+        int n = 0;
+        auto put = [&](int tab, int c, int k, int a, int b, int sg) {
+            int *r = rows + 6 * n++;
+            r[0] = tab; r[1] = c; r[2] = k; r[3] = a; r[4] = b; r[5] = sg;
+        };
+        for (int c = 0; c < 16; ++c) {
+            const int c1 = c >> 2, c2 = c & 3;
+            for (int k = 0; k < 16; ++k) put(0, c, k, 15 - k, (15 - k) ^ c ^ 15, T::pp_sign(c, 15 - k));
+            for (int k = 0; k < 16; ++k) put(1, c, k, 15 - k, (15 - k) ^ c ^ 15, T::ph_sign(c, 15 - k));
+            for (int k = 0; k < 4; ++k) put(2, c, k, 4 * c1 + T::inner(k), 4 * T::inner(k) + c2, T::rpa_sign(c, T::inner(k)));
+            for (int k = 0; k < 16; ++k) {
+                const int kap = T::inner(k >> 2), lam = T::inner(k & 3);
+                put(3, c, k, 4 * c1 + kap, 4 * lam + (c2 ^ kap ^ lam), T::chal_sign(c, kap, lam));
+            }
+            for (int k = 0; k < 16; ++k) {
+                const int l = 15 - k;
+                put(4, c, k, l, 4 * (c1 ^ (l >> 2) ^ (l & 3)) + c2, T::ichal_sign(c, l));
+            }
+            for (int k = 0; k < 4; ++k) {
+                const int lam = T::inner(k);
+                put(5, c, k, 4 * lam + (c1 ^ c2 ^ lam), 0, T::egg_sign(c, lam));
+            }
         }
     });
 }

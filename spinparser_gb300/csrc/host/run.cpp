@@ -29,6 +29,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <ctime>
 #include <dlfcn.h>
 #include <memory>
@@ -73,7 +74,7 @@ std::string fixed6(double v) {
 }
 
 // The numerics core behind the driver (FrgCoreFactory::newFrgCore, src/FrgCoreFactory.cpp:25-51):
-// SU(2) (spn_su2_*) or XYZ (spn_xyz_*).  The driver holds the state on the host in the
+// SU(2) (spn_su2_*), XYZ (spn_xyz_*) or TRI (spn_tri_*).  The driver holds the state on the host in the
 // checkpoint's array order and moves it through these calls.
 class Core {
 public:
@@ -244,6 +245,90 @@ private:
     float normalization_;
 };
 
+class TriCore : public Core {
+public:
+    TriCore(spn_lattice *lat, const std::vector<float> &freq, float normalization, int device)
+        : normalization_(normalization) {
+        spn_lattice_info info;
+        check(spn_lattice_get_info(lat, &info));
+        const int nl = info.n_sites, no = info.n_overlap, nr = info.n_range;
+        n_corr_ = int64_t(info.n_basis) * nr;
+        std::vector<int> srid(nl), irid(nl), optr(nl + 1), o1(no), o2(no), rr(nr), ri(nr), cr(n_corr_);
+        std::vector<int> sp(nl), ip(nl), p1(no), p2(no), rp(nr), rip(nr), cp(n_corr_);
+        check(spn_lattice_get_tables(lat, srid.data(), irid.data(), optr.data(), o1.data(), o2.data(), rr.data(),
+                                     ri.data(), cr.data(), nullptr, nullptr, nullptr));
+        check(spn_lattice_get_spin_tables(lat, sp.data(), ip.data(), p1.data(), p2.data(), rp.data(), rip.data(),
+                                          cp.data()));
+        spn_tri_desc d{};
+        d.n_freq = int(freq.size());
+        d.freq = freq.data();
+        d.n_sites = nl;
+        d.sites_rid = srid.data();
+        d.sites_perm = sp.data();
+        d.inv_sites_rid = irid.data();
+        d.inv_sites_perm = ip.data();
+        d.overlap_ptr = optr.data();
+        d.overlap_rid1 = o1.data();
+        d.overlap_rid2 = o2.data();
+        d.overlap_perm1 = p1.data();
+        d.overlap_perm2 = p2.data();
+        d.n_range = nr;
+        d.range_rid = rr.data();
+        d.range_inv_rid = ri.data();
+        d.n_corr = int(n_corr_);
+        d.corr_rid = cr.data();
+        d.corr_perm = cp.data();
+        d.device = device;
+        check(spn_tri_create(&d, &h_));
+        const int64_t n = int64_t(freq.size());
+        n_v2 = n;
+        n_v4 = n * n * (n + 1) / 2 * 16 * nl;
+        corr_.resize(size_t(10 * n_corr_));
+    }
+    ~TriCore() override { spn_tri_destroy(h_); }
+    const char *id() const override { return "TRI"; }
+    // TRIEffectiveAction::writeCheckpoint (src/TRI/TRIEffectiveAction.hpp:146-148)
+    std::vector<std::string> arrays() const override { return {"v4"}; }
+    // TRIMeasurementCorrelation::takeMeasurement (src/TRI/TRIMeasurementCorrelation.cpp:128-145)
+    std::vector<std::string> obs_groups() const override {
+        return {"TRICorXX", "TRICorXY", "TRICorXZ", "TRICorYX", "TRICorYY", "TRICorYZ", "TRICorZX", "TRICorZY", "TRICorZZ",
+                "TRICorDD"};
+    }
+    // TRIEffectiveAction at the first cutoff (src/TRI/TRIEffectiveAction.hpp:38-62)
+    void initial_state(const spn_lattice *lat, float *v2, std::vector<float *> &v4) override {
+        check(spn_tri_initial_state(lat, int(n_v2), normalization_, v2, v4[0]));
+    }
+    void set_state(float c, const float *v2, const std::vector<float *> &v4) override {
+        check(spn_tri_set_state(h_, c, v2, v4[0]));
+    }
+    void get_state(float &c, float *v2, const std::vector<float *> &v4) override {
+        check(spn_tri_get_state(h_, &c, v2, v4[0]));
+    }
+    void compute_step() override { check(spn_tri_compute_step(h_)); }
+    bool diverged() override {
+        int d = 0;
+        check(spn_tri_is_diverged(h_, &d));
+        return d != 0;
+    }
+    void finalize_step(float c) override { check(spn_tri_finalize_step(h_, c)); }
+    void measure(const std::vector<float *> &out) override {
+        check(spn_tri_measure_correlation(h_, corr_.data(), nullptr));
+        for (size_t q = 0; q < out.size(); ++q)
+            if (out[q]) std::memcpy(out[q], corr_.data() + q * n_corr_, sizeof(float) * size_t(n_corr_));
+    }
+    void synchronize() override {
+        int d = 0;
+        check(spn_tri_is_diverged(h_, &d));  // synchronises the flow's stream
+    }
+    void autotune(float, float) override {}
+
+private:
+    spn_tri *h_ = nullptr;
+    float normalization_;
+    int64_t n_corr_ = 0;
+    std::vector<float> corr_;
+};
+
 class Driver {
 public:
     Driver(Task &task, const spn_run_options &o, spn_run_result &res) : task_(task), o_(o), res_(res) {}
@@ -262,12 +347,11 @@ public:
                 throw Error(ErrorType::Initialization, "Measurement [correlation]: unknown option '" + m.options[0].first + "'.");
             any_deferred_ = any_deferred_ || m.defer;
         }
-        if (task_.symmetry == "TRI")
-            throw Error(ErrorType::Unsupported, "Spin model identifier 'TRI': the TRI core is not part of this build (SU2 and XYZ are).");
-        if (task_.symmetry != "SU2" && task_.symmetry != "XYZ")
+        if (task_.symmetry != "SU2" && task_.symmetry != "XYZ" && task_.symmetry != "TRI")
             throw Error(ErrorType::Argument, "Spin model identifier '" + task_.symmetry + "' does not exist.");
         // core options: model options that are not interaction parameters (src/TaskFileParser.cpp:310-317;
-        // SU2: spin and normalization, src/SU2/SU2FrgCore.cpp:19-29; XYZ: normalization, src/XYZ/XYZFrgCore.cpp:19-28)
+        // SU2: spin and normalization, src/SU2/SU2FrgCore.cpp:19-29; XYZ and TRI: normalization,
+        // src/XYZ/XYZFrgCore.cpp:19-28, src/TRI/TRIFrgCore.cpp:19-28)
         for (const auto &kv : task_.model_options) {
             if (lat_->model.parameters.count(kv.first)) continue;
             if (kv.first == "spin" && task_.symmetry == "SU2") spin_ = float(parse_number(kv.second));
@@ -299,6 +383,7 @@ public:
         check(spn_lattice_get_info(lat_.get(), &info));
         n_corr_ = int64_t(info.n_basis) * info.n_range;
         if (task_.symmetry == "XYZ") core_.reset(new XyzCore(lat_.get(), task_.frequencies, normalization_, o_.device));
+        else if (task_.symmetry == "TRI") core_.reset(new TriCore(lat_.get(), task_.frequencies, normalization_, o_.device));
         else core_.reset(new Su2Core(lat_.get(), task_.frequencies, spin_, normalization_, o_.device, o_.flags));
         v2_.resize(core_->n_v2);
         v4_.assign(core_->arrays().size(), std::vector<float>(core_->n_v4));

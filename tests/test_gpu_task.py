@@ -221,3 +221,78 @@ def test_xyz_checkpoint_resume_equals_uninterrupted_run(tmp_path):
         ca, da = h5lite.read_correlations(a, group)
         cb, db = h5lite.read_correlations(b, group)
         assert np.array_equal(ca, cb) and np.array_equal(da, db)
+
+
+# ---------------------------------------------------------------------------------------
+# TRI core through the driver (test_reference3.sh; test_reference2.sh's TRI task)
+# ---------------------------------------------------------------------------------------
+REF3_RES = os.path.join(GOLDEN, "res_honeycomb")
+TRI_GROUPS = ("TRICorXX", "TRICorXY", "TRICorXZ", "TRICorYX", "TRICorYY", "TRICorYZ", "TRICorZX", "TRICorZY",
+              "TRICorZZ", "TRICorDD")
+
+
+def reference3_task(tmp_path, name="r3.xml", cutoff=None, extra="", g_sign=1.0):
+    g = np.load(os.path.join(GOLDEN, "reference3_tri.npz"))
+    cmax, cmin, step = (float(x) for x in g["cutoff_spec"])
+    cut = cutoff or exponential_cutoffs(f"{cmax:g}", f"{cmin:g}", f"{step:g}")
+    params = f"<j>{float(g['j']):g}</j><k>{float(g['k']):g}</k><g>{g_sign * float(g['g']):g}</g>"
+    return write(tmp_path, name, lattice="honeycomb", rng=3, model="honeycomb-kitaev-gamma", symmetry="TRI",
+                 params=params, freq=manual_frequencies(), cutoff=cut, extra=extra), g
+
+
+def test_reference3_tri_task_reproduces_golden_obs(tmp_path):
+    p, g = reference3_task(tmp_path)
+    s = task.run_task(p, resource_path=REF3_RES, verbose=-1)
+    assert s.status == "finished" and not s.diverged and s.steps == len(g["cutoffs"]) - 1
+    obs = str(tmp_path / "r3.obs")
+    layout = json.load(open(os.path.join(GOLDEN, "reference3_layout.json")))
+    assert h5lite.skeleton(obs) == layout["skeleton"]
+    assert h5lite.layout_fingerprint(obs) == layout["fingerprint"]
+    for group in TRI_GROUPS:
+        cut, data = h5lite.read_correlations(obs, group)
+        assert np.array_equal(cut, g["cutoffs"])
+        assert float(np.abs(data - g[group[-2:].lower()]).max()) < 1e-5, group
+    # the checkpoint holds the TRI vertex as one array (TRIEffectiveAction.hpp:146-148)
+    ck = h5lite.open_file(str(tmp_path / "r3.checkpoint"))["checkpoint_0"]
+    assert ck.keys() == ["cutoff", "v2", "v4"]
+
+
+def test_reference3_tri_sign_flip_fails_golden(tmp_path):
+    """test_referenceFail.sh in TRI form: g -> -g must not reproduce the golden values."""
+    p, g = reference3_task(tmp_path, "f.xml", g_sign=-1.0)
+    task.run_task(p, resource_path=REF3_RES, verbose=-1)
+    _, data = h5lite.read_correlations(str(tmp_path / "f.obs"), "TRICorXY")
+    assert float(np.abs(data - g["xy"]).max()) > 1e-3
+
+
+def test_reference2_tri_task_reproduces_golden_obs(tmp_path):
+    """test_reference2.sh's second task: the XYZ golden through the TRI core."""
+    g = np.load(os.path.join(GOLDEN, "reference2_xyz.npz"))
+    cmax, cmin, step = (float(x) for x in g["cutoff_spec"])
+    p = write(tmp_path, "r2t.xml", lattice="hyperhoneycomb", rng=3, model="hyperhoneycomb-kitaev", symmetry="TRI",
+              params=f"<j>{float(g['j']):g}</j><k>{float(g['k']):g}</k>", freq=manual_frequencies(),
+              cutoff=exponential_cutoffs(f"{cmax:g}", f"{cmin:g}", f"{step:g}"))
+    s = task.run_task(p, resource_path=REF2_RES, verbose=-1)
+    assert s.status == "finished" and not s.diverged
+    obs = str(tmp_path / "r2t.obs")
+    for group, key in (("TRICorXX", "xx"), ("TRICorYY", "yy"), ("TRICorZZ", "zz"), ("TRICorDD", "dd")):
+        cut, data = h5lite.read_correlations(obs, group)
+        assert np.array_equal(cut, g["cutoffs"])
+        assert float(np.abs(data - g[key]).max()) < 1e-5, group
+
+
+def test_tri_checkpoint_resume_equals_uninterrupted_run(tmp_path):
+    full, _ = reference3_task(tmp_path, "full.xml")
+    part, _ = reference3_task(tmp_path, "part.xml", cutoff=exponential_cutoffs("10", "0.5", "0.9"))
+    task.run_task(full, resource_path=REF3_RES, force_restart=True, verbose=-1)
+    first = task.run_task(part, resource_path=REF3_RES, force_restart=True, verbose=-1)
+    assert first.status == "finished"
+    reference3_task(tmp_path, "part.xml", extra='<calculation status="running" startTime="1970-Jan-01 00:00:00" '
+                                                'checkpointTime="1970-Jan-01 00:00:00" />')
+    second = task.run_task(part, resource_path=REF3_RES, verbose=-1)
+    assert second.status == "finished" and 0 < second.steps < first.steps
+    a, b = str(tmp_path / "full.obs"), str(tmp_path / "part.obs")
+    for group in TRI_GROUPS:
+        ca, da = h5lite.read_correlations(a, group)
+        cb, db = h5lite.read_correlations(b, group)
+        assert np.array_equal(ca, cb) and np.array_equal(da, db)

@@ -34,6 +34,14 @@ def test_debug_lattice_writes_ldf_and_needs_no_device(tmp_path):
     assert open(str(tmp_path / "direct.ldf")).read() == ldf
 
 
+@pytest.mark.parametrize("symmetry", ["SU2", "XYZ", "TRI"])
+def test_every_core_identifier_is_accepted(tmp_path, symmetry):
+    """FrgCoreFactory's identifiers (src/FrgCoreFactory.cpp:25-51); the lattice stage needs no
+    device."""
+    s = task.run_task(write(tmp_path, symmetry=symmetry), debug_lattice=True, verbose=-1)
+    assert s.status == "new"
+
+
 def test_cli_debug_lattice(tmp_path, capfd):
     p = write(tmp_path)
     assert cli_main(["--debugLattice", p]) == 0
@@ -61,7 +69,7 @@ def test_cli_debug_lattice(tmp_path, capfd):
     (dict(params="<j>1.0</j><colour>red</colour>"), -3, "Unknown spin model option 'colour'."),
     (dict(params=""), -3, "Interaction parameter 'j' is not defined in the taskfile"),
     (dict(symmetry="U1"), -2, "Spin model identifier 'U1' does not exist."),
-    (dict(symmetry="TRI"), -8, "the TRI core is not part of this build"),
+    (dict(symmetry="su2"), -2, "Spin model identifier 'su2' does not exist."),
     (dict(lattice="nonexistent"), -3, "nonexistent"),
 ])
 def test_task_validation_errors(tmp_path, kw, code, message):
