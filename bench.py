@@ -65,7 +65,7 @@ XYZ_WORKLOADS = {
                                         cmax=50.0, cmin=0.05, cstep=0.98),
 }
 # the TRI core (time-reversal-invariant models with off-diagonal couplings): a
-# Heisenberg-Kitaev-Gamma flow; the first --steps cutoffs of the list are timed
+# Heisenberg-Kitaev-Gamma flow
 TRI_WORKLOADS = {
     "tri-honeycomb-kitaev-gamma-r9-n32": dict(lattice="honeycomb", range=9, model="honeycomb-kitaev-gamma",
                                               params={"j": "0.2", "k": "1.0", "g": "-0.1"}, n_freq=32, fmin=0.005,
@@ -474,10 +474,9 @@ def run_precision(args):
 
 
 def run_xyz(args):
-    """The XYZ or TRI core: one flow on the GPU (device-resident state, measurement at every
-    cutoff, as the driver runs it; XYZ the whole cutoff list, TRI its first --steps cutoffs),
-    against the core's oracle on the host cores (two right-hand sides at cutoffs a third and two
-    thirds into the timed list)."""
+    """The XYZ or TRI core: one whole flow on the GPU (device-resident state, measurement at
+    every cutoff, as the driver runs it), against the core's oracle on the host cores (two
+    right-hand sides at cutoffs a third and two thirds into the flow)."""
     import torch
 
     import spinparser_gb300 as spn
@@ -491,7 +490,6 @@ def run_xyz(args):
     cut = spn.cutoff_exponential(wl["cmax"], wl["cmin"], wl["cstep"])
     n_cut = len(cut)
     if tri:
-        cut = cut[:args.steps + 1]
         init = spn.tri_initial_state(lat, len(freq))
         flow = spn.TriFlow(tab, st, freq)
     else:
@@ -517,8 +515,7 @@ def run_xyz(args):
         "config": {"workload": args.workload, **{k: wl[k] for k in ("lattice", "range", "model", "params", "n_freq")},
                    "cutoff": [wl["cmax"], wl["cmin"], wl["cstep"]], "n_cutoffs": n_cut, "n_sites": tab.n_sites,
                    "n_overlap": tab.n_overlap,
-                   "timed": ("the first %d cutoff steps" % steps if tri else "the whole flow") +
-                            ", measurement at every cutoff"},
+                   "timed": "the whole flow, measurement at every cutoff"},
         "diverged": diverged, "clocks": clocks,
     }
     if not args.no_cpu_baseline:
