@@ -89,6 +89,8 @@ def parse_args():
     ap.add_argument("--policy", type=str, default="fifo",
                     help="serve-mixed: server arms to run at every rate, comma separated: fifo or sjf, "
                          "optionally @k for a k-flow slot limit (e.g. fifo,sjf@2)")
+    ap.add_argument("--flow-cutoffs", type=int, default=None,
+                    help="XYZ/TRI workloads: run only the first M cutoffs of the flow (short runs for profiling)")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU work budget of the baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -489,6 +491,8 @@ def run_xyz(args):
     freq = spn.frequency_exponential(wl["fmin"], wl["fmax"], wl["n_freq"])
     cut = spn.cutoff_exponential(wl["cmax"], wl["cmin"], wl["cstep"])
     n_cut = len(cut)
+    if args.flow_cutoffs:
+        cut = cut[:max(args.flow_cutoffs, 2)]
     if tri:
         init = spn.tri_initial_state(lat, len(freq))
         flow = spn.TriFlow(tab, st, freq)
@@ -515,7 +519,8 @@ def run_xyz(args):
         "config": {"workload": args.workload, **{k: wl[k] for k in ("lattice", "range", "model", "params", "n_freq")},
                    "cutoff": [wl["cmax"], wl["cmin"], wl["cstep"]], "n_cutoffs": n_cut, "n_sites": tab.n_sites,
                    "n_overlap": tab.n_overlap,
-                   "timed": "the whole flow, measurement at every cutoff"},
+                   "timed": ("the first %d cutoffs" % len(cut) if args.flow_cutoffs else "the whole flow") +
+                            ", measurement at every cutoff"},
         "diverged": diverged, "clocks": clocks,
     }
     if not args.no_cpu_baseline:
