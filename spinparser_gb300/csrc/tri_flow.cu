@@ -15,7 +15,7 @@
 // A step: the self-energy flow (one CTA per frequency), the loop-frequency node tables (the
 // SU(2) core's, shared), the vertex flow and the Euler update.  The vertex-flow kernel runs a
 // persistent grid whose warps take one (s,t,u) triple at a time from a device counter.  Per
-// channel, nodes go in batches of 32: each lane first builds one node's access buffers into a
+// channel, nodes go in batches of 16: a lane first builds one node's access buffers into a
 // shared-memory descriptor; then, node by node, the warp gathers the four 16-component slabs
 // of all sites into shared memory (t: and the 64 site-local values of the chalice diagrams),
 // and each lane evaluates the products for its sites from registers.
@@ -39,7 +39,7 @@ namespace {
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxSites = 128;
-constexpr int kTBatch = 32;  // nodes whose descriptors a warp builds at once
+constexpr int kTBatch = 16;  // nodes whose descriptors a warp builds at once
 constexpr int kCorrOut = 10;  // XX XY XZ YX YY YZ ZX ZY ZZ DD
 
 // The six spin permutations (X,Y,Z) (X,Z,Y) (Y,X,Z) (Y,Z,X) (Z,X,Y) (Z,Y,X): 2 bits per image
@@ -335,6 +335,39 @@ __device__ __forceinline__ void make_tdesc(const TriArgs &a, const float *pos, i
     d.c = c;
 }
 
+// One slab of a node for all sites (getValueSuperbundle): goff[e][c][j] is the offset of
+// component c of site j, e = 1 for the site-exchanged pair (components swapped, then permuted,
+// plus the representative's rid).  The sign of support i depends on the component only through
+// zeta(a) and zeta(b), so the four signed weights of each zeta class are formed once.
+__device__ __forceinline__ void gather_slab(const float *__restrict__ v4, const TAB4 &ab, const int *goff, int nl, int lane,
+                                            float *S) {
+    const int fl = ab.fl;
+    const bool ex = fl & kFlExch, tu = fl & kFlTu;
+    float sw[4][4];  // [class: bit 0 a is a spin component, bit 1 b is][support]
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float za = (k & 1) ? -1.0f : 1.0f, zb = (k & 2) ? -1.0f : 1.0f;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            float sg = tu ? za * zb : 1.0f;
+            if ((fl >> i) & 1) sg *= -(ex ? za : zb);
+            sw[k][i] = sg * ab.w[i];
+        }
+    }
+    const int *g = goff + (ex ? 16 * nl : 0);
+    for (int j = lane; j < nl; j += 32) {
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+            const int k = ((c >> 2) < 3 ? 1 : 0) | ((c & 3) < 3 ? 2 : 0);
+            const int o = g[c * nl + j];
+            float v = 0.0f;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) v += sw[k][i] * __ldg(v4 + ab.off[i] + o);
+            S[c * nl + j] = v;
+        }
+    }
+}
+
 // The two ladders for one site: per output c, a = 15..0 with the slab pairs (0,1) and (2,3)
 // (TRIFrgCore.cpp:198-711 particle-particle, 2389-2902 particle-hole).
 template <bool PH>
@@ -368,8 +401,11 @@ __device__ __forceinline__ void ladder(const float *S, int nl, int j, float *r) 
 // The t integrand for one site j (TRIFrgCore.cpp:733-2368): the RPA lattice sum over the
 // overlap pairs of rid j (4x4 products over the inner spin index, the factors' components
 // permuted by the pair's maps), then the chalice diagrams with the site-local values L.
-__device__ __forceinline__ void t_terms(const TriArgs &a, const float *S, const float *L, const unsigned char (*P16)[16],
-                                        int nl, int j, float *r) {
+// PN[p][c]: offset of component c permuted by p (4 P(a) + P(b)) times nl.  The RPA sums
+// the products without the factor 2 of the reference's terms and doubles the sum: scaling by
+// 2 commutes with every rounding, so the result is the same.
+__device__ __forceinline__ void t_terms(const TriArgs &a, const float *S, const float *L, const int (*PN)[16], int nl,
+                                        int j, float *r) {
     const float *S0 = S, *S1 = S + 16 * nl, *S2 = S + 32 * nl, *S3 = S + 48 * nl;
     float v[16];
 #pragma unroll
@@ -378,14 +414,20 @@ __device__ __forceinline__ void t_terms(const TriArgs &a, const float *S, const 
     for (int i = a.ov_ptr[j]; i < i1; ++i) {
         const int e = __ldg(a.ov_pk + i);
         const int r1 = e & 127, r2 = (e >> 7) & 127, p1 = (e >> 14) & 7, p2 = (e >> 17) & 7;
+        const int4 *pa = reinterpret_cast<const int4 *>(PN[p1]), *pb = reinterpret_cast<const int4 *>(PN[p2]);
         float x0[16], x2[16], y1[16], y3[16];
 #pragma unroll
-        for (int c = 0; c < 16; ++c) {
-            const int q1 = P16[p1][c] * nl + r1, q2 = P16[p2][c] * nl + r2;
-            x0[c] = S0[q1];
-            x2[c] = S2[q1];
-            y1[c] = S1[q2];
-            y3[c] = S3[q2];
+        for (int q = 0; q < 4; ++q) {
+            const int4 oa = pa[q], ob = pb[q];
+            const int qa[4] = {oa.x + r1, oa.y + r1, oa.z + r1, oa.w + r1};
+            const int qb[4] = {ob.x + r2, ob.y + r2, ob.z + r2, ob.w + r2};
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                x0[4 * q + u] = S0[qa[u]];
+                x2[4 * q + u] = S2[qa[u]];
+                y1[4 * q + u] = S1[qb[u]];
+                y3[4 * q + u] = S3[qb[u]];
+            }
         }
 #pragma unroll
         for (int c = 0; c < 16; ++c) {
@@ -393,18 +435,18 @@ __device__ __forceinline__ void t_terms(const TriArgs &a, const float *S, const 
 #pragma unroll
             for (int n = 0; n < 4; ++n) {
                 const int k = tri::inner(n);
-                const float t0 = 2.0f * x0[4 * mu + k] * y1[4 * k + nu];
-                const float t1 = 2.0f * x2[4 * mu + k] * y3[4 * k + nu];
                 if (tri::rpa_sign(c, k) > 0) {
-                    v[c] += t0;
-                    v[c] += t1;
+                    v[c] += x0[4 * mu + k] * y1[4 * k + nu];
+                    v[c] += x2[4 * mu + k] * y3[4 * k + nu];
                 } else {
-                    v[c] -= t0;
-                    v[c] -= t1;
+                    v[c] -= x0[4 * mu + k] * y1[4 * k + nu];
+                    v[c] -= x2[4 * mu + k] * y3[4 * k + nu];
                 }
             }
         }
     }
+#pragma unroll
+    for (int c = 0; c < 16; ++c) v[c] *= 2.0f;
     {  // chalice: slabs 0 and 2 with the local values of ab4, ab5
         float X0[16], X2[16];
 #pragma unroll
@@ -458,28 +500,31 @@ __device__ __forceinline__ void t_terms(const TriArgs &a, const float *S, const 
 __host__ __device__ constexpr size_t tri_warp_floats(int nl) {
     return 80 * size_t(nl) + 64 + kTBatch * (sizeof(TDesc) / sizeof(float));
 }
+// per CTA: the gather offsets goff[2][16][nl] (ints), then the warps' areas
+__host__ __device__ constexpr size_t tri_cta_head_floats(int nl) { return (32 * size_t(nl) + 3) / 4 * 4; }
 
 __global__ void __launch_bounds__(kThreads) tri_vertex_kernel(TriArgs a) {
     __shared__ float pos[kMaxFreq];
-    __shared__ int srid[kMaxSites], sprm[kMaxSites], irid[kMaxSites], iprm[kMaxSites];
-    __shared__ unsigned char P16[6][16];
-    // per warp: slabs S[4][16][nl], accumulator acc[16][nl], local values L[64], descriptors
+    __shared__ __align__(16) int PN[6][16];
+    // per CTA: gather offsets goff[2][16][nl]; per warp: slabs S[4][16][nl], accumulator
+    // acc[16][nl], local values L[64], node descriptors
     extern __shared__ __align__(16) float tsm[];
     const int n = a.n, nl = a.nl;
+    int *goff = reinterpret_cast<int *>(tsm);
     for (int i = threadIdx.x; i < n; i += blockDim.x) pos[i] = a.freq[i];
-    for (int i = threadIdx.x; i < nl; i += blockDim.x) {
-        srid[i] = a.sites[i];
-        sprm[i] = a.sites_perm[i];
-        irid[i] = a.inv_sites[i];
-        iprm[i] = a.inv_sites_perm[i];
+    for (int i = threadIdx.x; i < 32 * nl; i += blockDim.x) {
+        const int e = i / (16 * nl), c = (i / nl) & 15, j = i % nl;
+        const int ca = c >> 2, cb = c & 3;
+        const int r = e ? a.inv_sites[j] : a.sites[j], p = e ? a.inv_sites_perm[j] : a.sites_perm[j];
+        goff[i] = (4 * permc(p, e ? cb : ca) + permc(p, e ? ca : cb)) * nl + r;
     }
     for (int i = threadIdx.x; i < 96; i += blockDim.x) {
         const int p = i >> 4, c = i & 15;
-        P16[p][c] = (unsigned char)(4 * permc(p, c >> 2) + permc(p, c & 3));
+        PN[p][c] = (4 * permc(p, c >> 2) + permc(p, c & 3)) * nl;
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float *S = tsm + size_t(warp) * tri_warp_floats(nl);
+    float *S = tsm + tri_cta_head_floats(nl) + size_t(warp) * tri_warp_floats(nl);
     float *acc = S + 64 * nl;
     float *L = acc + 16 * nl;
     TDesc *desc = reinterpret_cast<TDesc *>(L + 64);
@@ -512,13 +557,8 @@ __global__ void __launch_bounds__(kThreads) tri_vertex_kernel(TriArgs a) {
                 for (int b = 0; b < nb; ++b) {
                     const TDesc &d = desc[b];
                     // gather the four slabs of all sites
-                    for (int q = lane; q < 64 * nl; q += 32) {
-                        const int slab = q / (16 * nl), rem = q - slab * 16 * nl;
-                        const int c = rem / nl, j = rem - c * nl;
-                        const TAB4 &ab = d.ab[slab];
-                        const bool ex = ab.fl & kFlExch;
-                        S[q] = tri_bundle(a.v4, nl, ab, c, ex ? irid[j] : srid[j], ex ? iprm[j] : sprm[j]);
-                    }
+#pragma unroll 1
+                    for (int q = 0; q < 4; ++q) gather_slab(a.v4, d.ab[q], goff, nl, lane, S + q * 16 * nl);
                     if (ch == 1)
                         for (int q = lane; q < 64; q += 32) L[q] = tri_local(a.v4, nl, d.ab[4 + (q >> 4)], (q & 15) >> 2, q & 3);
                     __syncwarp();
@@ -527,7 +567,7 @@ __global__ void __launch_bounds__(kThreads) tri_vertex_kernel(TriArgs a) {
                         float r[16];
                         if (ch == 0) ladder<false>(S, nl, j, r);
                         else if (ch == 2) ladder<true>(S, nl, j, r);
-                        else t_terms(a, S, L, P16, nl, j, r);
+                        else t_terms(a, S, L, PN, nl, j, r);
 #pragma unroll
                         for (int c = 0; c < 16; ++c) acc[c * nl + j] += cw * r[c];
                     }
@@ -684,7 +724,7 @@ void h2d(T *dst, const T *src, size_t count, cudaStream_t s) {
 
 int copy_grid(long long n) { return int(std::min<long long>((n + 255) / 256, 4096)); }
 
-size_t vertex_smem(int nl) { return size_t(kWarps) * tri_warp_floats(nl) * sizeof(float); }
+size_t vertex_smem(int nl) { return (tri_cta_head_floats(nl) + size_t(kWarps) * tri_warp_floats(nl)) * sizeof(float); }
 
 }  // namespace
 
