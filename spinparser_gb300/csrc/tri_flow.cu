@@ -847,6 +847,82 @@ void validate(const spn_tri_desc *d) {
     in_range(d->corr_perm, d->n_corr, 6, "corr_perm");
 }
 
+// The RPA pairs of each site, packed (rid1 | rid2 << 7 | perm1 << 14 | perm2 << 17) and put in
+// an order that keeps the shared-memory reads of a warp apart.  Lane j of a warp walks the
+// pairs of site j, and at step k the 32 lanes read, for every component c, the slab words
+// PN[perm][c] + rid of their k-th pair.  Two lanes whose different words fall into one bank
+// serialise.  Any order of a site's pairs gives the same sum up to rounding, so the pairs are
+// chosen greedily, step by step and site by site, with the fewest new bank collisions.
+std::vector<int> order_rpa_pairs(const spn_tri_desc *d) {
+    const int nl = d->n_sites;
+    const int *ptr = d->overlap_ptr;
+    std::vector<int> out(static_cast<size_t>(ptr[nl]), 0);
+    int pn[6][16];
+    for (int p = 0; p < 6; ++p)
+        for (int c = 0; c < 16; ++c) pn[p][c] = (4 * permc(p, c >> 2) + permc(p, c & 3)) * nl;
+    for (int g0 = 0; g0 < nl; g0 += 32) {
+        const int g1 = std::min(nl, g0 + 32);
+        std::vector<std::vector<int>> rem(g1 - g0);
+        for (int j = g0; j < g1; ++j)
+            for (int i = ptr[j]; i < ptr[j + 1]; ++i) rem[j - g0].push_back(i);
+        std::vector<int> fill(g1 - g0, 0);
+        for (;;) {
+            bool any = false;
+            // words already read in this step: per component and side, per bank
+            std::vector<int> occ(2 * 16 * 32 * 4, -1);  // up to 4 distinct words kept per bank
+            auto conflicts = [&](int side, int c, int word) {
+                const int *o = &occ[((side * 16 + c) * 32 + word % 32) * 4];
+                bool same = false, other = false;
+                for (int k = 0; k < 4; ++k) {
+                    if (o[k] < 0) break;
+                    if (o[k] == word) same = true;
+                    else other = true;
+                }
+                return (other && !same) ? 1 : 0;
+            };
+            auto take = [&](int side, int c, int word) {
+                int *o = &occ[((side * 16 + c) * 32 + word % 32) * 4];
+                for (int k = 0; k < 4; ++k) {
+                    if (o[k] == word) return;
+                    if (o[k] < 0) {
+                        o[k] = word;
+                        return;
+                    }
+                }
+            };
+            for (int j = g0; j < g1; ++j) {
+                std::vector<int> &cand = rem[j - g0];
+                if (cand.empty()) continue;
+                any = true;
+                size_t best = 0;
+                int best_cost = 1 << 30;
+                for (size_t q = 0; q < cand.size() && best_cost > 0; ++q) {
+                    const int i = cand[q];
+                    const int r1 = d->overlap_rid1[i], p1 = d->overlap_perm1[i];
+                    const int r2 = d->overlap_rid2[i], p2 = d->overlap_perm2[i];
+                    int cost = 0;
+                    for (int c = 0; c < 16; ++c) cost += conflicts(0, c, pn[p1][c] + r1) + conflicts(1, c, pn[p2][c] + r2);
+                    if (cost < best_cost) {
+                        best_cost = cost;
+                        best = q;
+                    }
+                }
+                const int i = cand[best];
+                cand.erase(cand.begin() + long(best));
+                const int r1 = d->overlap_rid1[i], p1 = d->overlap_perm1[i];
+                const int r2 = d->overlap_rid2[i], p2 = d->overlap_perm2[i];
+                for (int c = 0; c < 16; ++c) {
+                    take(0, c, pn[p1][c] + r1);
+                    take(1, c, pn[p2][c] + r2);
+                }
+                out[size_t(ptr[j] + fill[j - g0]++)] = r1 | r2 << 7 | p1 << 14 | p2 << 17;
+            }
+            if (!any) break;
+        }
+    }
+    return out;
+}
+
 void launch_correlation(spn_tri *h) {
     const TriArgs a = h->args();
     tri_corr_inner_kernel<<<2 * h->n + 4, 128, size_t(kWarps) * kCorrOut * h->nl * sizeof(double), h->stream>>>(a);
@@ -897,9 +973,7 @@ extern "C" int spn_tri_create(const spn_tri_desc *d, spn_tri **out) {
             put(d->inv_sites_rid, nl);
             put(d->inv_sites_perm, nl);
             put(d->overlap_ptr, nl + 1);
-            std::vector<int> packed(nov);
-            for (int i = 0; i < nov; ++i)
-                packed[i] = d->overlap_rid1[i] | d->overlap_rid2[i] << 7 | d->overlap_perm1[i] << 14 | d->overlap_perm2[i] << 17;
+            const std::vector<int> packed = order_rpa_pairs(d);
             put(packed.data(), nov);
             put(d->range_rid, nr);
             put(d->range_inv_rid, nr);
