@@ -61,7 +61,8 @@ struct TriArgs {
     float *dv2;
     const int *sites, *sites_perm, *inv_sites, *inv_sites_perm;
     const int *ov_ptr;
-    const int *ov_pk;  // rid1 | rid2 << 7 | perm1 << 14 | perm2 << 17 per pair
+    const int *ov_pk;  // per pair: rid1 | rid2 << 7 | the images of X, Y, Z under perm1 (2 bits
+                       // each) << 14 | the same for perm2 << 20
     const int *range_rid, *range_inv;
     const float *node_wp, *node_c;
     const int *node_cnt;
@@ -401,11 +402,11 @@ __device__ __forceinline__ void ladder(const float *S, int nl, int j, float *r) 
 // The t integrand for one site j (TRIFrgCore.cpp:733-2368): the RPA lattice sum over the
 // overlap pairs of rid j (4x4 products over the inner spin index, the factors' components
 // permuted by the pair's maps), then the chalice diagrams with the site-local values L.
-// PN[p][c]: offset of component c permuted by p (4 P(a) + P(b)) times nl.  The RPA sums
+// The RPA reads component (P a, P b) of a factor at (4 P(a) + P(b)) nl + rid: a row base per
+// a plus a column offset per b, from the permutation images packed into the pair word.  It sums
 // the products without the factor 2 of the reference's terms and doubles the sum: scaling by
 // 2 commutes with every rounding, so the result is the same.
-__device__ __forceinline__ void t_terms(const TriArgs &a, const float *S, const float *L, const int (*PN)[16], int nl,
-                                        int j, float *r) {
+__device__ __forceinline__ void t_terms(const TriArgs &a, const float *S, const float *L, int nl, int j, float *r) {
     const float *S0 = S, *S1 = S + 16 * nl, *S2 = S + 32 * nl, *S3 = S + 48 * nl;
     float v[16];
 #pragma unroll
@@ -413,20 +414,24 @@ __device__ __forceinline__ void t_terms(const TriArgs &a, const float *S, const 
     const int i1 = a.ov_ptr[j + 1];
     for (int i = a.ov_ptr[j]; i < i1; ++i) {
         const int e = __ldg(a.ov_pk + i);
-        const int r1 = e & 127, r2 = (e >> 7) & 127, p1 = (e >> 14) & 7, p2 = (e >> 17) & 7;
-        const int4 *pa = reinterpret_cast<const int4 *>(PN[p1]), *pb = reinterpret_cast<const int4 *>(PN[p2]);
+        const int r1 = e & 127, r2 = (e >> 7) & 127;
+        int col1[4], col2[4];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            col1[q] = ((e >> (14 + 2 * q)) & 3) * nl;
+            col2[q] = ((e >> (20 + 2 * q)) & 3) * nl;
+        }
+        col1[3] = col2[3] = 3 * nl;
         float x0[16], x2[16], y1[16], y3[16];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            const int4 oa = pa[q], ob = pb[q];
-            const int qa[4] = {oa.x + r1, oa.y + r1, oa.z + r1, oa.w + r1};
-            const int qb[4] = {ob.x + r2, ob.y + r2, ob.z + r2, ob.w + r2};
+            const int ra = 4 * col1[q] + r1, rb = 4 * col2[q] + r2;
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-                x0[4 * q + u] = S0[qa[u]];
-                x2[4 * q + u] = S2[qa[u]];
-                y1[4 * q + u] = S1[qb[u]];
-                y3[4 * q + u] = S3[qb[u]];
+                x0[4 * q + u] = S0[ra + col1[u]];
+                x2[4 * q + u] = S2[ra + col1[u]];
+                y1[4 * q + u] = S1[rb + col2[u]];
+                y3[4 * q + u] = S3[rb + col2[u]];
             }
         }
 #pragma unroll
@@ -505,7 +510,6 @@ __host__ __device__ constexpr size_t tri_cta_head_floats(int nl) { return (32 * 
 
 __global__ void __launch_bounds__(kThreads) tri_vertex_kernel(TriArgs a) {
     __shared__ float pos[kMaxFreq];
-    __shared__ __align__(16) int PN[6][16];
     // per CTA: gather offsets goff[2][16][nl]; per warp: slabs S[4][16][nl], accumulator
     // acc[16][nl], local values L[64], node descriptors
     extern __shared__ __align__(16) float tsm[];
@@ -517,10 +521,6 @@ __global__ void __launch_bounds__(kThreads) tri_vertex_kernel(TriArgs a) {
         const int ca = c >> 2, cb = c & 3;
         const int r = e ? a.inv_sites[j] : a.sites[j], p = e ? a.inv_sites_perm[j] : a.sites_perm[j];
         goff[i] = (4 * permc(p, e ? cb : ca) + permc(p, e ? ca : cb)) * nl + r;
-    }
-    for (int i = threadIdx.x; i < 96; i += blockDim.x) {
-        const int p = i >> 4, c = i & 15;
-        PN[p][c] = (4 * permc(p, c >> 2) + permc(p, c & 3)) * nl;
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -567,7 +567,7 @@ __global__ void __launch_bounds__(kThreads) tri_vertex_kernel(TriArgs a) {
                         float r[16];
                         if (ch == 0) ladder<false>(S, nl, j, r);
                         else if (ch == 2) ladder<true>(S, nl, j, r);
-                        else t_terms(a, S, L, PN, nl, j, r);
+                        else t_terms(a, S, L, nl, j, r);
 #pragma unroll
                         for (int c = 0; c < 16; ++c) acc[c * nl + j] += cw * r[c];
                     }
@@ -847,10 +847,10 @@ void validate(const spn_tri_desc *d) {
     in_range(d->corr_perm, d->n_corr, 6, "corr_perm");
 }
 
-// The RPA pairs of each site, packed (rid1 | rid2 << 7 | perm1 << 14 | perm2 << 17) and put in
+// The RPA pairs of each site, packed (see TriArgs::ov_pk) and put in
 // an order that keeps the shared-memory reads of a warp apart.  Lane j of a warp walks the
 // pairs of site j, and at step k the 32 lanes read, for every component c, the slab words
-// PN[perm][c] + rid of their k-th pair.  Two lanes whose different words fall into one bank
+// pn[perm][c] + rid of their k-th pair.  Two lanes whose different words fall into one bank
 // serialise.  Any order of a site's pairs gives the same sum up to rounding, so the pairs are
 // chosen greedily, step by step and site by site, with the fewest new bank collisions.
 std::vector<int> order_rpa_pairs(const spn_tri_desc *d) {
@@ -915,7 +915,9 @@ std::vector<int> order_rpa_pairs(const spn_tri_desc *d) {
                     take(0, c, pn[p1][c] + r1);
                     take(1, c, pn[p2][c] + r2);
                 }
-                out[size_t(ptr[j] + fill[j - g0]++)] = r1 | r2 << 7 | p1 << 14 | p2 << 17;
+                int word = r1 | r2 << 7;
+                for (int q = 0; q < 3; ++q) word |= permc(p1, q) << (14 + 2 * q) | permc(p2, q) << (20 + 2 * q);
+                out[size_t(ptr[j] + fill[j - g0]++)] = word;
             }
             if (!any) break;
         }
