@@ -36,7 +36,7 @@ namespace {
 
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
-constexpr int kSpt = 4;  // sites per lane (Nl <= 128)
+constexpr int kSpt = 4;  // sites per lane at most (Nl <= 128); the vertex kernel takes 1, 2 or 4
 constexpr int X = 0, Y = 1, Z = 2, D = 3;
 
 // The six spin permutations (X,Y,Z) (X,Z,Y) (Y,X,Z) (Y,Z,X) (Z,X,Y) (Z,Y,X): 2 bits per image
@@ -120,16 +120,19 @@ __global__ void xyz_node_table_kernel(FlowArgs f) { node_table_body(f, blockIdx.
 // ------------------------------------------------------------------------------------
 // vertex flow
 // ------------------------------------------------------------------------------------
-struct Lane4 {
-    int j[kSpt], rid[kSpt], prm[kSpt], irid[kSpt], iprm[kSpt];
-    bool valid[kSpt];
+template <int SPT>
+struct LaneT {
+    int j[SPT], rid[SPT], prm[SPT], irid[SPT], iprm[SPT];
+    bool valid[SPT];
 };
+using Lane4 = LaneT<kSpt>;
 
 // Interpolated slab of one access buffer for the lane's sites (getValueSuperbundle): X, Y, Z
 // of site j read the permuted components of its representative, D the signed density.
-__device__ __forceinline__ void gather4(const XyzArgs &a, const AB4 &ab, const Lane4 &ln, float4 *out) {
+template <int SPT>
+__device__ __forceinline__ void gather4(const XyzArgs &a, const AB4 &ab, const LaneT<SPT> &ln, float4 *out) {
 #pragma unroll
-    for (int k = 0; k < kSpt; ++k) {
+    for (int k = 0; k < SPT; ++k) {
         float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (ln.valid[k]) {
             const int r = ab.exch ? ln.irid[k] : ln.rid[k];
@@ -242,7 +245,8 @@ __device__ __forceinline__ void make_xdesc(const XyzArgs &a, const float *pos, i
 }
 
 // Phase B gather of buffer i of a descriptor (see gather4).
-__device__ __forceinline__ void gather_desc(const XyzArgs &a, const XDesc &d, int i, const Lane4 &ln, float4 *out) {
+template <int SPT>
+__device__ __forceinline__ void gather_desc(const XyzArgs &a, const XDesc &d, int i, const LaneT<SPT> &ln, float4 *out) {
     AB4 ab;
     const int4 o = d.off[i];
     const float4 w = d.w[i], sw = d.sw[i];
@@ -255,6 +259,7 @@ __device__ __forceinline__ void gather_desc(const XyzArgs &a, const XDesc &d, in
 
 constexpr int kXBatch = 32;  // nodes whose descriptors a warp builds at once
 
+template <int SPT>
 __global__ void __launch_bounds__(kThreads) xyz_vertex_kernel(XyzArgs a) {
     __shared__ float pos[kMaxFreq];
     // per warp: kXBatch node descriptors, then the first two t slabs of every site in all six
@@ -267,9 +272,9 @@ __global__ void __launch_bounds__(kThreads) xyz_vertex_kernel(XyzArgs a) {
     const int warp_f4 = kXBatch * int(sizeof(XDesc) / sizeof(float4)) + 12 * nl;
     XDesc *desc = reinterpret_cast<XDesc *>(xs + size_t(warp) * warp_f4);
     float4 *A6 = xs + size_t(warp) * warp_f4 + kXBatch * (sizeof(XDesc) / sizeof(float4)), *B6 = A6 + 6 * nl;
-    Lane4 ln;
+    LaneT<SPT> ln;
 #pragma unroll
-    for (int k = 0; k < kSpt; ++k) {
+    for (int k = 0; k < SPT; ++k) {
         const int j = lane + 32 * k;
         ln.j[k] = j;
         ln.valid[k] = j < nl;
@@ -293,9 +298,9 @@ __global__ void __launch_bounds__(kThreads) xyz_vertex_kernel(XyzArgs a) {
         const float s = pos[si], t = pos[ti], u = pos[ui];
         const float w1p = 0.5f * (s + t + u), w1 = 0.5f * (s - t + u), w2p = 0.5f * (s - t - u), w2 = 0.5f * (s + t - u);
 
-        float4 acc[kSpt];
+        float4 acc[SPT];
 #pragma unroll
-        for (int k = 0; k < kSpt; ++k) acc[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        for (int k = 0; k < SPT; ++k) acc[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         for (int ch = 0; ch < 3; ++ch) {
             const int xi = ch == 0 ? si : (ch == 1 ? ti : ui);
             const int cnt = a.node_cnt[xi];
@@ -308,26 +313,26 @@ __global__ void __launch_bounds__(kThreads) xyz_vertex_kernel(XyzArgs a) {
                 __syncwarp();
                 for (int b = 0; b < nb; ++b) {  // phase B: lane = site
                     const XDesc &d = desc[b];
-                    float4 S0[kSpt], S1[kSpt], S2[kSpt], S3[kSpt], r[kSpt];
+                    float4 S0[SPT], S1[SPT], S2[SPT], S3[SPT], r[SPT];
                     gather_desc(a, d, 0, ln, S0);
                     gather_desc(a, d, 1, ln, S1);
                     gather_desc(a, d, 2, ln, S2);
                     gather_desc(a, d, 3, ln, S3);
                     if (ch == 0) {  // XYZFrgCore.cpp:229-261
 #pragma unroll
-                        for (int k = 0; k < kSpt; ++k) {
+                        for (int k = 0; k < SPT; ++k) {
                             const float4 p = s_terms(S0[k], S1[k]), q = s_terms(S2[k], S3[k]);
                             r[k] = make_float4(p.x + q.x, p.y + q.y, p.z + q.z, p.w + q.w);
                         }
                     } else if (ch == 2) {  // XYZFrgCore.cpp:436-469
 #pragma unroll
-                        for (int k = 0; k < kSpt; ++k) {
+                        for (int k = 0; k < SPT; ++k) {
                             const float4 p = u_terms(S0[k], S1[k]), q = u_terms(S2[k], S3[k]);
                             r[k] = make_float4(p.x + q.x, p.y + q.y, p.z + q.z, p.w + q.w);
                         }
                     } else {  // t channel: RPA over the first two slabs of all sites, then local terms
 #pragma unroll
-                        for (int k = 0; k < kSpt; ++k)
+                        for (int k = 0; k < SPT; ++k)
                             if (ln.valid[k]) {
                                 const int j = ln.j[k];
                                 A6[0 * nl + j] = permuted<0>(S0[k]);
@@ -348,7 +353,7 @@ __global__ void __launch_bounds__(kThreads) xyz_vertex_kernel(XyzArgs a) {
                         const float cbv[4] = {cb.x, cb.y, cb.z, cb.w}, icav[4] = {ica.x, ica.y, ica.z, ica.w};
                         const float cb2v[4] = {cb2.x, cb2.y, cb2.z, cb2.w}, ica2v[4] = {ica2.x, ica2.y, ica2.z, ica2.w};
 #pragma unroll
-                        for (int k = 0; k < kSpt; ++k) {
+                        for (int k = 0; k < SPT; ++k) {
                             float rp[4] = {0.0f, 0.0f, 0.0f, 0.0f};
                             if (ln.valid[k]) {  // XYZFrgCore.cpp:282-305
                                 const int rid = ln.j[k];
@@ -416,7 +421,7 @@ __global__ void __launch_bounds__(kThreads) xyz_vertex_kernel(XyzArgs a) {
                     }
                     const float c = d.c;
 #pragma unroll
-                    for (int k = 0; k < kSpt; ++k) {
+                    for (int k = 0; k < SPT; ++k) {
                         acc[k].x += c * r[k].x;
                         acc[k].y += c * r[k].y;
                         acc[k].z += c * r[k].z;
@@ -427,7 +432,7 @@ __global__ void __launch_bounds__(kThreads) xyz_vertex_kernel(XyzArgs a) {
             }
         }
 #pragma unroll
-        for (int k = 0; k < kSpt; ++k)
+        for (int k = 0; k < SPT; ++k)
             if (ln.valid[k]) {
                 const float4 o = make_float4(acc[k].x / two_pi, acc[k].y / two_pi, acc[k].z / two_pi, acc[k].w / two_pi);
                 a.dsd[size_t(it) * nl + ln.j[k]] = o;
@@ -593,6 +598,7 @@ int copy_grid(long long n) { return int(std::min<long long>((n + 255) / 256, 409
 
 struct spn_xyz {
     int device = 0, n = 0, nl = 0, n_range = 0, n_corr = 0, n_overlap = 0, max_nodes = 0, sms = 0, grid = 0;
+    int spt = 4;  // sites per lane of the vertex kernel
     long long fn = 0;
     float cutoff = 0.0f;
     cudaStream_t stream = nullptr;
@@ -713,6 +719,13 @@ void validate(const spn_xyz_desc *d) {
     in_range(d->corr_perm, d->n_corr, 6, "corr_perm");
 }
 
+// the vertex kernel for SPT sites per lane (1 for Nl <= 32, 2 for Nl <= 64, else 4)
+const void *vertex_kernel(int spt) {
+    if (spt == 1) return reinterpret_cast<const void *>(&xyz_vertex_kernel<1>);
+    if (spt == 2) return reinterpret_cast<const void *>(&xyz_vertex_kernel<2>);
+    return reinterpret_cast<const void *>(&xyz_vertex_kernel<4>);
+}
+
 size_t vertex_smem(int nl) { return size_t(kWarps) * (kXBatch * sizeof(XDesc) + 12 * size_t(nl) * sizeof(float4)); }
 
 void launch_correlation(spn_xyz *h) {
@@ -794,11 +807,11 @@ extern "C" int spn_xyz_create(const spn_xyz_desc *d, spn_xyz **out) {
             check_cuda(cudaMemsetAsync(h->status, 0, sizeof(unsigned), h->stream), "memset");
             check_cuda(cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device), "device attribute");
             int per_sm = 0;
-            check_cuda(cudaFuncSetAttribute(xyz_vertex_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            int(vertex_smem(h->nl))),
+            h->spt = h->nl <= 32 ? 1 : (h->nl <= 64 ? 2 : 4);
+            const void *fn = vertex_kernel(h->spt);
+            check_cuda(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(vertex_smem(h->nl))),
                        "shared memory limit");
-            check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, xyz_vertex_kernel, kThreads, vertex_smem(h->nl)),
-                       "occupancy");
+            check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, vertex_smem(h->nl)), "occupancy");
             if (per_sm < 1) throw Error(ErrorType::Unsupported, "XYZ vertex-flow kernel does not fit on this device");
             h->grid = h->sms * per_sm;
             check_cuda(cudaStreamSynchronize(h->stream), "create sync");
@@ -890,9 +903,12 @@ extern "C" int spn_xyz_compute_step(spn_xyz *h) {
         check_cuda(cudaGetLastError(), "self-energy launch");
         xyz_node_table_kernel<<<(h->n + 63) / 64, 64, 0, h->stream>>>(h->node_args());
         check_cuda(cudaGetLastError(), "node table launch");
-        check_cuda(cudaFuncSetAttribute(xyz_vertex_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(vertex_smem(h->nl))),
+        check_cuda(cudaFuncSetAttribute(vertex_kernel(h->spt), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        int(vertex_smem(h->nl))),
                    "shared memory limit");
-        xyz_vertex_kernel<<<h->grid, kThreads, vertex_smem(h->nl), h->stream>>>(a);
+        if (h->spt == 1) xyz_vertex_kernel<1><<<h->grid, kThreads, vertex_smem(h->nl), h->stream>>>(a);
+        else if (h->spt == 2) xyz_vertex_kernel<2><<<h->grid, kThreads, vertex_smem(h->nl), h->stream>>>(a);
+        else xyz_vertex_kernel<4><<<h->grid, kThreads, vertex_smem(h->nl), h->stream>>>(a);
         check_cuda(cudaGetLastError(), "vertex flow launch");
     });
 }

@@ -46,7 +46,7 @@ def test_initial_state_matches_oracle():
     np.testing.assert_array_equal(v4, o4)
 
 
-@pytest.mark.parametrize("case", ["kitaev-gamma-r3", "kitaev-gamma-r11", "square-r11"])
+@pytest.mark.parametrize("case", ["kitaev-gamma-r3", "kitaev-gamma-r11", "square-r11", "square-r15"])
 def test_tri_rhs_matches_oracle(case):
     if case == "kitaev-gamma-r3":
         z, lat = kitaev_gamma()
@@ -57,6 +57,11 @@ def test_tri_rhs_matches_oracle(case):
         _, lat = kitaev_gamma(11)
         freq = spn.frequency_exponential(0.02, 20.0, 6)
         cut = spn.cutoff_exponential(20.0, 0.1, 0.85)
+        steps = 2
+    elif case == "square-r15":  # 72 sites: three site blocks per warp
+        lat = spn.Lattice("square", 15, "square-heisenberg", {"j": "1.0"})
+        freq = spn.frequency_exponential(0.01, 30.0, 4)
+        cut = spn.cutoff_exponential(30.0, 0.05, 0.9)
         steps = 2
     else:  # 42 sites of an SU(2)-symmetric model
         lat = spn.Lattice("square", 11, "square-heisenberg", {"j": "1.0"})

@@ -49,13 +49,18 @@ def test_initial_state_matches_oracle():
     np.testing.assert_array_equal(v4, o4)
 
 
-@pytest.mark.parametrize("case", ["kitaev", "square-r11"])
+@pytest.mark.parametrize("case", ["kitaev", "square-r11", "square-r15"])
 def test_xyz_rhs_matches_oracle(case):
     if case == "kitaev":
         z, lat = kitaev()
         freq = np.sort(z["frequencies"])
         cut = z["cutoffs"]
         steps = 5
+    elif case == "square-r15":  # 72 sites: four sites per lane
+        lat = spn.Lattice("square", 15, "square-heisenberg", {"j": "1.0"})
+        freq = spn.frequency_exponential(0.01, 30.0, 4)
+        cut = spn.cutoff_exponential(30.0, 0.05, 0.9)
+        steps = 2
     else:  # 42 sites: two sites per lane
         lat = spn.Lattice("square", 11, "square-heisenberg", {"j": "1.0"})
         freq = spn.frequency_exponential(0.01, 30.0, 6)
