@@ -296,3 +296,27 @@ def test_tri_checkpoint_resume_equals_uninterrupted_run(tmp_path):
         ca, da = h5lite.read_correlations(a, group)
         cb, db = h5lite.read_correlations(b, group)
         assert np.array_equal(ca, cb) and np.array_equal(da, db)
+
+
+def test_tri_deferred_measurements_equal_direct_ones(tmp_path):
+    """test_defer.sh with the TRI core: the archived 16-component vertex (.data, dataset v4)
+    evaluated in the post-processing run gives the direct run's ten groups."""
+    direct, _ = reference3_task(tmp_path, "nd.xml", cutoff=exponential_cutoffs("10", "1", "0.8"))
+    meas = '<measurements><measurement name="correlation" method="defer" /></measurements>'
+    g = np.load(os.path.join(GOLDEN, "reference3_tri.npz"))
+    params = f"<j>{float(g['j']):g}</j><k>{float(g['k']):g}</k><g>{float(g['g']):g}</g>"
+    deferred = write(tmp_path, "d.xml", lattice="honeycomb", rng=3, model="honeycomb-kitaev-gamma", symmetry="TRI",
+                     params=params, freq=manual_frequencies(), cutoff=exponential_cutoffs("10", "1", "0.8"),
+                     measurements=meas)
+    task.run_task(direct, resource_path=REF3_RES, force_restart=True, verbose=-1)
+    s1 = task.run_task(deferred, resource_path=REF3_RES, force_restart=True, verbose=-1)
+    assert s1.status == "postprocessing" and s1.measurements == 0
+    archive = h5lite.open_file(str(tmp_path / "d.data"))
+    assert len(archive.keys()) == s1.steps + 1
+    assert archive[archive.keys()[0]].keys() == ["cutoff", "v2", "v4"]
+    s2 = task.run_task(deferred, resource_path=REF3_RES, verbose=-1)
+    assert s2.status == "finished" and s2.measurements == s1.steps + 1
+    for group in TRI_GROUPS:
+        ca, da = h5lite.read_correlations(str(tmp_path / "nd.obs"), group)
+        cb, db = h5lite.read_correlations(str(tmp_path / "d.obs"), group)
+        assert np.array_equal(ca, cb) and np.array_equal(da, db), group
