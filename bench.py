@@ -118,6 +118,17 @@ def flops_nominal(tab, n):
     return float(fn) * (2 * n + 8) * (3 * 100 * tab.n_sites + 4 * tab.n_overlap)
 
 
+def gathers_evaluated(n, counts):
+    """Slab-segment gathers of the vertex flow for the node counts of a step: four access
+    buffers of four interpolation supports per node, each support one segment of Nl pairs."""
+    c = np.asarray(counts, np.float64)
+    tot = 0.0
+    for s in range(n):
+        for u in range(s + 1):
+            tot += n * (c[s] + c[u]) + float(np.sum(c))
+    return 16.0 * tot
+
+
 def flops_evaluated(tab, n, counts):
     """Same per-node costs, with the node counts the step actually used."""
     c = np.asarray(counts, np.float64)
@@ -614,6 +625,7 @@ def main():
     sampler.start()
     wall0 = time.perf_counter()
     flops_eval = 0.0
+    gathers_eval = 0.0
     for i, k in enumerate(schedule):
         flow.set_cutoff(float(cut[k]))
         with torch.cuda.stream(stream):
@@ -635,6 +647,7 @@ def main():
         flow.set_cutoff(float(cut[k]))
         flow.compute_step()
         flops_eval += flops_evaluated(tab, n, flow.node_counts())
+        gathers_eval += gathers_evaluated(n, flow.node_counts())
     # replicas: every rank ran its own flow; units summed, slowest rank's time
     from spinparser_gb300 import replicas
 
@@ -677,6 +690,18 @@ def main():
                 "diverged": flow.is_diverged()}
 
     fp32_peak, clk = spn.measure_fp32_peak(local)
+    gather = None
+    if tab.n_sites <= 32:
+        # the slab gathers against a pure gather kernel: state-sized (L2-resident) and
+        # L1-resident working sets; the larger rate is the denominator
+        g_l2 = spn.measure_gather_peak(tab.n_sites, flow.fn, local)
+        g_l1 = spn.measure_gather_peak(tab.n_sites, 512, local)
+        g_ach = gathers_eval / (prof["vertex_ms"] * 1e-3)
+        gather = {"kernel": "su2_vertex_flow_kernel", "achieved": g_ach / 1e9, "peak": max(g_l1, g_l2) / 1e9,
+                  "unit": "G segments/s", "frac": g_ach / max(g_l1, g_l2), "peak_l2_resident": g_l2 / 1e9,
+                  "peak_l1_resident": g_l1 / 1e9,
+                  "segment": f"{tab.n_sites} float2 pairs (one interpolation support of one access buffer)",
+                  "peak_source": "measured in-run: pure gather kernel on this GPU (spn_measure_gather_peak)"}
     avg_vertex_ms = prof["vertex_ms"] / max(1, prof["vertex_launches"])
     nominal = flops_nominal(tab, n)
     achieved = nominal / (avg_vertex_ms * 1e-3) / 1e12
@@ -709,7 +734,8 @@ def main():
                      "algorithmic_flops_per_launch": nominal, "avg_launch_ms": avg_vertex_ms,
                      "achieved_evaluated": achieved_eval, "frac_evaluated": achieved_eval / fp32_peak,
                      "peak_source": "measured in-run: pure-FFMA kernel on this GPU (MEASURED_PEAKS.json has no "
-                                    "FP32 CUDA-core figure)", "fp32_clock_ghz_implied": clk},
+                                    "FP32 CUDA-core figure)", "fp32_clock_ghz_implied": clk,
+                     "gather": gather},
         "vertex_variant": variant,
         "gpu_launches": KERNELS_PER_STEP * len(schedule),
         "clocks": clocks,

@@ -48,6 +48,13 @@ int spn_device_memory(int device, long long *free_bytes, long long *total_bytes)
  * this is its roofline denominator.  No reference counterpart (benchmark support). */
 int spn_measure_fp32_peak(int device, double *tflops, double *sm_clock_ghz_est);
 
+/* Measured slab-gather rate of a device: segments of n_sites (<= 32) float2 pairs per second
+ * that a pure gather kernel reads, one warp request per segment, at random starts among n_slabs
+ * slabs (best of several runs; n_slabs sets the working set: F_N for a flow's vertex, a few
+ * hundred for an L1-resident one).  The vertex flow's interpolation supports are such
+ * segments; this is the denominator of its gather roofline.  No reference counterpart. */
+int spn_measure_gather_peak(int device, int n_sites, int n_slabs, double *segments_per_s);
+
 /* ------------------------------------------------------------------------------------
  * Host side: lattice / spin model (LatticeModelFactory::newLatticeModel,
  * src/LatticeModelFactory.cpp:733-1047) and discretisations (src/TaskFileParser.cpp:107-198).

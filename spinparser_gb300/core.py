@@ -202,6 +202,14 @@ def measure_fp32_peak(device: int = 0):
     return t.value, g.value
 
 
+def measure_gather_peak(n_sites: int, n_slabs: int, device: int = 0) -> float:
+    """Segments of n_sites float2 pairs per second that a pure gather kernel reads at random
+    starts among n_slabs slabs (spn_measure_gather_peak)."""
+    r = C.c_double()
+    check(load_library().spn_measure_gather_peak(device, n_sites, n_slabs, C.byref(r)))
+    return r.value
+
+
 def make_desc(tables: LatticeTables, freq: np.ndarray, spin_length: float = 0.5, device: int = 0, flags: int = 0):
     """The spn_su2_desc of a flow, and the arrays it points into (keep them alive while the
     descriptor is used)."""

@@ -142,6 +142,28 @@ __global__ void __launch_bounds__(256) fp32_peak_kernel(float *out, float seed) 
     if (s == 12345.678f) out[0] = s;  // keeps the chains live
 }
 
+// Gather probe: each warp sums, for kGatherK slabs read from a table, the segment of n_sites
+// float2 pairs starting at slab * n_sites -- the slab gather of the vertex flow without its
+// arithmetic.  Slab indices are < n_slabs and lane < n_sites, so every load is in bounds.
+constexpr int kGatherK = 256;
+
+__global__ void __launch_bounds__(128) gather_peak_kernel(const float2 *__restrict__ st, const int *__restrict__ slabs,
+                                                          int n_sites, float *__restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int *sl = slabs + warp * kGatherK;
+    float ax = 0.0f, ay = 0.0f;
+    for (int k = 0; k < kGatherK; ++k) {
+        const int s = __ldg(sl + k);
+        if (lane < n_sites) {
+            const float2 v = __ldg(st + (long long)s * n_sites + lane);
+            ax += v.x;
+            ay += v.y;
+        }
+    }
+    if (ax + ay == 12345.678f) out[0] = ax;  // keeps the loads live
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------------------------
@@ -338,6 +360,51 @@ extern "C" int spn_measure_fp32_peak(int device, double *tflops, double *sm_cloc
         *tflops = best;
         // 128 FP32 lanes x 2 flops per SM per clock
         if (sm_clock_ghz_est) *sm_clock_ghz_est = best * 1e12 / (double(sms) * 256.0) / 1e9;
+    });
+}
+
+extern "C" int spn_measure_gather_peak(int device, int n_sites, int n_slabs, double *segments_per_s) {
+    return guarded([&] {
+        if (!segments_per_s || n_sites < 1 || n_sites > 32 || n_slabs < 1)
+            throw Error(ErrorType::Argument, "spn_measure_gather_peak: need 1 <= n_sites <= 32 and n_slabs >= 1");
+        cuda_check(cudaSetDevice(device), "cudaSetDevice");
+        int sms = 0;
+        cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "device attribute");
+        const int threads = 128, blocks = sms * 16;
+        const long long warps = (long long)blocks * threads / 32;
+        std::vector<int> table(size_t(warps) * kGatherK);
+        unsigned x = 12345u;
+        for (auto &t : table) {
+            x = x * 1664525u + 1013904223u;
+            t = int((x >> 8) % unsigned(n_slabs));
+        }
+        float2 *st = nullptr;
+        int *sl = nullptr;
+        float *out = nullptr;
+        cuda_check(cudaMalloc(&st, size_t(n_slabs) * n_sites * sizeof(float2)), "alloc");
+        cuda_check(cudaMalloc(&sl, table.size() * sizeof(int)), "alloc");
+        cuda_check(cudaMalloc(&out, sizeof(float)), "alloc");
+        cuda_check(cudaMemset(st, 0, size_t(n_slabs) * n_sites * sizeof(float2)), "memset");
+        cuda_check(cudaMemcpy(sl, table.data(), table.size() * sizeof(int), cudaMemcpyHostToDevice), "H2D");
+        cudaEvent_t e0, e1;
+        cuda_check(cudaEventCreate(&e0), "event");
+        cuda_check(cudaEventCreate(&e1), "event");
+        double best = 0.0;
+        for (int rep = 0; rep < 6; ++rep) {
+            cuda_check(cudaEventRecord(e0), "record");
+            gather_peak_kernel<<<blocks, threads>>>(st, sl, n_sites, out);
+            cuda_check(cudaEventRecord(e1), "record");
+            cuda_check(cudaEventSynchronize(e1), "sync");
+            float ms = 0.0f;
+            cuda_check(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+            if (rep > 0) best = std::max(best, double(warps) * kGatherK / (ms * 1e-3));
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFree(st);
+        cudaFree(sl);
+        cudaFree(out);
+        *segments_per_s = best;
     });
 }
 
