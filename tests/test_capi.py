@@ -55,3 +55,11 @@ def test_descriptor_validation_happens_before_device_use():
 
 def test_device_count_without_gpu_is_not_an_error():
     assert spn.device_count() >= 0
+
+
+def test_probe_arguments_are_checked_before_device_use():
+    """spn_measure_gather_peak validates its shape on the host (one warp request per segment)."""
+    for n_sites, n_slabs in ((0, 10), (33, 10), (8, 0)):
+        with pytest.raises(spn.SpnError) as e:
+            spn.measure_gather_peak(n_sites, n_slabs)
+        assert e.value.code == -2
