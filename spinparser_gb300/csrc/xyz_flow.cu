@@ -726,6 +726,74 @@ const void *vertex_kernel(int spt) {
     return reinterpret_cast<const void *>(&xyz_vertex_kernel<4>);
 }
 
+// The RPA pairs of each site, packed (rid1 | rid2 << 7 | perm1 << 14 | perm2 << 17) and put in
+// an order that keeps a warp's shared-memory reads apart.  Lane j walks the pairs of site j
+// (32 sites per warp step) and reads A6[perm1 nl + rid1] and B6[perm2 nl + rid2], one float4
+// each.  A 16-byte read is served per eight-lane phase, and two lanes of a phase whose
+// different float4 fall into one group of four banks serialise.  Any order of a site's pairs
+// gives the same sum up to rounding; the pairs are chosen greedily, step by step and site by
+// site, with the fewest new collisions.
+std::vector<int> order_rpa_pairs(const spn_xyz_desc *d) {
+    const int nl = d->n_sites;
+    const int *ptr = d->overlap_ptr;
+    std::vector<int> out(static_cast<size_t>(ptr[nl]), 0);
+    const int b_base = 6 * nl;  // B6 follows A6 in the warp's area
+    for (int g0 = 0; g0 < nl; g0 += 32) {
+        const int g1 = std::min(nl, g0 + 32);
+        std::vector<std::vector<int>> rem(g1 - g0);
+        for (int j = g0; j < g1; ++j)
+            for (int i = ptr[j]; i < ptr[j + 1]; ++i) rem[j - g0].push_back(i);
+        std::vector<int> fill(g1 - g0, 0);
+        for (;;) {
+            bool any = false;
+            // float4 words read in this step per (phase, bank group), up to 8 kept
+            std::vector<int> occ(4 * 8 * 8, -1);
+            auto collides = [&](int phase, int word) {
+                const int *o = &occ[(phase * 8 + word % 8) * 8];
+                bool same = false, other = false;
+                for (int k = 0; k < 8 && o[k] >= 0; ++k) (o[k] == word ? same : other) = true;
+                return (other && !same) ? 1 : 0;
+            };
+            auto take = [&](int phase, int word) {
+                int *o = &occ[(phase * 8 + word % 8) * 8];
+                for (int k = 0; k < 8; ++k) {
+                    if (o[k] == word) return;
+                    if (o[k] < 0) {
+                        o[k] = word;
+                        return;
+                    }
+                }
+            };
+            for (int j = g0; j < g1; ++j) {
+                std::vector<int> &cand = rem[j - g0];
+                if (cand.empty()) continue;
+                any = true;
+                const int phase = (j - g0) / 8;
+                size_t best = 0;
+                int best_cost = 1 << 30;
+                for (size_t q = 0; q < cand.size() && best_cost > 0; ++q) {
+                    const int i = cand[q];
+                    const int wa = d->overlap_perm1[i] * nl + d->overlap_rid1[i];
+                    const int wb = b_base + d->overlap_perm2[i] * nl + d->overlap_rid2[i];
+                    const int cost = collides(phase, wa) + collides(phase, wb);
+                    if (cost < best_cost) {
+                        best_cost = cost;
+                        best = q;
+                    }
+                }
+                const int i = cand[best];
+                cand.erase(cand.begin() + long(best));
+                take(phase, d->overlap_perm1[i] * nl + d->overlap_rid1[i]);
+                take(phase, b_base + d->overlap_perm2[i] * nl + d->overlap_rid2[i]);
+                out[size_t(ptr[j] + fill[j - g0]++)] =
+                    d->overlap_rid1[i] | d->overlap_rid2[i] << 7 | d->overlap_perm1[i] << 14 | d->overlap_perm2[i] << 17;
+            }
+            if (!any) break;
+        }
+    }
+    return out;
+}
+
 size_t vertex_smem(int nl) { return size_t(kWarps) * (kXBatch * sizeof(XDesc) + 12 * size_t(nl) * sizeof(float4)); }
 
 void launch_correlation(spn_xyz *h) {
@@ -783,9 +851,7 @@ extern "C" int spn_xyz_create(const spn_xyz_desc *d, spn_xyz **out) {
             put(d->overlap_rid2, nov);
             put(d->overlap_perm1, nov);
             put(d->overlap_perm2, nov);
-            std::vector<int> packed(nov);
-            for (int i = 0; i < nov; ++i)
-                packed[i] = d->overlap_rid1[i] | d->overlap_rid2[i] << 7 | d->overlap_perm1[i] << 14 | d->overlap_perm2[i] << 17;
+            const std::vector<int> packed = order_rpa_pairs(d);
             put(packed.data(), nov);
             put(d->range_rid, nr);
             put(d->range_inv_rid, nr);
