@@ -13,7 +13,7 @@
 // A step: the self-energy flow (one CTA per frequency), the loop-frequency node tables (the
 // SU(2) core's, shared), the vertex flow and the Euler update.  The vertex-flow kernel runs a
 // persistent grid whose warps take one (s,t,u) triple at a time from a device counter.  Per
-// channel, nodes go in batches of 32: first each lane builds one node's access buffers (and
+// channel, nodes go in batches of 16: first a lane builds one node's access buffers (and
 // the t channel's site-local values) into a shared-memory descriptor, then the lanes hold
 // the sites (up to four each) and walk the batch's nodes in order.  The t channel's RPA sum
 // exchanges the first two slabs of a node through shared memory in all six spin
@@ -257,7 +257,7 @@ __device__ __forceinline__ void gather_desc(const XyzArgs &a, const XDesc &d, in
     gather4(a, ab, ln, out);
 }
 
-constexpr int kXBatch = 32;  // nodes whose descriptors a warp builds at once
+constexpr int kXBatch = 16;  // nodes whose descriptors a warp builds at once
 
 template <int SPT>
 __global__ void __launch_bounds__(kThreads) xyz_vertex_kernel(XyzArgs a) {
