@@ -257,7 +257,7 @@ __device__ __forceinline__ void gather_desc(const XyzArgs &a, const XDesc &d, in
     gather4(a, ab, ln, out);
 }
 
-constexpr int kXBatch = 8;  // nodes whose descriptors a warp builds at once
+constexpr int kXBatch = 4;  // nodes whose descriptors a warp builds at once
 
 template <int SPT>
 __global__ void __launch_bounds__(kThreads) xyz_vertex_kernel(XyzArgs a) {
