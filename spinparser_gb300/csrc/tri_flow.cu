@@ -39,7 +39,7 @@ namespace {
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxSites = 128;
-constexpr int kTBatch = 16;  // nodes whose descriptors a warp builds at once
+constexpr int kTBatch = 4;  // nodes whose descriptors a warp builds at once
 constexpr int kCorrOut = 10;  // XX XY XZ YX YY YZ ZX ZY ZZ DD
 
 // The six spin permutations (X,Y,Z) (X,Z,Y) (Y,X,Z) (Y,Z,X) (Z,X,Y) (Z,Y,X): 2 bits per image
