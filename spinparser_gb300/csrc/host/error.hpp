@@ -14,7 +14,7 @@ enum class ErrorType : int {
     Cuda = -5,            // CUDA runtime failure (allocation, launch, copy)
     Device = -6,          // device-side status word reported a problem
     Internal = -7,        // consistency check failed
-    Unsupported = -8,     // size or feature beyond what this build supports
+    Unsupported = -8,     // size or feature beyond what the library supports
 };
 
 class Error : public std::runtime_error {

@@ -5,7 +5,7 @@
 // version-1 object headers, groups as symbol tables (v1 B-tree + local heap + symbol-table
 // nodes), contiguous float32 datasets, float32[3] array datasets and float32 attributes
 // (src/SU2/SU2MeasurementCorrelation.cpp:179-355, src/SU2/SU2EffectiveAction.hpp:79-205).
-// libhdf5 is not available to this build, so this module writes and reads exactly that
+// The library does not link libhdf5, so this module writes and reads exactly that
 // subset with the node sizes libhdf5 uses (group leaf K = 4, internal K = 16), so that any
 // HDF5 reader (h5py, the reference's obs.py) opens the files.
 //
