@@ -452,30 +452,36 @@ __device__ __forceinline__ void t_terms(const TriArgs &a, const float *S, const 
     }
 #pragma unroll
     for (int c = 0; c < 16; ++c) v[c] *= 2.0f;
-    {  // chalice: slabs 0 and 2 with the local values of ab4, ab5
+    {  // chalice: slabs 0 and 2 with the local values of ab4, ab5.  For an inner pair (kappa,
+       // lambda) the outputs (c1, c2) read the row L(lambda, .) at rho = c2 ^ kappa ^ lambda, so
+       // the row is loaded once; every output still adds its terms in (kappa, lambda) order.
         float X0[16], X2[16];
 #pragma unroll
         for (int c = 0; c < 16; ++c) {
             X0[c] = S0[c * nl + j];
             X2[c] = S2[c * nl + j];
         }
+        const float4 *L4 = reinterpret_cast<const float4 *>(L), *L5 = reinterpret_cast<const float4 *>(L + 16);
 #pragma unroll
-        for (int c = 0; c < 16; ++c) {
+        for (int n = 0; n < 16; ++n) {
+            const int kap = tri::inner(n >> 2), lam = tri::inner(n & 3);
+            const float4 q4 = L4[lam], q5 = L5[lam];
+            const float r4[4] = {q4.x, q4.y, q4.z, q4.w}, r5[4] = {q5.x, q5.y, q5.z, q5.w};
 #pragma unroll
-            for (int n = 0; n < 16; ++n) {
-                const int kap = tri::inner(n >> 2), lam = tri::inner(n & 3);
-                const int ai = 4 * (c >> 2) + kap, li = 4 * lam + ((c & 3) ^ kap ^ lam);
+            for (int c = 0; c < 16; ++c) {
+                const int ai = 4 * (c >> 2) + kap, rho = (c & 3) ^ kap ^ lam;
                 if (tri::chal_sign(c, kap, lam) > 0) {
-                    v[c] += X0[ai] * L[li];
-                    v[c] += X2[ai] * L[16 + li];
+                    v[c] += X0[ai] * r4[rho];
+                    v[c] += X2[ai] * r5[rho];
                 } else {
-                    v[c] -= X0[ai] * L[li];
-                    v[c] -= X2[ai] * L[16 + li];
+                    v[c] -= X0[ai] * r4[rho];
+                    v[c] -= X2[ai] * r5[rho];
                 }
             }
         }
     }
-    {  // inverse chalice: the local values of ab6, ab7 with slabs 1 and 3
+    {  // inverse chalice: the local values of ab6, ab7 with slabs 1 and 3, each value loaded
+       // once; every output adds its terms in the order l = 15 .. 0
         float X1[16], X3[16];
 #pragma unroll
         for (int c = 0; c < 16; ++c) {
@@ -483,17 +489,18 @@ __device__ __forceinline__ void t_terms(const TriArgs &a, const float *S, const 
             X3[c] = S3[c * nl + j];
         }
 #pragma unroll
-        for (int c = 0; c < 16; ++c) {
+        for (int n = 0; n < 16; ++n) {
+            const int l = 15 - n;
+            const float l6 = L[32 + l], l7 = L[48 + l];
 #pragma unroll
-            for (int n = 0; n < 16; ++n) {
-                const int l = 15 - n;
+            for (int c = 0; c < 16; ++c) {
                 const int bi = 4 * ((c >> 2) ^ (l >> 2) ^ (l & 3)) + (c & 3);
                 if (tri::ichal_sign(c, l) > 0) {
-                    v[c] += L[32 + l] * X1[bi];
-                    v[c] += L[48 + l] * X3[bi];
+                    v[c] += l6 * X1[bi];
+                    v[c] += l7 * X3[bi];
                 } else {
-                    v[c] -= L[32 + l] * X1[bi];
-                    v[c] -= L[48 + l] * X3[bi];
+                    v[c] -= l6 * X1[bi];
+                    v[c] -= l7 * X3[bi];
                 }
             }
         }
