@@ -127,6 +127,14 @@ int spn_lattice_get_interactions(const spn_lattice *lat, int *rid, float *coupli
 int spn_rpa_schedule(int n_sites, const int *overlap_ptr, const int *overlap_rid1, const int *overlap_rid2, int lanes,
                      int *info, int *sched, int *count, int *slot_base, int *seg_ptr);
 
+/* The order in which the XYZ (layout 0) or TRI (layout 1) vertex kernel walks each site's RPA
+ * pairs (diagnostics; host only): order[overlap_ptr[j] .. overlap_ptr[j+1]) is a permutation of
+ * site j's pair indices, chosen against shared-memory bank collisions of the kernel's reads.
+ * collisions[0] / [1]: collisions of the given order and of the chosen one (may be NULL). */
+int spn_rpa_pair_order(int layout, int n_sites, const int *overlap_ptr, const int *overlap_rid1,
+                       const int *overlap_rid2, const int *overlap_perm1, const int *overlap_perm2, int *order,
+                       long long *collisions);
+
 /* Writes the lattice debug file (.ldf) as `--debugLattice`-free SpinParser always does. */
 int spn_lattice_write_ldf(const spn_lattice *lat, const char *path);
 

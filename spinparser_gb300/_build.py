@@ -18,7 +18,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 
-HOST_SOURCES = ["host/xml.cpp", "host/lattice.cpp", "host/capi_host.cpp", "host/h5.cpp", "host/task.cpp",
+HOST_SOURCES = ["host/xml.cpp", "host/lattice.cpp", "host/capi_host.cpp", "host/pair_order.cpp", "host/h5.cpp", "host/task.cpp",
                 "host/su2_files.cpp", "host/run.cpp", "host/rpa_schedule.cpp"]
 CUDA_SOURCES = ["su2_flow.cu", "su2_vertex.cu", "su2_vertex64.cu", "su2_batch.cu", "xyz_flow.cu", "tri_flow.cu"]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -143,6 +143,8 @@ SIGNATURES = {
     "spn_tri_measure_correlation": (C.c_int, [C.c_void_p, c_float_p, c_float_p]),
     "spn_tri_is_diverged": (C.c_int, [C.c_void_p, c_int_p]),
     "spn_tri_tables": (C.c_int, [c_int_p]),
+    "spn_rpa_pair_order": (C.c_int, [C.c_int, C.c_int, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p,
+                                     C.POINTER(C.c_longlong)]),
     "spn_su2_set_state_f64": (C.c_int, [C.c_void_p, C.c_float, c_double_p, c_double_p, c_double_p]),
     "spn_su2_get_state_f64": (C.c_int, [C.c_void_p, c_float_p, c_double_p, c_double_p, c_double_p]),
     "spn_su2_get_flow_f64": (C.c_int, [C.c_void_p, c_double_p, c_double_p, c_double_p]),

@@ -5,6 +5,7 @@
 #include "log.hpp"
 #include "rpa_schedule.hpp"
 #include "../tri_algebra.hpp"
+#include "pair_order.hpp"
 #include "../../../include/spn_su2.h"
 #include <atomic>
 #include <cmath>
@@ -282,6 +283,34 @@ extern "C" int spn_tri_initial_state(const spn_lattice *lat, int n_freq, float n
                 for (int b = 0; b < 3; ++b)
                     for (const auto &ia : L.interactions)
                         v4[(it * 16 + 4 * a + b) * nl + ia.rid] += 0.25f * ia.J[a][b] / normalization;
+    });
+}
+
+extern "C" int spn_rpa_pair_order(int layout, int n_sites, const int *overlap_ptr, const int *overlap_rid1,
+                                  const int *overlap_rid2, const int *overlap_perm1, const int *overlap_perm2, int *order,
+                                  long long *collisions) {
+    return spn::guarded([&] {
+        if ((layout != 0 && layout != 1) || n_sites < 1 || n_sites > 128 || !overlap_ptr || !order)
+            throw spn::Error(spn::ErrorType::Argument, "spn_rpa_pair_order: bad argument");
+        const int nov = overlap_ptr[n_sites];
+        if (nov > 0 && (!overlap_rid1 || !overlap_rid2 || !overlap_perm1 || !overlap_perm2))
+            throw spn::Error(spn::ErrorType::Argument, "spn_rpa_pair_order: null pair table");
+        for (int i = 0; i < nov; ++i)
+            if (overlap_rid1[i] < 0 || overlap_rid1[i] >= n_sites || overlap_rid2[i] < 0 || overlap_rid2[i] >= n_sites ||
+                overlap_perm1[i] < 0 || overlap_perm1[i] >= 6 || overlap_perm2[i] < 0 || overlap_perm2[i] >= 6)
+                throw spn::Error(spn::ErrorType::Argument, "spn_rpa_pair_order: pair entry out of range");
+        const spn::PairBankModel m = layout == 0 ? spn::xyz_rpa_model() : spn::tri_rpa_model();
+        const auto words = layout == 0
+                               ? spn::xyz_rpa_words(n_sites, overlap_rid1, overlap_rid2, overlap_perm1, overlap_perm2)
+                               : spn::tri_rpa_words(n_sites, overlap_rid1, overlap_rid2, overlap_perm1, overlap_perm2);
+        const std::vector<int> o = spn::order_pairs_by_banks(n_sites, overlap_ptr, m, words);
+        std::memcpy(order, o.data(), o.size() * sizeof(int));
+        if (collisions) {
+            std::vector<int> natural(static_cast<size_t>(nov));
+            for (int i = 0; i < nov; ++i) natural[size_t(i)] = i;
+            collisions[0] = spn::pair_bank_collisions(n_sites, overlap_ptr, natural.data(), m, words);
+            collisions[1] = spn::pair_bank_collisions(n_sites, overlap_ptr, o.data(), m, words);
+        }
     });
 }
 

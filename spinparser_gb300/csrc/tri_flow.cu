@@ -29,6 +29,7 @@
 #include "su2_kernels.cuh"
 #include "tri_algebra.hpp"
 #include "host/capi_common.hpp"
+#include "host/pair_order.hpp"
 #include "../../include/spn_su2.h"
 
 using namespace spn;
@@ -854,80 +855,20 @@ void validate(const spn_tri_desc *d) {
     in_range(d->corr_perm, d->n_corr, 6, "corr_perm");
 }
 
-// The RPA pairs of each site, packed (see TriArgs::ov_pk) and put in
-// an order that keeps the shared-memory reads of a warp apart.  Lane j of a warp walks the
-// pairs of site j, and at step k the 32 lanes read, for every component c, the slab words
-// pn[perm][c] + rid of their k-th pair.  Two lanes whose different words fall into one bank
-// serialise.  Any order of a site's pairs gives the same sum up to rounding, so the pairs are
-// chosen greedily, step by step and site by site, with the fewest new bank collisions.
+// The RPA pairs of each site in the order of host/pair_order (against bank collisions of the
+// kernel's shared-memory reads), packed as TriArgs::ov_pk.
 std::vector<int> order_rpa_pairs(const spn_tri_desc *d) {
     const int nl = d->n_sites;
-    const int *ptr = d->overlap_ptr;
-    std::vector<int> out(static_cast<size_t>(ptr[nl]), 0);
-    int pn[6][16];
-    for (int p = 0; p < 6; ++p)
-        for (int c = 0; c < 16; ++c) pn[p][c] = (4 * permc(p, c >> 2) + permc(p, c & 3)) * nl;
-    for (int g0 = 0; g0 < nl; g0 += 32) {
-        const int g1 = std::min(nl, g0 + 32);
-        std::vector<std::vector<int>> rem(g1 - g0);
-        for (int j = g0; j < g1; ++j)
-            for (int i = ptr[j]; i < ptr[j + 1]; ++i) rem[j - g0].push_back(i);
-        std::vector<int> fill(g1 - g0, 0);
-        for (;;) {
-            bool any = false;
-            // words already read in this step: per component and side, per bank
-            std::vector<int> occ(2 * 16 * 32 * 4, -1);  // up to 4 distinct words kept per bank
-            auto conflicts = [&](int side, int c, int word) {
-                const int *o = &occ[((side * 16 + c) * 32 + word % 32) * 4];
-                bool same = false, other = false;
-                for (int k = 0; k < 4; ++k) {
-                    if (o[k] < 0) break;
-                    if (o[k] == word) same = true;
-                    else other = true;
-                }
-                return (other && !same) ? 1 : 0;
-            };
-            auto take = [&](int side, int c, int word) {
-                int *o = &occ[((side * 16 + c) * 32 + word % 32) * 4];
-                for (int k = 0; k < 4; ++k) {
-                    if (o[k] == word) return;
-                    if (o[k] < 0) {
-                        o[k] = word;
-                        return;
-                    }
-                }
-            };
-            for (int j = g0; j < g1; ++j) {
-                std::vector<int> &cand = rem[j - g0];
-                if (cand.empty()) continue;
-                any = true;
-                size_t best = 0;
-                int best_cost = 1 << 30;
-                for (size_t q = 0; q < cand.size() && best_cost > 0; ++q) {
-                    const int i = cand[q];
-                    const int r1 = d->overlap_rid1[i], p1 = d->overlap_perm1[i];
-                    const int r2 = d->overlap_rid2[i], p2 = d->overlap_perm2[i];
-                    int cost = 0;
-                    for (int c = 0; c < 16; ++c) cost += conflicts(0, c, pn[p1][c] + r1) + conflicts(1, c, pn[p2][c] + r2);
-                    if (cost < best_cost) {
-                        best_cost = cost;
-                        best = q;
-                    }
-                }
-                const int i = cand[best];
-                cand.erase(cand.begin() + long(best));
-                const int r1 = d->overlap_rid1[i], p1 = d->overlap_perm1[i];
-                const int r2 = d->overlap_rid2[i], p2 = d->overlap_perm2[i];
-                for (int c = 0; c < 16; ++c) {
-                    take(0, c, pn[p1][c] + r1);
-                    take(1, c, pn[p2][c] + r2);
-                }
-                int word = r1 | r2 << 7;
-                for (int q = 0; q < 3; ++q) word |= permc(p1, q) << (14 + 2 * q) | permc(p2, q) << (20 + 2 * q);
-                out[size_t(ptr[j] + fill[j - g0]++)] = word;
-            }
-            if (!any) break;
-        }
+    const std::vector<int> order =
+        order_pairs_by_banks(nl, d->overlap_ptr, tri_rpa_model(),
+                             tri_rpa_words(nl, d->overlap_rid1, d->overlap_rid2, d->overlap_perm1, d->overlap_perm2));
+    std::vector<int> out(order.size());
+    for (size_t k = 0; k < order.size(); ++k) {
+        const int i = order[k];
+        int word = d->overlap_rid1[i] | d->overlap_rid2[i] << 7;
+        for (int q = 0; q < 3; ++q)
+            word |= permc(d->overlap_perm1[i], q) << (14 + 2 * q) | permc(d->overlap_perm2[i], q) << (20 + 2 * q);
+        out[k] = word;
     }
     return out;
 }

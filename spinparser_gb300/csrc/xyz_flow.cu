@@ -27,6 +27,7 @@
 #include "su2_device.cuh"
 #include "su2_kernels.cuh"
 #include "host/capi_common.hpp"
+#include "host/pair_order.hpp"
 #include "../../include/spn_su2.h"
 
 using namespace spn;
@@ -726,70 +727,17 @@ const void *vertex_kernel(int spt) {
     return reinterpret_cast<const void *>(&xyz_vertex_kernel<4>);
 }
 
-// The RPA pairs of each site, packed (rid1 | rid2 << 7 | perm1 << 14 | perm2 << 17) and put in
-// an order that keeps a warp's shared-memory reads apart.  Lane j walks the pairs of site j
-// (32 sites per warp step) and reads A6[perm1 nl + rid1] and B6[perm2 nl + rid2], one float4
-// each.  A 16-byte read is served per eight-lane phase, and two lanes of a phase whose
-// different float4 fall into one group of four banks serialise.  Any order of a site's pairs
-// gives the same sum up to rounding; the pairs are chosen greedily, step by step and site by
-// site, with the fewest new collisions.
+// The RPA pairs of each site in the order of host/pair_order (against bank collisions of the
+// kernel's 16-byte reads of A6 and B6), packed rid1 | rid2 << 7 | perm1 << 14 | perm2 << 17.
 std::vector<int> order_rpa_pairs(const spn_xyz_desc *d) {
     const int nl = d->n_sites;
-    const int *ptr = d->overlap_ptr;
-    std::vector<int> out(static_cast<size_t>(ptr[nl]), 0);
-    const int b_base = 6 * nl;  // B6 follows A6 in the warp's area
-    for (int g0 = 0; g0 < nl; g0 += 32) {
-        const int g1 = std::min(nl, g0 + 32);
-        std::vector<std::vector<int>> rem(g1 - g0);
-        for (int j = g0; j < g1; ++j)
-            for (int i = ptr[j]; i < ptr[j + 1]; ++i) rem[j - g0].push_back(i);
-        std::vector<int> fill(g1 - g0, 0);
-        for (;;) {
-            bool any = false;
-            // float4 words read in this step per (phase, bank group), up to 8 kept
-            std::vector<int> occ(4 * 8 * 8, -1);
-            auto collides = [&](int phase, int word) {
-                const int *o = &occ[(phase * 8 + word % 8) * 8];
-                bool same = false, other = false;
-                for (int k = 0; k < 8 && o[k] >= 0; ++k) (o[k] == word ? same : other) = true;
-                return (other && !same) ? 1 : 0;
-            };
-            auto take = [&](int phase, int word) {
-                int *o = &occ[(phase * 8 + word % 8) * 8];
-                for (int k = 0; k < 8; ++k) {
-                    if (o[k] == word) return;
-                    if (o[k] < 0) {
-                        o[k] = word;
-                        return;
-                    }
-                }
-            };
-            for (int j = g0; j < g1; ++j) {
-                std::vector<int> &cand = rem[j - g0];
-                if (cand.empty()) continue;
-                any = true;
-                const int phase = (j - g0) / 8;
-                size_t best = 0;
-                int best_cost = 1 << 30;
-                for (size_t q = 0; q < cand.size() && best_cost > 0; ++q) {
-                    const int i = cand[q];
-                    const int wa = d->overlap_perm1[i] * nl + d->overlap_rid1[i];
-                    const int wb = b_base + d->overlap_perm2[i] * nl + d->overlap_rid2[i];
-                    const int cost = collides(phase, wa) + collides(phase, wb);
-                    if (cost < best_cost) {
-                        best_cost = cost;
-                        best = q;
-                    }
-                }
-                const int i = cand[best];
-                cand.erase(cand.begin() + long(best));
-                take(phase, d->overlap_perm1[i] * nl + d->overlap_rid1[i]);
-                take(phase, b_base + d->overlap_perm2[i] * nl + d->overlap_rid2[i]);
-                out[size_t(ptr[j] + fill[j - g0]++)] =
-                    d->overlap_rid1[i] | d->overlap_rid2[i] << 7 | d->overlap_perm1[i] << 14 | d->overlap_perm2[i] << 17;
-            }
-            if (!any) break;
-        }
+    const std::vector<int> order =
+        order_pairs_by_banks(nl, d->overlap_ptr, xyz_rpa_model(),
+                             xyz_rpa_words(nl, d->overlap_rid1, d->overlap_rid2, d->overlap_perm1, d->overlap_perm2));
+    std::vector<int> out(order.size());
+    for (size_t k = 0; k < order.size(); ++k) {
+        const int i = order[k];
+        out[k] = d->overlap_rid1[i] | d->overlap_rid2[i] << 7 | d->overlap_perm1[i] << 14 | d->overlap_perm2[i] << 17;
     }
     return out;
 }
