@@ -63,3 +63,18 @@ def test_probe_arguments_are_checked_before_device_use():
         with pytest.raises(spn.SpnError) as e:
             spn.measure_gather_peak(n_sites, n_slabs)
         assert e.value.code == -2
+
+
+def test_header_is_plain_c(tmp_path):
+    """include/spn_su2.h is the FFI boundary: it must compile as ISO C99 (cgo, ctypes, JNI stubs)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "use.c"
+    src.write_text('#include "spn_su2.h"\nint main(void) { spn_tri_desc d; spn_su2_desc s; (void)d; (void)s; return 0; }\n')
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(root, "include"),
+                        "-c", str(src), "-o", str(tmp_path / "use.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
