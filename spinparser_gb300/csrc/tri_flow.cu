@@ -28,6 +28,7 @@
 #include "su2_device.cuh"
 #include "su2_kernels.cuh"
 #include "tri_algebra.hpp"
+#include "cuda_host.cuh"
 #include "host/capi_common.hpp"
 #include "host/pair_order.hpp"
 #include "../../include/spn_su2.h"
@@ -714,23 +715,10 @@ __global__ void tri_euler_kernel(float *__restrict__ x, const float *__restrict_
         x[i] = __fadd_rn(x[i], __fmul_rn(step, dx[i]));
 }
 
-void check_cuda(cudaError_t e, const char *what) {
-    if (e != cudaSuccess) throw Error(ErrorType::Cuda, std::string(what) + ": " + cudaGetErrorString(e));
-}
-
-template <class T>
-T *dalloc(size_t count, const char *what) {
-    void *p = nullptr;
-    check_cuda(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T) + 16), what);
-    return static_cast<T *>(p);
-}
-
-template <class T>
-void h2d(T *dst, const T *src, size_t count, cudaStream_t s) {
-    if (count) check_cuda(cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync H2D");
-}
-
-int copy_grid(long long n) { return int(std::min<long long>((n + 255) / 256, 4096)); }
+using cuh::check_cuda;
+using cuh::copy_grid;
+using cuh::dalloc;
+using cuh::h2d;
 
 size_t vertex_smem(int nl) { return (tri_cta_head_floats(nl) + size_t(kWarps) * tri_warp_floats(nl)) * sizeof(float); }
 

@@ -26,6 +26,7 @@
 #include "su2_common.cuh"
 #include "su2_device.cuh"
 #include "su2_kernels.cuh"
+#include "cuda_host.cuh"
 #include "host/capi_common.hpp"
 #include "host/pair_order.hpp"
 #include "../../include/spn_su2.h"
@@ -577,23 +578,10 @@ __global__ void xyz_unpack_kernel(const float4 *__restrict__ v, float *__restric
     }
 }
 
-void check_cuda(cudaError_t e, const char *what) {
-    if (e != cudaSuccess) throw Error(ErrorType::Cuda, std::string(what) + ": " + cudaGetErrorString(e));
-}
-
-template <class T>
-T *dalloc(size_t count, const char *what) {
-    void *p = nullptr;
-    check_cuda(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T) + 16), what);
-    return static_cast<T *>(p);
-}
-
-template <class T>
-void h2d(T *dst, const T *src, size_t count, cudaStream_t s) {
-    if (count) check_cuda(cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync H2D");
-}
-
-int copy_grid(long long n) { return int(std::min<long long>((n + 255) / 256, 4096)); }
+using cuh::check_cuda;
+using cuh::copy_grid;
+using cuh::dalloc;
+using cuh::h2d;
 
 }  // namespace
 
