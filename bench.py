@@ -21,13 +21,21 @@ JSON line (rank 0):
   roofline  the vertex-flow kernel: algorithmic FP32 work per launch
             F_RHS = F_N (2N+8) (3*100*Nl + 4*sum O) over its CUDA-event launch time, against
             the FP32 FMA throughput measured in-run on the same GPU; "evaluated" uses the
-            node counts the step actually used instead of 2N+8
+            node counts the step actually used instead of 2N+8; "gather": the kernel's slab
+            gathers (16 segments of Nl pairs per evaluated node) per second against a pure
+            gather kernel timed in-run on the same GPU (spn_measure_gather_peak)
   cpu_baseline  the CPU oracle (restatement of the reference's SU(2) core) on this host's
             cores, on a bounded random sample of vertex triples at four cutoffs spread over
             the flow, extrapolated to one step
 
 --impl reference times the CPU oracle alone (the reference's own C++ build needs Boost and
 HDF5, absent here).  --gpus N > 1: replicas only (independent flows, no collective).
+
+Other workloads (--workload): pyrochlore-r5-n64, square-r3-n32 (the same line for other
+shapes); scan-square-j1j2-128 and serve-mixed (batched and served flows against sequential
+plain solves; --flows, --rates, --policy fifo|sjf[@slots]); precision-* (FP32 forms against
+the FP64 GPU flow); xyz-honeycomb-kitaev-r9-n48 and tri-honeycomb-kitaev-gamma-r9-n32 (whole
+flows of the XYZ and TRI cores against their oracles; --flow-cutoffs M for short runs).
 """
 from __future__ import annotations
 
