@@ -37,9 +37,11 @@ def test_debug_lattice_writes_ldf_and_needs_no_device(tmp_path):
 @pytest.mark.parametrize("symmetry", ["SU2", "XYZ", "TRI"])
 def test_every_core_identifier_is_accepted(tmp_path, symmetry):
     """FrgCoreFactory's identifiers (src/FrgCoreFactory.cpp:25-51); the lattice stage needs no
-    device."""
+    device.  Every core accepts a normalization option."""
     s = task.run_task(write(tmp_path, symmetry=symmetry), debug_lattice=True, verbose=-1)
     assert s.status == "new"
+    p = write(tmp_path, "n.xml", symmetry=symmetry, params="<j>1.0</j><normalization>2</normalization>")
+    assert task.run_task(p, debug_lattice=True, verbose=-1).status == "new"
 
 
 def test_cli_debug_lattice(tmp_path, capfd):
@@ -70,6 +72,9 @@ def test_cli_debug_lattice(tmp_path, capfd):
     (dict(params=""), -3, "Interaction parameter 'j' is not defined in the taskfile"),
     (dict(symmetry="U1"), -2, "Spin model identifier 'U1' does not exist."),
     (dict(symmetry="su2"), -2, "Spin model identifier 'su2' does not exist."),
+    # the XYZ and TRI cores take only a normalization (XYZFrgCore.cpp:19-28, TRIFrgCore.cpp:19-28)
+    (dict(symmetry="TRI", params="<j>1.0</j><spin>0.5</spin>"), -3, "Unknown spin model option 'spin'."),
+    (dict(symmetry="XYZ", params="<j>1.0</j><spin>0.5</spin>"), -3, "Unknown spin model option 'spin'."),
     (dict(lattice="nonexistent"), -3, "nonexistent"),
 ])
 def test_task_validation_errors(tmp_path, kw, code, message):
