@@ -263,9 +263,14 @@ int spn_su2_measure_correlation_f64(spn_su2 *h, double *zz, double *dd, double *
  * (1 064 960 bytes per GPU, held until the process exits), which limits n_freq <= 256 and
  * n_sites <= 128; larger sizes are rejected with SPN_E_UNSUPPORTED.  The first call on a device
  * looks up that array's device address (with the device current) and should come before any
- * stream capture.  Work is queued on `stream` (a cudaStream_t, NULL = default stream) and
- * the call returns without waiting.  All calls on one device share the array: calls whose
- * work overlaps on the GPU race and must be ordered by the caller. */
+ * stream capture.  The looked-up address is kept for the life of the process: a
+ * cudaDeviceReset() ends the context that holds the array, so after a reset this entry point
+ * must not be called on that device again in the same process.  Work is queued on `stream` (a
+ * cudaStream_t, NULL = default stream) and the call returns without waiting.  All calls on one
+ * device share the array: calls whose work overlaps on the GPU race and must be ordered by the
+ * caller.  The tables are read on the device and not checked on the host: sites_rid and
+ * inv_sites_rid entries must lie in [0, n_sites); a corr_rid entry outside [0, n_sites) gives
+ * NaN in its zz and dd outputs. */
 int spn_su2_correlation_noalloc(int n_freq, const float *freq, int n_sites, const int *sites_rid,
                                 const int *inv_sites_rid, int n_corr, const int *corr_rid, float spin_length,
                                 float cutoff, const float *v2, const float *v4ss, const float *v4dd, float *out,

@@ -1067,6 +1067,8 @@ static __device__ __align__(256) double g_corr_scratch[size_t(kMaxCorrNodes) * 2
 
 // Device address of g_corr_scratch per device.  In host code the array's name is only a
 // host-side stand-in, so the address is looked up once per device with that device current.
+// The cache is never invalidated: after a cudaDeviceReset() the address belongs to a context
+// that no longer exists (the header tells callers not to use this entry point after a reset).
 double *g_corr_scratch_addr[kNoAllocMaxDevices] = {};
 
 double *corr_scratch_for_current_device() {

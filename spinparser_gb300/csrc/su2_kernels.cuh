@@ -252,8 +252,15 @@ __device__ __forceinline__ void corr_final_body(const CorrArgsT<T> &a) {
     __syncthreads();
     for (int q = threadIdx.x; q < a.n_corr; q += blockDim.x) {
         const int r = a.corr_rid[q];
-        a.out[q] = T(chi[r]);
-        a.out[a.n_corr + q] = T(chi[a.nl + r]);
+        // an entry outside [0, nl) (possible only with caller-owned device tables) reads
+        // nothing and yields NaN
+        double zz = __longlong_as_double(0x7ff8000000000000LL), dd = zz;
+        if (r >= 0 && r < a.nl) {
+            zz = chi[r];
+            dd = chi[a.nl + r];
+        }
+        a.out[q] = T(zz);
+        a.out[a.n_corr + q] = T(dd);
     }
 }
 

@@ -92,10 +92,16 @@ def prepare(t: Ticket) -> None:
         t.work = expected_work(tab, freq, cut)
 
 
-def next_ticket(queue, policy: str) -> Ticket:
+def next_ticket(queue, policy: str, now: float | None = None, max_wait: float | None = None) -> Ticket:
     """The request a server admits next: the oldest ("fifo") or the one with the least expected
-    work, ties to the oldest ("sjf")."""
+    work, ties to the oldest ("sjf").  Under "sjf" a large request could wait for ever while
+    smaller ones keep arriving; with `max_wait` set, the oldest request goes first once it has
+    waited longer than that (seconds since its arrival at `now`)."""
     if policy == "sjf":
+        oldest = min(queue, key=lambda q: (q.t_arrival, q.id))
+        if max_wait is not None and now is not None and now - oldest.t_arrival > max_wait:
+            prepare(oldest)
+            return oldest
         for q in queue:
             prepare(q)
         return min(queue, key=lambda q: (q.work, q.id))
@@ -105,10 +111,12 @@ def next_ticket(queue, policy: str) -> Ticket:
 
 class FlowServer:
     def __init__(self, device: int = 0, memory_budget: int | None = None, max_flows: int | None = None,
-                 nodes_per_iteration: int = 1, use_graph: bool = True, clock=time.perf_counter, policy: str = "fifo"):
+                 nodes_per_iteration: int = 1, use_graph: bool = True, clock=time.perf_counter, policy: str = "fifo",
+                 max_wait: float | None = None):
         if policy not in ("fifo", "sjf"):
             raise ValueError("policy must be 'fifo' or 'sjf'")
         self.policy = policy
+        self.max_wait = max_wait
         self.batch = Su2Batch(device, nodes_per_iteration, use_graph)
         if memory_budget is None:
             free, _ = device_memory(device)
@@ -133,12 +141,14 @@ class FlowServer:
         while self.queue:
             if self.max_flows is not None and len(self.active) >= self.max_flows:
                 return
-            t = next_ticket(self.queue, self.policy)
+            t = next_ticket(self.queue, self.policy, self.clock(), self.max_wait)
             if self.active and self.used + t.footprint > self.budget:
                 return
-            self.queue.remove(t)
             tab, freq, cut = t._built
+            # the request leaves the queue only once the batch holds it: if add() raises (out
+            # of device memory, say), it stays queued and the error reaches the caller
             t.flow_id = self.batch.add(tab, freq, cut, flags=t.spec.flags)
+            self.queue.remove(t)
             t.t_admit = self.clock()
             self.used += t.footprint
             self.active[t.flow_id] = t

@@ -228,7 +228,9 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        raise SystemExit("usage: make_fixtures.py <reference checkout> [reference2|reference3]")
+    root = sys.argv[1]
     if len(sys.argv) > 2 and sys.argv[2] == "reference2":
         write_reference2(root)
     elif len(sys.argv) > 2 and sys.argv[2] == "reference3":

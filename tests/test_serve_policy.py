@@ -42,3 +42,30 @@ def test_unknown_policy_is_rejected():
     from spinparser_gb300.serve import FlowServer
     with pytest.raises(ValueError):
         FlowServer(policy="lifo")
+
+
+def test_sjf_admits_the_oldest_once_it_waited_too_long():
+    q = queue(spec(5, 16), spec(3, 8))  # arrivals at t = 0 (large) and t = 1 (small)
+    assert next_ticket(q, "sjf", now=5.0, max_wait=10.0) is q[1]
+    assert next_ticket(q, "sjf", now=12.0, max_wait=10.0) is q[0]
+    assert next_ticket(q, "sjf", now=12.0) is q[1]  # no bound: least work first
+
+
+class _FailingBatch:
+    def add(self, *a, **k):
+        raise MemoryError("device memory exhausted")
+
+
+def test_request_stays_queued_when_the_batch_cannot_take_it():
+    from collections import deque
+
+    from spinparser_gb300.serve import FlowServer
+
+    srv = FlowServer.__new__(FlowServer)  # host logic only: no device batch
+    srv.policy, srv.max_wait, srv.max_flows, srv.budget, srv.used = "fifo", None, None, 1 << 40, 0
+    srv.clock = lambda: 0.0
+    srv.batch = _FailingBatch()
+    srv.queue, srv.active = deque(queue(spec(3, 8))), {}
+    with pytest.raises(MemoryError):
+        srv._admit()
+    assert len(srv.queue) == 1 and not srv.active

@@ -36,11 +36,36 @@ def _state(tab, freq, cut, steps):
     return c, v2, ss, dd
 
 
-def test_noalloc_correlation_matches_handle_entry_point_twice():
+def _perturbed_initial_state(tab, n, seed):
+    """The model's initial condition plus a seeded perturbation of every entry (a state no
+    flow step is needed for, so the largest frequency count stays cheap)."""
+    v2, ss, dd = tab.initial_state(n)
+    rng = np.random.default_rng(seed)
+    v2 = (v2 + 0.01 * rng.standard_normal(v2.shape)).astype(np.float32)
+    ss = (ss + 0.05 * rng.standard_normal(ss.shape)).astype(np.float32)
+    dd = (dd + 0.05 * rng.standard_normal(dd.shape)).astype(np.float32)
+    return v2, ss, dd
+
+
+# (lattice, range, model, couplings, N, states): square r3 runs the one-site-per-lane kernel,
+# r11 (42 sites) two sites per lane, r15 (72 sites) four; N = 256 fills the scratch's rows
+# (2N + 4 of 2 * 256 + 8 node rows).  States: GPU flow steps from the initial condition, or
+# seeded perturbations of it at two cutoffs.
+CASES = [
+    ("square", 3, "square-j1j2heisenberg", {"j1": "1.0", "j2": "0.3"}, 20, ("steps", 6, 30)),
+    ("square", 11, "square-heisenberg", {"j": "1.0"}, 10, ("steps", 2, 5)),
+    ("square", 15, "square-heisenberg", {"j": "1.0"}, 8, ("steps", 2, 5)),
+    ("square", 3, "square-heisenberg", {"j": "1.0"}, 256, ("perturbed", 0.8, 0.05)),
+]
+
+
+@pytest.mark.parametrize("lattice,rng_,model,params,n,states", CASES,
+                         ids=["sites6-n20", "sites42-n10", "sites72-n8", "sites6-n256"])
+def test_noalloc_correlation_matches_handle_entry_point_twice(lattice, rng_, model, params, n, states):
     torch = pytest.importorskip("torch")
     lib = spn.load_library()
-    tab = spn.Lattice("square", 3, "square-j1j2heisenberg", {"j1": "1.0", "j2": "0.3"}).tables()
-    freq = spn.frequency_exponential(0.005, 50.0, 20)
+    tab = spn.Lattice(lattice, rng_, model, params).tables()
+    freq = spn.frequency_exponential(0.005, 50.0, n)
     cut = spn.cutoff_exponential(50.0, 0.05, 0.9)
     dev = torch.device("cuda:0")
 
@@ -55,8 +80,12 @@ def test_noalloc_correlation_matches_handle_entry_point_twice():
     out_d = torch.full((2 * n_corr + 2 * nl,), float("nan"), dtype=torch.float32, device=dev)
 
     first = None
-    for steps in (6, 30):  # two calls in a row, different states and cutoffs
-        c, v2, ss, dd = _state(tab, freq, cut, steps)
+    for k, x in enumerate(states[1:]):  # two calls in a row, different states and cutoffs
+        if states[0] == "steps":
+            c, v2, ss, dd = _state(tab, freq, cut, x)
+        else:
+            c = np.float32(x)
+            v2, ss, dd = _perturbed_initial_state(tab, n, 20261204 + k)
         v2_d, ss_d, dd_d = d(v2, np.float32), d(ss, np.float32), d(dd, np.float32)
         rc = lib.spn_su2_correlation_noalloc(
             len(freq), C.c_void_p(freq_d.data_ptr()), nl, C.c_void_p(sites_d.data_ptr()),
@@ -66,6 +95,7 @@ def test_noalloc_correlation_matches_handle_entry_point_twice():
         spn._capi.check(rc)
         torch.cuda.synchronize()
         out = out_d.cpu().numpy()
+        del v2_d, ss_d, dd_d
 
         flow = spn.Su2Flow(tab, freq)
         flow.set_state(float(c), v2, ss, dd)
