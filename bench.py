@@ -24,12 +24,15 @@ JSON line (rank 0):
             node counts the step actually used instead of 2N+8; "gather": the kernel's slab
             gathers (16 segments of Nl pairs per evaluated node) per second against a pure
             gather kernel timed in-run on the same GPU (spn_measure_gather_peak)
-  cpu_baseline  the CPU oracle (restatement of the reference's SU(2) core) on this host's
-            cores, on a bounded random sample of vertex triples at four cutoffs spread over
-            the flow, extrapolated to one step
+  cpu_baseline  the CPU port of the reference's SU(2) core (the oracle's sources built with the
+            reference's flags, -O3 -fopenmp) on all of this host's cores: three complete
+            cutoff steps (full RHS over every triple, measurement, Euler) at cutoffs spread
+            over the flow, from the GPU flow's final state; nproc and CPU model recorded
 
---impl reference times the CPU oracle alone (the reference's own C++ build needs Boost and
-HDF5, absent here).  --gpus N > 1: replicas only (independent flows, no collective).
+--impl reference times that CPU core alone (the reference's own C++ build needs Boost and
+HDF5, absent here): every timed step one complete cutoff step at the cutoffs the GPU arm
+times, so steps x ms_per_step is CPU time actually spent.  --gpus N > 1: replicas only
+(independent flows, no collective).
 
 Other workloads (--workload): pyrochlore-r5-n64, square-r3-n32 (the same line for other
 shapes); scan-square-j1j2-128 and serve-mixed (batched and served flows against sequential
@@ -42,6 +45,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import subprocess
 import sys
 import tempfile
@@ -80,6 +84,13 @@ TRI_WORKLOADS = {
                                               fmax=50.0, cmax=50.0, cmin=0.05, cstep=0.98),
 }
 METRIC = "cutoff steps/s per flow"
+PRECISION_FORMS = {
+    "fp64-self-energy": "FP32 vertex state and flow with Kahan-compensated loop-frequency sums; FP64 self-energy state, "
+                        "flow and Euler update, FP64 quadrature weights and FP64 measurement accumulation "
+                        "(SPN_SU2_FP64_SELF_ENERGY)",
+    "plain": "FP32 vertex and self-energy state (the reference's types) with Kahan-compensated loop-frequency sums; "
+             "FP64 quadrature weights and FP64 measurement accumulation",
+}
 KERNELS_PER_STEP = 8  # self-energy, node tables, vertex flow, 2 x correlation, 3 x Euler
 
 
@@ -99,8 +110,10 @@ def parse_args():
                          "optionally @k for a k-flow slot limit (e.g. fifo,sjf@2)")
     ap.add_argument("--flow-cutoffs", type=int, default=None,
                     help="XYZ/TRI workloads: run only the first M cutoffs of the flow (short runs for profiling)")
+    ap.add_argument("--precision", choices=["fp64-self-energy", "plain"], default="fp64-self-energy",
+                    help="single-flow workloads: the precision form timed (default: FP32 vertex with Kahan sums, FP64 "
+                         "self-energy, quadrature weights and measurement; plain: FP32 self-energy state)")
     ap.add_argument("--e2e-steps", type=int, default=10)
-    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU work budget of the baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-full-flow", action="store_true")
     return ap.parse_args()
@@ -201,67 +214,127 @@ class ClockSampler:
                 "samples": len(rows), "power_w_max": float(np.nanmax([num(r[3]) for r in rows]))}
 
 
-def cpu_baseline(tab, freq, cutoffs, state, budget_s):
-    """The oracle on all host cores: a random sample of vertex triples at each of the given
-    cutoffs (plus the full self-energy flow), extrapolated to one average step."""
-    from oracle import Oracle
-
-    threads = os.cpu_count() or 1
-    orc = Oracle(tab, freq)
-    v2, ss, dd = state
-    fn = orc.fn
-    rng = np.random.default_rng(20261203)
-    per_cut = budget_s / len(cutoffs)
-    t_steps, n_total, t_total = [], 0, 0.0
-    for c in cutoffs:
-        t0 = time.perf_counter()
-        dv2 = orc.self_energy(c, v2, ss, dd)
-        t_se = time.perf_counter() - t0
-        probe = rng.choice(fn, size=min(fn, 2 * threads), replace=False)
-        t0 = time.perf_counter()
-        orc.vertex_sample(c, v2, dv2, ss, dd, probe, threads)
-        per_triple = (time.perf_counter() - t0) / len(probe)
-        n = int(min(fn, max(len(probe), per_cut / max(per_triple, 1e-9))))
-        sample = rng.choice(fn, size=n, replace=False)
-        t0 = time.perf_counter()
-        orc.vertex_sample(c, v2, dv2, ss, dd, sample, threads)
-        t_s = time.perf_counter() - t0
-        t_steps.append(t_s * fn / n + t_se)
-        n_total += n
-        t_total += t_s
-    t_step = float(np.mean(t_steps))
-    return {"value": 1.0 / t_step, "unit": "steps/s", "cores": threads, "kind": "port",
-            "sample": f"{n_total} vertex triples (uniform random of {fn}, seed 20261203) at cutoffs "
-                      f"{[round(float(c), 4) for c in cutoffs]} + the full self-energy flow at each; {t_total:.1f} s "
-                      f"on {threads} threads; one average step extrapolated to {t_step:.2f} s"}
+def cpu_info() -> dict:
+    """Host cores and CPU model of the machine the CPU numbers come from."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"nproc": os.cpu_count() or 1, "cpu_model": model or platform.machine()}
 
 
-def baseline_cutoffs(cut):
-    return [float(cut[i]) for i in sampled_steps(len(cut), 0, 4)]
+CPU_BUILD = "oracle sources at the reference's flags: g++ -O3 -fopenmp (default FP contraction)"
+
+
+class CpuStep:
+    """One cutoff step of the CPU core, as the reference's loop runs it: the complete flow
+    right-hand side (self-energy flow, then the vertex flow of every triple, OpenMP over
+    triples on all host cores), the correlation measurement and the explicit Euler update,
+    with the oracle built at the reference's optimisation flags."""
+
+    def __init__(self, tab, freq, state):
+        from oracle import Oracle
+
+        self.orc = Oracle(tab, freq, timing=True)
+        self.threads = os.cpu_count() or 1
+        self.v2, self.ss, self.dd = (np.array(x, np.float32).reshape(-1) for x in state)
+        self.flush = np.empty(64 * 1024 * 1024, np.float32)  # 256 MB, larger than the host caches
+
+    def flush_caches(self, i):
+        self.flush.fill(float(i))
+
+    def run(self, cutoff, new_cutoff):
+        o = self.orc
+        dv2, dss, ddd = o.rhs(cutoff, self.v2, self.ss, self.dd, threads=self.threads)
+        o.correlation(cutoff, self.v2, self.ss, self.dd)
+        o.euler(cutoff, new_cutoff, self.v2, dv2)
+        o.euler(cutoff, new_cutoff, self.ss, dss)
+        o.euler(cutoff, new_cutoff, self.dd, ddd)
+
+    def warm(self, cutoff):
+        """An untimed warm-up: the self-energy flow and a 1 % triple sample (threads started,
+        pages touched)."""
+        o = self.orc
+        dv2 = o.self_energy(cutoff, self.v2, self.ss, self.dd)
+        sample = np.arange(0, o.fn, 100, dtype=np.int32)
+        o.vertex_sample(cutoff, self.v2, dv2, self.ss, self.dd, sample, self.threads)
+
+
+def cpu_baseline(tab, freq, cut, state, n_steps=3):
+    """The CPU core on all host cores: n_steps complete cutoff steps (full RHS, measurement,
+    Euler) at cutoffs spread evenly over the list, from the given state."""
+    step = CpuStep(tab, freq, state)
+    # the midpoints of n_steps equal parts of the list (the work of a step grows as the
+    # cutoff falls, so the mean over them follows the whole flow's mean)
+    idx = [min(len(cut) - 2, int((i + 0.5) * (len(cut) - 1) / n_steps)) for i in range(n_steps)]
+    step.warm(float(cut[idx[0]]))
+    secs = []
+    for i, k in enumerate(idx):
+        step.flush_caches(i)
+        t0 = time.perf_counter()
+        step.run(float(cut[k]), float(cut[k + 1]))
+        secs.append(time.perf_counter() - t0)
+    t_step = float(np.mean(secs))
+    info = cpu_info()
+    return {"value": 1.0 / t_step, "unit": "steps/s", "cores": step.threads, "kind": "port", **info,
+            "build": CPU_BUILD,
+            "sample": f"{n_steps} complete cutoff steps (every one of {step.orc.fn} triples, measurement, Euler) at "
+                      f"cutoffs {[round(float(cut[k]), 4) for k in idx]}; {sum(secs):.1f} s on {step.threads} threads; "
+                      f"mean {t_step:.2f} s per step"}
+
+
+def workload_config(args, wl, tab, cut, n, world=1):
+    """The workload as both arms print it."""
+    fn = n * n * (n + 1) // 2
+    return {"workload": args.workload, "lattice": wl["lattice"], "range": wl["range"], "model": wl["model"],
+            "params": wl["params"], "n_freq": n, "freq_range": [wl["fmin"], wl["fmax"]],
+            "cutoff": [wl["cmax"], wl["cmin"], wl["cstep"]], "n_cutoffs": len(cut), "n_sites": tab.n_sites,
+            "n_overlap": tab.n_overlap, "n_triples": fn, "parallelism": f"replicas x{world}",
+            "timed_steps": "spread evenly over the cutoff list",
+            "l2": "flushed (256 MB write) before every timed step"}
 
 
 def run_reference(args, wl):
-    """--impl reference: the CPU oracle only (rank 0)."""
+    """--impl reference: the reference's SU(2) core on the host cores (the oracle port built with
+    the reference's flags), rank 0 only.  Every timed step is one complete cutoff step (full
+    RHS over all triples, measurement, Euler) at the cutoffs the GPU arm times; the state is
+    the model's initial condition, advanced by these steps (the work of a step depends on the
+    cutoff, not on the state's values)."""
     if int(os.environ.get("RANK", "0")) != 0:
         return
     tab, freq, cut = setup(wl)
-    state = tab.initial_state(len(freq))
-    per_step = max(2.0, min(8.0, 150.0 / max(1, args.steps + args.warmup)))
+    n = len(freq)
+    step = CpuStep(tab, freq, tab.initial_state(n))
+    schedule = sampled_steps(len(cut), args.warmup, args.steps)
     for _ in range(args.warmup):
-        cpu_baseline(tab, freq, baseline_cutoffs(cut)[:1], state, 0.2)
-    vals, last = [], None
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        last = cpu_baseline(tab, freq, baseline_cutoffs(cut), state, per_step)
-        vals.append(last["value"])
-    wall = time.perf_counter() - t0
-    value = float(np.mean(vals))
+        step.warm(float(cut[schedule[0]]))
+    secs = []
+    wall0 = time.perf_counter()
+    for i, k in enumerate(schedule):
+        step.flush_caches(i)
+        t0 = time.perf_counter()
+        step.run(float(cut[k]), float(cut[k + 1]))
+        secs.append(time.perf_counter() - t0)
+    wall = time.perf_counter() - wall0
+    total = float(np.sum(secs))
+    value = len(schedule) / total
+    info = cpu_info()
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (model initial condition)",
-            "config": {"workload": args.workload, "lattice": wl["lattice"], "range": wl["range"], "model": wl["model"],
-                       "params": wl["params"], "n_freq": wl["n_freq"], "l2": "n/a (CPU)"},
-            "cpu_baseline": {**last, "value": value},
+            "steps": len(schedule), "warmup": args.warmup, "ms_per_step": 1e3 * total / len(schedule),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (model initial condition, advanced by the timed steps)",
+            "config": workload_config(args, wl, tab, cut, n),
+            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": step.threads, "kind": "port", **info,
+                             "build": CPU_BUILD,
+                             "sample": f"{len(schedule)} complete cutoff steps (full RHS over all {step.orc.fn} triples, "
+                                       f"measurement, Euler) at the GPU arm's cutoffs; warm-up steps: self-energy + "
+                                       f"1 % triple sample, untimed"},
+            "lattice_tables": "built by the repository's lattice factory (input, pinned by the hyperkagome golden)",
             "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "wall_s": wall}
     print(json.dumps(line))
@@ -279,22 +352,31 @@ def _plain_solve(spec):
     return meas, zz, dd, div
 
 
-def _cpu_flow_seconds(specs, budget_s):
-    """CPU oracle time of whole flows, per distinct (lattice, range, N): the per-step time from
-    a bounded triple sample at the four baseline cutoffs, times the flow's steps."""
+def _cpu_flow_seconds(specs, steps_per_class):
+    """CPU time of whole flows, per distinct (lattice, range, model, N): the mean time of
+    complete CPU steps at cutoffs spread over the flow, times the flow's steps."""
     classes = {}
     for sp in specs:
         classes.setdefault((sp.lattice, sp.range, sp.model, sp.n_freq), []).append(sp)
-    per_class = budget_s / max(1, len(classes))
-    total, samples = 0.0, []
+    total, samples, b = 0.0, [], None
     for (lat, rng_, model, n), members in classes.items():
         sp = members[0]
         tab, freq, cut = sp.build()
-        b = cpu_baseline(tab, freq, baseline_cutoffs(cut), tab.initial_state(len(freq)), per_class)
+        b = cpu_baseline(tab, freq, cut, tab.initial_state(len(freq)), steps_per_class)
         t_step = 1.0 / b["value"]
         total += t_step * (len(cut) - 1) * len(members)
-        samples.append(f"{lat} r{rng_} N{n}: {t_step:.2f} s/step x {len(members)}")
-    return total, samples, b["cores"]
+        samples.append(f"{lat} r{rng_} N{n}: {t_step:.3f} s/step x {len(members)}")
+    return total, samples, b
+
+
+def _by_class(specs, secs):
+    """Total seconds and flow count per (lattice, range, N) class."""
+    out = {}
+    for sp, t in zip(specs, secs):
+        k = f"{sp.lattice} r{sp.range} N{sp.n_freq}"
+        tot, cnt = out.get(k, (0.0, 0))
+        out[k] = (tot + float(t), cnt + 1)
+    return {k: {"seconds": round(v[0], 4), "flows": v[1]} for k, v in sorted(out.items())}
 
 
 def _check_same(a, b):
@@ -381,7 +463,8 @@ def run_multi(args):
                                "p50_s": float(np.percentile(plain_ttr, 50)), "p99_s": float(np.percentile(plain_ttr, 99))},
         }
     clocks = sampler.stop()
-    cpu_s, cpu_samples, cores = _cpu_flow_seconds(specs, args.cpu_seconds) if not args.no_cpu_baseline else (None, [], 0)
+    cpu_s, cpu_samples, cpu_b = (_cpu_flow_seconds(specs, 2 if scan else 1) if not args.no_cpu_baseline
+                                 else (None, [], None))
     top = arms[list(arms)[-1]]
     line = {
         "metric": "scan flows/s" if scan else "served flows/s",
@@ -392,14 +475,16 @@ def run_multi(args):
                    if scan else "square/cubic/pyrochlore J1-J2, J2 U[-0.5,0.5], range U{3..7}, N U{32,48,64}, "
                                 "grid [0.005,50], cutoff 50->0.05 x0.98, Poisson arrivals"},
         "plain_gpu_sequential": {"flows_per_s": n / t_plain, "seconds": t_plain,
-                                 "service_s_mean": float(service.mean()), "service_s_max": float(service.max())},
+                                 "service_s_mean": float(service.mean()), "service_s_max": float(service.max()),
+                                 "seconds_by_class": _by_class(specs, service)},
         "speedup_vs_plain": top["batched"]["flows_per_s"] / (n / t_plain),
         "arms": arms,
         "max_abs_diff_vs_plain": max_diff,
         "cpu_baseline": None if cpu_s is None else {
-            "value": n / cpu_s, "unit": "flows/s", "cores": cores, "kind": "port",
-            "sample": "per (lattice, range, N): oracle step time from a bounded triple sample at 4 cutoffs x steps; "
-                      + "; ".join(cpu_samples)},
+            "value": n / cpu_s, "unit": "flows/s", "cores": cpu_b["cores"], "kind": "port", "nproc": cpu_b["nproc"],
+            "cpu_model": cpu_b["cpu_model"], "build": CPU_BUILD,
+            "sample": "per (lattice, range, N): mean time of %d complete CPU steps spread over the flow, x its steps "
+                      "(extrapolated); " % (2 if scan else 1) + "; ".join(cpu_samples)},
         "clocks": clocks,
     }
     print(json.dumps(line))
@@ -599,7 +684,8 @@ def main():
     n = len(freq)
     if args.warmup + 2 > len(cut):
         raise SystemExit("not enough cutoff values")
-    flow = spn.Su2Flow(tab, freq, device=local)
+    flags = spn.FP64_SELF_ENERGY if args.precision == "fp64-self-energy" else 0
+    flow = spn.Su2Flow(tab, freq, device=local, flags=flags)
     stream = torch.cuda.Stream(device=local)
     flow.set_stream(stream.cuda_stream)
     flow.set_state(float(cut[0]), *tab.initial_state(n))
@@ -729,12 +815,7 @@ def main():
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": len(schedule),
         "warmup": args.warmup, "ms_per_step": total_ms / len(schedule), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (model initial condition, advanced by the flow)",
-        "config": {"workload": args.workload, "lattice": wl["lattice"], "range": wl["range"], "model": wl["model"],
-                   "params": wl["params"], "n_freq": n, "freq_range": [wl["fmin"], wl["fmax"]],
-                   "cutoff": [wl["cmax"], wl["cmin"], wl["cstep"]], "n_cutoffs": len(cut), "n_sites": tab.n_sites,
-                   "n_overlap": tab.n_overlap, "n_triples": flow.fn, "parallelism": f"replicas x{world}",
-                   "timed_steps": "spread evenly over the cutoff list",
-                   "l2": "flushed (256 MB write) before every timed step"},
+        "config": workload_config(args, wl, tab, cut, n, world),
         "e2e": {"value": len(e2e_sched) / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes + 8 * flow.n_corr},
         "roofline": {"bound": "fp32", "kernel": "su2_vertex_flow_kernel", "achieved": achieved, "peak": fp32_peak,
@@ -744,6 +825,7 @@ def main():
                      "peak_source": "measured in-run: pure-FFMA kernel on this GPU (MEASURED_PEAKS.json has no "
                                     "FP32 CUDA-core figure)", "fp32_clock_ghz_implied": clk,
                      "gather": gather},
+        "precision_form": PRECISION_FORMS[args.precision],
         "vertex_variant": variant,
         "gpu_launches": KERNELS_PER_STEP * len(schedule),
         "clocks": clocks,
@@ -753,7 +835,7 @@ def main():
     }
     if not args.no_cpu_baseline and world == 1:
         c, v2, ss, dd = flow.get_state()
-        line["cpu_baseline"] = cpu_baseline(tab, freq, baseline_cutoffs(cut), (v2, ss, dd), args.cpu_seconds)
+        line["cpu_baseline"] = cpu_baseline(tab, freq, cut, (v2, ss, dd), 3)
     print(json.dumps(line))
     flow.close()
     if dist:

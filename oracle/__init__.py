@@ -25,17 +25,20 @@ class OracleDesc(C.Structure):
     ]
 
 
-def library_path() -> str:
-    return os.path.join(_HERE, "_build", platform.machine(), "liboracle_su2.so")
+def library_path(timing: bool = False) -> str:
+    """The checker build (-O2 -ffp-contract=off) or, with timing=True, the build of the same
+    sources with the reference's optimisation flags (-O3, default contraction) that the CPU
+    baseline times."""
+    name = "liboracle_su2_o3.so" if timing else "liboracle_su2.so"
+    return os.path.join(_HERE, "_build", platform.machine(), name)
 
 
-_LIB = None
+_LIBS = {}
 
 
-def _lib():
-    global _LIB
-    if _LIB is None:
-        path = library_path()
+def _lib(timing: bool = False):
+    if timing not in _LIBS:
+        path = library_path(timing)
         if not os.path.exists(path):
             raise RuntimeError(f"oracle library not built ({path}); run __graft_entry__.build()")
         lib = C.CDLL(path)
@@ -53,8 +56,8 @@ def _lib():
         lib.oracle_su2_euler_f32.restype = None
         lib.oracle_su2_flow_f32.argtypes = [dsc, fp, i, fp, fp, fp, fp, fp, i]
         lib.oracle_su2_flow_f64.argtypes = [dsc, fp, i, dp, dp, dp, dp, dp, i]
-        _LIB = lib
-    return _LIB
+        _LIBS[timing] = lib
+    return _LIBS[timing]
 
 
 def _p(a, t):
@@ -64,8 +67,8 @@ def _p(a, t):
 class Oracle:
     """CPU restatement of the reference SU(2) core for one lattice + frequency mesh."""
 
-    def __init__(self, tables, freq, spin_length: float = 0.5):
-        self.lib = _lib()
+    def __init__(self, tables, freq, spin_length: float = 0.5, timing: bool = False):
+        self.lib = _lib(timing)
         self.freq = np.ascontiguousarray(freq, np.float32)
         self.n = len(self.freq)
         self.nl = int(tables.n_sites)
@@ -127,6 +130,11 @@ class Oracle:
                                                      _p(dd, f), _p(its, C.c_int), len(its), _p(dss, f), _p(ddd, f),
                                                      threads) == 0
         return dss, ddd
+
+    def euler(self, cutoff, new_cutoff, x, dx):
+        """x += (new_cutoff - cutoff) * dx in place, rounded like SU2FrgCore::finalizeStep."""
+        assert x.dtype == np.float32 and dx.dtype == np.float32 and x.flags.c_contiguous and dx.flags.c_contiguous
+        self.lib.oracle_su2_euler_f32(cutoff, new_cutoff, x.size, _p(x, C.c_float), _p(dx, C.c_float))
 
     def correlation(self, cutoff, v2, ss, dd, fp64: bool = False):
         """Per-rid static susceptibility (spin, density)."""

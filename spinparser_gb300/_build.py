@@ -98,13 +98,28 @@ def build_library(force: bool = False) -> str:
     return lib
 
 
+def oracle_timing_library_path() -> str:
+    return os.path.join(ORACLE_DIR, "_build", platform.machine(), "liboracle_su2_o3.so")
+
+
 def build_oracle(force: bool = False) -> str:
-    """Compiles the CPU oracle (test infrastructure) into oracle/_build/<machine>/."""
+    """Compiles the CPU oracle (test infrastructure) into oracle/_build/<machine>/: the checker
+    (-O2 -ffp-contract=off: every float operation rounded on its own, as the reference's
+    x86-64 build rounds) and, from the same sources, the timed CPU baseline built with the
+    reference's own optimisation flags (-O3, the compiler's default floating-point contraction;
+    CMakeLists.txt of the reference), in parallel."""
     out = oracle_library_path()
+    timing = oracle_timing_library_path()
     os.makedirs(os.path.dirname(out), exist_ok=True)
     srcs = [os.path.join(ORACLE_DIR, f) for f in ("su2_oracle.cpp", "xyz_oracle.cpp", "tri_oracle.cpp")]
+    jobs = []
     if force or _stale(out, srcs):
-        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp", *srcs, "-o", out])
+        jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp", *srcs, "-o", out])
+    if force or _stale(timing, srcs):
+        jobs.append(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", *srcs, "-o", timing])
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        for fut in [ex.submit(_run, j) for j in jobs]:
+            fut.result()
     return out
 
 

@@ -21,3 +21,15 @@ def built_library():
 
     __graft_entry__.build()
     return True
+
+
+# Normwise errors that the full-size parity tests measure, printed at the end of the run (also
+# with -q) so that a run's log states them.
+PARITY_REPORT: list[str] = []
+
+
+def pytest_terminal_summary(terminalreporter):
+    if PARITY_REPORT:
+        terminalreporter.section("parity errors (normwise, GPU vs oracle)")
+        for line in PARITY_REPORT:
+            terminalreporter.write_line(line)

@@ -1,0 +1,111 @@
+"""Full-size parity: whole right-hand sides and whole flows of the GB300 core against the CPU
+oracle (the restatement of src/SU2/SU2FrgCore.cpp:89-431), at the shapes the benchmark uses.
+
+* cubic J1-J2 r6, N = 64 (133 120 triples, 23 sites, 4095 RPA pairs): the complete RHS (self-
+  energy flow and both vertex flows, every triple) at an early, a mid-flow and the last cutoff
+  of the 377-value list 100 -> 0.05 x 0.98.  At the last cutoff every Katanin range of
+  SU2FrgCore.cpp:374-424 holds nodes for most transfer frequencies.  The states come from the
+  GPU flow itself, advanced from the initial condition and read back with get_state.
+* pyrochlore r5, N = 64 on [0.002, 100]: the complete RHS at the last cutoff of 100 -> 0.01 x 0.99
+  (917 values), from the GPU-advanced state.
+* square r3, N = 32 on [0.005, 50], 50 -> 0.05 x 0.98 (342 cutoffs, 341 RHS evaluations): the
+  whole flow on the GPU against the whole flow of the FP32 oracle (the reference's arithmetic)
+  and of the FP64 oracle.  Correlations are compared at every cutoff.
+
+Tolerances: one RHS, normwise relative error max|gpu - oracle| / max|oracle| <= 1e-5 per array;
+final correlations (static spin and density susceptibility per site) <= 1e-4 normwise, the same
+bound at every cutoff.
+"""
+import numpy as np
+import pytest
+
+import spinparser_gb300 as spn
+from conftest import PARITY_REPORT
+from oracle import Oracle
+from spinparser_gb300.driver import run_flow
+
+pytestmark = pytest.mark.gpu
+
+RHS_TOL = 1e-5
+CORR_TOL = 1e-4
+
+
+def normwise(g, r):
+    r = np.asarray(r, np.float64)
+    return float(np.max(np.abs(np.asarray(g, np.float64) - r)) / max(float(np.max(np.abs(r))), 1e-300))
+
+
+def advanced_states(tab, freq, cut, stops):
+    """GPU flow from the initial condition; the state (cutoff, v2, ss, dd) at each step index
+    in `stops` (ascending), read back from the device."""
+    flow = spn.Su2Flow(tab, freq)
+    flow.set_state(float(cut[0]), *tab.initial_state(len(freq)))
+    out, k = {}, 0
+    for stop in stops:
+        while k < stop:
+            flow.compute_step()
+            flow.finalize_step(float(cut[k + 1]))
+            k += 1
+        assert not flow.is_diverged()
+        out[stop] = flow.get_state()
+    return flow, out
+
+
+def check_rhs(flow, orc, state, label):
+    c, v2, ss, dd = state
+    flow.set_state(float(c), v2, ss, dd)
+    flow.compute_step()
+    g2, gss, gdd = flow.get_flow()
+    r2, rss, rdd = orc.rhs(c, v2, ss, dd)
+    errs = (normwise(g2, r2), normwise(gss, rss), normwise(gdd, rdd))
+    PARITY_REPORT.append(f"{label} cutoff {float(c):.6g}: self-energy {errs[0]:.2e}, spin vertex {errs[1]:.2e}, "
+                         f"density vertex {errs[2]:.2e} ({len(rss)} entries)")
+    assert np.all(np.isfinite(gss)) and np.all(np.isfinite(gdd))
+    for e in errs:
+        assert e <= RHS_TOL, (label, errs)
+
+
+def test_whole_rhs_cubic_j1j2_r6_n64_early_mid_late():
+    tab = spn.Lattice("cubic", 6, "cubic-j1j2heisenberg", {"j1": "1.0", "j2": "0.25"}).tables()
+    freq = spn.frequency_exponential(0.005, 100.0, 64)
+    cut = spn.cutoff_exponential(100.0, 0.05, 0.98)
+    assert len(cut) == 377
+    stops = (40, 188, 375)
+    flow, states = advanced_states(tab, freq, cut, stops)
+    orc = Oracle(tab, freq)
+    for k in stops:
+        check_rhs(flow, orc, states[k], f"cubic r6 N64 step {k}")
+    flow.close()
+
+
+def test_whole_rhs_pyrochlore_r5_n64_late():
+    tab = spn.Lattice("pyrochlore", 5, "pyrochlore-heisenberg", {"j": "1.0"}).tables()
+    freq = spn.frequency_exponential(0.002, 100.0, 64)
+    cut = spn.cutoff_exponential(100.0, 0.01, 0.99)
+    assert len(cut) == 917
+    flow, states = advanced_states(tab, freq, cut, (915,))
+    check_rhs(flow, Oracle(tab, freq), states[915], "pyrochlore r5 N64 step 915")
+    flow.close()
+
+
+def test_whole_flow_square_r3_n32_final_correlations():
+    tab = spn.Lattice("square", 3, "square-heisenberg", {"j": "1.0"}).tables()
+    freq = spn.frequency_exponential(0.005, 50.0, 32)
+    cut = spn.cutoff_exponential(50.0, 0.05, 0.98)
+    assert len(cut) == 342
+    init = tab.initial_state(32)
+    flow = spn.Su2Flow(tab, freq)
+    measured, _, _, cz, cd, div = run_flow(flow, cut, init)
+    flow.close()
+    assert not div and len(measured) == len(cut)
+    orc = Oracle(tab, freq)
+    n32, s32, d32, _ = orc.flow(cut, *init)
+    n64, s64, d64, _ = orc.flow(cut, *init, fp64=True)
+    assert n32 == n64 == len(cut)
+    for label, rs, rd in (("FP32 oracle", s32, d32), ("FP64 oracle", s64, d64)):
+        per_cut = [max(normwise(cz[k], rs[k]), normwise(cd[k], rd[k])) for k in range(len(cut))]
+        fin = (normwise(cz[-1], rs[-1]), normwise(cd[-1], rd[-1]))
+        PARITY_REPORT.append(f"square r3 N32 whole flow vs {label}: final chi_zz {fin[0]:.2e}, chi_dd {fin[1]:.2e}; "
+                             f"max over {len(cut)} cutoffs {max(per_cut):.2e}")
+        assert max(fin) <= CORR_TOL, (label, fin)
+        assert max(per_cut) <= CORR_TOL, (label, max(per_cut))
