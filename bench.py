@@ -106,8 +106,9 @@ def parse_args():
     ap.add_argument("--rates", type=str, default="0.5,1,2,4,inf",
                     help="serve-mixed: arrival rates as multiples of the sequential plain-GPU capacity")
     ap.add_argument("--policy", type=str, default="fifo",
-                    help="serve-mixed: server arms to run at every rate, comma separated: fifo or sjf, "
-                         "optionally @k for a k-flow slot limit (e.g. fifo,sjf@2)")
+                    help="serve-mixed: server arms to run at every rate, comma separated: fifo or sjf, optionally @k "
+                         "for a k-flow residency limit, or srpt@k (k flows with the least remaining work run at each "
+                         "step), e.g. fifo,sjf@2,srpt@1")
     ap.add_argument("--flow-cutoffs", type=int, default=None,
                     help="XYZ/TRI workloads: run only the first M cutoffs of the flow (short runs for profiling)")
     ap.add_argument("--precision", choices=["fp64-self-energy", "plain"], default="fp64-self-energy",
@@ -387,97 +388,150 @@ def _check_same(a, b):
     return float(max(np.nanmax(np.abs(azz.reshape(b.zz.shape) - b.zz)), np.nanmax(np.abs(add_.reshape(b.dd.shape) - b.dd))))
 
 
+def _serve_local(items, arrivals, policy, plain):
+    """One rank's server over its dealt requests: (index, spec) items arriving at their offsets
+    of the global stream.  Returns per item (time to result, largest difference from the same
+    flow solved alone) and the rank's makespan."""
+    from spinparser_gb300.serve import FlowServer
+
+    name, _, slots = policy.partition("@")
+    srv = FlowServer(policy=name, max_flows=int(slots) if slots else None, autotune=True)
+    order = sorted(range(len(items)), key=lambda j: arrivals[items[j][0]])
+    t0 = time.perf_counter()
+    tickets, k = {}, 0
+    while True:
+        now = time.perf_counter() - t0
+        while k < len(order) and arrivals[items[order[k]][0]] <= now:
+            j = order[k]
+            tickets[j] = srv.submit(items[j][1], t_arrival=t0 + arrivals[items[j][0]])
+            k += 1
+        if srv.pump() == 0:
+            if k >= len(order):
+                break
+            time.sleep(min(0.01, max(0.0, arrivals[items[order[k]][0]] - (time.perf_counter() - t0))))
+    makespan = time.perf_counter() - t0
+    steps = (srv.steps, srv.tunings[:4])
+    srv.close()
+    out = [(tickets[j].time_to_result, _check_same(plain[items[j][0]], tickets[j].result)) for j in range(len(items))]
+    return out, makespan, steps
+
+
 def run_multi(args):
-    """Multi-flow workloads: batched / served flows against sequential plain-GPU solves."""
+    """Multi-flow workloads: batched / served flows against sequential plain-GPU solves.  Under
+    torchrun the flows are dealt round-robin over the ranks (replicas.run_sharded), each rank
+    runs its own plain solves and its own batch or server, and flows/s is all flows over the
+    slowest rank's time (weak scaling: per-rank work is the dealt share)."""
     import torch
 
-    from spinparser_gb300 import workloads
-    from spinparser_gb300.serve import FlowServer, time_to_result_stats
+    from spinparser_gb300 import replicas, workloads
+    from spinparser_gb300.serve import time_to_result_stats
 
-    torch.cuda.set_device(0)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
     scan = args.workload.startswith("scan")
     n = args.flows or (128 if scan else 24)
     specs = workloads.scan_specs(n) if scan else workloads.serve_specs(n)
+    items = list(enumerate(specs))
     # warm-up (untimed): kernels loaded, caches warm, allocator primed
     warm = [workloads.FlowSpec("square", 3, "square-j1j2heisenberg", (("j1", "1.0"), ("j2", "0.3")), 16,
                                0.005, 50.0, 50.0, 5.0, 0.9)] * 3
     for sp in warm:
         _plain_solve(sp)
+    from spinparser_gb300.serve import FlowServer
+
     srv = FlowServer()
     for sp in warm:
         srv.submit(sp)
     srv.drain()
     srv.close()
 
-    sampler = ClockSampler(0)
+    sampler = ClockSampler(local)
     sampler.start()
-    # sequential plain-GPU solves (FIFO, all requests present at t = 0)
-    plain, plain_done = [], []
-    t0 = time.perf_counter()
-    for sp in specs:
-        ts = time.perf_counter()
-        plain.append(_plain_solve(sp))
-        plain_done.append((time.perf_counter() - t0, time.perf_counter() - ts))
-    t_plain = time.perf_counter() - t0
-    service = np.array([d[1] for d in plain_done])
+    plain = {}
+
+    # sequential plain-GPU solves of each rank's share (FIFO, all present at t = 0)
+    def plain_solve(local_items):
+        t0 = time.perf_counter()
+        res = []
+        for i, sp in local_items:
+            ts = time.perf_counter()
+            plain[i] = _plain_solve(sp)
+            res.append(time.perf_counter() - ts)
+        return res, time.perf_counter() - t0
+
+    if dist:
+        dist.barrier()
+    job_plain, service_all, mine = replicas.run_sharded(items, plain_solve)
+    service = np.array(service_all)
     arms = {}
-    rates = [float("inf")] if scan else [float(x) * (1.0 / service.mean()) for x in args.rates.split(",")]
+    rates = [float("inf")] if scan else [float(x) * world / service.mean() for x in args.rates.split(",")]
     max_diff = 0.0
     policies = ["fifo"] if scan else args.policy.split(",")
     for rate in rates:
         arrivals = workloads.poisson_arrivals(n, rate)
         served = {}
         for policy in policies:
-            name, _, slots = policy.partition("@")
-            srv = FlowServer(policy=name, max_flows=int(slots) if slots else None)
-            t0 = time.perf_counter()
-            tickets = []
-            i = 0
-            while True:
-                now = time.perf_counter() - t0
-                while i < n and arrivals[i] <= now:
-                    tickets.append(srv.submit(specs[i], t_arrival=t0 + arrivals[i]))
-                    i += 1
-                busy = srv.pump()
-                if busy == 0:
-                    if i >= n:
-                        break
-                    time.sleep(min(0.01, max(0.0, arrivals[i] - (time.perf_counter() - t0))))
-            makespan = time.perf_counter() - t0
-            for t in tickets:
-                max_diff = max(max_diff, _check_same(plain[t.id], t.result))
-            served[policy] = {"flows_per_s": n / makespan, "makespan_s": makespan, "steps": srv.steps,
-                              **time_to_result_stats(tickets)}
-            srv.close()
-        # the same arrivals served by the sequential plain path (FIFO queue of its service times)
-        free_at, plain_ttr = 0.0, []
+            stats = {}
+
+            def served_solve(local_items):
+                out, makespan, steps = _serve_local(local_items, arrivals, policy, plain)
+                stats["steps"] = steps
+                return out, makespan
+
+            if dist:
+                dist.barrier()
+            job, res, _ = replicas.run_sharded(items, served_solve)
+            max_diff = max(max_diff, max(r[1] for r in res))
+            ttr = np.array([r[0] for r in res])
+            served[policy] = {"flows_per_s": job.throughput, "makespan_s": job.seconds, "steps_rank0": stats["steps"][0],
+                              "autotune_rank0": stats["steps"][1],
+                              "n": n, "p50_s": float(np.percentile(ttr, 50)), "p99_s": float(np.percentile(ttr, 99)),
+                              "mean_s": float(ttr.mean()), "max_s": float(ttr.max())}
+        # the same arrivals served by each rank's sequential plain path (FIFO queue of its
+        # service times over its share of the stream)
+        plain_ttr, free_at = [], {}
         for k in range(n):
-            start = max(free_at, arrivals[k])
-            free_at = start + service[k]
-            plain_ttr.append(free_at - arrivals[k])
+            r_ = k % world
+            start = max(free_at.get(r_, 0.0), arrivals[k])
+            free_at[r_] = start + service[k]
+            plain_ttr.append(free_at[r_] - arrivals[k])
+        span = max(free_at.values())
         arms["inf" if not np.isfinite(rate) else f"{rate:.4g}"] = {
             "arrival_rate_per_s": None if not np.isfinite(rate) else rate,
             "batched": served[policies[0]],
             **({"batched_by_policy": served} if len(policies) > 1 else {}),
-            "plain_gpu_fifo": {"flows_per_s": n / max(free_at, 1e-9), "makespan_s": free_at,
+            "plain_gpu_fifo": {"flows_per_s": n / max(span, 1e-9), "makespan_s": span,
                                "p50_s": float(np.percentile(plain_ttr, 50)), "p99_s": float(np.percentile(plain_ttr, 99))},
         }
     clocks = sampler.stop()
-    cpu_s, cpu_samples, cpu_b = (_cpu_flow_seconds(specs, 2 if scan else 1) if not args.no_cpu_baseline
+    if dist:
+        dist.barrier()
+    if rank != 0:
+        dist.destroy_process_group()
+        return
+    cpu_s, cpu_samples, cpu_b = (_cpu_flow_seconds(specs, 2 if scan else 1) if not args.no_cpu_baseline and world == 1
                                  else (None, [], None))
     top = arms[list(arms)[-1]]
     line = {
         "metric": "scan flows/s" if scan else "served flows/s",
-        "value": top["batched"]["flows_per_s"], "unit": "flows/s", "n_gpus": 1,
+        "value": top["batched"]["flows_per_s"], "unit": "flows/s", "n_gpus": world,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": args.workload, "flows": n, "seed": workloads.SEED,
+                   "parallelism": f"replicas x{world} (flows dealt round-robin)",
                    "draws": "square J1-J2, J2 U[0,1], range U{3,5,7}, N U{32,48,64}, grid [0.005,50], cutoff 50->0.05 x0.98"
                    if scan else "square/cubic/pyrochlore J1-J2, J2 U[-0.5,0.5], range U{3..7}, N U{32,48,64}, "
                                 "grid [0.005,50], cutoff 50->0.05 x0.98, Poisson arrivals"},
-        "plain_gpu_sequential": {"flows_per_s": n / t_plain, "seconds": t_plain,
+        "plain_gpu_sequential": {"flows_per_s": job_plain.throughput, "seconds": job_plain.seconds,
                                  "service_s_mean": float(service.mean()), "service_s_max": float(service.max()),
                                  "seconds_by_class": _by_class(specs, service)},
-        "speedup_vs_plain": top["batched"]["flows_per_s"] / (n / t_plain),
+        "speedup_vs_plain": top["batched"]["flows_per_s"] / job_plain.throughput,
         "arms": arms,
         "max_abs_diff_vs_plain": max_diff,
         "cpu_baseline": None if cpu_s is None else {
@@ -488,6 +542,8 @@ def run_multi(args):
         "clocks": clocks,
     }
     print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
 
 
 def _flow_history(flow, cut, fp64):

@@ -312,6 +312,28 @@ int spn_batch_destroy(spn_batch *b);
 /* Vertex-flow variant of the batch (npi = 1 or 2) and whether steps are replayed as graphs.
  * Variants do not change results. */
 int spn_batch_set_variant(spn_batch *b, int npi, int use_graph);
+/* Cross-flow sharing in the vertex flow.  Flows of a batch that have the same frequency mesh,
+ * lattice tables, spin length and cutoff list and stand at the same cutoff (a parameter scan's
+ * flows of one lattice, range and frequency count, admitted together) have the same
+ * loop-frequency nodes and interpolation supports; groups of at least min_group such flows
+ * (0 = off; default 2) are evaluated by a kernel that builds each node's supports once per
+ * subgroup and evaluates them for all its flows.  Subgroups hold at most the kernel's flows
+ * per block divided by cap_divisor (1, 2 or 4; default 1).  No counterpart in the reference,
+ * which runs one flow per process.  Results are bit-identical to the per-flow kernel's. */
+int spn_batch_set_grouping(spn_batch *b, int min_group, int cap_divisor);
+/* Holds a flow out of the following steps (paused = 1) or lets it take part again (0).  A
+ * paused flow keeps its state, phase and results; a serving loop uses this to give the GPU to
+ * the flows with the least remaining work.  Results do not change. */
+int spn_batch_set_paused(spn_batch *b, int flow_id, int paused);
+/* Flows the current plan evaluates with the grouped kernel. */
+int spn_batch_grouped_flows(spn_batch *b, int *n_grouped);
+/* Batch autotuner: times the vertex flow of the current flows, `reps` launches per candidate,
+ * over nodes per iteration (1, 2) x RPA schedule staging (without sharing) and x sharing (full
+ * or half subgroups), and keeps the fastest (returned, with its time per launch in ms).
+ * Touches no flow's state or results; call it between steps, after the flows of interest are
+ * admitted.  Replaces the reference LoadManager's chunk-size choice
+ * (src/lib/LoadManager.hpp:796-852). */
+int spn_batch_autotune(spn_batch *b, int reps, int *npi, int *min_group, int *cap_divisor, float *best_ms);
 /* Device memory a flow takes in a batch (state, flow, tables, measurement history): the
  * admission measure of a serving loop. */
 int spn_batch_footprint(const spn_su2_desc *desc, int n_cutoffs, long long *bytes);

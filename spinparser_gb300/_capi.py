@@ -160,6 +160,10 @@ SIGNATURES = {
     "spn_batch_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
     "spn_batch_destroy": (C.c_int, [C.c_void_p]),
     "spn_batch_set_variant": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "spn_batch_set_grouping": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "spn_batch_grouped_flows": (C.c_int, [C.c_void_p, c_int_p]),
+    "spn_batch_set_paused": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "spn_batch_autotune": (C.c_int, [C.c_void_p, C.c_int, c_int_p, c_int_p, c_int_p, c_float_p]),
     "spn_batch_footprint": (C.c_int, [C.POINTER(Su2Desc), C.c_int, c_ll_p]),
     "spn_batch_add": (C.c_int, [C.c_void_p, C.POINTER(Su2Desc), C.c_int, c_float_p, c_float_p, c_float_p, c_float_p,
                                 c_int_p]),

@@ -54,6 +54,30 @@ class Su2Batch:
         """Kernel variant and graph replay; results do not change."""
         check(self._lib.spn_batch_set_variant(self._h, nodes_per_iteration, int(use_graph)))
 
+    def set_grouping(self, min_group: int = 2, cap_divisor: int = 1) -> None:
+        """Cross-flow sharing of node supports in the vertex flow: groups of at least
+        `min_group` flows with the same mesh, lattice tables and cutoff list at the same cutoff
+        (0 = off), in subgroups of at most the kernel's flows per block / cap_divisor.  Results
+        do not change."""
+        check(self._lib.spn_batch_set_grouping(self._h, int(min_group), int(cap_divisor)))
+
+    def autotune(self, reps: int = 2) -> dict:
+        """Times the vertex flow of the current flows under each candidate configuration
+        (nodes per iteration x cross-flow sharing) and keeps the fastest; no state changes."""
+        a, m, c, t = C.c_int(), C.c_int(), C.c_int(), C.c_float()
+        check(self._lib.spn_batch_autotune(self._h, int(reps), C.byref(a), C.byref(m), C.byref(c), C.byref(t)))
+        return {"nodes_per_iteration": a.value, "min_group": m.value, "cap_divisor": c.value, "vertex_ms": t.value}
+
+    def set_paused(self, flow_id: int, paused: bool) -> None:
+        """Holds a flow out of the following steps (its state and results stay as they are)."""
+        check(self._lib.spn_batch_set_paused(self._h, flow_id, int(bool(paused))))
+
+    def grouped_flows(self) -> int:
+        """Flows the current plan evaluates with the grouped kernel."""
+        n = C.c_int()
+        check(self._lib.spn_batch_grouped_flows(self._h, C.byref(n)))
+        return n.value
+
     @staticmethod
     def footprint(tables: LatticeTables, freq, n_cutoffs: int) -> int:
         """Device bytes a flow occupies in a batch (the admission measure)."""

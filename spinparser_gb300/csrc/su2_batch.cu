@@ -18,7 +18,9 @@
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <utility>
 #include <vector>
 #include "su2_common.cuh"
 #include "su2_device.cuh"
@@ -32,10 +34,12 @@ namespace {
 
 constexpr int kClasses = 3;  // measurement classes: sites per lane 1, 2, 4
 constexpr int kBatchSchedMaxInts = 3072;  // per-warp staged RPA schedule (12 KB) at most
+constexpr int kGroupClasses = 4;  // grouped vertex classes: vertex classes 0..3
+constexpr int kCounters = kVertexClasses + kGroupClasses;
 
 __global__ void batch_prepare_kernel(BatchFlow *flows, const int *list, int n, int *counters) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < kVertexClasses && blockIdx.x == 0) counters[i] = 0;
+    if (i < kCounters && blockIdx.x == 0) counters[i] = 0;
     if (i >= n) return;
     BatchFlow &f = flows[list[i]];
     if (f.phase != kPhaseDone) *f.a.status = 0u;
@@ -154,13 +158,23 @@ struct spn_batch {
         spn_su2 *h = nullptr;
         float *cutoffs = nullptr, *hist = nullptr;
         std::vector<float> host_cutoffs;
+        // what the vertex flow of flows in one group must share: mesh, lattice tables, spin
+        // length and cutoff list (the bytes of each, in a fixed order)
+        std::vector<unsigned char> share_key;
+        int share_id = -1;
         int n_cutoffs = 0, step = 0, phase = kPhaseDone;
         unsigned flags = 0;
         bool used = false;
+        bool paused = false;  // held out of the steps (keeps its state and phase)
         size_t hist_row = 0;
     };
     int device = 0, sms = 0, npi = 1;
     bool use_graph = true;
+    // grouped vertex flow: groups of at least min_group flows (0 = off) share node supports,
+    // in subgroups of at most gmax / group_cap_div flows per CTA
+    int min_group = 2, group_cap_div = 1;
+    bool stage_sched = false;  // per-flow kernel: each warp stages its flow's RPA schedule in shared memory
+    int next_share_id = 0;
     cudaStream_t stream = nullptr;
     std::vector<Flow> flows;
     BatchFlow *d_flows = nullptr;
@@ -179,6 +193,10 @@ struct spn_batch {
     // per vertex class (vertex_class): work lists, prefixes, shared memory, grid
     int off_cv[kVertexClasses] = {}, n_cv[kVertexClasses] = {}, off_cp[kVertexClasses] = {}, total_cv[kVertexClasses] = {};
     int warp_area[kVertexClasses] = {}, nl_max = 1, vgrid[kVertexClasses] = {}, sched_ints[kVertexClasses] = {};
+    // per grouped class: subgroup member table, item prefix, grid
+    int off_gm[kGroupClasses] = {}, off_gp[kGroupClasses] = {}, n_sg[kGroupClasses] = {}, total_g[kGroupClasses] = {};
+    int nseg_g[kGroupClasses] = {}, ggrid[kGroupClasses] = {};
+    int n_grouped = 0;  // flows evaluated by the grouped kernel in the current plan
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     long long steps_run = 0, graph_builds = 0;
@@ -268,9 +286,10 @@ struct spn_batch {
         n_max = 2;
         nl_max = 1;
         std::vector<int> flowing, measure, cm[kClasses], cv[kVertexClasses];
+        std::map<std::pair<int, int>, std::vector<int>> buckets;  // (share id, step) -> flows
         for (size_t i = 0; i < flows.size(); ++i) {
             const Flow &f = flows[i];
-            if (!f.used || f.phase == kPhaseDone) continue;
+            if (!f.used || f.phase == kPhaseDone || f.paused) continue;
             const int c = class_of(f.h->nl);
             measure.push_back(int(i));
             cm[c].push_back(int(i));
@@ -279,7 +298,40 @@ struct spn_batch {
             nl_max = std::max(nl_max, f.h->nl);
             if (f.phase == kPhaseFlowing) {
                 flowing.push_back(int(i));
-                cv[vc].push_back(int(i));
+                if (min_group > 0 && vc < kGroupClasses && group_vertex_eligible(f.h->nl))
+                    buckets[{f.share_id, f.step}].push_back(int(i));
+                else
+                    cv[vc].push_back(int(i));
+            }
+        }
+        // groups large enough go to the grouped kernel in balanced subgroups of at most
+        // gmax / group_cap_div flows; the rest to the per-flow kernel
+        std::vector<int> gm[kGroupClasses], gp[kGroupClasses];
+        n_grouped = 0;
+        for (int c = 0; c < kGroupClasses; ++c) {
+            gp[c].assign(1, 0);
+            nseg_g[c] = 0;
+        }
+        for (auto &kv : buckets) {
+            const std::vector<int> &v = kv.second;
+            const int vc = vertex_class(flows[v[0]].h->nl);
+            if (int(v.size()) < min_group) {
+                cv[vc].insert(cv[vc].end(), v.begin(), v.end());
+                continue;
+            }
+            const int gmax = group_vertex_gmax(vc);
+            const int cap = std::max(1, gmax / group_cap_div);
+            const int parts = (int(v.size()) + cap - 1) / cap;
+            size_t at = 0;
+            for (int q = 0; q < parts; ++q) {
+                const size_t take = (v.size() - at) / size_t(parts - q);  // balanced sizes
+                for (int m = 0; m < gmax; ++m) gm[vc].push_back(m < int(take) ? v[at + m] : -1);
+                const long long next = gp[vc].back() + flows[v[at]].h->fn;
+                if (next >= (1ll << 31)) throw Error(ErrorType::Unsupported, "batch work list beyond 2^31 items");
+                gp[vc].push_back(int(next));
+                for (size_t m = 0; m < take; ++m) nseg_g[vc] = std::max(nseg_g[vc], flows[v[at + m]].h->rpa_n_seg);
+                at += take;
+                n_grouped += int(take);
             }
         }
         auto put = [&](const std::vector<int> &v) {
@@ -313,7 +365,7 @@ struct spn_batch {
             total_cv[c] = prefix.back();
             warp_area[c] = int((area + 15) / 16 * 16);
             // each warp stages its flow's RPA schedule when the largest one is small
-            sched_ints[c] = sched <= kBatchSchedMaxInts ? sched : 0;
+            sched_ints[c] = (stage_sched && sched <= kBatchSchedMaxInts) ? sched : 0;
             vgrid[c] = 0;
             if (n_cv[c] > 0) {
                 const size_t smem = batch_vertex_smem_bytes(n_max, warp_area[c], sched_ints[c]);
@@ -321,6 +373,19 @@ struct spn_batch {
                 cudaGetLastError();
                 if (per_sm < 1) throw Error(ErrorType::Unsupported, "batched vertex-flow kernel does not fit for this batch");
                 vgrid[c] = sms * per_sm;
+            }
+        }
+        for (int c = 0; c < kGroupClasses; ++c) {
+            off_gm[c] = put(gm[c]);
+            off_gp[c] = put(gp[c]);
+            n_sg[c] = int(gp[c].size()) - 1;
+            total_g[c] = gp[c].back();
+            ggrid[c] = 0;
+            if (n_sg[c] > 0) {
+                const int per_sm = group_vertex_blocks_per_sm(c, nseg_g[c]);
+                cudaGetLastError();
+                if (per_sm < 1) throw Error(ErrorType::Unsupported, "grouped vertex-flow kernel does not fit for this batch");
+                ggrid[c] = sms * per_sm;
             }
         }
         ensure_lists(lists.size());
@@ -340,13 +405,27 @@ struct spn_batch {
         plan_valid = true;
     }
 
+    // A step: enqueue_front (status and counters cleared, self-energy flow, node tables),
+    // enqueue_vertex (the vertex flow), enqueue_back (measurement, Euler, advance).
     void enqueue_step() {
+        enqueue_front();
+        enqueue_vertex();
+        enqueue_back();
+    }
+
+    void enqueue_front() {
         const int *L = d_lists;
-        batch_prepare_kernel<<<(std::max(n_measure, kVertexClasses) + 127) / 128, 128, 0, stream>>>(d_flows, L + off_measure, n_measure,
-                                                                                             d_counters);
+        batch_prepare_kernel<<<(std::max(n_measure, kCounters) + 127) / 128, 128, 0, stream>>>(d_flows, L + off_measure,
+                                                                                               n_measure, d_counters);
         if (n_flowing > 0) {
             batch_self_energy_kernel<<<dim3(n_max, n_flowing), 128, 0, stream>>>(d_flows, L + off_flowing);
             batch_node_table_kernel<<<dim3((n_max + 63) / 64, n_flowing), 64, 0, stream>>>(d_flows, L + off_flowing);
+        }
+    }
+
+    void enqueue_vertex() {
+        const int *L = d_lists;
+        if (n_flowing > 0) {
             for (int c = 0; c < kVertexClasses; ++c) {
                 if (n_cv[c] == 0) continue;
                 BatchVertexArgs b;
@@ -361,7 +440,24 @@ struct spn_batch {
                 b.sched_ints = sched_ints[c];
                 launch_batch_vertex(b, c, npi, vgrid[c], stream);
             }
+            for (int c = 0; c < kGroupClasses; ++c) {
+                if (n_sg[c] == 0) continue;
+                GroupVertexArgs g;
+                g.flows = d_flows;
+                g.members = L + off_gm[c];
+                g.prefix = L + off_gp[c];
+                g.n_sg = n_sg[c];
+                g.total = total_g[c];
+                g.gmax = group_vertex_gmax(c);
+                g.counter = d_counters + kVertexClasses + c;
+                g.n_seg_max = nseg_g[c];
+                launch_group_vertex(g, c, ggrid[c], stream);
+            }
         }
+    }
+
+    void enqueue_back() {
+        const int *L = d_lists;
         for (int c = 0; c < kClasses; ++c) {
             if (n_cm[c] == 0) continue;
             const dim3 g(2 * n_max + 4, n_cm[c]);
@@ -378,6 +474,33 @@ struct spn_batch {
 };
 
 namespace {
+
+// The bytes that decide whether two flows' vertex flows can share node supports: frequency
+// mesh, lattice tables, spin length and cutoff list (equal keys = equal inputs of every
+// support and of the RPA schedule).
+std::vector<unsigned char> share_key_of(const spn_su2_desc *d, int n_cutoffs, const float *cutoffs) {
+    std::vector<unsigned char> k;
+    auto put = [&](const void *p, size_t bytes) {
+        const unsigned char *c = static_cast<const unsigned char *>(p);
+        k.insert(k.end(), c, c + bytes);
+    };
+    const int nov = d->overlap_ptr ? d->overlap_ptr[d->n_sites] : 0;
+    put(&d->n_freq, sizeof(int));
+    put(&d->n_sites, sizeof(int));
+    put(&nov, sizeof(int));
+    put(&n_cutoffs, sizeof(int));
+    put(&d->spin_length, sizeof(float));
+    put(d->freq, sizeof(float) * d->n_freq);
+    put(d->sites_rid, sizeof(int) * d->n_sites);
+    put(d->inv_sites_rid, sizeof(int) * d->n_sites);
+    if (d->overlap_ptr) {
+        put(d->overlap_ptr, sizeof(int) * (d->n_sites + 1));
+        put(d->overlap_rid1, sizeof(int) * nov);
+        put(d->overlap_rid2, sizeof(int) * nov);
+    }
+    put(cutoffs, sizeof(float) * n_cutoffs);
+    return k;
+}
 
 size_t footprint_bytes(const spn_su2_desc *d, int n_cutoffs) {
     const size_t n = size_t(d->n_freq), nl = size_t(d->n_sites);
@@ -403,7 +526,7 @@ extern "C" int spn_batch_create(int device, spn_batch **out) {
         cuda_check(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device), "device attribute");
         cuda_check(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
         cuda_check(cudaEventCreateWithFlags(&b->status_ev, cudaEventDisableTiming), "cudaEventCreate");
-        b->d_counters = dalloc<int>(kVertexClasses, "alloc batch counters");
+        b->d_counters = dalloc<int>(kCounters, "alloc batch counters");
         b->ensure_capacity(16);
         *out = b.release();
     });
@@ -420,6 +543,18 @@ extern "C" int spn_batch_set_variant(spn_batch *b, int npi, int use_graph) {
         if (npi != 1 && npi != 2) throw Error(ErrorType::Argument, "nodes per iteration must be 1 or 2");
         b->npi = npi;
         b->use_graph = use_graph != 0;
+        b->plan_valid = false;
+    });
+}
+
+extern "C" int spn_batch_set_grouping(spn_batch *b, int min_group, int cap_divisor) {
+    return guarded([&] {
+        if (!b) throw Error(ErrorType::Argument, "null handle");
+        if (min_group < 0 || min_group == 1) throw Error(ErrorType::Argument, "min_group must be 0 (off) or >= 2");
+        if (cap_divisor != 1 && cap_divisor != 2 && cap_divisor != 4)
+            throw Error(ErrorType::Argument, "cap_divisor must be 1, 2 or 4");
+        b->min_group = min_group;
+        b->group_cap_div = cap_divisor;
         b->plan_valid = false;
     });
 }
@@ -455,6 +590,14 @@ extern "C" int spn_batch_add(spn_batch *b, const spn_su2_desc *desc, int n_cutof
         b->ensure_capacity(slot + 1);
         spn_batch::Flow &f = b->flows[slot];
         try {
+            f.share_key = share_key_of(desc, n_cutoffs, cutoffs);
+            f.share_id = -1;
+            for (const auto &o : b->flows)
+                if (&o != &f && o.used && o.share_key == f.share_key) {
+                    f.share_id = o.share_id;
+                    break;
+                }
+            if (f.share_id < 0) f.share_id = b->next_share_id++;
             f.h = create_flow(desc, b->stream);
             f.n_cutoffs = n_cutoffs;
             f.host_cutoffs.assign(cutoffs, cutoffs + n_cutoffs);
@@ -517,7 +660,7 @@ extern "C" int spn_batch_step(spn_batch *b, int *n_active) {
             ++b->steps_run;
             // the host's view of every flow advances the same way the advance kernel does
             for (auto &f : b->flows) {
-                if (!f.used) continue;
+                if (!f.used || f.paused) continue;
                 if (f.phase == kPhaseFinal) {
                     f.phase = kPhaseDone;
                     b->plan_valid = false;
@@ -632,6 +775,99 @@ extern "C" int spn_batch_remove(spn_batch *b, int flow_id) {
         r.phase = kPhaseDone;
         cuda_check(cudaMemcpy(b->d_flows + flow_id, &r, sizeof(r), cudaMemcpyHostToDevice), "H2D record");
         b->plan_valid = false;
+    });
+}
+
+// Times the vertex flow of the batch's current flows under each candidate configuration and
+// keeps the fastest: nodes per group iteration of the per-flow kernel (1, 2) x its RPA schedule
+// (read from global memory, staged per warp in shared memory: more shared memory, fewer
+// resident blocks) without sharing, and (1, 2) x cross-flow sharing in subgroups of the
+// grouped kernel's full block or of half of it.  The front of a
+// step runs once first (self-energy flow and node tables of the current states); the timed
+// launches write only the flows' vertex-flow buffers, which hold nothing between steps, so
+// no flow's state or results change.  It replaces the reference LoadManager's choice of chunk
+// sizes (src/lib/LoadManager.hpp:796-852) for the batch.
+extern "C" int spn_batch_autotune(spn_batch *b, int reps, int *npi, int *min_group, int *cap_divisor, float *best_ms) {
+    return guarded([&] {
+        if (!b || reps < 1) throw Error(ErrorType::Argument, "spn_batch_autotune: bad argument");
+        cuda_check(cudaSetDevice(b->device), "cudaSetDevice");
+        cuda_check(cudaStreamSynchronize(b->stream), "batch sync");
+        b->absorb_status(true);
+        struct Cand {
+            int npi, min_group, cap;
+            bool stage;
+        };
+        const Cand cands[] = {{1, 0, 1, false}, {2, 0, 1, false}, {1, 0, 1, true}, {2, 0, 1, true},
+                              {1, 2, 1, false}, {2, 2, 1, false}, {1, 2, 2, false}, {2, 2, 2, false}};
+        const Cand keep{b->npi, b->min_group, b->group_cap_div, b->stage_sched};
+        Cand best = keep;
+        float best_t = -1.0f;
+        cudaEvent_t e0, e1;
+        cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
+        cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
+        bool front_done = false;
+        for (const Cand &c : cands) {
+            b->npi = c.npi;
+            b->min_group = c.min_group;
+            b->group_cap_div = c.cap;
+            b->stage_sched = c.stage;
+            b->build_plan();
+            if (b->n_flowing == 0) break;
+            if (c.min_group > 0 && b->n_grouped == 0) continue;  // nothing to share
+            if (!front_done) {
+                b->enqueue_front();
+                front_done = true;
+            }
+            cuda_check(cudaMemsetAsync(b->d_counters, 0, kCounters * sizeof(int), b->stream), "memset");
+            b->enqueue_vertex();  // warm-up
+            cuda_check(cudaEventRecord(e0, b->stream), "record");
+            for (int r = 0; r < reps; ++r) {
+                cuda_check(cudaMemsetAsync(b->d_counters, 0, kCounters * sizeof(int), b->stream), "memset");
+                b->enqueue_vertex();
+            }
+            cuda_check(cudaEventRecord(e1, b->stream), "record");
+            cuda_check(cudaEventSynchronize(e1), "sync");
+            cuda_check(cudaGetLastError(), "autotune launch");
+            float ms = 0.0f;
+            cuda_check(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+            ms /= float(reps);
+            if (best_t < 0.0f || ms < best_t) {
+                best_t = ms;
+                best = c;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        b->npi = best.npi;
+        b->min_group = best.min_group;
+        b->group_cap_div = best.cap;
+        b->stage_sched = best.stage;
+        b->plan_valid = false;
+        if (npi) *npi = best.npi;
+        if (min_group) *min_group = best.min_group;
+        if (cap_divisor) *cap_divisor = best.cap;
+        if (best_ms) *best_ms = best_t;
+    });
+}
+
+extern "C" int spn_batch_set_paused(spn_batch *b, int flow_id, int paused) {
+    return guarded([&] {
+        if (!b || flow_id < 0 || flow_id >= int(b->flows.size()) || !b->flows[flow_id].used)
+            throw Error(ErrorType::Argument, "spn_batch_set_paused: unknown flow");
+        spn_batch::Flow &f = b->flows[flow_id];
+        if (f.paused != (paused != 0)) {
+            f.paused = paused != 0;
+            b->plan_valid = false;
+        }
+    });
+}
+
+extern "C" int spn_batch_grouped_flows(spn_batch *b, int *n_grouped) {
+    return guarded([&] {
+        if (!b || !n_grouped) throw Error(ErrorType::Argument, "null argument");
+        cuda_check(cudaSetDevice(b->device), "cudaSetDevice");
+        if (!b->plan_valid) b->build_plan();
+        *n_grouped = b->n_grouped;
     });
 }
 

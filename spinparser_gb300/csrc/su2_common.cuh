@@ -132,6 +132,23 @@ struct BatchVertexArgs {
     int warp_area;
     int sched_ints;
 };
+// Grouped batches (flows sharing mesh, lattice tables and cutoff; see su2_vertex.cu): one
+// persistent launch per vertex class 0..3 over (subgroup, triple) items.  A subgroup holds up
+// to group_vertex_gmax(cls) flows: members[sg * gmax + q] is the record index of member q, -1
+// after the last; its items are prefix[sg] .. prefix[sg + 1] - 1 (its flows' F_N triples).
+// n_seg_max: the largest RPA segment count of the flows in the launch.
+struct GroupVertexArgs {
+    BatchFlow *flows;
+    const int *members, *prefix;
+    int n_sg, total, gmax;
+    int *counter;
+    int n_seg_max;
+};
+bool group_vertex_eligible(int nl);  // 5 <= nl <= 32
+int group_vertex_gmax(int cls);
+size_t group_vertex_smem_bytes(int cls, int n_seg_max);
+int group_vertex_blocks_per_sm(int cls, int n_seg_max);
+void launch_group_vertex(const GroupVertexArgs &g, int cls, int grid, cudaStream_t stream);
 size_t batch_vertex_warp_area(int nl, int n_seg, int npi);
 size_t batch_vertex_smem_bytes(int n_max, size_t warp_area, int sched_ints);
 int batch_vertex_blocks_per_sm(int cls, int npi, size_t smem);

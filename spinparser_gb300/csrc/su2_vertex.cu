@@ -26,6 +26,7 @@
 // schedule with deterministic segment partials (no divergent per-rid loops).
 // Accumulation over nodes is Kahan-compensated FP32 for the local terms (the RPA matrix sums
 // are plain FP32); group partials are combined by shuffles.
+#include <type_traits>
 #include "su2_common.cuh"
 #include "su2_device.cuh"
 
@@ -119,10 +120,74 @@ __device__ __forceinline__ void make_desc(const FlowArgs &a, const float *pos, c
     d.c = c;
 }
 
+// Supports of the four site-local access buffers of a t-channel node (the values cbs ... icad2
+// of make_desc are local_pair of these with a flow's state).
+struct LocDesc {
+    int4 off[4];
+    float4 w[4];
+    float4 sw[4];
+};
+
+// Phase A for flows that share the mesh, the lattice tables and the cutoff (a grouped batch):
+// the node's supports only, as make_desc builds them (same access buffers, same arguments);
+// the coefficient and the t channel's site-local values are per flow (group_local_values).
+template <int CH>
+__device__ __forceinline__ void make_supports(const FlowArgs &a, const float *pos, const Transfer &f, float wp, NodeDesc &d,
+                                              LocDesc &loc) {
+    AB4 ab;
+    int exch = 0;
+    const int nl = a.nl;
+    const MeshIndex m{pos, a.n, a.mesh_lo, a.mesh_base, a.mesh_shift};
+    if (CH == kS) {
+        access4m<kS>(m, nl, f.s, -f.w1 - wp, -f.w2 - wp, ab, f.si); put_ab(d, 0, ab); exch |= ab.exch << 0;
+        access4m<kS>(m, nl, f.s, f.w1p + wp, -f.w2p - wp, ab, f.si); put_ab(d, 1, ab); exch |= ab.exch << 1;
+        access4m<kS>(m, nl, f.s, f.w2 + wp, f.w1 + wp, ab, f.si); put_ab(d, 2, ab); exch |= ab.exch << 2;
+        access4m<kS>(m, nl, f.s, -f.w2p - wp, f.w1p + wp, ab, f.si); put_ab(d, 3, ab); exch |= ab.exch << 3;
+    } else if (CH == kT) {
+        access4m<kT>(m, nl, f.w1 - wp, f.t, f.w1p + wp, ab, f.ti); put_ab(d, 0, ab); exch |= ab.exch << 0;
+        access4m<kT>(m, nl, f.w2p - wp, f.t, -f.w2 - wp, ab, f.ti); put_ab(d, 1, ab); exch |= ab.exch << 1;
+        access4m<kT>(m, nl, f.w1p + wp, f.t, f.w1 - wp, ab, f.ti); put_ab(d, 2, ab); exch |= ab.exch << 2;
+        access4m<kT>(m, nl, f.w2 + wp, f.t, wp - f.w2p, ab, f.ti); put_ab(d, 3, ab); exch |= ab.exch << 3;
+        auto put_loc = [&](int i) {
+            loc.off[i] = make_int4(ab.off[0], ab.off[1], ab.off[2], ab.off[3]);
+            loc.w[i] = make_float4(ab.w[0], ab.w[1], ab.w[2], ab.w[3]);
+            loc.sw[i] = make_float4(ab.sw[0], ab.sw[1], ab.sw[2], ab.sw[3]);
+        };
+        access4m<kU>(m, nl, f.w2p - wp, -f.w2 - wp, f.t, ab, f.ti); put_loc(0);
+        access4m<kU>(m, nl, f.w1 - wp, -f.w1p - wp, -f.t, ab, f.ti); put_loc(1);
+        access4m<kU>(m, nl, f.w2 + wp, wp - f.w2p, f.t, ab, f.ti); put_loc(2);
+        access4m<kU>(m, nl, f.w1p + wp, wp - f.w1, -f.t, ab, f.ti); put_loc(3);
+    } else {
+        access4m<kU>(m, nl, f.w1 + wp, wp - f.w2p, f.u, ab, f.ui); put_ab(d, 0, ab); exch |= ab.exch << 0;
+        access4m<kU>(m, nl, f.w1p + wp, f.w2 - wp, f.u, ab, f.ui); put_ab(d, 1, ab); exch |= ab.exch << 1;
+        access4m<kU>(m, nl, f.w2p - wp, -f.w1 - wp, f.u, ab, f.ui); put_ab(d, 2, ab); exch |= ab.exch << 2;
+        access4m<kU>(m, nl, f.w2 - wp, f.w1p + wp, f.u, ab, f.ui); put_ab(d, 3, ab); exch |= ab.exch << 3;
+    }
+    d.exch = exch;
+    d.c = 0.0f;
+}
+
+// The t channel's eight site-local values of one node for one flow's state (make_desc's
+// local_pair of each local buffer, in the same order).
+__device__ __forceinline__ void group_local_values(const float2 *sd, const LocDesc &loc, float *lv) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int4 o = loc.off[i];
+        const float4 w = loc.w[i], sw = loc.sw[i];
+        float2 g = make_float2(0.0f, 0.0f);
+        g = fma2(make_float2(w.x, sw.x), __ldg(sd + o.x), g);
+        g = fma2(make_float2(w.y, sw.y), __ldg(sd + o.y), g);
+        g = fma2(make_float2(w.z, sw.z), __ldg(sd + o.z), g);
+        g = fma2(make_float2(w.w, sw.w), __ldg(sd + o.w), g);
+        lv[2 * i] = g.x;
+        lv[2 * i + 1] = g.y;
+    }
+}
+
 // Phase B: interpolated slab of buffer i for this lane's sites (getValueSuperbundle): per
 // support one 64-bit load of the (spin, density) element and one packed FMA.
-template <int SPT>
-__device__ __forceinline__ void gather(const FlowArgs &a, const NodeDesc &d, int i, const Lane<SPT> &ln, float *vs,
+template <int SPT, class A>
+__device__ __forceinline__ void gather(const A &a, const NodeDesc &d, int i, const Lane<SPT> &ln, float *vs,
                                        float *vd) {
     const int4 o = d.off[i];
     const float4 p0 = d.ws[i][0], p1 = d.ws[i][1];
@@ -169,19 +234,29 @@ struct OuterAcc {
     float2 m[MB > 0 ? MB : 1][MB > 0 ? 2 * MB : 1];
 };
 
+// A node as one lane group sees it: the supports (descriptor) and the flow's own coefficient
+// and t-channel site-local values.  In a single flow both come from the descriptor; flows that
+// share a descriptor (grouped batches) each bring their own.
+struct NodeView {
+    const NodeDesc *d;
+    float c;
+    const float *lv;
+};
+
 // K_X at NPI nodes for this lane's sites (one group evaluates NPI nodes per iteration so that
-// the t channel decodes each RPA schedule entry once for all of them).
-template <int CH, int SPT, int NPI>
-__device__ __forceinline__ void node_term(const FlowArgs &a, const NodeDesc *const *d, const Lane<SPT> &ln, int jl,
+// the t channel decodes each RPA schedule entry once for all of them).  `a` provides the
+// state (a.sd), the spin length and, for SPT > 1, the RPA schedule.
+template <int CH, int SPT, int NPI, class A>
+__device__ __forceinline__ void node_term(const A &a, const NodeView *v, const Lane<SPT> &ln, int jl,
                                           const TExchange *tx, float (*rs)[SPT], float (*rd)[SPT]) {
     float S0[NPI][SPT], S1[NPI][SPT], S2[NPI][SPT], S3[NPI][SPT], D0[NPI][SPT], D1[NPI][SPT], D2[NPI][SPT],
         D3[NPI][SPT];
 #pragma unroll
     for (int n = 0; n < NPI; ++n) {
-        gather<SPT>(a, *d[n], 0, ln, S0[n], D0[n]);
-        gather<SPT>(a, *d[n], 1, ln, S1[n], D1[n]);
-        gather<SPT>(a, *d[n], 2, ln, S2[n], D2[n]);
-        gather<SPT>(a, *d[n], 3, ln, S3[n], D3[n]);
+        gather<SPT>(a, *v[n].d, 0, ln, S0[n], D0[n]);
+        gather<SPT>(a, *v[n].d, 1, ln, S1[n], D1[n]);
+        gather<SPT>(a, *v[n].d, 2, ln, S2[n], D2[n]);
+        gather<SPT>(a, *v[n].d, 3, ln, S3[n], D3[n]);
     }
     if (CH == kS || CH == kU) {
 #pragma unroll
@@ -214,14 +289,14 @@ __device__ __forceinline__ void node_term(const FlowArgs &a, const NodeDesc *con
         return;
     }
     // t channel: RPA lattice sum (SU2FrgCore.cpp:249-266)
-    if (SPT == 1) {
+    if constexpr (SPT == 1) {
         // outer-product form: the node's panel (c * third slab, fourth slab); channel_sum adds
         // the panels' outer products to the warp's M accumulators after the trip
         if (ln.valid[0]) {
             const int j = ln.j[0];
 #pragma unroll
             for (int n = 0; n < NPI; ++n) {
-                const float c = d[n]->c;
+                const float c = v[n].c;
                 tx[n].A2[j] = make_float2(c * S2[n][0], c * D2[n][0]);
                 tx[n].B2[j] = make_float2(S3[n][0], D3[n][0]);
             }
@@ -270,12 +345,12 @@ __device__ __forceinline__ void node_term(const FlowArgs &a, const NodeDesc *con
     const float s2 = 2.0f * a.spin, s8 = 8.0f * a.spin;
 #pragma unroll
     for (int n = 0; n < NPI; ++n) {
-        const float cbs = d[n]->lv[0], cbd = d[n]->lv[1], icas = d[n]->lv[2], icad = d[n]->lv[3];
-        const float cbs2 = d[n]->lv[4], cbd2 = d[n]->lv[5], icas2 = d[n]->lv[6], icad2 = d[n]->lv[7];
+        const float cbs = v[n].lv[0], cbd = v[n].lv[1], icas = v[n].lv[2], icad = v[n].lv[3];
+        const float cbs2 = v[n].lv[4], cbd2 = v[n].lv[5], icas2 = v[n].lv[6], icad2 = v[n].lv[7];
 #pragma unroll
         for (int k = 0; k < SPT; ++k) {
             float rpa_s = 0.0f, rpa_d = 0.0f;
-            if (SPT != 1 && ln.valid[k]) {  // Nl <= 32: the RPA term enters once per triple
+            if (SPT != 1 && ln.valid[k]) {  // Nl > 32 (for Nl <= 32 the RPA term enters once per triple)
                 const int r = ln.j[k];
                 const int s0 = tx[0].seg_ptr[r], s1 = tx[0].seg_ptr[r + 1];
                 for (int q = s0; q < s1; ++q) {
@@ -363,12 +438,15 @@ __device__ __forceinline__ void channel_sum(const FlowArgs &a, const float *pos,
                 active[n] = k < nb;
                 d[n] = &desc[active[n] ? k : 0];
             }
+            NodeView v[NPI];
+#pragma unroll
+            for (int n = 0; n < NPI; ++n) v[n] = NodeView{d[n], d[n]->c, d[n]->lv};
             float rs[NPI][SPT], rd[NPI][SPT];
-            node_term<CH, SPT, NPI>(a, d, ln, jl, tx, rs, rd);
+            node_term<CH, SPT, NPI>(a, v, ln, jl, tx, rs, rd);
 #pragma unroll
             for (int n = 0; n < NPI; ++n)
                 if (active[n]) {
-                    const float c = d[n]->c;
+                    const float c = v[n].c;
 #pragma unroll
                     for (int q = 0; q < SPT; ++q) {
                         kahan_add(acc_s[q], cmp_s[q], c * rs[n][q]);
@@ -747,6 +825,331 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_batch_kernel(BatchVertexA
     }
 }
 
+// ------------------------------------------------------------------------------------
+// Grouped batches: flows that share the frequency mesh, the lattice tables and the current
+// cutoff (a parameter scan's members of one lattice, range and frequency count, started
+// together) have the same loop-frequency node positions and the same interpolation supports
+// for every (triple, node); only the state, the node coefficients (through the self-energy)
+// and the t channel's site-local values differ.  A CTA takes one triple for a subgroup of up to
+// kGroupWarps * 32 / W flows: its threads build each node's supports once, in chunks of 32
+// nodes, and every warp evaluates them for 32 / W flows at once, lane = (flow, site).
+//
+// The result of every flow is the single-flow kernel's, bit for bit: a flow's W lanes keep the
+// single-flow kernel's G = 32 / W Kahan accumulator pairs (node k of a channel adds into pair
+// k mod G, the RPA term into pair 0 after the t channel) and combine them in its order, and
+// the outer-product matrix M adds the nodes' panels in ascending order.  The pair walk follows
+// the same 32-chunk schedule, each of the flow's W lanes walking chunks l, l + W, ...
+// ------------------------------------------------------------------------------------
+constexpr int kGroupWarps = 4;
+constexpr int kGroupChunk = 32;  // nodes whose supports the CTA builds at once
+
+// What a lane of a grouped warp needs of its flow (node_term reads a.sd and a.spin).
+struct GroupLaneArgs {
+    const float2 *sd;
+    float spin;
+};
+
+__host__ __device__ constexpr int group_cb(int W) { return W == 8 ? 2 : 4; }
+
+// Adds the outer product of the flow's panel (A2 = c * third slab, B2 = fourth slab; w entries
+// each) to the lane's R x C block of M; the flow's W lanes form a (W / Cb) x Cb grid.
+template <int W, int MB>
+__device__ __forceinline__ void group_outer_update(const float2 *pan, int jl, float2 (*m)[8 * MB / group_cb(W)]) {
+    constexpr int w = 8 * MB, Cb = group_cb(W), Rb = W / Cb, R = w / Rb, C = w / Cb;
+    const int rb = jl / Cb, cb = jl % Cb;
+    float2 av[R], bv[C];
+#pragma unroll
+    for (int i = 0; i < R; ++i) av[i] = pan[rb * R + i];
+#pragma unroll
+    for (int j = 0; j < C; ++j) bv[j] = pan[w + cb * C + j];
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+#pragma unroll
+        for (int j = 0; j < C; ++j) m[i][j] = fma2(av[i], bv[j], m[i][j]);
+}
+
+template <int W, int MB>
+struct GroupShape {
+    static constexpr int F = 32 / W;                 // flows per warp
+    static constexpr int GMAX = kGroupWarps * F;     // flows per CTA
+    static constexpr int G = 32 / W;                 // single-flow node groups (accumulator pairs)
+    static constexpr int w = 8 * MB;                 // outer-product width
+    static constexpr int Cb = group_cb(W), R = w / (W / Cb), C = w / Cb;
+};
+
+// Shared-memory layout of the grouped kernel (bytes from the dynamic base, all 16-aligned).
+struct GroupSmem {
+    size_t fa, ptrs, pos, build_desc, build_loc, build_c, build_lv, stage, panels, total;
+};
+__host__ __device__ inline GroupSmem group_smem_layout(int W, int MB, int n_seg_max) {
+    const int F = 32 / W, GMAX = kGroupWarps * F, w = 8 * MB;
+    GroupSmem L;
+    size_t o = 0;
+    L.fa = o; o += align16(sizeof(FlowArgs));
+    L.ptrs = o; o += align16(size_t(GMAX) * (2 * sizeof(void *) + sizeof(void *) + sizeof(void *) + sizeof(int)));
+    L.pos = o; o += align16(sizeof(float) * kMaxFreq);
+    // union: the chunk build area, or (after the t channel) each flow's staged M and slots
+    const size_t u0 = o;
+    L.build_desc = o; o += kGroupChunk * sizeof(NodeDesc);
+    L.build_loc = o; o += kGroupChunk * sizeof(LocDesc);
+    L.build_c = o; o += align16(sizeof(float) * kGroupChunk * GMAX);
+    L.build_lv = o; o += align16(sizeof(float) * 8 * kGroupChunk * GMAX);
+    const size_t build_end = o;
+    L.stage = u0;
+    const size_t stage_end = u0 + align16(sizeof(float2) * size_t(GMAX) * (size_t(w) * w + n_seg_max));
+    o = build_end > stage_end ? build_end : stage_end;
+    L.panels = o; o += align16(sizeof(float2) * size_t(GMAX) * 2 * w);
+    L.total = o;
+    return L;
+}
+
+template <int W, int MB>
+__global__ void __launch_bounds__(kGroupWarps * 32) su2_vertex_group_kernel(GroupVertexArgs g) {
+    using S = GroupShape<W, MB>;
+    constexpr int F = S::F, GMAX = S::GMAX, G = S::G, w = S::w, R = S::R, C = S::C;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_item;
+    const GroupSmem L = group_smem_layout(W, MB, g.n_seg_max);
+    FlowArgs *fa = reinterpret_cast<FlowArgs *>(smem_raw + L.fa);
+    unsigned char *pb = smem_raw + L.ptrs;
+    const float2 **m_sd = reinterpret_cast<const float2 **>(pb);
+    float2 **m_dsd = reinterpret_cast<float2 **>(pb + GMAX * sizeof(void *));
+    const float **m_nc = reinterpret_cast<const float **>(pb + 2 * GMAX * sizeof(void *));
+    unsigned **m_status = reinterpret_cast<unsigned **>(pb + 3 * GMAX * sizeof(void *));
+    int *m_on = reinterpret_cast<int *>(pb + 4 * GMAX * sizeof(void *));  // member flowing this step
+    float *pos = reinterpret_cast<float *>(smem_raw + L.pos);
+    NodeDesc *desc = reinterpret_cast<NodeDesc *>(smem_raw + L.build_desc);
+    LocDesc *loc = reinterpret_cast<LocDesc *>(smem_raw + L.build_loc);
+    float *ctab = reinterpret_cast<float *>(smem_raw + L.build_c);   // [node][member]
+    float *lvtab = reinterpret_cast<float *>(smem_raw + L.build_lv);  // [node][member][8]
+    float2 *stage = reinterpret_cast<float2 *>(smem_raw + L.stage);
+    float2 *panels = reinterpret_cast<float2 *>(smem_raw + L.panels);
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int gg = lane / W, jl = lane - gg * W;  // flow slot in the warp, site
+    const int fs = warp * F + gg;                 // member index in the subgroup
+    float2 *pan = panels + size_t(fs) * 2 * w;
+    // panel entries of sites >= Nl are never written and stay zero
+    for (int i = tid; i < GMAX * 2 * w; i += blockDim.x) panels[i] = make_float2(0.0f, 0.0f);
+
+    int cur = -1, base = 0, nf = 0;
+    bool live = false;
+    for (;;) {
+        __syncthreads();  // the previous item is finished with the shared areas
+        if (tid == 0) s_item = atomicAdd(g.counter, 1);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= g.total) break;
+        int lo = 0, hi = g.n_sg - 1;  // last subgroup with prefix <= item
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(g.prefix + mid) <= item) lo = mid;
+            else hi = mid - 1;
+        }
+        if (lo != cur) {
+            cur = lo;
+            base = __ldg(g.prefix + lo);
+            // leader: the first member that is flowing this step (its node tables are current)
+            int lead = -1, cnt = 0;
+            for (int q = 0; q < GMAX; ++q) {
+                const int fi = __ldg(g.members + size_t(lo) * GMAX + q);
+                if (fi < 0) break;
+                ++cnt;
+                if (lead < 0 && g.flows[fi].phase == kPhaseFlowing) lead = fi;
+            }
+            nf = cnt;
+            live = lead >= 0;
+            if (live) {
+                const BatchFlow *lf = g.flows + lead;
+                const int *src = reinterpret_cast<const int *>(&lf->a);
+                int *dst = reinterpret_cast<int *>(fa);
+                for (int i = tid; i < int(sizeof(FlowArgs) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+                if (tid < GMAX) {
+                    const int fi = tid < cnt ? __ldg(g.members + size_t(lo) * GMAX + tid) : -1;
+                    const bool on = fi >= 0 && g.flows[fi].phase == kPhaseFlowing;
+                    const BatchFlow *bf = g.flows + (on ? fi : lead);  // idle slots read the leader's data
+                    m_sd[tid] = bf->a.sd;
+                    m_dsd[tid] = bf->a.dsd;
+                    m_nc[tid] = bf->a.node_c;
+                    m_status[tid] = bf->a.status;
+                    m_on[tid] = on ? 1 : 0;
+                }
+            }
+            __syncthreads();
+            if (live)
+                for (int i = tid; i < fa->n; i += blockDim.x) pos[i] = fa->freq[i];
+            __syncthreads();
+        }
+        if (!live) continue;
+        const int it = item - base;
+        const FlowArgs &a = *fa;
+
+        // the triple (as vertex_triple decodes it)
+        const int su = it / a.n, ti = it - su * a.n;
+        int si = int((sqrtf(8.0f * float(su) + 1.0f) - 1.0f) * 0.5f);
+        while (si * (si + 1) / 2 > su) --si;
+        while ((si + 1) * (si + 2) / 2 <= su) ++si;
+        const int ui = su - si * (si + 1) / 2;
+        Transfer f;
+        f.s = pos[si];
+        f.t = pos[ti];
+        f.u = pos[ui];
+        f.w1p = 0.5f * (f.s + f.t + f.u);
+        f.w1 = 0.5f * (f.s - f.t + f.u);
+        f.w2p = 0.5f * (f.s - f.t - f.u);
+        f.w2 = 0.5f * (f.s + f.t - f.u);
+        f.si = si;
+        f.ti = ti;
+        f.ui = ui;
+
+        const bool mine = fs < nf && m_on[fs];
+        const GroupLaneArgs la{m_sd[fs < nf ? fs : 0], a.spin};
+        Lane<1> ln;
+        ln.j[0] = jl;
+        ln.valid[0] = jl < a.nl;
+        ln.site[0] = ln.valid[0] ? a.sites[jl] : 0;
+        ln.isite[0] = ln.valid[0] ? a.inv_sites[jl] : 0;
+        TExchange tx;
+        tx.A2 = pan;
+        tx.B2 = pan + w;
+
+        float acc_s[G], cmp_s[G], acc_d[G], cmp_d[G];
+#pragma unroll
+        for (int q = 0; q < G; ++q) acc_s[q] = cmp_s[q] = acc_d[q] = cmp_d[q] = 0.0f;
+        float2 M[R][C];
+#pragma unroll
+        for (int i = 0; i < R; ++i)
+#pragma unroll
+            for (int j = 0; j < C; ++j) M[i][j] = make_float2(0.0f, 0.0f);
+
+        // node k of a channel adds into pair k mod G: the pairs rotate after every node, and
+        // pair 0 is realigned at the end of each channel
+        auto rotate = [&]() {
+#pragma unroll
+            for (int q = 0; q + 1 < G; ++q) {
+                float t;
+                t = acc_s[q]; acc_s[q] = acc_s[q + 1]; acc_s[q + 1] = t;
+                t = cmp_s[q]; cmp_s[q] = cmp_s[q + 1]; cmp_s[q + 1] = t;
+                t = acc_d[q]; acc_d[q] = acc_d[q + 1]; acc_d[q + 1] = t;
+                t = cmp_d[q]; cmp_d[q] = cmp_d[q + 1]; cmp_d[q + 1] = t;
+            }
+        };
+
+        auto channel = [&](auto chc, int xi) {
+            constexpr int CH = decltype(chc)::value;
+            const int cnt = __ldg(a.node_cnt + xi);
+            const float *nwp = a.node_wp + size_t(xi) * a.max_nodes;
+            for (int b0 = 0; b0 < cnt; b0 += kGroupChunk) {
+                const int nb = min(kGroupChunk, cnt - b0);
+                __syncthreads();  // the previous chunk is consumed
+                if (warp == 0) {
+                    if (lane < nb) make_supports<CH>(a, pos, f, __ldg(nwp + b0 + lane), desc[lane], loc[lane]);
+                } else {
+                    for (int p = tid - 32; p < nb * GMAX; p += blockDim.x - 32) {
+                        const int k = p / GMAX, q = p - k * GMAX;
+                        float c = __ldg(m_nc[q] + size_t(xi) * a.max_nodes + b0 + k);
+                        if (CH == kU) c = -c;
+                        ctab[p] = c;
+                    }
+                }
+                __syncthreads();
+                if constexpr (CH == kT) {
+                    for (int p = tid; p < nb * GMAX; p += blockDim.x) {
+                        const int k = p / GMAX, q = p - k * GMAX;
+                        group_local_values(m_sd[q], loc[k], lvtab + size_t(p) * 8);
+                    }
+                    __syncthreads();
+                }
+                for (int k = 0; k < nb; ++k) {
+                    const int p = k * GMAX + fs;
+                    NodeView v{&desc[k], ctab[p], lvtab + size_t(p) * 8};
+                    float rs[1][1], rd[1][1];
+                    node_term<CH, 1, 1>(la, &v, ln, jl, &tx, rs, rd);
+                    kahan_add(acc_s[0], cmp_s[0], v.c * rs[0][0]);
+                    kahan_add(acc_d[0], cmp_d[0], v.c * rd[0][0]);
+                    rotate();
+                    if constexpr (CH == kT) {
+                        __syncwarp();  // panel written
+                        group_outer_update<W, MB>(pan, jl, M);
+                        __syncwarp();  // panel read
+                    }
+                }
+            }
+            // realign: pair 0 holds residue 0 again
+            const int extra = (G - cnt % G) % G;
+            for (int r = 0; r < extra; ++r) rotate();
+        };
+
+        channel(std::integral_constant<int, kS>{}, si);
+        channel(std::integral_constant<int, kT>{}, ti);
+
+        // RPA term: stage each flow's M, walk the 32-chunk schedule (chunks jl, jl + W, ...)
+        __syncthreads();  // the build area is free
+        {
+            float2 *Ms = stage + size_t(fs) * (size_t(w) * w + g.n_seg_max);
+            float2 *slots = Ms + w * w;
+            const int rb = jl / S::Cb, cb = jl % S::Cb;
+#pragma unroll
+            for (int i = 0; i < R; ++i)
+#pragma unroll
+                for (int j = 0; j < C; ++j) Ms[(rb * R + i) * w + cb * C + j] = M[i][j];
+            __syncwarp();
+            const int lanes = a.rpa.lanes;
+            const char *mb = reinterpret_cast<const char *>(Ms);
+            for (int ch = jl; ch < lanes; ch += W) {
+                const int cntq = __ldg(a.rpa.count + ch);
+                int slot = __ldg(a.rpa.slot_base + ch);
+                const int *sched = a.rpa.sched + ch;
+                float2 acc = make_float2(0.0f, 0.0f);
+                for (int i = 0; i < cntq; ++i) {
+                    const int e = __ldg(sched + size_t(i) * lanes);
+                    const float2 v = *reinterpret_cast<const float2 *>(mb + (e & 0xffff));
+                    const float m = float((e >> 16) & 0xff);
+                    acc = fma2(make_float2(m, m), v, acc);
+                    if (e < 0) {
+                        slots[slot++] = acc;
+                        acc = make_float2(0.0f, 0.0f);
+                    }
+                }
+            }
+            __syncwarp();
+            if (ln.valid[0]) {
+                float os = 0.0f, od = 0.0f;
+                for (int q = __ldg(a.rpa.seg_ptr + jl); q < __ldg(a.rpa.seg_ptr + jl + 1); ++q) {
+                    const float2 p = slots[q];
+                    os += p.x;
+                    od += p.y;
+                }
+                kahan_add(acc_s[0], cmp_s[0], (2.0f * a.spin) * os);  // SU2FrgCore.cpp:265-266
+                kahan_add(acc_d[0], cmp_d[0], (8.0f * a.spin) * od);
+            }
+        }
+        channel(std::integral_constant<int, kU>{}, ui);
+
+        // the single-flow kernel's combination of its groups: xor-shuffle order
+        float vs[G], vd[G];
+#pragma unroll
+        for (int q = 0; q < G; ++q) {
+            vs[q] = acc_s[q] - cmp_s[q];
+            vd[q] = acc_d[q] - cmp_d[q];
+        }
+        float ts = vs[0], td = vd[0];
+        if constexpr (G == 2) {
+            ts = vs[0] + vs[1];
+            td = vd[0] + vd[1];
+        } else if constexpr (G == 4) {
+            ts = (vs[0] + vs[1]) + (vs[2] + vs[3]);
+            td = (vd[0] + vd[1]) + (vd[2] + vd[3]);
+        }
+        if (mine && ln.valid[0]) {
+            const float two_pi = 2.0f * float(kPi);
+            const float os = ts / two_pi, od = td / two_pi;
+            m_dsd[fs][size_t(it) * a.nl + jl] = make_float2(os, od);
+            if (isnan(os) || isnan(od)) atomicOr(m_status[fs], kStatusNaN);
+        }
+    }
+}
+
 int spt_of(int nl) { return nl <= 32 ? 1 : (nl <= 64 ? 2 : 4); }
 
 int wsite_of(int nl) {
@@ -849,6 +1252,42 @@ int batch_vertex_blocks_per_sm(int cls, int npi, size_t smem) {
 void launch_batch_vertex(const BatchVertexArgs &b, int cls, int npi, int grid, cudaStream_t stream) {
     const size_t smem = batch_vertex_smem_bytes(b.n_max, size_t(b.warp_area), b.sched_ints);
     batch_kernel(cls, npi)<<<grid, kThreads, smem, stream>>>(b);
+}
+
+namespace {
+using GroupKernel = void (*)(GroupVertexArgs);
+GroupKernel group_kernel(int cls) {
+    switch (cls) {
+        case 0: return su2_vertex_group_kernel<8, 1>;
+        case 1: return su2_vertex_group_kernel<16, 2>;
+        case 2: return su2_vertex_group_kernel<32, 3>;
+        default: return su2_vertex_group_kernel<32, 4>;
+    }
+}
+int group_w(int cls) { return cls == 0 ? 8 : (cls == 1 ? 16 : 32); }
+}  // namespace
+
+bool group_vertex_eligible(int nl) { return nl >= 5 && nl <= 32; }
+
+int group_vertex_gmax(int cls) { return kGroupWarps * (32 / group_w(cls)); }
+
+size_t group_vertex_smem_bytes(int cls, int n_seg_max) {
+    return group_smem_layout(group_w(cls), cls + 1, n_seg_max).total;
+}
+
+int group_vertex_blocks_per_sm(int cls, int n_seg_max) {
+    GroupKernel k = group_kernel(cls);
+    const size_t smem = group_vertex_smem_bytes(cls, n_seg_max);
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess) return -1;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kGroupWarps * 32, smem) != cudaSuccess) return -1;
+    return per_sm;
+}
+
+// The shared-memory limit is raised by group_vertex_blocks_per_sm when the plan is built, so
+// this launch can be captured into a graph.
+void launch_group_vertex(const GroupVertexArgs &g, int cls, int grid, cudaStream_t stream) {
+    group_kernel(cls)<<<grid, kGroupWarps * 32, group_vertex_smem_bytes(cls, g.n_seg_max), stream>>>(g);
 }
 
 }  // namespace spn

@@ -44,3 +44,37 @@ def aggregate(local_units: float, local_seconds: float, group=None) -> JobTiming
     dist.all_reduce(units, op=dist.ReduceOp.SUM, group=group)
     dist.all_reduce(secs, op=dist.ReduceOp.MAX, group=group)
     return JobTiming(float(units.item()), float(secs.item()), dist.get_world_size(group))
+
+
+def _rank_world(group=None) -> tuple[int, int]:
+    import torch.distributed as dist
+
+    if dist.is_available() and dist.is_initialized():
+        return dist.get_rank(group), dist.get_world_size(group)
+    return 0, 1
+
+
+def run_sharded(items: list, solve, group=None):
+    """Runs independent flows on all ranks: the items are dealt round-robin (``shard``), each
+    rank calls ``solve(local_items) -> (results, seconds)`` on its own GPU, and the results are
+    gathered on every rank in the items' order.  Nothing crosses ranks on the data path: the
+    only exchanges are the two scalars of ``aggregate`` and the gathered results after the
+    timed work.  Returns (JobTiming over all ranks, results[len(items)], local indices)."""
+    import torch.distributed as dist
+
+    rank, world = _rank_world(group)
+    mine = shard(len(items), rank, world)
+    results, seconds = solve([items[i] for i in mine])
+    if len(results) != len(mine):
+        raise ValueError("solve returned a different number of results than items")
+    job = aggregate(len(mine), seconds, group)
+    out = [None] * len(items)
+    if world == 1:
+        parts = [(mine, results)]
+    else:
+        parts = [None] * world
+        dist.all_gather_object(parts, (mine, results), group=group)
+    for idx, res in parts:
+        for i, r in zip(idx, res):
+            out[i] = r
+    return job, out, mine

@@ -4,7 +4,9 @@ Requests (``FlowSpec``: lattice, range, model, couplings, frequency grid, cutoff
 queued as they arrive.  Between batch steps the server admits queued requests -- in arrival
 order ("fifo") or smallest expected work first ("sjf": the flow's nominal work per step times
 its number of steps) -- while their device footprint fits the memory budget (and, optionally,
-a flow-count limit);
+a flow-count limit).  Under "srpt" every request that fits is admitted in arrival order, and
+before each step only the k resident flows with the least remaining work run (the others are
+paused, keeping their state): shortest-remaining-work-first with preemption between steps;
 every admitted flow keeps its vertex and self-energy state resident on the device until it
 finishes, and all resident flows advance together, one cutoff step per batch step.  Finished
 flows are retired at once (results copied out, memory released) so that waiting requests take
@@ -112,11 +114,24 @@ def next_ticket(queue, policy: str, now: float | None = None, max_wait: float | 
 class FlowServer:
     def __init__(self, device: int = 0, memory_budget: int | None = None, max_flows: int | None = None,
                  nodes_per_iteration: int = 1, use_graph: bool = True, clock=time.perf_counter, policy: str = "fifo",
-                 max_wait: float | None = None):
-        if policy not in ("fifo", "sjf"):
-            raise ValueError("policy must be 'fifo' or 'sjf'")
+                 max_wait: float | None = None, autotune: bool = False, autotune_interval: int = 20):
+        if policy not in ("fifo", "sjf", "srpt"):
+            raise ValueError("policy must be 'fifo', 'sjf' or 'srpt'")
         self.policy = policy
         self.max_wait = max_wait
+        # srpt: flows that run at each step (the rest are paused); max_flows keeps its meaning
+        # of a residency limit for the other policies
+        self.running = max(1, int(max_flows)) if (policy == "srpt" and max_flows) else 1
+        if policy == "srpt":
+            max_flows = None
+        self._paused: set[int] = set()
+        # batch autotuner: re-run when the set of running flows changed, at most every
+        # autotune_interval steps
+        self.autotune = autotune
+        self.autotune_interval = autotune_interval
+        self._tuned_set: frozenset | None = None
+        self._tuned_at = -10 ** 9
+        self.tunings: list[dict] = []
         self.batch = Su2Batch(device, nodes_per_iteration, use_graph)
         if memory_budget is None:
             free, _ = device_memory(device)
@@ -141,7 +156,7 @@ class FlowServer:
         while self.queue:
             if self.max_flows is not None and len(self.active) >= self.max_flows:
                 return
-            t = next_ticket(self.queue, self.policy, self.clock(), self.max_wait)
+            t = next_ticket(self.queue, "fifo" if self.policy == "srpt" else self.policy, self.clock(), self.max_wait)
             if self.active and self.used + t.footprint > self.budget:
                 return
             tab, freq, cut = t._built
@@ -159,6 +174,7 @@ class FlowServer:
             if phase != PHASE_DONE:
                 continue
             t = self.active.pop(fid)
+            self._paused.discard(fid)
             t.result = self.batch.result(fid)
             t.t_done = self.clock()
             self.batch.remove(fid)
@@ -166,11 +182,38 @@ class FlowServer:
             t._built = None
             self.finished.append(t)
 
+    def _choose_running(self) -> None:
+        """srpt: the `running` resident flows with the least remaining work take the next step
+        (ties to the older request); every other resident flow is paused."""
+        rem = []
+        for fid, t in self.active.items():
+            _, step, _ = self.batch.poll(fid)
+            n_cut = len(t._built[2])
+            rem.append((t.work * max(n_cut - 1 - step, 0) / max(n_cut - 1, 1), t.id, fid))
+        rem.sort()
+        run = {fid for _, _, fid in rem[:self.running]}
+        for fid in self.active:
+            want = fid not in run
+            if want != (fid in self._paused):
+                self.batch.set_paused(fid, want)
+                if want:
+                    self._paused.add(fid)
+                else:
+                    self._paused.discard(fid)
+
     def pump(self) -> int:
-        """Admits what fits, advances every resident flow by one step and retires finished
-        flows.  Returns the number of flows resident or queued."""
+        """Admits what fits, advances the resident flows by one step (under "srpt" only the
+        ones with the least remaining work) and retires finished flows.  Returns the number of
+        flows resident or queued."""
         self._admit()
         if self.active:
+            if self.policy == "srpt":
+                self._choose_running()
+            if self.autotune:
+                running = frozenset(f for f in self.active if f not in self._paused)
+                if running != self._tuned_set and self.steps - self._tuned_at >= self.autotune_interval:
+                    self.tunings.append({"step": self.steps, "flows": len(running), **self.batch.autotune(1)})
+                    self._tuned_set, self._tuned_at = running, self.steps
             self.batch.step()
             self.steps += 1
             self._retire()

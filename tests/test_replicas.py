@@ -81,3 +81,60 @@ def test_two_gloo_ranks_split_flows_and_time_by_slowest_rank():
     tab.interaction_J = np.abs(tab.interaction_J) * (0.5 + 0.25 * 3)
     n, cs, _, _ = Oracle(tab, freq).flow(cut, *tab.initial_state(len(freq)))
     assert np.array_equal(np.array(flows[3], np.float32), cs[n - 1])
+
+
+def _scan_rank(rank, world, port, out):
+    """A rank of the sharded scan driver: flows dealt by replicas.run_sharded, the CPU oracle
+    standing in for the rank's GPU batch."""
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import time
+
+    import spinparser_gb300 as spn
+    from oracle import Oracle
+
+    freq = spn.frequency_exponential(0.05, 10.0, 6)
+    cut = spn.cutoff_exponential(10.0, 1.0, 0.8)
+    specs = [(2 + (i % 2), 0.1 * i) for i in range(7)]  # (range, J2) of seven flows
+
+    def solve(local):
+        t0 = time.perf_counter()
+        res = []
+        for rng_, j2 in local:
+            tab = spn.Lattice("square", rng_, "square-j1j2heisenberg", {"j1": "1.0", "j2": str(j2)}).tables()
+            n, cs, _, _ = Oracle(tab, freq).flow(cut, *tab.initial_state(len(freq)))
+            res.append(cs[n - 1].tolist())
+        return res, (time.perf_counter() - t0) + 5.0 * rank  # rank 1 is made the slow one
+
+    job, results, mine = replicas.run_sharded(specs, solve)
+    out[rank] = {"units": job.units, "seconds": job.seconds, "world": job.world, "mine": mine, "results": results}
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_sharded_scan_driver_on_two_gloo_ranks():
+    ctx = mp.get_context("spawn")
+    with ctx.Manager() as m:
+        out = m.dict()
+        port = _free_port()
+        procs = [ctx.Process(target=_scan_rank, args=(r, 2, port, out)) for r in range(2)]
+        for p in procs:
+            p.start()
+        for p in procs:
+            p.join(timeout=240)
+        assert all(p.exitcode == 0 for p in procs)
+        res = dict(out)
+    assert res[0]["mine"] == [0, 2, 4, 6] and res[1]["mine"] == [1, 3, 5]
+    for r in (0, 1):
+        assert res[r]["units"] == 7 and res[r]["world"] == 2
+        assert res[r]["seconds"] >= 5.0  # the slowest rank's time
+    assert res[0]["results"] == res[1]["results"]  # every rank holds every flow's result
+    import spinparser_gb300 as spn
+    from oracle import Oracle
+
+    freq = spn.frequency_exponential(0.05, 10.0, 6)
+    cut = spn.cutoff_exponential(10.0, 1.0, 0.8)
+    for i in (3, 6):  # a flow's result does not depend on the rank that ran it
+        tab = spn.Lattice("square", 2 + (i % 2), "square-j1j2heisenberg", {"j1": "1.0", "j2": str(0.1 * i)}).tables()
+        n, cs, _, _ = Oracle(tab, freq).flow(cut, *tab.initial_state(len(freq)))
+        assert np.array_equal(np.array(res[0]["results"][i], np.float32), cs[n - 1])

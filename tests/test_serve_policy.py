@@ -69,3 +69,37 @@ def test_request_stays_queued_when_the_batch_cannot_take_it():
     with pytest.raises(MemoryError):
         srv._admit()
     assert len(srv.queue) == 1 and not srv.active
+
+
+class _FakeBatch:
+    """poll() answers from a step table; set_paused() records the flows held out."""
+
+    def __init__(self, steps):
+        self.steps, self.paused = steps, set()
+
+    def poll(self, fid):
+        return 0, self.steps[fid], 0
+
+    def set_paused(self, fid, paused):
+        (self.paused.add if paused else self.paused.discard)(fid)
+
+
+def test_srpt_runs_the_flows_with_least_remaining_work():
+    from spinparser_gb300.serve import FlowServer, prepare
+
+    srv = FlowServer.__new__(FlowServer)  # host logic only: no device batch
+    srv.policy, srv.running, srv._paused = "srpt", 1, set()
+    big, small = Ticket(0, spec(5, 16), 0.0), Ticket(1, spec(3, 8), 1.0)
+    for t in (big, small):
+        prepare(t)
+    n_cut = len(big._built[2])
+    srv.active = {10: big, 11: small}
+    srv.batch = _FakeBatch({10: 0, 11: 0})
+    srv._choose_running()
+    assert srv.batch.paused == {10}  # the small request runs first
+    srv.batch.steps = {10: n_cut - 2, 11: 0}  # the big one is almost done: least remaining work
+    srv._choose_running()
+    assert srv.batch.paused == {11}
+    srv.running = 2
+    srv._choose_running()
+    assert srv.batch.paused == set()
