@@ -109,6 +109,9 @@ def parse_args():
                     help="serve-mixed: server arms to run at every rate, comma separated: fifo or sjf, optionally @k "
                          "for a k-flow residency limit, or srpt@k (k flows with the least remaining work run at each "
                          "step), e.g. fifo,sjf@2,srpt@1")
+    ap.add_argument("--grouping", choices=["auto", "off"], default="auto",
+                    help="scan/serve: batch configuration chosen by the batch autotuner (auto) or the per-flow "
+                         "kernel without cross-flow sharing (off)")
     ap.add_argument("--flow-cutoffs", type=int, default=None,
                     help="XYZ/TRI workloads: run only the first M cutoffs of the flow (short runs for profiling)")
     ap.add_argument("--precision", choices=["fp64-self-energy", "plain"], default="fp64-self-energy",
@@ -388,14 +391,16 @@ def _check_same(a, b):
     return float(max(np.nanmax(np.abs(azz.reshape(b.zz.shape) - b.zz)), np.nanmax(np.abs(add_.reshape(b.dd.shape) - b.dd))))
 
 
-def _serve_local(items, arrivals, policy, plain):
+def _serve_local(items, arrivals, policy, plain, grouping="auto"):
     """One rank's server over its dealt requests: (index, spec) items arriving at their offsets
     of the global stream.  Returns per item (time to result, largest difference from the same
     flow solved alone) and the rank's makespan."""
     from spinparser_gb300.serve import FlowServer
 
     name, _, slots = policy.partition("@")
-    srv = FlowServer(policy=name, max_flows=int(slots) if slots else None, autotune=True)
+    srv = FlowServer(policy=name, max_flows=int(slots) if slots else None, autotune=(grouping == "auto"))
+    if grouping == "off":
+        srv.batch.set_grouping(0)
     order = sorted(range(len(items)), key=lambda j: arrivals[items[j][0]])
     t0 = time.perf_counter()
     tickets, k = {}, 0
@@ -481,7 +486,7 @@ def run_multi(args):
             stats = {}
 
             def served_solve(local_items):
-                out, makespan, steps = _serve_local(local_items, arrivals, policy, plain)
+                out, makespan, steps = _serve_local(local_items, arrivals, policy, plain, args.grouping)
                 stats["steps"] = steps
                 return out, makespan
 
@@ -523,7 +528,7 @@ def run_multi(args):
         "metric": "scan flows/s" if scan else "served flows/s",
         "value": top["batched"]["flows_per_s"], "unit": "flows/s", "n_gpus": world,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": args.workload, "flows": n, "seed": workloads.SEED,
+        "config": {"workload": args.workload, "flows": n, "seed": workloads.SEED, "grouping": args.grouping,
                    "parallelism": f"replicas x{world} (flows dealt round-robin)",
                    "draws": "square J1-J2, J2 U[0,1], range U{3,5,7}, N U{32,48,64}, grid [0.005,50], cutoff 50->0.05 x0.98"
                    if scan else "square/cubic/pyrochlore J1-J2, J2 U[-0.5,0.5], range U{3..7}, N U{32,48,64}, "

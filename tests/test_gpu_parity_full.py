@@ -12,9 +12,16 @@ oracle (the restatement of src/SU2/SU2FrgCore.cpp:89-431), at the shapes the ben
   whole flow on the GPU against the whole flow of the FP32 oracle (the reference's arithmetic)
   and of the FP64 oracle.  Correlations are compared at every cutoff.
 
-Tolerances: one RHS, normwise relative error max|gpu - oracle| / max|oracle| <= 1e-5 per array;
-final correlations (static spin and density susceptibility per site) <= 1e-4 normwise, the same
-bound at every cutoff.
+Tolerances, normwise relative error max|a - b| / max|b| per array:
+  * one RHS: the GPU within 1e-5 of the FP64 oracle (the exact RHS of the same state), and
+    within 1e-5 of the FP32 oracle plus the FP32 oracle's own distance from the FP64 one.  Late
+    in the cubic flow (cutoff 0.05, vertex entries near 100) the reference's FP32 arithmetic is
+    itself 3.8e-5 away from the exact RHS (uncompensated sums with cancellation), while the GPU's
+    Kahan-compensated sums stay within 7e-6 of it; a bound of 1e-5 on the plain GPU-vs-FP32
+    difference would test the reference's rounding, not the GPU.  Where the reference is accurate
+    (early and mid-flow) the second bound is the plain 1e-5;
+  * final correlations (static spin and density susceptibility per site) <= 1e-4, the same
+    bound at every cutoff.
 """
 import numpy as np
 import pytest
@@ -55,14 +62,16 @@ def check_rhs(flow, orc, state, label):
     c, v2, ss, dd = state
     flow.set_state(float(c), v2, ss, dd)
     flow.compute_step()
-    g2, gss, gdd = flow.get_flow()
-    r2, rss, rdd = orc.rhs(c, v2, ss, dd)
-    errs = (normwise(g2, r2), normwise(gss, rss), normwise(gdd, rdd))
-    PARITY_REPORT.append(f"{label} cutoff {float(c):.6g}: self-energy {errs[0]:.2e}, spin vertex {errs[1]:.2e}, "
-                         f"density vertex {errs[2]:.2e} ({len(rss)} entries)")
-    assert np.all(np.isfinite(gss)) and np.all(np.isfinite(gdd))
-    for e in errs:
-        assert e <= RHS_TOL, (label, errs)
+    gpu = flow.get_flow()
+    r32 = orc.rhs(c, v2, ss, dd)
+    r64 = orc.rhs(np.float64(c), *(np.asarray(x, np.float64) for x in (v2, ss, dd)), fp64=True)
+    assert np.all(np.isfinite(gpu[1])) and np.all(np.isfinite(gpu[2]))
+    for name, g, a, b in zip(("self-energy", "spin vertex", "density vertex"), gpu, r32, r64):
+        e32, e64, ref = normwise(g, a), normwise(g, b), normwise(a, b)
+        PARITY_REPORT.append(f"{label} cutoff {float(c):.6g} {name}: GPU-FP32 oracle {e32:.2e}, GPU-FP64 oracle "
+                             f"{e64:.2e}, FP32 oracle-FP64 oracle {ref:.2e} ({len(a)} entries)")
+        assert e64 <= RHS_TOL, (label, name, e64)
+        assert e32 <= RHS_TOL + ref, (label, name, e32, ref)
 
 
 def test_whole_rhs_cubic_j1j2_r6_n64_early_mid_late():
