@@ -323,6 +323,51 @@ __device__ __forceinline__ void access4m(const M &m, int nl, T s, T t, T u, AB4T
     }
 }
 
+// One mesh interpolation (lo, hi, bias) of |w|.  The access buffers of a node interpolate at
+// most four distinct magnitudes: a coordinate and its negation (-a - b is bitwise -(a + b)
+// under round-to-nearest) fold to the same value, so make_desc looks each up once.
+template <class T>
+struct Interp {
+    int lo, hi;
+    T b;
+};
+template <class T, class M>
+__device__ __forceinline__ Interp<T> interp_abs(const M &m, T w) {
+    Interp<T> r;
+    mesh_interp_m(m, w < T(0) ? -w : w, r.lo, r.hi, r.b);
+    return r;
+}
+
+// access4m with the two interpolations given: ia for the first interpolated coordinate after
+// folding (t for S, s for T and U), ib for the second (u for S and T, t for U).  The caller
+// passes interp_abs of the matching coordinates; folding, weights and offsets are access4m's.
+template <int CH, class T>
+__device__ __forceinline__ void access4i(int n, int nl, T s, T t, T u, const Interp<T> &ia, const Interp<T> &ib,
+                                         int e, AB4T<T> &ab) {
+    ab.exch = fold(s, t, u);
+    const int stepT = n * nl;
+    const int la = ia.lo, ua = ia.hi, lb = ib.lo, ub = ib.hi;
+    const T ba = ia.b, bb = ib.b;
+    const T na = rn_sub(T(1), ba), nb = rn_sub(T(1), bb);
+    const T w0 = rn_mul(nb, na), w1 = rn_mul(nb, ba), w2 = rn_mul(bb, na), w3 = rn_mul(bb, ba);
+    if (CH == kS) {
+        slab(e, la, lb, stepT, nl, ab.off[0], w0, ab.w[0], ab.sw[0]);
+        slab(e, ua, lb, stepT, nl, ab.off[1], w1, ab.w[1], ab.sw[1]);
+        slab(e, la, ub, stepT, nl, ab.off[2], w2, ab.w[2], ab.sw[2]);
+        slab(e, ua, ub, stepT, nl, ab.off[3], w3, ab.w[3], ab.sw[3]);
+    } else if (CH == kT) {
+        slab(la, e, lb, stepT, nl, ab.off[0], w0, ab.w[0], ab.sw[0]);
+        slab(ua, e, lb, stepT, nl, ab.off[1], w1, ab.w[1], ab.sw[1]);
+        slab(la, e, ub, stepT, nl, ab.off[2], w2, ab.w[2], ab.sw[2]);
+        slab(ua, e, ub, stepT, nl, ab.off[3], w3, ab.w[3], ab.sw[3]);
+    } else {
+        slab(la, lb, e, stepT, nl, ab.off[0], w0, ab.w[0], ab.sw[0]);
+        slab(ua, lb, e, stepT, nl, ab.off[1], w1, ab.w[1], ab.sw[1]);
+        slab(la, ub, e, stepT, nl, ab.off[2], w2, ab.w[2], ab.sw[2]);
+        slab(ua, ub, e, stepT, nl, ab.off[3], w3, ab.w[3], ab.sw[3]);
+    }
+}
+
 template <int CH, class T>
 __device__ __forceinline__ void access4(const T *pos, int n, int nl, T s, T t, T u, AB4T<T> &ab) {
     access4m<CH>(MeshSearch<T>{pos, n}, nl, s, t, u, ab);

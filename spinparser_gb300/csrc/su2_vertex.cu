@@ -42,8 +42,9 @@ constexpr double kPi = 3.14159265358979323846;
 
 struct __align__(16) NodeDesc {
     int4 off[4];
-    float4 ws[4][2];  // per buffer: (w0, sw0, w1, sw1), (w2, sw2, w3, sw3): weight, sign * weight
-    int exch;  // bit i: buffer i reads the site-exchanged pairs (inverted sites)
+    float4 w[4];  // per buffer: the four interpolation weights
+    int exch;  // bit i: buffer i reads the site-exchanged pairs (inverted sites); bit 4 + 4i + q:
+               // support q of buffer i is a swapped (s < u) slab, whose density weight is -w
     float c;   // node coefficient, channel sign included
     float lv[8];  // t channel: site-local values cbs, cbd, icas, icad, cbs2, cbd2, icas2, icad2
     int pad[2];
@@ -71,10 +72,20 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
     return d;
 }
 
-__device__ __forceinline__ void put_ab(NodeDesc &d, int i, const AB4 &ab) {
+// Stores buffer i of a node; returns its sign bits (bit 4 + 4i + q set when sw[q] = -w[q], the
+// density weight of a swapped slab; sw is exactly +-w, so the pair is rebuilt without loss).
+__device__ __forceinline__ int put_ab(NodeDesc &d, int i, const AB4 &ab) {
     d.off[i] = make_int4(ab.off[0], ab.off[1], ab.off[2], ab.off[3]);
-    d.ws[i][0] = make_float4(ab.w[0], ab.sw[0], ab.w[1], ab.sw[1]);
-    d.ws[i][1] = make_float4(ab.w[2], ab.sw[2], ab.w[3], ab.sw[3]);
+    d.w[i] = make_float4(ab.w[0], ab.w[1], ab.w[2], ab.w[3]);
+    int bits = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) bits |= int(__float_as_int(ab.sw[q]) != __float_as_int(ab.w[q])) << q;
+    return bits << (4 + 4 * i);
+}
+
+// (w, sign * w) of support q from the weight and the descriptor's sign bit.
+__device__ __forceinline__ float2 wpair(float w, int exch, int bit) {
+    return make_float2(w, __int_as_float(__float_as_int(w) ^ (((exch >> bit) & 1) << 31)));
 }
 
 // Site-local (rid 0) (spin, density) value of an access buffer: spin sum w * ss, density sum
@@ -87,34 +98,54 @@ __device__ __forceinline__ void local_pair(const FlowArgs &a, const AB4 &ab, flo
     vd = g.y;
 }
 
-// Phase A: descriptor of one node (lane = node).
+// Phase A: descriptor of one node (lane = node).  The node's access buffers interpolate four
+// distinct magnitudes (interp_abs), each looked up once; folding, weights and offsets are
+// access4m's, so the descriptor is the one eight (s, u) or sixteen (t) separate lookups give.
 template <int CH>
 __device__ __forceinline__ void make_desc(const FlowArgs &a, const float *pos, const Transfer &f, float wp, float c,
                                           NodeDesc &d) {
     AB4 ab;
     int exch = 0;
-    const int nl = a.nl;
+    const int nl = a.nl, n = a.n;
     const MeshIndex m{pos, a.n, a.mesh_lo, a.mesh_base, a.mesh_shift};
     if (CH == kS) {  // integralKernelS, SU2FrgCore.cpp:202-206
-        access4m<kS>(m, nl, f.s, -f.w1 - wp, -f.w2 - wp, ab, f.si); put_ab(d, 0, ab); exch |= ab.exch << 0;
-        access4m<kS>(m, nl, f.s, f.w1p + wp, -f.w2p - wp, ab, f.si); put_ab(d, 1, ab); exch |= ab.exch << 1;
-        access4m<kS>(m, nl, f.s, f.w2 + wp, f.w1 + wp, ab, f.si); put_ab(d, 2, ab); exch |= ab.exch << 2;
-        access4m<kS>(m, nl, f.s, -f.w2p - wp, f.w1p + wp, ab, f.si); put_ab(d, 3, ab); exch |= ab.exch << 3;
+        {  // buffers 0 and 2 interpolate |w1 + wp| and |w2 + wp|
+            const Interp<float> iA = interp_abs(m, f.w1 + wp), iB = interp_abs(m, f.w2 + wp);
+            access4i<kS>(n, nl, f.s, -f.w1 - wp, -f.w2 - wp, iA, iB, f.si, ab); exch |= put_ab(d, 0, ab) | (int(ab.exch) << 0);
+            access4i<kS>(n, nl, f.s, f.w2 + wp, f.w1 + wp, iB, iA, f.si, ab); exch |= put_ab(d, 2, ab) | (int(ab.exch) << 2);
+        }
+        {  // buffers 1 and 3: |w1p + wp| and |w2p + wp|
+            const Interp<float> iP = interp_abs(m, f.w1p + wp), iQ = interp_abs(m, f.w2p + wp);
+            access4i<kS>(n, nl, f.s, f.w1p + wp, -f.w2p - wp, iP, iQ, f.si, ab); exch |= put_ab(d, 1, ab) | (int(ab.exch) << 1);
+            access4i<kS>(n, nl, f.s, -f.w2p - wp, f.w1p + wp, iQ, iP, f.si, ab); exch |= put_ab(d, 3, ab) | (int(ab.exch) << 3);
+        }
     } else if (CH == kT) {  // integralKernelT, SU2FrgCore.cpp:233-239, 269-284
-        access4m<kT>(m, nl, f.w1 - wp, f.t, f.w1p + wp, ab, f.ti); put_ab(d, 0, ab); exch |= ab.exch << 0;
-        access4m<kT>(m, nl, f.w2p - wp, f.t, -f.w2 - wp, ab, f.ti); put_ab(d, 1, ab); exch |= ab.exch << 1;
-        access4m<kT>(m, nl, f.w1p + wp, f.t, f.w1 - wp, ab, f.ti); put_ab(d, 2, ab); exch |= ab.exch << 2;
-        access4m<kT>(m, nl, f.w2 + wp, f.t, wp - f.w2p, ab, f.ti); put_ab(d, 3, ab); exch |= ab.exch << 3;
         float v0, v1;
-        access4m<kU>(m, nl, f.w2p - wp, -f.w2 - wp, f.t, ab, f.ti); local_pair(a, ab, v0, v1); d.lv[0] = v0; d.lv[1] = v1;
-        access4m<kU>(m, nl, f.w1 - wp, -f.w1p - wp, -f.t, ab, f.ti); local_pair(a, ab, v0, v1); d.lv[2] = v0; d.lv[3] = v1;
-        access4m<kU>(m, nl, f.w2 + wp, wp - f.w2p, f.t, ab, f.ti); local_pair(a, ab, v0, v1); d.lv[4] = v0; d.lv[5] = v1;
-        access4m<kU>(m, nl, f.w1p + wp, wp - f.w1, -f.t, ab, f.ti); local_pair(a, ab, v0, v1); d.lv[6] = v0; d.lv[7] = v1;
+        {  // buffers 0, 2 and local buffers 1, 3: |w1 - wp| and |w1p + wp|
+            const Interp<float> iC = interp_abs(m, f.w1 - wp), iP = interp_abs(m, f.w1p + wp);
+            access4i<kT>(n, nl, f.w1 - wp, f.t, f.w1p + wp, iC, iP, f.ti, ab); exch |= put_ab(d, 0, ab) | (int(ab.exch) << 0);
+            access4i<kT>(n, nl, f.w1p + wp, f.t, f.w1 - wp, iP, iC, f.ti, ab); exch |= put_ab(d, 2, ab) | (int(ab.exch) << 2);
+            access4i<kU>(n, nl, f.w1 - wp, -f.w1p - wp, -f.t, iC, iP, f.ti, ab); local_pair(a, ab, v0, v1); d.lv[2] = v0; d.lv[3] = v1;
+            access4i<kU>(n, nl, f.w1p + wp, wp - f.w1, -f.t, iP, iC, f.ti, ab); local_pair(a, ab, v0, v1); d.lv[6] = v0; d.lv[7] = v1;
+        }
+        {  // buffers 1, 3 and local buffers 0, 2: |w2p - wp| and |w2 + wp|
+            const Interp<float> iD = interp_abs(m, f.w2p - wp), iB = interp_abs(m, f.w2 + wp);
+            access4i<kT>(n, nl, f.w2p - wp, f.t, -f.w2 - wp, iD, iB, f.ti, ab); exch |= put_ab(d, 1, ab) | (int(ab.exch) << 1);
+            access4i<kT>(n, nl, f.w2 + wp, f.t, wp - f.w2p, iB, iD, f.ti, ab); exch |= put_ab(d, 3, ab) | (int(ab.exch) << 3);
+            access4i<kU>(n, nl, f.w2p - wp, -f.w2 - wp, f.t, iD, iB, f.ti, ab); local_pair(a, ab, v0, v1); d.lv[0] = v0; d.lv[1] = v1;
+            access4i<kU>(n, nl, f.w2 + wp, wp - f.w2p, f.t, iB, iD, f.ti, ab); local_pair(a, ab, v0, v1); d.lv[4] = v0; d.lv[5] = v1;
+        }
     } else {  // integralKernelU, SU2FrgCore.cpp:309-313
-        access4m<kU>(m, nl, f.w1 + wp, wp - f.w2p, f.u, ab, f.ui); put_ab(d, 0, ab); exch |= ab.exch << 0;
-        access4m<kU>(m, nl, f.w1p + wp, f.w2 - wp, f.u, ab, f.ui); put_ab(d, 1, ab); exch |= ab.exch << 1;
-        access4m<kU>(m, nl, f.w2p - wp, -f.w1 - wp, f.u, ab, f.ui); put_ab(d, 2, ab); exch |= ab.exch << 2;
-        access4m<kU>(m, nl, f.w2 - wp, f.w1p + wp, f.u, ab, f.ui); put_ab(d, 3, ab); exch |= ab.exch << 3;
+        {  // buffers 0 and 2: |w1 + wp| and |w2p - wp|
+            const Interp<float> iA = interp_abs(m, f.w1 + wp), iD = interp_abs(m, f.w2p - wp);
+            access4i<kU>(n, nl, f.w1 + wp, wp - f.w2p, f.u, iA, iD, f.ui, ab); exch |= put_ab(d, 0, ab) | (int(ab.exch) << 0);
+            access4i<kU>(n, nl, f.w2p - wp, -f.w1 - wp, f.u, iD, iA, f.ui, ab); exch |= put_ab(d, 2, ab) | (int(ab.exch) << 2);
+        }
+        {  // buffers 1 and 3: |w1p + wp| and |w2 - wp|
+            const Interp<float> iP = interp_abs(m, f.w1p + wp), iE = interp_abs(m, f.w2 - wp);
+            access4i<kU>(n, nl, f.w1p + wp, f.w2 - wp, f.u, iP, iE, f.ui, ab); exch |= put_ab(d, 1, ab) | (int(ab.exch) << 1);
+            access4i<kU>(n, nl, f.w2 - wp, f.w1p + wp, f.u, iE, iP, f.ui, ab); exch |= put_ab(d, 3, ab) | (int(ab.exch) << 3);
+        }
     }
     d.exch = exch;
     d.c = c;
@@ -136,32 +167,50 @@ __device__ __forceinline__ void make_supports(const FlowArgs &a, const float *po
                                               LocDesc &loc) {
     AB4 ab;
     int exch = 0;
-    const int nl = a.nl;
+    const int nl = a.nl, n = a.n;
     const MeshIndex m{pos, a.n, a.mesh_lo, a.mesh_base, a.mesh_shift};
     if (CH == kS) {
-        access4m<kS>(m, nl, f.s, -f.w1 - wp, -f.w2 - wp, ab, f.si); put_ab(d, 0, ab); exch |= ab.exch << 0;
-        access4m<kS>(m, nl, f.s, f.w1p + wp, -f.w2p - wp, ab, f.si); put_ab(d, 1, ab); exch |= ab.exch << 1;
-        access4m<kS>(m, nl, f.s, f.w2 + wp, f.w1 + wp, ab, f.si); put_ab(d, 2, ab); exch |= ab.exch << 2;
-        access4m<kS>(m, nl, f.s, -f.w2p - wp, f.w1p + wp, ab, f.si); put_ab(d, 3, ab); exch |= ab.exch << 3;
+        {  // buffers 0 and 2 interpolate |w1 + wp| and |w2 + wp|
+            const Interp<float> iA = interp_abs(m, f.w1 + wp), iB = interp_abs(m, f.w2 + wp);
+            access4i<kS>(n, nl, f.s, -f.w1 - wp, -f.w2 - wp, iA, iB, f.si, ab); exch |= put_ab(d, 0, ab) | (int(ab.exch) << 0);
+            access4i<kS>(n, nl, f.s, f.w2 + wp, f.w1 + wp, iB, iA, f.si, ab); exch |= put_ab(d, 2, ab) | (int(ab.exch) << 2);
+        }
+        {  // buffers 1 and 3: |w1p + wp| and |w2p + wp|
+            const Interp<float> iP = interp_abs(m, f.w1p + wp), iQ = interp_abs(m, f.w2p + wp);
+            access4i<kS>(n, nl, f.s, f.w1p + wp, -f.w2p - wp, iP, iQ, f.si, ab); exch |= put_ab(d, 1, ab) | (int(ab.exch) << 1);
+            access4i<kS>(n, nl, f.s, -f.w2p - wp, f.w1p + wp, iQ, iP, f.si, ab); exch |= put_ab(d, 3, ab) | (int(ab.exch) << 3);
+        }
     } else if (CH == kT) {
-        access4m<kT>(m, nl, f.w1 - wp, f.t, f.w1p + wp, ab, f.ti); put_ab(d, 0, ab); exch |= ab.exch << 0;
-        access4m<kT>(m, nl, f.w2p - wp, f.t, -f.w2 - wp, ab, f.ti); put_ab(d, 1, ab); exch |= ab.exch << 1;
-        access4m<kT>(m, nl, f.w1p + wp, f.t, f.w1 - wp, ab, f.ti); put_ab(d, 2, ab); exch |= ab.exch << 2;
-        access4m<kT>(m, nl, f.w2 + wp, f.t, wp - f.w2p, ab, f.ti); put_ab(d, 3, ab); exch |= ab.exch << 3;
         auto put_loc = [&](int i) {
             loc.off[i] = make_int4(ab.off[0], ab.off[1], ab.off[2], ab.off[3]);
             loc.w[i] = make_float4(ab.w[0], ab.w[1], ab.w[2], ab.w[3]);
             loc.sw[i] = make_float4(ab.sw[0], ab.sw[1], ab.sw[2], ab.sw[3]);
         };
-        access4m<kU>(m, nl, f.w2p - wp, -f.w2 - wp, f.t, ab, f.ti); put_loc(0);
-        access4m<kU>(m, nl, f.w1 - wp, -f.w1p - wp, -f.t, ab, f.ti); put_loc(1);
-        access4m<kU>(m, nl, f.w2 + wp, wp - f.w2p, f.t, ab, f.ti); put_loc(2);
-        access4m<kU>(m, nl, f.w1p + wp, wp - f.w1, -f.t, ab, f.ti); put_loc(3);
+        {
+            const Interp<float> iC = interp_abs(m, f.w1 - wp), iP = interp_abs(m, f.w1p + wp);
+            access4i<kT>(n, nl, f.w1 - wp, f.t, f.w1p + wp, iC, iP, f.ti, ab); exch |= put_ab(d, 0, ab) | (int(ab.exch) << 0);
+            access4i<kT>(n, nl, f.w1p + wp, f.t, f.w1 - wp, iP, iC, f.ti, ab); exch |= put_ab(d, 2, ab) | (int(ab.exch) << 2);
+            access4i<kU>(n, nl, f.w1 - wp, -f.w1p - wp, -f.t, iC, iP, f.ti, ab); put_loc(1);
+            access4i<kU>(n, nl, f.w1p + wp, wp - f.w1, -f.t, iP, iC, f.ti, ab); put_loc(3);
+        }
+        {
+            const Interp<float> iD = interp_abs(m, f.w2p - wp), iB = interp_abs(m, f.w2 + wp);
+            access4i<kT>(n, nl, f.w2p - wp, f.t, -f.w2 - wp, iD, iB, f.ti, ab); exch |= put_ab(d, 1, ab) | (int(ab.exch) << 1);
+            access4i<kT>(n, nl, f.w2 + wp, f.t, wp - f.w2p, iB, iD, f.ti, ab); exch |= put_ab(d, 3, ab) | (int(ab.exch) << 3);
+            access4i<kU>(n, nl, f.w2p - wp, -f.w2 - wp, f.t, iD, iB, f.ti, ab); put_loc(0);
+            access4i<kU>(n, nl, f.w2 + wp, wp - f.w2p, f.t, iB, iD, f.ti, ab); put_loc(2);
+        }
     } else {
-        access4m<kU>(m, nl, f.w1 + wp, wp - f.w2p, f.u, ab, f.ui); put_ab(d, 0, ab); exch |= ab.exch << 0;
-        access4m<kU>(m, nl, f.w1p + wp, f.w2 - wp, f.u, ab, f.ui); put_ab(d, 1, ab); exch |= ab.exch << 1;
-        access4m<kU>(m, nl, f.w2p - wp, -f.w1 - wp, f.u, ab, f.ui); put_ab(d, 2, ab); exch |= ab.exch << 2;
-        access4m<kU>(m, nl, f.w2 - wp, f.w1p + wp, f.u, ab, f.ui); put_ab(d, 3, ab); exch |= ab.exch << 3;
+        {  // buffers 0 and 2: |w1 + wp| and |w2p - wp|
+            const Interp<float> iA = interp_abs(m, f.w1 + wp), iD = interp_abs(m, f.w2p - wp);
+            access4i<kU>(n, nl, f.w1 + wp, wp - f.w2p, f.u, iA, iD, f.ui, ab); exch |= put_ab(d, 0, ab) | (int(ab.exch) << 0);
+            access4i<kU>(n, nl, f.w2p - wp, -f.w1 - wp, f.u, iD, iA, f.ui, ab); exch |= put_ab(d, 2, ab) | (int(ab.exch) << 2);
+        }
+        {  // buffers 1 and 3: |w1p + wp| and |w2 - wp|
+            const Interp<float> iP = interp_abs(m, f.w1p + wp), iE = interp_abs(m, f.w2 - wp);
+            access4i<kU>(n, nl, f.w1p + wp, f.w2 - wp, f.u, iP, iE, f.ui, ab); exch |= put_ab(d, 1, ab) | (int(ab.exch) << 1);
+            access4i<kU>(n, nl, f.w2 - wp, f.w1p + wp, f.u, iE, iP, f.ui, ab); exch |= put_ab(d, 3, ab) | (int(ab.exch) << 3);
+        }
     }
     d.exch = exch;
     d.c = 0.0f;
@@ -190,16 +239,18 @@ template <int SPT, class A>
 __device__ __forceinline__ void gather(const A &a, const NodeDesc &d, int i, const Lane<SPT> &ln, float *vs,
                                        float *vd) {
     const int4 o = d.off[i];
-    const float4 p0 = d.ws[i][0], p1 = d.ws[i][1];
-    const bool ex = (d.exch >> i) & 1;
+    const float4 w = d.w[i];
+    const int ex = d.exch;
+    const float2 p0 = wpair(w.x, ex, 4 + 4 * i), p1 = wpair(w.y, ex, 5 + 4 * i);
+    const float2 p2 = wpair(w.z, ex, 6 + 4 * i), p3 = wpair(w.w, ex, 7 + 4 * i);
 #pragma unroll
     for (int k = 0; k < SPT; ++k) {
-        const float2 *v = a.sd + (ex ? ln.isite[k] : ln.site[k]);
+        const float2 *v = a.sd + (((ex >> i) & 1) ? ln.isite[k] : ln.site[k]);
         float2 g = make_float2(0.0f, 0.0f);
-        g = fma2(make_float2(p0.x, p0.y), __ldg(v + o.x), g);
-        g = fma2(make_float2(p0.z, p0.w), __ldg(v + o.y), g);
-        g = fma2(make_float2(p1.x, p1.y), __ldg(v + o.z), g);
-        g = fma2(make_float2(p1.z, p1.w), __ldg(v + o.w), g);
+        g = fma2(p0, __ldg(v + o.x), g);
+        g = fma2(p1, __ldg(v + o.y), g);
+        g = fma2(p2, __ldg(v + o.z), g);
+        g = fma2(p3, __ldg(v + o.w), g);
         vs[k] = g.x;
         vd[k] = g.y;
     }
