@@ -91,7 +91,7 @@ PRECISION_FORMS = {
     "plain": "FP32 vertex and self-energy state (the reference's types) with Kahan-compensated loop-frequency sums; "
              "FP64 quadrature weights and FP64 measurement accumulation",
 }
-KERNELS_PER_STEP = 8  # self-energy, node tables, vertex flow, 2 x correlation, 3 x Euler
+KERNELS_PER_STEP = 7  # self-energy, node tables, vertex flow, 2 x correlation, 2 x Euler (state, self-energy)
 
 
 def parse_args():

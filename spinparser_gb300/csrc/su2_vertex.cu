@@ -216,6 +216,54 @@ __device__ __forceinline__ void make_supports(const FlowArgs &a, const float *po
     d.c = 0.0f;
 }
 
+// make_supports split over the four threads of a quad (q = 0..3), for a CTA that builds 32
+// nodes with 128 threads.  Thread q builds main buffer b(q) and, in the t channel, local buffer
+// l(q), from the two magnitudes (y1, y2) that those buffers interpolate; the coordinates come
+// from selects, so the quad runs one instruction stream.  Every coordinate is the value
+// make_supports passes (negations are exact), so the supports are the same bits.  Returns the
+// exchange and sign bits of the thread's buffer; the quad ORs them into d.exch.
+template <int CH>
+__device__ __forceinline__ int make_part(const FlowArgs &a, const float *pos, const Transfer &f, float wp, int q,
+                                         NodeDesc &d, LocDesc &loc) {
+    AB4 ab;
+    const int nl = a.nl, n = a.n;
+    const MeshIndex m{pos, a.n, a.mesh_lo, a.mesh_base, a.mesh_shift};
+    const bool lo2 = q < 2, odd = q & 1;
+    if (CH == kS) {
+        // buffers (t, u): 0 (-A, -B), 1 (P, -Q), 2 (B, A), 3 (-Q, P); (y1, y2) = (A, B) or (P, Q)
+        const float y1 = odd ? f.w1p + wp : f.w1 + wp, y2 = odd ? f.w2p + wp : f.w2 + wp;
+        const Interp<float> i1 = interp_abs(m, y1), i2 = interp_abs(m, y2);
+        const float t = lo2 ? (odd ? y1 : -y1) : (odd ? -y2 : y2);
+        const float u = lo2 ? -y2 : y1;
+        access4i<kS>(n, nl, f.s, t, u, lo2 ? i1 : i2, lo2 ? i2 : i1, f.si, ab);
+        return put_ab(d, q, ab) | (int(ab.exch) << q);
+    } else if (CH == kU) {
+        // buffers (s, t): 0 (A, -D), 1 (P, E), 2 (D, -A), 3 (E, P); (y1, y2) = (A, D) or (P, E)
+        const float y1 = odd ? f.w1p + wp : f.w1 + wp, y2 = odd ? f.w2 - wp : f.w2p - wp;
+        const Interp<float> i1 = interp_abs(m, y1), i2 = interp_abs(m, y2);
+        const float sv = lo2 ? y1 : y2;
+        const float t = lo2 ? (odd ? y2 : -y2) : (odd ? y1 : -y1);
+        access4i<kU>(n, nl, sv, t, f.u, lo2 ? i1 : i2, lo2 ? i2 : i1, f.ui, ab);
+        return put_ab(d, q, ab) | (int(ab.exch) << q);
+    } else {
+        // main buffers (s, u): 0 (C, P), 2 (P, C), 1 (D, -B), 3 (B, -D); local buffers (s, t, u):
+        // 1 (C, -P, -t), 3 (P, -C, -t), 0 (D, -B, t), 2 (B, -D, t); (y1, y2) = (C, P), (P, C),
+        // (D, B), (B, D) for q = 0..3
+        const float C = f.w1 - wp, P = f.w1p + wp, D = f.w2p - wp, B = f.w2 + wp;
+        const float x1 = lo2 ? C : D, x2 = lo2 ? P : B;
+        const float y1 = odd ? x2 : x1, y2 = odd ? x1 : x2;
+        const Interp<float> i1 = interp_abs(m, y1), i2 = interp_abs(m, y2);
+        const int bi = (int(odd) << 1) | (q >> 1), li = (int(odd) << 1) | (1 - (q >> 1));
+        access4i<kT>(n, nl, y1, f.t, lo2 ? y2 : -y2, i1, i2, f.ti, ab);
+        const int bits = put_ab(d, bi, ab) | (int(ab.exch) << bi);
+        access4i<kU>(n, nl, y1, -y2, lo2 ? -f.t : f.t, i1, i2, f.ti, ab);
+        loc.off[li] = make_int4(ab.off[0], ab.off[1], ab.off[2], ab.off[3]);
+        loc.w[li] = make_float4(ab.w[0], ab.w[1], ab.w[2], ab.w[3]);
+        loc.sw[li] = make_float4(ab.sw[0], ab.sw[1], ab.sw[2], ab.sw[3]);
+        return bits;
+    }
+}
+
 // The t channel's eight site-local values of one node for one flow's state (make_desc's
 // local_pair of each local buffer, in the same order).
 __device__ __forceinline__ void group_local_values(const float2 *sd, const LocDesc &loc, float *lv) {
@@ -892,7 +940,8 @@ __global__ void __launch_bounds__(kThreads) su2_vertex_batch_kernel(BatchVertexA
 // the same 32-chunk schedule, each of the flow's W lanes walking chunks l, l + W, ...
 // ------------------------------------------------------------------------------------
 constexpr int kGroupWarps = 4;
-constexpr int kGroupChunk = 32;  // nodes whose supports the CTA builds at once
+constexpr int kGroupChunk = 32;  // nodes whose supports the CTA builds at once (four threads per node)
+static_assert(kGroupWarps * 32 == 4 * kGroupChunk, "the grouped kernel builds a chunk with four threads per node");
 
 // What a lane of a grouped warp needs of its flow (node_term reads a.sd and a.spin).
 struct GroupLaneArgs {
@@ -1093,12 +1142,19 @@ __global__ void __launch_bounds__(kGroupWarps * 32) su2_vertex_group_kernel(Grou
             for (int b0 = 0; b0 < cnt; b0 += kGroupChunk) {
                 const int nb = min(kGroupChunk, cnt - b0);
                 __syncthreads();  // the previous chunk is consumed
-                if (warp == 0) {
-                    if (lane < nb) make_supports<CH>(a, pos, f, __ldg(nwp + b0 + lane), desc[lane], loc[lane]);
-                } else {
-                    for (int p = tid - 32; p < nb * GMAX; p += blockDim.x - 32) {
-                        const int k = p / GMAX, q = p - k * GMAX;
-                        float c = __ldg(m_nc[q] + size_t(xi) * a.max_nodes + b0 + k);
+                {  // four threads per node build its supports (the CTA's 128 threads: 32 nodes)
+                    const int k = tid >> 2, q = tid & 3;
+                    int bits = 0;
+                    if (k < nb) bits = make_part<CH>(a, pos, f, __ldg(nwp + b0 + k), q, desc[k], loc[k]);
+                    bits |= __shfl_xor_sync(0xffffffffu, bits, 1);
+                    bits |= __shfl_xor_sync(0xffffffffu, bits, 2);
+                    if (k < nb && q == 0) {
+                        desc[k].exch = bits;
+                        desc[k].c = 0.0f;
+                    }
+                    for (int p = tid; p < nb * GMAX; p += blockDim.x) {
+                        const int kk = p / GMAX, qq = p - kk * GMAX;
+                        float c = __ldg(m_nc[qq] + size_t(xi) * a.max_nodes + b0 + kk);
                         if (CH == kU) c = -c;
                         ctab[p] = c;
                     }
