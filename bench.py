@@ -63,6 +63,10 @@ WORKLOADS = {
                           n_freq=32, fmin=0.005, fmax=50.0, cmax=50.0, cmin=0.05, cstep=0.98),
     "pyrochlore-r5-n64": dict(lattice="pyrochlore", range=5, model="pyrochlore-heisenberg", params={"j": "1.0"},
                               n_freq=64, fmin=0.002, fmax=100.0, cmax=100.0, cmin=0.01, cstep=0.99),
+    # the reference README's quick-start task (square r4, N = 32, cutoff 50 -> 0.1 x 0.95): the
+    # sanity check of the CPU timings against the one figure the reference publishes
+    "readme-square-r4-n32": dict(lattice="square", range=4, model="square-heisenberg", params={"j": "1.0"},
+                                 n_freq=32, fmin=0.005, fmax=50.0, cmax=50.0, cmin=0.1, cstep=0.95),
 }
 DEFAULT_WORKLOAD = "cubic-j1j2-r6-n64"
 # multi-flow workloads (spinparser_gb300/workloads.py): the seeded scan and the serving stream
@@ -120,6 +124,9 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-full-flow", action="store_true")
+    ap.add_argument("--cpu-full-flow", action="store_true",
+                    help="--impl reference: time the whole flow (every cutoff: RHS, measurement, Euler) on the "
+                         "host cores instead of sampled steps")
     return ap.parse_args()
 
 
@@ -313,6 +320,9 @@ def run_reference(args, wl):
         return
     tab, freq, cut = setup(wl)
     n = len(freq)
+    if args.cpu_full_flow:
+        run_reference_flow(args, wl, tab, freq, cut)
+        return
     step = CpuStep(tab, freq, tab.initial_state(n))
     schedule = sampled_steps(len(cut), args.warmup, args.steps)
     for _ in range(args.warmup):
@@ -341,6 +351,33 @@ def run_reference(args, wl):
             "lattice_tables": "built by the repository's lattice factory (input, pinned by the hyperkagome golden)",
             "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "wall_s": wall}
+    print(json.dumps(line))
+
+
+def run_reference_flow(args, wl, tab, freq, cut):
+    """The whole flow of the workload on the host cores, as the reference's loop runs it
+    (measurement at every cutoff, RHS, Euler), with the oracle built at the reference's flags;
+    wall time of the complete flow."""
+    from oracle import Oracle
+
+    orc = Oracle(tab, freq, timing=True)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    n_meas, _, _, _ = orc.flow(cut, *tab.initial_state(len(freq)), threads=threads)
+    secs = time.perf_counter() - t0
+    steps = n_meas - 1
+    info = cpu_info()
+    line = {"impl": "reference", "metric": METRIC, "value": steps / secs, "unit": "steps/s", "n_gpus": args.gpus,
+            "steps": steps, "warmup": 0, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (model initial condition, advanced by the flow)",
+            "config": workload_config(args, wl, tab, cut, len(freq)),
+            "cpu_baseline": {"value": steps / secs, "unit": "steps/s", "cores": threads, "kind": "port", **info,
+                             "build": CPU_BUILD,
+                             "sample": f"the whole flow: {len(cut)} cutoffs, {steps} RHS evaluations, measurement at "
+                                       f"every cutoff; {secs:.2f} s wall"},
+            "full_flow_seconds": secs,
+            "e2e": {"value": steps / secs, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
