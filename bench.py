@@ -410,6 +410,36 @@ def _cpu_flow_seconds(specs, steps_per_class):
     return total, samples, b
 
 
+def run_multi_reference(args):
+    """--impl reference for the scan and serving workloads: the CPU port's flows/s, rank 0 only.
+    Per (lattice, range, model, N) class of the seeded flows, the mean time of complete CPU
+    steps (full RHS, measurement, Euler) at cutoffs spread over the flow, times the flow's steps
+    and the class's flows (extrapolated to whole flows)."""
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    from spinparser_gb300 import workloads
+
+    scan = args.workload.startswith("scan")
+    n = args.flows or (128 if scan else 24)
+    specs = workloads.scan_specs(n) if scan else workloads.serve_specs(n)
+    t0 = time.perf_counter()
+    cpu_s, samples, b = _cpu_flow_seconds(specs, 2 if scan else 1)
+    wall = time.perf_counter() - t0
+    value = n / cpu_s
+    line = {"impl": "reference", "metric": "scan flows/s" if scan else "served flows/s", "value": value,
+            "unit": "flows/s", "n_gpus": args.gpus, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": args.workload, "flows": n, "seed": workloads.SEED},
+            "cpu_baseline": {"value": value, "unit": "flows/s", "cores": b["cores"], "kind": "port", "nproc": b["nproc"],
+                             "cpu_model": b["cpu_model"], "build": CPU_BUILD,
+                             "sample": "per (lattice, range, N): mean time of %d complete CPU steps spread over the "
+                                       "flow, x its steps (extrapolated); " % (2 if scan else 1) + "; ".join(samples)},
+            "cpu_seconds_for_all_flows": cpu_s,
+            "e2e": {"value": value, "unit": "flows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": wall}
+    print(json.dumps(line))
+
+
 def _by_class(specs, secs):
     """Total seconds and flow count per (lattice, range, N) class."""
     out = {}
@@ -752,7 +782,10 @@ def main():
         run_xyz(args)
         return
     if args.workload in MULTI_WORKLOADS:
-        run_multi(args)
+        if args.impl == "reference":
+            run_multi_reference(args)
+        else:
+            run_multi(args)
         return
     if args.workload in PRECISION_WORKLOADS:
         run_precision(args)
