@@ -165,6 +165,39 @@ __device__ __forceinline__ void tri_access4(const M &m, int nl, float s, float t
     ab.fl = fl;
 }
 
+// tri_access4 with the two interpolations given (interp_abs of the interpolated coordinates,
+// as for access4i): a node's buffers interpolate four distinct magnitudes, each looked up once.
+template <int CH>
+__device__ __forceinline__ void tri_access4i(int n, int nl, float s, float t, float u, int e, const Interp<float> &ia,
+                                             const Interp<float> &ib, TAB4 &ab) {
+    int fl = tri_fold(s, t, u);
+    const int step_t = 16 * nl, step_su = n * step_t;
+    const int la = ia.lo, ua = ia.hi, lb = ib.lo, ub = ib.hi;
+    const float ba = ia.b, bb = ib.b;
+    const float na = rn_sub(1.0f, ba), nb = rn_sub(1.0f, bb);
+    ab.w[0] = rn_mul(nb, na);
+    ab.w[1] = rn_mul(nb, ba);
+    ab.w[2] = rn_mul(bb, na);
+    ab.w[3] = rn_mul(bb, ba);
+    if (CH == kS) {
+        tri_slab(e, la, lb, step_su, step_t, 0, ab.off[0], fl);
+        tri_slab(e, ua, lb, step_su, step_t, 1, ab.off[1], fl);
+        tri_slab(e, la, ub, step_su, step_t, 2, ab.off[2], fl);
+        tri_slab(e, ua, ub, step_su, step_t, 3, ab.off[3], fl);
+    } else if (CH == kT) {
+        tri_slab(la, e, lb, step_su, step_t, 0, ab.off[0], fl);
+        tri_slab(ua, e, lb, step_su, step_t, 1, ab.off[1], fl);
+        tri_slab(la, e, ub, step_su, step_t, 2, ab.off[2], fl);
+        tri_slab(ua, e, ub, step_su, step_t, 3, ab.off[3], fl);
+    } else {
+        tri_slab(la, lb, e, step_su, step_t, 0, ab.off[0], fl);
+        tri_slab(ua, lb, e, step_su, step_t, 1, ab.off[1], fl);
+        tri_slab(la, ub, e, step_su, step_t, 2, ab.off[2], fl);
+        tri_slab(ua, ub, e, step_su, step_t, 3, ab.off[3], fl);
+    }
+    ab.fl = fl;
+}
+
 // generateAccessBuffer(s, t, u): trilinear (TRIVertexTwoParticle.hpp:514-584)
 __device__ __forceinline__ void tri_access8(const float *pos, int n, int nl, float s, float t, float u, TAB8 &ab) {
     int fl = tri_fold(s, t, u);
@@ -314,26 +347,46 @@ struct __align__(16) TDesc {
 __device__ __forceinline__ void make_tdesc(const TriArgs &a, const float *pos, int ch, int e, float s, float t, float u,
                                            float w1p, float w1, float w2p, float w2, float wp, float c, TDesc &d) {
     const MeshSearch<float> m{pos, a.n};
-    const int nl = a.nl;
+    const int nl = a.nl, n = a.n;
+    // each pair of buffers interpolates two of the node's four distinct magnitudes (a
+    // coordinate and its negation fold alike; -a - b is bitwise -(a + b), -a + b is b - a)
     if (ch == 0) {  // integralKernelS, TRIFrgCore.cpp:184-188
-        tri_access4<kS>(m, nl, s, w2 + wp, w1 + wp, e, d.ab[0]);
-        tri_access4<kS>(m, nl, s, -w2p - wp, w1p + wp, e, d.ab[1]);
-        tri_access4<kS>(m, nl, s, -w1 - wp, -w2 - wp, e, d.ab[2]);
-        tri_access4<kS>(m, nl, s, w1p + wp, -w2p - wp, e, d.ab[3]);
+        {
+            const Interp<float> iA = interp_abs(m, w1 + wp), iB = interp_abs(m, w2 + wp);
+            tri_access4i<kS>(n, nl, s, w2 + wp, w1 + wp, e, iB, iA, d.ab[0]);
+            tri_access4i<kS>(n, nl, s, -w1 - wp, -w2 - wp, e, iA, iB, d.ab[2]);
+        }
+        {
+            const Interp<float> iP = interp_abs(m, w1p + wp), iQ = interp_abs(m, w2p + wp);
+            tri_access4i<kS>(n, nl, s, -w2p - wp, w1p + wp, e, iQ, iP, d.ab[1]);
+            tri_access4i<kS>(n, nl, s, w1p + wp, -w2p - wp, e, iP, iQ, d.ab[3]);
+        }
     } else if (ch == 1) {  // integralKernelT, TRIFrgCore.cpp:718-724, 1257-1259, 1814-1816
-        tri_access4<kT>(m, nl, w1 - wp, t, w1p + wp, e, d.ab[0]);
-        tri_access4<kT>(m, nl, w2p - wp, t, -w2 - wp, e, d.ab[1]);
-        tri_access4<kT>(m, nl, w1p + wp, t, w1 - wp, e, d.ab[2]);
-        tri_access4<kT>(m, nl, w2 + wp, t, -w2p + wp, e, d.ab[3]);
-        tri_access4<kU>(m, nl, w2p - wp, -w2 - wp, t, e, d.ab[4]);
-        tri_access4<kU>(m, nl, w2 + wp, -w2p + wp, t, e, d.ab[5]);
-        tri_access4<kU>(m, nl, w1 - wp, -w1p - wp, -t, e, d.ab[6]);
-        tri_access4<kU>(m, nl, w1p + wp, -w1 + wp, -t, e, d.ab[7]);
+        {
+            const Interp<float> iC = interp_abs(m, w1 - wp), iP = interp_abs(m, w1p + wp);
+            tri_access4i<kT>(n, nl, w1 - wp, t, w1p + wp, e, iC, iP, d.ab[0]);
+            tri_access4i<kT>(n, nl, w1p + wp, t, w1 - wp, e, iP, iC, d.ab[2]);
+            tri_access4i<kU>(n, nl, w1 - wp, -w1p - wp, -t, e, iC, iP, d.ab[6]);
+            tri_access4i<kU>(n, nl, w1p + wp, -w1 + wp, -t, e, iP, iC, d.ab[7]);
+        }
+        {
+            const Interp<float> iD = interp_abs(m, w2p - wp), iB = interp_abs(m, w2 + wp);
+            tri_access4i<kT>(n, nl, w2p - wp, t, -w2 - wp, e, iD, iB, d.ab[1]);
+            tri_access4i<kT>(n, nl, w2 + wp, t, -w2p + wp, e, iB, iD, d.ab[3]);
+            tri_access4i<kU>(n, nl, w2p - wp, -w2 - wp, t, e, iD, iB, d.ab[4]);
+            tri_access4i<kU>(n, nl, w2 + wp, -w2p + wp, t, e, iB, iD, d.ab[5]);
+        }
     } else {  // integralKernelU, TRIFrgCore.cpp:2375-2379
-        tri_access4<kU>(m, nl, w1 + wp, -w2p + wp, u, e, d.ab[0]);
-        tri_access4<kU>(m, nl, w1p + wp, w2 - wp, u, e, d.ab[1]);
-        tri_access4<kU>(m, nl, w2p - wp, -w1 - wp, u, e, d.ab[2]);
-        tri_access4<kU>(m, nl, w2 - wp, w1p + wp, u, e, d.ab[3]);
+        {
+            const Interp<float> iA = interp_abs(m, w1 + wp), iD = interp_abs(m, w2p - wp);
+            tri_access4i<kU>(n, nl, w1 + wp, -w2p + wp, u, e, iA, iD, d.ab[0]);
+            tri_access4i<kU>(n, nl, w2p - wp, -w1 - wp, u, e, iD, iA, d.ab[2]);
+        }
+        {
+            const Interp<float> iP = interp_abs(m, w1p + wp), iE = interp_abs(m, w2 - wp);
+            tri_access4i<kU>(n, nl, w1p + wp, w2 - wp, u, e, iP, iE, d.ab[1]);
+            tri_access4i<kU>(n, nl, w2 - wp, w1p + wp, u, e, iE, iP, d.ab[3]);
+        }
     }
     d.c = c;
 }

@@ -219,28 +219,48 @@ __device__ __forceinline__ void put_desc(XDesc &d, int i, const AB4 &ab) {
 __device__ __forceinline__ void make_xdesc(const XyzArgs &a, const float *pos, int ch, int e, float s, float t, float u,
                                            float w1p, float w1, float w2p, float w2, float wp, float c, XDesc &d) {
     const MeshSearch<float> m{pos, a.n};
-    const int nl = a.nl;
+    const int nl = a.nl, n = a.n;
     AB4 ab;
     int ex = 0;
+    // each pair of buffers interpolates two of the node's four distinct magnitudes (a
+    // coordinate and its negation fold alike; -a - b is bitwise -(a + b))
     if (ch == 0) {  // integralKernelS, XYZFrgCore.cpp:218-224
-        access4m<kS>(m, nl, s, -w1 - wp, -w2 - wp, ab, e); put_desc(d, 0, ab); ex |= ab.exch << 0;
-        access4m<kS>(m, nl, s, w1p + wp, -w2p - wp, ab, e); put_desc(d, 1, ab); ex |= ab.exch << 1;
-        access4m<kS>(m, nl, s, w2 + wp, w1 + wp, ab, e); put_desc(d, 2, ab); ex |= ab.exch << 2;
-        access4m<kS>(m, nl, s, -w2p - wp, w1p + wp, ab, e); put_desc(d, 3, ab); ex |= ab.exch << 3;
+        {
+            const Interp<float> iA = interp_abs(m, w1 + wp), iB = interp_abs(m, w2 + wp);
+            access4i<kS>(n, nl, s, -w1 - wp, -w2 - wp, iA, iB, e, ab); put_desc(d, 0, ab); ex |= ab.exch << 0;
+            access4i<kS>(n, nl, s, w2 + wp, w1 + wp, iB, iA, e, ab); put_desc(d, 2, ab); ex |= ab.exch << 2;
+        }
+        {
+            const Interp<float> iP = interp_abs(m, w1p + wp), iQ = interp_abs(m, w2p + wp);
+            access4i<kS>(n, nl, s, w1p + wp, -w2p - wp, iP, iQ, e, ab); put_desc(d, 1, ab); ex |= ab.exch << 1;
+            access4i<kS>(n, nl, s, -w2p - wp, w1p + wp, iQ, iP, e, ab); put_desc(d, 3, ab); ex |= ab.exch << 3;
+        }
     } else if (ch == 1) {  // integralKernelT, XYZFrgCore.cpp:268-276, 323-345
-        access4m<kT>(m, nl, w1 - wp, t, w1p + wp, ab, e); put_desc(d, 0, ab); ex |= ab.exch << 0;
-        access4m<kT>(m, nl, w2p - wp, t, -w2 - wp, ab, e); put_desc(d, 1, ab); ex |= ab.exch << 1;
-        access4m<kT>(m, nl, w1p + wp, t, w1 - wp, ab, e); put_desc(d, 2, ab); ex |= ab.exch << 2;
-        access4m<kT>(m, nl, w2 + wp, t, wp - w2p, ab, e); put_desc(d, 3, ab); ex |= ab.exch << 3;
-        access4m<kU>(m, nl, w2p - wp, -w2 - wp, t, ab, e); d.lv[0] = local4(a, ab);
-        access4m<kU>(m, nl, w1 - wp, -w1p - wp, -t, ab, e); d.lv[1] = local4(a, ab);
-        access4m<kU>(m, nl, w2 + wp, wp - w2p, t, ab, e); d.lv[2] = local4(a, ab);
-        access4m<kU>(m, nl, w1p + wp, wp - w1, -t, ab, e); d.lv[3] = local4(a, ab);
+        {
+            const Interp<float> iC = interp_abs(m, w1 - wp), iP = interp_abs(m, w1p + wp);
+            access4i<kT>(n, nl, w1 - wp, t, w1p + wp, iC, iP, e, ab); put_desc(d, 0, ab); ex |= ab.exch << 0;
+            access4i<kT>(n, nl, w1p + wp, t, w1 - wp, iP, iC, e, ab); put_desc(d, 2, ab); ex |= ab.exch << 2;
+            access4i<kU>(n, nl, w1 - wp, -w1p - wp, -t, iC, iP, e, ab); d.lv[1] = local4(a, ab);
+            access4i<kU>(n, nl, w1p + wp, wp - w1, -t, iP, iC, e, ab); d.lv[3] = local4(a, ab);
+        }
+        {
+            const Interp<float> iD = interp_abs(m, w2p - wp), iB = interp_abs(m, w2 + wp);
+            access4i<kT>(n, nl, w2p - wp, t, -w2 - wp, iD, iB, e, ab); put_desc(d, 1, ab); ex |= ab.exch << 1;
+            access4i<kT>(n, nl, w2 + wp, t, wp - w2p, iB, iD, e, ab); put_desc(d, 3, ab); ex |= ab.exch << 3;
+            access4i<kU>(n, nl, w2p - wp, -w2 - wp, t, iD, iB, e, ab); d.lv[0] = local4(a, ab);
+            access4i<kU>(n, nl, w2 + wp, wp - w2p, t, iB, iD, e, ab); d.lv[2] = local4(a, ab);
+        }
     } else {  // integralKernelU, XYZFrgCore.cpp:424-430
-        access4m<kU>(m, nl, w1 + wp, wp - w2p, u, ab, e); put_desc(d, 0, ab); ex |= ab.exch << 0;
-        access4m<kU>(m, nl, w1p + wp, w2 - wp, u, ab, e); put_desc(d, 1, ab); ex |= ab.exch << 1;
-        access4m<kU>(m, nl, w2p - wp, -w1 - wp, u, ab, e); put_desc(d, 2, ab); ex |= ab.exch << 2;
-        access4m<kU>(m, nl, w2 - wp, w1p + wp, u, ab, e); put_desc(d, 3, ab); ex |= ab.exch << 3;
+        {
+            const Interp<float> iA = interp_abs(m, w1 + wp), iD = interp_abs(m, w2p - wp);
+            access4i<kU>(n, nl, w1 + wp, wp - w2p, u, iA, iD, e, ab); put_desc(d, 0, ab); ex |= ab.exch << 0;
+            access4i<kU>(n, nl, w2p - wp, -w1 - wp, u, iD, iA, e, ab); put_desc(d, 2, ab); ex |= ab.exch << 2;
+        }
+        {
+            const Interp<float> iP = interp_abs(m, w1p + wp), iE = interp_abs(m, w2 - wp);
+            access4i<kU>(n, nl, w1p + wp, w2 - wp, u, iP, iE, e, ab); put_desc(d, 1, ab); ex |= ab.exch << 1;
+            access4i<kU>(n, nl, w2 - wp, w1p + wp, u, iE, iP, e, ab); put_desc(d, 3, ab); ex |= ab.exch << 3;
+        }
     }
     d.exch = ex;
     d.c = c;
