@@ -116,6 +116,10 @@ def parse_args():
     ap.add_argument("--grouping", choices=["auto", "off"], default="auto",
                     help="scan/serve: batch configuration chosen by the batch autotuner (auto) or the per-flow "
                          "kernel without cross-flow sharing (off)")
+    ap.add_argument("--profile-window", type=str, default=None,
+                    help="scan/serve: START,COUNT -- run the batch alone (no plain arm, no graph replay) for START "
+                         "steps, then COUNT steps inside an NVTX range 'batch_steps' (for ncu --nvtx-include), "
+                         "print their time and exit")
     ap.add_argument("--flow-cutoffs", type=int, default=None,
                     help="XYZ/TRI workloads: run only the first M cutoffs of the flow (short runs for profiling)")
     ap.add_argument("--precision", choices=["fp64-self-energy", "plain"], default="fp64-self-energy",
@@ -408,6 +412,45 @@ def _cpu_flow_seconds(specs, steps_per_class):
         total += t_step * (len(cut) - 1) * len(members)
         samples.append(f"{lat} r{rng_} N{n}: {t_step:.3f} s/step x {len(members)}")
     return total, samples, b
+
+
+def run_batch_window(args):
+    """The batch of the scan or serving workload's flows (all admitted at once), steps START ..
+    START + COUNT - 1 inside an NVTX range 'batch_steps'; no graph replay, so every kernel is a
+    plain launch that a profiler sees by name."""
+    import torch
+
+    from spinparser_gb300 import workloads
+    from spinparser_gb300.batch import Su2Batch
+
+    start, count = (int(x) for x in args.profile_window.split(","))
+    scan = args.workload.startswith("scan")
+    n = args.flows or (128 if scan else 24)
+    specs = workloads.scan_specs(n) if scan else workloads.serve_specs(n)
+    torch.cuda.set_device(0)
+    b = Su2Batch(use_graph=False)
+    for sp in specs:
+        tab, freq, cut = sp.build()
+        b.add(tab, freq, cut, flags=sp.flags)
+    tune = None
+    if args.grouping == "off":
+        b.set_grouping(0)
+    else:
+        tune = b.autotune(1)
+    for _ in range(start):
+        b.step()
+    b.synchronize()
+    torch.cuda.nvtx.range_push("batch_steps")
+    t0 = time.perf_counter()
+    for _ in range(count):
+        b.step()
+    b.synchronize()
+    secs = time.perf_counter() - t0
+    torch.cuda.nvtx.range_pop()
+    print(json.dumps({"workload": args.workload, "flows": n, "grouping": args.grouping, "autotune": tune,
+                      "grouped_flows": b.grouped_flows(), "window": [start, count], "seconds": secs,
+                      "ms_per_step": 1e3 * secs / max(count, 1)}))
+    b.close()
 
 
 def run_multi_reference(args):
@@ -782,7 +825,9 @@ def main():
         run_xyz(args)
         return
     if args.workload in MULTI_WORKLOADS:
-        if args.impl == "reference":
+        if args.profile_window:
+            run_batch_window(args)
+        elif args.impl == "reference":
             run_multi_reference(args)
         else:
             run_multi(args)
