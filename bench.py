@@ -113,9 +113,9 @@ def parse_args():
                     help="serve-mixed: server arms to run at every rate, comma separated: fifo or sjf, optionally @k "
                          "for a k-flow residency limit, or srpt@k (k flows with the least remaining work run at each "
                          "step), e.g. fifo,sjf@2,srpt@1")
-    ap.add_argument("--grouping", choices=["auto", "off"], default="auto",
-                    help="scan/serve: batch configuration chosen by the batch autotuner (auto) or the per-flow "
-                         "kernel without cross-flow sharing (off)")
+    ap.add_argument("--grouping", choices=["auto", "on", "off"], default="auto",
+                    help="scan/serve: batch configuration chosen by the batch autotuner (auto), cross-flow sharing "
+                         "for every group of >= 2 flows (on), or the per-flow kernel without sharing (off)")
     ap.add_argument("--profile-window", type=str, default=None,
                     help="scan/serve: START,COUNT -- run the batch alone (no plain arm, no graph replay) for START "
                          "steps, then COUNT steps inside an NVTX range 'batch_steps' (for ncu --nvtx-include), "
@@ -435,6 +435,8 @@ def run_batch_window(args):
     tune = None
     if args.grouping == "off":
         b.set_grouping(0)
+    elif args.grouping == "on":
+        b.set_grouping(2)
     else:
         tune = b.autotune(1)
     for _ in range(start):
@@ -511,6 +513,8 @@ def _serve_local(items, arrivals, policy, plain, grouping="auto"):
     srv = FlowServer(policy=name, max_flows=int(slots) if slots else None, autotune=(grouping == "auto"))
     if grouping == "off":
         srv.batch.set_grouping(0)
+    elif grouping == "on":
+        srv.batch.set_grouping(2)
     order = sorted(range(len(items)), key=lambda j: arrivals[items[j][0]])
     t0 = time.perf_counter()
     tickets, k = {}, 0
