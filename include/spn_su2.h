@@ -316,8 +316,8 @@ int spn_batch_set_variant(spn_batch *b, int npi, int use_graph);
  * lattice tables, spin length and cutoff list and stand at the same cutoff (a parameter scan's
  * flows of one lattice, range and frequency count, admitted together) have the same
  * loop-frequency nodes and interpolation supports; groups of at least min_group such flows
- * (0 = off; default 2) are evaluated by a kernel that builds each node's supports once per
- * subgroup and evaluates them for all its flows.  Subgroups hold at most the kernel's flows
+ * (0 = off, the default; spn_batch_autotune may switch it on) are evaluated by a kernel that
+ * builds each node's supports once per subgroup and evaluates them for all its flows.  Subgroups hold at most the kernel's flows
  * per block divided by cap_divisor (1, 2 or 4; default 1).  No counterpart in the reference,
  * which runs one flow per process.  Results are bit-identical to the per-flow kernel's. */
 int spn_batch_set_grouping(spn_batch *b, int min_group, int cap_divisor);

@@ -172,7 +172,7 @@ struct spn_batch {
     bool use_graph = true;
     // grouped vertex flow: groups of at least min_group flows (0 = off) share node supports,
     // in subgroups of at most gmax / group_cap_div flows per CTA
-    int min_group = 2, group_cap_div = 1;
+    int min_group = 0, group_cap_div = 1;
     bool stage_sched = false;  // per-flow kernel: each warp stages its flow's RPA schedule in shared memory
     int next_share_id = 0;
     cudaStream_t stream = nullptr;

@@ -114,7 +114,7 @@ def next_ticket(queue, policy: str, now: float | None = None, max_wait: float | 
 class FlowServer:
     def __init__(self, device: int = 0, memory_budget: int | None = None, max_flows: int | None = None,
                  nodes_per_iteration: int = 1, use_graph: bool = True, clock=time.perf_counter, policy: str = "fifo",
-                 max_wait: float | None = None, autotune: bool = False, autotune_interval: int = 20):
+                 max_wait: float | None = None, autotune: bool = False, autotune_interval: int = 50):
         if policy not in ("fifo", "sjf", "srpt"):
             raise ValueError("policy must be 'fifo', 'sjf' or 'srpt'")
         self.policy = policy
@@ -125,12 +125,14 @@ class FlowServer:
         if policy == "srpt":
             max_flows = None
         self._paused: set[int] = set()
-        # batch autotuner: re-run when the set of running flows changed, at most every
-        # autotune_interval steps
+        # batch autotuner: run once a set of running flows has stepped together for
+        # autotune_interval steps (the first steps of a flow, at large cutoffs, have few
+        # loop-frequency nodes and do not show which configuration wins later)
         self.autotune = autotune
         self.autotune_interval = autotune_interval
         self._tuned_set: frozenset | None = None
-        self._tuned_at = -10 ** 9
+        self._seen_set: frozenset | None = None
+        self._set_since = 0
         self.tunings: list[dict] = []
         self.batch = Su2Batch(device, nodes_per_iteration, use_graph)
         if memory_budget is None:
@@ -211,9 +213,11 @@ class FlowServer:
                 self._choose_running()
             if self.autotune:
                 running = frozenset(f for f in self.active if f not in self._paused)
-                if running != self._tuned_set and self.steps - self._tuned_at >= self.autotune_interval:
+                if running != self._seen_set:
+                    self._seen_set, self._set_since = running, self.steps
+                if running != self._tuned_set and self.steps - self._set_since >= self.autotune_interval:
                     self.tunings.append({"step": self.steps, "flows": len(running), **self.batch.autotune(1)})
-                    self._tuned_set, self._tuned_at = running, self.steps
+                    self._tuned_set = running
             self.batch.step()
             self.steps += 1
             self._retire()

@@ -97,6 +97,7 @@ def test_grouped_flows_equal_flows_alone(cap_divisor, use_graph):
 def test_group_with_diverging_first_member():
     cut = spn.cutoff_exponential(*CUT)
     b = Su2Batch()
+    b.set_grouping(2)
     specs = [(5, j2, 8) for j2 in (0.1, 0.3, 0.5, 0.7, 0.9)]
     ids = [add(b, *sp, cut, poison=(i == 0)) for i, sp in enumerate(specs)]
     assert b.grouped_flows() == 5
@@ -112,6 +113,7 @@ def test_late_joiners_and_other_cutoff_lists_are_not_grouped_with_running_flows(
     cut = spn.cutoff_exponential(*CUT)
     other = spn.cutoff_exponential(20.0, 1.0, 0.8)
     b = Su2Batch()
+    b.set_grouping(2)
     first = [(3, j2, 10) for j2 in (0.2, 0.4, 0.6)]
     ids = [add(b, *sp, cut) for sp in first]
     fid_other = add(b, 3, 0.5, 10, other)
