@@ -66,20 +66,23 @@ def test_rhs_square_r3_n32_matches_oracle(square_r3):
     assert not flow.is_diverged()
 
 
-@pytest.mark.parametrize("lattice,rng,model,params", [
-    ("square", 3, "square-heisenberg", {"j": "1.0"}),
-    ("cubic", 3, "cubic-j1j2heisenberg", {"j1": "1.0", "j2": "0.25"}),
+@pytest.mark.parametrize("lattice,rng,model,params,n", [
+    ("square", 3, "square-heisenberg", {"j": "1.0"}, 14),
+    ("cubic", 3, "cubic-j1j2heisenberg", {"j1": "1.0", "j2": "0.25"}, 14),
+    ("square", 11, "square-heisenberg", {"j": "1.0"}, 8),   # 42 sites: two per lane, per-node pair walk
+    ("square", 15, "square-heisenberg", {"j": "1.0"}, 6),   # 72 sites: four per lane
 ])
-def test_every_vertex_variant_matches_oracle(lattice, rng, model, params):
+def test_every_vertex_variant_matches_oracle(lattice, rng, model, params, n):
     """Each kernel variant the autotuner may pick (1 or 2 nodes per site-group iteration, RPA
     schedule in shared or global memory) reproduces the oracle, and all variants give the
     same bits (a group takes its nodes in the same order whatever the variant), so autotuning
-    never changes a result."""
+    never changes a result.  Lattices of 6, 8, 42 and 72 sites cover one, two and four sites
+    per lane (outer-product RPA up to 32 sites, a pair walk per node above)."""
     tab = spn.Lattice(lattice, rng, model, params).tables()
-    freq = spn.frequency_exponential(0.01, 30.0, 14)
+    freq = spn.frequency_exponential(0.01, 30.0, n)
     orc = Oracle(tab, freq)
     cut = np.array([3.0, 2.0, 1.0, 0.4], np.float32)
-    c, v2, ss, dd = oracle_state(orc, cut, *tab.initial_state(14), steps=2)
+    c, v2, ss, dd = oracle_state(orc, cut, *tab.initial_state(n), steps=2)
     r2, rss, rdd = orc.rhs(c, v2, ss, dd)
     flow = spn.Su2Flow(tab, freq)
     flow.set_state(float(c), v2, ss, dd)
