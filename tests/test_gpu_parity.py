@@ -87,9 +87,15 @@ def test_every_vertex_variant_matches_oracle(lattice, rng, model, params, n):
     flow = spn.Su2Flow(tab, freq)
     flow.set_state(float(c), v2, ss, dd)
     first = None
+    ran = 0
     for npi in (1, 2):
         for sm in (False, True):
-            flow.set_variant(npi, sm)
+            try:
+                flow.set_variant(npi, sm)
+            except spn.SpnError as e:  # a variant whose shared memory does not fit this lattice
+                assert e.code == -8, e
+                continue
+            ran += 1
             flow.compute_step()
             g2, gss, gdd = flow.get_flow()
             assert normwise(gss, rss) <= RHS_TOL, (npi, sm)
@@ -97,6 +103,7 @@ def test_every_vertex_variant_matches_oracle(lattice, rng, model, params, n):
             if first is None:
                 first = (gss.copy(), gdd.copy())
             assert np.array_equal(gss, first[0]) and np.array_equal(gdd, first[1]), (npi, sm)
+    assert ran >= 2
     choice = flow.autotune(2)
     assert choice["nodes_per_iteration"] in (1, 2) and choice["grid"] > 0
     flow.compute_step()
