@@ -193,6 +193,7 @@ struct spn_batch {
     // per vertex class (vertex_class): work lists, prefixes, shared memory, grid
     int off_cv[kVertexClasses] = {}, n_cv[kVertexClasses] = {}, off_cp[kVertexClasses] = {}, total_cv[kVertexClasses] = {};
     int warp_area[kVertexClasses] = {}, nl_max = 1, vgrid[kVertexClasses] = {}, sched_ints[kVertexClasses] = {};
+    int nseg_v[kVertexClasses] = {};  // classes 6-8: the largest RPA segment count of the list
     // per grouped class: subgroup member table, item prefix, grid
     int off_gm[kGroupClasses] = {}, off_gp[kGroupClasses] = {}, n_sg[kGroupClasses] = {}, total_g[kGroupClasses] = {};
     int nseg_g[kGroupClasses] = {}, ggrid[kGroupClasses] = {};
@@ -352,23 +353,27 @@ struct spn_batch {
             n_cv[c] = int(cv[c].size());
             std::vector<int> prefix(1, 0);
             size_t area = 0;
-            int sched = 0;
+            int sched = 0, nseg = 0;
             for (int i : cv[c]) {
                 const spn_su2 *h = flows[i].h;
                 const long long next = prefix.back() + h->fn;
                 if (next >= (1ll << 31)) throw Error(ErrorType::Unsupported, "batch work list beyond 2^31 items");
                 prefix.push_back(int(next));
-                area = std::max(area, batch_vertex_warp_area(h->nl, h->rpa_n_seg, npi));
+                if (c < 6) area = std::max(area, batch_vertex_warp_area(h->nl, h->rpa_n_seg, npi));
                 sched = std::max(sched, rpa_smem_ints(h->args().rpa, h->nl));
+                nseg = std::max(nseg, h->rpa_n_seg);
             }
+            nseg_v[c] = nseg;
             off_cp[c] = put(prefix);
             total_cv[c] = prefix.back();
             warp_area[c] = int((area + 15) / 16 * 16);
-            // each warp stages its flow's RPA schedule when the largest one is small
-            sched_ints[c] = (stage_sched && sched <= kBatchSchedMaxInts) ? sched : 0;
+            // each warp stages its flow's RPA schedule when the largest one is small (warp-per-
+            // triple classes; the CTA-per-triple classes 6-8 read it from global memory)
+            sched_ints[c] = (c < 6 && stage_sched && sched <= kBatchSchedMaxInts) ? sched : 0;
             vgrid[c] = 0;
             if (n_cv[c] > 0) {
-                const size_t smem = batch_vertex_smem_bytes(n_max, warp_area[c], sched_ints[c]);
+                const size_t smem = c >= 6 ? batch_big_smem_bytes(c, nseg_v[c])
+                                           : batch_vertex_smem_bytes(n_max, warp_area[c], sched_ints[c]);
                 const int per_sm = batch_vertex_blocks_per_sm(c, npi, smem);
                 cudaGetLastError();
                 if (per_sm < 1) throw Error(ErrorType::Unsupported, "batched vertex-flow kernel does not fit for this batch");
@@ -438,6 +443,7 @@ struct spn_batch {
                 b.counter = d_counters + c;
                 b.warp_area = warp_area[c];
                 b.sched_ints = sched_ints[c];
+                b.n_seg_max = nseg_v[c];
                 launch_batch_vertex(b, c, npi, vgrid[c], stream);
             }
             for (int c = 0; c < kGroupClasses; ++c) {

@@ -131,6 +131,7 @@ struct BatchVertexArgs {
     int *counter;
     int warp_area;
     int sched_ints;
+    int n_seg_max;  // classes 6-8 (CTA per triple): the largest RPA segment count of the list
 };
 // Grouped batches (flows sharing mesh, lattice tables and cutoff; see su2_vertex.cu): one
 // persistent launch per vertex class 0..3 over (subgroup, triple) items.  A subgroup holds up
@@ -155,8 +156,11 @@ int batch_vertex_blocks_per_sm(int cls, int npi, size_t smem);
 void launch_batch_vertex(const BatchVertexArgs &b, int cls, int npi, int grid, cudaStream_t stream);
 int vertex_spt(int nl);  // sites per lane of a flow with nl sites
 // Vertex-kernel class of a flow (one kernel instance per class): 0-3 for nl <= 32 (outer-product
-// RPA with w = 8, 16, 24, 32), 4 for 2 sites per lane, 5 for 4.
-constexpr int kVertexClasses = 6;
+// RPA with w = 8, 16, 24, 32, a warp per triple), 6-8 for 33 <= nl <= 80 (outer-product RPA with
+// w = 48, 64, 80, a CTA per triple), 5 for 81 <= nl <= 128 (four sites per lane, an RPA pair
+// walk per node); 4 (two sites per lane, pair walk) is not chosen any more.
+constexpr int kVertexClasses = 9;
 int vertex_class(int nl);
+size_t batch_big_smem_bytes(int cls, int n_seg_max);
 
 }  // namespace spn

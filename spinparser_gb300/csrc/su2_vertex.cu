@@ -345,7 +345,9 @@ struct NodeView {
 // K_X at NPI nodes for this lane's sites (one group evaluates NPI nodes per iteration so that
 // the t channel decodes each RPA schedule entry once for all of them).  `a` provides the
 // state (a.sd), the spin length and, for SPT > 1, the RPA schedule.
-template <int CH, int SPT, int NPI, class A>
+// PANEL: the t channel writes the node's panel (c * third slab, fourth slab) for every site of
+// the lane instead of walking the RPA pair list (the outer-product forms; always so for Nl <= 32).
+template <int CH, int SPT, int NPI, class A, bool PANEL = false>
 __device__ __forceinline__ void node_term(const A &a, const NodeView *v, const Lane<SPT> &ln, int jl,
                                           const TExchange *tx, float (*rs)[SPT], float (*rd)[SPT]) {
     float S0[NPI][SPT], S1[NPI][SPT], S2[NPI][SPT], S3[NPI][SPT], D0[NPI][SPT], D1[NPI][SPT], D2[NPI][SPT],
@@ -388,18 +390,20 @@ __device__ __forceinline__ void node_term(const A &a, const NodeView *v, const L
         return;
     }
     // t channel: RPA lattice sum (SU2FrgCore.cpp:249-266)
-    if constexpr (SPT == 1) {
-        // outer-product form: the node's panel (c * third slab, fourth slab); channel_sum adds
-        // the panels' outer products to the warp's M accumulators after the trip
-        if (ln.valid[0]) {
-            const int j = ln.j[0];
+    if constexpr (SPT == 1 || PANEL) {
+        // outer-product form: the node's panel (c * third slab, fourth slab); the caller adds
+        // the panels' outer products to its M accumulators
 #pragma unroll
-            for (int n = 0; n < NPI; ++n) {
-                const float c = v[n].c;
-                tx[n].A2[j] = make_float2(c * S2[n][0], c * D2[n][0]);
-                tx[n].B2[j] = make_float2(S3[n][0], D3[n][0]);
+        for (int k = 0; k < SPT; ++k)
+            if (ln.valid[k]) {
+                const int j = ln.j[k];
+#pragma unroll
+                for (int n = 0; n < NPI; ++n) {
+                    const float c = v[n].c;
+                    tx[n].A2[j] = make_float2(c * S2[n][k], c * D2[n][k]);
+                    tx[n].B2[j] = make_float2(S3[n][k], D3[n][k]);
+                }
             }
-        }
     } else {
 #pragma unroll
         for (int n = 0; n < NPI; ++n)
@@ -449,7 +453,7 @@ __device__ __forceinline__ void node_term(const A &a, const NodeView *v, const L
 #pragma unroll
         for (int k = 0; k < SPT; ++k) {
             float rpa_s = 0.0f, rpa_d = 0.0f;
-            if (SPT != 1 && ln.valid[k]) {  // Nl > 32 (for Nl <= 32 the RPA term enters once per triple)
+            if (SPT != 1 && !PANEL && ln.valid[k]) {  // the per-node walk (outer-product forms: once per triple)
                 const int r = ln.j[k];
                 const int s0 = tx[0].seg_ptr[r], s1 = tx[0].seg_ptr[r + 1];
                 for (int q = s0; q < s1; ++q) {
@@ -480,7 +484,7 @@ __device__ __forceinline__ void node_term(const A &a, const NodeView *v, const L
             rd[n][k] = y;
         }
     }
-    if (SPT != 1) __syncwarp();
+    if (SPT != 1 && !PANEL) __syncwarp();
 }
 
 // Adds the outer products of the panels of nodes k = (r*NPI+n)*G+gg < nb (ascending k) to the
@@ -1257,6 +1261,277 @@ __global__ void __launch_bounds__(kGroupWarps * 32) su2_vertex_group_kernel(Grou
     }
 }
 
+// ------------------------------------------------------------------------------------
+// Lattices of 33 to 80 sites: one CTA per triple (su2_vertex_big_kernel<R>).
+//
+// Above 32 sites the t channel's outer-product matrix M = sum over nodes of (c A) x B (w x w,
+// w = 16 R >= Nl) no longer fits one warp's registers, and a warp that owns a triple walks the
+// whole merged RPA pair list for every t-channel node (585 entries per lane and node for the
+// 70-site pyrochlore range 7).  Here the CTA's 128 threads share a triple: they build up to 128
+// node descriptors at once (one per thread), the four warps evaluate the nodes round-robin
+// (lane = site, ceil(w / 32) sites per lane), and in the t channel each warp writes its node's
+// panel to shared memory (double-buffered: one block barrier per round of four nodes), after
+// which every thread adds the round's panels to its R x 2R block of M (the threads form a
+// 16 x 8 grid).  After the t channel M is staged in shared memory and the merged pair list is
+// walked once per triple.  Each warp keeps Kahan sums over its nodes per site; the four warps'
+// sums and the RPA term are combined in a fixed order, so results do not depend on the launch.
+// ------------------------------------------------------------------------------------
+constexpr int kBigThreads = 128;
+constexpr int kBigBatch = 128;  // node descriptors built at once (one per thread)
+
+__host__ __device__ constexpr int big_spt(int R) { return (16 * R + 31) / 32; }
+
+struct BigSmem {
+    size_t pos, u, panels, parts, rpa, total;
+};
+__host__ __device__ inline BigSmem big_smem_layout(int R, int n_seg) {
+    const int w = 16 * R;
+    BigSmem L;
+    size_t o = 0;
+    L.pos = o; o += align16(sizeof(float) * kMaxFreq);
+    // union: the descriptors of a node batch, or (after the t channel) M and the pair walk's
+    // segment partials
+    L.u = o;
+    const size_t d = kBigBatch * sizeof(NodeDesc), m = sizeof(float2) * (size_t(w) * w + n_seg);
+    o += align16(d > m ? d : m);
+    L.panels = o; o += align16(sizeof(float2) * 2 * 4 * 2 * size_t(w));  // 2 buffers x 4 warps x (A, B)
+    L.parts = o; o += align16(sizeof(float2) * 4 * size_t(w));          // per warp and site
+    L.rpa = o; o += align16(sizeof(float2) * size_t(w));
+    L.total = o;
+    return L;
+}
+
+// Adds a panel (A = c * third slab, B = fourth slab, w entries each) to the thread's R x 2R block.
+template <int R>
+__device__ __forceinline__ void big_outer_update(const float2 *pan, int tid, float2 (*M)[2 * R]) {
+    constexpr int w = 16 * R, C = 2 * R;
+    const int tr = tid >> 3, tc = tid & 7;
+    float2 av[R], bv[C];
+#pragma unroll
+    for (int i = 0; i < R; ++i) av[i] = pan[tr * R + i];
+#pragma unroll
+    for (int j = 0; j < C; ++j) bv[j] = pan[w + tc * C + j];
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+#pragma unroll
+        for (int j = 0; j < C; ++j) M[i][j] = fma2(av[i], bv[j], M[i][j]);
+}
+
+// The flow of triple `it` of flow `a` by the whole CTA; `pos` the mesh in shared memory.
+template <int R>
+__device__ __forceinline__ void big_triple(const FlowArgs &a, const float *pos, int it, unsigned char *smem,
+                                           const BigSmem &L) {
+    constexpr int SPT = big_spt(R), w = 16 * R, C = 2 * R;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    NodeDesc *desc = reinterpret_cast<NodeDesc *>(smem + L.u);
+    float2 *Ms = reinterpret_cast<float2 *>(smem + L.u);
+    float2 *slots = Ms + w * w;
+    float2 *panels = reinterpret_cast<float2 *>(smem + L.panels);
+    float2 *parts = reinterpret_cast<float2 *>(smem + L.parts);
+    float2 *rpa = reinterpret_cast<float2 *>(smem + L.rpa);
+
+    const int su = it / a.n, ti = it - su * a.n;
+    int si = int((sqrtf(8.0f * float(su) + 1.0f) - 1.0f) * 0.5f);
+    while (si * (si + 1) / 2 > su) --si;
+    while ((si + 1) * (si + 2) / 2 <= su) ++si;
+    const int ui = su - si * (si + 1) / 2;
+    Transfer f;
+    f.s = pos[si];
+    f.t = pos[ti];
+    f.u = pos[ui];
+    f.w1p = 0.5f * (f.s + f.t + f.u);
+    f.w1 = 0.5f * (f.s - f.t + f.u);
+    f.w2p = 0.5f * (f.s - f.t - f.u);
+    f.w2 = 0.5f * (f.s + f.t - f.u);
+    f.si = si;
+    f.ti = ti;
+    f.ui = ui;
+
+    Lane<SPT> ln;
+#pragma unroll
+    for (int k = 0; k < SPT; ++k) {
+        const int j = lane + 32 * k;
+        ln.j[k] = j;
+        ln.valid[k] = j < a.nl;
+        ln.site[k] = ln.valid[k] ? a.sites[j] : 0;
+        ln.isite[k] = ln.valid[k] ? a.inv_sites[j] : 0;
+    }
+    float acc_s[SPT], cmp_s[SPT], acc_d[SPT], cmp_d[SPT];
+#pragma unroll
+    for (int k = 0; k < SPT; ++k) acc_s[k] = cmp_s[k] = acc_d[k] = cmp_d[k] = 0.0f;
+    float2 M[R][C];
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+#pragma unroll
+        for (int j = 0; j < C; ++j) M[i][j] = make_float2(0.0f, 0.0f);
+    int round = 0;
+
+    auto channel = [&](auto chc, int xi) {
+        constexpr int CH = decltype(chc)::value;
+        const int cnt = __ldg(a.node_cnt + xi);
+        const float *nwp = a.node_wp + size_t(xi) * a.max_nodes;
+        const float *nc = a.node_c + size_t(xi) * a.max_nodes;
+        for (int b0 = 0; b0 < cnt; b0 += kBigBatch) {
+            const int nb = min(kBigBatch, cnt - b0);
+            __syncthreads();  // the previous batch's descriptors (or M) are no longer read
+            if (tid < nb) {
+                float c = __ldg(nc + b0 + tid);
+                if (CH == kU) c = -c;
+                make_desc<CH>(a, pos, f, __ldg(nwp + b0 + tid), c, desc[tid]);
+            }
+            __syncthreads();
+            if constexpr (CH != kT) {
+                for (int k = warp; k < nb; k += 4) {
+                    const NodeView v{&desc[k], desc[k].c, desc[k].lv};
+                    float rs[1][SPT], rd[1][SPT];
+                    node_term<CH, SPT, 1>(a, &v, ln, lane, nullptr, rs, rd);
+#pragma unroll
+                    for (int q = 0; q < SPT; ++q) {
+                        kahan_add(acc_s[q], cmp_s[q], v.c * rs[0][q]);
+                        kahan_add(acc_d[q], cmp_d[q], v.c * rd[0][q]);
+                    }
+                }
+            } else {
+                for (int r0 = 0; r0 < nb; r0 += 4, ++round) {
+                    const int k = r0 + warp;
+                    float2 *buf = panels + size_t(round & 1) * 4 * 2 * w;
+                    if (k < nb) {
+                        const NodeView v{&desc[k], desc[k].c, desc[k].lv};
+                        TExchange tx;
+                        tx.A2 = buf + warp * 2 * w;
+                        tx.B2 = tx.A2 + w;
+                        float rs[1][SPT], rd[1][SPT];
+                        node_term<kT, SPT, 1, FlowArgs, true>(a, &v, ln, lane, &tx, rs, rd);
+#pragma unroll
+                        for (int q = 0; q < SPT; ++q) {
+                            kahan_add(acc_s[q], cmp_s[q], v.c * rs[0][q]);
+                            kahan_add(acc_d[q], cmp_d[q], v.c * rd[0][q]);
+                        }
+                    }
+                    __syncthreads();  // the round's panels are written
+                    const int np = min(4, nb - r0);
+                    for (int p = 0; p < np; ++p) big_outer_update<R>(buf + p * 2 * w, tid, M);
+                }
+            }
+        }
+    };
+
+    channel(std::integral_constant<int, kS>{}, si);
+    channel(std::integral_constant<int, kT>{}, ti);
+    // RPA term: M staged, the merged pair list walked once (32 chunks, warp 0), per-site sums
+    __syncthreads();  // every panel update and every descriptor read is done
+    {
+        const int tr = tid >> 3, tc = tid & 7;
+#pragma unroll
+        for (int i = 0; i < R; ++i)
+#pragma unroll
+            for (int j = 0; j < C; ++j) Ms[(tr * R + i) * w + tc * C + j] = M[i][j];
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const int lanes = a.rpa.lanes;
+        const int cntq = __ldg(a.rpa.count + lane);
+        int slot = __ldg(a.rpa.slot_base + lane);
+        const int *sched = a.rpa.sched + lane;
+        float2 acc = make_float2(0.0f, 0.0f);
+        for (int i = 0; i < cntq; ++i) {
+            const int e = __ldg(sched + size_t(i) * lanes);
+            const float m = float((e >> 14) & 0xff);
+            const int ra = e & 0x7f, rb = (e >> 7) & 0x7f;
+            acc = fma2(make_float2(m, m), Ms[ra * w + rb], acc);
+            if (e & (1 << 22)) {
+                slots[slot++] = acc;
+                acc = make_float2(0.0f, 0.0f);
+            }
+        }
+    }
+    __syncthreads();
+    if (tid < a.nl) {
+        float2 sum = make_float2(0.0f, 0.0f);
+        for (int q = __ldg(a.rpa.seg_ptr + tid); q < __ldg(a.rpa.seg_ptr + tid + 1); ++q) {
+            const float2 p = slots[q];
+            sum.x += p.x;
+            sum.y += p.y;
+        }
+        rpa[tid] = sum;
+    }
+    channel(std::integral_constant<int, kU>{}, ui);  // its first barrier publishes rpa[]
+
+    // the four warps' sums per site, then the RPA term (SU2FrgCore.cpp:265-266), in this order
+#pragma unroll
+    for (int k = 0; k < SPT; ++k)
+        if (ln.valid[k]) parts[warp * w + ln.j[k]] = make_float2(acc_s[k] - cmp_s[k], acc_d[k] - cmp_d[k]);
+    __syncthreads();
+    if (tid < a.nl) {
+        const float2 p0 = parts[tid], p1 = parts[w + tid], p2 = parts[2 * w + tid], p3 = parts[3 * w + tid];
+        const float2 r = rpa[tid];
+        const float vs = ((p0.x + p1.x) + (p2.x + p3.x)) + (2.0f * a.spin) * r.x;
+        const float vd = ((p0.y + p1.y) + (p2.y + p3.y)) + (8.0f * a.spin) * r.y;
+        const float two_pi = 2.0f * float(kPi);
+        const float os = vs / two_pi, od = vd / two_pi;
+        a.dsd[size_t(it) * a.nl + tid] = make_float2(os, od);
+        if (isnan(os) || isnan(od)) atomicOr(a.status, kStatusNaN);
+    }
+}
+
+template <int R>
+__global__ void __launch_bounds__(kBigThreads) su2_vertex_big_kernel(FlowArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_item;
+    const BigSmem L = big_smem_layout(R, a.rpa.n_seg);
+    float *pos = reinterpret_cast<float *>(smem_raw + L.pos);
+    for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
+    for (;;) {
+        __syncthreads();  // the previous triple is finished with shared memory
+        if (threadIdx.x == 0) s_item = atomicAdd(a.work_counter, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= a.fn) break;
+        big_triple<R>(a, pos, it, smem_raw, L);
+    }
+}
+
+// Batched form: a persistent grid over the ragged (flow, triple) list of the batch's flows of
+// one big class; the CTA reloads the flow's argument block and mesh when the flow changes
+// (items are numbered flow by flow).
+template <int R>
+__global__ void __launch_bounds__(kBigThreads) su2_vertex_big_batch_kernel(BatchVertexArgs b) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_item;
+    __shared__ __align__(16) FlowArgs fa;
+    const BigSmem L = big_smem_layout(R, b.n_seg_max);
+    float *pos = reinterpret_cast<float *>(smem_raw + L.pos);
+    int cur = -1, base = 0;
+    bool skip = false;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(b.counter, 1);
+        __syncthreads();
+        const int w = s_item;
+        if (w >= b.total) break;
+        int lo = 0, hi = b.n_list - 1;  // last f with prefix[f] <= w
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(b.prefix + mid) <= w) lo = mid;
+            else hi = mid - 1;
+        }
+        if (lo != cur) {
+            cur = lo;
+            base = __ldg(b.prefix + lo);
+            const BatchFlow *bf = b.flows + __ldg(b.list + lo);
+            const int *src = reinterpret_cast<const int *>(&bf->a);
+            int *dst = reinterpret_cast<int *>(&fa);
+            for (int i = threadIdx.x; i < int(sizeof(FlowArgs) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+            skip = bf->phase != kPhaseFlowing;
+            __syncthreads();
+            for (int i = threadIdx.x; i < fa.n; i += blockDim.x) pos[i] = fa.freq[i];
+            __syncthreads();
+        }
+        if (skip) continue;
+        big_triple<R>(fa, pos, w - base, smem_raw, L);
+    }
+}
+
 int spt_of(int nl) { return nl <= 32 ? 1 : (nl <= 64 ? 2 : 4); }
 
 int wsite_of(int nl) {
@@ -1270,12 +1545,18 @@ int outer_w_of(int nl) { return nl <= 32 ? rpa_outer_width(nl) : 0; }
 
 }  // namespace
 
+// Lattices of 33 to 80 sites use the CTA-per-triple kernel: R = 3, 4, 5 (w = 48, 64, 80).
+int big_r_of(int nl) { return nl <= 32 || nl > 80 ? 0 : (nl <= 48 ? 3 : (nl <= 64 ? 4 : 5)); }
+
 int vertex_class(int nl) {
+    const int r = big_r_of(nl);
+    if (r) return 3 + r;  // 6, 7, 8: the CTA-per-triple kernel with w = 48, 64, 80
     if (nl > 32) return nl <= 64 ? 4 : 5;
     return rpa_outer_width(nl) / 8 - 1;  // 0..3: outer-product blocks of 1..4 rows
 }
 
 size_t vertex_flow_smem_bytes(int nl, const RpaSchedule &rpa, int npi) {
+    if (const int r = big_r_of(nl)) return big_smem_layout(r, rpa.n_seg).total;
     const int spt = spt_of(nl);
     return kMaxFreq * sizeof(float) + sched_bytes(rpa, nl) +
            kWarps * warp_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, rpa.n_seg, outer_w_of(nl));
@@ -1294,25 +1575,33 @@ VertexKernel vertex_kernel(int cls, int npi) {
         case 2: return vertex_kernel_npi<1, 3>(npi);
         case 3: return vertex_kernel_npi<1, 4>(npi);
         case 4: return vertex_kernel_npi<2, 0>(npi);
+        case 6: return su2_vertex_big_kernel<3>;
+        case 7: return su2_vertex_big_kernel<4>;
+        case 8: return su2_vertex_big_kernel<5>;
         default: return vertex_kernel_npi<4, 0>(npi);
     }
 }
+int threads_of(int cls) { return cls >= 6 ? kBigThreads : kThreads; }
 }  // namespace
 
+// The CTA-per-triple kernel (33..80 sites) has no variants: nodes per iteration and the
+// schedule's place do not apply, and every setting launches the same kernel.
 int vertex_flow_blocks_per_sm(int nl, const RpaSchedule &rpa, int npi) {
     const size_t smem = vertex_flow_smem_bytes(nl, rpa, npi);
-    VertexKernel k = vertex_kernel(vertex_class(nl), npi);
+    const int cls = vertex_class(nl);
+    VertexKernel k = vertex_kernel(cls, npi);
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess) return -1;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, smem) != cudaSuccess) return -1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads_of(cls), smem) != cudaSuccess) return -1;
     return per_sm;
 }
 
 void launch_vertex_flow(const FlowArgs &a, int npi, int grid, cudaStream_t stream) {
     const size_t smem = vertex_flow_smem_bytes(a.nl, a.rpa, npi);
-    VertexKernel k = vertex_kernel(vertex_class(a.nl), npi);
+    const int cls = vertex_class(a.nl);
+    VertexKernel k = vertex_kernel(cls, npi);
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    k<<<grid, kThreads, smem, stream>>>(a);
+    k<<<grid, threads_of(cls), smem, stream>>>(a);
 }
 
 int vertex_spt(int nl) { return spt_of(nl); }
@@ -1341,24 +1630,30 @@ BatchKernel batch_kernel(int cls, int npi) {
         case 2: return batch_kernel_npi<1, 3>(npi);
         case 3: return batch_kernel_npi<1, 4>(npi);
         case 4: return batch_kernel_npi<2, 0>(npi);
+        case 6: return su2_vertex_big_batch_kernel<3>;
+        case 7: return su2_vertex_big_batch_kernel<4>;
+        case 8: return su2_vertex_big_batch_kernel<5>;
         default: return batch_kernel_npi<4, 0>(npi);
     }
 }
 }  // namespace
 
+size_t batch_big_smem_bytes(int cls, int n_seg_max) { return big_smem_layout(cls - 3, n_seg_max).total; }
+
 int batch_vertex_blocks_per_sm(int cls, int npi, size_t smem) {
     BatchKernel k = batch_kernel(cls, npi);
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess) return -1;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, smem) != cudaSuccess) return -1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads_of(cls), smem) != cudaSuccess) return -1;
     return per_sm;
 }
 
 // The kernel's shared-memory limit is raised by batch_vertex_blocks_per_sm when the plan is
 // built, so this launch can be captured into a graph.
 void launch_batch_vertex(const BatchVertexArgs &b, int cls, int npi, int grid, cudaStream_t stream) {
-    const size_t smem = batch_vertex_smem_bytes(b.n_max, size_t(b.warp_area), b.sched_ints);
-    batch_kernel(cls, npi)<<<grid, kThreads, smem, stream>>>(b);
+    const size_t smem = cls >= 6 ? batch_big_smem_bytes(cls, b.n_seg_max)
+                                 : batch_vertex_smem_bytes(b.n_max, size_t(b.warp_area), b.sched_ints);
+    batch_kernel(cls, npi)<<<grid, threads_of(cls), smem, stream>>>(b);
 }
 
 namespace {
