@@ -156,10 +156,9 @@ int batch_vertex_blocks_per_sm(int cls, int npi, size_t smem);
 void launch_batch_vertex(const BatchVertexArgs &b, int cls, int npi, int grid, cudaStream_t stream);
 int vertex_spt(int nl);  // sites per lane of a flow with nl sites
 // Vertex-kernel class of a flow (one kernel instance per class): 0-3 for nl <= 32 (outer-product
-// RPA with w = 8, 16, 24, 32, a warp per triple), 6-8 for 33 <= nl <= 80 (outer-product RPA with
-// w = 48, 64, 80, a CTA per triple), 5 for 81 <= nl <= 128 (four sites per lane, an RPA pair
-// walk per node); 4 (two sites per lane, pair walk) is not chosen any more.
-constexpr int kVertexClasses = 9;
+// RPA with w = 8, 16, 24, 32, a warp per triple), 6-10 for 33 <= nl <= 128 (outer-product RPA
+// with w = 48, 64, 80, 96, 128, a CTA per triple); 4 and 5 are unused.
+constexpr int kVertexClasses = 11;
 int vertex_class(int nl);
 size_t batch_big_smem_bytes(int cls, int n_seg_max);
 

@@ -1262,21 +1262,21 @@ __global__ void __launch_bounds__(kGroupWarps * 32) su2_vertex_group_kernel(Grou
 }
 
 // ------------------------------------------------------------------------------------
-// Lattices of 33 to 80 sites: one CTA per triple (su2_vertex_big_kernel<R>).
+// Lattices of 33 to 128 sites: one CTA per triple (su2_vertex_big_kernel<R, NT>).
 //
 // Above 32 sites the t channel's outer-product matrix M = sum over nodes of (c A) x B (w x w,
-// w = 16 R >= Nl) no longer fits one warp's registers, and a warp that owns a triple walks the
-// whole merged RPA pair list for every t-channel node (585 entries per lane and node for the
-// 70-site pyrochlore range 7).  Here the CTA's 128 threads share a triple: they build up to 128
-// node descriptors at once (one per thread), the four warps evaluate the nodes round-robin
-// (lane = site, ceil(w / 32) sites per lane), and in the t channel each warp writes its node's
-// panel to shared memory (double-buffered: one block barrier per round of four nodes), after
-// which every thread adds the round's panels to its R x 2R block of M (the threads form a
-// 16 x 8 grid).  After the t channel M is staged in shared memory and the merged pair list is
-// walked once per triple.  Each warp keeps Kahan sums over its nodes per site; the four warps'
-// sums and the RPA term are combined in a fixed order, so results do not depend on the launch.
+// w = 16 R >= Nl) no longer fits one warp's registers, and a warp that owns a triple would walk
+// the whole merged RPA pair list for every t-channel node (585 entries per lane and node for the
+// 70-site pyrochlore range 7).  Here the CTA's NT threads (128 or 256) share a triple: they
+// build up to 128 node descriptors at once (one per thread), the NT / 32 warps evaluate the
+// nodes round-robin (lane = site, ceil(w / 32) sites per lane), and in the t channel each warp
+// writes its node's panel to shared memory (double-buffered: one block barrier per round of
+// NT / 32 nodes), after which every thread adds the round's panels to its block of M (the
+// threads form a 16 x NT/16 grid; a block is R x 2R for 128 threads, R x R for 256).  After
+// the t channel M is staged in shared memory and the merged pair list is walked once per triple.
+// Each warp keeps Kahan sums over its nodes per site; the warps' sums and the RPA term are
+// combined in a fixed order, so results do not depend on the launch.
 // ------------------------------------------------------------------------------------
-constexpr int kBigThreads = 128;
 constexpr int kBigBatch = 128;  // node descriptors built at once (one per thread)
 
 __host__ __device__ constexpr int big_spt(int R) { return (16 * R + 31) / 32; }
@@ -1284,8 +1284,8 @@ __host__ __device__ constexpr int big_spt(int R) { return (16 * R + 31) / 32; }
 struct BigSmem {
     size_t pos, u, panels, parts, rpa, total;
 };
-__host__ __device__ inline BigSmem big_smem_layout(int R, int n_seg) {
-    const int w = 16 * R;
+__host__ __device__ inline BigSmem big_smem_layout(int R, int NT, int n_seg) {
+    const int w = 16 * R, NW = NT / 32;
     BigSmem L;
     size_t o = 0;
     L.pos = o; o += align16(sizeof(float) * kMaxFreq);
@@ -1294,18 +1294,18 @@ __host__ __device__ inline BigSmem big_smem_layout(int R, int n_seg) {
     L.u = o;
     const size_t d = kBigBatch * sizeof(NodeDesc), m = sizeof(float2) * (size_t(w) * w + n_seg);
     o += align16(d > m ? d : m);
-    L.panels = o; o += align16(sizeof(float2) * 2 * 4 * 2 * size_t(w));  // 2 buffers x 4 warps x (A, B)
-    L.parts = o; o += align16(sizeof(float2) * 4 * size_t(w));          // per warp and site
+    L.panels = o; o += align16(sizeof(float2) * 2 * NW * 2 * size_t(w));  // 2 buffers x warps x (A, B)
+    L.parts = o; o += align16(sizeof(float2) * NW * size_t(w));           // per warp and site
     L.rpa = o; o += align16(sizeof(float2) * size_t(w));
     L.total = o;
     return L;
 }
 
-// Adds a panel (A = c * third slab, B = fourth slab, w entries each) to the thread's R x 2R block.
-template <int R>
-__device__ __forceinline__ void big_outer_update(const float2 *pan, int tid, float2 (*M)[2 * R]) {
-    constexpr int w = 16 * R, C = 2 * R;
-    const int tr = tid >> 3, tc = tid & 7;
+// Adds a panel (A = c * third slab, B = fourth slab, w entries each) to the thread's block of M.
+template <int R, int NT>
+__device__ __forceinline__ void big_outer_update(const float2 *pan, int tid, float2 (*M)[16 * R / (NT / 16)]) {
+    constexpr int w = 16 * R, TC = NT / 16, C = w / TC;
+    const int tr = tid / TC, tc = tid % TC;
     float2 av[R], bv[C];
 #pragma unroll
     for (int i = 0; i < R; ++i) av[i] = pan[tr * R + i];
@@ -1318,10 +1318,11 @@ __device__ __forceinline__ void big_outer_update(const float2 *pan, int tid, flo
 }
 
 // The flow of triple `it` of flow `a` by the whole CTA; `pos` the mesh in shared memory.
-template <int R>
+template <int R, int NT>
 __device__ __forceinline__ void big_triple(const FlowArgs &a, const float *pos, int it, unsigned char *smem,
                                            const BigSmem &L) {
-    constexpr int SPT = big_spt(R), w = 16 * R, C = 2 * R;
+    constexpr int SPT = big_spt(R), w = 16 * R, NW = NT / 32, TC = NT / 16, C = w / TC;
+    static_assert(NW == 4 || NW == 8, "the warps' sums combine as a tree of 4 or 8");
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     NodeDesc *desc = reinterpret_cast<NodeDesc *>(smem + L.u);
     float2 *Ms = reinterpret_cast<float2 *>(smem + L.u);
@@ -1381,7 +1382,7 @@ __device__ __forceinline__ void big_triple(const FlowArgs &a, const float *pos, 
             }
             __syncthreads();
             if constexpr (CH != kT) {
-                for (int k = warp; k < nb; k += 4) {
+                for (int k = warp; k < nb; k += NW) {
                     const NodeView v{&desc[k], desc[k].c, desc[k].lv};
                     float rs[1][SPT], rd[1][SPT];
                     node_term<CH, SPT, 1>(a, &v, ln, lane, nullptr, rs, rd);
@@ -1392,9 +1393,9 @@ __device__ __forceinline__ void big_triple(const FlowArgs &a, const float *pos, 
                     }
                 }
             } else {
-                for (int r0 = 0; r0 < nb; r0 += 4, ++round) {
+                for (int r0 = 0; r0 < nb; r0 += NW, ++round) {
                     const int k = r0 + warp;
-                    float2 *buf = panels + size_t(round & 1) * 4 * 2 * w;
+                    float2 *buf = panels + size_t(round & 1) * NW * 2 * w;
                     if (k < nb) {
                         const NodeView v{&desc[k], desc[k].c, desc[k].lv};
                         TExchange tx;
@@ -1409,8 +1410,8 @@ __device__ __forceinline__ void big_triple(const FlowArgs &a, const float *pos, 
                         }
                     }
                     __syncthreads();  // the round's panels are written
-                    const int np = min(4, nb - r0);
-                    for (int p = 0; p < np; ++p) big_outer_update<R>(buf + p * 2 * w, tid, M);
+                    const int np = min(NW, nb - r0);
+                    for (int p = 0; p < np; ++p) big_outer_update<R, NT>(buf + p * 2 * w, tid, M);
                 }
             }
         }
@@ -1421,7 +1422,7 @@ __device__ __forceinline__ void big_triple(const FlowArgs &a, const float *pos, 
     // RPA term: M staged, the merged pair list walked once (32 chunks, warp 0), per-site sums
     __syncthreads();  // every panel update and every descriptor read is done
     {
-        const int tr = tid >> 3, tc = tid & 7;
+        const int tr = tid / TC, tc = tid % TC;
 #pragma unroll
         for (int i = 0; i < R; ++i)
 #pragma unroll
@@ -1457,16 +1458,23 @@ __device__ __forceinline__ void big_triple(const FlowArgs &a, const float *pos, 
     }
     channel(std::integral_constant<int, kU>{}, ui);  // its first barrier publishes rpa[]
 
-    // the four warps' sums per site, then the RPA term (SU2FrgCore.cpp:265-266), in this order
+    // the warps' sums per site (a pairwise tree), then the RPA term (SU2FrgCore.cpp:265-266)
 #pragma unroll
     for (int k = 0; k < SPT; ++k)
         if (ln.valid[k]) parts[warp * w + ln.j[k]] = make_float2(acc_s[k] - cmp_s[k], acc_d[k] - cmp_d[k]);
     __syncthreads();
     if (tid < a.nl) {
-        const float2 p0 = parts[tid], p1 = parts[w + tid], p2 = parts[2 * w + tid], p3 = parts[3 * w + tid];
+        float2 p[NW];
+#pragma unroll
+        for (int q = 0; q < NW; ++q) p[q] = parts[q * w + tid];
+        float vs = (p[0].x + p[1].x) + (p[2].x + p[3].x), vd = (p[0].y + p[1].y) + (p[2].y + p[3].y);
+        if constexpr (NW == 8) {
+            vs = vs + ((p[4].x + p[5].x) + (p[6].x + p[7].x));
+            vd = vd + ((p[4].y + p[5].y) + (p[6].y + p[7].y));
+        }
         const float2 r = rpa[tid];
-        const float vs = ((p0.x + p1.x) + (p2.x + p3.x)) + (2.0f * a.spin) * r.x;
-        const float vd = ((p0.y + p1.y) + (p2.y + p3.y)) + (8.0f * a.spin) * r.y;
+        vs = vs + (2.0f * a.spin) * r.x;
+        vd = vd + (8.0f * a.spin) * r.y;
         const float two_pi = 2.0f * float(kPi);
         const float os = vs / two_pi, od = vd / two_pi;
         a.dsd[size_t(it) * a.nl + tid] = make_float2(os, od);
@@ -1474,11 +1482,11 @@ __device__ __forceinline__ void big_triple(const FlowArgs &a, const float *pos, 
     }
 }
 
-template <int R>
-__global__ void __launch_bounds__(kBigThreads) su2_vertex_big_kernel(FlowArgs a) {
+template <int R, int NT>
+__global__ void __launch_bounds__(NT) su2_vertex_big_kernel(FlowArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_item;
-    const BigSmem L = big_smem_layout(R, a.rpa.n_seg);
+    const BigSmem L = big_smem_layout(R, NT, a.rpa.n_seg);
     float *pos = reinterpret_cast<float *>(smem_raw + L.pos);
     for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
     for (;;) {
@@ -1487,19 +1495,19 @@ __global__ void __launch_bounds__(kBigThreads) su2_vertex_big_kernel(FlowArgs a)
         __syncthreads();
         const int it = s_item;
         if (it >= a.fn) break;
-        big_triple<R>(a, pos, it, smem_raw, L);
+        big_triple<R, NT>(a, pos, it, smem_raw, L);
     }
 }
 
 // Batched form: a persistent grid over the ragged (flow, triple) list of the batch's flows of
 // one big class; the CTA reloads the flow's argument block and mesh when the flow changes
 // (items are numbered flow by flow).
-template <int R>
-__global__ void __launch_bounds__(kBigThreads) su2_vertex_big_batch_kernel(BatchVertexArgs b) {
+template <int R, int NT>
+__global__ void __launch_bounds__(NT) su2_vertex_big_batch_kernel(BatchVertexArgs b) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_item;
     __shared__ __align__(16) FlowArgs fa;
-    const BigSmem L = big_smem_layout(R, b.n_seg_max);
+    const BigSmem L = big_smem_layout(R, NT, b.n_seg_max);
     float *pos = reinterpret_cast<float *>(smem_raw + L.pos);
     int cur = -1, base = 0;
     bool skip = false;
@@ -1528,7 +1536,7 @@ __global__ void __launch_bounds__(kBigThreads) su2_vertex_big_batch_kernel(Batch
             __syncthreads();
         }
         if (skip) continue;
-        big_triple<R>(fa, pos, w - base, smem_raw, L);
+        big_triple<R, NT>(fa, pos, w - base, smem_raw, L);
     }
 }
 
@@ -1545,18 +1553,27 @@ int outer_w_of(int nl) { return nl <= 32 ? rpa_outer_width(nl) : 0; }
 
 }  // namespace
 
-// Lattices of 33 to 80 sites use the CTA-per-triple kernel: R = 3, 4, 5 (w = 48, 64, 80).
-int big_r_of(int nl) { return nl <= 32 || nl > 80 ? 0 : (nl <= 48 ? 3 : (nl <= 64 ? 4 : 5)); }
+// Lattices of 33 to 128 sites use the CTA-per-triple kernel: w = 16 R >= Nl, R = 3, 4 with 128
+// threads, R = 5, 6, 8 with 256 (classes 6..10).
+int big_r_of(int nl) {
+    return nl <= 32 ? 0 : (nl <= 48 ? 3 : (nl <= 64 ? 4 : (nl <= 80 ? 5 : (nl <= 96 ? 6 : 8))));
+}
+int big_class_r(int cls) { return cls == 6 ? 3 : (cls == 7 ? 4 : (cls == 8 ? 5 : (cls == 9 ? 6 : 8))); }
+int big_threads(int r) { return r <= 4 ? 128 : 256; }
 
 int vertex_class(int nl) {
-    const int r = big_r_of(nl);
-    if (r) return 3 + r;  // 6, 7, 8: the CTA-per-triple kernel with w = 48, 64, 80
-    if (nl > 32) return nl <= 64 ? 4 : 5;
-    return rpa_outer_width(nl) / 8 - 1;  // 0..3: outer-product blocks of 1..4 rows
+    switch (big_r_of(nl)) {
+        case 0: return rpa_outer_width(nl) / 8 - 1;  // 0..3: a warp per triple, blocks of 1..4 rows
+        case 3: return 6;
+        case 4: return 7;
+        case 5: return 8;
+        case 6: return 9;
+        default: return 10;
+    }
 }
 
 size_t vertex_flow_smem_bytes(int nl, const RpaSchedule &rpa, int npi) {
-    if (const int r = big_r_of(nl)) return big_smem_layout(r, rpa.n_seg).total;
+    if (const int r = big_r_of(nl)) return big_smem_layout(r, big_threads(r), rpa.n_seg).total;
     const int spt = spt_of(nl);
     return kMaxFreq * sizeof(float) + sched_bytes(rpa, nl) +
            kWarps * warp_bytes(spt == 1 ? wsite_of(nl) : 32, spt, npi, rpa.n_seg, outer_w_of(nl));
@@ -1574,17 +1591,17 @@ VertexKernel vertex_kernel(int cls, int npi) {
         case 1: return vertex_kernel_npi<1, 2>(npi);
         case 2: return vertex_kernel_npi<1, 3>(npi);
         case 3: return vertex_kernel_npi<1, 4>(npi);
-        case 4: return vertex_kernel_npi<2, 0>(npi);
-        case 6: return su2_vertex_big_kernel<3>;
-        case 7: return su2_vertex_big_kernel<4>;
-        case 8: return su2_vertex_big_kernel<5>;
-        default: return vertex_kernel_npi<4, 0>(npi);
+        case 6: return su2_vertex_big_kernel<3, 128>;
+        case 7: return su2_vertex_big_kernel<4, 128>;
+        case 8: return su2_vertex_big_kernel<5, 256>;
+        case 9: return su2_vertex_big_kernel<6, 256>;
+        default: return su2_vertex_big_kernel<8, 256>;
     }
 }
-int threads_of(int cls) { return cls >= 6 ? kBigThreads : kThreads; }
+int threads_of(int cls) { return cls >= 6 ? big_threads(big_class_r(cls)) : kThreads; }
 }  // namespace
 
-// The CTA-per-triple kernel (33..80 sites) has no variants: nodes per iteration and the
+// The CTA-per-triple kernel (33..128 sites) has no variants: nodes per iteration and the
 // schedule's place do not apply, and every setting launches the same kernel.
 int vertex_flow_blocks_per_sm(int nl, const RpaSchedule &rpa, int npi) {
     const size_t smem = vertex_flow_smem_bytes(nl, rpa, npi);
@@ -1629,16 +1646,19 @@ BatchKernel batch_kernel(int cls, int npi) {
         case 1: return batch_kernel_npi<1, 2>(npi);
         case 2: return batch_kernel_npi<1, 3>(npi);
         case 3: return batch_kernel_npi<1, 4>(npi);
-        case 4: return batch_kernel_npi<2, 0>(npi);
-        case 6: return su2_vertex_big_batch_kernel<3>;
-        case 7: return su2_vertex_big_batch_kernel<4>;
-        case 8: return su2_vertex_big_batch_kernel<5>;
-        default: return batch_kernel_npi<4, 0>(npi);
+        case 6: return su2_vertex_big_batch_kernel<3, 128>;
+        case 7: return su2_vertex_big_batch_kernel<4, 128>;
+        case 8: return su2_vertex_big_batch_kernel<5, 256>;
+        case 9: return su2_vertex_big_batch_kernel<6, 256>;
+        default: return su2_vertex_big_batch_kernel<8, 256>;
     }
 }
 }  // namespace
 
-size_t batch_big_smem_bytes(int cls, int n_seg_max) { return big_smem_layout(cls - 3, n_seg_max).total; }
+size_t batch_big_smem_bytes(int cls, int n_seg_max) {
+    const int r = big_class_r(cls);
+    return big_smem_layout(r, big_threads(r), n_seg_max).total;
+}
 
 int batch_vertex_blocks_per_sm(int cls, int npi, size_t smem) {
     BatchKernel k = batch_kernel(cls, npi);
