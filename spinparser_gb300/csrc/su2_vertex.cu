@@ -311,17 +311,12 @@ __device__ __forceinline__ void kahan_add(float &sum, float &comp, float v) {
     sum = t;
 }
 
-// Per-group shared-memory exchange area of the t channel.
-//   Nl <= 32: the node's panel, A2[w] = c * (spin, density) of the third slab and B2[w] =
-//     (spin, density) of the fourth slab per site (w = rpa_outer_width(Nl)); the warp adds the
-//     outer products of the panels of a trip to its M accumulators;
-//   Nl > 32: separate 32-bit arrays As, Ad, Bs, Bd of the third and fourth slab, then the RPA
-//     segment partials of the node's own walk.
+// Shared-memory exchange area of a node's t channel: its panel, A2[w] = c * (spin, density) of
+// the third slab and B2[w] = (spin, density) of the fourth slab per site (w >= Nl); the owner
+// adds the panels' outer products to its M accumulators and walks the RPA schedule once per
+// triple.
 struct TExchange {
-    float *As, *Ad;  // [sites] spin / density of the third slab   (Nl > 32)
-    float *Bs, *Bd;  // [sites] spin / density of the fourth slab  (Nl > 32)
-    float2 *A2, *B2;  // [w] panel (Nl <= 32)
-    float2 *slots;   // [n_seg] RPA segment partials (Nl > 32)
+    float2 *A2, *B2;
     const int *sched, *count, *slot_base, *seg_ptr;  // RPA schedule (shared or global memory)
 };
 
@@ -345,9 +340,9 @@ struct NodeView {
 // K_X at NPI nodes for this lane's sites (one group evaluates NPI nodes per iteration so that
 // the t channel decodes each RPA schedule entry once for all of them).  `a` provides the
 // state (a.sd), the spin length and, for SPT > 1, the RPA schedule.
-// PANEL: the t channel writes the node's panel (c * third slab, fourth slab) for every site of
-// the lane instead of walking the RPA pair list (the outer-product forms; always so for Nl <= 32).
-template <int CH, int SPT, int NPI, class A, bool PANEL = false>
+// The t channel writes the node's panel (c * third slab, fourth slab) for every site of the
+// lane; the caller adds its outer product to M and walks the RPA pair list once per triple.
+template <int CH, int SPT, int NPI, class A>
 __device__ __forceinline__ void node_term(const A &a, const NodeView *v, const Lane<SPT> &ln, int jl,
                                           const TExchange *tx, float (*rs)[SPT], float (*rd)[SPT]) {
     float S0[NPI][SPT], S1[NPI][SPT], S2[NPI][SPT], S3[NPI][SPT], D0[NPI][SPT], D1[NPI][SPT], D2[NPI][SPT],
@@ -390,7 +385,7 @@ __device__ __forceinline__ void node_term(const A &a, const NodeView *v, const L
         return;
     }
     // t channel: RPA lattice sum (SU2FrgCore.cpp:249-266)
-    if constexpr (SPT == 1 || PANEL) {
+    {
         // outer-product form: the node's panel (c * third slab, fourth slab); the caller adds
         // the panels' outer products to its M accumulators
 #pragma unroll
@@ -404,46 +399,6 @@ __device__ __forceinline__ void node_term(const A &a, const NodeView *v, const L
                     tx[n].B2[j] = make_float2(S3[n][k], D3[n][k]);
                 }
             }
-    } else {
-#pragma unroll
-        for (int n = 0; n < NPI; ++n)
-#pragma unroll
-            for (int k = 0; k < SPT; ++k)
-                if (ln.valid[k]) {
-                    const int j = ln.j[k];
-                    tx[n].As[j] = S2[n][k];
-                    tx[n].Ad[j] = D2[n][k];
-                    tx[n].Bs[j] = S3[n][k];
-                    tx[n].Bd[j] = D3[n][k];
-                }
-        __syncwarp();
-        const int lanes = a.rpa.lanes;
-        const int cnt = tx[0].count[jl];
-        int slot = tx[0].slot_base[jl];
-        float acc_s[NPI], acc_d[NPI];
-#pragma unroll
-        for (int n = 0; n < NPI; ++n) acc_s[n] = acc_d[n] = 0.0f;
-        const int *sched = tx[0].sched + jl;
-        for (int i = 0; i < cnt; ++i) {
-            const int e = sched[i * lanes];
-            const float m = float((e >> 14) & 0xff);
-            const int ra = e & 0x7f, rb = (e >> 7) & 0x7f;
-#pragma unroll
-            for (int n = 0; n < NPI; ++n) {
-                acc_s[n] = fmaf(tx[n].As[ra] * m, tx[n].Bs[rb], acc_s[n]);
-                acc_d[n] = fmaf(tx[n].Ad[ra] * m, tx[n].Bd[rb], acc_d[n]);
-            }
-            if (e & (1 << 22)) {
-#pragma unroll
-                for (int n = 0; n < NPI; ++n) {
-                    tx[n].slots[slot] = make_float2(acc_s[n], acc_d[n]);
-                    acc_s[n] = 0.0f;
-                    acc_d[n] = 0.0f;
-                }
-                ++slot;
-            }
-        }
-        __syncwarp();
     }
     const float s2 = 2.0f * a.spin, s8 = 8.0f * a.spin;
 #pragma unroll
@@ -452,16 +407,7 @@ __device__ __forceinline__ void node_term(const A &a, const NodeView *v, const L
         const float cbs2 = v[n].lv[4], cbd2 = v[n].lv[5], icas2 = v[n].lv[6], icad2 = v[n].lv[7];
 #pragma unroll
         for (int k = 0; k < SPT; ++k) {
-            float rpa_s = 0.0f, rpa_d = 0.0f;
-            if (SPT != 1 && !PANEL && ln.valid[k]) {  // the per-node walk (outer-product forms: once per triple)
-                const int r = ln.j[k];
-                const int s0 = tx[0].seg_ptr[r], s1 = tx[0].seg_ptr[r + 1];
-                for (int q = s0; q < s1; ++q) {
-                    const float2 p = tx[n].slots[q];
-                    rpa_s += p.x;
-                    rpa_d += p.y;
-                }
-            }
+            const float rpa_s = 0.0f, rpa_d = 0.0f;  // the RPA term enters once per triple
             float x = 0.0f + s2 * rpa_s;  // SU2FrgCore.cpp:265, 286-293
             x -= cbd * S0[n][k];
             x += (0.25f * cbs) * S0[n][k];
@@ -484,7 +430,6 @@ __device__ __forceinline__ void node_term(const A &a, const NodeView *v, const L
             rd[n][k] = y;
         }
     }
-    if (SPT != 1 && !PANEL) __syncwarp();
 }
 
 // Adds the outer products of the panels of nodes k = (r*NPI+n)*G+gg < nb (ascending k) to the
@@ -660,17 +605,11 @@ __device__ __forceinline__ void setup_ctx(const FlowArgs &a, int lane, NodeDesc 
         __syncwarp();
     }
     unsigned char *gbase = groups + size_t(c.g) * NPI * nab;
-    const int ws = c.W * SPT;
 #pragma unroll
     for (int n = 0; n < NPI; ++n) {
         float *gx = reinterpret_cast<float *>(gbase + n * nab);
-        c.tx[n].As = gx;
-        c.tx[n].Ad = gx + ws;
-        c.tx[n].Bs = gx + 2 * ws;
-        c.tx[n].Bd = gx + 3 * ws;
-        c.tx[n].A2 = reinterpret_cast<float2 *>(gx);       // same bytes, used when Nl <= 32
+        c.tx[n].A2 = reinterpret_cast<float2 *>(gx);
         c.tx[n].B2 = reinterpret_cast<float2 *>(gx) + 8 * MB;
-        c.tx[n].slots = reinterpret_cast<float2 *>(gx + 4 * ws);
         c.tx[n].sched = sched;
         c.tx[n].count = count;
         c.tx[n].slot_base = slot_base;
@@ -1402,7 +1341,7 @@ __device__ __forceinline__ void big_triple(const FlowArgs &a, const float *pos, 
                         tx.A2 = buf + warp * 2 * w;
                         tx.B2 = tx.A2 + w;
                         float rs[1][SPT], rd[1][SPT];
-                        node_term<kT, SPT, 1, FlowArgs, true>(a, &v, ln, lane, &tx, rs, rd);
+                        node_term<kT, SPT, 1>(a, &v, ln, lane, &tx, rs, rd);
 #pragma unroll
                         for (int q = 0; q < SPT; ++q) {
                             kahan_add(acc_s[q], cmp_s[q], v.c * rs[0][q]);
