@@ -160,6 +160,9 @@ int vertex_spt(int nl);  // sites per lane of a flow with nl sites
 // with w = 48, 64, 80, 96, 128, a CTA per triple); 4 and 5 are unused.
 constexpr int kVertexClasses = 11;
 int vertex_class(int nl);
+// Lanes of the RPA schedule the vertex kernel of an nl-site flow walks: 32 (a warp per triple)
+// or the CTA's threads (33 to 128 sites).
+int vertex_rpa_lanes(int nl);
 size_t batch_big_smem_bytes(int cls, int n_seg_max);
 
 }  // namespace spn

@@ -505,8 +505,10 @@ spn_su2 *spn::create_flow(const spn_su2_desc *d, cudaStream_t stream) {
             cuda_check(cudaMemsetAsync(h->v2d, 0, h->n * sizeof(double), h->stream), "memset");
             cuda_check(cudaMemsetAsync(h->dv2d, 0, h->n * sizeof(double), h->stream), "memset");
             cuda_check(cudaMemsetAsync(h->status, 0, sizeof(unsigned), h->stream), "memset");
-            // RPA schedule balanced over the 32 lanes of a warp
-            RpaHostSchedule rpa = build_rpa_schedule(h->nl, d->overlap_ptr, d->overlap_rid1, d->overlap_rid2, 32);
+            // RPA schedule balanced over the lanes that walk it (a warp's 32, or the 128 or 256
+            // threads of the CTA-per-triple kernel above 32 sites)
+            RpaHostSchedule rpa = build_rpa_schedule(h->nl, d->overlap_ptr, d->overlap_rid1, d->overlap_rid2,
+                                                     vertex_rpa_lanes(h->nl));
             h->rpa_lanes = rpa.lanes;
             h->rpa_n_seg = rpa.n_seg;
             h->rpa_len = rpa.len;

@@ -1358,7 +1358,7 @@ __device__ __forceinline__ void big_triple(const FlowArgs &a, const float *pos, 
 
     channel(std::integral_constant<int, kS>{}, si);
     channel(std::integral_constant<int, kT>{}, ti);
-    // RPA term: M staged, the merged pair list walked once (32 chunks, warp 0), per-site sums
+    // RPA term: M staged, the merged pair list walked once (one chunk per thread), per-site sums
     __syncthreads();  // every panel update and every descriptor read is done
     {
         const int tr = tid / TC, tc = tid % TC;
@@ -1368,11 +1368,11 @@ __device__ __forceinline__ void big_triple(const FlowArgs &a, const float *pos, 
             for (int j = 0; j < C; ++j) Ms[(tr * R + i) * w + tc * C + j] = M[i][j];
     }
     __syncthreads();
-    if (warp == 0) {
+    if (tid < a.rpa.lanes) {  // the schedule of these lattices has one chunk per thread
         const int lanes = a.rpa.lanes;
-        const int cntq = __ldg(a.rpa.count + lane);
-        int slot = __ldg(a.rpa.slot_base + lane);
-        const int *sched = a.rpa.sched + lane;
+        const int cntq = __ldg(a.rpa.count + tid);
+        int slot = __ldg(a.rpa.slot_base + tid);
+        const int *sched = a.rpa.sched + tid;
         float2 acc = make_float2(0.0f, 0.0f);
         for (int i = 0; i < cntq; ++i) {
             const int e = __ldg(sched + size_t(i) * lanes);
@@ -1499,6 +1499,8 @@ int big_r_of(int nl) {
 }
 int big_class_r(int cls) { return cls == 6 ? 3 : (cls == 7 ? 4 : (cls == 8 ? 5 : (cls == 9 ? 6 : 8))); }
 int big_threads(int r) { return r <= 4 ? 128 : 256; }
+
+int vertex_rpa_lanes(int nl) { return big_r_of(nl) ? big_threads(big_r_of(nl)) : 32; }
 
 int vertex_class(int nl) {
     switch (big_r_of(nl)) {
