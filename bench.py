@@ -119,8 +119,8 @@ def parse_args():
                     help="serve-mixed: arrival rates as multiples of the sequential plain-GPU capacity")
     ap.add_argument("--policy", type=str, default="fifo",
                     help="serve-mixed: server arms to run at every rate, comma separated: fifo or sjf, optionally @k "
-                         "for a k-flow residency limit, or srpt@k (k flows with the least remaining work run at each "
-                         "step), e.g. fifo,sjf@2,srpt@1")
+                         "for a k-flow residency limit, srpt@k (k flows with the least remaining work run at each "
+                         "step) or srpt+old@k (those and the oldest request), e.g. fifo,sjf@2,srpt@1,srpt+old@1")
     ap.add_argument("--grouping", choices=["auto", "on", "off"], default="auto",
                     help="scan/serve: batch configuration chosen by the batch autotuner (auto), cross-flow sharing "
                          "for every group of >= 2 flows (on), or the per-flow kernel without sharing (off)")
@@ -518,7 +518,12 @@ def _serve_local(items, arrivals, policy, plain, grouping="auto"):
     from spinparser_gb300.serve import FlowServer
 
     name, _, slots = policy.partition("@")
-    srv = FlowServer(policy=name, max_flows=int(slots) if slots else None, autotune=(grouping == "auto"))
+    keep_oldest = name.endswith("+old")
+    name = name[:-len("+old")] if keep_oldest else name
+    # the scan (every flow admitted at once) is tuned once its flows have stepped together; a
+    # request stream's running set changes too often for tuning to pay
+    srv = FlowServer(policy=name, max_flows=int(slots) if slots else None, keep_oldest=keep_oldest,
+                     autotune=(grouping == "auto" and not np.any(arrivals)))
     if grouping == "off":
         srv.batch.set_grouping(0)
     elif grouping == "on":

@@ -114,7 +114,8 @@ def next_ticket(queue, policy: str, now: float | None = None, max_wait: float | 
 class FlowServer:
     def __init__(self, device: int = 0, memory_budget: int | None = None, max_flows: int | None = None,
                  nodes_per_iteration: int = 1, use_graph: bool = True, clock=time.perf_counter, policy: str = "fifo",
-                 max_wait: float | None = None, autotune: bool = False, autotune_interval: int = 50):
+                 max_wait: float | None = None, autotune: bool = False, autotune_interval: int = 50,
+                 keep_oldest: bool = False):
         if policy not in ("fifo", "sjf", "srpt"):
             raise ValueError("policy must be 'fifo', 'sjf' or 'srpt'")
         self.policy = policy
@@ -125,6 +126,9 @@ class FlowServer:
         if policy == "srpt":
             max_flows = None
         self._paused: set[int] = set()
+        # srpt: the oldest resident request runs at every step as well, so that the request the
+        # policy would defer longest keeps making progress (bounds the tail of time to result)
+        self.keep_oldest = keep_oldest
         # batch autotuner: run once a set of running flows has stepped together for
         # autotune_interval steps (the first steps of a flow, at large cutoffs, have few
         # loop-frequency nodes and do not show which configuration wins later)
@@ -186,7 +190,8 @@ class FlowServer:
 
     def _choose_running(self) -> None:
         """srpt: the `running` resident flows with the least remaining work take the next step
-        (ties to the older request); every other resident flow is paused."""
+        (ties to the older request), and with keep_oldest also the oldest resident request;
+        every other resident flow is paused."""
         rem = []
         for fid, t in self.active.items():
             _, step, _ = self.batch.poll(fid)
@@ -194,6 +199,8 @@ class FlowServer:
             rem.append((t.work * max(n_cut - 1 - step, 0) / max(n_cut - 1, 1), t.id, fid))
         rem.sort()
         run = {fid for _, _, fid in rem[:self.running]}
+        if self.keep_oldest and self.active:
+            run.add(min(self.active, key=lambda f: (self.active[f].t_arrival, self.active[f].id)))
         for fid in self.active:
             want = fid not in run
             if want != (fid in self._paused):

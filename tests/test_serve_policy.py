@@ -103,3 +103,17 @@ def test_srpt_runs_the_flows_with_least_remaining_work():
     srv.running = 2
     srv._choose_running()
     assert srv.batch.paused == set()
+
+
+def test_srpt_keeps_the_oldest_request_running():
+    from spinparser_gb300.serve import FlowServer, prepare
+
+    srv = FlowServer.__new__(FlowServer)
+    srv.policy, srv.running, srv._paused, srv.keep_oldest = "srpt", 1, set(), True
+    big, small = Ticket(0, spec(5, 16), 0.0), Ticket(1, spec(3, 8), 1.0)
+    for t in (big, small):
+        prepare(t)
+    srv.active = {10: big, 11: small}
+    srv.batch = _FakeBatch({10: 0, 11: 0})
+    srv._choose_running()
+    assert srv.batch.paused == set()  # the least remaining work and the oldest request both run
