@@ -88,7 +88,7 @@ def test_srpt_runs_the_flows_with_least_remaining_work():
     from spinparser_gb300.serve import FlowServer, prepare
 
     srv = FlowServer.__new__(FlowServer)  # host logic only: no device batch
-    srv.policy, srv.running, srv._paused = "srpt", 1, set()
+    srv.policy, srv.running, srv._paused, srv.keep_oldest = "srpt", 1, set(), False
     big, small = Ticket(0, spec(5, 16), 0.0), Ticket(1, spec(3, 8), 1.0)
     for t in (big, small):
         prepare(t)
