@@ -808,10 +808,25 @@ extern "C" int spn_batch_autotune(spn_batch *b, int reps, int *npi, int *min_gro
         const Cand keep{b->npi, b->min_group, b->group_cap_div, b->stage_sched};
         Cand best = keep;
         float best_t = -1.0f;
-        cudaEvent_t e0, e1;
-        cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
-        cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
+        struct Events {  // released on every path out
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            ~Events() {
+                if (e0) cudaEventDestroy(e0);
+                if (e1) cudaEventDestroy(e1);
+            }
+        } ev;
+        cuda_check(cudaEventCreate(&ev.e0), "cudaEventCreate");
+        cuda_check(cudaEventCreate(&ev.e1), "cudaEventCreate");
+        cudaEvent_t e0 = ev.e0, e1 = ev.e1;
+        auto restore = [&](const Cand &c) {
+            b->npi = c.npi;
+            b->min_group = c.min_group;
+            b->group_cap_div = c.cap;
+            b->stage_sched = c.stage;
+            b->plan_valid = false;
+        };
         bool front_done = false;
+        try {
         for (const Cand &c : cands) {
             b->npi = c.npi;
             b->min_group = c.min_group;
@@ -842,13 +857,11 @@ extern "C" int spn_batch_autotune(spn_batch *b, int reps, int *npi, int *min_gro
                 best = c;
             }
         }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        b->npi = best.npi;
-        b->min_group = best.min_group;
-        b->group_cap_div = best.cap;
-        b->stage_sched = best.stage;
-        b->plan_valid = false;
+        } catch (...) {
+            restore(keep);  // a failed candidate leaves the batch as it was
+            throw;
+        }
+        restore(best);
         if (npi) *npi = best.npi;
         if (min_group) *min_group = best.min_group;
         if (cap_divisor) *cap_divisor = best.cap;
