@@ -827,36 +827,36 @@ extern "C" int spn_batch_autotune(spn_batch *b, int reps, int *npi, int *min_gro
         };
         bool front_done = false;
         try {
-        for (const Cand &c : cands) {
-            b->npi = c.npi;
-            b->min_group = c.min_group;
-            b->group_cap_div = c.cap;
-            b->stage_sched = c.stage;
-            b->build_plan();
-            if (b->n_flowing == 0) break;
-            if (c.min_group > 0 && b->n_grouped == 0) continue;  // nothing to share
-            if (!front_done) {
-                b->enqueue_front();
-                front_done = true;
-            }
-            cuda_check(cudaMemsetAsync(b->d_counters, 0, kCounters * sizeof(int), b->stream), "memset");
-            b->enqueue_vertex();  // warm-up
-            cuda_check(cudaEventRecord(e0, b->stream), "record");
-            for (int r = 0; r < reps; ++r) {
+            for (const Cand &c : cands) {
+                b->npi = c.npi;
+                b->min_group = c.min_group;
+                b->group_cap_div = c.cap;
+                b->stage_sched = c.stage;
+                b->build_plan();
+                if (b->n_flowing == 0) break;
+                if (c.min_group > 0 && b->n_grouped == 0) continue;  // nothing to share
+                if (!front_done) {
+                    b->enqueue_front();
+                    front_done = true;
+                }
                 cuda_check(cudaMemsetAsync(b->d_counters, 0, kCounters * sizeof(int), b->stream), "memset");
-                b->enqueue_vertex();
+                b->enqueue_vertex();  // warm-up
+                cuda_check(cudaEventRecord(e0, b->stream), "record");
+                for (int r = 0; r < reps; ++r) {
+                    cuda_check(cudaMemsetAsync(b->d_counters, 0, kCounters * sizeof(int), b->stream), "memset");
+                    b->enqueue_vertex();
+                }
+                cuda_check(cudaEventRecord(e1, b->stream), "record");
+                cuda_check(cudaEventSynchronize(e1), "sync");
+                cuda_check(cudaGetLastError(), "autotune launch");
+                float ms = 0.0f;
+                cuda_check(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+                ms /= float(reps);
+                if (best_t < 0.0f || ms < best_t) {
+                    best_t = ms;
+                    best = c;
+                }
             }
-            cuda_check(cudaEventRecord(e1, b->stream), "record");
-            cuda_check(cudaEventSynchronize(e1), "sync");
-            cuda_check(cudaGetLastError(), "autotune launch");
-            float ms = 0.0f;
-            cuda_check(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
-            ms /= float(reps);
-            if (best_t < 0.0f || ms < best_t) {
-                best_t = ms;
-                best = c;
-            }
-        }
         } catch (...) {
             restore(keep);  // a failed candidate leaves the batch as it was
             throw;
