@@ -328,8 +328,9 @@ int spn_batch_set_paused(spn_batch *b, int flow_id, int paused);
 /* Flows the current plan evaluates with the grouped kernel. */
 int spn_batch_grouped_flows(spn_batch *b, int *n_grouped);
 /* Batch autotuner: times the vertex flow of the current flows, `reps` launches per candidate,
- * over nodes per iteration (1, 2) x RPA schedule staging (without sharing) and x sharing (full
- * or half subgroups), and keeps the fastest (returned, with its time per launch in ms).
+ * over nodes per iteration (1, 2) x RPA schedule staging (without sharing) and, if sharing is
+ * enabled (spn_batch_set_grouping), x sharing (full or half subgroups), and keeps the fastest
+ * (returned, with its time per launch in ms).
  * Touches no flow's state or results; call it between steps, after the flows of interest are
  * admitted.  Replaces the reference LoadManager's chunk-size choice
  * (src/lib/LoadManager.hpp:796-852). */

@@ -787,8 +787,8 @@ extern "C" int spn_batch_remove(spn_batch *b, int flow_id) {
 // Times the vertex flow of the batch's current flows under each candidate configuration and
 // keeps the fastest: nodes per group iteration of the per-flow kernel (1, 2) x its RPA schedule
 // (read from global memory, staged per warp in shared memory: more shared memory, fewer
-// resident blocks) without sharing, and (1, 2) x cross-flow sharing in subgroups of the
-// grouped kernel's full block or of half of it.  The front of a
+// resident blocks) without sharing, and, when the caller enabled sharing, (1, 2) x cross-flow
+// sharing in subgroups of the grouped kernel's full block or of half of it.  The front of a
 // step runs once first (self-energy flow and node tables of the current states); the timed
 // launches write only the flows' vertex-flow buffers, which hold nothing between steps, so
 // no flow's state or results change.  It replaces the reference LoadManager's choice of chunk
@@ -806,6 +806,9 @@ extern "C" int spn_batch_autotune(spn_batch *b, int reps, int *npi, int *min_gro
         const Cand cands[] = {{1, 0, 1, false}, {2, 0, 1, false}, {1, 0, 1, true}, {2, 0, 1, true},
                               {1, 2, 1, false}, {2, 2, 1, false}, {1, 2, 2, false}, {2, 2, 2, false}};
         const Cand keep{b->npi, b->min_group, b->group_cap_div, b->stage_sched};
+        // sharing is a candidate only when the caller enabled it (spn_batch_set_grouping): on
+        // a scan it wins in the first steps and loses in the later ones, which dominate
+        const bool sharing = b->min_group > 0;
         Cand best = keep;
         float best_t = -1.0f;
         struct Events {  // released on every path out
@@ -832,9 +835,10 @@ extern "C" int spn_batch_autotune(spn_batch *b, int reps, int *npi, int *min_gro
                 b->min_group = c.min_group;
                 b->group_cap_div = c.cap;
                 b->stage_sched = c.stage;
+                if (c.min_group > 0 && !sharing) continue;
                 b->build_plan();
                 if (b->n_flowing == 0) break;
-                if (c.min_group > 0 && b->n_grouped == 0) continue;  // nothing to share
+                if (c.min_group > 0 && (!sharing || b->n_grouped == 0)) continue;  // not enabled / nothing to share
                 if (!front_done) {
                     b->enqueue_front();
                     front_done = true;

@@ -133,6 +133,7 @@ def test_late_joiners_and_other_cutoff_lists_are_not_grouped_with_running_flows(
 def test_autotuned_batch_keeps_results():
     cut = spn.cutoff_exponential(*CUT)
     b = Su2Batch()
+    b.set_grouping(2)  # sharing enabled: the autotuner weighs it against the per-flow kernel
     specs = [(3, j2, 10) for j2 in (0.1, 0.3, 0.5, 0.7)] + [(7, j2, 8) for j2 in (0.2, 0.8)] + [(11, 0.4, 6)]
     ids = [add(b, *sp, cut) for sp in specs]
     b.step()  # the autotuner runs between steps, on states a step has produced
