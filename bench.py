@@ -34,11 +34,15 @@ HDF5, absent here): every timed step one complete cutoff step at the cutoffs the
 times, so steps x ms_per_step is CPU time actually spent.  --gpus N > 1: replicas only
 (independent flows, no collective).
 
-Other workloads (--workload): pyrochlore-r5-n64, square-r3-n32 (the same line for other
-shapes); scan-square-j1j2-128 and serve-mixed (batched and served flows against sequential
-plain solves; --flows, --rates, --policy fifo|sjf[@slots]); precision-* (FP32 forms against
-the FP64 GPU flow); xyz-honeycomb-kitaev-r9-n48 and tri-honeycomb-kitaev-gamma-r9-n32 (whole
-flows of the XYZ and TRI cores against their oracles; --flow-cutoffs M for short runs).
+Other workloads (--workload): pyrochlore-r5-n64, square-r3-n32, the serving mix's largest
+classes pyrochlore-j1j2-r6-n64 / -r7-n64 and the reference README's readme-square-r4-n32 (the
+same line for other shapes; --impl reference --cpu-full-flow times a whole CPU flow);
+scan-square-j1j2-128 and serve-mixed (batched and served flows against sequential plain solves,
+dealt over ranks under torchrun; --flows, --rates, --policy fifo|sjf[@k]|srpt[@k]|srpt+old[@k],
+--grouping auto|on|off; --impl reference: the CPU port's flows/s; --profile-window START,COUNT:
+batch steps inside an NVTX range for ncu); precision-* (FP32 forms against the FP64 GPU flow);
+xyz-honeycomb-kitaev-r9-n48 and tri-honeycomb-kitaev-gamma-r9-n32 (whole flows of the XYZ and
+TRI cores against their oracles; --flow-cutoffs M for short runs).
 """
 from __future__ import annotations
 
