@@ -997,8 +997,10 @@ def main():
     nominal = flops_nominal(tab, n)
     achieved = nominal / (avg_vertex_ms * 1e-3) / 1e12
     achieved_eval = flops_eval / (prof["vertex_ms"] * 1e-3) / 1e12
+    # the dominant kernel: a warp per triple up to 32 sites, a CTA per triple above
+    kernel = "su2_vertex_flow_kernel" if tab.n_sites <= 32 else "su2_vertex_big_kernel"
     traffic = None
-    prof_file = os.path.join(ROOT, "profiles", f"vertex_flow_{args.workload}.json")
+    prof_file = os.path.join(ROOT, "profiles", f"{kernel.replace('su2_', '').replace('_kernel', '')}_{args.workload}.json")
     if os.path.exists(prof_file):
         traffic = json.load(open(prof_file)).get("dram_bytes_per_launch")
 
@@ -1015,7 +1017,7 @@ def main():
         "config": workload_config(args, wl, tab, cut, n, world),
         "e2e": {"value": len(e2e_sched) / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": state_bytes,
                 "d2h_bytes_per_step": state_bytes + 8 * flow.n_corr},
-        "roofline": {"bound": "fp32", "kernel": "su2_vertex_flow_kernel", "achieved": achieved, "peak": fp32_peak,
+        "roofline": {"bound": "fp32", "kernel": kernel, "achieved": achieved, "peak": fp32_peak,
                      "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": traffic,
                      "algorithmic_flops_per_launch": nominal, "avg_launch_ms": avg_vertex_ms,
                      "achieved_evaluated": achieved_eval, "frac_evaluated": achieved_eval / fp32_peak,
@@ -1023,7 +1025,7 @@ def main():
                                     "FP32 CUDA-core figure)", "fp32_clock_ghz_implied": clk,
                      "gather": gather},
         "precision_form": PRECISION_FORMS[args.precision],
-        "vertex_variant": variant,
+        "vertex_variant": dict(variant, kernel=kernel),
         "gpu_launches": KERNELS_PER_STEP * len(schedule),
         "clocks": clocks,
         "full_flow": full,
