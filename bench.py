@@ -67,8 +67,8 @@ WORKLOADS = {
                           n_freq=32, fmin=0.005, fmax=50.0, cmax=50.0, cmin=0.05, cstep=0.98),
     "pyrochlore-r5-n64": dict(lattice="pyrochlore", range=5, model="pyrochlore-heisenberg", params={"j": "1.0"},
                               n_freq=64, fmin=0.002, fmax=100.0, cmax=100.0, cmin=0.01, cstep=0.99),
-    # the largest request classes of the serving mix: pyrochlore range 6 (48 sites, two per
-    # lane) and range 7 (70 sites, four per lane), J1-J2 with J2 = 0.25
+    # the largest request classes of the serving mix: pyrochlore range 6 (48 sites) and range 7
+    # (70 sites), both on the CTA-per-triple kernel, J1-J2 with J2 = 0.25
     "pyrochlore-j1j2-r6-n64": dict(lattice="pyrochlore", range=6, model="pyrochlore-j1j2heisenberg",
                                    params={"j1": "1.0", "j2": "0.25"}, n_freq=64, fmin=0.005, fmax=50.0, cmax=50.0,
                                    cmin=0.05, cstep=0.98),

@@ -264,6 +264,60 @@ __device__ __forceinline__ int make_part(const FlowArgs &a, const float *pos, co
     }
 }
 
+// make_desc split over the two threads of a lane pair (h = 0, 1), for a CTA that builds 128
+// nodes with 256 threads.  Thread h builds the two main buffers that share its pair of
+// interpolated magnitudes, buffers h and h + 2 (and in the t channel the two local buffers of
+// the same magnitudes, whose values go to lv); the coordinates come from selects, so the pair
+// runs one instruction stream.  Every coordinate is the value make_desc passes (negations are
+// exact), so the descriptor is the same bits.  Returns the exchange and sign bits of the
+// thread's buffers; the pair ORs them into d.exch.
+template <int CH>
+__device__ __forceinline__ int make_pair(const FlowArgs &a, const float *pos, const Transfer &f, float wp, int h,
+                                         NodeDesc &d) {
+    AB4 ab;
+    const int nl = a.nl, n = a.n;
+    const MeshIndex m{pos, a.n, a.mesh_lo, a.mesh_base, a.mesh_shift};
+    const bool odd = h & 1;
+    int bits = 0;
+    if (CH == kS) {
+        // buffers (t, u): 0 (-A, -B), 2 (B, A) from (A, B); 1 (P, -Q), 3 (-Q, P) from (P, Q)
+        const float y1 = odd ? f.w1p + wp : f.w1 + wp, y2 = odd ? f.w2p + wp : f.w2 + wp;
+        const Interp<float> i1 = interp_abs(m, y1), i2 = interp_abs(m, y2);
+        access4i<kS>(n, nl, f.s, odd ? y1 : -y1, -y2, i1, i2, f.si, ab);
+        bits |= put_ab(d, h, ab) | (int(ab.exch) << h);
+        access4i<kS>(n, nl, f.s, odd ? -y2 : y2, y1, i2, i1, f.si, ab);
+        bits |= put_ab(d, h + 2, ab) | (int(ab.exch) << (h + 2));
+    } else if (CH == kU) {
+        // buffers (s, t): 0 (A, -D), 2 (D, -A) from (A, D); 1 (P, E), 3 (E, P) from (P, E)
+        const float y1 = odd ? f.w1p + wp : f.w1 + wp, y2 = odd ? f.w2 - wp : f.w2p - wp;
+        const Interp<float> i1 = interp_abs(m, y1), i2 = interp_abs(m, y2);
+        access4i<kU>(n, nl, y1, odd ? y2 : -y2, f.u, i1, i2, f.ui, ab);
+        bits |= put_ab(d, h, ab) | (int(ab.exch) << h);
+        access4i<kU>(n, nl, y2, odd ? y1 : -y1, f.u, i2, i1, f.ui, ab);
+        bits |= put_ab(d, h + 2, ab) | (int(ab.exch) << (h + 2));
+    } else {
+        // main buffers (s, u): 0 (C, P), 2 (P, C) from (C, P); 1 (D, -B), 3 (B, -D) from (D, B);
+        // local buffers (s, t, u) to lv: 1 (C, -P, -t), 3 (P, -C, -t); 0 (D, -B, t), 2 (B, -D, t)
+        const float x1 = odd ? f.w2p - wp : f.w1 - wp, x2 = odd ? f.w2 + wp : f.w1p + wp;
+        const Interp<float> i1 = interp_abs(m, x1), i2 = interp_abs(m, x2);
+        access4i<kT>(n, nl, x1, f.t, odd ? -x2 : x2, i1, i2, f.ti, ab);
+        bits |= put_ab(d, h, ab) | (int(ab.exch) << h);
+        access4i<kT>(n, nl, x2, f.t, odd ? -x1 : x1, i2, i1, f.ti, ab);
+        bits |= put_ab(d, h + 2, ab) | (int(ab.exch) << (h + 2));
+        const float tl = odd ? f.t : -f.t;
+        float v0, v1;
+        access4i<kU>(n, nl, x1, -x2, tl, i1, i2, f.ti, ab);
+        local_pair(a, ab, v0, v1);
+        d.lv[odd ? 0 : 2] = v0;
+        d.lv[odd ? 1 : 3] = v1;
+        access4i<kU>(n, nl, x2, -x1, tl, i2, i1, f.ti, ab);
+        local_pair(a, ab, v0, v1);
+        d.lv[odd ? 4 : 6] = v0;
+        d.lv[odd ? 5 : 7] = v1;
+    }
+    return bits;
+}
+
 // The t channel's eight site-local values of one node for one flow's state (make_desc's
 // local_pair of each local buffer, in the same order).
 __device__ __forceinline__ void group_local_values(const float2 *sd, const LocDesc &loc, float *lv) {
@@ -1219,6 +1273,9 @@ __global__ void __launch_bounds__(kGroupWarps * 32) su2_vertex_group_kernel(Grou
 constexpr int kBigBatch = 128;  // node descriptors built at once (one per thread)
 
 __host__ __device__ constexpr int big_spt(int R) { return (16 * R + 31) / 32; }
+// CTAs per SM the register budget is sized for (128 registers a thread up to w = 96; M of
+// w = 128 takes a whole SM's shared memory anyway)
+__host__ __device__ constexpr int big_min_blocks(int R, int NT) { return R > 6 ? 1 : 65536 / (128 * NT); }
 
 struct BigSmem {
     size_t pos, u, panels, parts, rpa, total;
@@ -1293,8 +1350,11 @@ __device__ __forceinline__ void big_triple(const FlowArgs &a, const float *pos, 
         const int j = lane + 32 * k;
         ln.j[k] = j;
         ln.valid[k] = j < a.nl;
-        ln.site[k] = ln.valid[k] ? a.sites[j] : 0;
-        ln.isite[k] = ln.valid[k] ? a.inv_sites[j] : 0;
+        // a lane past the last site reads the last site's element (same cache line as its
+        // slot's valid lanes; the value is never used)
+        const int jc = ln.valid[k] ? j : a.nl - 1;
+        ln.site[k] = a.sites[jc];
+        ln.isite[k] = a.inv_sites[jc];
     }
     float acc_s[SPT], cmp_s[SPT], acc_d[SPT], cmp_d[SPT];
 #pragma unroll
@@ -1314,7 +1374,21 @@ __device__ __forceinline__ void big_triple(const FlowArgs &a, const float *pos, 
         for (int b0 = 0; b0 < cnt; b0 += kBigBatch) {
             const int nb = min(kBigBatch, cnt - b0);
             __syncthreads();  // the previous batch's descriptors (or M) are no longer read
-            if (tid < nb) {
+            if constexpr (NT >= 2 * kBigBatch) {  // a lane pair per node, half its buffers each
+                const int k = tid >> 1;
+                float c = 0.0f;
+                int bits = 0;
+                if (k < nb) {
+                    c = __ldg(nc + b0 + k);
+                    if (CH == kU) c = -c;
+                    bits = make_pair<CH>(a, pos, f, __ldg(nwp + b0 + k), tid & 1, desc[k]);
+                }
+                bits |= __shfl_xor_sync(0xffffffffu, bits, 1);
+                if (k < nb && !(tid & 1)) {
+                    desc[k].exch = bits;
+                    desc[k].c = c;
+                }
+            } else if (tid < nb) {
                 float c = __ldg(nc + b0 + tid);
                 if (CH == kU) c = -c;
                 make_desc<CH>(a, pos, f, __ldg(nwp + b0 + tid), c, desc[tid]);
@@ -1422,7 +1496,7 @@ __device__ __forceinline__ void big_triple(const FlowArgs &a, const float *pos, 
 }
 
 template <int R, int NT>
-__global__ void __launch_bounds__(NT) su2_vertex_big_kernel(FlowArgs a) {
+__global__ void __launch_bounds__(NT, big_min_blocks(R, NT)) su2_vertex_big_kernel(FlowArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_item;
     const BigSmem L = big_smem_layout(R, NT, a.rpa.n_seg);
@@ -1442,7 +1516,7 @@ __global__ void __launch_bounds__(NT) su2_vertex_big_kernel(FlowArgs a) {
 // one big class; the CTA reloads the flow's argument block and mesh when the flow changes
 // (items are numbered flow by flow).
 template <int R, int NT>
-__global__ void __launch_bounds__(NT) su2_vertex_big_batch_kernel(BatchVertexArgs b) {
+__global__ void __launch_bounds__(NT, big_min_blocks(R, NT)) su2_vertex_big_batch_kernel(BatchVertexArgs b) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_item;
     __shared__ __align__(16) FlowArgs fa;
