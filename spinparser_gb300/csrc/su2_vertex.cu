@@ -1261,7 +1261,8 @@ __global__ void __launch_bounds__(kGroupWarps * 32) su2_vertex_group_kernel(Grou
 // w = 16 R >= Nl) no longer fits one warp's registers, and a warp that owns a triple would walk
 // the whole merged RPA pair list for every t-channel node (585 entries per lane and node for the
 // 70-site pyrochlore range 7).  Here the CTA's NT threads (128 or 256) share a triple: they
-// build up to 128 node descriptors at once (one per thread), the NT / 32 warps evaluate the
+// build up to 128 node descriptors at once (one per thread at 128 threads, one per lane pair
+// at 256, make_pair), the NT / 32 warps evaluate the
 // nodes round-robin (lane = site, ceil(w / 32) sites per lane), and in the t channel each warp
 // writes its node's panel to shared memory (double-buffered: one block barrier per round of
 // NT / 32 nodes), after which every thread adds the round's panels to its block of M (the
@@ -1270,7 +1271,7 @@ __global__ void __launch_bounds__(kGroupWarps * 32) su2_vertex_group_kernel(Grou
 // Each warp keeps Kahan sums over its nodes per site; the warps' sums and the RPA term are
 // combined in a fixed order, so results do not depend on the launch.
 // ------------------------------------------------------------------------------------
-constexpr int kBigBatch = 128;  // node descriptors built at once (one per thread)
+constexpr int kBigBatch = 128;  // node descriptors built at once
 
 __host__ __device__ constexpr int big_spt(int R) { return (16 * R + 31) / 32; }
 // CTAs per SM the register budget is sized for (128 registers a thread up to w = 96; M of
@@ -1566,13 +1567,13 @@ int outer_w_of(int nl) { return nl <= 32 ? rpa_outer_width(nl) : 0; }
 
 }  // namespace
 
-// Lattices of 33 to 128 sites use the CTA-per-triple kernel: w = 16 R >= Nl, R = 3, 4 with 128
-// threads, R = 5, 6, 8 with 256 (classes 6..10).
+// Lattices of 33 to 128 sites use the CTA-per-triple kernel: w = 16 R >= Nl, R = 3 with 128
+// threads, R = 4, 5, 6, 8 with 256 (classes 6..10).
 int big_r_of(int nl) {
     return nl <= 32 ? 0 : (nl <= 48 ? 3 : (nl <= 64 ? 4 : (nl <= 80 ? 5 : (nl <= 96 ? 6 : 8))));
 }
 int big_class_r(int cls) { return cls == 6 ? 3 : (cls == 7 ? 4 : (cls == 8 ? 5 : (cls == 9 ? 6 : 8))); }
-int big_threads(int r) { return r <= 4 ? 128 : 256; }
+int big_threads(int r) { return r <= 3 ? 128 : 256; }
 
 int vertex_rpa_lanes(int nl) { return big_r_of(nl) ? big_threads(big_r_of(nl)) : 32; }
 
@@ -1607,7 +1608,7 @@ VertexKernel vertex_kernel(int cls, int npi) {
         case 2: return vertex_kernel_npi<1, 3>(npi);
         case 3: return vertex_kernel_npi<1, 4>(npi);
         case 6: return su2_vertex_big_kernel<3, 128>;
-        case 7: return su2_vertex_big_kernel<4, 128>;
+        case 7: return su2_vertex_big_kernel<4, 256>;
         case 8: return su2_vertex_big_kernel<5, 256>;
         case 9: return su2_vertex_big_kernel<6, 256>;
         default: return su2_vertex_big_kernel<8, 256>;
@@ -1662,7 +1663,7 @@ BatchKernel batch_kernel(int cls, int npi) {
         case 2: return batch_kernel_npi<1, 3>(npi);
         case 3: return batch_kernel_npi<1, 4>(npi);
         case 6: return su2_vertex_big_batch_kernel<3, 128>;
-        case 7: return su2_vertex_big_batch_kernel<4, 128>;
+        case 7: return su2_vertex_big_batch_kernel<4, 256>;
         case 8: return su2_vertex_big_batch_kernel<5, 256>;
         case 9: return su2_vertex_big_batch_kernel<6, 256>;
         default: return su2_vertex_big_batch_kernel<8, 256>;

@@ -70,6 +70,7 @@ def test_rhs_square_r3_n32_matches_oracle(square_r3):
     ("square", 3, "square-heisenberg", {"j": "1.0"}, 14),
     ("cubic", 3, "cubic-j1j2heisenberg", {"j1": "1.0", "j2": "0.25"}, 14),
     ("square", 11, "square-heisenberg", {"j": "1.0"}, 8),   # 42 sites: a CTA per triple, w = 48
+    ("square", 13, "square-heisenberg", {"j": "1.0"}, 6),   # 56 sites: w = 64
     ("square", 15, "square-heisenberg", {"j": "1.0"}, 6),   # 72 sites: w = 80, 256 threads
     ("square", 17, "square-heisenberg", {"j": "1.0"}, 4),   # 90 sites: w = 96
     ("square", 20, "square-heisenberg", {"j": "1.0"}, 4),   # 121 sites: w = 128
@@ -79,7 +80,8 @@ def test_every_vertex_variant_matches_oracle(lattice, rng, model, params, n):
     schedule in shared or global memory) reproduces the oracle, and all variants give the
     same bits (a group takes its nodes in the same order whatever the variant), so autotuning
     never changes a result.  Lattices of 6 and 8 sites run the warp-per-triple kernel, of 42,
-    72, 90 and 121 sites the CTA-per-triple kernel (w = 48, 80, 96, 128), which has no variants."""
+    56, 72, 90 and 121 sites the CTA-per-triple kernel (w = 48, 64, 80, 96, 128), which has no
+    variants."""
     tab = spn.Lattice(lattice, rng, model, params).tables()
     freq = spn.frequency_exponential(0.01, 30.0, n)
     orc = Oracle(tab, freq)
