@@ -1351,8 +1351,8 @@ __device__ __forceinline__ void big_triple(const FlowArgs &a, const float *pos, 
         const int j = lane + 32 * k;
         ln.j[k] = j;
         ln.valid[k] = j < a.nl;
-        // a lane past the last site reads the last site's element (same cache line as its
-        // slot's valid lanes; the value is never used)
+        // a lane past the last site reads the last site's element (never used), which lies
+        // among the elements its slot's valid lanes read, not the slab's first line
         const int jc = ln.valid[k] ? j : a.nl - 1;
         ln.site[k] = a.sites[jc];
         ln.isite[k] = a.inv_sites[jc];

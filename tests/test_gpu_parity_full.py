@@ -8,6 +8,9 @@ oracle (the restatement of src/SU2/SU2FrgCore.cpp:89-431), at the shapes the ben
   GPU flow itself, advanced from the initial condition and read back with get_state.
 * pyrochlore r5, N = 64 on [0.002, 100]: the complete RHS at the last cutoff of 100 -> 0.01 x 0.99
   (917 values), from the GPU-advanced state.
+* pyrochlore J1-J2 r6 and r7, N = 64 on [0.005, 50] (48 and 70 sites: the CTA-per-triple kernel at
+  128 and at 256 threads): the complete RHS at a mid-flow and at the last cutoff of 50 -> 0.05 x
+  0.98 (342 values), from the GPU-advanced state.
 * square r3, N = 32 on [0.005, 50], 50 -> 0.05 x 0.98 (342 cutoffs, 341 RHS evaluations): the
   whole flow on the GPU against the whole flow of the FP32 oracle (the reference's arithmetic)
   and of the FP64 oracle.  Correlations are compared at every cutoff.
@@ -94,6 +97,18 @@ def test_whole_rhs_pyrochlore_r5_n64_late():
     assert len(cut) == 917
     flow, states = advanced_states(tab, freq, cut, (915,))
     check_rhs(flow, Oracle(tab, freq), states[915], "pyrochlore r5 N64 step 915")
+    flow.close()
+
+
+@pytest.mark.parametrize("rng,stop", [(6, 171), (7, 340)])
+def test_whole_rhs_pyrochlore_j1j2_cta_per_triple(rng, stop):
+    tab = spn.Lattice("pyrochlore", rng, "pyrochlore-j1j2heisenberg", {"j1": "1.0", "j2": "0.25"}).tables()
+    assert tab.n_sites == {6: 48, 7: 70}[rng]
+    freq = spn.frequency_exponential(0.005, 50.0, 64)
+    cut = spn.cutoff_exponential(50.0, 0.05, 0.98)
+    assert len(cut) == 342
+    flow, states = advanced_states(tab, freq, cut, (stop,))
+    check_rhs(flow, Oracle(tab, freq), states[stop], f"pyrochlore J1-J2 r{rng} N64 step {stop}")
     flow.close()
 
 
