@@ -119,7 +119,9 @@ int spn_lattice_get_sites(const spn_lattice *lat, int *site_params, int *pair_ri
 int spn_lattice_get_interactions(const spn_lattice *lat, int *rid, float *coupling);
 
 /* The RPA schedule the device uses for a lattice (diagnostics; host only): the merged pair
- * lists of all rids cut into `lanes` balanced chunks (csrc/host/rpa_schedule.hpp).
+ * lists of all rids cut into `lanes` balanced chunks (csrc/host/rpa_schedule.hpp; 1 <= lanes <=
+ * 256: the device walks it with a warp's 32 lanes up to 32 sites, with the 128 or 256 threads of
+ * a CTA above), the entries of each segment ordered against shared-memory bank collisions.
  * info[5] = {entries per lane, segments, total ints of sched, packed encoding (Nl <= 32),
  * row width of the outer-product matrix the packed entries index (0 otherwise)}.
  * With sched = NULL only info is filled; otherwise sched must hold info[2] ints, count and

@@ -347,7 +347,7 @@ extern "C" int spn_tri_tables(int *rows) {
 extern "C" int spn_rpa_schedule(int n_sites, const int *overlap_ptr, const int *overlap_rid1, const int *overlap_rid2,
                                 int lanes, int *info, int *sched, int *count, int *slot_base, int *seg_ptr) {
     return spn::guarded([&] {
-        if (n_sites < 1 || n_sites > 128 || !overlap_ptr || !info || lanes < 1 || lanes > 32)
+        if (n_sites < 1 || n_sites > 128 || !overlap_ptr || !info || lanes < 1 || lanes > 256)
             throw spn::Error(spn::ErrorType::Argument, "spn_rpa_schedule: bad argument");
         const int nov = overlap_ptr[n_sites];
         for (int r = 0; r < n_sites; ++r)

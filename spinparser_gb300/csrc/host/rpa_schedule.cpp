@@ -64,6 +64,34 @@ RpaHostSchedule build_rpa_schedule(int nl, const int *ptr, const int *r1, const 
     s.packed = nl <= 32;
     s.width = s.packed ? rpa_outer_width(nl) : 0;
 
+    // Order the entries inside each segment against shared-memory bank collisions: the walk
+    // reads the float2 element M[rid1][rid2], and a 64-bit read is served per half warp, 16
+    // lanes in one wavefront when they hit 16 distinct bank pairs.  Step by step, each lane of a
+    // half warp takes from the rest of its current segment the first entry whose bank pair
+    // ((rid1 * row + rid2) mod 16; the row width is a multiple of 16 above 32 sites) no lower
+    // lane of the half warp took at that step (else one whose bank pair the fewest took).  A
+    // segment's sum is the same set of terms in another order.
+    auto bank = [&](const Pair &p) { return int(unsigned(s.packed ? p.a * s.width + p.b : p.b) & 15u); };
+    for (int h0 = 0; h0 < lanes; h0 += 16) {
+        const int h1 = std::min(lanes, h0 + 16);
+        std::vector<size_t> si(size_t(h1 - h0), 0);
+        for (int i = 0; i < L; ++i) {
+            int taken[16] = {0};
+            for (int l = h0; l < h1; ++l) {
+                if (i >= s.count[l]) continue;
+                size_t &k = si[size_t(l - h0)];
+                if (i == seg_end[l][k]) ++k;  // position i opens the lane's next segment
+                const int end = seg_end[l][k];
+                auto &o = order[l];
+                int pick = i;
+                for (int j = i; j < end && taken[bank(o[size_t(pick)])] > 0; ++j)
+                    if (taken[bank(o[size_t(j)])] < taken[bank(o[size_t(pick)])]) pick = j;
+                std::swap(o[size_t(i)], o[size_t(pick)]);
+                ++taken[bank(o[size_t(i)])];
+            }
+        }
+    }
+
     for (int l = 0; l < lanes; ++l) {
         size_t si = 0;
         for (int i = 0; i < s.count[l]; ++i) {

@@ -45,6 +45,14 @@ def test_descriptor_validation_happens_before_device_use():
     with pytest.raises(spn.SpnError) as e:
         spn.Su2Flow(tab, np.linspace(0.1, 1, 300).astype(np.float32))  # N above the supported maximum
     assert e.value.code == -8
+    with pytest.raises(spn.SpnError) as e:  # one frequency above the largest supported mesh (256)
+        spn.Su2Flow(tab, spn.frequency_exponential(0.005, 50.0, 257))
+    assert e.value.code == -8 and "n_freq" in str(e.value)
+    big = spn.Lattice("square", 21, "square-heisenberg", {"j": 1}).tables()
+    assert big.n_sites == 132  # above the largest supported lattice (128 reduced sites)
+    with pytest.raises(spn.SpnError) as e:
+        spn.Su2Flow(big, spn.frequency_exponential(0.005, 50.0, 8))
+    assert e.value.code == -8 and "n_sites" in str(e.value)
     bad = spn.Lattice("square", 2, "square-heisenberg", {"j": 1}).tables()
     bad.overlap_rid1 = bad.overlap_rid1.copy()
     bad.overlap_rid1[0] = 99

@@ -165,6 +165,40 @@ def test_rhs_large_configs_sampled(lattice, rng, model, params, n):
         assert float(np.abs(gdd[a:b] - rdd).max()) <= RHS_TOL * scale_d
 
 
+def test_rhs_largest_mesh_sampled(square_r3):
+    """The largest supported mesh (N = 256: 8 421 376 triples, up to 2N + 8 = 520 nodes per
+    channel) at a late cutoff: the whole self-energy flow and sampled vertex triples (the first,
+    the last and random ones) against the oracle."""
+    tab = square_r3
+    n = 256
+    freq = spn.frequency_exponential(0.005, 50.0, n)
+    cut = np.array([0.2, 0.1, 0.05, 0.02], np.float32)
+    flow = spn.Su2Flow(tab, freq)
+    flow.set_state(float(cut[0]), *tab.initial_state(n))
+    for k in range(2):
+        flow.compute_step()
+        flow.finalize_step(float(cut[k + 1]))
+    assert not flow.is_diverged()
+    c, v2, ss, dd = flow.get_state()
+    flow.compute_step()
+    g2, gss, gdd = flow.get_flow()
+    assert int(flow.node_counts().max()) > 2 * 64, "late cutoff: long node lists"
+    orc = Oracle(tab, freq)
+    r2 = orc.self_energy(c, v2, ss, dd)
+    assert normwise(g2, r2) <= RHS_TOL
+    nl, fn = tab.n_sites, flow.fn
+    assert fn == n * n * (n + 1) // 2
+    rng_ = np.random.default_rng(4321)
+    starts = sorted(rng_.choice(fn - 8, size=6, replace=False).tolist()) + [0, fn - 8]
+    scale_s, scale_d = float(np.abs(gss).max()), float(np.abs(gdd).max())
+    for s in starts:
+        rss, rdd = orc.vertex_range(c, v2, r2, ss, dd, s, s + 8)
+        a, b = s * nl, (s + 8) * nl
+        assert float(np.abs(gss[a:b] - rss).max()) <= RHS_TOL * scale_s
+        assert float(np.abs(gdd[a:b] - rdd).max()) <= RHS_TOL * scale_d
+    flow.close()
+
+
 def test_euler_update_bit_exact(square_r3):
     tab = square_r3
     freq = spn.frequency_exponential(0.05, 50.0, 10)
