@@ -41,7 +41,7 @@ namespace {
 constexpr int kThreads = 128;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxSites = 128;
-constexpr int kTBatch = 4;  // nodes whose descriptors a warp builds at once
+constexpr int kTBatch = 4;  // nodes whose descriptors a warp builds at once (a quad of lanes each)
 constexpr int kCorrOut = 10;  // XX XY XZ YX YY YZ ZX ZY ZZ DD
 
 // The six spin permutations (X,Y,Z) (X,Z,Y) (Y,X,Z) (Y,Z,X) (Z,X,Y) (Z,Y,X): 2 bits per image
@@ -335,7 +335,7 @@ __global__ void tri_node_table_kernel(FlowArgs f) { node_table_body(f, blockIdx.
 // ------------------------------------------------------------------------------------
 // vertex flow
 // ------------------------------------------------------------------------------------
-// Node descriptor (lane = node while it is built): the four access buffers of the channel's
+// Node descriptor (built by a quad of lanes, make_tpart): the four access buffers of the channel's
 // integrand and, for the t channel, the four of the chalice diagrams' site-local values.
 struct __align__(16) TDesc {
     TAB4 ab[8];
@@ -343,52 +343,43 @@ struct __align__(16) TDesc {
     int pad[3];
 };
 
-// Phase A: the descriptor of one node of channel ch (0 = s, 1 = t, 2 = u).
-__device__ __forceinline__ void make_tdesc(const TriArgs &a, const float *pos, int ch, int e, float s, float t, float u,
-                                           float w1p, float w1, float w2p, float w2, float wp, float c, TDesc &d) {
+// Phase A: the descriptor of one node of channel ch (0 = s, 1 = t, 2 = u), built by the four
+// lanes of a quad (q = 0..3): integralKernelS (TRIFrgCore.cpp:184-188), integralKernelT
+// (TRIFrgCore.cpp:718-724, 1257-1259, 1814-1816) and integralKernelU (TRIFrgCore.cpp:2375-2379)
+// read four access buffers each (the t channel four more for its chalice diagrams' site-local
+// values), and every buffer interpolates two of the node's four distinct magnitudes A = |w1 + wp|,
+// B = |w2 + wp|, C = |w1 - wp|, D = |w2p - wp|, E = |w2 - wp|, P = |w1p + wp|, Q = |w2p + wp|
+// (a coordinate and its negation fold alike; -a - b is bitwise -(a + b), -a + b is b - a).  Lane
+// q builds the buffers of one pair of magnitudes, with the coordinates from selects, so the quad
+// runs one instruction stream: slot q ^ 2 (s channel), slot q (u channel), slots (q & 1) << 1 |
+// q >> 1 and 4 + (q ^ 2) (t channel).
+__device__ __forceinline__ void make_tpart(const TriArgs &a, const float *pos, int ch, int e, float s, float t, float u,
+                                           float w1p, float w1, float w2p, float w2, float wp, int q, TDesc &d) {
     const MeshSearch<float> m{pos, a.n};
     const int nl = a.nl, n = a.n;
-    // each pair of buffers interpolates two of the node's four distinct magnitudes (a
-    // coordinate and its negation fold alike; -a - b is bitwise -(a + b), -a + b is b - a)
-    if (ch == 0) {  // integralKernelS, TRIFrgCore.cpp:184-188
-        {
-            const Interp<float> iA = interp_abs(m, w1 + wp), iB = interp_abs(m, w2 + wp);
-            tri_access4i<kS>(n, nl, s, w2 + wp, w1 + wp, e, iB, iA, d.ab[0]);
-            tri_access4i<kS>(n, nl, s, -w1 - wp, -w2 - wp, e, iA, iB, d.ab[2]);
-        }
-        {
-            const Interp<float> iP = interp_abs(m, w1p + wp), iQ = interp_abs(m, w2p + wp);
-            tri_access4i<kS>(n, nl, s, -w2p - wp, w1p + wp, e, iQ, iP, d.ab[1]);
-            tri_access4i<kS>(n, nl, s, w1p + wp, -w2p - wp, e, iP, iQ, d.ab[3]);
-        }
-    } else if (ch == 1) {  // integralKernelT, TRIFrgCore.cpp:718-724, 1257-1259, 1814-1816
-        {
-            const Interp<float> iC = interp_abs(m, w1 - wp), iP = interp_abs(m, w1p + wp);
-            tri_access4i<kT>(n, nl, w1 - wp, t, w1p + wp, e, iC, iP, d.ab[0]);
-            tri_access4i<kT>(n, nl, w1p + wp, t, w1 - wp, e, iP, iC, d.ab[2]);
-            tri_access4i<kU>(n, nl, w1 - wp, -w1p - wp, -t, e, iC, iP, d.ab[6]);
-            tri_access4i<kU>(n, nl, w1p + wp, -w1 + wp, -t, e, iP, iC, d.ab[7]);
-        }
-        {
-            const Interp<float> iD = interp_abs(m, w2p - wp), iB = interp_abs(m, w2 + wp);
-            tri_access4i<kT>(n, nl, w2p - wp, t, -w2 - wp, e, iD, iB, d.ab[1]);
-            tri_access4i<kT>(n, nl, w2 + wp, t, -w2p + wp, e, iB, iD, d.ab[3]);
-            tri_access4i<kU>(n, nl, w2p - wp, -w2 - wp, t, e, iD, iB, d.ab[4]);
-            tri_access4i<kU>(n, nl, w2 + wp, -w2p + wp, t, e, iB, iD, d.ab[5]);
-        }
-    } else {  // integralKernelU, TRIFrgCore.cpp:2375-2379
-        {
-            const Interp<float> iA = interp_abs(m, w1 + wp), iD = interp_abs(m, w2p - wp);
-            tri_access4i<kU>(n, nl, w1 + wp, -w2p + wp, u, e, iA, iD, d.ab[0]);
-            tri_access4i<kU>(n, nl, w2p - wp, -w1 - wp, u, e, iD, iA, d.ab[2]);
-        }
-        {
-            const Interp<float> iP = interp_abs(m, w1p + wp), iE = interp_abs(m, w2 - wp);
-            tri_access4i<kU>(n, nl, w1p + wp, w2 - wp, u, e, iP, iE, d.ab[1]);
-            tri_access4i<kU>(n, nl, w2 - wp, w1p + wp, u, e, iE, iP, d.ab[3]);
-        }
+    const bool lo2 = q < 2, odd = q & 1;
+    if (ch == 0) {
+        // slots (t, u): 2 (-A, -B), 3 (P, -Q), 0 (B, A), 1 (-Q, P); (y1, y2) = (A, B) or (P, Q)
+        const float y1 = odd ? w1p + wp : w1 + wp, y2 = odd ? w2p + wp : w2 + wp;
+        const Interp<float> i1 = interp_abs(m, y1), i2 = interp_abs(m, y2);
+        tri_access4i<kS>(n, nl, s, lo2 ? (odd ? y1 : -y1) : (odd ? -y2 : y2), lo2 ? -y2 : y1, e, lo2 ? i1 : i2,
+                         lo2 ? i2 : i1, d.ab[q ^ 2]);
+    } else if (ch == 2) {
+        // slots (s, t): 0 (A, -D), 1 (P, E), 2 (D, -A), 3 (E, P); (y1, y2) = (A, D) or (P, E)
+        const float y1 = odd ? w1p + wp : w1 + wp, y2 = odd ? w2 - wp : w2p - wp;
+        const Interp<float> i1 = interp_abs(m, y1), i2 = interp_abs(m, y2);
+        tri_access4i<kU>(n, nl, lo2 ? y1 : y2, lo2 ? (odd ? y2 : -y2) : (odd ? y1 : -y1), u, e, lo2 ? i1 : i2,
+                         lo2 ? i2 : i1, d.ab[q]);
+    } else {
+        // main slots (s, u): 0 (C, P), 2 (P, C), 1 (D, -B), 3 (B, -D); chalice slots (s, t, u):
+        // 6 (C, -P, -t), 7 (P, -C, -t), 4 (D, -B, t), 5 (B, -D, t); (y1, y2) = (C, P), (P, C),
+        // (D, B), (B, D) for q = 0..3
+        const float x1 = lo2 ? w1 - wp : w2p - wp, x2 = lo2 ? w1p + wp : w2 + wp;
+        const float y1 = odd ? x2 : x1, y2 = odd ? x1 : x2;
+        const Interp<float> i1 = interp_abs(m, y1), i2 = interp_abs(m, y2);
+        tri_access4i<kT>(n, nl, y1, t, lo2 ? y2 : -y2, e, i1, i2, d.ab[(int(odd) << 1) | (q >> 1)]);
+        tri_access4i<kU>(n, nl, y1, -y2, lo2 ? -t : t, e, i1, i2, d.ab[4 + (q ^ 2)]);
     }
-    d.c = c;
 }
 
 // One slab of a node for all sites (getValueSuperbundle): goff[e][c][j] is the offset of
@@ -613,8 +604,11 @@ __global__ void __launch_bounds__(kThreads) tri_vertex_kernel(TriArgs a) {
             const float *nc = a.node_c + size_t(xi) * a.max_nodes;
             for (int b0 = 0; b0 < cnt; b0 += kTBatch) {
                 const int nb = min(kTBatch, cnt - b0);
-                if (lane < nb)
-                    make_tdesc(a, pos, ch, xi, s, t, u, w1p, w1, w2p, w2, nwp[b0 + lane], nc[b0 + lane], desc[lane]);
+                if ((lane >> 2) < nb) {  // phase A: a quad of lanes per node
+                    const int k = lane >> 2;
+                    make_tpart(a, pos, ch, xi, s, t, u, w1p, w1, w2p, w2, nwp[b0 + k], lane & 3, desc[k]);
+                    if ((lane & 3) == 0) desc[k].c = nc[b0 + k];
+                }
                 __syncwarp();
                 for (int b = 0; b < nb; ++b) {
                     const TDesc &d = desc[b];
