@@ -130,7 +130,9 @@ struct LaneT {
 using Lane4 = LaneT<kSpt>;
 
 // Interpolated slab of one access buffer for the lane's sites (getValueSuperbundle): X, Y, Z
-// of site j read the permuted components of its representative, D the signed density.
+// of site j read the permuted components of its representative, D the signed density.  The
+// four supports are summed per stored component (one fused multiply-add each) and the sums
+// permuted once, instead of selecting a permuted component of every support.
 template <int SPT>
 __device__ __forceinline__ void gather4(const XyzArgs &a, const AB4 &ab, const LaneT<SPT> &ln, float4 *out) {
 #pragma unroll
@@ -139,15 +141,16 @@ __device__ __forceinline__ void gather4(const XyzArgs &a, const AB4 &ab, const L
         if (ln.valid[k]) {
             const int r = ab.exch ? ln.irid[k] : ln.rid[k];
             const int p = ab.exch ? ln.iprm[k] : ln.prm[k];
-            const int c0 = perm_c(p, 0), c1 = perm_c(p, 1), c2 = perm_c(p, 2);
+            float4 h = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const float4 v = __ldg(a.sd + ab.off[q] + r);
-                g.x += ab.w[q] * comp_of(v, c0);
-                g.y += ab.w[q] * comp_of(v, c1);
-                g.z += ab.w[q] * comp_of(v, c2);
-                g.w += ab.sw[q] * v.w;
+                h.x += ab.w[q] * v.x;
+                h.y += ab.w[q] * v.y;
+                h.z += ab.w[q] * v.z;
+                h.w += ab.sw[q] * v.w;
             }
+            g = make_float4(comp_of(h, perm_c(p, 0)), comp_of(h, perm_c(p, 1)), comp_of(h, perm_c(p, 2)), h.w);
         }
         out[k] = g;
     }
