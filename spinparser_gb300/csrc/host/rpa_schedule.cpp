@@ -106,4 +106,74 @@ RpaHostSchedule build_rpa_schedule(int nl, const int *ptr, const int *r1, const 
     return s;
 }
 
+LaneSchedule lane_schedule(int nl, const int *ptr, const std::vector<int> &packed, int lanes, int last_bit, int reads,
+                           int banks, int group, int (*bank)(int word, int k, int nl)) {
+    const int P = int(packed.size());
+    const int L = std::max(1, (P + lanes - 1) / lanes);
+    LaneSchedule r;
+    r.len = L;
+    r.sched.assign(size_t(L) * lanes, 0);
+    r.count.assign(size_t(lanes), 0);
+    r.slot_base.assign(size_t(lanes), 0);
+    r.seg_ptr.assign(size_t(nl) + 1, -1);
+    std::vector<int> owner(static_cast<size_t>(P));  // the site of each pair
+    for (int j = 0; j < nl; ++j)
+        for (int i = ptr[j]; i < ptr[j + 1]; ++i) owner[size_t(i)] = j;
+    std::vector<std::vector<int>> words(static_cast<size_t>(lanes)), ends(static_cast<size_t>(lanes));
+    int seg = -1;
+    for (int l = 0; l < lanes; ++l) {
+        const int b0 = l * L, b1 = std::min(P, (l + 1) * L);
+        r.count[size_t(l)] = std::max(0, b1 - b0);
+        r.slot_base[size_t(l)] = seg + 1;
+        for (int i = b0; i < b1; ++i) {
+            if (i == b0 || owner[size_t(i - 1)] != owner[size_t(i)]) {
+                ++seg;
+                if (r.seg_ptr[size_t(owner[size_t(i)])] < 0) r.seg_ptr[size_t(owner[size_t(i)])] = seg;
+            }
+            words[size_t(l)].push_back(packed[size_t(i)]);
+            if (i + 1 == b1 || owner[size_t(i + 1)] != owner[size_t(i)]) ends[size_t(l)].push_back(i + 1 - b0);
+        }
+    }
+    r.n_seg = seg + 1;
+    r.seg_ptr[size_t(nl)] = r.n_seg;
+    for (int j = nl - 1; j >= 0; --j)
+        if (r.seg_ptr[size_t(j)] < 0) r.seg_ptr[size_t(j)] = r.seg_ptr[size_t(j + 1)];
+    if (reads > 0 && bank && group > 0 && banks > 0) {
+        std::vector<int> taken(size_t(reads) * banks);
+        for (int g0 = 0; g0 < lanes; g0 += group) {
+            const int g1 = std::min(lanes, g0 + group);
+            std::vector<size_t> si(size_t(g1 - g0), 0);
+            for (int i = 0; i < L; ++i) {
+                std::fill(taken.begin(), taken.end(), 0);
+                for (int l = g0; l < g1; ++l) {
+                    if (i >= r.count[size_t(l)]) continue;
+                    size_t &k = si[size_t(l - g0)];
+                    if (i == ends[size_t(l)][k]) ++k;  // position i opens the lane's next segment
+                    auto &w = words[size_t(l)];
+                    int pick = i, best = 1 << 30;
+                    for (int q = i; q < ends[size_t(l)][k] && best > 0; ++q) {
+                        int cost = 0;
+                        for (int x = 0; x < reads; ++x) cost += taken[size_t(x) * banks + bank(w[size_t(q)], x, nl)];
+                        if (cost < best) {
+                            best = cost;
+                            pick = q;
+                        }
+                    }
+                    std::swap(w[size_t(i)], w[size_t(pick)]);
+                    for (int x = 0; x < reads; ++x) ++taken[size_t(x) * banks + bank(w[size_t(i)], x, nl)];
+                }
+            }
+        }
+    }
+    for (int l = 0; l < lanes; ++l) {
+        size_t k = 0;
+        for (int i = 0; i < r.count[size_t(l)]; ++i) {
+            const bool last = i + 1 == ends[size_t(l)][k];
+            if (last) ++k;
+            r.sched[size_t(i) * lanes + l] = words[size_t(l)][size_t(i)] | (last ? 1 << last_bit : 0);
+        }
+    }
+    return r;
+}
+
 }  // namespace spn

@@ -37,4 +37,20 @@ struct RpaHostSchedule {
 
 RpaHostSchedule build_rpa_schedule(int nl, const int *ptr, const int *r1, const int *r2, int lanes);
 
+// Lane-balanced walk over per-site RPA pair lists (the XYZ and TRI t channels, where a pair
+// carries spin permutations and pairs are not merged): the packed pair words in site order
+// (site j's at ptr[j] .. ptr[j+1]) cut into `lanes` chunks of equal length; a run of one site in
+// a chunk is a segment.  Entry i of lane l is sched[i * lanes + l], the word with bit `last_bit`
+// set on a segment's last entry; a segment's partial goes to slot slot_base[l], +1, ...; site j
+// sums slots seg_ptr[j] .. seg_ptr[j+1] - 1 in order.  With `reads` > 0 the entries inside each
+// segment are ordered against shared-memory bank collisions: bank(word, k) is the bank position
+// (0 .. banks - 1) of the pair's k-th read, `group` lanes are served together, and step by step
+// each lane takes the entry of its segment whose reads the fewest lower lanes of its group took.
+struct LaneSchedule {
+    std::vector<int> sched, count, slot_base, seg_ptr;
+    int n_seg = 0, len = 0;
+};
+LaneSchedule lane_schedule(int nl, const int *ptr, const std::vector<int> &packed, int lanes, int last_bit,
+                           int reads = 0, int banks = 0, int group = 0, int (*bank)(int word, int k, int nl) = nullptr);
+
 }  // namespace spn

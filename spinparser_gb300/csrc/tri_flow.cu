@@ -65,6 +65,12 @@ struct TriArgs {
     const int *ov_ptr;
     const int *ov_pk;  // per pair: rid1 | rid2 << 7 | the images of X, Y, Z under perm1 (2 bits
                        // each) << 14 | the same for perm2 << 20
+    // the t channel's RPA pairs of all sites in one lane-balanced walk (lane_schedule): entry i of
+    // lane l is sched[32 i + l] (ov_pk's word, bit 26 set on the last entry of a site's run in the
+    // lane); the runs' partial sums (16 components) go to slots slot_base[l], ... and site j sums
+    // slots seg_ptr[j] .. seg_ptr[j + 1] - 1
+    const int *rpa_sched, *rpa_count, *rpa_slot_base, *rpa_seg_ptr;
+    int rpa_n_seg;
     const int *range_rid, *range_inv;
     const float *node_wp, *node_c;
     const int *node_cnt;
@@ -452,14 +458,10 @@ __device__ __forceinline__ void ladder(const float *S, int nl, int j, float *r) 
 // a plus a column offset per b, from the permutation images packed into the pair word.  It sums
 // the products without the factor 2 of the reference's terms and doubles the sum: scaling by
 // 2 commutes with every rounding, so the result is the same.
-__device__ __forceinline__ void t_terms(const TriArgs &a, const float *S, const float *L, int nl, int j, float *r) {
+// One RPA pair (packed word e) added to v[16].
+__device__ __forceinline__ void rpa_pair(const float *S, int nl, int e, float *v) {
     const float *S0 = S, *S1 = S + 16 * nl, *S2 = S + 32 * nl, *S3 = S + 48 * nl;
-    float v[16];
-#pragma unroll
-    for (int c = 0; c < 16; ++c) v[c] = 0.0f;
-    const int i1 = a.ov_ptr[j + 1];
-    for (int i = a.ov_ptr[j]; i < i1; ++i) {
-        const int e = __ldg(a.ov_pk + i);
+    {
         const int r1 = e & 127, r2 = (e >> 7) & 127;
         int col1[4], col2[4];
 #pragma unroll
@@ -496,6 +498,39 @@ __device__ __forceinline__ void t_terms(const TriArgs &a, const float *S, const 
             }
         }
     }
+}
+
+// The lane-balanced walk of the RPA pairs of all sites (TriArgs::rpa_*) for the t-channel node
+// whose slabs are in S: each lane sums its chunk's runs into slots (16 floats per run).
+__device__ __forceinline__ void rpa_walk(const TriArgs &a, const float *S, int nl, int lane, int cnt, int base,
+                                         float *slots) {
+    float p[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) p[c] = 0.0f;
+    int slot = base;
+    for (int i = 0; i < cnt; ++i) {
+        const int e = __ldg(a.rpa_sched + 32 * i + lane);
+        rpa_pair(S, nl, e, p);
+        if (e & (1 << 26)) {
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+                slots[16 * slot + c] = p[c];
+                p[c] = 0.0f;
+            }
+            ++slot;
+        }
+    }
+}
+
+__device__ __forceinline__ void t_terms(const TriArgs &a, const float *S, const float *L, const float *slots, int nl,
+                                        int j, float *r) {
+    const float *S0 = S, *S1 = S + 16 * nl, *S2 = S + 32 * nl, *S3 = S + 48 * nl;
+    float v[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) v[c] = 0.0f;
+    for (int q = a.rpa_seg_ptr[j]; q < a.rpa_seg_ptr[j + 1]; ++q)  // the site's run partials, in order
+#pragma unroll
+        for (int c = 0; c < 16; ++c) v[c] += slots[16 * q + c];
 #pragma unroll
     for (int c = 0; c < 16; ++c) v[c] *= 2.0f;
     {  // chalice: slabs 0 and 2 with the local values of ab4, ab5.  For an inner pair (kappa,
@@ -555,8 +590,8 @@ __device__ __forceinline__ void t_terms(const TriArgs &a, const float *S, const 
     for (int c = 0; c < 16; ++c) r[c] = v[c];
 }
 
-__host__ __device__ constexpr size_t tri_warp_floats(int nl) {
-    return 80 * size_t(nl) + 64 + kTBatch * (sizeof(TDesc) / sizeof(float));
+__host__ __device__ constexpr size_t tri_warp_floats(int nl, int n_seg) {
+    return 80 * size_t(nl) + 64 + kTBatch * (sizeof(TDesc) / sizeof(float)) + 16 * size_t(n_seg);
 }
 // per CTA: the gather offsets goff[2][16][nl] (ints), then the warps' areas
 __host__ __device__ constexpr size_t tri_cta_head_floats(int nl) { return (32 * size_t(nl) + 3) / 4 * 4; }
@@ -577,10 +612,12 @@ __global__ void __launch_bounds__(kThreads) tri_vertex_kernel(TriArgs a) {
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float *S = tsm + tri_cta_head_floats(nl) + size_t(warp) * tri_warp_floats(nl);
+    float *S = tsm + tri_cta_head_floats(nl) + size_t(warp) * tri_warp_floats(nl, a.rpa_n_seg);
     float *acc = S + 64 * nl;
     float *L = acc + 16 * nl;
     TDesc *desc = reinterpret_cast<TDesc *>(L + 64);
+    float *slots = reinterpret_cast<float *>(desc + kTBatch);
+    const int rpa_cnt = a.rpa_count[lane], rpa_base = a.rpa_slot_base[lane];
     const float two_pi = 2.0f * float(kPiD);
 
     for (;;) {
@@ -618,12 +655,16 @@ __global__ void __launch_bounds__(kThreads) tri_vertex_kernel(TriArgs a) {
                     if (ch == 1)
                         for (int q = lane; q < 64; q += 32) L[q] = tri_local(a.v4, nl, d.ab[4 + (q >> 4)], (q & 15) >> 2, q & 3);
                     __syncwarp();
+                    if (ch == 1) {
+                        rpa_walk(a, S, nl, lane, rpa_cnt, rpa_base, slots);
+                        __syncwarp();
+                    }
                     const float cw = d.c;
                     for (int j = lane; j < nl; j += 32) {
                         float r[16];
                         if (ch == 0) ladder<false>(S, nl, j, r);
                         else if (ch == 2) ladder<true>(S, nl, j, r);
-                        else t_terms(a, S, L, nl, j, r);
+                        else t_terms(a, S, L, slots, nl, j, r);
 #pragma unroll
                         for (int c = 0; c < 16; ++c) acc[c * nl + j] += cw * r[c];
                     }
@@ -767,7 +808,19 @@ using cuh::copy_grid;
 using cuh::dalloc;
 using cuh::h2d;
 
-size_t vertex_smem(int nl) { return (tri_cta_head_floats(nl) + size_t(kWarps) * tri_warp_floats(nl)) * sizeof(float); }
+// Bank position of read k of an RPA pair in the lane-balanced walk (rpa_pair): reads 0..15 take
+// component (P1(a), P1(b)) of the first factor at (4 P1(a) + P1(b)) nl + rid1, reads 16..31 the
+// same for the second factor; 4-byte words, 32 banks, one 32-lane phase.
+int tri_walk_bank(int e, int k, int nl) {
+    const int f = k >> 4, a = (k >> 2) & 3, b = k & 3;
+    const int rid = f ? (e >> 7) & 127 : e & 127, sh = f ? 20 : 14;
+    const int pa = a == 3 ? 3 : (e >> (sh + 2 * a)) & 3, pb = b == 3 ? 3 : (e >> (sh + 2 * b)) & 3;
+    return ((4 * pa + pb) * nl + rid) & 31;
+}
+
+size_t vertex_smem(int nl, int n_seg) {
+    return (tri_cta_head_floats(nl) + size_t(kWarps) * tri_warp_floats(nl, n_seg)) * sizeof(float);
+}
 
 }  // namespace
 
@@ -780,7 +833,8 @@ struct spn_tri {
           *node_c = nullptr, *corr_out = nullptr;
     int *ints = nullptr;  // all integer tables in one allocation
     int *sites, *sites_perm, *inv_sites, *inv_sites_perm, *ov_ptr, *ov_pk, *range_rid, *range_inv, *corr_rid,
-        *corr_perm, *node_cnt, *work_counter;
+        *corr_perm, *node_cnt, *work_counter, *rpa_sched, *rpa_count, *rpa_slot_base, *rpa_seg_ptr;
+    int rpa_n_seg = 0;
     unsigned *status = nullptr;
     double *partial = nullptr;
 
@@ -806,6 +860,11 @@ struct spn_tri {
         a.inv_sites_perm = inv_sites_perm;
         a.ov_ptr = ov_ptr;
         a.ov_pk = ov_pk;
+        a.rpa_sched = rpa_sched;
+        a.rpa_count = rpa_count;
+        a.rpa_slot_base = rpa_slot_base;
+        a.rpa_seg_ptr = rpa_seg_ptr;
+        a.rpa_n_seg = rpa_n_seg;
         a.range_rid = range_rid;
         a.range_inv = range_inv;
         a.node_wp = node_wp;
@@ -960,16 +1019,23 @@ extern "C" int spn_tri_create(const spn_tri_desc *d, spn_tri **out) {
             put(d->overlap_ptr, nl + 1);
             const std::vector<int> packed = order_rpa_pairs(d);
             put(packed.data(), nov);
+            const LaneSchedule rpa = lane_schedule(nl, d->overlap_ptr, packed, 32, 26, 32, 32, 32, tri_walk_bank);
+            h->rpa_n_seg = rpa.n_seg;
             put(d->range_rid, nr);
             put(d->range_inv_rid, nr);
             put(d->corr_rid, nc);
             put(d->corr_perm, nc);
             put(nullptr, h->n);  // node counts
             put(nullptr, 1);     // work counter
+            put(rpa.sched.data(), int(rpa.sched.size()));
+            put(rpa.count.data(), 32);
+            put(rpa.slot_base.data(), 32);
+            put(rpa.seg_ptr.data(), nl + 1);
             h->ints = dalloc<int>(img.size(), "alloc lattice tables");
             h2d(h->ints, img.data(), img.size(), h->stream);
             int **fields[] = {&h->sites, &h->sites_perm, &h->inv_sites, &h->inv_sites_perm, &h->ov_ptr, &h->ov_pk,
-                              &h->range_rid, &h->range_inv, &h->corr_rid, &h->corr_perm, &h->node_cnt, &h->work_counter};
+                              &h->range_rid, &h->range_inv, &h->corr_rid, &h->corr_perm, &h->node_cnt, &h->work_counter,
+                              &h->rpa_sched, &h->rpa_count, &h->rpa_slot_base, &h->rpa_seg_ptr};
             for (size_t k = 0; k < at.size(); ++k) *fields[k] = h->ints + at[k];
             h2d(h->freq, d->freq, h->n, h->stream);
             check_cuda(cudaMemsetAsync(h->v4, 0, vsz * sizeof(float), h->stream), "memset");
@@ -980,9 +1046,9 @@ extern "C" int spn_tri_create(const spn_tri_desc *d, spn_tri **out) {
             check_cuda(cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device), "device attribute");
             int per_sm = 0;
             check_cuda(cudaFuncSetAttribute(tri_vertex_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            int(vertex_smem(h->nl))),
+                                            int(vertex_smem(h->nl, h->rpa_n_seg))),
                        "shared memory limit");
-            check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tri_vertex_kernel, kThreads, vertex_smem(h->nl)),
+            check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tri_vertex_kernel, kThreads, vertex_smem(h->nl, h->rpa_n_seg)),
                        "occupancy");
             if (per_sm < 1) throw Error(ErrorType::Unsupported, "TRI vertex-flow kernel does not fit on this device");
             h->grid = h->sms * per_sm;
@@ -1051,9 +1117,9 @@ extern "C" int spn_tri_compute_step(spn_tri *h) {
         check_cuda(cudaGetLastError(), "self-energy launch");
         tri_node_table_kernel<<<(h->n + 63) / 64, 64, 0, h->stream>>>(h->node_args());
         check_cuda(cudaGetLastError(), "node table launch");
-        check_cuda(cudaFuncSetAttribute(tri_vertex_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(vertex_smem(h->nl))),
+        check_cuda(cudaFuncSetAttribute(tri_vertex_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(vertex_smem(h->nl, h->rpa_n_seg))),
                    "shared memory limit");
-        tri_vertex_kernel<<<h->grid, kThreads, vertex_smem(h->nl), h->stream>>>(a);
+        tri_vertex_kernel<<<h->grid, kThreads, vertex_smem(h->nl, h->rpa_n_seg), h->stream>>>(a);
         check_cuda(cudaGetLastError(), "vertex flow launch");
     });
 }

@@ -60,6 +60,12 @@ struct XyzArgs {
     const int *sites, *sites_perm, *inv_sites, *inv_sites_perm;
     const int *ov_ptr, *ov_r1, *ov_r2, *ov_p1, *ov_p2;
     const int *ov_pk;  // rid1 | rid2 << 7 | perm1 << 14 | perm2 << 17 per pair
+    // the t channel's RPA pairs of all sites in one lane-balanced walk (xyz_rpa_schedule): entry
+    // i of lane l is sched[32 i + l] (ov_pk's word, bit 20 set on the last entry of a site's run
+    // in the lane), count[l] entries, the runs' partial sums go to slots slot_base[l], ... and
+    // site j sums slots seg_ptr[j] .. seg_ptr[j + 1] - 1
+    const int *rpa_sched, *rpa_count, *rpa_slot_base, *rpa_seg_ptr;
+    int rpa_n_seg;
     const int *range_rid, *range_inv;
     const float *node_wp, *node_c;
     const int *node_cnt;
@@ -288,15 +294,17 @@ template <int SPT>
 __global__ void __launch_bounds__(kThreads) xyz_vertex_kernel(XyzArgs a) {
     __shared__ float pos[kMaxFreq];
     // per warp: kXBatch node descriptors, then the first two t slabs of every site in all six
-    // spin permutations, A6[p][nl] and B6[p][nl]
+    // spin permutations, A6[p][nl] and B6[p][nl], then the RPA walk's run partials
     extern __shared__ float4 xs[];
     for (int i = threadIdx.x; i < a.n; i += blockDim.x) pos[i] = a.freq[i];
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int n = a.n, nl = a.nl;
-    const int warp_f4 = kXBatch * int(sizeof(XDesc) / sizeof(float4)) + 12 * nl;
+    const int warp_f4 = kXBatch * int(sizeof(XDesc) / sizeof(float4)) + 12 * nl + a.rpa_n_seg;
     XDesc *desc = reinterpret_cast<XDesc *>(xs + size_t(warp) * warp_f4);
     float4 *A6 = xs + size_t(warp) * warp_f4 + kXBatch * (sizeof(XDesc) / sizeof(float4)), *B6 = A6 + 6 * nl;
+    float4 *slots = B6 + 6 * nl;
+    const int rpa_cnt = a.rpa_count[lane], rpa_base = a.rpa_slot_base[lane];
     LaneT<SPT> ln;
 #pragma unroll
     for (int k = 0; k < SPT; ++k) {
@@ -377,19 +385,34 @@ __global__ void __launch_bounds__(kThreads) xyz_vertex_kernel(XyzArgs a) {
                         const float4 cb = d.lv[0], ica = d.lv[1], cb2 = d.lv[2], ica2 = d.lv[3];
                         const float cbv[4] = {cb.x, cb.y, cb.z, cb.w}, icav[4] = {ica.x, ica.y, ica.z, ica.w};
                         const float cb2v[4] = {cb2.x, cb2.y, cb2.z, cb2.w}, ica2v[4] = {ica2.x, ica2.y, ica2.z, ica2.w};
+                        {  // RPA (XYZFrgCore.cpp:282-305): every site's pairs in one lane-balanced walk
+                            float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                            int slot = rpa_base;
+                            for (int i = 0; i < rpa_cnt; ++i) {
+                                const int e = __ldg(a.rpa_sched + 32 * i + lane);
+                                const float4 x1 = A6[((e >> 14) & 7) * nl + (e & 127)];
+                                const float4 x2 = B6[((e >> 17) & 7) * nl + ((e >> 7) & 127)];
+                                p.x += x1.x * x2.x;
+                                p.y += x1.y * x2.y;
+                                p.z += x1.z * x2.z;
+                                p.w += x1.w * x2.w;
+                                if (e & (1 << 20)) {
+                                    slots[slot++] = p;
+                                    p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                                }
+                            }
+                        }
+                        __syncwarp();
 #pragma unroll
                         for (int k = 0; k < SPT; ++k) {
                             float rp[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-                            if (ln.valid[k]) {  // XYZFrgCore.cpp:282-305
-                                const int rid = ln.j[k];
-                                for (int i = a.ov_ptr[rid]; i < a.ov_ptr[rid + 1]; ++i) {
-                                    const int e = __ldg(a.ov_pk + i);
-                                    const float4 x1 = A6[((e >> 14) & 7) * nl + (e & 127)];
-                                    const float4 x2 = B6[((e >> 17) & 7) * nl + ((e >> 7) & 127)];
-                                    rp[0] += x1.x * x2.x;
-                                    rp[1] += x1.y * x2.y;
-                                    rp[2] += x1.z * x2.z;
-                                    rp[3] += x1.w * x2.w;
+                            if (ln.valid[k]) {  // the site's run partials, in order
+                                for (int q = a.rpa_seg_ptr[ln.j[k]]; q < a.rpa_seg_ptr[ln.j[k] + 1]; ++q) {
+                                    const float4 v = slots[q];
+                                    rp[0] += v.x;
+                                    rp[1] += v.y;
+                                    rp[2] += v.z;
+                                    rp[3] += v.w;
                                 }
                             }
                             const float a0[4] = {S0[k].x, S0[k].y, S0[k].z, S0[k].w};
@@ -619,7 +642,9 @@ struct spn_xyz {
     float4 *sd = nullptr, *dsd = nullptr;
     int *ints = nullptr;  // all integer tables in one allocation
     int *sites, *sites_perm, *inv_sites, *inv_sites_perm, *ov_ptr, *ov_r1, *ov_r2, *ov_p1, *ov_p2, *ov_pk,
-        *range_rid, *range_inv, *corr_rid, *corr_perm, *node_cnt, *work_counter;
+        *range_rid, *range_inv, *corr_rid, *corr_perm, *node_cnt, *work_counter, *rpa_sched, *rpa_count,
+        *rpa_slot_base, *rpa_seg_ptr;
+    int rpa_n_seg = 0;
     unsigned *status = nullptr;
     double *partial = nullptr;
 
@@ -647,6 +672,11 @@ struct spn_xyz {
         a.ov_p1 = ov_p1;
         a.ov_p2 = ov_p2;
         a.ov_pk = ov_pk;
+        a.rpa_sched = rpa_sched;
+        a.rpa_count = rpa_count;
+        a.rpa_slot_base = rpa_slot_base;
+        a.rpa_seg_ptr = rpa_seg_ptr;
+        a.rpa_n_seg = rpa_n_seg;
         a.range_rid = range_rid;
         a.range_inv = range_inv;
         a.node_wp = node_wp;
@@ -753,7 +783,15 @@ std::vector<int> order_rpa_pairs(const spn_xyz_desc *d) {
     return out;
 }
 
-size_t vertex_smem(int nl) { return size_t(kWarps) * (kXBatch * sizeof(XDesc) + 12 * size_t(nl) * sizeof(float4)); }
+// Bank positions of the two 16-byte reads of an RPA pair in the lane-balanced walk:
+// A6[perm1 nl + rid1] and B6[perm2 nl + rid2] (eight positions, eight lanes per phase).
+int xyz_walk_bank(int e, int k, int nl) {
+    return k == 0 ? (((e >> 14) & 7) * nl + (e & 127)) & 7 : (((e >> 17) & 7) * nl + ((e >> 7) & 127)) & 7;
+}
+
+size_t vertex_smem(int nl, int n_seg) {
+    return size_t(kWarps) * (kXBatch * sizeof(XDesc) + (12 * size_t(nl) + size_t(n_seg)) * sizeof(float4));
+}
 
 void launch_correlation(spn_xyz *h) {
     const XyzArgs a = h->args();
@@ -812,17 +850,24 @@ extern "C" int spn_xyz_create(const spn_xyz_desc *d, spn_xyz **out) {
             put(d->overlap_perm2, nov);
             const std::vector<int> packed = order_rpa_pairs(d);
             put(packed.data(), nov);
+            const LaneSchedule rpa = lane_schedule(nl, d->overlap_ptr, packed, 32, 20, 2, 8, 8, xyz_walk_bank);
+            h->rpa_n_seg = rpa.n_seg;
             put(d->range_rid, nr);
             put(d->range_inv_rid, nr);
             put(d->corr_rid, nc);
             put(d->corr_perm, nc);
             put(nullptr, h->n);  // node counts
             put(nullptr, 1);     // work counter
+            put(rpa.sched.data(), int(rpa.sched.size()));
+            put(rpa.count.data(), 32);
+            put(rpa.slot_base.data(), 32);
+            put(rpa.seg_ptr.data(), nl + 1);
             h->ints = dalloc<int>(img.size(), "alloc lattice tables");
             h2d(h->ints, img.data(), img.size(), h->stream);
             int **fields[] = {&h->sites, &h->sites_perm, &h->inv_sites, &h->inv_sites_perm, &h->ov_ptr, &h->ov_r1,
                               &h->ov_r2, &h->ov_p1, &h->ov_p2, &h->ov_pk, &h->range_rid, &h->range_inv,
-                              &h->corr_rid, &h->corr_perm, &h->node_cnt, &h->work_counter};
+                              &h->corr_rid, &h->corr_perm, &h->node_cnt, &h->work_counter, &h->rpa_sched,
+                              &h->rpa_count, &h->rpa_slot_base, &h->rpa_seg_ptr};
             for (size_t k = 0; k < at.size(); ++k) *fields[k] = h->ints + at[k];
             h2d(h->freq, d->freq, h->n, h->stream);
             check_cuda(cudaMemsetAsync(h->sd, 0, vsz * sizeof(float4), h->stream), "memset");
@@ -834,9 +879,9 @@ extern "C" int spn_xyz_create(const spn_xyz_desc *d, spn_xyz **out) {
             int per_sm = 0;
             h->spt = h->nl <= 32 ? 1 : (h->nl <= 64 ? 2 : 4);
             const void *fn = vertex_kernel(h->spt);
-            check_cuda(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(vertex_smem(h->nl))),
+            check_cuda(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(vertex_smem(h->nl, h->rpa_n_seg))),
                        "shared memory limit");
-            check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, vertex_smem(h->nl)), "occupancy");
+            check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, vertex_smem(h->nl, h->rpa_n_seg)), "occupancy");
             if (per_sm < 1) throw Error(ErrorType::Unsupported, "XYZ vertex-flow kernel does not fit on this device");
             h->grid = h->sms * per_sm;
             check_cuda(cudaStreamSynchronize(h->stream), "create sync");
@@ -929,11 +974,11 @@ extern "C" int spn_xyz_compute_step(spn_xyz *h) {
         xyz_node_table_kernel<<<(h->n + 63) / 64, 64, 0, h->stream>>>(h->node_args());
         check_cuda(cudaGetLastError(), "node table launch");
         check_cuda(cudaFuncSetAttribute(vertex_kernel(h->spt), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        int(vertex_smem(h->nl))),
+                                        int(vertex_smem(h->nl, h->rpa_n_seg))),
                    "shared memory limit");
-        if (h->spt == 1) xyz_vertex_kernel<1><<<h->grid, kThreads, vertex_smem(h->nl), h->stream>>>(a);
-        else if (h->spt == 2) xyz_vertex_kernel<2><<<h->grid, kThreads, vertex_smem(h->nl), h->stream>>>(a);
-        else xyz_vertex_kernel<4><<<h->grid, kThreads, vertex_smem(h->nl), h->stream>>>(a);
+        if (h->spt == 1) xyz_vertex_kernel<1><<<h->grid, kThreads, vertex_smem(h->nl, h->rpa_n_seg), h->stream>>>(a);
+        else if (h->spt == 2) xyz_vertex_kernel<2><<<h->grid, kThreads, vertex_smem(h->nl, h->rpa_n_seg), h->stream>>>(a);
+        else xyz_vertex_kernel<4><<<h->grid, kThreads, vertex_smem(h->nl, h->rpa_n_seg), h->stream>>>(a);
         check_cuda(cudaGetLastError(), "vertex flow launch");
     });
 }
