@@ -62,12 +62,10 @@ struct TriArgs {
     const float *v2;
     float *dv2;
     const int *sites, *sites_perm, *inv_sites, *inv_sites_perm;
-    const int *ov_ptr;
-    const int *ov_pk;  // per pair: rid1 | rid2 << 7 | the images of X, Y, Z under perm1 (2 bits
-                       // each) << 14 | the same for perm2 << 20
     // the t channel's RPA pairs of all sites in one lane-balanced walk (lane_schedule): entry i of
-    // lane l is sched[32 i + l] (ov_pk's word, bit 26 set on the last entry of a site's run in the
-    // lane); the runs' partial sums (16 components) go to slots slot_base[l], ... and site j sums
+    // lane l is sched[32 i + l], the pair's word rid1 | rid2 << 7 | the images of X, Y, Z under
+    // perm1 (2 bits each) << 14 | the same for perm2 << 20 (order_rpa_pairs), bit 26 set on the
+    // last entry of a site's run in the lane; the runs' partial sums (16 components) go to slots slot_base[l], ... and site j sums
     // slots seg_ptr[j] .. seg_ptr[j + 1] - 1
     const int *rpa_sched, *rpa_count, *rpa_slot_base, *rpa_seg_ptr;
     int rpa_n_seg;
@@ -832,7 +830,7 @@ struct spn_tri {
     float *freq = nullptr, *v2 = nullptr, *dv2 = nullptr, *v4 = nullptr, *dv4 = nullptr, *node_wp = nullptr,
           *node_c = nullptr, *corr_out = nullptr;
     int *ints = nullptr;  // all integer tables in one allocation
-    int *sites, *sites_perm, *inv_sites, *inv_sites_perm, *ov_ptr, *ov_pk, *range_rid, *range_inv, *corr_rid,
+    int *sites, *sites_perm, *inv_sites, *inv_sites_perm, *range_rid, *range_inv, *corr_rid,
         *corr_perm, *node_cnt, *work_counter, *rpa_sched, *rpa_count, *rpa_slot_base, *rpa_seg_ptr;
     int rpa_n_seg = 0;
     unsigned *status = nullptr;
@@ -858,8 +856,6 @@ struct spn_tri {
         a.sites_perm = sites_perm;
         a.inv_sites = inv_sites;
         a.inv_sites_perm = inv_sites_perm;
-        a.ov_ptr = ov_ptr;
-        a.ov_pk = ov_pk;
         a.rpa_sched = rpa_sched;
         a.rpa_count = rpa_count;
         a.rpa_slot_base = rpa_slot_base;
@@ -950,7 +946,7 @@ void validate(const spn_tri_desc *d) {
 }
 
 // The RPA pairs of each site in the order of host/pair_order (against bank collisions of the
-// kernel's shared-memory reads), packed as TriArgs::ov_pk.
+// kernel's shared-memory reads), packed as the words of TriArgs::rpa_sched.
 std::vector<int> order_rpa_pairs(const spn_tri_desc *d) {
     const int nl = d->n_sites;
     const std::vector<int> order =
@@ -1016,9 +1012,7 @@ extern "C" int spn_tri_create(const spn_tri_desc *d, spn_tri **out) {
             put(d->sites_perm, nl);
             put(d->inv_sites_rid, nl);
             put(d->inv_sites_perm, nl);
-            put(d->overlap_ptr, nl + 1);
             const std::vector<int> packed = order_rpa_pairs(d);
-            put(packed.data(), nov);
             const LaneSchedule rpa = lane_schedule(nl, d->overlap_ptr, packed, 32, 26, 32, 32, 32, tri_walk_bank);
             h->rpa_n_seg = rpa.n_seg;
             put(d->range_rid, nr);
@@ -1033,7 +1027,7 @@ extern "C" int spn_tri_create(const spn_tri_desc *d, spn_tri **out) {
             put(rpa.seg_ptr.data(), nl + 1);
             h->ints = dalloc<int>(img.size(), "alloc lattice tables");
             h2d(h->ints, img.data(), img.size(), h->stream);
-            int **fields[] = {&h->sites, &h->sites_perm, &h->inv_sites, &h->inv_sites_perm, &h->ov_ptr, &h->ov_pk,
+            int **fields[] = {&h->sites, &h->sites_perm, &h->inv_sites, &h->inv_sites_perm,
                               &h->range_rid, &h->range_inv, &h->corr_rid, &h->corr_perm, &h->node_cnt, &h->work_counter,
                               &h->rpa_sched, &h->rpa_count, &h->rpa_slot_base, &h->rpa_seg_ptr};
             for (size_t k = 0; k < at.size(); ++k) *fields[k] = h->ints + at[k];

@@ -58,10 +58,9 @@ struct XyzArgs {
     const float *v2;
     float *dv2;
     const int *sites, *sites_perm, *inv_sites, *inv_sites_perm;
-    const int *ov_ptr, *ov_r1, *ov_r2, *ov_p1, *ov_p2;
-    const int *ov_pk;  // rid1 | rid2 << 7 | perm1 << 14 | perm2 << 17 per pair
-    // the t channel's RPA pairs of all sites in one lane-balanced walk (xyz_rpa_schedule): entry
-    // i of lane l is sched[32 i + l] (ov_pk's word, bit 20 set on the last entry of a site's run
+    // the t channel's RPA pairs of all sites in one lane-balanced walk (lane_schedule): entry i
+    // of lane l is sched[32 i + l], the pair's word rid1 | rid2 << 7 | perm1 << 14 | perm2 << 17
+    // (order_rpa_pairs) with bit 20 set on the last entry of a site's run
     // in the lane), count[l] entries, the runs' partial sums go to slots slot_base[l], ... and
     // site j sums slots seg_ptr[j] .. seg_ptr[j + 1] - 1
     const int *rpa_sched, *rpa_count, *rpa_slot_base, *rpa_seg_ptr;
@@ -641,8 +640,7 @@ struct spn_xyz {
           *corr_out = nullptr;
     float4 *sd = nullptr, *dsd = nullptr;
     int *ints = nullptr;  // all integer tables in one allocation
-    int *sites, *sites_perm, *inv_sites, *inv_sites_perm, *ov_ptr, *ov_r1, *ov_r2, *ov_p1, *ov_p2, *ov_pk,
-        *range_rid, *range_inv, *corr_rid, *corr_perm, *node_cnt, *work_counter, *rpa_sched, *rpa_count,
+    int *sites, *sites_perm, *inv_sites, *inv_sites_perm, *range_rid, *range_inv, *corr_rid, *corr_perm, *node_cnt, *work_counter, *rpa_sched, *rpa_count,
         *rpa_slot_base, *rpa_seg_ptr;
     int rpa_n_seg = 0;
     unsigned *status = nullptr;
@@ -666,12 +664,6 @@ struct spn_xyz {
         a.sites_perm = sites_perm;
         a.inv_sites = inv_sites;
         a.inv_sites_perm = inv_sites_perm;
-        a.ov_ptr = ov_ptr;
-        a.ov_r1 = ov_r1;
-        a.ov_r2 = ov_r2;
-        a.ov_p1 = ov_p1;
-        a.ov_p2 = ov_p2;
-        a.ov_pk = ov_pk;
         a.rpa_sched = rpa_sched;
         a.rpa_count = rpa_count;
         a.rpa_slot_base = rpa_slot_base;
@@ -843,13 +835,7 @@ extern "C" int spn_xyz_create(const spn_xyz_desc *d, spn_xyz **out) {
             put(d->sites_perm, nl);
             put(d->inv_sites_rid, nl);
             put(d->inv_sites_perm, nl);
-            put(d->overlap_ptr, nl + 1);
-            put(d->overlap_rid1, nov);
-            put(d->overlap_rid2, nov);
-            put(d->overlap_perm1, nov);
-            put(d->overlap_perm2, nov);
             const std::vector<int> packed = order_rpa_pairs(d);
-            put(packed.data(), nov);
             const LaneSchedule rpa = lane_schedule(nl, d->overlap_ptr, packed, 32, 20, 2, 8, 8, xyz_walk_bank);
             h->rpa_n_seg = rpa.n_seg;
             put(d->range_rid, nr);
@@ -864,8 +850,7 @@ extern "C" int spn_xyz_create(const spn_xyz_desc *d, spn_xyz **out) {
             put(rpa.seg_ptr.data(), nl + 1);
             h->ints = dalloc<int>(img.size(), "alloc lattice tables");
             h2d(h->ints, img.data(), img.size(), h->stream);
-            int **fields[] = {&h->sites, &h->sites_perm, &h->inv_sites, &h->inv_sites_perm, &h->ov_ptr, &h->ov_r1,
-                              &h->ov_r2, &h->ov_p1, &h->ov_p2, &h->ov_pk, &h->range_rid, &h->range_inv,
+            int **fields[] = {&h->sites, &h->sites_perm, &h->inv_sites, &h->inv_sites_perm, &h->range_rid, &h->range_inv,
                               &h->corr_rid, &h->corr_perm, &h->node_cnt, &h->work_counter, &h->rpa_sched,
                               &h->rpa_count, &h->rpa_slot_base, &h->rpa_seg_ptr};
             for (size_t k = 0; k < at.size(); ++k) *fields[k] = h->ints + at[k];
