@@ -129,9 +129,11 @@ int spn_lattice_get_interactions(const spn_lattice *lat, int *rid, float *coupli
 int spn_rpa_schedule(int n_sites, const int *overlap_ptr, const int *overlap_rid1, const int *overlap_rid2, int lanes,
                      int *info, int *sched, int *count, int *slot_base, int *seg_ptr);
 
-/* The order in which the XYZ (layout 0) or TRI (layout 1) vertex kernel walks each site's RPA
- * pairs (diagnostics; host only): order[overlap_ptr[j] .. overlap_ptr[j+1]) is a permutation of
- * site j's pair indices, chosen against shared-memory bank collisions of the kernel's reads.
+/* The per-site order of the RPA pairs of the XYZ (layout 0) or TRI (layout 1) core (diagnostics;
+ * host only): order[overlap_ptr[j] .. overlap_ptr[j+1]) is a permutation of site j's pair
+ * indices, chosen against shared-memory bank collisions of a walk with lane = site.  The vertex
+ * kernels cut the site-ordered lists into 32 lane-balanced chunks and reorder the entries of each
+ * run against the collisions of that walk (csrc/host/rpa_schedule.hpp, lane_schedule).
  * collisions[0] / [1]: collisions of the given order and of the chosen one (may be NULL). */
 int spn_rpa_pair_order(int layout, int n_sites, const int *overlap_ptr, const int *overlap_rid1,
                        const int *overlap_rid2, const int *overlap_perm1, const int *overlap_perm2, int *order,

@@ -1,11 +1,12 @@
 // Order of the RPA overlap pairs of each site, chosen against shared-memory bank collisions.
 //
-// The XYZ and TRI vertex kernels walk the RPA pairs of site j in lane j of a warp (32 sites per
-// warp step).  At step k every lane reads, for each of `slots` load instructions, one word of
-// its k-th pair; lanes of one phase (all 32 for 4-byte reads, 8 for 16-byte reads) whose
-// different words fall into the same bank serialise.  Any order of a site's pairs gives the same
-// RPA sum up to rounding, so the pairs are chosen greedily, step by step and site by site, with
-// the fewest new collisions.
+// A walk of the RPA pairs of site j in lane j of a warp (32 sites per warp step): at step k every
+// lane reads, for each of `slots` load instructions, one word of its k-th pair; lanes of one
+// phase (all 32 for 4-byte reads, 8 for 16-byte reads) whose different words fall into the same
+// bank serialise.  Any order of a site's pairs gives the same RPA sum up to rounding, so the
+// pairs are chosen greedily, step by step and site by site, with the fewest new collisions.  The
+// XYZ and TRI vertex kernels walk the site-ordered lists in lane-balanced chunks instead
+// (lane_schedule, rpa_schedule.hpp), which orders the entries of each run again for that walk.
 #pragma once
 
 #include <functional>
