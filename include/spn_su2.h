@@ -139,6 +139,15 @@ int spn_rpa_pair_order(int layout, int n_sites, const int *overlap_ptr, const in
                        const int *overlap_rid2, const int *overlap_perm1, const int *overlap_perm2, int *order,
                        long long *collisions);
 
+/* The lane-balanced walk of the XYZ (layout 1) or TRI (layout 2) vertex kernel's RPA pairs, or
+ * the same chunking without the bank ordering (layout 0, last-entry bit 26) (diagnostics; host
+ * only; csrc/host/rpa_schedule.hpp, lane_schedule): `words` are the site-ordered pair words
+ * (site j's at overlap_ptr[j] .. overlap_ptr[j+1]), 32 lanes.  info[4] = {entries per lane,
+ * segments, total ints of sched, last-entry bit}.  With sched = NULL only info is filled;
+ * otherwise sched holds info[2] ints, count and slot_base 32 ints, seg_ptr Nl + 1 ints. */
+int spn_rpa_lane_schedule(int layout, int n_sites, const int *overlap_ptr, const int *words, int *info, int *sched,
+                          int *count, int *slot_base, int *seg_ptr);
+
 /* Writes the lattice debug file (.ldf) as `--debugLattice`-free SpinParser always does. */
 int spn_lattice_write_ldf(const spn_lattice *lat, const char *path);
 

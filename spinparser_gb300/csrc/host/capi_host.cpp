@@ -314,6 +314,35 @@ extern "C" int spn_rpa_pair_order(int layout, int n_sites, const int *overlap_pt
     });
 }
 
+extern "C" int spn_rpa_lane_schedule(int layout, int n_sites, const int *overlap_ptr, const int *words, int *info,
+                                     int *sched, int *count, int *slot_base, int *seg_ptr) {
+    return spn::guarded([&] {
+        if (layout < 0 || layout > 2 || n_sites < 1 || n_sites > 128 || !overlap_ptr || !info)
+            throw spn::Error(spn::ErrorType::Argument, "spn_rpa_lane_schedule: bad argument");
+        const int nov = overlap_ptr[n_sites];
+        for (int r = 0; r < n_sites; ++r)
+            if (overlap_ptr[r + 1] < overlap_ptr[r]) throw spn::Error(spn::ErrorType::Argument, "overlap_ptr must be non-decreasing");
+        if (nov > 0 && !words) throw spn::Error(spn::ErrorType::Argument, "spn_rpa_lane_schedule: null words");
+        const int last_bit = layout == 1 ? 20 : 26;
+        for (int i = 0; i < nov; ++i)
+            if (words[i] < 0 || words[i] >= (1 << last_bit) || (words[i] & 127) >= n_sites || ((words[i] >> 7) & 127) >= n_sites)
+                throw spn::Error(spn::ErrorType::Argument, "spn_rpa_lane_schedule: pair word out of range");
+        const std::vector<int> w(words, words + nov);
+        const spn::LaneSchedule s = layout == 1   ? spn::xyz_lane_schedule(n_sites, overlap_ptr, w)
+                                    : layout == 2 ? spn::tri_lane_schedule(n_sites, overlap_ptr, w)
+                                                  : spn::lane_schedule(n_sites, overlap_ptr, w, 32, last_bit);
+        info[0] = s.len;
+        info[1] = s.n_seg;
+        info[2] = int(s.sched.size());
+        info[3] = last_bit;
+        if (!sched) return;
+        std::memcpy(sched, s.sched.data(), s.sched.size() * sizeof(int));
+        if (count) std::memcpy(count, s.count.data(), s.count.size() * sizeof(int));
+        if (slot_base) std::memcpy(slot_base, s.slot_base.data(), s.slot_base.size() * sizeof(int));
+        if (seg_ptr) std::memcpy(seg_ptr, s.seg_ptr.data(), s.seg_ptr.size() * sizeof(int));
+    });
+}
+
 extern "C" int spn_tri_tables(int *rows) {
     return spn::guarded([&] {
         if (!rows) throw spn::Error(spn::ErrorType::Argument, "spn_tri_tables: null argument");

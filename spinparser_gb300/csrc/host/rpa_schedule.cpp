@@ -106,6 +106,25 @@ RpaHostSchedule build_rpa_schedule(int nl, const int *ptr, const int *r1, const 
     return s;
 }
 
+int xyz_walk_bank(int e, int k, int nl) {
+    return k == 0 ? (((e >> 14) & 7) * nl + (e & 127)) & 7 : (((e >> 17) & 7) * nl + ((e >> 7) & 127)) & 7;
+}
+
+int tri_walk_bank(int e, int k, int nl) {
+    const int f = k >> 4, a = (k >> 2) & 3, b = k & 3;
+    const int rid = f ? (e >> 7) & 127 : e & 127, sh = f ? 20 : 14;
+    const int pa = a == 3 ? 3 : (e >> (sh + 2 * a)) & 3, pb = b == 3 ? 3 : (e >> (sh + 2 * b)) & 3;
+    return ((4 * pa + pb) * nl + rid) & 31;
+}
+
+LaneSchedule xyz_lane_schedule(int nl, const int *ptr, const std::vector<int> &packed) {
+    return lane_schedule(nl, ptr, packed, 32, 20, 2, 8, 8, xyz_walk_bank);
+}
+
+LaneSchedule tri_lane_schedule(int nl, const int *ptr, const std::vector<int> &packed) {
+    return lane_schedule(nl, ptr, packed, 32, 26, 32, 32, 32, tri_walk_bank);
+}
+
 LaneSchedule lane_schedule(int nl, const int *ptr, const std::vector<int> &packed, int lanes, int last_bit, int reads,
                            int banks, int group, int (*bank)(int word, int k, int nl)) {
     const int P = int(packed.size());

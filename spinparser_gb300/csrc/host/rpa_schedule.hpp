@@ -53,4 +53,15 @@ struct LaneSchedule {
 LaneSchedule lane_schedule(int nl, const int *ptr, const std::vector<int> &packed, int lanes, int last_bit,
                            int reads = 0, int banks = 0, int group = 0, int (*bank)(int word, int k, int nl) = nullptr);
 
+// The bank models of the two walks.  XYZ (word rid1 | rid2 << 7 | perm1 << 14 | perm2 << 17,
+// last-entry bit 20): the two 16-byte reads A6[perm1 nl + rid1] and B6[perm2 nl + rid2], eight
+// bank positions, eight lanes per phase.  TRI (word rid1 | rid2 << 7 | the images of X, Y, Z under
+// perm1, 2 bits each, << 14 | the same for perm2 << 20, last-entry bit 26): reads 0..15 take
+// component (P1(a), P1(b)) of the first factor at (4 P1(a) + P1(b)) nl + rid1, reads 16..31 the
+// same for the second factor; 4-byte words, 32 banks, one 32-lane phase.
+int xyz_walk_bank(int word, int k, int nl);
+int tri_walk_bank(int word, int k, int nl);
+LaneSchedule xyz_lane_schedule(int nl, const int *ptr, const std::vector<int> &packed);
+LaneSchedule tri_lane_schedule(int nl, const int *ptr, const std::vector<int> &packed);
+
 }  // namespace spn

@@ -806,16 +806,6 @@ using cuh::copy_grid;
 using cuh::dalloc;
 using cuh::h2d;
 
-// Bank position of read k of an RPA pair in the lane-balanced walk (rpa_pair): reads 0..15 take
-// component (P1(a), P1(b)) of the first factor at (4 P1(a) + P1(b)) nl + rid1, reads 16..31 the
-// same for the second factor; 4-byte words, 32 banks, one 32-lane phase.
-int tri_walk_bank(int e, int k, int nl) {
-    const int f = k >> 4, a = (k >> 2) & 3, b = k & 3;
-    const int rid = f ? (e >> 7) & 127 : e & 127, sh = f ? 20 : 14;
-    const int pa = a == 3 ? 3 : (e >> (sh + 2 * a)) & 3, pb = b == 3 ? 3 : (e >> (sh + 2 * b)) & 3;
-    return ((4 * pa + pb) * nl + rid) & 31;
-}
-
 size_t vertex_smem(int nl, int n_seg) {
     return (tri_cta_head_floats(nl) + size_t(kWarps) * tri_warp_floats(nl, n_seg)) * sizeof(float);
 }
@@ -1013,7 +1003,7 @@ extern "C" int spn_tri_create(const spn_tri_desc *d, spn_tri **out) {
             put(d->inv_sites_rid, nl);
             put(d->inv_sites_perm, nl);
             const std::vector<int> packed = order_rpa_pairs(d);
-            const LaneSchedule rpa = lane_schedule(nl, d->overlap_ptr, packed, 32, 26, 32, 32, 32, tri_walk_bank);
+            const LaneSchedule rpa = tri_lane_schedule(nl, d->overlap_ptr, packed);
             h->rpa_n_seg = rpa.n_seg;
             put(d->range_rid, nr);
             put(d->range_inv_rid, nr);

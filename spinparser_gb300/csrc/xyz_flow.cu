@@ -775,12 +775,6 @@ std::vector<int> order_rpa_pairs(const spn_xyz_desc *d) {
     return out;
 }
 
-// Bank positions of the two 16-byte reads of an RPA pair in the lane-balanced walk:
-// A6[perm1 nl + rid1] and B6[perm2 nl + rid2] (eight positions, eight lanes per phase).
-int xyz_walk_bank(int e, int k, int nl) {
-    return k == 0 ? (((e >> 14) & 7) * nl + (e & 127)) & 7 : (((e >> 17) & 7) * nl + ((e >> 7) & 127)) & 7;
-}
-
 size_t vertex_smem(int nl, int n_seg) {
     return size_t(kWarps) * (kXBatch * sizeof(XDesc) + (12 * size_t(nl) + size_t(n_seg)) * sizeof(float4));
 }
@@ -836,7 +830,7 @@ extern "C" int spn_xyz_create(const spn_xyz_desc *d, spn_xyz **out) {
             put(d->inv_sites_rid, nl);
             put(d->inv_sites_perm, nl);
             const std::vector<int> packed = order_rpa_pairs(d);
-            const LaneSchedule rpa = lane_schedule(nl, d->overlap_ptr, packed, 32, 20, 2, 8, 8, xyz_walk_bank);
+            const LaneSchedule rpa = xyz_lane_schedule(nl, d->overlap_ptr, packed);
             h->rpa_n_seg = rpa.n_seg;
             put(d->range_rid, nr);
             put(d->range_inv_rid, nr);
