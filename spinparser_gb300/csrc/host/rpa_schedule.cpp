@@ -106,27 +106,27 @@ RpaHostSchedule build_rpa_schedule(int nl, const int *ptr, const int *r1, const 
     return s;
 }
 
-int xyz_walk_bank(int e, int k, int nl) {
-    return k == 0 ? (((e >> 14) & 7) * nl + (e & 127)) & 7 : (((e >> 17) & 7) * nl + ((e >> 7) & 127)) & 7;
+int xyz_walk_addr(int e, int k, int nl) {
+    return k == 0 ? ((e >> 14) & 7) * nl + (e & 127) : ((e >> 17) & 7) * nl + ((e >> 7) & 127);
 }
 
-int tri_walk_bank(int e, int k, int nl) {
+int tri_walk_addr(int e, int k, int nl) {
     const int f = k >> 4, a = (k >> 2) & 3, b = k & 3;
     const int rid = f ? (e >> 7) & 127 : e & 127, sh = f ? 20 : 14;
     const int pa = a == 3 ? 3 : (e >> (sh + 2 * a)) & 3, pb = b == 3 ? 3 : (e >> (sh + 2 * b)) & 3;
-    return ((4 * pa + pb) * nl + rid) & 31;
+    return (4 * pa + pb) * nl + rid;
 }
 
 LaneSchedule xyz_lane_schedule(int nl, const int *ptr, const std::vector<int> &packed) {
-    return lane_schedule(nl, ptr, packed, 32, 20, 2, 8, 8, xyz_walk_bank);
+    return lane_schedule(nl, ptr, packed, 32, 20, 2, 8, 8, xyz_walk_addr);
 }
 
 LaneSchedule tri_lane_schedule(int nl, const int *ptr, const std::vector<int> &packed) {
-    return lane_schedule(nl, ptr, packed, 32, 26, 32, 32, 32, tri_walk_bank);
+    return lane_schedule(nl, ptr, packed, 32, 26, 32, 32, 32, tri_walk_addr);
 }
 
 LaneSchedule lane_schedule(int nl, const int *ptr, const std::vector<int> &packed, int lanes, int last_bit, int reads,
-                           int banks, int group, int (*bank)(int word, int k, int nl)) {
+                           int banks, int group, int (*addr)(int word, int k, int nl)) {
     const int P = int(packed.size());
     const int L = std::max(1, (P + lanes - 1) / lanes);
     LaneSchedule r;
@@ -157,13 +157,24 @@ LaneSchedule lane_schedule(int nl, const int *ptr, const std::vector<int> &packe
     r.seg_ptr[size_t(nl)] = r.n_seg;
     for (int j = nl - 1; j >= 0; --j)
         if (r.seg_ptr[size_t(j)] < 0) r.seg_ptr[size_t(j)] = r.seg_ptr[size_t(j + 1)];
-    if (reads > 0 && bank && group > 0 && banks > 0) {
-        std::vector<int> taken(size_t(reads) * banks);
+    if (reads > 0 && addr && group > 0 && banks > 0) {
+        // per (read, bank): the distinct addresses lower lanes of the group read at this step (a
+        // repeated address is a broadcast, a new one in an occupied bank one more wavefront)
+        std::vector<std::vector<int>> taken(size_t(reads) * banks);
+        auto cost_of = [&](int word) {
+            int c = 0;
+            for (int x = 0; x < reads; ++x) {
+                const int a = addr(word, x, nl);
+                const auto &t = taken[size_t(x) * banks + size_t(a & (banks - 1))];
+                if (std::find(t.begin(), t.end(), a) == t.end()) c += int(t.size());
+            }
+            return c;
+        };
         for (int g0 = 0; g0 < lanes; g0 += group) {
             const int g1 = std::min(lanes, g0 + group);
             std::vector<size_t> si(size_t(g1 - g0), 0);
             for (int i = 0; i < L; ++i) {
-                std::fill(taken.begin(), taken.end(), 0);
+                for (auto &t : taken) t.clear();
                 for (int l = g0; l < g1; ++l) {
                     if (i >= r.count[size_t(l)]) continue;
                     size_t &k = si[size_t(l - g0)];
@@ -171,15 +182,18 @@ LaneSchedule lane_schedule(int nl, const int *ptr, const std::vector<int> &packe
                     auto &w = words[size_t(l)];
                     int pick = i, best = 1 << 30;
                     for (int q = i; q < ends[size_t(l)][k] && best > 0; ++q) {
-                        int cost = 0;
-                        for (int x = 0; x < reads; ++x) cost += taken[size_t(x) * banks + bank(w[size_t(q)], x, nl)];
+                        const int cost = cost_of(w[size_t(q)]);
                         if (cost < best) {
                             best = cost;
                             pick = q;
                         }
                     }
                     std::swap(w[size_t(i)], w[size_t(pick)]);
-                    for (int x = 0; x < reads; ++x) ++taken[size_t(x) * banks + bank(w[size_t(i)], x, nl)];
+                    for (int x = 0; x < reads; ++x) {
+                        const int a = addr(w[size_t(i)], x, nl);
+                        auto &t = taken[size_t(x) * banks + size_t(a & (banks - 1))];
+                        if (std::find(t.begin(), t.end(), a) == t.end()) t.push_back(a);
+                    }
                 }
             }
         }

@@ -43,24 +43,25 @@ RpaHostSchedule build_rpa_schedule(int nl, const int *ptr, const int *r1, const 
 // a chunk is a segment.  Entry i of lane l is sched[i * lanes + l], the word with bit `last_bit`
 // set on a segment's last entry; a segment's partial goes to slot slot_base[l], +1, ...; site j
 // sums slots seg_ptr[j] .. seg_ptr[j+1] - 1 in order.  With `reads` > 0 the entries inside each
-// segment are ordered against shared-memory bank collisions: bank(word, k) is the bank position
-// (0 .. banks - 1) of the pair's k-th read, `group` lanes are served together, and step by step
-// each lane takes the entry of its segment whose reads the fewest lower lanes of its group took.
+// segment are ordered against shared-memory bank collisions: addr(word, k) is the word address
+// (in bank-width units) of the pair's k-th read, its bank addr mod `banks` (a power of two),
+// `group` lanes are served together, and step by step each lane takes the entry of its segment
+// whose reads add the fewest new addresses to banks that lower lanes of its group already read.
 struct LaneSchedule {
     std::vector<int> sched, count, slot_base, seg_ptr;
     int n_seg = 0, len = 0;
 };
 LaneSchedule lane_schedule(int nl, const int *ptr, const std::vector<int> &packed, int lanes, int last_bit,
-                           int reads = 0, int banks = 0, int group = 0, int (*bank)(int word, int k, int nl) = nullptr);
+                           int reads = 0, int banks = 0, int group = 0, int (*addr)(int word, int k, int nl) = nullptr);
 
-// The bank models of the two walks.  XYZ (word rid1 | rid2 << 7 | perm1 << 14 | perm2 << 17,
+// The shared-memory reads of the two walks.  XYZ (word rid1 | rid2 << 7 | perm1 << 14 | perm2 << 17,
 // last-entry bit 20): the two 16-byte reads A6[perm1 nl + rid1] and B6[perm2 nl + rid2], eight
 // bank positions, eight lanes per phase.  TRI (word rid1 | rid2 << 7 | the images of X, Y, Z under
 // perm1, 2 bits each, << 14 | the same for perm2 << 20, last-entry bit 26): reads 0..15 take
 // component (P1(a), P1(b)) of the first factor at (4 P1(a) + P1(b)) nl + rid1, reads 16..31 the
 // same for the second factor; 4-byte words, 32 banks, one 32-lane phase.
-int xyz_walk_bank(int word, int k, int nl);
-int tri_walk_bank(int word, int k, int nl);
+int xyz_walk_addr(int word, int k, int nl);
+int tri_walk_addr(int word, int k, int nl);
 LaneSchedule xyz_lane_schedule(int nl, const int *ptr, const std::vector<int> &packed);
 LaneSchedule tri_lane_schedule(int nl, const int *ptr, const std::vector<int> &packed);
 

@@ -147,15 +147,14 @@ def walk_collisions(info, sched, count, nl, layout):
 
 
 @pytest.mark.parametrize("layout,lattice,rng,model,params,gain", [
-    (1, "honeycomb", 9, "honeycomb-kitaev", {"j": "0.1", "k": "-1.0"}, 0.5),
-    (2, "honeycomb", 9, "honeycomb-kitaev-gamma", {"j": "0.2", "k": "1.0", "g": "-0.1"}, 0.95),
-    (1, "pyrochlore", 3, "pyrochlore-heisenberg", {"j": "1"}, None),
+    (1, "honeycomb", 9, "honeycomb-kitaev", {"j": "0.1", "k": "-1.0"}, 0.3),
+    (2, "honeycomb", 9, "honeycomb-kitaev-gamma", {"j": "0.2", "k": "1.0", "g": "-0.1"}, 0.3),
+    (1, "pyrochlore", 3, "pyrochlore-heisenberg", {"j": "1"}, 0.5),
 ])
 def test_lane_schedule_covers_every_pair_and_orders_against_banks(layout, lattice, rng, model, params, gain):
     """Every site's pairs appear exactly once, in runs of that site only, whose slots the site
-    sums in order; on the benchmark lattices the bank-ordered walk has well below the collisions
-    of the same chunks unordered (the greedy choice counts a shared address as a collision, so on
-    a 9-site lattice with 12 entries per lane it need not win)."""
+    sums in order; the bank-ordered walk has well below the collisions of the same chunks
+    unordered."""
     lat = spn.Lattice(lattice, rng, model, params)
     tab, st = lat.tables(), lat.spin_tables()
     nl, ptr = tab.n_sites, np.asarray(tab.overlap_ptr)
@@ -176,6 +175,5 @@ def test_lane_schedule_covers_every_pair_and_orders_against_banks(layout, lattic
     for j in range(nl):
         got = sorted(e for q in range(seg[j], seg[j + 1]) for e in runs[q])
         assert got == sorted(words[ptr[j]:ptr[j + 1]].tolist()), j
-    if gain is not None:
-        plain = lane_schedule(0, tab, words)
-        assert walk_collisions(info, sched, count, nl, layout) < gain * walk_collisions(*plain[:3], nl, layout)
+    plain = lane_schedule(0, tab, words)
+    assert walk_collisions(info, sched, count, nl, layout) < gain * walk_collisions(*plain[:3], nl, layout)
