@@ -65,8 +65,8 @@ struct TriArgs {
     // the t channel's RPA pairs of all sites in one lane-balanced walk (lane_schedule): entry i of
     // lane l is sched[32 i + l], the pair's word rid1 | rid2 << 7 | the images of X, Y, Z under
     // perm1 (2 bits each) << 14 | the same for perm2 << 20 (order_rpa_pairs), bit 26 set on the
-    // last entry of a site's run in the lane; the runs' partial sums (16 components) go to slots slot_base[l], ... and site j sums
-    // slots seg_ptr[j] .. seg_ptr[j + 1] - 1
+    // last entry of a site's run in the lane; the runs' partial sums (16 components) go to slots
+    // slot_base[l], ... and site j sums slots seg_ptr[j] .. seg_ptr[j + 1] - 1
     const int *rpa_sched, *rpa_count, *rpa_slot_base, *rpa_seg_ptr;
     int rpa_n_seg;
     const int *range_rid, *range_inv;
@@ -449,14 +449,12 @@ __device__ __forceinline__ void ladder(const float *S, int nl, int j, float *r) 
     }
 }
 
-// The t integrand for one site j (TRIFrgCore.cpp:733-2368): the RPA lattice sum over the
-// overlap pairs of rid j (4x4 products over the inner spin index, the factors' components
-// permuted by the pair's maps), then the chalice diagrams with the site-local values L.
-// The RPA reads component (P a, P b) of a factor at (4 P(a) + P(b)) nl + rid: a row base per
-// a plus a column offset per b, from the permutation images packed into the pair word.  It sums
-// the products without the factor 2 of the reference's terms and doubles the sum: scaling by
-// 2 commutes with every rounding, so the result is the same.
-// One RPA pair (packed word e) added to v[16].
+// One overlap pair (packed word e) of the t integrand's RPA lattice sum (TRIFrgCore.cpp:733-2368)
+// added to v[16]: 4x4 products over the inner spin index, the factors' components permuted by the
+// pair's maps.  The RPA reads component (P a, P b) of a factor at (4 P(a) + P(b)) nl + rid: a row
+// base per a plus a column offset per b, from the permutation images packed into the pair word.
+// The products are summed without the factor 2 of the reference's terms; t_terms doubles the sum
+// (scaling by 2 commutes with every rounding).
 __device__ __forceinline__ void rpa_pair(const float *S, int nl, int e, float *v) {
     const float *S0 = S, *S1 = S + 16 * nl, *S2 = S + 32 * nl, *S3 = S + 48 * nl;
     {
@@ -520,6 +518,8 @@ __device__ __forceinline__ void rpa_walk(const TriArgs &a, const float *S, int n
     }
 }
 
+// The t integrand for one site j (TRIFrgCore.cpp:733-2368): the RPA lattice sum (the site's run
+// partials of rpa_walk, in order, doubled), then the chalice diagrams with the site-local values L.
 __device__ __forceinline__ void t_terms(const TriArgs &a, const float *S, const float *L, const float *slots, int nl,
                                         int j, float *r) {
     const float *S0 = S, *S1 = S + 16 * nl, *S2 = S + 32 * nl, *S3 = S + 48 * nl;
