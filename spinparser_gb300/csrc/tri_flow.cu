@@ -990,7 +990,7 @@ extern "C" int spn_tri_create(const spn_tri_desc *d, spn_tri **out) {
             h->corr_out = dalloc<float>(size_t(kCorrOut) * h->n_corr + 16 * h->nl, "alloc correlation output");
             h->partial = dalloc<double>(size_t(kMaxCorrNodes) * kCorrOut * h->nl, "alloc correlation scratch");
             h->status = dalloc<unsigned>(1, "alloc status");
-            const int nl = h->nl, nov = h->n_overlap, nr = h->n_range, nc = h->n_corr;
+            const int nl = h->nl, nr = h->n_range, nc = h->n_corr;
             std::vector<int> img;
             std::vector<size_t> at;
             auto put = [&](const int *src, int cnt) {

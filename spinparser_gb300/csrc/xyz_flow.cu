@@ -60,9 +60,9 @@ struct XyzArgs {
     const int *sites, *sites_perm, *inv_sites, *inv_sites_perm;
     // the t channel's RPA pairs of all sites in one lane-balanced walk (lane_schedule): entry i
     // of lane l is sched[32 i + l], the pair's word rid1 | rid2 << 7 | perm1 << 14 | perm2 << 17
-    // (order_rpa_pairs) with bit 20 set on the last entry of a site's run
-    // in the lane), count[l] entries, the runs' partial sums go to slots slot_base[l], ... and
-    // site j sums slots seg_ptr[j] .. seg_ptr[j + 1] - 1
+    // (order_rpa_pairs) with bit 20 set on the last entry of a site's run in the lane; count[l]
+    // entries; the runs' partial sums go to slots slot_base[l], ... and site j sums slots
+    // seg_ptr[j] .. seg_ptr[j + 1] - 1
     const int *rpa_sched, *rpa_count, *rpa_slot_base, *rpa_seg_ptr;
     int rpa_n_seg;
     const int *range_rid, *range_inv;
@@ -640,8 +640,8 @@ struct spn_xyz {
           *corr_out = nullptr;
     float4 *sd = nullptr, *dsd = nullptr;
     int *ints = nullptr;  // all integer tables in one allocation
-    int *sites, *sites_perm, *inv_sites, *inv_sites_perm, *range_rid, *range_inv, *corr_rid, *corr_perm, *node_cnt, *work_counter, *rpa_sched, *rpa_count,
-        *rpa_slot_base, *rpa_seg_ptr;
+    int *sites, *sites_perm, *inv_sites, *inv_sites_perm, *range_rid, *range_inv, *corr_rid, *corr_perm, *node_cnt,
+        *work_counter, *rpa_sched, *rpa_count, *rpa_slot_base, *rpa_seg_ptr;
     int rpa_n_seg = 0;
     unsigned *status = nullptr;
     double *partial = nullptr;
@@ -817,7 +817,7 @@ extern "C" int spn_xyz_create(const spn_xyz_desc *d, spn_xyz **out) {
             h->partial = dalloc<double>(size_t(kMaxCorrNodes) * 4 * h->nl, "alloc correlation scratch");
             h->status = dalloc<unsigned>(1, "alloc status");
             // integer tables, one allocation
-            const int nl = h->nl, nov = h->n_overlap, nr = h->n_range, nc = h->n_corr;
+            const int nl = h->nl, nr = h->n_range, nc = h->n_corr;
             std::vector<int> img;
             std::vector<size_t> at;
             auto put = [&](const int *src, int cnt) {
