@@ -85,6 +85,63 @@ def test_schedule_reproduces_rpa_sums(lat):
 
 
 
+def half_warp_wavefronts(nl, lanes, packed, width, entries):
+    """Mean shared-memory wavefronts of one half warp's 64-bit reads of M per walk step: the
+    largest number of distinct elements in one of the 16 bank pairs.  `entries(l, i)` gives the
+    (rid1, rid2) lane l reads at step i, or None."""
+    tot = steps = 0
+    for h0 in range(0, lanes, 16):
+        i = 0
+        while True:
+            per, any_ = {}, False
+            for l in range(h0, h0 + 16):
+                e = entries(l, i)
+                if e is None:
+                    continue
+                any_ = True
+                a, b = e
+                elem = a * width + b if packed else a * 128 + b
+                per.setdefault((a * width + b if packed else b) & 15, set()).add(elem)
+            if not any_:
+                break
+            tot += max(len(v) for v in per.values())
+            steps += 1
+            i += 1
+    return tot / steps
+
+
+@pytest.mark.parametrize("lattice,rng,model,params,lanes", [
+    ("cubic", 6, "cubic-j1j2heisenberg", {"j1": "1", "j2": "0.25"}, 32),
+    ("pyrochlore", 7, "pyrochlore-j1j2heisenberg", {"j1": "1", "j2": "0.25"}, 256),
+])
+def test_schedule_orders_segments_against_bank_collisions(lattice, rng, model, params, lanes):
+    """The entries inside each segment are ordered against bank collisions of the walk's reads of
+    M: fewer wavefronts per half-warp step than the same chunks in (rid, rid1, rid2) order."""
+    tab = spn.Lattice(lattice, rng, model, params).tables()
+    nl = tab.n_sites
+    info, sched, count, base, seg = schedule(tab, lanes)
+    L, packed, width = int(info[0]), bool(info[3]), int(info[4])
+
+    def ordered(l, i):
+        if i >= count[l]:
+            return None
+        e = int(np.uint32(sched[i * lanes + l]))
+        if packed:
+            return divmod((e & 0xFFFF) // 8, width)
+        return e & 0x7F, (e >> 7) & 0x7F
+    ptr, r1, r2 = tab.overlap_ptr, tab.overlap_rid1, tab.overlap_rid2
+    merged = [(r, a, b) for r in range(nl) for (a, b) in sorted(set(zip(r1[ptr[r]:ptr[r + 1]].tolist(),
+                                                                        r2[ptr[r]:ptr[r + 1]].tolist())))]
+    assert len(merged) == int(count.sum())
+
+    def plain(l, i):
+        j = l * L + i
+        return merged[j][1:] if i < L and j < min(len(merged), (l + 1) * L) else None
+    got = half_warp_wavefronts(nl, lanes, packed, width, ordered)
+    before = half_warp_wavefronts(nl, lanes, packed, width, plain)
+    assert got < 0.75 * before, (got, before)
+
+
 # ---- the lane-balanced walk of the XYZ and TRI t channels (spn_rpa_lane_schedule) ----
 
 # images of (X, Y, Z) under the six spin permutations (X,Y,Z) (X,Z,Y) (Y,X,Z) (Y,Z,X) (Z,X,Y) (Z,Y,X)
