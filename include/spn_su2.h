@@ -55,6 +55,22 @@ int spn_measure_fp32_peak(int device, double *tflops, double *sm_clock_ghz_est);
  * segments; this is the denominator of its gather roofline.  No reference counterpart. */
 int spn_measure_gather_peak(int device, int n_sites, int n_slabs, double *segments_per_s);
 
+/* The frequency-mesh lookups of the vertex kernels, run on the host by the same code (diagnostics;
+ * no device use).  pos: the n ascending positive mesh values.  lesser / greater: the mesh value of
+ * FrequencyDiscretization::lesser / greater on the symmetric mesh (src/FrequencyDiscretization.hpp);
+ * offset: FrequencyDiscretization::offset of |w|; lo, hi, bias: interpolateOffset of |w|.  Any
+ * output may be NULL. */
+int spn_mesh_probe(const float *pos, int n, float w, float *lesser, float *greater, int *offset, int *lo, int *hi,
+                   float *bias);
+
+/* The loop-frequency quadrature nodes of the node tables on the symmetric mesh, run on the host by
+ * the same code (diagnostics; no device use): rule 0 ImplicitIntegrator's
+ * integrateWithObscureLeftBoundary(min, last), 1 integrateWithObscureRightBoundary(beginNegative,
+ * max), 2 integrateWithObscureBoundaries(min, max) (src/lib/Integrator.hpp:137-287).  The integral
+ * of f is sum weight[i] * f(wp[i]).  Up to cap pairs are written; *count is the number of nodes. */
+int spn_quadrature_nodes(const float *pos, int n, int rule, float min, float max, float *wp, double *weight, int cap,
+                         int *count);
+
 /* ------------------------------------------------------------------------------------
  * Host side: lattice / spin model (LatticeModelFactory::newLatticeModel,
  * src/LatticeModelFactory.cpp:733-1047) and discretisations (src/TaskFileParser.cpp:107-198).

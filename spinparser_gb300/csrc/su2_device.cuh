@@ -53,20 +53,36 @@ struct SplitState {
     }
 };
 
+// The mesh searches, interpolations and quadrature rules below also compile for the host, where
+// the library's diagnostics (spn_mesh_probe, spn_quadrature_nodes) run the same code.
+#define SPN_HDI __host__ __device__ __forceinline__
+
 // Single IEEE operations rounded to nearest in the working precision T (float: the
-// reference's types; double: the FP64 flow).
-__device__ __forceinline__ float rn_add(float a, float b) { return __fadd_rn(a, b); }
-__device__ __forceinline__ double rn_add(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ float rn_sub(float a, float b) { return __fsub_rn(a, b); }
-__device__ __forceinline__ double rn_sub(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ float rn_mul(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ double rn_mul(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ float rn_div(float a, float b) { return __fdiv_rn(a, b); }
-__device__ __forceinline__ double rn_div(double a, double b) { return __ddiv_rn(a, b); }
+// reference's types; double: the FP64 flow).  On the host: plain operators, compiled without
+// floating-point contraction.
+#ifdef __CUDA_ARCH__
+SPN_HDI float rn_add(float a, float b) { return __fadd_rn(a, b); }
+SPN_HDI double rn_add(double a, double b) { return __dadd_rn(a, b); }
+SPN_HDI float rn_sub(float a, float b) { return __fsub_rn(a, b); }
+SPN_HDI double rn_sub(double a, double b) { return __dsub_rn(a, b); }
+SPN_HDI float rn_mul(float a, float b) { return __fmul_rn(a, b); }
+SPN_HDI double rn_mul(double a, double b) { return __dmul_rn(a, b); }
+SPN_HDI float rn_div(float a, float b) { return __fdiv_rn(a, b); }
+SPN_HDI double rn_div(double a, double b) { return __ddiv_rn(a, b); }
+#else
+SPN_HDI float rn_add(float a, float b) { return a + b; }
+SPN_HDI double rn_add(double a, double b) { return a + b; }
+SPN_HDI float rn_sub(float a, float b) { return a - b; }
+SPN_HDI double rn_sub(double a, double b) { return a - b; }
+SPN_HDI float rn_mul(float a, float b) { return a * b; }
+SPN_HDI double rn_mul(double a, double b) { return a * b; }
+SPN_HDI float rn_div(float a, float b) { return a / b; }
+SPN_HDI double rn_div(double a, double b) { return a / b; }
+#endif
 
 // First index i in [1, n) with pos[i] > w; n if none (also for NaN w).
 template <class T>
-__device__ __forceinline__ int first_greater(const T *pos, int n, T w) {
+SPN_HDI int first_greater(const T *pos, int n, T w) {
     int lo = 1, hi = n;
     while (lo < hi) {
         int mid = (lo + hi) >> 1;
@@ -78,7 +94,7 @@ __device__ __forceinline__ int first_greater(const T *pos, int n, T w) {
 
 // First index i in [1, n) with pos[i] >= w; n if none.
 template <class T>
-__device__ __forceinline__ int first_geq(const T *pos, int n, T w) {
+SPN_HDI int first_geq(const T *pos, int n, T w) {
     int lo = 1, hi = n;
     while (lo < hi) {
         int mid = (lo + hi) >> 1;
@@ -90,7 +106,7 @@ __device__ __forceinline__ int first_geq(const T *pos, int n, T w) {
 
 // FrequencyDiscretization::offset (w >= 0): index of the mesh point equal to w.
 template <class T>
-__device__ __forceinline__ int mesh_offset(const T *pos, int n, T w) {
+SPN_HDI int mesh_offset(const T *pos, int n, T w) {
     if (w <= pos[0]) return 0;
     int i = first_geq(pos, n, w);
     return i < n ? i : n - 1;
@@ -98,7 +114,7 @@ __device__ __forceinline__ int mesh_offset(const T *pos, int n, T w) {
 
 // FrequencyDiscretization::interpolateOffset (w >= 0).
 template <class T>
-__device__ __forceinline__ void mesh_interp(const T *pos, int n, T w, int &lo, int &hi, T &bias) {
+SPN_HDI void mesh_interp(const T *pos, int n, T w, int &lo, int &hi, T &bias) {
     if (w <= pos[0]) {
         lo = hi = 0;
         bias = T(0);
@@ -184,28 +200,28 @@ __device__ __forceinline__ void mesh_interp_m(const M &m, T w, int &lo, int &hi,
 
 // Index into the symmetric mesh -w[n-1] .. -w[0], w[0] .. w[n-1] (0 .. 2n-1).
 template <class T>
-__device__ __forceinline__ T full_value(const T *pos, int n, int k) { return k < n ? -pos[n - 1 - k] : pos[k - n]; }
+SPN_HDI T full_value(const T *pos, int n, int k) { return k < n ? -pos[n - 1 - k] : pos[k - n]; }
 
 template <class T>
-__device__ __forceinline__ int pos_lesser(const T *pos, int n, T w) {  // w >= 0, returns positive index
+SPN_HDI int pos_lesser(const T *pos, int n, T w) {  // w >= 0, returns positive index
     if (w <= pos[0]) return 0;
     int i = first_greater(pos, n, w);
     return i < n ? i - 1 : n - 1;
 }
 template <class T>
-__device__ __forceinline__ int pos_greater(const T *pos, int n, T w) {  // w >= 0
+SPN_HDI int pos_greater(const T *pos, int n, T w) {  // w >= 0
     if (w <= pos[0]) return 0;
     int i = first_greater(pos, n, w);
     return i < n ? i : n - 1;
 }
 // FrequencyDiscretization::lesser / greater on the full mesh (full index).
 template <class T>
-__device__ __forceinline__ int full_lesser(const T *pos, int n, T w) {
+SPN_HDI int full_lesser(const T *pos, int n, T w) {
     if (w < 0) return n - 1 - pos_greater(pos, n, -w);
     return n + pos_lesser(pos, n, w);
 }
 template <class T>
-__device__ __forceinline__ int full_greater(const T *pos, int n, T w) {
+SPN_HDI int full_greater(const T *pos, int n, T w) {
     if (w < 0) return n - 1 - pos_lesser(pos, n, -w);
     return n + pos_greater(pos, n, w);
 }
@@ -430,7 +446,7 @@ __device__ __forceinline__ T value_none(const T *pos, int n, int nl, const S &v,
 
 // integrateWithObscureLeftBoundary(min, last)
 template <class T, class Emit>
-__device__ void nodes_left(const T *pos, int n, T min, Emit &&emit) {
+__host__ __device__ void nodes_left(const T *pos, int n, T min, Emit &&emit) {
     const int maxi = 2 * n - 1;
     int um = full_greater(pos, n, min);
     if (um != maxi) {
@@ -448,7 +464,7 @@ __device__ void nodes_left(const T *pos, int n, T min, Emit &&emit) {
 
 // integrateWithObscureRightBoundary(beginNegative, max)
 template <class T, class Emit>
-__device__ void nodes_right(const T *pos, int n, T max, Emit &&emit) {
+__host__ __device__ void nodes_right(const T *pos, int n, T max, Emit &&emit) {
     int um = 0;
     const int ux = full_lesser(pos, n, max);
     if (um != ux) {
@@ -466,7 +482,7 @@ __device__ void nodes_right(const T *pos, int n, T max, Emit &&emit) {
 
 // integrateWithObscureBoundaries(min, max)
 template <class T, class Emit>
-__device__ void nodes_both(const T *pos, int n, T min, T max, Emit &&emit) {
+__host__ __device__ void nodes_both(const T *pos, int n, T min, T max, Emit &&emit) {
     int um = full_greater(pos, n, min);
     const int ux = full_lesser(pos, n, max);
     if (ux >= um) {

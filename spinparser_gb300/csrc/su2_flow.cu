@@ -363,6 +363,53 @@ extern "C" int spn_measure_fp32_peak(int device, double *tflops, double *sm_cloc
     });
 }
 
+namespace {
+void check_mesh(const float *pos, int n) {
+    if (!pos || n < 2 || n > kMaxFreq) throw Error(ErrorType::Argument, "mesh: need 2 <= n <= 256 values");
+    for (int i = 0; i < n; ++i)
+        if (!(pos[i] > 0.0f) || (i > 0 && !(pos[i] > pos[i - 1])))
+            throw Error(ErrorType::Argument, "mesh: values must be positive and strictly ascending");
+}
+}  // namespace
+
+extern "C" int spn_mesh_probe(const float *pos, int n, float w, float *lesser, float *greater, int *offset, int *lo,
+                              int *hi, float *bias) {
+    return guarded([&] {
+        check_mesh(pos, n);
+        if (lesser) *lesser = dev::full_value(pos, n, dev::full_lesser(pos, n, w));
+        if (greater) *greater = dev::full_value(pos, n, dev::full_greater(pos, n, w));
+        const float a = w < 0.0f ? -w : w;
+        if (offset) *offset = dev::mesh_offset(pos, n, a);
+        int l = 0, h = 0;
+        float b = 0.0f;
+        dev::mesh_interp(pos, n, a, l, h, b);
+        if (lo) *lo = l;
+        if (hi) *hi = h;
+        if (bias) *bias = b;
+    });
+}
+
+extern "C" int spn_quadrature_nodes(const float *pos, int n, int rule, float min, float max, float *wp, double *weight,
+                                    int cap, int *count) {
+    return guarded([&] {
+        check_mesh(pos, n);
+        if (rule < 0 || rule > 2 || !count || cap < 0 || (cap > 0 && (!wp || !weight)))
+            throw Error(ErrorType::Argument, "spn_quadrature_nodes: bad argument");
+        int k = 0;
+        auto emit = [&](float x, double c) {
+            if (k < cap) {
+                wp[k] = x;
+                weight[k] = c;
+            }
+            ++k;
+        };
+        if (rule == 0) dev::nodes_left(pos, n, min, emit);
+        else if (rule == 1) dev::nodes_right(pos, n, max, emit);
+        else dev::nodes_both(pos, n, min, max, emit);
+        *count = k;
+    });
+}
+
 extern "C" int spn_measure_gather_peak(int device, int n_sites, int n_slabs, double *segments_per_s) {
     return guarded([&] {
         if (!segments_per_s || n_sites < 1 || n_sites > 32 || n_slabs < 1)
