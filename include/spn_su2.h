@@ -63,6 +63,20 @@ int spn_measure_gather_peak(int device, int n_sites, int n_slabs, double *segmen
 int spn_mesh_probe(const float *pos, int n, float w, float *lesser, float *greater, int *offset, int *lo, int *hi,
                    float *bias);
 
+/* The bucket index of the FP32 kernels' mesh lookups against binary search, on the host with the
+ * kernels' code (diagnostics; no device use): *mismatches counts the w[k] for which the first
+ * mesh index above (or at or above) w differs between the two. */
+int spn_mesh_index_check(const float *pos, int n, const float *w, int count, int *mismatches);
+
+/* One vertex read of the kernels on the host with their code (diagnostics; no device use), on a
+ * state in the reference's layout (ss, dd: F_N * n_sites floats, element ((s(s+1)/2 + u) N + t)
+ * n_sites + rid) and the pair's rid and exchanged rid: channel -1 getValue(..., None) (a direct
+ * trilinear read), 0 / 1 / 2 an access buffer whose s / t / u coordinate is a mesh value
+ * (generateAccessBuffer(s, t, u, S / T / U)), 3 the trilinear access buffer; density selects the
+ * density or the spin vertex (src/SU2/SU2VertexTwoParticle.hpp:185-490). */
+int spn_vertex_probe(const float *pos, int n, int n_sites, const float *ss, const float *dd, int rid12, int rid21,
+                     float s, float t, float u, int channel, int density, float *value);
+
 /* The loop-frequency quadrature nodes of the node tables on the symmetric mesh, run on the host by
  * the same code (diagnostics; no device use): rule 0 ImplicitIntegrator's
  * integrateWithObscureLeftBoundary(min, last), 1 integrateWithObscureRightBoundary(beginNegative,

@@ -9,6 +9,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <cstring>
 
 namespace spn {
 namespace dev {
@@ -145,18 +146,27 @@ struct MeshIndex {
     const unsigned short *lo;  // [kMeshBuckets]
     unsigned base;
     int shift;
-    __device__ __forceinline__ int start(float w) const {
+    SPN_HDI int start(float w) const {
+#ifdef __CUDA_ARCH__
         const unsigned key = __float_as_uint(w);
+#else
+        unsigned key;
+        std::memcpy(&key, &w, sizeof key);
+#endif
         unsigned b = key >= base ? (key - base) >> shift : 0u;
         if (b >= unsigned(kMeshBuckets)) b = kMeshBuckets - 1;
+#ifdef __CUDA_ARCH__
         return __ldg(lo + b);
+#else
+        return lo[b];
+#endif
     }
-    __device__ __forceinline__ int first_greater(float w) const {  // as first_greater(pos, n, w)
+    SPN_HDI int first_greater(float w) const {  // as first_greater(pos, n, w)
         int i = start(w);
         while (i < n && !(pos[i] > w)) ++i;
         return i;
     }
-    __device__ __forceinline__ int first_geq(float w) const {  // as first_geq(pos, n, w)
+    SPN_HDI int first_geq(float w) const {  // as first_geq(pos, n, w)
         int i = start(w);
         while (i < n && !(pos[i] >= w)) ++i;
         return i;
@@ -169,19 +179,19 @@ template <class T>
 struct MeshSearch {
     const T *pos;
     int n;
-    __device__ __forceinline__ int first_greater(T w) const { return dev::first_greater(pos, n, w); }
-    __device__ __forceinline__ int first_geq(T w) const { return dev::first_geq(pos, n, w); }
+    SPN_HDI int first_greater(T w) const { return dev::first_greater(pos, n, w); }
+    SPN_HDI int first_geq(T w) const { return dev::first_geq(pos, n, w); }
 };
 
 template <class T, class M>
-__device__ __forceinline__ int mesh_offset_m(const M &m, T w) {
+SPN_HDI int mesh_offset_m(const M &m, T w) {
     if (w <= m.pos[0]) return 0;
     int i = m.first_geq(w);
     return i < m.n ? i : m.n - 1;
 }
 
 template <class T, class M>
-__device__ __forceinline__ void mesh_interp_m(const M &m, T w, int &lo, int &hi, T &bias) {
+SPN_HDI void mesh_interp_m(const M &m, T w, int &lo, int &hi, T &bias) {
     if (w <= m.pos[0]) {
         lo = hi = 0;
         bias = T(0);
@@ -262,7 +272,7 @@ using AB8 = AB8T<float>;
 
 // _generateAccessBufferOffset: storage keeps s >= u; a swapped pair flips the density sign.
 template <class T>
-__device__ __forceinline__ void slab(int si, int ti, int ui, int stepT, int nl, int &off, T w, T &wout, T &swout) {
+SPN_HDI void slab(int si, int ti, int ui, int stepT, int nl, int &off, T w, T &wout, T &swout) {
     if (si < ui) {
         off = (ui * (ui + 1) / 2 + si) * stepT + ti * nl;
         wout = w;
@@ -276,7 +286,7 @@ __device__ __forceinline__ void slab(int si, int ti, int ui, int stepT, int nl, 
 
 // Frequency folding into the stored sector (SU2VertexTwoParticle.hpp:405-427).
 template <class T>
-__device__ __forceinline__ bool fold(T &s, T &t, T &u) {
+SPN_HDI bool fold(T &s, T &t, T &u) {
     bool exch = false;
     if (s < 0 && u < 0) {
         s = -s;
@@ -301,7 +311,7 @@ enum Channel { kS = 0, kT = 1, kU = 2 };
 // the exact mesh index of the channel's own coordinate, which the caller knows when that
 // coordinate is (up to sign) a mesh value (offset(w_i) = i on a strictly ascending mesh).
 template <int CH, class T, class M>
-__device__ __forceinline__ void access4m(const M &m, int nl, T s, T t, T u, AB4T<T> &ab, int e_known = -1) {
+SPN_HDI void access4m(const M &m, int nl, T s, T t, T u, AB4T<T> &ab, int e_known = -1) {
     ab.exch = fold(s, t, u);
     const int stepT = m.n * nl;
     int e, la, ua, lb, ub;
@@ -348,7 +358,7 @@ struct Interp {
     T b;
 };
 template <class T, class M>
-__device__ __forceinline__ Interp<T> interp_abs(const M &m, T w) {
+SPN_HDI Interp<T> interp_abs(const M &m, T w) {
     Interp<T> r;
     mesh_interp_m(m, w < T(0) ? -w : w, r.lo, r.hi, r.b);
     return r;
@@ -358,7 +368,7 @@ __device__ __forceinline__ Interp<T> interp_abs(const M &m, T w) {
 // folding (t for S, s for T and U), ib for the second (u for S and T, t for U).  The caller
 // passes interp_abs of the matching coordinates; folding, weights and offsets are access4m's.
 template <int CH, class T>
-__device__ __forceinline__ void access4i(int n, int nl, T s, T t, T u, const Interp<T> &ia, const Interp<T> &ib,
+SPN_HDI void access4i(int n, int nl, T s, T t, T u, const Interp<T> &ia, const Interp<T> &ib,
                                          int e, AB4T<T> &ab) {
     ab.exch = fold(s, t, u);
     const int stepT = n * nl;
@@ -385,13 +395,13 @@ __device__ __forceinline__ void access4i(int n, int nl, T s, T t, T u, const Int
 }
 
 template <int CH, class T>
-__device__ __forceinline__ void access4(const T *pos, int n, int nl, T s, T t, T u, AB4T<T> &ab) {
+SPN_HDI void access4(const T *pos, int n, int nl, T s, T t, T u, AB4T<T> &ab) {
     access4m<CH>(MeshSearch<T>{pos, n}, nl, s, t, u, ab);
 }
 
 // generateAccessBuffer(s, t, u): trilinear, eight supports (SU2VertexTwoParticle.hpp:500-557).
 template <class T>
-__device__ __forceinline__ void access8(const T *pos, int n, int nl, T s, T t, T u, AB8T<T> &ab) {
+SPN_HDI void access8(const T *pos, int n, int nl, T s, T t, T u, AB8T<T> &ab) {
     ab.exch = fold(s, t, u);
     const int stepT = n * nl;
     int ls, us, lt, ut, lu, uu;
@@ -413,7 +423,7 @@ __device__ __forceinline__ void access8(const T *pos, int n, int nl, T s, T t, T
 // SU2VertexTwoParticle::_directAccessMapFrequencyExchange for one site (density: the density
 // channel, whose sign flips when the stored sector swaps s and u; else the spin channel).
 template <class T, class S>
-__device__ __forceinline__ T direct(const S &v, int si, int ti, int ui, int site, int stepT, int nl, bool density) {
+SPN_HDI T direct(const S &v, int si, int ti, int ui, int site, int stepT, int nl, bool density) {
     if (si >= ui) {
         const int i = (si * (si + 1) / 2 + ui) * stepT + ti * nl + site;
         return density ? v.density(i) : v.spin(i);
@@ -425,7 +435,7 @@ __device__ __forceinline__ T direct(const S &v, int si, int ti, int ui, int site
 // getValue(i1, i2, s, t, u, symmetry, FrequencyChannel::None) where the site pair enters
 // through its rid (rid12) and the rid of the exchanged pair (rid21).
 template <class T, class S>
-__device__ __forceinline__ T value_none(const T *pos, int n, int nl, const S &v, bool density, int rid12, int rid21,
+SPN_HDI T value_none(const T *pos, int n, int nl, const S &v, bool density, int rid12, int rid21,
                                         T s, T t, T u) {
     bool exch = fold(s, t, u);
     const int site = exch ? rid21 : rid12;

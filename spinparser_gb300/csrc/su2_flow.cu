@@ -364,6 +364,37 @@ extern "C" int spn_measure_fp32_peak(int device, double *tflops, double *sm_cloc
 }
 
 namespace {
+// Bucket index of an ascending positive mesh (dev::MeshIndex): the smallest shift that puts the
+// bit patterns of pos[0] .. pos[n-1] into kMeshBuckets buckets, and per bucket the first index
+// >= 1 whose mesh value lies at or above the bucket's start.
+struct MeshBuckets {
+    std::vector<unsigned short> lo;
+    unsigned base = 0;
+    int shift = 0;
+};
+MeshBuckets mesh_buckets(const float *pos, int n) {
+    auto bits = [](float x) { unsigned u; std::memcpy(&u, &x, sizeof u); return u; };
+    MeshBuckets m;
+    m.base = bits(pos[0]);
+    const unsigned span = bits(pos[n - 1]) - m.base;
+    while ((span >> m.shift) >= unsigned(kMeshBuckets)) ++m.shift;
+    m.lo.assign(kMeshBuckets, 0);
+    int i = 0;
+    for (int b = 0; b < kMeshBuckets; ++b) {
+        const unsigned long long start = (unsigned long long)m.base + ((unsigned long long)b << m.shift);
+        while (i < n && (unsigned long long)bits(pos[i]) < start) ++i;
+        m.lo[size_t(b)] = (unsigned short)std::max(1, i);
+    }
+    return m;
+}
+
+// The state of a diagnostic read: the two arrays of the reference's layout on the host.
+struct HostState {
+    const float *ss, *dd;
+    __host__ __device__ float spin(int i) const { return ss[i]; }
+    __host__ __device__ float density(int i) const { return dd[i]; }
+};
+
 void check_mesh(const float *pos, int n) {
     if (!pos || n < 2 || n > kMaxFreq) throw Error(ErrorType::Argument, "mesh: need 2 <= n <= 256 values");
     for (int i = 0; i < n; ++i)
@@ -386,6 +417,53 @@ extern "C" int spn_mesh_probe(const float *pos, int n, float w, float *lesser, f
         if (lo) *lo = l;
         if (hi) *hi = h;
         if (bias) *bias = b;
+    });
+}
+
+extern "C" int spn_mesh_index_check(const float *pos, int n, const float *w, int count, int *mismatches) {
+    return guarded([&] {
+        check_mesh(pos, n);
+        if (count < 0 || (count > 0 && !w) || !mismatches) throw Error(ErrorType::Argument, "spn_mesh_index_check: bad argument");
+        const MeshBuckets mb = mesh_buckets(pos, n);
+        const dev::MeshIndex mi{pos, n, mb.lo.data(), mb.base, mb.shift};
+        const dev::MeshSearch<float> ms{pos, n};
+        int bad = 0;
+        for (int k = 0; k < count; ++k)
+            if (mi.first_greater(w[k]) != ms.first_greater(w[k]) || mi.first_geq(w[k]) != ms.first_geq(w[k])) ++bad;
+        *mismatches = bad;
+    });
+}
+
+extern "C" int spn_vertex_probe(const float *pos, int n, int n_sites, const float *ss, const float *dd, int rid12,
+                                int rid21, float s, float t, float u, int channel, int density, float *value) {
+    return guarded([&] {
+        check_mesh(pos, n);
+        if (n_sites < 1 || n_sites > kMaxSites || !ss || !dd || !value || rid12 < 0 || rid12 >= n_sites || rid21 < 0 ||
+            rid21 >= n_sites || channel < -1 || channel > 3)
+            throw Error(ErrorType::Argument, "spn_vertex_probe: bad argument");
+        const HostState v{ss, dd};
+        if (channel < 0) {
+            *value = dev::value_none(pos, n, n_sites, v, density != 0, rid12, rid21, s, t, u);
+            return;
+        }
+        auto read = [&](const int *off, const float *w, const float *sw, bool exch, int q) {
+            const int site = exch ? rid21 : rid12;
+            float g = 0.0f;
+            for (int k = 0; k < q; ++k) g += (density ? sw[k] : w[k]) * (density ? v.density(off[k] + site) : v.spin(off[k] + site));
+            return g;
+        };
+        const dev::MeshSearch<float> m{pos, n};
+        if (channel == 3) {
+            dev::AB8 ab;
+            dev::access8(pos, n, n_sites, s, t, u, ab);
+            *value = read(ab.off, ab.w, ab.sw, ab.exch, 8);
+            return;
+        }
+        dev::AB4 ab;
+        if (channel == 0) dev::access4m<dev::kS>(m, n_sites, s, t, u, ab);
+        else if (channel == 1) dev::access4m<dev::kT>(m, n_sites, s, t, u, ab);
+        else dev::access4m<dev::kU>(m, n_sites, s, t, u, ab);
+        *value = read(ab.off, ab.w, ab.sw, ab.exch, 4);
     });
 }
 
@@ -518,26 +596,13 @@ spn_su2 *spn::create_flow(const spn_su2_desc *d, cudaStream_t stream) {
             h->corr_partial = dev_alloc<double>(size_t(kMaxCorrNodes) * 2 * h->nl, "alloc corr scratch");
             if (!f64) h->corr_out = dev_alloc<float>(2 * size_t(h->n_corr) + 2 * h->nl, "alloc corr out");
             upload(h->freq, d->freq, h->n, h->stream);
-            // bucket index of the mesh (dev::MeshIndex): the smallest shift that puts the bit
-            // patterns of freq[0] .. freq[n-1] into kMeshBuckets buckets, and per bucket the
-            // first index >= 1 whose mesh value lies at or above the bucket's start
             {
-                auto bits = [](float x) { unsigned u; std::memcpy(&u, &x, sizeof u); return u; };
-                const unsigned base = bits(d->freq[0]), span = bits(d->freq[h->n - 1]) - base;
-                int shift = 0;
-                while ((span >> shift) >= unsigned(kMeshBuckets)) ++shift;
-                std::vector<unsigned short> lo(kMeshBuckets);
-                int i = 0;
-                for (int b = 0; b < kMeshBuckets; ++b) {
-                    const unsigned long long start = (unsigned long long)base + ((unsigned long long)b << shift);
-                    while (i < h->n && (unsigned long long)bits(d->freq[i]) < start) ++i;
-                    lo[b] = (unsigned short)std::max(1, i);
-                }
+                const MeshBuckets mb = mesh_buckets(d->freq, h->n);
                 h->mesh_lo = dev_alloc<unsigned short>(kMeshBuckets, "alloc mesh index");
-                upload(h->mesh_lo, lo.data(), kMeshBuckets, h->stream);
-                h->mesh_base = base;
-                h->mesh_shift = shift;
-                cuda_check(cudaStreamSynchronize(h->stream), "mesh index sync");  // lo leaves scope
+                upload(h->mesh_lo, mb.lo.data(), kMeshBuckets, h->stream);
+                h->mesh_base = mb.base;
+                h->mesh_shift = mb.shift;
+                cuda_check(cudaStreamSynchronize(h->stream), "mesh index sync");  // mb leaves scope
             }
             upload(h->sites, d->sites_rid, h->nl, h->stream);
             upload(h->inv_sites, d->inv_sites_rid, h->nl, h->stream);

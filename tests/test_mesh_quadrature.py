@@ -93,3 +93,90 @@ def test_bad_meshes_are_rejected():
         pos = np.ascontiguousarray(mesh, np.float32)
         with pytest.raises(SpnError):
             check(lib.spn_quadrature_nodes(pos.ctypes.data_as(fp), len(pos), 0, 1.0, 0.0, None, None, 0, C.byref(cnt)))
+
+
+def test_bucket_index_matches_binary_search():
+    """The FP32 kernels look the mesh up through a bucket index; it must give the binary
+    search's answer everywhere: mesh points, their float neighbours, outside the mesh, NaN."""
+    lib = load_library()
+    import spinparser_gb300 as spn
+    for mesh in (MESH10, list(spn.frequency_exponential(0.005, 100.0, 64)), list(spn.frequency_exponential(0.002, 100.0, 256))):
+        pos = np.ascontiguousarray(mesh, np.float32)
+        pts = [pos, np.nextafter(pos, 0).astype(np.float32), np.nextafter(pos, np.inf).astype(np.float32),
+               np.float32([0.0, 1e-30, 1e-6, 1e3, 1e30, np.inf, np.nan]),
+               np.random.default_rng(5).uniform(0, 1.2 * pos[-1], 4000).astype(np.float32)]
+        w = np.ascontiguousarray(np.concatenate(pts), np.float32)
+        bad = C.c_int()
+        check(lib.spn_mesh_index_check(pos.ctypes.data_as(fp), len(pos), w.ctypes.data_as(fp), len(w), C.byref(bad)))
+        assert bad.value == 0
+
+
+# ---- vertex reads (test/test_SU2VertexTwoParticle.cpp:120-245: mesh {1, ..., 5}, square lattice
+# range 3, state value i in the spin vertex and i + 1 in the density vertex at element i) ----
+
+def vertex_fixture():
+    import spinparser_gb300 as spn
+    tab = spn.Lattice("square", 3, "square-heisenberg", {"j": "1"}).tables()
+    n, nl = 5, tab.n_sites
+    fn = n * n * (n + 1) // 2
+    ss = np.arange(fn * nl, dtype=np.float32)
+    dd = ss + np.float32(1.0)
+    rid12 = 1                                 # the second site of the range of the basis site
+    rid21 = int(tab.inv_sites_rid[rid12])     # the same pair, sites exchanged
+    return np.float32(MESH5), nl, ss, dd, rid12, rid21
+
+
+def vread(fx, s, t, u, channel=-1, density=False, exchanged=False):
+    pos, nl, ss, dd, r12, r21 = fx
+    if exchanged:
+        r12, r21 = r21, r12
+    out = C.c_float()
+    check(load_library().spn_vertex_probe(pos.ctypes.data_as(fp), len(pos), nl, ss.ctypes.data_as(fp),
+                                          dd.ctypes.data_as(fp), r12, r21, s, t, u, channel, int(density),
+                                          C.byref(out)))
+    return out.value
+
+
+@pytest.mark.parametrize("density", [False, True])
+def test_vertex_symmetries(density):
+    """getValueSymmetry: s -> -s and u -> -u exchange the sites, t -> -t changes nothing, s <-> u
+    flips the sign of the density vertex only."""
+    fx = vertex_fixture()
+    s, t, u = 1.0, 2.0, 3.0
+    v = vread(fx, s, t, u, density=density)
+    assert v == vread(fx, -s, t, u, density=density, exchanged=True)
+    assert v == vread(fx, s, -t, u, density=density)
+    assert v == vread(fx, s, t, -u, density=density, exchanged=True)
+    assert v == (-1.0 if density else 1.0) * vread(fx, u, t, s, density=density)
+
+
+@pytest.mark.parametrize("density", [False, True])
+@pytest.mark.parametrize("channel,axis", [(-1, 0), (0, 1), (1, 2), (2, 0)])
+def test_vertex_interpolation_is_linear(density, channel, axis):
+    """getValueInterpolation: between two mesh values the read is the linear interpolation of the
+    reads at them, for the direct read (None) and the s-, t- and u-channel access buffers (the
+    interpolated coordinate is one the channel leaves free)."""
+    fx = vertex_fixture()
+    w_exact, w_lower, w_upper, lam = 1.0, 2.0, 3.0, 0.2
+    mid = np.float32((1.0 - lam) * w_lower + lam * w_upper)
+
+    def at(x):
+        c = [w_exact, w_exact, w_exact]
+        c[axis] = x
+        return c
+    lower, upper = vread(fx, *at(w_lower), density=density), vread(fx, *at(w_upper), density=density)
+    exact = vread(fx, *at(mid), channel=channel, density=density)
+    assert exact == pytest.approx((1.0 - lam) * lower + lam * upper, rel=1e-6)
+
+
+@pytest.mark.parametrize("density", [False, True])
+@pytest.mark.parametrize("s,t,u,channel", [
+    (1.1, 2.2, 3.3, 3), (2.0, 3.0, 4.0, 3), (2.0, 3.5, 4.5, 0), (2.5, 3.0, 4.5, 1), (2.5, 3.5, 4.0, 2),
+    (-2.0, 3.5, 4.5, 0), (2.5, -3.0, -4.5, 1), (-2.5, 3.5, 4.0, 2), (-1.1, 2.2, -3.3, 3),
+])
+def test_access_buffer_read_equals_direct_read(density, s, t, u, channel):
+    """getValueBuffered: a read through an access buffer equals the direct read at the same
+    frequencies (the buffer's channel coordinate is a mesh value); negative frequencies fold."""
+    fx = vertex_fixture()
+    assert vread(fx, s, t, u, channel=channel, density=density) == pytest.approx(
+        vread(fx, s, t, u, density=density), rel=1e-6)
