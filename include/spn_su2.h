@@ -77,6 +77,10 @@ int spn_mesh_index_check(const float *pos, int n, const float *w, int count, int
 int spn_vertex_probe(const float *pos, int n, int n_sites, const float *ss, const float *dd, int rid12, int rid21,
                      float s, float t, float u, int channel, int density, float *value);
 
+/* The self-energy read of the kernels (SU2VertexSingleParticle::getValue, odd in w and linearly
+ * interpolated on the positive mesh) on the host with their code (diagnostics; no device use). */
+int spn_self_energy_probe(const float *pos, int n, const float *data, float w, double *value);
+
 /* The loop-frequency quadrature nodes of the node tables on the symmetric mesh, run on the host by
  * the same code (diagnostics; no device use): rule 0 ImplicitIntegrator's
  * integrateWithObscureLeftBoundary(min, last), 1 integrateWithObscureRightBoundary(beginNegative,

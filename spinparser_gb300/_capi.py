@@ -95,6 +95,7 @@ SIGNATURES = {
     "spn_quadrature_nodes": (C.c_int, [c_float_p, C.c_int, C.c_int, C.c_float, C.c_float, c_float_p, c_double_p,
                                        C.c_int, c_int_p]),
     "spn_mesh_index_check": (C.c_int, [c_float_p, C.c_int, c_float_p, C.c_int, c_int_p]),
+    "spn_self_energy_probe": (C.c_int, [c_float_p, C.c_int, c_float_p, C.c_float, c_double_p]),
     "spn_vertex_probe": (C.c_int, [c_float_p, C.c_int, C.c_int, c_float_p, c_float_p, C.c_int, C.c_int, C.c_float,
                                    C.c_float, C.c_float, C.c_int, C.c_int, c_float_p]),
     "spn_lattice_create": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_char_p, C.c_int,

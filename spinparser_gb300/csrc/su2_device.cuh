@@ -239,7 +239,7 @@ SPN_HDI int full_greater(const T *pos, int n, T w) {
 // Linear interpolation of a function stored on the positive mesh and odd in w
 // (SU2VertexSingleParticle::getValue, src/SU2/SU2VertexSingleParticle.hpp:73-87).
 template <class P, class T>
-__device__ __forceinline__ double odd_interp(const P *pos, int n, const T *data, P w) {
+SPN_HDI double odd_interp(const P *pos, int n, const T *data, P w) {
     double sign = 1.0;
     if (w < 0) {
         w = -w;

@@ -467,6 +467,14 @@ extern "C" int spn_vertex_probe(const float *pos, int n, int n_sites, const floa
     });
 }
 
+extern "C" int spn_self_energy_probe(const float *pos, int n, const float *data, float w, double *value) {
+    return guarded([&] {
+        check_mesh(pos, n);
+        if (!data || !value) throw Error(ErrorType::Argument, "spn_self_energy_probe: bad argument");
+        *value = dev::odd_interp(pos, n, data, w);
+    });
+}
+
 extern "C" int spn_quadrature_nodes(const float *pos, int n, int rule, float min, float max, float *wp, double *weight,
                                     int cap, int *count) {
     return guarded([&] {

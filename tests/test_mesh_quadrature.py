@@ -180,3 +180,38 @@ def test_access_buffer_read_equals_direct_read(density, s, t, u, channel):
     fx = vertex_fixture()
     assert vread(fx, s, t, u, channel=channel, density=density) == pytest.approx(
         vread(fx, s, t, u, density=density), rel=1e-6)
+
+
+@pytest.mark.parametrize("density", [False, True])
+def test_local_and_superbundle_reads(density):
+    """getValueLocal and getValueSuperbundle: through the trilinear access buffer, the read of the
+    pair (origin, origin) and of (origin, rid) for every rid equals the direct read."""
+    pos, nl, ss, dd, _, _ = vertex_fixture()
+    import spinparser_gb300 as spn
+    inv = spn.Lattice("square", 3, "square-heisenberg", {"j": "1"}).tables().inv_sites_rid
+    for rid in range(nl):
+        fx = (pos, nl, ss, dd, rid, int(inv[rid]))
+        assert vread(fx, 1.1, 2.2, 3.3, channel=3, density=density) == pytest.approx(
+            vread(fx, 1.1, 2.2, 3.3, density=density), rel=1e-6)
+
+
+def se_read(data, w):
+    out = C.c_double()
+    pos = np.float32(MESH5)
+    d = np.ascontiguousarray(data, np.float32)
+    check(load_library().spn_self_energy_probe(pos.ctypes.data_as(fp), len(pos), d.ctypes.data_as(fp), w,
+                                               C.byref(out)))
+    return out.value
+
+
+def test_self_energy_reads():
+    """test/test_SU2VertexSingleParticle.cpp:75-105: the value at mesh point i is data[i], the read
+    is odd in w, and between two mesh points it is the linear interpolation."""
+    data = np.arange(5, dtype=np.float32)
+    for i, w in enumerate(MESH5):
+        assert se_read(data, w) == data[i]
+        assert se_read(data, w) == -se_read(data, -w)
+    data = np.float32([2.0, 3.0, 0.0, 0.0, 0.0])
+    lam = 0.2
+    w = np.float32((1.0 - lam) * MESH5[0] + lam * MESH5[1])
+    assert se_read(data, float(w)) == pytest.approx((1.0 - lam) * 2.0 + lam * 3.0, rel=1e-6)
