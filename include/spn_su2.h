@@ -514,6 +514,18 @@ int spn_xyz_finalize_step(spn_xyz *h, float new_cutoff);
 int spn_xyz_measure_correlation(spn_xyz *h, float *xx, float *yy, float *zz, float *dd, float *chi);
 int spn_xyz_is_diverged(spn_xyz *h, int *diverged);
 
+/* One vertex read of the XYZ kernels on the host with their code (diagnostics; no device use), on
+ * a state in the layout of spn_xyz_set_state (v4xx ... v4dd: F_N * n_sites floats each), for the
+ * pair with rid rid12 and spin permutation perm12 and the site-exchanged pair (rid21, perm21):
+ * value[4] = X, Y, Z, D.  channel -1: getValue(..., None) (a direct trilinear read; identity
+ * permutations); 0 / 1 / 2: the superbundle gather through an access buffer whose s / t / u
+ * coordinate is a mesh value; 3: the correlation's gather through the trilinear access buffer.
+ * local != 0 (channels 0-3): getValueLocal instead of the pair's read
+ * (src/XYZ/XYZVertexTwoParticle.hpp:185-612). */
+int spn_xyz_vertex_probe(const float *pos, int n, int n_sites, const float *v4xx, const float *v4yy,
+                         const float *v4zz, const float *v4dd, int rid12, int rid21, int perm12, int perm21, float s,
+                         float t, float u, int channel, int local, float *value);
+
 /* ------------------------------------------------------------------------------------
  * TRI core: time-reversal-invariant models with general, also off-diagonal, couplings
  * (Heisenberg-Kitaev-Gamma, ...), 16 vertex components (a, b), a, b in X, Y, Z, density
@@ -542,6 +554,15 @@ int spn_tri_finalize_step(spn_tri *h, float new_cutoff);
  * pointer may be NULL. */
 int spn_tri_measure_correlation(spn_tri *h, float *corr, float *chi);
 int spn_tri_is_diverged(spn_tri *h, int *diverged);
+
+/* One vertex read of the TRI kernels on the host with their code (diagnostics; no device use), on
+ * a state v4 in the reference layout, with the arguments of spn_xyz_vertex_probe: value[16] =
+ * component 4a + b.  channel -1: getValue(..., a, b, None); 0 / 1 / 2: the vertex kernel's slab
+ * gather through an access buffer whose s / t / u coordinate is a mesh value; 3: the
+ * correlation's superbundle read through the trilinear access buffer; local != 0: getValueLocal
+ * (src/TRI/TRIVertexTwoParticle.hpp:190-671). */
+int spn_tri_vertex_probe(const float *pos, int n, int n_sites, const float *v4, int rid12, int rid21, int perm12,
+                         int perm21, float s, float t, float u, int channel, int local, float *value);
 
 /* The coefficient tables the TRI kernels evaluate, as rows (table, output, n, a, b, sign):
  * table 0 particle-particle ladder, 1 particle-hole ladder, 2 RPA, 3 chalice, 4 inverse

@@ -98,6 +98,11 @@ SIGNATURES = {
     "spn_self_energy_probe": (C.c_int, [c_float_p, C.c_int, c_float_p, C.c_float, c_double_p]),
     "spn_vertex_probe": (C.c_int, [c_float_p, C.c_int, C.c_int, c_float_p, c_float_p, C.c_int, C.c_int, C.c_float,
                                    C.c_float, C.c_float, C.c_int, C.c_int, c_float_p]),
+    "spn_xyz_vertex_probe": (C.c_int, [c_float_p, C.c_int, C.c_int, c_float_p, c_float_p, c_float_p, c_float_p,
+                                       C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int,
+                                       C.c_int, c_float_p]),
+    "spn_tri_vertex_probe": (C.c_int, [c_float_p, C.c_int, C.c_int, c_float_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, c_float_p]),
     "spn_lattice_create": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_char_p, C.c_int,
                                      C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.POINTER(C.c_void_p)]),
     "spn_lattice_destroy": (C.c_int, [C.c_void_p]),

@@ -30,5 +30,22 @@ void h2d(T *dst, const T *src, size_t count, cudaStream_t s) {
 // blocks of 256 threads for an elementwise kernel over n items (grid-stride beyond 4096 blocks)
 inline int copy_grid(long long n) { return int(std::min<long long>((n + 255) / 256, 4096)); }
 
+// The frequency mesh of a diagnostic read: 2 <= n <= max_n positive, strictly ascending values.
+inline void check_mesh(const float *pos, int n, int max_n) {
+    if (!pos || n < 2 || n > max_n)
+        throw Error(ErrorType::Argument, "mesh: need 2 <= n <= " + std::to_string(max_n) + " values");
+    for (int i = 0; i < n; ++i)
+        if (!(pos[i] > 0.0f) || (i > 0 && !(pos[i] > pos[i - 1])))
+            throw Error(ErrorType::Argument, "mesh: values must be positive and strictly ascending");
+}
+
+// The index of the mesh value |w| (the channel's own frequency of an access buffer).
+inline int mesh_index_of(const float *pos, int n, float w) {
+    const float a = w < 0.0f ? -w : w;
+    for (int i = 0; i < n; ++i)
+        if (pos[i] == a) return i;
+    throw Error(ErrorType::Argument, "the channel's own frequency must be a mesh value");
+}
+
 }  // namespace cuh
 }  // namespace spn

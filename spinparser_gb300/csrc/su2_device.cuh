@@ -81,6 +81,17 @@ SPN_HDI float rn_div(float a, float b) { return a / b; }
 SPN_HDI double rn_div(double a, double b) { return a / b; }
 #endif
 
+// A read of the flow's read-only state: through the non-coherent cache on the device, a plain
+// read on the host.
+template <class T>
+SPN_HDI T ro_load(const T *p) {
+#ifdef __CUDA_ARCH__
+    return __ldg(p);
+#else
+    return *p;
+#endif
+}
+
 // First index i in [1, n) with pos[i] > w; n if none (also for NaN w).
 template <class T>
 SPN_HDI int first_greater(const T *pos, int n, T w) {

@@ -29,6 +29,7 @@
 #include "su2_device.cuh"
 #include "su2_kernels.cuh"
 #include "su2_handle.cuh"
+#include "cuda_host.cuh"
 #include "host/rpa_schedule.hpp"
 #include "host/capi_common.hpp"
 #include "../../include/spn_su2.h"
@@ -395,12 +396,7 @@ struct HostState {
     __host__ __device__ float density(int i) const { return dd[i]; }
 };
 
-void check_mesh(const float *pos, int n) {
-    if (!pos || n < 2 || n > kMaxFreq) throw Error(ErrorType::Argument, "mesh: need 2 <= n <= 256 values");
-    for (int i = 0; i < n; ++i)
-        if (!(pos[i] > 0.0f) || (i > 0 && !(pos[i] > pos[i - 1])))
-            throw Error(ErrorType::Argument, "mesh: values must be positive and strictly ascending");
-}
+void check_mesh(const float *pos, int n) { cuh::check_mesh(pos, n, kMaxFreq); }
 }  // namespace
 
 extern "C" int spn_mesh_probe(const float *pos, int n, float w, float *lesser, float *greater, int *offset, int *lo,

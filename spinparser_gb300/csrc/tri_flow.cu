@@ -51,7 +51,7 @@ constexpr unsigned long long kPermBits =
 __host__ __device__ __forceinline__ int permc(int p, int c) {
     return c == 3 ? 3 : int((kPermBits >> (6 * p + 2 * c)) & 3ull);
 }
-__device__ __forceinline__ float zeta(int c) { return c <= 2 ? -1.0f : 1.0f; }
+SPN_HDI float zeta(int c) { return c <= 2 ? -1.0f : 1.0f; }
 
 struct TriArgs {
     int n, nl, fn, max_nodes, n_range, n_corr;
@@ -94,14 +94,14 @@ using TAB4 = TABT<4>;
 using TAB8 = TABT<8>;
 
 // sign[i][a][b] of the access buffer (TRIVertexTwoParticle.hpp:401-448, 643-671)
-__device__ __forceinline__ float tab_sign(int fl, int i, int a, int b) {
+SPN_HDI float tab_sign(int fl, int i, int a, int b) {
     float s = 1.0f;
     if (fl & kFlTu) s *= zeta(a) * zeta(b);
     if ((fl >> i) & 1) s *= -((fl & kFlExch) ? zeta(a) : zeta(b));
     return s;
 }
 
-__device__ __forceinline__ int tri_fold(float &s, float &t, float &u) {
+SPN_HDI int tri_fold(float &s, float &t, float &u) {
     int fl = 0;
     if (s < 0) {
         s = -s;
@@ -118,7 +118,7 @@ __device__ __forceinline__ int tri_fold(float &s, float &t, float &u) {
     return fl;
 }
 
-__device__ __forceinline__ void tri_slab(int si, int ti, int ui, int step_su, int step_t, int i, int &off, int &fl) {
+SPN_HDI void tri_slab(int si, int ti, int ui, int step_su, int step_t, int i, int &off, int &fl) {
     if (si < ui) {
         off = (ui * (ui + 1) / 2 + si) * step_su + ti * step_t;
         fl |= 1 << i;
@@ -127,53 +127,13 @@ __device__ __forceinline__ void tri_slab(int si, int ti, int ui, int step_su, in
     }
 }
 
-// generateAccessBuffer(s, t, u, channel) (TRIVertexTwoParticle.hpp:401-505); e = the exact mesh
-// index of the channel's own coordinate, which every caller here knows.
-template <int CH, class M>
-__device__ __forceinline__ void tri_access4(const M &m, int nl, float s, float t, float u, int e, TAB4 &ab) {
-    int fl = tri_fold(s, t, u);
-    const int step_t = 16 * nl, step_su = m.n * step_t;
-    int la, ua, lb, ub;
-    float ba, bb;
-    if (CH == kS) {
-        mesh_interp_m(m, t, la, ua, ba);
-        mesh_interp_m(m, u, lb, ub, bb);
-    } else if (CH == kT) {
-        mesh_interp_m(m, s, la, ua, ba);
-        mesh_interp_m(m, u, lb, ub, bb);
-    } else {
-        mesh_interp_m(m, s, la, ua, ba);
-        mesh_interp_m(m, t, lb, ub, bb);
-    }
-    const float na = rn_sub(1.0f, ba), nb = rn_sub(1.0f, bb);
-    ab.w[0] = rn_mul(nb, na);
-    ab.w[1] = rn_mul(nb, ba);
-    ab.w[2] = rn_mul(bb, na);
-    ab.w[3] = rn_mul(bb, ba);
-    if (CH == kS) {
-        tri_slab(e, la, lb, step_su, step_t, 0, ab.off[0], fl);
-        tri_slab(e, ua, lb, step_su, step_t, 1, ab.off[1], fl);
-        tri_slab(e, la, ub, step_su, step_t, 2, ab.off[2], fl);
-        tri_slab(e, ua, ub, step_su, step_t, 3, ab.off[3], fl);
-    } else if (CH == kT) {
-        tri_slab(la, e, lb, step_su, step_t, 0, ab.off[0], fl);
-        tri_slab(ua, e, lb, step_su, step_t, 1, ab.off[1], fl);
-        tri_slab(la, e, ub, step_su, step_t, 2, ab.off[2], fl);
-        tri_slab(ua, e, ub, step_su, step_t, 3, ab.off[3], fl);
-    } else {
-        tri_slab(la, lb, e, step_su, step_t, 0, ab.off[0], fl);
-        tri_slab(ua, lb, e, step_su, step_t, 1, ab.off[1], fl);
-        tri_slab(la, ub, e, step_su, step_t, 2, ab.off[2], fl);
-        tri_slab(ua, ub, e, step_su, step_t, 3, ab.off[3], fl);
-    }
-    ab.fl = fl;
-}
-
-// tri_access4 with the two interpolations given (interp_abs of the interpolated coordinates,
-// as for access4i): a node's buffers interpolate four distinct magnitudes, each looked up once.
+// generateAccessBuffer(s, t, u, channel) (TRIVertexTwoParticle.hpp:401-505) with e the exact mesh
+// index of the channel's own coordinate, which every caller knows, and the two interpolations
+// given (interp_abs of the interpolated coordinates, as for access4i): a node's buffers
+// interpolate four distinct magnitudes, each looked up once.
 template <int CH>
-__device__ __forceinline__ void tri_access4i(int n, int nl, float s, float t, float u, int e, const Interp<float> &ia,
-                                             const Interp<float> &ib, TAB4 &ab) {
+SPN_HDI void tri_access4i(int n, int nl, float s, float t, float u, int e, const Interp<float> &ia,
+                          const Interp<float> &ib, TAB4 &ab) {
     int fl = tri_fold(s, t, u);
     const int step_t = 16 * nl, step_su = n * step_t;
     const int la = ia.lo, ua = ia.hi, lb = ib.lo, ub = ib.hi;
@@ -203,7 +163,7 @@ __device__ __forceinline__ void tri_access4i(int n, int nl, float s, float t, fl
 }
 
 // generateAccessBuffer(s, t, u): trilinear (TRIVertexTwoParticle.hpp:514-584)
-__device__ __forceinline__ void tri_access8(const float *pos, int n, int nl, float s, float t, float u, TAB8 &ab) {
+SPN_HDI void tri_access8(const float *pos, int n, int nl, float s, float t, float u, TAB8 &ab) {
     int fl = tri_fold(s, t, u);
     const int step_t = 16 * nl, step_su = n * step_t;
     int ls, us, lt, ut, lu, uu;
@@ -234,7 +194,7 @@ __device__ __forceinline__ void tri_access8(const float *pos, int n, int nl, flo
 // getValueLocal(a, b, ab) (TRIVertexTwoParticle.hpp:347-356): the components are exchanged
 // first and index the sign table in that order.
 template <int K>
-__device__ __forceinline__ float tri_local(const float *v4, int nl, const TABT<K> &ab, int ca, int cb) {
+SPN_HDI float tri_local(const float *v4, int nl, const TABT<K> &ab, int ca, int cb) {
     if (ab.fl & kFlExch) {
         const int x = ca;
         ca = cb;
@@ -243,27 +203,28 @@ __device__ __forceinline__ float tri_local(const float *v4, int nl, const TABT<K
     const int o = (4 * ca + cb) * nl;
     float v = 0.0f;
 #pragma unroll
-    for (int i = 0; i < K; ++i) v += tab_sign(ab.fl, i, ca, cb) * ab.w[i] * __ldg(v4 + ab.off[i] + o);
+    for (int i = 0; i < K; ++i) v += tab_sign(ab.fl, i, ca, cb) * ab.w[i] * ro_load(v4 + ab.off[i] + o);
     return v;
 }
 
 // getValueSuperbundle component c of site j (TRIVertexTwoParticle.hpp:364-391): the
 // (exchanged, then permuted) component of the site's representative.
 template <int K>
-__device__ __forceinline__ float tri_bundle(const float *v4, int nl, const TABT<K> &ab, int c, int r, int p) {
+SPN_HDI float tri_bundle(const float *v4, int nl, const TABT<K> &ab, int c, int r, int p) {
     const int ca = c >> 2, cb = c & 3;
     const bool ex = ab.fl & kFlExch;
     const int o = (4 * permc(p, ex ? cb : ca) + permc(p, ex ? ca : cb)) * nl + r;
     float v = 0.0f;
 #pragma unroll
-    for (int i = 0; i < K; ++i) v += tab_sign(ab.fl, i, ca, cb) * ab.w[i] * __ldg(v4 + ab.off[i] + o);
+    for (int i = 0; i < K; ++i) v += tab_sign(ab.fl, i, ca, cb) * ab.w[i] * ro_load(v4 + ab.off[i] + o);
     return v;
 }
 
 // getValue(i1, i2, s, t, u, a, b, FrequencyChannel::None) (TRIVertexTwoParticle.hpp:190-312)
-// for the pairs the self-energy reads: through rid12 / rid21 with identity spin maps.
-__device__ float tri_value_none(const float *pos, const TriArgs &a, int ca, int cb, int rid12, int rid21, float s,
-                                float t, float u) {
+// for the pairs the self-energy reads: through rid12 / rid21 with identity spin maps, on the
+// state v4 of n frequencies and nl sites.
+__host__ __device__ float tri_value_none(const float *pos, int n, int nl, const float *v4, int ca, int cb, int rid12,
+                                         int rid21, float s, float t, float u) {
     float sign = 1.0f;
     bool sw = false;
     if (s < 0) {
@@ -282,16 +243,16 @@ __device__ float tri_value_none(const float *pos, const TriArgs &a, int ca, int 
         sign *= zeta(ca) * zeta(cb);
     }
     const int site = sw ? rid21 : rid12;
-    const int nl = a.nl, step_t = 16 * nl, step_su = a.n * step_t, co = (4 * ca + cb) * nl + site;
+    const int step_t = 16 * nl, step_su = n * step_t, co = (4 * ca + cb) * nl + site;
     const float zb = -zeta(cb);
     int ls, us, lt, ut, lu, uu;
     float bs, bt, bu;
-    mesh_interp(pos, a.n, s, ls, us, bs);
-    mesh_interp(pos, a.n, t, lt, ut, bt);
-    mesh_interp(pos, a.n, u, lu, uu, bu);
+    mesh_interp(pos, n, s, ls, us, bs);
+    mesh_interp(pos, n, t, lt, ut, bt);
+    mesh_interp(pos, n, u, lu, uu, bu);
     auto Dv = [&](int x, int y, int z) {
-        if (x >= z) return __ldg(a.v4 + (x * (x + 1) / 2 + z) * step_su + y * step_t + co);
-        return zb * __ldg(a.v4 + (z * (z + 1) / 2 + x) * step_su + y * step_t + co);
+        if (x >= z) return ro_load(v4 + (x * (x + 1) / 2 + z) * step_su + y * step_t + co);
+        return zb * ro_load(v4 + (z * (z + 1) / 2 + x) * step_su + y * step_t + co);
     };
     return sign * ((1 - bu) * ((1 - bt) * ((1 - bs) * Dv(ls, lt, lu) + bs * Dv(us, lt, lu)) +
                                bt * ((1 - bs) * Dv(ls, ut, lu) + bs * Dv(us, ut, lu))) +
@@ -313,8 +274,8 @@ __global__ void __launch_bounds__(128) tri_self_energy_kernel(TriArgs a) {
     double part = 0.0;
     for (int j = threadIdx.x; j < a.n_range; j += blockDim.x) {
         const int r12 = a.range_rid[j], r21 = a.range_inv[j];
-        part += double(tri_value_none(pos, a, 3, 3, r12, r21, wpl, 0.0f, wml)) -
-                double(tri_value_none(pos, a, 3, 3, r12, r21, wml, 0.0f, wpl));
+        part += double(tri_value_none(pos, a.n, a.nl, a.v4, 3, 3, r12, r21, wpl, 0.0f, wml)) -
+                double(tri_value_none(pos, a.n, a.nl, a.v4, 3, 3, r12, r21, wml, 0.0f, wpl));
     }
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
@@ -324,8 +285,8 @@ __global__ void __launch_bounds__(128) tri_self_energy_kernel(TriArgs a) {
         for (int k = 0; k < int(blockDim.x >> 5); ++k) sum += red[k];
         double val = -2.0 * sum;
         for (int c = 0; c < 4; ++c)
-            val += double(tri_value_none(pos, a, c, c, 0, 0, wpl, wml, 0.0f)) -
-                   double(tri_value_none(pos, a, c, c, 0, 0, wml, wpl, 0.0f));
+            val += double(tri_value_none(pos, a.n, a.nl, a.v4, c, c, 0, 0, wpl, wml, 0.0f)) -
+                   double(tri_value_none(pos, a.n, a.nl, a.v4, c, c, 0, 0, wml, wpl, 0.0f));
         val /= (2.0 * kPiD * (double(L) + odd_interp(pos, a.n, a.v2, L)));
         const float outv = float(val);
         a.dv2[i] = outv;
@@ -386,12 +347,18 @@ __device__ __forceinline__ void make_tpart(const TriArgs &a, const float *pos, i
     }
 }
 
+// Entry goff[e][c][j] of gather_slab's offsets: component c = 4a + b of the site whose
+// representative is r under spin permutation p; e = 1 for the site-exchanged pair (components
+// swapped, then permuted).
+SPN_HDI int gather_offset(int e, int c, int nl, int r, int p) {
+    const int ca = c >> 2, cb = c & 3;
+    return (4 * permc(p, e ? cb : ca) + permc(p, e ? ca : cb)) * nl + r;
+}
+
 // One slab of a node for all sites (getValueSuperbundle): goff[e][c][j] is the offset of
-// component c of site j, e = 1 for the site-exchanged pair (components swapped, then permuted,
-// plus the representative's rid).  The sign of support i depends on the component only through
+// component c of site j (gather_offset of the site's representative and permutation).  The sign of support i depends on the component only through
 // zeta(a) and zeta(b), so the four signed weights of each zeta class are formed once.
-__device__ __forceinline__ void gather_slab(const float *__restrict__ v4, const TAB4 &ab, const int *goff, int nl, int lane,
-                                            float *S) {
+SPN_HDI void gather_slab(const float *__restrict__ v4, const TAB4 &ab, const int *goff, int nl, int lane, float *S) {
     const int fl = ab.fl;
     const bool ex = fl & kFlExch, tu = fl & kFlTu;
     float sw[4][4];  // [class: bit 0 a is a spin component, bit 1 b is][support]
@@ -413,7 +380,7 @@ __device__ __forceinline__ void gather_slab(const float *__restrict__ v4, const 
             const int o = g[c * nl + j];
             float v = 0.0f;
 #pragma unroll
-            for (int i = 0; i < 4; ++i) v += sw[k][i] * __ldg(v4 + ab.off[i] + o);
+            for (int i = 0; i < 4; ++i) v += sw[k][i] * ro_load(v4 + ab.off[i] + o);
             S[c * nl + j] = v;
         }
     }
@@ -604,9 +571,8 @@ __global__ void __launch_bounds__(kThreads) tri_vertex_kernel(TriArgs a) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) pos[i] = a.freq[i];
     for (int i = threadIdx.x; i < 32 * nl; i += blockDim.x) {
         const int e = i / (16 * nl), c = (i / nl) & 15, j = i % nl;
-        const int ca = c >> 2, cb = c & 3;
         const int r = e ? a.inv_sites[j] : a.sites[j], p = e ? a.inv_sites_perm[j] : a.sites_perm[j];
-        goff[i] = (4 * permc(p, e ? cb : ca) + permc(p, e ? ca : cb)) * nl + r;
+        goff[i] = gather_offset(e, c, nl, r, p);
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1146,5 +1112,54 @@ extern "C" int spn_tri_is_diverged(spn_tri *h, int *diverged) {
         check_cuda(cudaStreamSynchronize(h->stream), "status sync");
         if (st & kStatusNodeOverflow) throw Error(ErrorType::Device, "loop-frequency node table overflow");
         *diverged = (st & kStatusNaN) ? 1 : 0;
+    });
+}
+
+extern "C" int spn_tri_vertex_probe(const float *pos, int n, int n_sites, const float *v4, int rid12, int rid21,
+                                    int perm12, int perm21, float s, float t, float u, int channel, int local,
+                                    float *value) {
+    return guarded([&] {
+        cuh::check_mesh(pos, n, kMaxFreq);
+        if (n_sites < 1 || n_sites > kMaxSites || !v4 || !value || rid12 < 0 || rid12 >= n_sites || rid21 < 0 ||
+            rid21 >= n_sites || perm12 < 0 || perm12 > 5 || perm21 < 0 || perm21 > 5 || channel < -1 || channel > 3 ||
+            (channel < 0 && (local || perm12 || perm21)))
+            throw Error(ErrorType::Argument, "spn_tri_vertex_probe: bad argument");
+        const int nl = n_sites;
+        if (channel < 0) {
+            for (int c = 0; c < 16; ++c) value[c] = tri_value_none(pos, n, nl, v4, c >> 2, c & 3, rid12, rid21, s, t, u);
+            return;
+        }
+        if (channel == 3) {
+            TAB8 ab;
+            tri_access8(pos, n, nl, s, t, u, ab);
+            const bool ex = ab.fl & kFlExch;
+            for (int c = 0; c < 16; ++c)
+                value[c] = local ? tri_local(v4, nl, ab, c >> 2, c & 3)
+                                 : tri_bundle(v4, nl, ab, c, ex ? rid21 : rid12, ex ? perm21 : perm12);
+            return;
+        }
+        // the channel's own frequency is a mesh value; the two others are interpolated in the
+        // order tri_access4i takes them (t, u for S; s, u for T; s, t for U)
+        const MeshSearch<float> m{pos, n};
+        const float own[3] = {s, t, u};
+        const int e = cuh::mesh_index_of(pos, n, own[channel]);
+        const Interp<float> ia = interp_abs(m, channel == 0 ? t : s), ib = interp_abs(m, channel == 2 ? t : u);
+        TAB4 ab;
+        if (channel == 0) tri_access4i<kS>(n, nl, s, t, u, e, ia, ib, ab);
+        else if (channel == 1) tri_access4i<kT>(n, nl, s, t, u, e, ia, ib, ab);
+        else tri_access4i<kU>(n, nl, s, t, u, e, ia, ib, ab);
+        if (local) {
+            for (int c = 0; c < 16; ++c) value[c] = tri_local(v4, nl, ab, c >> 2, c & 3);
+            return;
+        }
+        // the vertex kernel's slab gather, every site of the table standing for the probed pair
+        std::vector<int> goff(32 * size_t(nl));
+        for (int i = 0; i < 32 * nl; ++i) {
+            const int ex = i / (16 * nl), c = (i / nl) & 15;
+            goff[i] = gather_offset(ex, c, nl, ex ? rid21 : rid12, ex ? perm21 : perm12);
+        }
+        std::vector<float> S(16 * size_t(nl));
+        gather_slab(v4, ab, goff.data(), nl, 0, S.data());
+        for (int c = 0; c < 16; ++c) value[c] = S[size_t(c) * nl];
     });
 }

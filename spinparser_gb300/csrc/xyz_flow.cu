@@ -47,7 +47,7 @@ constexpr unsigned long long kPermBits =
     36ull | (24ull << 6) | (33ull << 12) | (9ull << 18) | (18ull << 24) | (6ull << 30);
 __host__ __device__ __forceinline__ int perm_c(int p, int c) { return int((kPermBits >> (6 * p + 2 * c)) & 3ull); }
 
-__device__ __forceinline__ float comp_of(const float4 &v, int c) { return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w)); }
+SPN_HDI float comp_of(const float4 &v, int c) { return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w)); }
 
 struct XyzArgs {
     int n, nl, fn, max_nodes, n_range, n_corr;
@@ -80,12 +80,11 @@ struct XyzArgs {
 struct QuadComp {
     const float4 *v;
     int c;
-    __device__ __forceinline__ float spin(int i) const { return comp_of(__ldg(v + i), c); }
-    __device__ __forceinline__ float density(int i) const { return __ldg(v + i).w; }
+    SPN_HDI float spin(int i) const { return comp_of(ro_load(v + i), c); }
+    SPN_HDI float density(int i) const { return ro_load(v + i).w; }
 };
 
-__device__ __forceinline__ float value4(const float *pos, const XyzArgs &a, int c, int rid12, int rid21, float s, float t,
-                                        float u) {
+SPN_HDI float value4(const float *pos, const XyzArgs &a, int c, int rid12, int rid21, float s, float t, float u) {
     return value_none(pos, a.n, a.nl, QuadComp{a.sd, c}, c == D, rid12, rid21, s, t, u);
 }
 
@@ -139,7 +138,7 @@ using Lane4 = LaneT<kSpt>;
 // four supports are summed per stored component (one fused multiply-add each) and the sums
 // permuted once, instead of selecting a permuted component of every support.
 template <int SPT>
-__device__ __forceinline__ void gather4(const XyzArgs &a, const AB4 &ab, const LaneT<SPT> &ln, float4 *out) {
+SPN_HDI void gather4(const XyzArgs &a, const AB4 &ab, const LaneT<SPT> &ln, float4 *out) {
 #pragma unroll
     for (int k = 0; k < SPT; ++k) {
         float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -149,7 +148,7 @@ __device__ __forceinline__ void gather4(const XyzArgs &a, const AB4 &ab, const L
             float4 h = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                const float4 v = __ldg(a.sd + ab.off[q] + r);
+                const float4 v = ro_load(a.sd + ab.off[q] + r);
                 h.x += ab.w[q] * v.x;
                 h.y += ab.w[q] * v.y;
                 h.z += ab.w[q] * v.z;
@@ -162,11 +161,11 @@ __device__ __forceinline__ void gather4(const XyzArgs &a, const AB4 &ab, const L
 }
 
 // getValueLocal of the four components at rid 0 (identity permutation).
-__device__ __forceinline__ float4 local4(const XyzArgs &a, const AB4 &ab) {
+SPN_HDI float4 local4(const XyzArgs &a, const AB4 &ab) {
     float4 g = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-        const float4 v = __ldg(a.sd + ab.off[q]);
+        const float4 v = ro_load(a.sd + ab.off[q]);
         g.x += ab.w[q] * v.x;
         g.y += ab.w[q] * v.y;
         g.z += ab.w[q] * v.z;
@@ -493,6 +492,17 @@ __global__ void __launch_bounds__(kThreads) xyz_vertex_kernel(XyzArgs a) {
 // outer node accumulates the inner integral per site in FP64, a final CTA adds the outer
 // weights and the on-site term and scatters to (basis, site in range) entries.
 // ------------------------------------------------------------------------------------
+// getValueSuperbundle through a trilinear buffer for one site: X, Y, Z the components of the
+// representative r under permutation p, D the signed density.
+SPN_HDI void bundle8(const XyzArgs &a, const AB8 &ab, int r, int p, float g[4]) {
+    g[0] = g[1] = g[2] = g[3] = 0.0f;
+    for (int q = 0; q < 8; ++q) {
+        const float4 v = ro_load(a.sd + ab.off[q] + r);
+        for (int c = 0; c < 3; ++c) g[c] += ab.w[q] * comp_of(v, perm_c(p, c));
+        g[3] += ab.sw[q] * v.w;
+    }
+}
+
 __global__ void __launch_bounds__(128) xyz_corr_inner_kernel(XyzArgs a) {
     __shared__ float pos[kMaxFreq];
     __shared__ float nwp[kMaxCorrNodes];
@@ -535,14 +545,8 @@ __global__ void __launch_bounds__(128) xyz_corr_inner_kernel(XyzArgs a) {
 #pragma unroll
         for (int k = 0; k < kSpt; ++k) {
             if (!ln.valid[k]) continue;
-            const int r = ab.exch ? ln.irid[k] : ln.rid[k];
-            const int p = ab.exch ? ln.iprm[k] : ln.prm[k];
-            float g[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            for (int q = 0; q < 8; ++q) {
-                const float4 v = __ldg(a.sd + ab.off[q] + r);
-                for (int c = 0; c < 3; ++c) g[c] += ab.w[q] * comp_of(v, perm_c(p, c));
-                g[3] += ab.sw[q] * v.w;
-            }
+            float g[4];
+            bundle8(a, ab, ab.exch ? ln.irid[k] : ln.rid[k], ab.exch ? ln.iprm[k] : ln.prm[k], g);
             double rr[4] = {-double(g[0]), -double(g[1]), -double(g[2]), -4.0 * double(g[3])};  // dumbbell
             if (ln.j[k] == 0) {  // egg diagram
                 rr[0] += 0.5 * (double(vv[0]) - vv[1] - vv[2] + vv[3]);
@@ -1004,5 +1008,63 @@ extern "C" int spn_xyz_is_diverged(spn_xyz *h, int *diverged) {
         check_cuda(cudaStreamSynchronize(h->stream), "status sync");
         if (st & kStatusNodeOverflow) throw Error(ErrorType::Device, "loop-frequency node table overflow");
         *diverged = (st & kStatusNaN) ? 1 : 0;
+    });
+}
+
+extern "C" int spn_xyz_vertex_probe(const float *pos, int n, int n_sites, const float *xx, const float *yy,
+                                    const float *zz, const float *dd, int rid12, int rid21, int perm12, int perm21,
+                                    float s, float t, float u, int channel, int local, float *value) {
+    return guarded([&] {
+        cuh::check_mesh(pos, n, kMaxFreq);
+        if (n_sites < 1 || n_sites > 32 * kSpt || !xx || !yy || !zz || !dd || !value || rid12 < 0 ||
+            rid12 >= n_sites || rid21 < 0 || rid21 >= n_sites || perm12 < 0 || perm12 > 5 || perm21 < 0 ||
+            perm21 > 5 || channel < -1 || channel > 3 || (channel < 0 && (local || perm12 || perm21)))
+            throw Error(ErrorType::Argument, "spn_xyz_vertex_probe: bad argument");
+        // the device layout: one float4 (X, Y, Z, D) per element
+        const size_t vsz = size_t(n) * n * (n + 1) / 2 * n_sites;
+        std::vector<float4> sd(vsz);
+        for (size_t i = 0; i < vsz; ++i) sd[i] = make_float4(xx[i], yy[i], zz[i], dd[i]);
+        XyzArgs a{};
+        a.n = n;
+        a.nl = n_sites;
+        a.sd = sd.data();
+        float g[4];
+        if (channel < 0) {
+            for (int c = 0; c < 4; ++c) g[c] = value4(pos, a, c, rid12, rid21, s, t, u);
+        } else if (channel == 3) {
+            AB8 ab;
+            access8(pos, n, n_sites, s, t, u, ab);
+            if (local) bundle8(a, ab, 0, 0, g);
+            else bundle8(a, ab, ab.exch ? rid21 : rid12, ab.exch ? perm21 : perm12, g);
+        } else {
+            // the channel's own frequency is a mesh value; the two others are interpolated in
+            // the order access4i takes them (t, u for S; s, u for T; s, t for U)
+            const MeshSearch<float> m{pos, n};
+            const float own[3] = {s, t, u};
+            const int e = cuh::mesh_index_of(pos, n, own[channel]);
+            const Interp<float> ia = interp_abs(m, channel == 0 ? t : s), ib = interp_abs(m, channel == 2 ? t : u);
+            AB4 ab;
+            if (channel == 0) access4i<kS>(n, n_sites, s, t, u, ia, ib, e, ab);
+            else if (channel == 1) access4i<kT>(n, n_sites, s, t, u, ia, ib, e, ab);
+            else access4i<kU>(n, n_sites, s, t, u, ia, ib, e, ab);
+            float4 v;
+            if (local) {
+                v = local4(a, ab);
+            } else {
+                LaneT<1> ln;
+                ln.j[0] = 0;
+                ln.valid[0] = true;
+                ln.rid[0] = rid12;
+                ln.prm[0] = perm12;
+                ln.irid[0] = rid21;
+                ln.iprm[0] = perm21;
+                gather4(a, ab, ln, &v);
+            }
+            g[0] = v.x;
+            g[1] = v.y;
+            g[2] = v.z;
+            g[3] = v.w;
+        }
+        for (int c = 0; c < 4; ++c) value[c] = g[c];
     });
 }
