@@ -189,6 +189,12 @@ int spn_lattice_write_ldf(const spn_lattice *lat, const char *path);
  * (src/TaskFileParser.cpp:121-123).  out has room for `count` floats. */
 int spn_frequency_exponential(float min, float max, int count, float *out);
 
+/* A number of the task, lattice and model files (InputParser::stringToDouble,
+ * src/lib/InputParser.hpp:24-56): sqrt(x) terms are evaluated first, then x*y and x/y left to
+ * right, each result written back with 20 decimals, then the text is read as a double.  The
+ * files' float values are (float) of it. */
+int spn_parse_number(const char *text, double *value);
+
 /* Exponential cutoff list: repeated float multiplication max, max*step, ... while > min
  * (src/TaskFileParser.cpp:171-176).  Writes at most `cap` values, *n receives the count
  * (which may exceed cap; call again with a larger buffer). */

@@ -119,6 +119,7 @@ SIGNATURES = {
     "spn_rpa_lane_schedule": (C.c_int, [C.c_int, C.c_int, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p,
                                         c_int_p]),
     "spn_frequency_exponential": (C.c_int, [C.c_float, C.c_float, C.c_int, c_float_p]),
+    "spn_parse_number": (C.c_int, [C.c_char_p, c_double_p]),
     "spn_cutoff_exponential": (C.c_int, [C.c_float, C.c_float, C.c_float, c_float_p, C.c_int, c_int_p]),
     "spn_su2_initial_state": (C.c_int, [C.c_void_p, C.c_int, C.c_float, c_float_p, c_float_p, c_float_p]),
     "spn_su2_create": (C.c_int, [C.POINTER(Su2Desc), C.POINTER(C.c_void_p)]),

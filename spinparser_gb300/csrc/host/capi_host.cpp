@@ -217,6 +217,13 @@ extern "C" int spn_frequency_exponential(float min, float max, int count, float 
     });
 }
 
+extern "C" int spn_parse_number(const char *text, double *value) {
+    return spn::guarded([&] {
+        if (!text || !value) throw spn::Error(spn::ErrorType::Argument, "spn_parse_number: null argument");
+        *value = spn::parse_number(text);
+    });
+}
+
 extern "C" int spn_cutoff_exponential(float max, float min, float step, float *out, int cap, int *n) {
     return spn::guarded([&] {
         if (!n || (cap > 0 && !out)) throw spn::Error(spn::ErrorType::Argument, "spn_cutoff_exponential: null output");

@@ -100,6 +100,32 @@ def test_number_syntax_of_unit_cells():
     assert np.float32(tab.interaction_J[0, 0, 0]) == np.float32(0.5)
 
 
+def parse_number(text):
+    import ctypes as C
+    from spinparser_gb300._capi import check, load_library
+    v = C.c_double()
+    check(load_library().spn_parse_number(text.encode(), C.byref(v)))
+    return v.value
+
+
+@pytest.mark.parametrize("text,value", [
+    ("1.5*3.9", 1.5 * 3.9), ("1.5/3.9", 1.5 / 3.9), ("-1.5*3.9", -1.5 * 3.9), ("-1.5/3.9", -1.5 / 3.9),
+    ("1.5*3.9/2.1", 1.5 * 3.9 / 2.1), ("1.5/3.9*2.1", 1.5 / 3.9 * 2.1), ("-1.5*3.9/2.1", -1.5 * 3.9 / 2.1),
+    ("-1.5/3.9*2.1", -1.5 / 3.9 * 2.1), ("-1.5*sqrt(3.9)/2.1", -1.5 * np.sqrt(3.9) / 2.1),
+    ("0.25", 0.25), ("-2", -2.0), ("sqrt(2)", np.sqrt(2.0)),
+])
+def test_number_syntax(text, value):
+    """test/test_InputParser.cpp:8-37: stringToDouble equals the double arithmetic exactly and
+    stringToFloat within 1e-4 %."""
+    assert parse_number(text) == value
+    assert np.float32(parse_number(text)) == pytest.approx(value, rel=1e-6)
+
+
+def test_number_syntax_rejects_garbage():
+    with pytest.raises(spn.SpnError):
+        parse_number("one half")
+
+
 def test_cutoff_grid_is_repeated_float_multiplication():
     got = spn.cutoff_exponential(50.0, 0.05, 0.98)
     exp, v = [], np.float32(50.0)
