@@ -611,7 +611,6 @@ extern "C" int spn_batch_add(spn_batch *b, const spn_su2_desc *desc, int n_cutof
             f.hist_row = 2 * size_t(f.h->n_corr) + 2 * f.h->nl;
             f.hist = dalloc<float>(size_t(n_cutoffs) * f.hist_row, "alloc measurement history");
             cuda_check(cudaMemcpyAsync(f.cutoffs, cutoffs, n_cutoffs * sizeof(float), cudaMemcpyHostToDevice, b->stream), "H2D");
-            const size_t vsz = size_t(f.h->fn) * f.h->nl;
             cuda_check(cudaMemcpyAsync(f.h->v2, v2, f.h->n * sizeof(float), cudaMemcpyHostToDevice, b->stream), "H2D");
             // staged through the new flow's (still unused) flow buffer
             upload_state(f.h, v4ss, v4dd, reinterpret_cast<float *>(f.h->dsd), b->stream);
@@ -759,7 +758,6 @@ extern "C" int spn_batch_get_state(spn_batch *b, int flow_id, float *cutoff, flo
         const spn_batch::Flow &f = b->flows[flow_id];
         BatchFlow r;
         cuda_check(cudaMemcpy(&r, b->d_flows + flow_id, sizeof(r), cudaMemcpyDeviceToHost), "D2H record");
-        const size_t vsz = size_t(f.h->fn) * f.h->nl;
         if (cutoff) *cutoff = r.a.cutoff;
         if (v2) cuda_check(cudaMemcpy(v2, f.h->v2, f.h->n * sizeof(float), cudaMemcpyDeviceToHost), "D2H");
         // staged through the flow buffer: between batch steps it holds nothing that is used again

@@ -397,6 +397,20 @@ struct HostState {
 };
 
 void check_mesh(const float *pos, int n) { cuh::check_mesh(pos, n, kMaxFreq); }
+
+// The emitter of spn_quadrature_nodes: the first cap nodes into (wp, weight), k counts all.
+struct NodeList {
+    float *wp;
+    double *weight;
+    int cap, k;
+    __host__ __device__ void operator()(float x, double c) {
+        if (k < cap) {
+            wp[k] = x;
+            weight[k] = c;
+        }
+        ++k;
+    }
+};
 }  // namespace
 
 extern "C" int spn_mesh_probe(const float *pos, int n, float w, float *lesser, float *greater, int *offset, int *lo,
@@ -477,18 +491,11 @@ extern "C" int spn_quadrature_nodes(const float *pos, int n, int rule, float min
         check_mesh(pos, n);
         if (rule < 0 || rule > 2 || !count || cap < 0 || (cap > 0 && (!wp || !weight)))
             throw Error(ErrorType::Argument, "spn_quadrature_nodes: bad argument");
-        int k = 0;
-        auto emit = [&](float x, double c) {
-            if (k < cap) {
-                wp[k] = x;
-                weight[k] = c;
-            }
-            ++k;
-        };
+        NodeList emit{wp, weight, cap, 0};
         if (rule == 0) dev::nodes_left(pos, n, min, emit);
         else if (rule == 1) dev::nodes_right(pos, n, max, emit);
         else dev::nodes_both(pos, n, min, max, emit);
-        *count = k;
+        *count = emit.k;
     });
 }
 
