@@ -192,7 +192,10 @@ SPN_HDI void tri_access8(const float *pos, int n, int nl, float s, float t, floa
 }
 
 // getValueLocal(a, b, ab) (TRIVertexTwoParticle.hpp:347-356): the components are exchanged
-// first and index the sign table in that order.
+// first and index the sign table in that order.  getValue and getValueSuperbundle (tri_bundle)
+// index it with the original order, so for a site-exchanging buffer the two differ in the sign
+// of the mixed spin/density components on supports whose stored sector swaps s and u; this is
+// the reference's convention, kept.
 template <int K>
 SPN_HDI float tri_local(const float *v4, int nl, const TABT<K> &ab, int ca, int cb) {
     if (ab.fl & kFlExch) {
